@@ -1,0 +1,75 @@
+"""Pin the oracle against the reference's own golden values.
+
+The reference's regression driver runs `ellipticMain` and compares the printed
+`Solution norm` with a golden value to an absolute 1e-5 (test/test.py:63,129-137).
+The same settings run through the CPU restatement must land inside that band.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden_case_settings
+from oracle.oracle import Oracle
+
+ON_PATH = ("testEllipticHex_C0", "testEllipticHex_C0_Jacobi", "testEllipticHex_C0_ParAlmond",
+           "testEllipticHex_C0_Multigrid", "testEllipticHex_C0_AllNeumann")
+
+
+@pytest.mark.parametrize("name", ON_PATH)
+def test_reference_golden_norm(reference_norms, name):
+    case = reference_norms["cases"][name]
+    o = Oracle(golden_case_settings(case))
+    r = o.run()
+    assert abs(r["norm"] - case["norm"]) < reference_norms["tolerance"], (name, r["norm"], case["norm"])
+    assert r["iterations"] > 0
+
+
+def test_golden_cases_off_path_are_listed(reference_norms):
+    # SEMFEM and OAS preconditioners are other discretisation paths (out of scope).
+    off = set(reference_norms["cases"]) - set(ON_PATH)
+    assert off == {"testEllipticHex_C0_Semfem", "testEllipticHex_C0_OAS"}
+
+
+def test_gll_nodes_weights():
+    from oracle.oracle import lib
+    import ctypes
+    for N in range(1, 9):
+        x = np.zeros(N + 1)
+        w = np.zeros(N + 1)
+        lib().orc_jacobiGLL(N, x.ctypes.data_as(ctypes.c_void_p), w.ctypes.data_as(ctypes.c_void_p))
+        xr, wr = np.polynomial.legendre.leggauss(N + 1)  # Gauss, used only for moments
+        # GLL quadrature integrates x^k exactly for k <= 2N-1
+        for k in range(2 * N):
+            exact = 0.0 if k % 2 else 2.0 / (k + 1)
+            assert abs(np.dot(w, x ** k) - exact) < 1e-13
+        assert abs(x[0] + 1) < 1e-15 and abs(x[-1] - 1) < 1e-15
+
+
+def test_dmatrix_differentiates_polynomials():
+    from oracle.oracle import lib
+    import ctypes
+    for N in (1, 3, 5, 7):
+        x = np.zeros(N + 1)
+        D = np.zeros((N + 1) * (N + 1))
+        lib().orc_jacobiGLL(N, x.ctypes.data_as(ctypes.c_void_p), None)
+        lib().orc_dmatrix1D(N, x.ctypes.data_as(ctypes.c_void_p), D.ctypes.data_as(ctypes.c_void_p))
+        D = D.reshape(N + 1, N + 1)
+        for k in range(N + 1):
+            d = D @ (x ** k)
+            ex = k * x ** (k - 1) if k > 0 else 0 * x
+            assert np.max(np.abs(d - ex)) < 1e-12
+
+
+def test_hessenberg_eigenvalues_match_numpy():
+    from oracle.oracle import lib
+    import ctypes
+    rng = np.random.default_rng(0)
+    for n in (1, 2, 3, 5, 10):
+        H = np.triu(rng.standard_normal((n, n)), -1)
+        wr, wi = np.zeros(n), np.zeros(n)
+        Hc = np.asfortranarray(H).ravel(order="F")
+        lib().orc_hessenberg_eigenvalues(n, Hc.ctypes.data_as(ctypes.c_void_p),
+                                         wr.ctypes.data_as(ctypes.c_void_p),
+                                         wi.ctypes.data_as(ctypes.c_void_p))
+        ours = np.sort_complex(wr + 1j * wi)
+        ref = np.sort_complex(np.linalg.eigvals(H))
+        assert np.max(np.abs(ours - ref)) < 1e-10 * max(1, np.max(np.abs(ref)))
