@@ -1,0 +1,162 @@
+/*
+ * libparanumal_gb300: C ABI of the GB300 (sm_103a) C0 hexahedral elliptic path.
+ *
+ * Two levels:
+ *   1. kernel entry points: device pointers, explicit sizes, a cudaStream_t passed
+ *      as void*; each returns an int status (LPG_OK = 0, negative on error, text by
+ *      lpg_last_error()). They never allocate unless stated.
+ *   2. solver objects: an elliptic_t built from a settings text in the reference's
+ *      .rc format, with Operator / precon / Solve / Run entry points.
+ *
+ * Every entry point cites the reference interface it replaces (paths are relative
+ * to the libParanumal source tree). No C++ exception crosses this boundary.
+ */
+#ifndef LPG_H
+#define LPG_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ status */
+#define LPG_OK 0
+#define LPG_ERR_INVALID (-1)       /* bad argument */
+#define LPG_ERR_CUDA (-2)          /* CUDA runtime error */
+#define LPG_ERR_UNSUPPORTED (-3)   /* e.g. polynomial degree outside 1..8 */
+#define LPG_ERR_NOT_CONVERGED (-4) /* solver hit MAXIT */
+#define LPG_ERR_ALLOC (-5)         /* device allocation failed */
+#define LPG_ERR_SETTINGS (-6)      /* unknown or malformed setting */
+#define LPG_ERR_BREAKDOWN (-7)     /* NaN/Inf or non-positive curvature in (F)PCG */
+
+/* Replaces LIBP_ABORT's message (include/utils.hpp:57-76): text of the last error on
+ * this thread. */
+const char *lpg_last_error(void);
+const char *lpg_version(void);
+
+/* Device memory helpers for callers without a CUDA runtime of their own
+ * (platform_t::malloc / memory copies, include/platform.hpp:163-205). */
+int lpg_device_malloc(void **ptr, uint64_t bytes);
+int lpg_device_free(void *ptr);
+int lpg_memcpy_h2d(void *dst, const void *src, uint64_t bytes, void *stream);
+int lpg_memcpy_d2h(void *dst, const void *src, uint64_t bytes, void *stream);
+int lpg_stream_sync(void *stream);
+
+/* ------------------------------------------------------------------ operator kernels */
+/*
+ * Matrix-free screened-Poisson operator on hexahedra with fused assembly:
+ *   Aq[g] = sum over local copies n of g of ( D^T G D q_e + lambda_e wJ q_e )[n]
+ * Replaces ellipticPartialAxHex3D (solvers/elliptic/okl/ellipticAxHex3D.okl:156-295)
+ * followed by ogsMasked.Gather(Aq, AqL, Add, Trans) (solvers/elliptic/src/ellipticOperator.cpp:29-106).
+ *   N              polynomial degree, 1..8
+ *   Nelements      elements to process; elementList (int32, may be NULL = 0..Nelements-1)
+ *   GlobalToLocal  int32 per local node (E*Np): assembled dof index or -1 (masked)
+ *   ggeo, wJ       geometric factors: ggeo[e*geoStride + c*Np + n] for c = G00,G01,G02,G11,G12,G22
+ *                  and wJ[e*wJStride + n]. The reference layout is geoStride = 6*Np, wJStride = Np;
+ *                  the packed layout used by this library's own objects is geoStride = wJStride = 7*Np
+ *                  with wJ = ggeo + 6*Np.
+ *   D              (N+1)^2 derivative matrix, row-major, D[i*Nq+j] = l_j'(r_i)
+ *   lambda         scalar; lambdaE (per element, may be NULL) overrides it
+ *   q              assembled input (Nglobal); Aq assembled output (Nglobal), overwritten
+ * _f64: FP64 storage and arithmetic. _f32: FP32 vectors and geometry. _bf16g: BF16
+ * geometric factors with FP32 vectors and FP32 accumulation.
+ */
+int lpg_ax_hex_f64(int N, int64_t Nelements, const int32_t *elementList, const int32_t *GlobalToLocal,
+                   const double *ggeo, int64_t geoStride, const double *wJ, int64_t wJStride,
+                   const double *D, double lambda, const double *lambdaE,
+                   const double *q, double *Aq, int64_t Nglobal, void *stream);
+int lpg_ax_hex_f32(int N, int64_t Nelements, const int32_t *elementList, const int32_t *GlobalToLocal,
+                   const float *ggeo, int64_t geoStride, const float *wJ, int64_t wJStride,
+                   const float *D, float lambda, const float *lambdaE,
+                   const float *q, float *Aq, int64_t Nglobal, void *stream);
+int lpg_ax_hex_bf16g(int N, int64_t Nelements, const int32_t *elementList, const int32_t *GlobalToLocal,
+                     const void *ggeo_bf16, int64_t geoStride, const void *wJ_bf16, int64_t wJStride,
+                     const float *D, float lambda, const float *lambdaE,
+                     const float *q, float *Aq, int64_t Nglobal, void *stream);
+
+/* Unassembled variant with the reference kernel's exact contract: writes the local
+ * result AqL[e*Np + n] for the listed elements (ellipticAxHex3D.okl:156-295). */
+int lpg_partial_ax_hex_f64(int N, int64_t Nelements, const int32_t *elementList,
+                           const int32_t *GlobalToLocal, const double *ggeo, int64_t geoStride,
+                           const double *wJ, int64_t wJStride, const double *D, double lambda,
+                           const double *lambdaE, const double *q, double *AqL, void *stream);
+
+/* ------------------------------------------------------------------ gather-scatter */
+/* ogs_t::Gather(gv, v, 1, Add, Trans) (libs/ogs/ogs.cpp:213-285): gv[g] = sum of v over
+ * copies; overwrites gv. Uses GlobalToLocal (-1 entries skipped). */
+int lpg_ogs_gather_add_f64(int64_t Nlocal, const int32_t *GlobalToLocal, const double *v,
+                           double *gv, int64_t Nglobal, void *stream);
+/* ogs_t::Gather(gv, v, 1, Add, NoTrans): one copy per dof, picked by ownerLocal[g]. */
+int lpg_ogs_gather_owner_f64(int64_t Nglobal, const int32_t *ownerLocal, const double *v, double *gv,
+                             void *stream);
+/* ogs_t::Scatter(v, gv, 1, NoTrans) (libs/ogs/ogs.cpp:287-330): v[n] = gv[GlobalToLocal[n]],
+ * masked nodes set to 0. */
+int lpg_ogs_scatter_f64(int64_t Nlocal, const int32_t *GlobalToLocal, const double *gv, double *v,
+                        void *stream);
+
+/* ------------------------------------------------------------------ vector kernels */
+/* linAlg_t (include/linAlg.hpp:37-208; libs/linAlg/okl/linAlg*.okl). Reductions write their
+ * result to a device scalar (no host synchronisation); partial sums use a
+ * library-owned scratch buffer allocated on first use. */
+int lpg_axpy_f64(int64_t N, double alpha, const double *x, double beta, double *y, void *stream);
+int lpg_amxpy_f64(int64_t N, double alpha, const double *x, const double *y, double beta, double *z,
+                  void *stream);
+int lpg_dot_f64(int64_t N, const double *x, const double *y, double *result_dev, void *stream);
+int lpg_norm2sq_f64(int64_t N, const double *x, double *result_dev, void *stream);
+/* linearSolverUpdatePCG.okl:29-75 + pcg::UpdatePCG (linearSolverPCG.cpp:153-171):
+ * x += alpha p; r -= alpha Ap; result_dev = r.r */
+int lpg_pcg_update_f64(int64_t N, double alpha, const double *p, const double *Ap, double *x, double *r,
+                       double *result_dev, void *stream);
+
+/* ------------------------------------------------------------------ solver objects */
+/* elliptic_t (solvers/elliptic/elliptic.hpp:56-170) built from settings in the
+ * reference's .rc format ([KEY] newline value). Supported keys are listed in
+ * INTEGRATION.md; unknown keys fail with LPG_ERR_SETTINGS, as the reference aborts
+ * (solvers/elliptic/src/ellipticSettings.cpp:144-146). */
+typedef struct lpg_elliptic lpg_elliptic;
+
+int lpg_elliptic_create(const char *settings, lpg_elliptic **out);
+int lpg_elliptic_destroy(lpg_elliptic *e);
+
+#define LPG_INFO_NELEMENTS 0
+#define LPG_INFO_NP 1
+#define LPG_INFO_NGLOBAL 2
+#define LPG_INFO_NLOCAL 3
+#define LPG_INFO_N 4
+#define LPG_INFO_ALLNEUMANN 5
+#define LPG_INFO_MG_PLEVELS 6
+#define LPG_INFO_MG_AMGLEVELS 7
+#define LPG_INFO_COARSE_N 8
+#define LPG_INFO_DEVICE_BYTES 9
+int64_t lpg_elliptic_info(const lpg_elliptic *e, int what);
+
+/* Copy a named setup array to host memory: "GlobalToLocal" (int32), "ownerLocal" (int32),
+ * "ggeo" (E*6*Np double, reference layout), "wJ", "D", "weightG", "lambdaE", "invDiag". */
+int lpg_elliptic_get(const lpg_elliptic *e, const char *name, void *host_out, uint64_t bytes);
+
+/* Device pointers owned by the object (valid until destroy): "q_in", "Aq_out", "x", "r"
+ * are FP64 vectors of length Nglobal usable as scratch by the caller. */
+int lpg_elliptic_device_ptr(const lpg_elliptic *e, const char *name, void **ptr);
+
+/* elliptic_t::Operator (ellipticOperator.cpp:29-106): Aq = A q, device pointers (Nglobal). */
+int lpg_elliptic_operator(lpg_elliptic *e, const double *q, double *Aq, void *stream);
+/* precon_t::Operator (include/precon.hpp:36-56): z = M^{-1} r, device pointers. */
+int lpg_elliptic_precon(lpg_elliptic *e, const double *r, double *z, void *stream);
+/* elliptic_t::Solve (ellipticSolve.cpp:29-39): (F)PCG on device vectors x (initial
+ * guess, overwritten) and r (right-hand side, overwritten by the residual).
+ * Returns the iteration count in *iters. */
+int lpg_elliptic_solve(lpg_elliptic *e, double *x, double *r, double tol, int maxit, int *iters);
+/* The assembled right-hand side of elliptic_t::Run (forcing, Dirichlet lifting,
+ * Gather(Trans)) into a device vector r (Nglobal). */
+int lpg_elliptic_rhs(lpg_elliptic *e, double *r, void *stream);
+/* elliptic_t::Run (ellipticRun.cpp:30-248): rhs, timed solve, scatter + AddBC, then the
+ * mass-weighted solution norm and, for manufactured data, the error norm.
+ * xL_host (Nlocal doubles) may be NULL; solve_seconds is the wall time of the solve. */
+int lpg_elliptic_run(lpg_elliptic *e, double *xL_host, int *iters, double *norm, double *err,
+                     double *solve_seconds);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

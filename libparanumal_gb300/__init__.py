@@ -1,0 +1,202 @@
+"""libparanumal_gb300: GB300-native C0 hexahedral elliptic path.
+
+Python view of the C ABI in include/lpg.h. The compute path is the CUDA library
+libparanumal_gb300/_build/liblpg.so (built by libparanumal_gb300.build); importing
+an entry point without it raises -- there is no CPU fallback.
+
+Device buffers are passed as integers (device addresses), e.g. torch tensors'
+``data_ptr()``; streams as integers (``torch.cuda.current_stream().cuda_stream``) or 0.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "liblpg.so")
+
+LPG_OK = 0
+STATUS = {0: "OK", -1: "INVALID", -2: "CUDA", -3: "UNSUPPORTED", -4: "NOT_CONVERGED",
+          -5: "ALLOC", -6: "SETTINGS", -7: "BREAKDOWN"}
+INFO = dict(nelements=0, np=1, nglobal=2, nlocal=3, n=4, allneumann=5, mg_plevels=6,
+            mg_amglevels=7, coarse_n=8, device_bytes=9)
+
+_lib = None
+
+
+class LPGError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s (%d): %s" % (STATUS.get(status, "?"), status, msg))
+        self.status = status
+
+
+def lib():
+    """Load the CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError("libparanumal_gb300: %s is missing; build it with "
+                           "`python -c 'import __graft_entry__ as g; g.build()'`" % LIB_PATH)
+    L = ctypes.CDLL(LIB_PATH)
+    vp, i32, i64, f64, f32 = (ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_double,
+                              ctypes.c_float)
+    L.lpg_last_error.restype = ctypes.c_char_p
+    L.lpg_version.restype = ctypes.c_char_p
+    ax64 = [i32, i64, vp, vp, vp, i64, vp, i64, vp, f64, vp, vp, vp, i64, vp]
+    ax32 = [i32, i64, vp, vp, vp, i64, vp, i64, vp, f32, vp, vp, vp, i64, vp]
+    sig = {
+        "lpg_device_malloc": [ctypes.POINTER(ctypes.c_void_p), ctypes.c_uint64],
+        "lpg_device_free": [vp],
+        "lpg_memcpy_h2d": [vp, vp, ctypes.c_uint64, vp],
+        "lpg_memcpy_d2h": [vp, vp, ctypes.c_uint64, vp],
+        "lpg_stream_sync": [vp],
+        "lpg_ax_hex_f64": ax64,
+        "lpg_ax_hex_f32": ax32,
+        "lpg_ax_hex_bf16g": ax32,
+        "lpg_partial_ax_hex_f64": [i32, i64, vp, vp, vp, i64, vp, i64, vp, f64, vp, vp, vp, vp],
+        "lpg_ogs_gather_add_f64": [i64, vp, vp, vp, i64, vp],
+        "lpg_ogs_gather_owner_f64": [i64, vp, vp, vp, vp],
+        "lpg_ogs_scatter_f64": [i64, vp, vp, vp, vp],
+        "lpg_axpy_f64": [i64, f64, vp, f64, vp, vp],
+        "lpg_amxpy_f64": [i64, f64, vp, vp, f64, vp, vp],
+        "lpg_dot_f64": [i64, vp, vp, vp, vp],
+        "lpg_norm2sq_f64": [i64, vp, vp, vp],
+        "lpg_pcg_update_f64": [i64, f64, vp, vp, vp, vp, vp, vp],
+        "lpg_elliptic_create": [ctypes.c_char_p, ctypes.POINTER(ctypes.c_void_p)],
+        "lpg_elliptic_destroy": [vp],
+        "lpg_elliptic_get": [vp, ctypes.c_char_p, vp, ctypes.c_uint64],
+        "lpg_elliptic_device_ptr": [vp, ctypes.c_char_p, ctypes.POINTER(ctypes.c_void_p)],
+        "lpg_elliptic_operator": [vp, vp, vp, vp],
+        "lpg_elliptic_precon": [vp, vp, vp, vp],
+        "lpg_elliptic_solve": [vp, vp, vp, f64, i32, ctypes.POINTER(ctypes.c_int)],
+        "lpg_elliptic_rhs": [vp, vp, vp],
+        "lpg_elliptic_run": [vp, vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double),
+                             ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)],
+    }
+    for name, args in sig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = ctypes.c_int
+    L.lpg_elliptic_info.argtypes = [vp, i32]
+    L.lpg_elliptic_info.restype = i64
+    _lib = L
+    return L
+
+
+def declared_symbols():
+    """Entry points declared in include/lpg.h (parsed from the header)."""
+    import re
+    hdr = os.path.join(os.path.dirname(_HERE), "include", "lpg.h")
+    txt = open(hdr).read()
+    return sorted(set(re.findall(r"\b(lpg_[a-z0-9_]+)\s*\(", txt)))
+
+
+def check(status):
+    if status != LPG_OK:
+        raise LPGError(status, lib().lpg_last_error().decode())
+    return status
+
+
+def settings_text(d):
+    """Render {KEY: value} in the reference's .rc format ([KEY] newline value)."""
+    if isinstance(d, str):
+        return d
+    return "".join("[%s]\n%s\n\n" % (k, v) for k, v in d.items())
+
+
+def _ptr(x):
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    return x.data_ptr()
+
+
+class Elliptic:
+    """elliptic_t for a box mesh (solvers/elliptic/elliptic.hpp:56-170).
+
+    Settings use the reference's .rc keys. Operator / precon /
+    Solve act on device vectors of length Nglobal.
+    """
+
+    def __init__(self, settings):
+        h = ctypes.c_void_p()
+        check(lib().lpg_elliptic_create(settings_text(settings).encode(), ctypes.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().lpg_elliptic_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def info(self, what):
+        return int(lib().lpg_elliptic_info(self.h, INFO[what]))
+
+    @property
+    def Nglobal(self):
+        return self.info("nglobal")
+
+    @property
+    def Nlocal(self):
+        return self.info("nlocal")
+
+    def get(self, name):
+        E, Np, Ng, Nl = self.info("nelements"), self.info("np"), self.Nglobal, self.Nlocal
+        Nq = self.info("n") + 1
+        spec = {"GlobalToLocal": (Nl, np.int32), "ownerLocal": (Ng, np.int32),
+                "weightG": (Ng, np.float64), "D": (Nq * Nq, np.float64),
+                "lambdaE": (E, np.float64), "ggeo": (E * 6 * Np, np.float64),
+                "wJ": (E * Np, np.float64), "geo": (E * 7 * Np, np.float64),
+                "invDiag": (Ng, np.float64)}[name]
+        out = np.zeros(spec[0], dtype=spec[1])
+        check(lib().lpg_elliptic_get(self.h, name.encode(), out.ctypes.data_as(ctypes.c_void_p),
+                                     out.nbytes))
+        return out
+
+    def device_ptr(self, name):
+        p = ctypes.c_void_p()
+        check(lib().lpg_elliptic_device_ptr(self.h, name.encode(), ctypes.byref(p)))
+        return p.value
+
+    def Operator(self, q, Aq, stream=0):
+        check(lib().lpg_elliptic_operator(self.h, _ptr(q), _ptr(Aq), stream or None))
+
+    def precon(self, r, z, stream=0):
+        check(lib().lpg_elliptic_precon(self.h, _ptr(r), _ptr(z), stream or None))
+
+    def rhs(self, r):
+        check(lib().lpg_elliptic_rhs(self.h, _ptr(r), None))
+
+    def Solve(self, x, r, tol=1e-8, maxit=5000):
+        it = ctypes.c_int(0)
+        st = lib().lpg_elliptic_solve(self.h, _ptr(x), _ptr(r), tol, maxit, ctypes.byref(it))
+        if st not in (LPG_OK, -4):
+            check(st)
+        return it.value
+
+    def Run(self, want_solution=False):
+        xL = np.zeros(self.Nlocal) if want_solution else None
+        it, nrm, err, sec = ctypes.c_int(0), ctypes.c_double(0), ctypes.c_double(0), ctypes.c_double(0)
+        st = lib().lpg_elliptic_run(self.h, xL.ctypes.data_as(ctypes.c_void_p) if xL is not None else None,
+                                    ctypes.byref(it), ctypes.byref(nrm), ctypes.byref(err),
+                                    ctypes.byref(sec))
+        if st not in (LPG_OK, -4):
+            check(st)
+        return dict(iterations=it.value, norm=nrm.value, error=err.value, solve_seconds=sec.value,
+                    xL=xL, converged=(st == LPG_OK))
+
+
+def ax_hex(prec, N, Nelements, g2l, ggeo, geo_stride, wJ, wJ_stride, D, lam, q, Aq, Nglobal,
+           lambdaE=None, element_list=None, stream=0):
+    """Assembled Ax through lpg_ax_hex_{f64,f32,bf16g}; device pointers or tensors."""
+    fn = {"f64": lib().lpg_ax_hex_f64, "f32": lib().lpg_ax_hex_f32,
+          "bf16g": lib().lpg_ax_hex_bf16g}[prec]
+    check(fn(N, Nelements, _ptr(element_list), _ptr(g2l), _ptr(ggeo), geo_stride, _ptr(wJ),
+             wJ_stride, _ptr(D), lam, _ptr(lambdaE), _ptr(q), _ptr(Aq), Nglobal, stream or None))

@@ -1,0 +1,435 @@
+// extern "C" boundary: solver objects (elliptic_t built from .rc settings) and the
+// kernel entry points for gather-scatter and vector operations. No C++ exception
+// crosses this boundary; every function returns an LPG status.
+#include "objects.hpp"
+
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <sstream>
+
+using namespace lpg;
+
+struct lpg_elliptic {
+  Settings settings;
+  Platform plat;
+  MeshConfig mcfg;
+  std::unique_ptr<Elliptic> el;
+  std::unique_ptr<Precon> precon;
+  PCGWork work;
+  bool flexible = false, stopRhs = false;
+  double tol = 1e-8;
+  int maxit = 5000;
+  DevBuf<double> q_in, Aq_out, x, r, xL, norms;
+};
+
+namespace {
+
+#define LPG_GUARD_BEGIN try {
+#define LPG_GUARD_END                                                          \
+  }                                                                            \
+  catch (const std::bad_alloc&) { return set_error(LPG_ERR_ALLOC, "host allocation failed"); } \
+  catch (const std::exception& ex) { return set_error(LPG_ERR_INVALID, ex.what()); }            \
+  catch (...) { return set_error(LPG_ERR_INVALID, "unknown exception"); }
+
+// Library-owned reduction scratch per device (partial sums of the two-stage reductions).
+std::mutex g_scratch_mu;
+double* g_scratch[64] = {nullptr};
+
+int reduction_scratch(double** out) {
+  int dev = 0;
+  LPG_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return set_error(LPG_ERR_INVALID, "device index out of range");
+  std::lock_guard<std::mutex> lk(g_scratch_mu);
+  if (!g_scratch[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, sizeof(double) * kReducePartials);
+    if (e != cudaSuccess) return set_error(LPG_ERR_ALLOC, std::string("reduction scratch: ") + cudaGetErrorString(e));
+    g_scratch[dev] = (double*)p;
+  }
+  *out = g_scratch[dev];
+  return LPG_OK;
+}
+
+std::vector<int> parse_int_list(const std::string& v) {
+  std::vector<int> out;
+  std::string cur;
+  for (char ch : v + ",") {
+    if (ch >= '0' && ch <= '9') cur += ch;
+    else if (!cur.empty()) { out.push_back(std::atoi(cur.c_str())); cur.clear(); }
+  }
+  return out;
+}
+
+int build(lpg_elliptic* h) {
+  Settings& S = h->settings;
+  if (S.get("MESH FILE", "BOX") != "BOX") return set_error(LPG_ERR_UNSUPPORTED, "only MESH FILE = BOX is supported");
+  if (S.geti("ELEMENT TYPE", 12) != 12 || S.geti("MESH DIMENSION", 3) != 3)
+    return set_error(LPG_ERR_UNSUPPORTED, "only hexahedra (ELEMENT TYPE 12, MESH DIMENSION 3) are supported");
+  if (S.get("DISCRETIZATION", "CONTINUOUS") != "CONTINUOUS")
+    return set_error(LPG_ERR_UNSUPPORTED, "only the CONTINUOUS discretization is supported");
+  MeshConfig& c = h->mcfg;
+  c.nx = S.geti("BOX GLOBAL NX", 0) > 0 ? S.geti("BOX GLOBAL NX", 0) : S.geti("BOX NX", 10);
+  c.ny = S.geti("BOX GLOBAL NY", 0) > 0 ? S.geti("BOX GLOBAL NY", 0) : S.geti("BOX NY", 10);
+  c.nz = S.geti("BOX GLOBAL NZ", 0) > 0 ? S.geti("BOX GLOBAL NZ", 0) : S.geti("BOX NZ", 10);
+  c.dimx = S.getd("BOX DIMX", 10);
+  c.dimy = S.getd("BOX DIMY", 10);
+  c.dimz = S.getd("BOX DIMZ", 10);
+  c.bcflag = S.geti("BOX BOUNDARY FLAG", 1);
+  c.jitter = S.getd("MESH JITTER", 0.0);
+  c.jitterSeed = (uint64_t)std::strtoull(S.get("MESH JITTER SEED", "0").c_str(), nullptr, 10);
+  const int N = S.geti("POLYNOMIAL DEGREE", 4);
+  const double lambda = S.getd("LAMBDA", 1.0);
+  const int64_t E = (int64_t)c.nx * c.ny * c.nz;
+  std::vector<double> lamE;
+  const bool lognormal = S.is("LAMBDA FIELD", "LOGNORMAL");
+  if (lognormal) {
+    // lambda_e = exp(z), z ~ N(0,1) by Box-Muller on hashed uniforms keyed by element id
+    const uint64_t seed = (uint64_t)std::strtoull(S.get("LAMBDA SEED", "2").c_str(), nullptr, 10);
+    lamE.resize(E);
+    for (int64_t e = 0; e < E; ++e) {
+      const double u1 = 1.0 - hash_u01(seed, 4, (uint64_t)e);
+      const double u2 = hash_u01(seed, 5, (uint64_t)e);
+      lamE[e] = std::exp(std::sqrt(-2.0 * std::log(u1)) * std::cos(2.0 * 3.14159265358979323846 * u2));
+    }
+  }
+  int rc;
+  if ((rc = h->plat.init())) return rc;
+  h->el = std::make_unique<Elliptic>();
+  if ((rc = h->el->setup(&h->plat, c, N, lambda, lognormal ? &lamE : nullptr, h->plat.stream))) return rc;
+  Elliptic* el = h->el.get();
+  // right-hand side data
+  const std::string rhsField = S.get("RHS FIELD", "SINE");
+  if (rhsField == "GAUSSIAN SOURCES") {
+    el->rhsKind = 1;
+    const uint64_t seed = (uint64_t)std::strtoull(S.get("RHS SEED", "3").c_str(), nullptr, 10);
+    const int ns = S.geti("RHS SOURCES", 16);
+    el->sources.resize(4 * ns);
+    for (int k = 0; k < ns; ++k) {
+      el->sources[4 * k + 0] = -c.dimx / 2 + c.dimx * hash_u01(seed, 6, (uint64_t)k);
+      el->sources[4 * k + 1] = -c.dimy / 2 + c.dimy * hash_u01(seed, 7, (uint64_t)k);
+      el->sources[4 * k + 2] = -c.dimz / 2 + c.dimz * hash_u01(seed, 8, (uint64_t)k);
+      el->sources[4 * k + 3] = 0.05 + 0.15 * hash_u01(seed, 9, (uint64_t)k);
+    }
+    if ((rc = el->sources_d.alloc(4 * ns)) || (rc = el->sources_d.upload(el->sources.data(), 4 * ns, h->plat.stream)))
+      return rc;
+  } else if (rhsField != "SINE") {
+    return set_error(LPG_ERR_SETTINGS, "RHS FIELD must be SINE or GAUSSIAN SOURCES");
+  }
+  // linear solver
+  const std::string ls = S.get("LINEAR SOLVER", "PCG");
+  if (ls != "PCG" && ls != "FPCG") return set_error(LPG_ERR_UNSUPPORTED, "LINEAR SOLVER must be PCG or FPCG");
+  h->flexible = (ls == "FPCG");
+  h->stopRhs = S.is("LINEAR SOLVER STOPPING CRITERION", "ABS/REL-RHS-2NORM");
+  h->tol = S.getd("SOLVER TOLERANCE", 1e-8);
+  h->maxit = S.geti("MAXIMUM ITERATIONS", 5000);
+  // preconditioner
+  const std::string pre = S.get("PRECONDITIONER", "NONE");
+  if (pre == "NONE") h->precon = make_identity(el);
+  else if (pre == "JACOBI") h->precon = make_jacobi(el, &rc);
+  else if (pre == "MULTIGRID" || pre == "PARALMOND") {
+    MGOptions o;
+    o.amgOnly = (pre == "PARALMOND");
+    o.degrees = degree_schedule(N, S.get("MULTIGRID COARSENING", "HALFDOFS"), parse_int_list(S.get("MULTIGRID DEGREES", "")));
+    o.smoother = S.is("MULTIGRID SMOOTHER", "DAMPEDJACOBI") ? 1 : 0;
+    o.chebDegree = S.geti("MULTIGRID CHEBYSHEV DEGREE", 2);
+    const std::string prec = S.get("PRECONDITIONER PRECISION", "FP64");
+    if (prec == "FP64") o.prec = Prec::F64;
+    else if (prec == "FP32") o.prec = Prec::F32;
+    else if (prec == "BF16GEO") o.prec = Prec::BF16G;
+    else return set_error(LPG_ERR_SETTINGS, "PRECONDITIONER PRECISION must be FP64, FP32 or BF16GEO");
+    o.amgSmoother = S.is("PARALMOND SMOOTHER", "DAMPEDJACOBI") ? 1 : 0;
+    o.amgChebDegree = S.geti("PARALMOND CHEBYSHEV DEGREE", 2);
+    o.amgUnsmoothed = S.is("PARALMOND AGGREGATION", "UNSMOOTHED");
+    o.amgRugeStuben = S.is("PARALMOND STRENGTH", "RUGESTUBEN");
+    if (S.get("PARALMOND CYCLE", "VCYCLE") != "VCYCLE")
+      return set_error(LPG_ERR_UNSUPPORTED, "PARALMOND CYCLE must be VCYCLE");
+    h->precon = make_multigrid(el, c, o, &rc);
+  } else {
+    return set_error(LPG_ERR_UNSUPPORTED, "PRECONDITIONER must be NONE, JACOBI, MULTIGRID or PARALMOND");
+  }
+  if (rc) return rc;
+  if (!h->precon) return set_error(LPG_ERR_INVALID, "preconditioner setup failed");
+  const int64_t Ng = el->Nglobal;
+  if ((rc = h->q_in.alloc(Ng)) || (rc = h->Aq_out.alloc(Ng)) || (rc = h->x.alloc(Ng)) || (rc = h->r.alloc(Ng)) ||
+      (rc = h->norms.alloc(2)))
+    return rc;
+  if ((rc = h->work.ensure(Ng))) return rc;
+  LPG_CUDA_TRY(cudaStreamSynchronize(h->plat.stream));
+  return LPG_OK;
+}
+
+cudaStream_t pick(lpg_elliptic* h, void* stream) {
+  return stream ? (cudaStream_t)stream : h->plat.stream;
+}
+
+}  // namespace
+
+// ================================================================ misc
+extern "C" const char* lpg_version(void) { return "libparanumal_gb300 0.1 (sm_103a)"; }
+
+extern "C" int lpg_device_malloc(void** ptr, uint64_t bytes) {
+  if (!ptr) return set_error(LPG_ERR_INVALID, "null ptr");
+  LPG_CUDA_TRY(cudaMalloc(ptr, bytes));
+  return LPG_OK;
+}
+extern "C" int lpg_device_free(void* ptr) {
+  LPG_CUDA_TRY(cudaFree(ptr));
+  return LPG_OK;
+}
+extern "C" int lpg_memcpy_h2d(void* dst, const void* src, uint64_t bytes, void* stream) {
+  LPG_CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, (cudaStream_t)stream));
+  return LPG_OK;
+}
+extern "C" int lpg_memcpy_d2h(void* dst, const void* src, uint64_t bytes, void* stream) {
+  LPG_CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+  return LPG_OK;
+}
+extern "C" int lpg_stream_sync(void* stream) {
+  LPG_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+  return LPG_OK;
+}
+
+// ================================================================ kernel entry points
+extern "C" int lpg_ogs_gather_add_f64(int64_t Nlocal, const int32_t* g2l, const double* v, double* gv, int64_t Nglobal,
+                                      void* stream) {
+  if (Nlocal < 0 || Nglobal < 0 || (Nlocal > 0 && (!g2l || !v)) || (Nglobal > 0 && !gv))
+    return set_error(LPG_ERR_INVALID, "ogs gather: bad arguments");
+  return gather_add<double>(Nlocal, g2l, v, gv, Nglobal, true, (cudaStream_t)stream);
+}
+extern "C" int lpg_ogs_gather_owner_f64(int64_t Nglobal, const int32_t* owner, const double* v, double* gv, void* stream) {
+  if (Nglobal < 0 || (Nglobal > 0 && (!owner || !v || !gv))) return set_error(LPG_ERR_INVALID, "ogs gather: bad arguments");
+  return gather_owner<double>(Nglobal, owner, v, gv, (cudaStream_t)stream);
+}
+extern "C" int lpg_ogs_scatter_f64(int64_t Nlocal, const int32_t* g2l, const double* gv, double* v, void* stream) {
+  if (Nlocal < 0 || (Nlocal > 0 && (!g2l || !gv || !v))) return set_error(LPG_ERR_INVALID, "ogs scatter: bad arguments");
+  return scatter<double>(Nlocal, g2l, gv, v, (cudaStream_t)stream);
+}
+extern "C" int lpg_axpy_f64(int64_t N, double alpha, const double* x, double beta, double* y, void* stream) {
+  if (N < 0 || (N > 0 && (!x || !y))) return set_error(LPG_ERR_INVALID, "axpy: bad arguments");
+  return axpy<double>(N, alpha, x, beta, y, (cudaStream_t)stream);
+}
+extern "C" int lpg_amxpy_f64(int64_t N, double alpha, const double* x, const double* y, double beta, double* z,
+                             void* stream) {
+  if (N < 0 || (N > 0 && (!x || !y || !z))) return set_error(LPG_ERR_INVALID, "amxpy: bad arguments");
+  return amxpy<double>(N, alpha, x, y, beta, z, (cudaStream_t)stream);
+}
+extern "C" int lpg_dot_f64(int64_t N, const double* x, const double* y, double* result_dev, void* stream) {
+  if (N < 0 || !result_dev || (N > 0 && (!x || !y))) return set_error(LPG_ERR_INVALID, "dot: bad arguments");
+  double* scratch;
+  int rc = reduction_scratch(&scratch);
+  if (rc) return rc;
+  return dot(N, x, y, result_dev, scratch, (cudaStream_t)stream);
+}
+extern "C" int lpg_norm2sq_f64(int64_t N, const double* x, double* result_dev, void* stream) {
+  return lpg_dot_f64(N, x, x, result_dev, stream);
+}
+extern "C" int lpg_pcg_update_f64(int64_t N, double alpha, const double* p, const double* Ap, double* x, double* r,
+                                  double* result_dev, void* stream) {
+  if (N < 0 || !result_dev || (N > 0 && (!p || !Ap || !x || !r))) return set_error(LPG_ERR_INVALID, "pcg update: bad arguments");
+  double* scratch;
+  int rc = reduction_scratch(&scratch);
+  if (rc) return rc;
+  return pcg_update(N, alpha, p, Ap, x, r, result_dev, scratch, (cudaStream_t)stream);
+}
+
+// ================================================================ solver objects
+extern "C" int lpg_elliptic_create(const char* settings, lpg_elliptic** out) {
+  if (!settings || !out) return set_error(LPG_ERR_INVALID, "null argument");
+  *out = nullptr;
+  LPG_GUARD_BEGIN
+  auto h = std::make_unique<lpg_elliptic>();
+  int rc = h->settings.parse(settings);
+  if (rc) return rc;
+  if ((rc = build(h.get()))) return rc;
+  *out = h.release();
+  return LPG_OK;
+  LPG_GUARD_END
+}
+
+extern "C" int lpg_elliptic_destroy(lpg_elliptic* e) {
+  LPG_GUARD_BEGIN
+  delete e;
+  return LPG_OK;
+  LPG_GUARD_END
+}
+
+extern "C" int64_t lpg_elliptic_info(const lpg_elliptic* e, int what) {
+  if (!e || !e->el) return -1;
+  switch (what) {
+    case LPG_INFO_NELEMENTS: return e->el->mesh.E;
+    case LPG_INFO_NP: return e->el->mesh.Np;
+    case LPG_INFO_NGLOBAL: return e->el->Nglobal;
+    case LPG_INFO_NLOCAL: return e->el->Nlocal;
+    case LPG_INFO_N: return e->el->mesh.N;
+    case LPG_INFO_ALLNEUMANN: return e->el->allNeumann ? 1 : 0;
+    case LPG_INFO_MG_PLEVELS: return e->precon ? e->precon->levels_p() : 0;
+    case LPG_INFO_MG_AMGLEVELS: return e->precon ? e->precon->levels_amg() : 0;
+    case LPG_INFO_COARSE_N: return e->precon ? e->precon->coarse_n() : 0;
+    case LPG_INFO_DEVICE_BYTES: return device_bytes_in_use();
+    default: return -1;
+  }
+}
+
+extern "C" int lpg_elliptic_get(const lpg_elliptic* e, const char* name, void* host_out, uint64_t bytes) {
+  if (!e || !name || !host_out) return set_error(LPG_ERR_INVALID, "null argument");
+  LPG_GUARD_BEGIN
+  Elliptic* el = e->el.get();
+  cudaStream_t s = e->plat.stream;
+  const std::string n(name);
+  const int64_t E = el->mesh.E, Np = el->mesh.Np;
+  auto need = [&](uint64_t b) { return bytes < b ? set_error(LPG_ERR_INVALID, "output buffer too small") : LPG_OK; };
+  int rc;
+  if (n == "GlobalToLocal") {
+    if ((rc = need(sizeof(int32_t) * el->Nlocal))) return rc;
+    return el->g2l.download((int32_t*)host_out, el->Nlocal, s);
+  }
+  if (n == "ownerLocal") {
+    if ((rc = need(sizeof(int32_t) * el->Nglobal))) return rc;
+    return el->owner.download((int32_t*)host_out, el->Nglobal, s);
+  }
+  if (n == "weightG") {
+    if ((rc = need(sizeof(double) * el->Nglobal))) return rc;
+    return el->weightG.download((double*)host_out, el->Nglobal, s);
+  }
+  if (n == "D") {
+    if ((rc = need(sizeof(double) * el->mesh.D.size()))) return rc;
+    std::memcpy(host_out, el->mesh.D.data(), sizeof(double) * el->mesh.D.size());
+    return LPG_OK;
+  }
+  if (n == "lambdaE") {
+    if (!el->hasLambdaE) return set_error(LPG_ERR_INVALID, "no lambda field");
+    if ((rc = need(sizeof(double) * E))) return rc;
+    std::memcpy(host_out, el->lambdaE_h.data(), sizeof(double) * E);
+    return LPG_OK;
+  }
+  if (n == "ggeo" || n == "wJ" || n == "geo") {
+    std::vector<double> geo(E * 7 * Np);
+    if ((rc = el->mesh.geo.download(geo.data(), E * 7 * Np, s))) return rc;
+    double* out = (double*)host_out;
+    if (n == "geo") {
+      if ((rc = need(sizeof(double) * E * 7 * Np))) return rc;
+      std::memcpy(out, geo.data(), sizeof(double) * E * 7 * Np);
+    } else if (n == "ggeo") {
+      if ((rc = need(sizeof(double) * E * 6 * Np))) return rc;
+      for (int64_t e2 = 0; e2 < E; ++e2) std::memcpy(out + e2 * 6 * Np, geo.data() + e2 * 7 * Np, sizeof(double) * 6 * Np);
+    } else {
+      if ((rc = need(sizeof(double) * E * Np))) return rc;
+      for (int64_t e2 = 0; e2 < E; ++e2) std::memcpy(out + e2 * Np, geo.data() + e2 * 7 * Np + 6 * Np, sizeof(double) * Np);
+    }
+    return LPG_OK;
+  }
+  if (n == "invDiag") {
+    if ((rc = need(sizeof(double) * el->Nglobal))) return rc;
+    DevBuf<double> d;
+    if ((rc = d.alloc(el->Nglobal)) || (rc = el->BuildDiagonal(d.p, s)) || (rc = inverse_f64(el->Nglobal, d.p, d.p, s)))
+      return rc;
+    return d.download((double*)host_out, el->Nglobal, s);
+  }
+  return set_error(LPG_ERR_INVALID, "unknown array name: " + n);
+  LPG_GUARD_END
+}
+
+extern "C" int lpg_elliptic_device_ptr(const lpg_elliptic* e, const char* name, void** ptr) {
+  if (!e || !name || !ptr) return set_error(LPG_ERR_INVALID, "null argument");
+  const std::string n(name);
+  if (n == "q_in") *ptr = e->q_in.p;
+  else if (n == "Aq_out") *ptr = e->Aq_out.p;
+  else if (n == "x") *ptr = e->x.p;
+  else if (n == "r") *ptr = e->r.p;
+  else if (n == "GlobalToLocal") *ptr = e->el->g2l.p;
+  else if (n == "geo") *ptr = e->el->mesh.geo.p;
+  else if (n == "D") *ptr = e->el->mesh.D_d.p;
+  else if (n == "stream") *ptr = (void*)e->plat.stream;
+  else return set_error(LPG_ERR_INVALID, "unknown device pointer name: " + n);
+  return LPG_OK;
+}
+
+extern "C" int lpg_elliptic_operator(lpg_elliptic* e, const double* q, double* Aq, void* stream) {
+  if (!e || !q || !Aq) return set_error(LPG_ERR_INVALID, "null argument");
+  LPG_GUARD_BEGIN
+  return e->el->Operator(q, Aq, pick(e, stream));
+  LPG_GUARD_END
+}
+
+extern "C" int lpg_elliptic_precon(lpg_elliptic* e, const double* r, double* z, void* stream) {
+  if (!e || !r || !z) return set_error(LPG_ERR_INVALID, "null argument");
+  LPG_GUARD_BEGIN
+  cudaStream_t s = pick(e, stream);
+  if (s != e->plat.stream) {
+    // the preconditioner's scratch lives on the object's stream: order the work
+    LPG_CUDA_TRY(cudaStreamSynchronize(s));
+    int rc = e->precon->apply(r, z, e->plat.stream);
+    if (rc) return rc;
+    LPG_CUDA_TRY(cudaStreamSynchronize(e->plat.stream));
+    return LPG_OK;
+  }
+  return e->precon->apply(r, z, s);
+  LPG_GUARD_END
+}
+
+extern "C" int lpg_elliptic_rhs(lpg_elliptic* e, double* r, void* stream) {
+  if (!e || !r) return set_error(LPG_ERR_INVALID, "null argument");
+  LPG_GUARD_BEGIN
+  (void)stream;
+  return e->el->BuildRhs(r, e->plat.stream);
+  LPG_GUARD_END
+}
+
+static int solve_impl(lpg_elliptic* e, double* x, double* r, double tol, int maxit, int* iters) {
+  Elliptic* el = e->el.get();
+  cudaStream_t s = e->plat.stream;
+  int rc;
+  if (el->allNeumann) {  // elliptic_t::Solve removes the mean of r (ellipticSolve.cpp:33-34)
+    if ((rc = sum(el->Nglobal, r, e->plat.scalars.p + 1, e->plat.partials.p, s))) return rc;
+    if ((rc = add_scalar(el->Nglobal, e->plat.scalars.p + 1, -el->allNeumannScale * el->allNeumannScale, r, s))) return rc;
+  }
+  PCGResult res;
+  if ((rc = pcg_solve(&e->plat, el, e->precon.get(), e->work, e->flexible, e->stopRhs, x, r, tol, maxit, res))) return rc;
+  if (iters) *iters = res.iters;
+  if (res.breakdown) return set_error(LPG_ERR_BREAKDOWN, "(F)PCG breakdown: non-positive p.Ap or non-finite residual");
+  if (res.iters >= maxit) return set_error(LPG_ERR_NOT_CONVERGED, "(F)PCG reached the iteration limit");
+  return LPG_OK;
+}
+
+extern "C" int lpg_elliptic_solve(lpg_elliptic* e, double* x, double* r, double tol, int maxit, int* iters) {
+  if (!e || !x || !r) return set_error(LPG_ERR_INVALID, "null argument");
+  LPG_GUARD_BEGIN
+  return solve_impl(e, x, r, tol, maxit, iters);
+  LPG_GUARD_END
+}
+
+extern "C" int lpg_elliptic_run(lpg_elliptic* e, double* xL_host, int* iters, double* norm, double* err,
+                                double* solve_seconds) {
+  if (!e) return set_error(LPG_ERR_INVALID, "null argument");
+  LPG_GUARD_BEGIN
+  Elliptic* el = e->el.get();
+  cudaStream_t s = e->plat.stream;
+  int rc;
+  if ((rc = el->BuildRhs(e->r.p, s))) return rc;
+  LPG_CUDA_TRY(cudaMemsetAsync(e->x.p, 0, sizeof(double) * el->Nglobal, s));
+  if (!e->xL.p && (rc = e->xL.alloc(el->Nlocal))) return rc;
+  LPG_CUDA_TRY(cudaStreamSynchronize(s));
+  const auto t0 = std::chrono::steady_clock::now();
+  int it = 0;
+  rc = solve_impl(e, e->x.p, e->r.p, e->tol, e->maxit, &it);
+  if (rc && rc != LPG_ERR_NOT_CONVERGED) return rc;
+  const int solveStatus = rc;
+  if ((rc = scatter<double>(el->Nlocal, el->g2l.p, e->x.p, e->xL.p, s))) return rc;
+  if ((rc = solution_norms(el->mesh.N, el->mesh.E, el->mesh.EX.p, el->mesh.EY.p, el->mesh.EZ.p, el->mesh.r1d_d.p,
+                           el->mesh.geo.p, el->g2l.p, el->rhsKind, e->xL.p, e->norms.p, s)))
+    return rc;
+  LPG_CUDA_TRY(cudaStreamSynchronize(s));
+  const auto t1 = std::chrono::steady_clock::now();
+  double nrm[2];
+  if ((rc = e->norms.download(nrm, 2, s))) return rc;
+  if (iters) *iters = it;
+  if (norm) *norm = std::sqrt(nrm[0]);
+  if (err) *err = (el->rhsKind == 0) ? std::sqrt(nrm[1]) : -1.0;
+  if (solve_seconds) *solve_seconds = std::chrono::duration<double>(t1 - t0).count();
+  if (xL_host && (rc = e->xL.download(xL_host, el->Nlocal, s))) return rc;
+  return solveStatus;
+  LPG_GUARD_END
+}

@@ -1,0 +1,313 @@
+// mesh_t / elliptic_t for structured hexahedral boxes.
+//
+// Host work is limited to what is O(elements): vertex coordinates (with optional
+// interior jitter), per-element dof offsets of the box numbering, the lambda field
+// and RHS source parameters. Node-level setup (geometric factors, GlobalToLocal,
+// owner copies, multiplicities) runs on the GPU.
+//
+// Reference counterparts: meshSetupBoxHex3D.cpp:31-232, meshReferenceNodesHex3D.cpp:31-74,
+// meshGeometricFactorsHex3D.cpp:31-193, meshConnectNodes.cpp:32-117,
+// ellipticBoundarySetup.cpp:30-140, ellipticOperator.cpp:29-106,
+// ellipticBuildOperatorDiagonal.cpp:998-1057, ellipticRun.cpp:139-185,
+// ellipticBuildOperatorMatrixContinuous.cpp:697-880.
+#include "objects.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace lpg {
+
+// ---------------------------------------------------------------- mesh
+int Mesh::setup(const MeshConfig& c, int N_, cudaStream_t s) {
+  cfg = c;
+  N = N_;
+  Nq = N + 1;
+  Np = Nq * Nq * Nq;
+  if (N < 1 || N > 8) return set_error(LPG_ERR_UNSUPPORTED, "POLYNOMIAL DEGREE must be 1..8");
+  if (c.nx < 1 || c.ny < 1 || c.nz < 1) return set_error(LPG_ERR_INVALID, "BOX NX/NY/NZ must be >= 1");
+  E = (int64_t)c.nx * c.ny * c.nz;
+  if (E * Np >= (int64_t)INT32_MAX) return set_error(LPG_ERR_UNSUPPORTED, "more than 2^31 local nodes");
+  gll_nodes_weights(N, r1d, w1d);
+  gll_derivative(N, r1d, D);
+
+  // vertex coordinates per element (meshSetupBoxHex3D.cpp:112-152) + interior jitter
+  const bool periodic = (c.bcflag == -1);
+  const double dx = c.dimx / c.nx, dy = c.dimy / c.ny, dz = c.dimz / c.nz;
+  const double X0 = -c.dimx / 2.0, Y0 = -c.dimy / 2.0, Z0 = -c.dimz / 2.0;
+  const int64_t NnX = periodic ? c.nx : c.nx + 1, NnY = periodic ? c.ny : c.ny + 1;
+  std::vector<double> ex(E * 8), ey(E * 8), ez(E * 8);
+  static const int ox[8] = {0, 1, 1, 0, 0, 1, 1, 0}, oy[8] = {0, 0, 1, 1, 0, 0, 1, 1}, oz[8] = {0, 0, 0, 0, 1, 1, 1, 1};
+#pragma omp parallel for
+  for (int64_t e = 0; e < E; ++e) {
+    const int i = (int)(e % c.nx), j = (int)((e / c.nx) % c.ny), k = (int)(e / ((int64_t)c.nx * c.ny));
+    for (int v = 0; v < 8; ++v) {
+      const int vi = i + ox[v], vj = j + oy[v], vk = k + oz[v];
+      double x = X0 + dx * i + (ox[v] ? dx : 0.0);
+      double y = Y0 + dy * j + (oy[v] ? dy : 0.0);
+      double z = Z0 + dz * k + (oz[v] ? dz : 0.0);
+      if (c.jitter != 0.0 && !periodic && vi > 0 && vi < c.nx && vj > 0 && vj < c.ny && vk > 0 && vk < c.nz) {
+        const uint64_t vid = (uint64_t)(vi + vj * NnX + (int64_t)vk * NnX * NnY);
+        x += (2.0 * hash_u01(c.jitterSeed, 0, vid) - 1.0) * c.jitter * dx;
+        y += (2.0 * hash_u01(c.jitterSeed, 1, vid) - 1.0) * c.jitter * dy;
+        z += (2.0 * hash_u01(c.jitterSeed, 2, vid) - 1.0) * c.jitter * dz;
+      }
+      ex[e * 8 + v] = x;
+      ey[e * 8 + v] = y;
+      ez[e * 8 + v] = z;
+    }
+  }
+  int rc;
+  if ((rc = EX.alloc(E * 8)) || (rc = EY.alloc(E * 8)) || (rc = EZ.alloc(E * 8))) return rc;
+  if ((rc = EX.upload(ex.data(), E * 8, s)) || (rc = EY.upload(ey.data(), E * 8, s)) ||
+      (rc = EZ.upload(ez.data(), E * 8, s)))
+    return rc;
+  if ((rc = D_d.alloc(Nq * Nq)) || (rc = r1d_d.alloc(Nq)) || (rc = w1d_d.alloc(Nq))) return rc;
+  if ((rc = D_d.upload(D.data(), Nq * Nq, s)) || (rc = r1d_d.upload(r1d.data(), Nq, s)) ||
+      (rc = w1d_d.upload(w1d.data(), Nq, s)))
+    return rc;
+  if ((rc = geo.alloc(E * 7 * Np))) return rc;
+  DevBuf<int> bad;
+  if ((rc = bad.alloc(1))) return rc;
+  LPG_CUDA_TRY(cudaMemsetAsync(bad.p, 0, sizeof(int), s));
+  if ((rc = geometric_factors(N, E, EX.p, EY.p, EZ.p, D_d.p, r1d_d.p, w1d_d.p, geo.p, bad.p, s))) return rc;
+  int nbad = 0;
+  if ((rc = bad.download(&nbad, 1, s))) return rc;
+  if (nbad) return set_error(LPG_ERR_INVALID, "negative or tiny Jacobian at " + std::to_string(nbad) + " nodes");
+  return LPG_OK;
+}
+
+int Mesh::make_f32(cudaStream_t s) {
+  if (geo32.p) return LPG_OK;
+  int rc;
+  if ((rc = geo32.alloc(E * 7 * Np)) || (rc = D32.alloc(Nq * Nq))) return rc;
+  if ((rc = convert<double, float>(E * 7 * Np, geo.p, geo32.p, s))) return rc;
+  return convert<double, float>(Nq * Nq, D_d.p, D32.p, s);
+}
+
+int Mesh::make_bf16(cudaStream_t s) {
+  if (geo16.p) return LPG_OK;
+  int rc;
+  if ((rc = geo16.alloc(E * 7 * Np))) return rc;
+  if ((rc = convert<double, __nv_bfloat16>(E * 7 * Np, geo.p, geo16.p, s))) return rc;
+  if (!D32.p) {
+    if ((rc = D32.alloc(Nq * Nq))) return rc;
+    return convert<double, float>(Nq * Nq, D_d.p, D32.p, s);
+  }
+  return LPG_OK;
+}
+
+// ---------------------------------------------------------------- elliptic
+int Elliptic::setup(Platform* p, const MeshConfig& c, int N, double lam, const std::vector<double>* lamE,
+                    cudaStream_t s) {
+  plat = p;
+  lambda = lam;
+  if (c.bcflag != 1 && c.bcflag != -1)
+    return set_error(LPG_ERR_UNSUPPORTED, "BOX BOUNDARY FLAG must be 1 (Dirichlet) or -1 (periodic)");
+  if (c.bcflag == -1 && (c.nx < 2 || c.ny < 2 || c.nz < 2))
+    return set_error(LPG_ERR_UNSUPPORTED, "periodic boxes need at least 2 elements per direction");
+  int rc = mesh.setup(c, N, s);
+  if (rc) return rc;
+  const int64_t E = mesh.E, Np = mesh.Np;
+  Nlocal = E * Np;
+
+  // per-element dof offsets of the box numbering (owned box of nodes per element)
+  const bool periodic = (c.bcflag == -1), dirichlet = (c.bcflag == 1);
+  auto range = [&](int e, int n, int& lo, int& hi) {
+    if (periodic) { lo = (e == 0) ? 0 : 1; hi = (e == n - 1) ? N - 1 : N; }
+    else if (dirichlet) { lo = 1; hi = (e == n - 1) ? N - 1 : N; }
+    else { lo = (e == 0) ? 0 : 1; hi = N; }
+  };
+  std::vector<int64_t> base(E + 1, 0);
+  for (int64_t e = 0; e < E; ++e) {
+    const int i = (int)(e % c.nx), j = (int)((e / c.nx) % c.ny), k = (int)(e / ((int64_t)c.nx * c.ny));
+    int lx, hx, ly, hy, lz, hz;
+    range(i, c.nx, lx, hx);
+    range(j, c.ny, ly, hy);
+    range(k, c.nz, lz, hz);
+    const int64_t cnt = (int64_t)std::max(0, hx - lx + 1) * std::max(0, hy - ly + 1) * std::max(0, hz - lz + 1);
+    base[e + 1] = base[e] + cnt;
+  }
+  Nglobal = base[E];
+  if (Nglobal <= 0) return set_error(LPG_ERR_INVALID, "no unknowns after masking");
+  DevBuf<int64_t> base_d;
+  DevBuf<int32_t> mult;
+  if ((rc = base_d.alloc(E + 1)) || (rc = base_d.upload(base.data(), E + 1, s))) return rc;
+  if ((rc = g2l.alloc(Nlocal)) || (rc = owner.alloc(Nglobal)) || (rc = mult.alloc(Nglobal)) ||
+      (rc = weightG.alloc(Nglobal)))
+    return rc;
+  BoxNumbering b{c.nx, c.ny, c.nz, N, periodic ? 1 : 0, dirichlet ? 1 : 0};
+  if ((rc = box_numbering(b, base_d.p, g2l.p, owner.p, mult.p, Nglobal, s))) return rc;
+  if ((rc = multiplicity_to_weight(Nglobal, mult.p, weightG.p, s))) return rc;
+
+  hasLambdaE = (lamE != nullptr);
+  allNeumann = (lam == 0.0 && !hasLambdaE && !dirichlet);
+  allNeumannScale = 1.0 / std::sqrt((double)Nglobal);
+  if (hasLambdaE) {
+    lambdaE_h = *lamE;
+    std::vector<float> l32(lambdaE_h.begin(), lambdaE_h.end());
+    if ((rc = lambdaE.alloc(E)) || (rc = lambdaE.upload(lambdaE_h.data(), E, s))) return rc;
+    if ((rc = lambdaE32.alloc(E)) || (rc = lambdaE32.upload(l32.data(), E, s))) return rc;
+  }
+  LPG_CUDA_TRY(cudaStreamSynchronize(s));
+  return LPG_OK;
+}
+
+int Elliptic::make_f32(bool bf16, cudaStream_t s) {
+  int rc = bf16 ? mesh.make_bf16(s) : mesh.make_f32(s);
+  if (rc) return rc;
+  if (!weightG32.p) {
+    if ((rc = weightG32.alloc(Nglobal))) return rc;
+    if ((rc = convert<double, float>(Nglobal, weightG.p, weightG32.p, s))) return rc;
+  }
+  return LPG_OK;
+}
+
+int Elliptic::Operator(const double* q, double* Aq, cudaStream_t s) {
+  AxArgs<double, double> a;
+  const int64_t Np = mesh.Np;
+  a.N = mesh.N; a.Nelements = mesh.E; a.g2l = g2l.p;
+  a.ggeo = mesh.geo.p; a.geoStride = 7 * Np; a.wJ = mesh.geo.p + 6 * Np; a.wJStride = 7 * Np;
+  a.D = mesh.D_d.p; a.lambda = lambda; a.lambdaE = hasLambdaE ? lambdaE.p : nullptr;
+  a.q = q; a.out = Aq; a.Nglobal = Nglobal;
+  return ax_hex<double, double>(a, AxMode::Assemble, s);
+}
+
+int Elliptic::OperatorF32(const float* q, float* Aq, Prec prec, cudaStream_t s) {
+  const int64_t Np = mesh.Np;
+  if (prec == Prec::BF16G) {
+    AxArgs<float, __nv_bfloat16> a;
+    a.N = mesh.N; a.Nelements = mesh.E; a.g2l = g2l.p;
+    a.ggeo = mesh.geo16.p; a.geoStride = 7 * Np; a.wJ = mesh.geo16.p + 6 * Np; a.wJStride = 7 * Np;
+    a.D = mesh.D32.p; a.lambda = (float)lambda; a.lambdaE = hasLambdaE ? lambdaE32.p : nullptr;
+    a.q = q; a.out = Aq; a.Nglobal = Nglobal;
+    return ax_hex<float, __nv_bfloat16>(a, AxMode::Assemble, s);
+  }
+  AxArgs<float, float> a;
+  a.N = mesh.N; a.Nelements = mesh.E; a.g2l = g2l.p;
+  a.ggeo = mesh.geo32.p; a.geoStride = 7 * Np; a.wJ = mesh.geo32.p + 6 * Np; a.wJStride = 7 * Np;
+  a.D = mesh.D32.p; a.lambda = (float)lambda; a.lambdaE = hasLambdaE ? lambdaE32.p : nullptr;
+  a.q = q; a.out = Aq; a.Nglobal = Nglobal;
+  return ax_hex<float, float>(a, AxMode::Assemble, s);
+}
+
+int Elliptic::BuildDiagonal(double* diagG, cudaStream_t s) {
+  DevBuf<double> dL;
+  int rc = dL.alloc(Nlocal);
+  if (rc) return rc;
+  const double boost = allNeumann ? allNeumannScale * allNeumannScale : 0.0;
+  if ((rc = operator_diagonal_local(mesh.N, mesh.E, mesh.geo.p, mesh.D_d.p, lambda,
+                                    hasLambdaE ? lambdaE.p : nullptr, g2l.p, boost, dL.p, s)))
+    return rc;
+  if ((rc = gather_add<double>(Nlocal, g2l.p, dL.p, diagG, Nglobal, true, s))) return rc;
+  LPG_CUDA_TRY(cudaStreamSynchronize(s));
+  return LPG_OK;
+}
+
+int Elliptic::BuildRhs(double* r, cudaStream_t s) {
+  DevBuf<double> rL, gL;
+  int rc;
+  if ((rc = rL.alloc(Nlocal)) || (rc = gL.alloc(Nlocal))) return rc;
+  RhsSpec spec{rhsKind, (int)(sources.size() / 4), sources_d.p};
+  if ((rc = rhs_local(mesh.N, mesh.E, mesh.EX.p, mesh.EY.p, mesh.EZ.p, mesh.r1d_d.p, mesh.geo.p,
+                      hasLambdaE ? lambdaE.p : nullptr, lambda, g2l.p, spec, rL.p, gL.p, s)))
+    return rc;
+  if (rhsKind == 0 && mesh.cfg.bcflag == 1) {
+    // Dirichlet lifting rhs -= A_e g (ellipticRhsBCHex3D.okl:60-290)
+    AxArgs<double, double> a;
+    const int64_t Np = mesh.Np;
+    a.N = mesh.N; a.Nelements = mesh.E; a.g2l = g2l.p;
+    a.ggeo = mesh.geo.p; a.geoStride = 7 * Np; a.wJ = mesh.geo.p + 6 * Np; a.wJStride = 7 * Np;
+    a.D = mesh.D_d.p; a.lambda = lambda; a.lambdaE = hasLambdaE ? lambdaE.p : nullptr;
+    a.q = gL.p; a.out = rL.p;
+    if ((rc = ax_hex<double, double>(a, AxMode::LocalInSubtract, s))) return rc;
+  }
+  if ((rc = gather_add<double>(Nlocal, g2l.p, rL.p, r, Nglobal, true, s))) return rc;
+  LPG_CUDA_TRY(cudaStreamSynchronize(s));
+  return LPG_OK;
+}
+
+// Assembled stiffness (+ lambda mass) of this degree on the host, sorted (row, col)
+// with duplicates summed; element entries below 1e-7 are dropped as in the reference.
+int Elliptic::BuildMatrix(std::vector<int64_t>& rows, std::vector<int32_t>& cols, std::vector<double>& vals,
+                          cudaStream_t s) {
+  const int Nq = mesh.Nq, Np = mesh.Np;
+  const int64_t E = mesh.E;
+  std::vector<double> geo(E * 7 * Np);
+  std::vector<int32_t> map(Nlocal);
+  int rc;
+  if ((rc = mesh.geo.download(geo.data(), E * 7 * Np, s)) || (rc = g2l.download(map.data(), Nlocal, s))) return rc;
+  const double* Dm = mesh.D.data();
+  struct NZ { int64_t row; int32_t col; double val; };
+  std::vector<std::vector<NZ>> parts;
+  int nthreads = 1;
+#ifdef _OPENMP
+  nthreads = omp_get_max_threads();
+#endif
+  parts.resize(nthreads);
+#pragma omp parallel
+  {
+    int tid = 0;
+#ifdef _OPENMP
+    tid = omp_get_thread_num();
+#endif
+    std::vector<NZ>& out = parts[tid];
+#pragma omp for schedule(static)
+    for (int64_t e = 0; e < E; ++e) {
+      const double* gg = geo.data() + e * 7 * Np;
+      const double lam = hasLambdaE ? lambdaE_h[e] : lambda;
+      for (int nz = 0; nz < Nq; nz++) for (int ny = 0; ny < Nq; ny++) for (int nx = 0; nx < Nq; nx++) {
+        const int idn = nx + ny * Nq + nz * Nq * Nq;
+        const int32_t gn = map[e * Np + idn];
+        if (gn < 0) continue;
+        for (int mz = 0; mz < Nq; mz++) for (int my = 0; my < Nq; my++) for (int mx = 0; mx < Nq; mx++) {
+          const int idm = mx + my * Nq + mz * Nq * Nq;
+          const int32_t gm = map[e * Np + idm];
+          if (gm < 0) continue;
+          double val = 0;
+          int id;
+          if (ny == my && nz == mz)
+            for (int k = 0; k < Nq; k++) { id = k + ny * Nq + nz * Nq * Nq; val += gg[0 * Np + id] * Dm[nx + k * Nq] * Dm[mx + k * Nq]; }
+          if (nz == mz) {
+            id = mx + ny * Nq + nz * Nq * Nq; val += gg[1 * Np + id] * Dm[nx + mx * Nq] * Dm[my + ny * Nq];
+            id = nx + my * Nq + nz * Nq * Nq; val += gg[1 * Np + id] * Dm[mx + nx * Nq] * Dm[ny + my * Nq];
+          }
+          if (ny == my) {
+            id = mx + ny * Nq + nz * Nq * Nq; val += gg[2 * Np + id] * Dm[nx + mx * Nq] * Dm[mz + nz * Nq];
+            id = nx + ny * Nq + mz * Nq * Nq; val += gg[2 * Np + id] * Dm[mx + nx * Nq] * Dm[nz + mz * Nq];
+          }
+          if (nx == mx && nz == mz)
+            for (int k = 0; k < Nq; k++) { id = nx + k * Nq + nz * Nq * Nq; val += gg[3 * Np + id] * Dm[ny + k * Nq] * Dm[my + k * Nq]; }
+          if (nx == mx) {
+            id = nx + my * Nq + nz * Nq * Nq; val += gg[4 * Np + id] * Dm[ny + my * Nq] * Dm[mz + nz * Nq];
+            id = nx + ny * Nq + mz * Nq * Nq; val += gg[4 * Np + id] * Dm[my + ny * Nq] * Dm[nz + mz * Nq];
+          }
+          if (nx == mx && ny == my)
+            for (int k = 0; k < Nq; k++) { id = nx + ny * Nq + k * Nq * Nq; val += gg[5 * Np + id] * Dm[nz + k * Nq] * Dm[mz + k * Nq]; }
+          if (nx == mx && ny == my && nz == mz) val += gg[6 * Np + idn] * lam;
+          if (std::fabs(val) >= 1e-7) out.push_back(NZ{gn, gm, val});
+        }
+      }
+    }
+  }
+  size_t total = 0;
+  for (auto& p : parts) total += p.size();
+  std::vector<NZ> all;
+  all.reserve(total);
+  for (auto& p : parts) { all.insert(all.end(), p.begin(), p.end()); std::vector<NZ>().swap(p); }
+  std::stable_sort(all.begin(), all.end(), [](const NZ& a, const NZ& b) {
+    return a.row < b.row || (a.row == b.row && a.col < b.col);
+  });
+  rows.clear(); cols.clear(); vals.clear();
+  rows.reserve(all.size() / 4); cols.reserve(all.size() / 4); vals.reserve(all.size() / 4);
+  for (size_t i = 0; i < all.size(); ++i) {
+    if (!rows.empty() && rows.back() == all[i].row && cols.back() == all[i].col) vals.back() += all[i].val;
+    else { rows.push_back(all[i].row); cols.push_back(all[i].col); vals.push_back(all[i].val); }
+  }
+  return LPG_OK;
+}
+
+}  // namespace lpg

@@ -1,0 +1,854 @@
+// p-multigrid V-cycle over a parAlmond-style smoothed-aggregation AMG coarse hierarchy.
+//
+// p-levels (matrix-free, device): ellipticPreconMultiGrid.cpp:31-154 and
+// ellipticPreconMultiGridLevel.cpp:30-473 (Chebyshev / damped Jacobi smoothing,
+// weighted restriction, prolongation, Arnoldi estimate of rho(D^{-1}A) from a drand48
+// start vector). The p-levels run in FP64, FP32, or FP32 with BF16 geometric factors.
+// AMG levels (assembled CSR, FP64): parAlmondAMGSetup.cpp:35-144 (setup on the host,
+// as in the reference), parAlmondVcycle.cpp:34-60, parAlmondAMGSmoother.cpp:35-160,
+// parAlmondCoarseExact.cpp:35-227 (dense inverse of the <= 1000-row base level).
+// The drand48 stream is seeded with 0 and consumed in the reference's order: p-level
+// Arnoldi vectors, then per AMG level the Arnoldi vector and the MIS-2 priorities.
+#include "objects.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <type_traits>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace lpg {
+
+// ================================================================ host sparse matrices
+struct NZ {
+  int64_t r;
+  int32_t c;
+  double v;
+};
+
+struct HCSR {
+  int64_t n = 0, m = 0;
+  std::vector<int64_t> rs;
+  std::vector<int32_t> cols;
+  std::vector<double> vals;
+  int64_t nnz() const { return (int64_t)cols.size(); }
+};
+
+static HCSR csr_from_coo(int64_t n, int64_t m, std::vector<NZ>& e) {
+  std::stable_sort(e.begin(), e.end(), [](const NZ& a, const NZ& b) { return a.r < b.r || (a.r == b.r && a.c < b.c); });
+  HCSR A;
+  A.n = n;
+  A.m = m;
+  A.rs.assign(n + 1, 0);
+  A.cols.reserve(e.size());
+  A.vals.reserve(e.size());
+  int64_t lastR = -1;
+  int32_t lastC = -1;
+  for (const NZ& z : e) {
+    if (z.r == lastR && z.c == lastC) { A.vals.back() += z.v; continue; }
+    A.cols.push_back(z.c);
+    A.vals.push_back(z.v);
+    A.rs[z.r + 1]++;
+    lastR = z.r;
+    lastC = z.c;
+  }
+  for (int64_t i = 0; i < n; ++i) A.rs[i + 1] += A.rs[i];
+  return A;
+}
+
+static void spmv_host(const HCSR& A, const double* x, double* y) {
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < A.n; ++i) {
+    double s = 0;
+    for (int64_t j = A.rs[i]; j < A.rs[i + 1]; ++j) s += A.vals[j] * x[A.cols[j]];
+    y[i] = s;
+  }
+}
+
+static HCSR transpose(const HCSR& A) {
+  HCSR T;
+  T.n = A.m;
+  T.m = A.n;
+  T.rs.assign(T.n + 1, 0);
+  for (int32_t c : A.cols) T.rs[c + 1]++;
+  for (int64_t i = 0; i < T.n; ++i) T.rs[i + 1] += T.rs[i];
+  T.cols.resize(A.nnz());
+  T.vals.resize(A.nnz());
+  std::vector<int64_t> pos(T.rs.begin(), T.rs.end() - 1);
+  for (int64_t i = 0; i < A.n; ++i)
+    for (int64_t j = A.rs[i]; j < A.rs[i + 1]; ++j) {
+      const int64_t p = pos[A.cols[j]]++;
+      T.cols[p] = (int32_t)i;
+      T.vals[p] = A.vals[j];
+    }
+  return T;
+}
+
+// C = A B by rows with a dense accumulator; columns of each row sorted.
+static HCSR spmm(const HCSR& A, const HCSR& B) {
+  HCSR C;
+  C.n = A.n;
+  C.m = B.m;
+  C.rs.assign(A.n + 1, 0);
+  int nth = 1;
+#ifdef _OPENMP
+  nth = omp_get_max_threads();
+#endif
+  std::vector<std::vector<int32_t>> pc(nth);
+  std::vector<std::vector<double>> pv(nth);
+  std::vector<int64_t> chunkStart(nth + 1, 0);
+  std::vector<int64_t> rowCount(A.n, 0);
+#pragma omp parallel
+  {
+    int t = 0;
+#ifdef _OPENMP
+    t = omp_get_thread_num();
+#endif
+    const int64_t lo = A.n * t / nth, hi = A.n * (t + 1) / nth;
+    std::vector<double> acc(B.m, 0.0);
+    std::vector<int32_t> mark(B.m, -1), list;
+    for (int64_t i = lo; i < hi; ++i) {
+      list.clear();
+      for (int64_t j = A.rs[i]; j < A.rs[i + 1]; ++j) {
+        const int32_t k = A.cols[j];
+        const double a = A.vals[j];
+        for (int64_t jj = B.rs[k]; jj < B.rs[k + 1]; ++jj) {
+          const int32_t c = B.cols[jj];
+          if (mark[c] != (int32_t)i) { mark[c] = (int32_t)i; acc[c] = 0.0; list.push_back(c); }
+          acc[c] += a * B.vals[jj];
+        }
+      }
+      std::sort(list.begin(), list.end());
+      for (int32_t c : list) { pc[t].push_back(c); pv[t].push_back(acc[c]); }
+      rowCount[i] = (int64_t)list.size();
+    }
+  }
+  for (int64_t i = 0; i < A.n; ++i) C.rs[i + 1] = C.rs[i] + rowCount[i];
+  C.cols.reserve(C.rs[A.n]);
+  C.vals.reserve(C.rs[A.n]);
+  for (int t = 0; t < nth; ++t) {
+    C.cols.insert(C.cols.end(), pc[t].begin(), pc[t].end());
+    C.vals.insert(C.vals.end(), pv[t].begin(), pv[t].end());
+  }
+  return C;
+}
+
+// ================================================================ device CSR
+struct DCSR {
+  int64_t n = 0, m = 0;
+  DevBuf<int64_t> rs;
+  DevBuf<int32_t> cols;
+  DevBuf<double> vals;
+  int upload(const HCSR& A, cudaStream_t s) {
+    n = A.n;
+    m = A.m;
+    int rc;
+    if ((rc = rs.alloc(n + 1)) || (rc = rs.upload(A.rs.data(), n + 1, s))) return rc;
+    if (A.nnz() > 0) {
+      if ((rc = cols.alloc(A.nnz())) || (rc = cols.upload(A.cols.data(), A.nnz(), s))) return rc;
+      if ((rc = vals.alloc(A.nnz())) || (rc = vals.upload(A.vals.data(), A.nnz(), s))) return rc;
+    }
+    return LPG_OK;
+  }
+};
+
+// ================================================================ AMG setup (host)
+struct ALevel {
+  HCSR A, P, R;
+  DCSR dA, dP, dR;
+  std::vector<double> diagA, diagInv;
+  DevBuf<double> dDiagInv;
+  double rho = 0, lambda0 = 0, lambda1 = 0, jlambda = 0;
+  DevBuf<double> rhs, x, res, s1, s2, s3;
+};
+
+// parCSR::rhoDinvA (parAlmondparCSR.cpp:351-440): 10-step Arnoldi on D^{-1}A on the host.
+static double rho_dinv_a(const HCSR& A, const std::vector<double>& diagInv, Rand48& rng) {
+  const int64_t N = A.n;
+  int k = 10;
+  if (k > N) k = (int)N;
+  std::vector<double> H(k * k, 0.0);
+  std::vector<std::vector<double>> V(k + 1, std::vector<double>(N));
+  std::vector<double> Vx(N);
+  for (int64_t n = 0; n < N; ++n) Vx[n] = rng.next();
+  double nrm = 0;
+  for (int64_t n = 0; n < N; ++n) nrm += Vx[n] * Vx[n];
+  nrm = std::sqrt(nrm);
+  for (int64_t n = 0; n < N; ++n) V[0][n] = Vx[n] * (1.0 / nrm);
+  for (int j = 0; j < k; ++j) {
+    spmv_host(A, V[j].data(), V[j + 1].data());
+    for (int64_t n = 0; n < N; ++n) V[j + 1][n] *= diagInv[n];
+    for (int i = 0; i <= j; ++i) {
+      double hij = 0;
+      for (int64_t n = 0; n < N; ++n) hij += V[i][n] * V[j + 1][n];
+      for (int64_t n = 0; n < N; ++n) V[j + 1][n] += -hij * V[i][n];
+      H[i + j * k] = hij;
+    }
+    if (j + 1 < k) {
+      double nj = 0;
+      for (int64_t n = 0; n < N; ++n) nj += V[j + 1][n] * V[j + 1][n];
+      nj = std::sqrt(nj);
+      H[j + 1 + j * k] = nj;
+      for (int64_t n = 0; n < N; ++n) V[j + 1][n] *= (1. / nj);
+    }
+  }
+  return hessenberg_spectral_radius(k, H);
+}
+
+static void diag_setup(ALevel& L, Rand48& rng) {
+  const int64_t N = L.A.n;
+  L.diagA.assign(N, 0.0);
+  L.diagInv.assign(N, 0.0);
+  for (int64_t i = 0; i < N; ++i)
+    for (int64_t j = L.A.rs[i]; j < L.A.rs[i + 1]; ++j)
+      if (L.A.cols[j] == i) L.diagA[i] = L.A.vals[j];
+  for (int64_t i = 0; i < N; ++i) L.diagInv[i] = (L.diagA[i] != 0.0) ? 1.0 / L.diagA[i] : 0.0;
+  L.rho = rho_dinv_a(L.A, L.diagInv, rng);
+}
+
+static bool custom_less(int smax, double rmax, int64_t imax, int s, double r, int64_t i) {
+  if (s > smax) return true;
+  if (smax > s) return false;
+  if (r > rmax) return true;
+  if (rmax > r) return false;
+  return i > imax;
+}
+
+// Strength of connection (parAlmondStrongGraph.cpp) and distance-2 maximal independent
+// set aggregation (parAlmondFormAggregates.cpp:54-251).
+static int64_t form_aggregates(const ALevel& L, double theta, bool rugeStuben, std::vector<int64_t>& F2C, Rand48& rng) {
+  const HCSR& A = L.A;
+  const int64_t N = A.n;
+  std::vector<int64_t> Crs(N + 1, 0);
+  std::vector<int64_t> Ccols;
+  Ccols.reserve(A.nnz());
+  for (int64_t i = 0; i < N; ++i) {
+    if (rugeStuben) {
+      const int sign = (L.diagA[i] >= 0) ? 1 : -1;
+      double maxOD = 0;
+      for (int64_t jj = A.rs[i]; jj < A.rs[i + 1]; ++jj) {
+        if (A.cols[jj] == i) continue;
+        const double OD = -sign * A.vals[jj];
+        if (OD > maxOD) maxOD = OD;
+      }
+      for (int64_t jj = A.rs[i]; jj < A.rs[i + 1]; ++jj) {
+        const int64_t col = A.cols[jj];
+        if (col == i) { Ccols.push_back(col); continue; }
+        if (-sign * A.vals[jj] > theta * maxOD) Ccols.push_back(col);
+      }
+    } else {
+      const double Aii = std::fabs(L.diagA[i]);
+      for (int64_t jj = A.rs[i]; jj < A.rs[i + 1]; ++jj) {
+        const int64_t col = A.cols[jj];
+        if (col == i) { Ccols.push_back(col); continue; }
+        const double Ajj = std::fabs(L.diagA[col]);
+        if (std::fabs(A.vals[jj]) > theta * std::sqrt(Aii * Ajj)) Ccols.push_back(col);
+      }
+    }
+    Crs[i + 1] = (int64_t)Ccols.size();
+  }
+  std::vector<double> rands(N), Tr(N);
+  std::vector<int> states(N, 0), Ts(N);
+  std::vector<int64_t> Ti(N), Tc(N);
+  for (int64_t i = 0; i < N; ++i) rands[i] = rng.next();
+  std::vector<int> colCnt(N, 0);
+  for (int64_t c : Ccols) colCnt[c]++;
+  for (int64_t i = 0; i < N; ++i) rands[i] += colCnt[i];
+  for (;;) {
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < N; ++i) {
+      int smax = states[i];
+      double rmax = rands[i];
+      int64_t imax = i;
+      if (smax != 1)
+        for (int64_t jj = Crs[i]; jj < Crs[i + 1]; ++jj) {
+          const int64_t col = Ccols[jj];
+          if (col == i) continue;
+          if (custom_less(smax, rmax, imax, states[col], rands[col], col)) { smax = states[col]; rmax = rands[col]; imax = col; }
+        }
+      Ts[i] = smax; Tr[i] = rmax; Ti[i] = imax;
+    }
+    int64_t undecided = 0;
+#pragma omp parallel for schedule(static) reduction(+ : undecided)
+    for (int64_t i = 0; i < N; ++i) {
+      int smax = Ts[i];
+      double rmax = Tr[i];
+      int64_t imax = Ti[i];
+      for (int64_t jj = Crs[i]; jj < Crs[i + 1]; ++jj) {
+        const int64_t col = Ccols[jj];
+        if (col == i) continue;
+        if (custom_less(smax, rmax, imax, Ts[col], Tr[col], Ti[col])) { smax = Ts[col]; rmax = Tr[col]; imax = Ti[col]; }
+      }
+      if (states[i] == 0 && imax == i) states[i] = 1;
+      if (states[i] == 0 && smax == 1) states[i] = -1;
+      if (states[i] == 0) undecided++;
+    }
+    if (undecided == 0) break;
+  }
+  int64_t numAggs = 0;
+  F2C.assign(N, -1);
+  for (int64_t i = 0; i < N; ++i)
+    if (states[i] == 1) F2C[i] = numAggs++;
+  // first neighbours: the pass reads F2C of MIS nodes only, so it is order independent
+  for (int64_t i = 0; i < N; ++i) {
+    int smax = states[i];
+    double rmax = rands[i];
+    int64_t imax = i, cmax = F2C[i];
+    if (smax != 1)
+      for (int64_t jj = Crs[i]; jj < Crs[i + 1]; ++jj) {
+        const int64_t col = Ccols[jj];
+        if (col == i) continue;
+        if (custom_less(smax, rmax, imax, states[col], rands[col], col)) {
+          smax = states[col]; rmax = rands[col]; imax = col; cmax = F2C[col];
+        }
+      }
+    Ts[i] = smax; Tr[i] = rmax; Ti[i] = imax; Tc[i] = cmax;
+    if (F2C[i] == -1 && smax == 1 && cmax > -1) F2C[i] = cmax;
+  }
+  std::vector<int64_t> F2Cnew(F2C);
+  for (int64_t i = 0; i < N; ++i) {
+    int smax = Ts[i];
+    double rmax = Tr[i];
+    int64_t imax = Ti[i], cmax = Tc[i];
+    for (int64_t jj = Crs[i]; jj < Crs[i + 1]; ++jj) {
+      const int64_t col = Ccols[jj];
+      if (col == i) continue;
+      if (custom_less(smax, rmax, imax, Ts[col], Tr[col], Ti[col])) { smax = Ts[col]; rmax = Tr[col]; imax = Ti[col]; cmax = Tc[col]; }
+    }
+    if (F2Cnew[i] == -1 && smax == 1 && cmax > -1) F2Cnew[i] = cmax;
+  }
+  F2C.swap(F2Cnew);
+  return numAggs;
+}
+
+// coarsenAmgLevel (parAlmondCoarsenLevel.cpp:33-84)
+static int amg_coarsen(ALevel& L, ALevel& Lc, std::vector<double>& nullv, double theta, bool rs, bool unsmoothed,
+                       Rand48& rng) {
+  const int64_t N = L.A.n;
+  std::vector<int64_t> F2C;
+  const int64_t Nc = form_aggregates(L, theta, rs, F2C, rng);
+  for (int64_t i = 0; i < N; ++i)
+    if (F2C[i] < 0) return set_error(LPG_ERR_INVALID, "AMG: unaggregated row");
+  // tentative prolongator with normalised columns (parAlmondTentativeProlongator.cpp:33-94)
+  HCSR T;
+  T.n = N; T.m = Nc;
+  T.rs.resize(N + 1);
+  T.cols.resize(N);
+  T.vals.resize(N);
+  for (int64_t i = 0; i <= N; ++i) T.rs[i] = i;
+  std::vector<double> cn(Nc, 0.0);
+  for (int64_t i = 0; i < N; ++i) { T.cols[i] = (int32_t)F2C[i]; T.vals[i] = nullv[i]; cn[F2C[i]] += nullv[i] * nullv[i]; }
+  for (int64_t c = 0; c < Nc; ++c) cn[c] = std::sqrt(cn[c]);
+  for (int64_t i = 0; i < N; ++i) T.vals[i] /= cn[T.cols[i]];
+  nullv.assign(cn.begin(), cn.end());
+  if (!unsmoothed) {
+    // P = (I - omega D^{-1} A) T, omega = 4/3/rho (parAlmondSmoothPrologator.cpp:33-301)
+    const double omega = (4. / 3.) / L.rho;
+    std::vector<NZ> pe;
+    pe.reserve(L.A.nnz() + N);
+    for (int64_t i = 0; i < N; ++i) {
+      pe.push_back(NZ{i, T.cols[i], T.vals[i]});
+      const double invDi = 1.0 / L.diagA[i];
+      for (int64_t j = L.A.rs[i]; j < L.A.rs[i + 1]; ++j) {
+        const int32_t col = L.A.cols[j];
+        pe.push_back(NZ{i, T.cols[col], -omega * invDi * L.A.vals[j] * T.vals[col]});
+      }
+    }
+    L.P = csr_from_coo(N, Nc, pe);
+  } else {
+    L.P = T;
+  }
+  L.R = transpose(L.P);
+  HCSR AP = spmm(L.A, L.P);
+  Lc.A = spmm(L.R, AP);
+  diag_setup(Lc, rng);
+  return LPG_OK;
+}
+
+// dense inverse by LU with partial pivoting (row-major, in place)
+static int dense_inverse(int64_t n, std::vector<double>& A) {
+  std::vector<double> LU(A);
+  std::vector<int64_t> piv(n);
+  for (int64_t k = 0; k < n; ++k) {
+    int64_t p = k;
+    double amax = std::fabs(LU[k * n + k]);
+    for (int64_t i = k + 1; i < n; ++i)
+      if (std::fabs(LU[i * n + k]) > amax) { amax = std::fabs(LU[i * n + k]); p = i; }
+    piv[k] = p;
+    if (amax == 0.0) return set_error(LPG_ERR_INVALID, "AMG coarse matrix is singular");
+    if (p != k)
+      for (int64_t j = 0; j < n; ++j) std::swap(LU[k * n + j], LU[p * n + j]);
+    const double inv = 1.0 / LU[k * n + k];
+#pragma omp parallel for schedule(static)
+    for (int64_t i = k + 1; i < n; ++i) {
+      const double l = LU[i * n + k] * inv;
+      LU[i * n + k] = l;
+      if (l != 0.0)
+        for (int64_t j = k + 1; j < n; ++j) LU[i * n + j] -= l * LU[k * n + j];
+    }
+  }
+#pragma omp parallel for schedule(static)
+  for (int64_t j = 0; j < n; ++j) {
+    std::vector<double> col(n, 0.0);
+    col[j] = 1.0;
+    for (int64_t k = 0; k < n; ++k)
+      if (piv[k] != k) std::swap(col[k], col[piv[k]]);
+    for (int64_t i = 0; i < n; ++i) {
+      double s = col[i];
+      for (int64_t q = 0; q < i; ++q) s -= LU[i * n + q] * col[q];
+      col[i] = s;
+    }
+    for (int64_t i = n - 1; i >= 0; --i) {
+      double s = col[i];
+      for (int64_t q = i + 1; q < n; ++q) s -= LU[i * n + q] * col[q];
+      col[i] = s / LU[i * n + i];
+    }
+    for (int64_t i = 0; i < n; ++i) A[i * n + j] = col[i];
+  }
+  return LPG_OK;
+}
+
+// ================================================================ p-level
+struct PLevel {
+  Elliptic* el = nullptr;
+  Elliptic* elC = nullptr;
+  int Nf = 0, Nc = 0;
+  double lambda0 = 0, lambda1 = 0;
+  DevBuf<double> invDiag64, P64;
+  DevBuf<float> invDiag32, P32;
+  DevBuf<double> rhs64, x64, res64;  // this level's vectors (levels > 0 own rhs/x)
+  DevBuf<float> rhs32, x32, res32;
+};
+
+class MultiGrid : public Precon {
+ public:
+  Platform* plat = nullptr;
+  Elliptic* fine = nullptr;
+  MGOptions opt;
+  std::vector<std::unique_ptr<Elliptic>> owned;
+  std::vector<std::unique_ptr<PLevel>> p;
+  std::vector<std::unique_ptr<ALevel>> a;
+  DevBuf<double> coarseInv;
+  int64_t coarseN = 0;
+  // smoother scratch (largest p-level)
+  DevBuf<double> s64[3];
+  DevBuf<float> s32[3];
+  // coarse vectors of the last p-level, FP64 view for the AMG hierarchy
+  DevBuf<double> aRhs0, aX0;
+  DevBuf<float> in32, out32;
+
+  int levels_p() const override { return (int)p.size(); }
+  int levels_amg() const override { return (int)a.size(); }
+  int64_t coarse_n() const override { return coarseN; }
+
+  int setup(Elliptic* el, const MeshConfig& c, const MGOptions& o);
+  int apply(const double* r, double* z, cudaStream_t s) override;
+
+ private:
+  bool f32() const { return opt.prec != Prec::F64; }
+  template <typename T> T* vec(DevBuf<double>& d, DevBuf<float>& f);
+  template <typename T> int op(Elliptic* el, const T* q, T* Aq, cudaStream_t s);
+  template <typename T> int smooth(PLevel& L, const T* r, T* x, bool xIsZero, cudaStream_t s);
+  template <typename T> int vcycle_p(int k, const T* rhs, T* x, cudaStream_t s);
+  int vcycle_a(int k, const double* rhs, double* x, cudaStream_t s);
+  int smooth_a(ALevel& L, const double* b, double* x, bool xIsZero, cudaStream_t s);
+  int setup_amg(Elliptic* el, Rand48& rng);
+};
+
+template <> double* MultiGrid::vec<double>(DevBuf<double>& d, DevBuf<float>&) { return d.p; }
+template <> float* MultiGrid::vec<float>(DevBuf<double>&, DevBuf<float>& f) { return f.p; }
+
+template <>
+int MultiGrid::op<double>(Elliptic* el, const double* q, double* Aq, cudaStream_t s) {
+  return el->Operator(q, Aq, s);
+}
+template <>
+int MultiGrid::op<float>(Elliptic* el, const float* q, float* Aq, cudaStream_t s) {
+  return el->OperatorF32(q, Aq, opt.prec, s);
+}
+
+// ---------------------------------------------------------------- p-level smoothing
+template <typename T>
+int MultiGrid::smooth(PLevel& L, const T* r, T* X, bool xIsZero, cudaStream_t s) {
+  const int64_t N = L.el->Nglobal;
+  T* invDiag = vec<T>(L.invDiag64, L.invDiag32);
+  T* RES = vec<T>(s64[0], s32[0]);
+  T* Ad = vec<T>(s64[1], s32[1]);
+  T* d = vec<T>(s64[2], s32[2]);
+  int rc;
+  if (opt.smoother == 1) {  // damped Jacobi, invDiag pre-scaled by 4/3/rho
+    if (xIsZero) return amxpy<T>(N, T(1), invDiag, r, T(0), X, s);
+    if ((rc = op<T>(L.el, X, RES, s))) return rc;
+    if ((rc = axpy<T>(N, T(1), r, T(-1), RES, s))) return rc;
+    return amxpy<T>(N, T(1), invDiag, RES, T(1), X, s);
+  }
+  const double theta = 0.5 * (L.lambda1 + L.lambda0);
+  const double delta = 0.5 * (L.lambda1 - L.lambda0);
+  const double invTheta = 1.0 / theta;
+  const double sigma = theta / delta;
+  double rho_n = 1. / sigma, rho_np1;
+  if (xIsZero) {
+    if ((rc = amxpy<T>(N, T(1), invDiag, r, T(0), RES, s))) return rc;
+  } else {
+    if ((rc = op<T>(L.el, X, RES, s))) return rc;
+    if ((rc = axpy<T>(N, T(1), r, T(-1), RES, s))) return rc;
+    if ((rc = amxpy<T>(N, T(1), invDiag, RES, T(0), RES, s))) return rc;
+  }
+  if ((rc = axpy<T>(N, (T)invTheta, RES, T(0), d, s))) return rc;
+  for (int k = 0; k < opt.chebDegree; ++k) {
+    if (xIsZero && k == 0) rc = axpy<T>(N, T(1), d, T(0), X, s);
+    else rc = axpy<T>(N, T(1), d, T(1), X, s);
+    if (rc) return rc;
+    if ((rc = op<T>(L.el, d, Ad, s))) return rc;
+    rho_np1 = 1.0 / (2. * sigma - rho_n);
+    const double rhoDivDelta = 2.0 * rho_np1 / delta;
+    if ((rc = cheb_update<T>(N, invDiag, Ad, RES, d, (T)(rho_np1 * rho_n), (T)rhoDivDelta, s))) return rc;
+    rho_n = rho_np1;
+  }
+  return axpy<T>(N, T(1), d, T(1), X, s);
+}
+
+template <typename T>
+int MultiGrid::vcycle_p(int k, const T* RHS, T* X, cudaStream_t s) {
+  PLevel& L = *p[k];
+  const int64_t N = L.el->Nglobal;
+  T* RES = vec<T>(L.res64, L.res32);
+  int rc;
+  if ((rc = smooth<T>(L, RHS, X, true, s))) return rc;
+  if ((rc = op<T>(L.el, X, RES, s))) return rc;
+  if ((rc = axpy<T>(N, T(1), RHS, T(-1), RES, s))) return rc;
+  const bool last = (k + 1 == (int)p.size());
+  T* weight = vec<T>(L.el->weightG, L.el->weightG32);
+  const T* P = vec<T>(L.P64, L.P32);
+  if (!last) {
+    T* rhsC = vec<T>(p[k + 1]->rhs64, p[k + 1]->rhs32);
+    T* xC = vec<T>(p[k + 1]->x64, p[k + 1]->x32);
+    if ((rc = pmg_coarsen<T>(L.Nf, L.Nc, L.el->mesh.E, L.el->g2l.p, weight, RES, P, L.elC->g2l.p, rhsC,
+                             L.elC->Nglobal, s)))
+      return rc;
+    if ((rc = vcycle_p<T>(k + 1, rhsC, xC, s))) return rc;
+    if ((rc = pmg_prolongate_map<T>(L.Nf, L.Nc, L.el->mesh.E, L.elC->g2l.p, xC, P, L.el->g2l.p, L.el->owner.p,
+                                    X, s)))
+      return rc;
+  } else {
+    // coarse space of the last p-level = level 0 of the FP64 AMG hierarchy
+    const int64_t NC = L.elC->Nglobal;
+    const T* xCT = nullptr;
+    if constexpr (std::is_same<T, double>::value) {
+      if ((rc = pmg_coarsen<T>(L.Nf, L.Nc, L.el->mesh.E, L.el->g2l.p, weight, RES, P, L.elC->g2l.p, aRhs0.p, NC,
+                               s)))
+        return rc;
+      if ((rc = vcycle_a(0, aRhs0.p, aX0.p, s))) return rc;
+      xCT = aX0.p;
+    } else {
+      if ((rc = pmg_coarsen<T>(L.Nf, L.Nc, L.el->mesh.E, L.el->g2l.p, weight, RES, P, L.elC->g2l.p, in32.p, NC,
+                               s)))
+        return rc;
+      if ((rc = convert<float, double>(NC, in32.p, aRhs0.p, s))) return rc;
+      if ((rc = vcycle_a(0, aRhs0.p, aX0.p, s))) return rc;
+      if ((rc = convert<double, float>(NC, aX0.p, out32.p, s))) return rc;
+      xCT = out32.p;
+    }
+    if ((rc = pmg_prolongate_map<T>(L.Nf, L.Nc, L.el->mesh.E, L.elC->g2l.p, xCT, P, L.el->g2l.p, L.el->owner.p, X,
+                                    s)))
+      return rc;
+  }
+  return smooth<T>(L, RHS, X, false, s);
+}
+
+// ---------------------------------------------------------------- AMG V-cycle (device)
+int MultiGrid::smooth_a(ALevel& L, const double* b, double* x, bool xIsZero, cudaStream_t s) {
+  const int64_t N = L.A.n;
+  int rc;
+  if (opt.amgSmoother == 1) {
+    if (xIsZero) return amxpy<double>(N, L.jlambda, L.dDiagInv.p, b, 0.0, x, s);
+    // d = lambda D^{-1}(b - A x); x += d
+    if ((rc = csr_cheb_residual(N, L.dA.rs.p, L.dA.cols.p, L.dA.vals.p, 0.0, 1.0, L.dDiagInv.p, b, x, L.s1.p, s)))
+      return rc;
+    return axpy<double>(N, L.jlambda, L.s1.p, 1.0, x, s);
+  }
+  const double theta = 0.5 * (L.lambda1 + L.lambda0);
+  const double delta = 0.5 * (L.lambda1 - L.lambda0);
+  const double invTheta = 1.0 / theta;
+  const double sigma = theta / delta;
+  double rho_n = 1. / sigma, rho_np1;
+  double* d = L.s1.p;
+  double* r = L.s2.p;
+  if (xIsZero) {
+    if ((rc = csr_cheb_start(N, invTheta, L.dDiagInv.p, b, r, d, x, s))) return rc;
+  } else {
+    if ((rc = csr_cheb_residual(N, L.dA.rs.p, L.dA.cols.p, L.dA.vals.p, 0.0, 1.0, L.dDiagInv.p, b, x, r, s))) return rc;
+    if ((rc = csr_cheb_update(N, 0.0, invTheta, opt.amgChebDegree == 0, r, d, x, s))) return rc;
+  }
+  for (int k = 0; k < opt.amgChebDegree; ++k) {
+    if ((rc = csr_cheb_residual(N, L.dA.rs.p, L.dA.cols.p, L.dA.vals.p, 1.0, 0.0, L.dDiagInv.p, b, d, r, s))) return rc;
+    rho_np1 = 1.0 / (2. * sigma - rho_n);
+    if ((rc = csr_cheb_update(N, rho_np1 * rho_n, 2.0 * rho_np1 / delta, k == opt.amgChebDegree - 1, r, d, x, s)))
+      return rc;
+    rho_n = rho_np1;
+  }
+  return LPG_OK;
+}
+
+int MultiGrid::vcycle_a(int k, const double* RHS, double* X, cudaStream_t s) {
+  if (k == (int)a.size() - 1) return gemv(coarseN, coarseInv.p, RHS, X, s);
+  ALevel& L = *a[k];
+  ALevel& C = *a[k + 1];
+  const int64_t N = L.A.n;
+  int rc;
+  if ((rc = smooth_a(L, RHS, X, true, s))) return rc;
+  if ((rc = csr_spmv(N, L.dA.rs.p, L.dA.cols.p, L.dA.vals.p, -1.0, X, 0.0, L.res.p, s))) return rc;
+  if ((rc = axpy<double>(N, 1.0, RHS, 1.0, L.res.p, s))) return rc;
+  if ((rc = csr_spmv(L.R.n, L.dR.rs.p, L.dR.cols.p, L.dR.vals.p, 1.0, L.res.p, 0.0, C.rhs.p, s))) return rc;
+  if ((rc = vcycle_a(k + 1, C.rhs.p, C.x.p, s))) return rc;
+  if ((rc = csr_spmv(N, L.dP.rs.p, L.dP.cols.p, L.dP.vals.p, 1.0, C.x.p, 1.0, X, s))) return rc;
+  return smooth_a(L, RHS, X, false, s);
+}
+
+int MultiGrid::apply(const double* r, double* z, cudaStream_t s) {
+  int rc;
+  if (p.empty()) {
+    rc = vcycle_a(0, r, z, s);
+  } else if (!f32()) {
+    rc = vcycle_p<double>(0, r, z, s);
+  } else {
+    const int64_t N = fine->Nglobal;
+    PLevel& L0 = *p[0];
+    if ((rc = convert<double, float>(N, r, L0.rhs32.p, s))) return rc;
+    if ((rc = vcycle_p<float>(0, L0.rhs32.p, L0.x32.p, s))) return rc;
+    rc = convert<float, double>(N, L0.x32.p, z, s);
+  }
+  if (rc) return rc;
+  if (fine->allNeumann) {  // ZeroMean (ellipticZeroMean.cpp:29-37)
+    if ((rc = sum(fine->Nglobal, z, plat->scalars.p + 1, plat->partials.p, s))) return rc;
+    rc = add_scalar(fine->Nglobal, plat->scalars.p + 1, -fine->allNeumannScale * fine->allNeumannScale, z, s);
+  }
+  return rc;
+}
+
+// ---------------------------------------------------------------- setup
+int MultiGrid::setup_amg(Elliptic* el, Rand48& rng) {
+  cudaStream_t s = plat->stream;
+  std::vector<int64_t> rows;
+  std::vector<int32_t> cols;
+  std::vector<double> vals;
+  int rc = el->BuildMatrix(rows, cols, vals, s);
+  if (rc) return rc;
+  auto L0 = std::make_unique<ALevel>();
+  L0->A.n = L0->A.m = el->Nglobal;
+  L0->A.rs.assign(el->Nglobal + 1, 0);
+  for (int64_t r0 : rows) L0->A.rs[r0 + 1]++;
+  for (int64_t i = 0; i < el->Nglobal; ++i) L0->A.rs[i + 1] += L0->A.rs[i];
+  L0->A.cols.swap(cols);
+  L0->A.vals.swap(vals);
+  std::vector<int64_t>().swap(rows);
+  diag_setup(*L0, rng);
+  a.push_back(std::move(L0));
+  const int64_t Nrows = a[0]->A.n;
+  std::vector<double> nullv(Nrows, 1.0 / std::sqrt((double)Nrows));
+  const int64_t target = 1000;
+  int64_t globalSize = Nrows;
+  double theta = opt.amgRugeStuben ? 0.5 : 0.08;
+  if (globalSize > target) {
+    for (;;) {
+      ALevel& L = *a.back();
+      if (opt.amgSmoother == 1) L.jlambda = (4. / 3.) / L.rho;
+      else { L.lambda1 = L.rho; L.lambda0 = L.rho / 10.; }
+      auto Lc = std::make_unique<ALevel>();
+      if ((rc = amg_coarsen(L, *Lc, nullv, theta, opt.amgRugeStuben, opt.amgUnsmoothed, rng))) return rc;
+      a.push_back(std::move(Lc));
+      if (!opt.amgRugeStuben) theta /= 2;
+      const int64_t coarseSize = a.back()->A.n;
+      if (coarseSize <= target || globalSize < 2 * coarseSize) break;
+      globalSize = coarseSize;
+    }
+  }
+  // exact coarse solver: dense inverse (+ null-space penalty for all-Neumann problems)
+  ALevel& B = *a.back();
+  coarseN = B.A.n;
+  std::vector<double> dense(coarseN * coarseN, 0.0);
+  for (int64_t i = 0; i < coarseN; ++i)
+    for (int64_t j = B.A.rs[i]; j < B.A.rs[i + 1]; ++j) dense[i * coarseN + B.A.cols[j]] = B.A.vals[j];
+  if (el->allNeumann)
+    for (int64_t i = 0; i < coarseN; ++i)
+      for (int64_t j = 0; j < coarseN; ++j) dense[i * coarseN + j] += nullv[i] * nullv[j];
+  if ((rc = dense_inverse(coarseN, dense))) return rc;
+  if ((rc = coarseInv.alloc(coarseN * coarseN)) || (rc = coarseInv.upload(dense.data(), coarseN * coarseN, s))) return rc;
+  // device copies and work vectors
+  for (size_t k = 0; k < a.size(); ++k) {
+    ALevel& L = *a[k];
+    const int64_t n = L.A.n;
+    if ((rc = L.rhs.alloc(n)) || (rc = L.x.alloc(n)) || (rc = L.res.alloc(n)) || (rc = L.s1.alloc(n)) ||
+        (rc = L.s2.alloc(n)))
+      return rc;
+    if (k + 1 < a.size()) {
+      if ((rc = L.dA.upload(L.A, s)) || (rc = L.dP.upload(L.P, s)) || (rc = L.dR.upload(L.R, s))) return rc;
+      if ((rc = L.dDiagInv.alloc(n)) || (rc = L.dDiagInv.upload(L.diagInv.data(), n, s))) return rc;
+    }
+  }
+  return LPG_OK;
+}
+
+int MultiGrid::setup(Elliptic* el, const MeshConfig& c, const MGOptions& o) {
+  fine = el;
+  plat = el->plat;
+  opt = o;
+  cudaStream_t s = plat->stream;
+  Rand48 rng;
+  rng.seed(0);  // srand48(rank) in buildParAlmondKernels (parAlmondKernels.cpp:55-58)
+  int rc;
+  if (o.amgOnly) {
+    if ((rc = setup_amg(el, rng))) return rc;
+    return LPG_OK;
+  }
+  const std::vector<int>& deg = o.degrees;
+  Elliptic* cur = el;
+  size_t maxN = 0;
+  for (size_t l = 0; l + 1 < deg.size(); ++l) {
+    auto L = std::make_unique<PLevel>();
+    L->el = cur;
+    L->Nf = deg[l];
+    L->Nc = deg[l + 1];
+    const int64_t N = cur->Nglobal;
+    maxN = std::max<size_t>(maxN, (size_t)N);
+    // smoother setup (SetupSmoother, ellipticPreconMultiGridLevel.cpp:345-383)
+    DevBuf<double> diag;
+    if ((rc = diag.alloc(N)) || (rc = cur->BuildDiagonal(diag.p, s))) return rc;
+    if ((rc = L->invDiag64.alloc(N)) || (rc = inverse_f64(N, diag.p, L->invDiag64.p, s))) return rc;
+    {
+      // maxEigSmoothAx (ellipticPreconMultiGridLevel.cpp:393-473), FP64 on the device
+      int k = 10;
+      if (k > N) k = (int)N;
+      std::vector<double> H(k * k, 0.0), Vx(N);
+      for (int64_t i = 0; i < N; ++i) Vx[i] = rng.next();
+      std::vector<std::unique_ptr<DevBuf<double>>> V;
+      for (int i = 0; i <= k; ++i) {
+        V.push_back(std::make_unique<DevBuf<double>>());
+        if ((rc = V.back()->alloc(N))) return rc;
+      }
+      DevBuf<double> AVx;
+      if ((rc = AVx.alloc(N)) || (rc = AVx.upload(Vx.data(), N, s))) return rc;
+      double nrm2;
+      if ((rc = plat->norm2sq(N, AVx.p, nrm2))) return rc;
+      if ((rc = axpy<double>(N, 1. / std::sqrt(nrm2), AVx.p, 0.0, V[0]->p, s))) return rc;
+      for (int j = 0; j < k; ++j) {
+        if ((rc = cur->Operator(V[j]->p, AVx.p, s))) return rc;
+        if ((rc = amxpy<double>(N, 1.0, L->invDiag64.p, AVx.p, 0.0, V[j + 1]->p, s))) return rc;
+        for (int i = 0; i <= j; ++i) {
+          double hij;
+          if ((rc = plat->dot(N, V[i]->p, V[j + 1]->p, hij))) return rc;
+          if ((rc = axpy<double>(N, -hij, V[i]->p, 1.0, V[j + 1]->p, s))) return rc;
+          H[i + j * k] = hij;
+        }
+        if (j + 1 < k) {
+          double nj2;
+          if ((rc = plat->norm2sq(N, V[j + 1]->p, nj2))) return rc;
+          const double nj = std::sqrt(nj2);
+          if ((rc = axpy<double>(N, 0.0, V[j + 1]->p, 1.0 / nj, V[j + 1]->p, s))) return rc;
+          H[j + 1 + j * k] = nj;
+        }
+      }
+      const double rho = hessenberg_spectral_radius(k, H);
+      if (o.smoother == 0) {
+        L->lambda1 = rho;
+        L->lambda0 = rho / 10.;
+      } else {
+        L->lambda0 = (4. / 3.) / rho;
+        if ((rc = axpy<double>(N, 0.0, L->invDiag64.p, L->lambda0, L->invDiag64.p, s))) return rc;
+      }
+    }
+    std::vector<double> P;
+    gll_interpolation(L->Nc, L->Nf, P);
+    if ((rc = L->P64.alloc((int64_t)P.size())) || (rc = L->P64.upload(P.data(), (int64_t)P.size(), s))) return rc;
+    // next (coarser) level
+    auto next = std::make_unique<Elliptic>();
+    if ((rc = next->setup(plat, c, L->Nc, el->lambda, el->hasLambdaE ? &el->lambdaE_h : nullptr, s))) return rc;
+    L->elC = next.get();
+    cur = next.get();
+    owned.push_back(std::move(next));
+    p.push_back(std::move(L));
+  }
+  if ((rc = setup_amg(cur, rng))) return rc;
+  // work vectors and reduced-precision copies
+  const int64_t NC = cur->Nglobal;
+  if ((rc = aRhs0.alloc(NC)) || (rc = aX0.alloc(NC))) return rc;
+  for (size_t k = 0; k < p.size(); ++k) {
+    PLevel& L = *p[k];
+    const int64_t N = L.el->Nglobal;
+    if (!f32()) {
+      if ((rc = L.res64.alloc(N))) return rc;
+      if (k > 0 && ((rc = L.rhs64.alloc(N)) || (rc = L.x64.alloc(N)))) return rc;
+    } else {
+      if ((rc = L.el->make_f32(opt.prec == Prec::BF16G, s))) return rc;
+      if ((rc = L.res32.alloc(N)) || (rc = L.rhs32.alloc(N)) || (rc = L.x32.alloc(N))) return rc;
+      if ((rc = L.invDiag32.alloc(N)) || (rc = convert<double, float>(N, L.invDiag64.p, L.invDiag32.p, s))) return rc;
+      if ((rc = L.P32.alloc(L.P64.n)) || (rc = convert<double, float>(L.P64.n, L.P64.p, L.P32.p, s))) return rc;
+      L.invDiag64.release();
+    }
+  }
+  if (f32()) {
+    if ((rc = in32.alloc(NC)) || (rc = out32.alloc(NC))) return rc;
+    for (int i = 0; i < 3; ++i)
+      if ((rc = s32[i].alloc((int64_t)maxN))) return rc;
+  } else {
+    for (int i = 0; i < 3; ++i)
+      if ((rc = s64[i].alloc((int64_t)maxN))) return rc;
+  }
+  LPG_CUDA_TRY(cudaStreamSynchronize(s));
+  return LPG_OK;
+}
+
+std::unique_ptr<Precon> make_multigrid(Elliptic* el, const MeshConfig& c, const MGOptions& o, int* status) {
+  auto mg = std::make_unique<MultiGrid>();
+  *status = mg->setup(el, c, o);
+  if (*status) return nullptr;
+  return mg;
+}
+
+// ================================================================ Identity / Jacobi
+class IdentityPrecon : public Precon {
+ public:
+  Elliptic* el;
+  explicit IdentityPrecon(Elliptic* e) : el(e) {}
+  int apply(const double* r, double* z, cudaStream_t s) override {
+    LPG_CUDA_TRY(cudaMemcpyAsync(z, r, sizeof(double) * el->Nglobal, cudaMemcpyDeviceToDevice, s));
+    return LPG_OK;
+  }
+};
+
+class JacobiPrecon : public Precon {
+ public:
+  Elliptic* el;
+  DevBuf<double> invDiag;
+  explicit JacobiPrecon(Elliptic* e) : el(e) {}
+  int apply(const double* r, double* z, cudaStream_t s) override {
+    int rc = amxpy<double>(el->Nglobal, 1.0, invDiag.p, r, 0.0, z, s);
+    if (rc) return rc;
+    if (el->allNeumann) {
+      Platform* plat = el->plat;
+      if ((rc = sum(el->Nglobal, z, plat->scalars.p + 1, plat->partials.p, s))) return rc;
+      rc = add_scalar(el->Nglobal, plat->scalars.p + 1, -el->allNeumannScale * el->allNeumannScale, z, s);
+    }
+    return rc;
+  }
+};
+
+std::unique_ptr<Precon> make_identity(Elliptic* el) { return std::make_unique<IdentityPrecon>(el); }
+
+std::unique_ptr<Precon> make_jacobi(Elliptic* el, int* status) {
+  auto j = std::make_unique<JacobiPrecon>(el);
+  DevBuf<double> diag;
+  cudaStream_t s = el->plat->stream;
+  int rc;
+  if ((rc = diag.alloc(el->Nglobal)) || (rc = el->BuildDiagonal(diag.p, s)) || (rc = j->invDiag.alloc(el->Nglobal)) ||
+      (rc = inverse_f64(el->Nglobal, diag.p, j->invDiag.p, s))) {
+    *status = rc;
+    return nullptr;
+  }
+  *status = LPG_OK;
+  return j;
+}
+
+}  // namespace lpg

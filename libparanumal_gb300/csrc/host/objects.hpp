@@ -1,0 +1,183 @@
+// Host-side objects mirroring the reference's class surface for the C0 hex path:
+// settings_t, platform_t, mesh_t, ogs (masked, Signed + unique), elliptic_t, precon_t
+// (Identity / Jacobi / MultiGrid with p-levels and parAlmond AMG levels) and the
+// (flexible) PCG linear solver. Device arrays live in HBM; host code orchestrates.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+
+#include <cstdint>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../lpg_internal.hpp"
+#include "../lpg_errors.hpp"
+
+namespace lpg {
+
+int set_error(int status, const std::string& msg);
+
+// ---------------------------------------------------------------- settings_t
+// Parses the reference's .rc format: "[KEY]" lines followed by a value line.
+struct Settings {
+  std::map<std::string, std::string> kv;
+  int parse(const std::string& text);      // LPG_OK or LPG_ERR_SETTINGS
+  std::string get(const std::string& k, const std::string& def) const;
+  int geti(const std::string& k, int def) const;
+  double getd(const std::string& k, double def) const;
+  bool is(const std::string& k, const std::string& v) const { return get(k, "") == v; }
+};
+
+// ---------------------------------------------------------------- device buffers
+template <typename T>
+struct DevBuf {
+  T* p = nullptr;
+  int64_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  int alloc(int64_t count);
+  int upload(const T* host, int64_t count, cudaStream_t s);
+  int download(T* host, int64_t count, cudaStream_t s) const;
+  void release();
+  int64_t bytes() const { return n * (int64_t)sizeof(T); }
+};
+
+int64_t device_bytes_in_use();
+
+// ---------------------------------------------------------------- drand48 stream
+struct Rand48 {
+  uint64_t x = 0;
+  void seed(long s) { x = (((uint64_t)(uint32_t)s) << 16) | 0x330EULL; }
+  double next() {
+    x = (0x5DEECE66DULL * x + 0xBULL) & ((1ULL << 48) - 1);
+    return (double)x * (1.0 / 281474976710656.0);
+  }
+};
+
+uint64_t splitmix64(uint64_t x);
+double hash_u01(uint64_t seed, uint64_t stream, uint64_t key);
+
+// ---------------------------------------------------------------- 1D basis
+void gll_nodes_weights(int N, std::vector<double>& x, std::vector<double>& w);
+void gll_derivative(int N, const std::vector<double>& x, std::vector<double>& D);
+// Interpolation from GLL(Nc) to GLL(Nf): P[i*(Nc+1)+m] = l_m(x_i)
+void gll_interpolation(int Nc, int Nf, std::vector<double>& P);
+double hessenberg_spectral_radius(int k, const std::vector<double>& Hcolmajor);
+
+// ---------------------------------------------------------------- platform_t
+struct Platform {
+  cudaStream_t stream = nullptr;
+  DevBuf<double> partials;   // reduction partial sums
+  DevBuf<double> scalars;    // device scalars for reductions
+  double* hostScalars = nullptr;  // pinned mirror
+  int init();
+  ~Platform();
+  // blocking reductions (one device->host copy per call, as linAlg.cpp:172-185)
+  int dot(int64_t n, const double* x, const double* y, double& out);
+  int norm2sq(int64_t n, const double* x, double& out) { return dot(n, x, x, out); }
+  int sum(int64_t n, const double* x, double& out);
+};
+
+// ---------------------------------------------------------------- mesh_t (one degree)
+struct MeshConfig {
+  int nx = 10, ny = 10, nz = 10;
+  double dimx = 10, dimy = 10, dimz = 10;
+  int bcflag = 1;
+  double jitter = 0.0;
+  uint64_t jitterSeed = 0;
+};
+
+struct Mesh {
+  MeshConfig cfg;
+  int N = 0, Nq = 0, Np = 0;
+  int64_t E = 0;
+  std::vector<double> r1d, w1d, D;
+  DevBuf<double> EX, EY, EZ;      // [E][8]
+  DevBuf<double> D_d, r1d_d, w1d_d;
+  DevBuf<double> geo;             // [E][7][Np] FP64
+  DevBuf<float> geo32, D32;       // FP32 copies (preconditioner)
+  DevBuf<__nv_bfloat16> geo16;    // BF16 copy
+  int setup(const MeshConfig& c, int N, cudaStream_t s);
+  int make_f32(cudaStream_t s);
+  int make_bf16(cudaStream_t s);
+};
+
+// ---------------------------------------------------------------- elliptic_t
+enum class Prec { F64 = 0, F32 = 1, BF16G = 2 };
+
+struct Elliptic {
+  Platform* plat = nullptr;
+  Mesh mesh;
+  double lambda = 0;
+  bool hasLambdaE = false;
+  std::vector<double> lambdaE_h;
+  DevBuf<double> lambdaE;
+  DevBuf<float> lambdaE32;
+  int64_t Nglobal = 0, Nlocal = 0;
+  bool allNeumann = false;
+  double allNeumannScale = 1;
+  DevBuf<int32_t> g2l, owner;
+  DevBuf<double> weightG;
+  DevBuf<float> weightG32;
+  int rhsKind = 0;                 // 0 sine, 1 Gaussian sources
+  std::vector<double> sources;     // nsources*4
+  DevBuf<double> sources_d;
+
+  int setup(Platform* p, const MeshConfig& c, int N, double lambda, const std::vector<double>* lamE,
+            cudaStream_t s);
+  int make_f32(bool bf16, cudaStream_t s);
+  int Operator(const double* q, double* Aq, cudaStream_t s);
+  int OperatorF32(const float* q, float* Aq, Prec prec, cudaStream_t s);
+  int BuildDiagonal(double* diagG, cudaStream_t s);   // assembled diag(A)
+  int BuildRhs(double* r, cudaStream_t s);            // forcing + lifting, gathered
+  // host copy of the assembled N-degree stiffness (+lambda mass), COO sorted (row, col)
+  int BuildMatrix(std::vector<int64_t>& rows, std::vector<int32_t>& cols, std::vector<double>& vals,
+                  cudaStream_t s);
+};
+
+// ---------------------------------------------------------------- preconditioners
+struct Precon {
+  virtual ~Precon() = default;
+  virtual int apply(const double* r, double* z, cudaStream_t s) = 0;
+  virtual int levels_p() const { return 0; }
+  virtual int levels_amg() const { return 0; }
+  virtual int64_t coarse_n() const { return 0; }
+};
+
+std::unique_ptr<Precon> make_identity(Elliptic* el);
+std::unique_ptr<Precon> make_jacobi(Elliptic* el, int* status);
+struct MGOptions {
+  std::vector<int> degrees;       // fine..1
+  int smoother = 0;               // 0 Chebyshev, 1 damped Jacobi
+  int chebDegree = 2;
+  Prec prec = Prec::F64;
+  int amgSmoother = 0;
+  int amgChebDegree = 2;
+  bool amgUnsmoothed = false;
+  bool amgRugeStuben = false;
+  bool amgOnly = false;           // PARALMOND: AMG on the fine matrix
+};
+std::unique_ptr<Precon> make_multigrid(Elliptic* el, const MeshConfig& c, const MGOptions& o, int* status);
+
+// ---------------------------------------------------------------- linear solver
+struct PCGResult {
+  int iters = 0;
+  double rdotr = 0;
+  bool breakdown = false;
+};
+struct PCGWork {
+  DevBuf<double> p, z, Ax, Ap;
+  int ensure(int64_t n);
+};
+int pcg_solve(Platform* plat, Elliptic* el, Precon* pc, PCGWork& w, bool flexible, bool stopRhs,
+              double* x, double* r, double tol, int maxit, PCGResult& res);
+
+// degree schedule of the p-multigrid hierarchy (ellipticPreconMultiGrid.cpp:49-84)
+std::vector<int> degree_schedule(int N, const std::string& coarsening, const std::vector<int>& explicitList);
+
+}  // namespace lpg

@@ -1,0 +1,130 @@
+// Internal (C++) interfaces between the host objects and the CUDA kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <cstdint>
+
+namespace lpg {
+
+
+// ---------------------------------------------------------------- operator
+enum class AxMode { Assemble, AccumulateAssembled, PartialLocal, LocalInSubtract };
+
+template <typename T, typename G>
+struct AxArgs {
+  int N = 0;
+  int64_t Nelements = 0;
+  const int32_t* elementList = nullptr;
+  const int32_t* g2l = nullptr;
+  const G* ggeo = nullptr;
+  int64_t geoStride = 0;
+  const G* wJ = nullptr;
+  int64_t wJStride = 0;
+  const T* D = nullptr;
+  T lambda = 0;
+  const T* lambdaE = nullptr;
+  const T* q = nullptr;
+  T* out = nullptr;
+  int64_t Nglobal = 0;
+};
+
+template <typename T, typename G>
+int ax_hex(const AxArgs<T, G>& a, AxMode mode, cudaStream_t s);
+
+// ---------------------------------------------------------------- setup kernels
+// Geometric factors of trilinear hexahedra from their 8 vertices
+// (meshPhysicalNodesHex3D.cpp + meshGeometricFactorsHex3D.cpp), packed [e][7][Np]:
+// G00,G01,G02,G11,G12,G22,wJ. Counts nodes with J < 1e-12 into *badCount (device).
+int geometric_factors(int N, int64_t E, const double* EX, const double* EY, const double* EZ,
+                      const double* D, const double* r1d, const double* w1d, double* geo,
+                      int* badCount, cudaStream_t s);
+
+// Box-mesh numbering (closed form of ConnectNodes + ogs ordering): GlobalToLocal per
+// local node, ownerLocal per dof and multiplicity per dof.
+struct BoxNumbering {
+  int nx, ny, nz, N;
+  int periodic;       // BOX BOUNDARY FLAG == -1
+  int dirichlet;      // faces are Dirichlet (flag 1)
+};
+int box_numbering(const BoxNumbering& b, const int64_t* elemBase, int32_t* g2l, int32_t* owner,
+                  int32_t* mult, int64_t Nglobal, cudaStream_t s);
+
+// Right-hand side forcing * wJ per local node and Dirichlet data g at masked nodes.
+struct RhsSpec {
+  int kind;            // 0 sine, 1 Gaussian sources
+  int nsources;
+  const double* src;   // nsources * 4: cx, cy, cz, w (device)
+};
+int rhs_local(int N, int64_t E, const double* EX, const double* EY, const double* EZ,
+              const double* r1d, const double* geo, const double* lambdaE, double lambda,
+              const int32_t* g2l, RhsSpec spec, double* rL, double* gL, cudaStream_t s);
+// Solution norm / error: sum of wJ*xL^2 and wJ*(xL-u)^2 (u manufactured, sine only) into
+// out[0], out[1] (device). xL gets Dirichlet data at masked nodes.
+int solution_norms(int N, int64_t E, const double* EX, const double* EY, const double* EZ,
+                   const double* r1d, const double* geo, const int32_t* g2l, int kind, double* xL,
+                   double* out, cudaStream_t s);
+// Operator diagonal per local node (ellipticBuildOperatorDiagonal.cpp:998-1057).
+int operator_diagonal_local(int N, int64_t E, const double* geo, const double* D, double lambda,
+                            const double* lambdaE, const int32_t* g2l, double rankBoost,
+                            double* diagL, cudaStream_t s);
+
+// ---------------------------------------------------------------- ogs + vectors
+template <typename T>
+int gather_add(int64_t Nlocal, const int32_t* g2l, const T* v, T* gv, int64_t Nglobal, bool zero,
+               cudaStream_t s);
+template <typename T>
+int gather_owner(int64_t Nglobal, const int32_t* owner, const T* v, T* gv, cudaStream_t s);
+template <typename T>
+int scatter(int64_t Nlocal, const int32_t* g2l, const T* gv, T* v, cudaStream_t s);
+
+// y = a x + b y (b == 0 ignores y)
+template <typename T> int axpy(int64_t N, T a, const T* x, T b, T* y, cudaStream_t s);
+// z = a x.*y + b z
+template <typename T> int amxpy(int64_t N, T a, const T* x, const T* y, T b, T* z, cudaStream_t s);
+template <typename T> int fill(int64_t N, T v, T* x, cudaStream_t s);
+template <typename Tin, typename Tout> int convert(int64_t N, const Tin* x, Tout* y, cudaStream_t s);
+int inverse_in_place(int64_t N, double* x, cudaStream_t s);   // x = 1/x where x > 0 else 0
+int inverse_f64(int64_t N, const double* x, double* y, cudaStream_t s);  // y = 1/x
+int multiplicity_to_weight(int64_t N, const int32_t* mult, double* w, cudaStream_t s);  // w = 1/mult
+
+// Deterministic two-stage reductions into a device scalar; `partials` holds
+// kReducePartials doubles.
+constexpr int kReducePartials = 1024;
+int dot(int64_t N, const double* x, const double* y, double* out, double* partials, cudaStream_t s);
+int dot_f32(int64_t N, const float* x, const float* y, double* out, double* partials, cudaStream_t s);
+int sum(int64_t N, const double* x, double* out, double* partials, cudaStream_t s);
+int pcg_update(int64_t N, double alpha, const double* p, const double* Ap, double* x, double* r,
+               double* out, double* partials, cudaStream_t s);
+int add_scalar(int64_t N, const double* scalarDev, double scale, double* x, cudaStream_t s);
+
+// Chebyshev smoother vector updates (ellipticPreconMultiGridLevel.cpp:154-206)
+template <typename T>
+int cheb_update(int64_t N, const T* invDiag, const T* Ad, T* res, T* d, T a, T b, cudaStream_t s);
+
+// ---------------------------------------------------------------- p-multigrid transfers
+// xC = assembled sum over coarse copies of P^T (weightF .* xF) per element (xC overwritten)
+template <typename T>
+int pmg_coarsen(int Nf, int Nc, int64_t E, const int32_t* g2lF, const T* weightF, const T* xF,
+                const T* P, const int32_t* g2lC, T* xC, int64_t NglobalC, cudaStream_t s);
+// xF += owning-copy value of P xC per element
+template <typename T>
+int pmg_prolongate_map(int Nf, int Nc, int64_t E, const int32_t* g2lC, const T* xC, const T* P,
+                       const int32_t* g2lF, const int32_t* ownerF, T* xF, cudaStream_t s);
+
+// ---------------------------------------------------------------- sparse / dense
+// y = alpha A x + beta y (CSR, FP64)
+int csr_spmv(int64_t Nrows, const int64_t* rowStarts, const int32_t* cols, const double* vals,
+             double alpha, const double* x, double beta, double* y, cudaStream_t s);
+// Chebyshev CSR pieces (parAlmond okl/SmoothChebyshev.okl)
+int csr_cheb_start(int64_t N, double invTheta, const double* diagInv, const double* b, double* r,
+                   double* d, double* x, cudaStream_t s);
+int csr_cheb_residual(int64_t N, const int64_t* rowStarts, const int32_t* cols, const double* vals,
+                      double alpha, double beta, const double* diagInv, const double* b,
+                      const double* x, double* r, cudaStream_t s);
+int csr_cheb_update(int64_t N, double a, double b, int lastIt, const double* r, double* d,
+                    double* x, cudaStream_t s);
+// dense y = A x, A row-major n x n
+int gemv(int64_t n, const double* A, const double* x, double* y, cudaStream_t s);
+
+}  // namespace lpg

@@ -1,0 +1,313 @@
+// Gather-scatter, streaming vector kernels and deterministic reductions.
+//
+// Reductions (linAlgInnerProd.okl / linAlgNorm2.okl / linAlgSum.okl and the fused
+// linearSolverUpdatePCG.okl of the reference) run as two fixed-shape stages:
+// a grid of at most kReducePartials CTAs writes one partial each, then one CTA
+// sums the partials in a fixed tree. The result stays in device memory, so the
+// caller decides when (and whether) to synchronise; the summation order depends
+// only on N, which makes repeated runs bit-identical.
+#include "lpg_common.cuh"
+#include "lpg_internal.hpp"
+
+namespace lpg {
+
+static inline unsigned grid_for(int64_t n, int threads, int64_t cap) {
+  int64_t b = (n + threads - 1) / threads;
+  if (b > cap) b = cap;
+  if (b < 1) b = 1;
+  return (unsigned)b;
+}
+constexpr int64_t kStreamCap = 152 * 32;
+
+// ---------------------------------------------------------------- ogs
+template <typename T>
+__global__ void gather_add_kernel(const int64_t Nlocal, const int32_t* __restrict__ g2l,
+                                  const T* __restrict__ v, T* __restrict__ gv) {
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < Nlocal;
+       n += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t g = g2l[n];
+    if (g >= 0) atomicAdd(gv + g, v[n]);
+  }
+}
+
+template <typename T>
+int gather_add(int64_t Nlocal, const int32_t* g2l, const T* v, T* gv, int64_t Nglobal, bool zero,
+               cudaStream_t s) {
+  if (zero && Nglobal > 0) LPG_CUDA_TRY(cudaMemsetAsync(gv, 0, sizeof(T) * Nglobal, s));
+  if (Nlocal <= 0) return LPG_OK;
+  gather_add_kernel<T><<<grid_for(Nlocal, 256, kStreamCap), 256, 0, s>>>(Nlocal, g2l, v, gv);
+  LPG_LAUNCH_CHECK("gather_add_kernel");
+  return LPG_OK;
+}
+
+template <typename T>
+__global__ void gather_owner_kernel(const int64_t Ng, const int32_t* __restrict__ owner,
+                                    const T* __restrict__ v, T* __restrict__ gv) {
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < Ng;
+       g += (int64_t)gridDim.x * blockDim.x)
+    gv[g] = v[owner[g]];
+}
+
+template <typename T>
+int gather_owner(int64_t Nglobal, const int32_t* owner, const T* v, T* gv, cudaStream_t s) {
+  if (Nglobal <= 0) return LPG_OK;
+  gather_owner_kernel<T><<<grid_for(Nglobal, 256, kStreamCap), 256, 0, s>>>(Nglobal, owner, v, gv);
+  LPG_LAUNCH_CHECK("gather_owner_kernel");
+  return LPG_OK;
+}
+
+template <typename T>
+__global__ void scatter_kernel(const int64_t Nlocal, const int32_t* __restrict__ g2l,
+                               const T* __restrict__ gv, T* __restrict__ v) {
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < Nlocal;
+       n += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t g = g2l[n];
+    v[n] = (g >= 0) ? gv[g] : T(0);
+  }
+}
+
+template <typename T>
+int scatter(int64_t Nlocal, const int32_t* g2l, const T* gv, T* v, cudaStream_t s) {
+  if (Nlocal <= 0) return LPG_OK;
+  scatter_kernel<T><<<grid_for(Nlocal, 256, kStreamCap), 256, 0, s>>>(Nlocal, g2l, gv, v);
+  LPG_LAUNCH_CHECK("scatter_kernel");
+  return LPG_OK;
+}
+
+template int gather_add<double>(int64_t, const int32_t*, const double*, double*, int64_t, bool, cudaStream_t);
+template int gather_add<float>(int64_t, const int32_t*, const float*, float*, int64_t, bool, cudaStream_t);
+template int gather_owner<double>(int64_t, const int32_t*, const double*, double*, cudaStream_t);
+template int gather_owner<float>(int64_t, const int32_t*, const float*, float*, cudaStream_t);
+template int scatter<double>(int64_t, const int32_t*, const double*, double*, cudaStream_t);
+template int scatter<float>(int64_t, const int32_t*, const float*, float*, cudaStream_t);
+
+// ---------------------------------------------------------------- streaming
+template <typename T>
+__global__ void axpy_kernel(const int64_t N, const T a, const T* __restrict__ x, const T b,
+                            T* __restrict__ y) {
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x)
+    y[n] = (b != T(0)) ? a * x[n] + b * y[n] : a * x[n];
+}
+template <typename T>
+int axpy(int64_t N, T a, const T* x, T b, T* y, cudaStream_t s) {
+  if (N <= 0) return LPG_OK;
+  axpy_kernel<T><<<grid_for(N, 256, kStreamCap), 256, 0, s>>>(N, a, x, b, y);
+  LPG_LAUNCH_CHECK("axpy_kernel");
+  return LPG_OK;
+}
+
+template <typename T>
+__global__ void amxpy_kernel(const int64_t N, const T a, const T* __restrict__ x, const T* __restrict__ y,
+                             const T b, T* __restrict__ z) {
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x)
+    z[n] = (b != T(0)) ? a * x[n] * y[n] + b * z[n] : a * x[n] * y[n];
+}
+template <typename T>
+int amxpy(int64_t N, T a, const T* x, const T* y, T b, T* z, cudaStream_t s) {
+  if (N <= 0) return LPG_OK;
+  amxpy_kernel<T><<<grid_for(N, 256, kStreamCap), 256, 0, s>>>(N, a, x, y, b, z);
+  LPG_LAUNCH_CHECK("amxpy_kernel");
+  return LPG_OK;
+}
+
+template <typename T>
+__global__ void fill_kernel(const int64_t N, const T v, T* __restrict__ x) {
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x)
+    x[n] = v;
+}
+template <typename T>
+int fill(int64_t N, T v, T* x, cudaStream_t s) {
+  if (N <= 0) return LPG_OK;
+  fill_kernel<T><<<grid_for(N, 256, kStreamCap), 256, 0, s>>>(N, v, x);
+  LPG_LAUNCH_CHECK("fill_kernel");
+  return LPG_OK;
+}
+
+template <typename Tin, typename Tout>
+__global__ void convert_kernel(const int64_t N, const Tin* __restrict__ x, Tout* __restrict__ y) {
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x)
+    y[n] = (Tout)x[n];
+}
+template <>
+__global__ void convert_kernel<double, __nv_bfloat16>(const int64_t N, const double* __restrict__ x,
+                                                      __nv_bfloat16* __restrict__ y) {
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x)
+    y[n] = __double2bfloat16(x[n]);
+}
+template <typename Tin, typename Tout>
+int convert(int64_t N, const Tin* x, Tout* y, cudaStream_t s) {
+  if (N <= 0) return LPG_OK;
+  convert_kernel<Tin, Tout><<<grid_for(N, 256, kStreamCap), 256, 0, s>>>(N, x, y);
+  LPG_LAUNCH_CHECK("convert_kernel");
+  return LPG_OK;
+}
+
+__global__ void inverse_kernel(const int64_t N, const double* __restrict__ x, double* __restrict__ y,
+                               const int guard) {
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x) {
+    const double v = x[n];
+    y[n] = guard ? ((v > 0.0) ? 1.0 / v : 0.0) : 1.0 / v;
+  }
+}
+int inverse_in_place(int64_t N, double* x, cudaStream_t s) {
+  if (N <= 0) return LPG_OK;
+  inverse_kernel<<<grid_for(N, 256, kStreamCap), 256, 0, s>>>(N, x, x, 1);
+  LPG_LAUNCH_CHECK("inverse_kernel");
+  return LPG_OK;
+}
+int inverse_f64(int64_t N, const double* x, double* y, cudaStream_t s) {
+  if (N <= 0) return LPG_OK;
+  inverse_kernel<<<grid_for(N, 256, kStreamCap), 256, 0, s>>>(N, x, y, 0);
+  LPG_LAUNCH_CHECK("inverse_kernel");
+  return LPG_OK;
+}
+
+__global__ void mult_to_weight_kernel(const int64_t n, const int32_t* __restrict__ m, double* __restrict__ w) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    w[i] = (m[i] > 0) ? 1.0 / (double)m[i] : 0.0;
+}
+int multiplicity_to_weight(int64_t N, const int32_t* mult, double* w, cudaStream_t s) {
+  if (N <= 0) return LPG_OK;
+  mult_to_weight_kernel<<<grid_for(N, 256, kStreamCap), 256, 0, s>>>(N, mult, w);
+  LPG_LAUNCH_CHECK("mult_to_weight_kernel");
+  return LPG_OK;
+}
+
+template int axpy<double>(int64_t, double, const double*, double, double*, cudaStream_t);
+template int axpy<float>(int64_t, float, const float*, float, float*, cudaStream_t);
+template int amxpy<double>(int64_t, double, const double*, const double*, double, double*, cudaStream_t);
+template int amxpy<float>(int64_t, float, const float*, const float*, float, float*, cudaStream_t);
+template int fill<double>(int64_t, double, double*, cudaStream_t);
+template int fill<float>(int64_t, float, float*, cudaStream_t);
+template int convert<double, float>(int64_t, const double*, float*, cudaStream_t);
+template int convert<float, double>(int64_t, const float*, double*, cudaStream_t);
+template int convert<double, __nv_bfloat16>(int64_t, const double*, __nv_bfloat16*, cudaStream_t);
+
+// ---------------------------------------------------------------- reductions
+constexpr int kRedThreads = 512;
+
+__device__ __forceinline__ double block_sum(double v) {
+  __shared__ double s_w[32];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) s_w[warp] = v;
+  __syncthreads();
+  v = (threadIdx.x < (blockDim.x >> 5)) ? s_w[lane] : 0.0;
+  if (warp == 0)
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Stage 1 variants
+enum { RED_DOT = 0, RED_SUM = 1, RED_DOT32 = 2 };
+
+template <int KIND>
+__global__ void __launch_bounds__(kRedThreads)
+reduce_stage1(const int64_t N, const void* __restrict__ xv, const void* __restrict__ yv,
+              double* __restrict__ partials) {
+  double acc = 0;
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x) {
+    if (KIND == RED_DOT) acc += ((const double*)xv)[n] * ((const double*)yv)[n];
+    else if (KIND == RED_SUM) acc += ((const double*)xv)[n];
+    else acc += (double)((const float*)xv)[n] * (double)((const float*)yv)[n];
+  }
+  acc = block_sum(acc);
+  if (threadIdx.x == 0) partials[blockIdx.x] = acc;
+}
+
+__global__ void __launch_bounds__(kRedThreads)
+reduce_stage2(const int nparts, const double* __restrict__ partials, double* __restrict__ out) {
+  double acc = 0;
+  for (int i = threadIdx.x; i < nparts; i += blockDim.x) acc += partials[i];
+  acc = block_sum(acc);
+  if (threadIdx.x == 0) *out = acc;
+}
+
+static inline int red_blocks(int64_t N) {
+  int64_t b = (N + kRedThreads * 4 - 1) / (kRedThreads * 4);
+  if (b > kReducePartials) b = kReducePartials;
+  if (b < 1) b = 1;
+  return (int)b;
+}
+
+template <int KIND>
+static int reduce(int64_t N, const void* x, const void* y, double* out, double* partials, cudaStream_t s) {
+  const int nb = red_blocks(N);
+  reduce_stage1<KIND><<<nb, kRedThreads, 0, s>>>(N, x, y, partials);
+  LPG_LAUNCH_CHECK("reduce_stage1");
+  reduce_stage2<<<1, kRedThreads, 0, s>>>(nb, partials, out);
+  LPG_LAUNCH_CHECK("reduce_stage2");
+  return LPG_OK;
+}
+
+int dot(int64_t N, const double* x, const double* y, double* out, double* partials, cudaStream_t s) {
+  return reduce<RED_DOT>(N, x, y, out, partials, s);
+}
+int dot_f32(int64_t N, const float* x, const float* y, double* out, double* partials, cudaStream_t s) {
+  return reduce<RED_DOT32>(N, x, y, out, partials, s);
+}
+int sum(int64_t N, const double* x, double* out, double* partials, cudaStream_t s) {
+  return reduce<RED_SUM>(N, x, nullptr, out, partials, s);
+}
+
+__global__ void __launch_bounds__(kRedThreads)
+pcg_update_stage1(const int64_t N, const double alpha, const double* __restrict__ p,
+                  const double* __restrict__ Ap, double* __restrict__ x, double* __restrict__ r,
+                  double* __restrict__ partials) {
+  double acc = 0;
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x) {
+    x[n] += alpha * p[n];
+    const double rn = r[n] - alpha * Ap[n];
+    r[n] = rn;
+    acc += rn * rn;
+  }
+  acc = block_sum(acc);
+  if (threadIdx.x == 0) partials[blockIdx.x] = acc;
+}
+
+int pcg_update(int64_t N, double alpha, const double* p, const double* Ap, double* x, double* r,
+               double* out, double* partials, cudaStream_t s) {
+  const int nb = red_blocks(N);
+  pcg_update_stage1<<<nb, kRedThreads, 0, s>>>(N, alpha, p, Ap, x, r, partials);
+  LPG_LAUNCH_CHECK("pcg_update_stage1");
+  reduce_stage2<<<1, kRedThreads, 0, s>>>(nb, partials, out);
+  LPG_LAUNCH_CHECK("reduce_stage2");
+  return LPG_OK;
+}
+
+__global__ void add_scalar_kernel(const int64_t N, const double* __restrict__ sdev, const double scale,
+                                  double* __restrict__ x) {
+  const double v = (*sdev) * scale;
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x)
+    x[n] += v;
+}
+int add_scalar(int64_t N, const double* scalarDev, double scale, double* x, cudaStream_t s) {
+  if (N <= 0) return LPG_OK;
+  add_scalar_kernel<<<grid_for(N, 256, kStreamCap), 256, 0, s>>>(N, scalarDev, scale, x);
+  LPG_LAUNCH_CHECK("add_scalar_kernel");
+  return LPG_OK;
+}
+
+// ---------------------------------------------------------------- Chebyshev
+// res -= invDiag .* Ad ;  d = a d + b res   (one pass of the level smoother loop)
+template <typename T>
+__global__ void cheb_update_kernel(const int64_t N, const T* __restrict__ invDiag, const T* __restrict__ Ad,
+                                   T* __restrict__ res, T* __restrict__ d, const T a, const T b) {
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x) {
+    const T rn = res[n] - invDiag[n] * Ad[n];
+    res[n] = rn;
+    d[n] = b * rn + a * d[n];
+  }
+}
+template <typename T>
+int cheb_update(int64_t N, const T* invDiag, const T* Ad, T* res, T* d, T a, T b, cudaStream_t s) {
+  if (N <= 0) return LPG_OK;
+  cheb_update_kernel<T><<<grid_for(N, 256, kStreamCap), 256, 0, s>>>(N, invDiag, Ad, res, d, a, b);
+  LPG_LAUNCH_CHECK("cheb_update_kernel");
+  return LPG_OK;
+}
+template int cheb_update<double>(int64_t, const double*, const double*, double*, double*, double, double, cudaStream_t);
+template int cheb_update<float>(int64_t, const float*, const float*, float*, float*, float, float, cudaStream_t);
+
+}  // namespace lpg

@@ -1,0 +1,126 @@
+"""End-to-end parity of the CUDA solver path (FPCG/PCG with Jacobi, p-multigrid
+and AMG preconditioners) with the oracle and with the reference's golden norms.
+
+Bars: the reference's own tolerance on `Solution norm` (1e-5 absolute,
+test/test.py:63), identical iteration counts to the oracle for FP64 paths, and
+for reduced-precision preconditioners a discretisation error within 1 % of the
+FP64 oracle's."""
+import numpy as np
+import pytest
+import torch
+
+import libparanumal_gb300 as lpg
+from conftest import golden_case_settings
+from gpu_helpers import box, rel_err
+from oracle.oracle import Oracle
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = ("testEllipticHex_C0", "testEllipticHex_C0_Jacobi", "testEllipticHex_C0_ParAlmond",
+          "testEllipticHex_C0_Multigrid", "testEllipticHex_C0_AllNeumann")
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    import __graft_entry__ as g
+    g.build()
+    torch.cuda.set_device(0)
+
+
+@pytest.mark.parametrize("name", GOLDEN)
+def test_reference_golden_norms(reference_norms, name):
+    case = reference_norms["cases"][name]
+    s = golden_case_settings(case)
+    r = lpg.Elliptic(s).Run()
+    ro = Oracle(s).run()
+    assert r["converged"]
+    assert abs(r["norm"] - case["norm"]) < reference_norms["tolerance"], (r["norm"], case["norm"])
+    assert abs(r["norm"] - ro["norm"]) < 1e-9
+    assert abs(r["iterations"] - ro["iterations"]) <= (0 if "ParAlmond" not in name else 1), \
+        (r["iterations"], ro["iterations"])
+
+
+def config1(**over):
+    d = {"BOX NX": 8, "BOX NY": 8, "BOX NZ": 8, "BOX DIMX": 2, "BOX DIMY": 2, "BOX DIMZ": 2,
+         "BOX BOUNDARY FLAG": 1, "POLYNOMIAL DEGREE": 5, "LAMBDA": 0.0, "LINEAR SOLVER": "FPCG",
+         "PRECONDITIONER": "JACOBI"}
+    d.update(over)
+    return d
+
+
+def test_config1_fpcg_jacobi_iterations_and_error():
+    s = config1()
+    r = lpg.Elliptic(s).Run(want_solution=True)
+    ro = Oracle(s).run()
+    assert r["iterations"] == ro["iterations"]
+    assert abs(r["error"] - ro["error"]) <= 1e-6 * ro["error"]
+    assert rel_err(r["xL"], ro["xL"]) < 1e-7
+    assert r["error"] < 1e-3
+
+
+def test_pcg_and_fpcg_agree_on_solution():
+    s = config1(**{"BOX NX": 4, "BOX NY": 4, "BOX NZ": 4})
+    a = lpg.Elliptic(dict(s, **{"LINEAR SOLVER": "PCG"})).Run(want_solution=True)
+    b = lpg.Elliptic(s).Run(want_solution=True)
+    assert rel_err(a["xL"], b["xL"]) < 1e-7
+
+
+MG = dict(config1(), **{"BOX NX": 6, "BOX NY": 5, "BOX NZ": 4, "POLYNOMIAL DEGREE": 7,
+                        "MESH JITTER": 0.1, "PRECONDITIONER": "MULTIGRID", "MULTIGRID DEGREES": "7,3,1",
+                        "PARALMOND AGGREGATION": "SMOOTHED"})
+
+
+def test_pmg_fp64_iterations_match_oracle():
+    r = lpg.Elliptic(MG).Run()
+    ro = Oracle(MG).run()
+    assert r["converged"]
+    assert r["iterations"] == ro["iterations"], (r["iterations"], ro["iterations"])
+    assert abs(r["error"] - ro["error"]) <= 1e-6 * ro["error"]
+
+
+def test_pmg_preconditioner_application_matches_oracle():
+    e = lpg.Elliptic(MG)
+    o = Oracle(MG)
+    rng = np.random.default_rng(2)
+    rh = rng.standard_normal(e.Nglobal)
+    r = torch.tensor(rh, device="cuda")
+    z = torch.zeros_like(r)
+    e.precon(r, z)
+    torch.cuda.synchronize()
+    assert rel_err(z.cpu().numpy(), o.precon(rh)) < 1e-9
+
+
+@pytest.mark.parametrize("prec", ["FP32", "BF16GEO"])
+def test_mixed_precision_preconditioner_keeps_fp64_accuracy(prec):
+    s = dict(MG, **{"PRECONDITIONER PRECISION": prec})
+    r = lpg.Elliptic(s).Run()
+    ro = Oracle(MG).run()
+    assert r["converged"]
+    assert r["iterations"] <= ro["iterations"] + 3
+    assert abs(r["error"] - ro["error"]) <= 0.01 * ro["error"]
+
+
+def test_lognormal_lambda_and_gaussian_sources_solve():
+    s = dict(MG, **{"LAMBDA FIELD": "LOGNORMAL", "LAMBDA SEED": 2, "RHS FIELD": "GAUSSIAN SOURCES",
+                    "RHS SEED": 3, "RHS SOURCES": 16})
+    r = lpg.Elliptic(s).Run(want_solution=True)
+    ro = Oracle(s).run()
+    assert r["iterations"] == ro["iterations"]
+    assert rel_err(r["xL"], ro["xL"]) < 1e-7
+    assert abs(r["norm"] - ro["norm"]) < 1e-9 * ro["norm"]
+
+
+def test_solver_level_api_and_not_converged_status():
+    s = config1(**{"BOX NX": 3, "BOX NY": 3, "BOX NZ": 3})
+    e = lpg.Elliptic(s)
+    r = torch.zeros(e.Nglobal, dtype=torch.float64, device="cuda")
+    e.rhs(r)
+    x = torch.zeros_like(r)
+    it = e.Solve(x, r.clone(), tol=1e-8, maxit=2)
+    assert it == 2
+    x.zero_()
+    it = e.Solve(x, r.clone(), tol=1e-8, maxit=5000)
+    o = Oracle(s)
+    xo, ito, _ = o.pcg(o.rhs(), tol=1e-8)
+    assert it == ito
+    assert rel_err(x.cpu().numpy(), xo) < 1e-8
