@@ -1,0 +1,285 @@
+"""Benchmark of the C0 hex elliptic hot path on GB300.
+
+Workload (one step = one pass of the hot path over one batch): one assembled
+screened-Poisson operator application y = A q (matrix-free sum-factorised Ax with the
+gather-scatter assembly fused) on a 64x64x64 jittered hex box, N = 7 (512 GLL nodes per
+element, 134,217,728 local nodes, 89,314,623 assembled dofs), lambda = 1, full per-node
+geometric factors (7 FP64 values/node), q ~ U[-1,1] keyed by global lattice node id
+(seed 1). Inputs (9.5 GB) exceed the 129 MB L2, so no flush is needed between steps.
+
+value   : local GDOF/s (Nlocal / step time), device-resident inputs
+e2e     : same metric through the C ABI with host buffers: pinned H2D of q, operator,
+          D2H of A q, all inside each timed step
+roofline: algorithmic bytes Nlocal*60 + Nglobal*16 per application over the measured
+          launch time, against the measured HBM copy bandwidth
+cpu_baseline: the oracle (CPU port of the reference algorithm) on a bounded sample
+--impl reference: the reference's CPU implementation (oracle port) on all host threads
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--nx 64] [--N 7]
+Multi-GPU (torchrun): each rank runs an independent replica of the workload
+("replicas only": this path is not sharded across GPUs here); value sums all ranks
+over the max-over-ranks time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Poisson time-to-1e-8: learned+mixed vs FP64 p-MG FPCG on GB300; Ax GDOF/s, %HBM"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300")
+    ap.add_argument("--nx", type=int, default=64)
+    ap.add_argument("--N", type=int, default=7)
+    ap.add_argument("--cpu-sample-nx", type=int, default=16)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    return ap.parse_args()
+
+
+def settings(nx, N):
+    return {"BOX NX": nx, "BOX NY": nx, "BOX NZ": nx, "BOX DIMX": 2, "BOX DIMY": 2, "BOX DIMZ": 2,
+            "BOX BOUNDARY FLAG": 1, "POLYNOMIAL DEGREE": N, "LAMBDA": 1.0, "MESH JITTER": 0.1,
+            "MESH JITTER SEED": 0, "LINEAR SOLVER": "FPCG", "PRECONDITIONER": "NONE"}
+
+
+def workload_name(nx, N):
+    return "screened-Poisson assembled Ax, %d^3 jittered hex box, N=%d, lambda=1, FP64 geometry" % (nx, N)
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("uuid,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, uuid):
+        self.uuid = (uuid or "").lower()
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            row = [x.strip() for x in line.split(",")]
+            if not self.uuid or self.uuid in row[0].lower():
+                self.rows.append(row)
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                smax = float(r[2])
+                for k, nm in enumerate(names):
+                    if r[5 + k].lower().startswith("active"):
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(nx_sample, N, budget_s=12.0, nthreads=0):
+    """Oracle (CPU port of the reference algorithm) operator throughput on a bounded sample."""
+    from oracle.oracle import Oracle, threads
+    o = Oracle(settings(nx_sample, N))
+    nl = o.Nlocal
+    t1 = o.time_operator(1, nthreads)
+    reps = max(1, int(budget_s / max(t1, 1e-3)))
+    t = o.time_operator(reps, nthreads)
+    used = nthreads if nthreads > 0 else threads()
+    return {"value": nl * reps / t / 1e9, "unit": "GDOF/s", "cores": used, "kind": "port",
+            "sample": "%d^3-element jittered box, N=%d, lambda=1 (%d local nodes), %d operator "
+                      "applications, %d OpenMP threads" % (nx_sample, N, nl, reps, used)}
+
+
+def run_reference(a):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    base = cpu_baseline(a.cpu_sample_nx, a.N, budget_s=max(5.0, 2.0 * a.steps))
+    line = {"impl": "reference", "metric": METRIC, "value": base["value"], "unit": "GDOF/s",
+            "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup, "higher_is_better": True,
+            "dtype": "f64", "data": "synthetic", "config": {"workload": workload_name(a.nx, a.N)},
+            "cpu_baseline": base, "vs_baseline": None,
+            "e2e": {"value": base["value"], "unit": "GDOF/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        return run_reference(a)
+    import numpy as np
+    import torch
+    import libparanumal_gb300 as lpg
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    import __graft_entry__ as g
+    if rank == 0:
+        g.build()
+    if dist:
+        dist.barrier()
+    lpg.lib()
+
+    t_setup = time.time()
+    e = lpg.Elliptic(settings(a.nx, a.N))
+    Nl, Ng = e.Nlocal, e.Nglobal
+    q = torch.empty(Ng, dtype=torch.float64, device="cuda")
+    Aq = torch.empty_like(q)
+    e.random_vector(q, 1)
+    torch.cuda.synchronize()
+    t_setup = time.time() - t_setup
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+
+    for _ in range(a.warmup):
+        e.Operator(q, Aq, sp)
+    torch.cuda.synchronize()
+
+    try:
+        uuid = str(torch.cuda.get_device_properties(local).uuid)
+    except Exception:
+        uuid = ""
+    clocks = ClockSampler(uuid)
+    clocks.start()
+    time.sleep(0.3)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(a.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(a.steps)]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for k in range(a.steps):
+        starts[k].record(stream)
+        e.Operator(q, Aq, sp)
+        ends[k].record(stream)
+    t1.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    total_ms = t0.elapsed_time(t1)
+    per = [s.elapsed_time(x) for s, x in zip(starts, ends)]
+    launch_ms = statistics.mean(per)
+    ms = total_ms / a.steps
+    if dist:
+        tt = torch.tensor([ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt)
+
+    # end to end through the C ABI with host buffers (pinned), copies inside the step
+    qh = torch.empty(Ng, dtype=torch.float64).pin_memory()
+    yh = torch.empty(Ng, dtype=torch.float64).pin_memory()
+    qh.copy_(q.cpu())
+    for _ in range(2):
+        q.copy_(qh, non_blocking=True)
+        e.Operator(q, Aq, sp)
+        yh.copy_(Aq, non_blocking=True)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(a.e2e_steps):
+        q.copy_(qh, non_blocking=True)
+        e.Operator(q, Aq, sp)
+        yh.copy_(Aq, non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / a.e2e_steps
+    if dist:
+        tt = torch.tensor([e2e_ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_ms = float(tt)
+
+    if rank != 0:
+        dist.destroy_process_group()
+        return
+    peak, peak_kind = measured_peaks()
+    alg_bytes = Nl * 60 + Ng * 16
+    flops = (12 * (a.N + 1) + 18) * Nl
+    achieved = alg_bytes / (launch_ms * 1e-3) / 1e9
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "ax_hex_f64_64cubed_N7.txt")
+    if os.path.exists(tfile):
+        for line in open(tfile):
+            if line.startswith("traffic_bytes_per_launch:"):
+                traffic = float(line.split(":")[1])
+    value = world * Nl / (ms * 1e-3) / 1e9
+    out = {
+        "metric": METRIC, "value": value, "unit": "GDOF/s", "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": workload_name(a.nx, a.N), "elements": a.nx ** 3, "N": a.N,
+                   "local_nodes": Nl, "assembled_dofs": Ng, "lambda": 1.0, "jitter": 0.1,
+                   "l2": "inputs %.1f GB > 129 MB L2, no flush between steps" % (alg_bytes / 1e9),
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "gdofs_assembled": world * Ng / (ms * 1e-3) / 1e9,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                     "algorithmic_bytes_per_launch": alg_bytes, "launch_ms": launch_ms},
+        "compute": {"fp64_flops_per_launch": flops, "achieved_tflops": flops / (launch_ms * 1e-3) / 1e12,
+                    "fp64_nominal_tflops": 1.25},
+        "e2e": {"value": world * Nl / (e2e_ms * 1e-3) / 1e9, "unit": "GDOF/s",
+                "h2d_bytes_per_step": Ng * 8, "d2h_bytes_per_step": Ng * 8, "ms_per_step": e2e_ms},
+        "gpu_launches": a.steps,
+        "clocks": clk,
+        "setup_seconds": t_setup,
+    }
+    if not a.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(a.cpu_sample_nx, a.N)
+    print(json.dumps(out), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

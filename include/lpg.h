@@ -139,6 +139,11 @@ int lpg_elliptic_get(const lpg_elliptic *e, const char *name, void *host_out, ui
  * are FP64 vectors of length Nglobal usable as scratch by the caller. */
 int lpg_elliptic_device_ptr(const lpg_elliptic *e, const char *name, void **ptr);
 
+/* Seeded input vector with no reference counterpart (the reference's tests use
+ * manufactured data only): q[g] = 2u-1, u uniform in [0,1) keyed by (seed, global
+ * lattice node id of dof g), so the vector does not depend on numbering or partition. */
+int lpg_elliptic_random_vector(lpg_elliptic *e, uint64_t seed, double *q, void *stream);
+
 /* elliptic_t::Operator (ellipticOperator.cpp:29-106): Aq = A q, device pointers (Nglobal). */
 int lpg_elliptic_operator(lpg_elliptic *e, const double *q, double *Aq, void *stream);
 /* precon_t::Operator (include/precon.hpp:36-56): z = M^{-1} r, device pointers. */

@@ -67,6 +67,7 @@ def lib():
         "lpg_elliptic_destroy": [vp],
         "lpg_elliptic_get": [vp, ctypes.c_char_p, vp, ctypes.c_uint64],
         "lpg_elliptic_device_ptr": [vp, ctypes.c_char_p, ctypes.POINTER(ctypes.c_void_p)],
+        "lpg_elliptic_random_vector": [vp, ctypes.c_uint64, vp, vp],
         "lpg_elliptic_operator": [vp, vp, vp, vp],
         "lpg_elliptic_precon": [vp, vp, vp, vp],
         "lpg_elliptic_solve": [vp, vp, vp, f64, i32, ctypes.POINTER(ctypes.c_int)],
@@ -164,6 +165,9 @@ class Elliptic:
         p = ctypes.c_void_p()
         check(lib().lpg_elliptic_device_ptr(self.h, name.encode(), ctypes.byref(p)))
         return p.value
+
+    def random_vector(self, q, seed, stream=0):
+        check(lib().lpg_elliptic_random_vector(self.h, seed, _ptr(q), stream or None))
 
     def Operator(self, q, Aq, stream=0):
         check(lib().lpg_elliptic_operator(self.h, _ptr(q), _ptr(Aq), stream or None))

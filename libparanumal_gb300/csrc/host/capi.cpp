@@ -347,6 +347,15 @@ extern "C" int lpg_elliptic_device_ptr(const lpg_elliptic* e, const char* name, 
   return LPG_OK;
 }
 
+extern "C" int lpg_elliptic_random_vector(lpg_elliptic* e, uint64_t seed, double* q, void* stream) {
+  if (!e || !q) return set_error(LPG_ERR_INVALID, "null argument");
+  LPG_GUARD_BEGIN
+  const MeshConfig& c = e->mcfg;
+  BoxNumbering b{c.nx, c.ny, c.nz, e->el->mesh.N, c.bcflag == -1 ? 1 : 0, c.bcflag == 1 ? 1 : 0};
+  return lattice_random(b, e->el->Nglobal, e->el->owner.p, seed, q, pick(e, stream));
+  LPG_GUARD_END
+}
+
 extern "C" int lpg_elliptic_operator(lpg_elliptic* e, const double* q, double* Aq, void* stream) {
   if (!e || !q || !Aq) return set_error(LPG_ERR_INVALID, "null argument");
   LPG_GUARD_BEGIN

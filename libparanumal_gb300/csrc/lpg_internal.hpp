@@ -50,6 +50,11 @@ struct BoxNumbering {
 int box_numbering(const BoxNumbering& b, const int64_t* elemBase, int32_t* g2l, int32_t* owner,
                   int32_t* mult, int64_t Nglobal, cudaStream_t s);
 
+// q[g] = 2u-1 with u keyed by (seed, global lattice node id of dof g): the input
+// vector of the operator-throughput workload, independent of numbering and partition.
+int lattice_random(const BoxNumbering& b, int64_t Nglobal, const int32_t* owner, uint64_t seed, double* q,
+                   cudaStream_t s);
+
 // Right-hand side forcing * wJ per local node and Dirichlet data g at masked nodes.
 struct RhsSpec {
   int kind;            // 0 sine, 1 Gaussian sources

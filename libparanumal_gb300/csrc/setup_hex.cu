@@ -167,6 +167,42 @@ int box_numbering(const BoxNumbering& b, const int64_t* elemBase, int32_t* g2l, 
   return LPG_OK;
 }
 
+// ---------------------------------------------------------------- seeded input vectors
+__device__ __forceinline__ uint64_t splitmix64_dev(uint64_t x) {
+  uint64_t z = x + 0x9E3779B97F4A7C15ULL;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+
+// q[g] = 2u - 1, u uniform [0,1) keyed by (seed, stream 3, lattice id of dof g's owner node)
+__global__ void lattice_random_kernel(const BoxNumbering b, const int64_t Nglobal, const int32_t* __restrict__ owner,
+                                      const uint64_t seed, double* __restrict__ q) {
+  const int Nq = b.N + 1, Np = Nq * Nq * Nq;
+  const int64_t NnX = b.periodic ? (int64_t)b.nx * b.N : (int64_t)b.nx * b.N + 1;
+  const int64_t NnY = b.periodic ? (int64_t)b.ny * b.N : (int64_t)b.ny * b.N + 1;
+  const uint64_t h0 = splitmix64_dev(seed ^ (3ULL << 56));
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < Nglobal; g += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t id = owner[g];
+    const int64_t e = id / Np;
+    const int n = (int)(id % Np);
+    const int a = n % Nq, bb = (n / Nq) % Nq, c = n / (Nq * Nq);
+    const int64_t ex = e % b.nx, ey = (e / b.nx) % b.ny, ez = e / ((int64_t)b.nx * b.ny);
+    const int64_t key = (ex * b.N + a) + (ey * b.N + bb) * NnX + (ez * b.N + c) * NnX * NnY;
+    const uint64_t h = splitmix64_dev(h0 + (uint64_t)key);
+    q[g] = 2.0 * ((double)(h >> 11) * (1.0 / 9007199254740992.0)) - 1.0;
+  }
+}
+
+int lattice_random(const BoxNumbering& b, int64_t Nglobal, const int32_t* owner, uint64_t seed, double* q,
+                   cudaStream_t s) {
+  if (Nglobal <= 0) return LPG_OK;
+  const int64_t blocks = std::min<int64_t>((Nglobal + 255) / 256, 152 * 32);
+  lattice_random_kernel<<<(unsigned)blocks, 256, 0, s>>>(b, Nglobal, owner, seed, q);
+  LPG_LAUNCH_CHECK("lattice_random_kernel");
+  return LPG_OK;
+}
+
 // ---------------------------------------------------------------- rhs / norms
 #define LPG_PI 3.14159265358979323846
 

@@ -146,7 +146,7 @@ int orc_parse_settings(const char *text, orc_settings *s) {
       char *e = strchr(tmp, ']');
       if (!e) { rc = -1; break; }
       *e = 0;
-      strncpy(key, tmp + 1, sizeof(key) - 1);
+      snprintf(key, sizeof(key), "%s", tmp + 1);
       trim(key);
       havekey = 1;
     } else if (havekey) {

@@ -77,7 +77,10 @@ def test_lattice_keyed_input_and_linearity():
     e = lpg.Elliptic(cfg)
     o = Oracle(cfg)
     qh = lattice_q(o.array("GlobalToLocal"), 7, 2, 3, 2)
-    q = torch.tensor(qh, device="cuda")
+    q = torch.zeros(e.Nglobal, dtype=torch.float64, device="cuda")
+    e.random_vector(q, 1)
+    torch.cuda.synchronize()
+    assert np.array_equal(q.cpu().numpy(), qh)
     Aq = torch.zeros_like(q)
     e.Operator(q, Aq)
     ref = o.operator(qh)
