@@ -104,6 +104,15 @@ int lpg_amxpy_f64(int64_t N, double alpha, const double *x, const double *y, dou
                   void *stream);
 int lpg_dot_f64(int64_t N, const double *x, const double *y, double *result_dev, void *stream);
 int lpg_norm2sq_f64(int64_t N, const double *x, double *result_dev, void *stream);
+/* No counterpart in the reference. Same result as lpg_dot_f64, but allocates nothing:
+ * for callers that cannot let a library call cudaMalloc -- host frameworks that own all
+ * device memory through their own pool, and latency-sensitive loops where cudaMalloc /
+ * cudaFree would synchronise the device. The partial sums live in a fixed 8 KB device
+ * array (1024 doubles) that every GPU loading the library holds until exit. The first
+ * call on each device looks up that array's address (with the device current) and should
+ * come before any stream capture. N must be 0..2^40; larger N fails with LPG_ERR_INVALID.
+ * All calls share the array, so calls that overlap on the GPU race. */
+int lpg_dot_f64_noalloc(int64_t N, const double *x, const double *y, double *result_dev, void *stream);
 /* linearSolverUpdatePCG.okl:29-75 + pcg::UpdatePCG (linearSolverPCG.cpp:153-171):
  * x += alpha p; r -= alpha Ap; result_dev = r.r */
 int lpg_pcg_update_f64(int64_t N, double alpha, const double *p, const double *Ap, double *x, double *r,

@@ -62,6 +62,7 @@ def lib():
         "lpg_amxpy_f64": [i64, f64, vp, vp, f64, vp, vp],
         "lpg_dot_f64": [i64, vp, vp, vp, vp],
         "lpg_norm2sq_f64": [i64, vp, vp, vp],
+        "lpg_dot_f64_noalloc": [i64, vp, vp, vp, vp],
         "lpg_pcg_update_f64": [i64, f64, vp, vp, vp, vp, vp, vp],
         "lpg_elliptic_create": [ctypes.c_char_p, ctypes.POINTER(ctypes.c_void_p)],
         "lpg_elliptic_destroy": [vp],

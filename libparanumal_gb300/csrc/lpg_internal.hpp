@@ -96,6 +96,7 @@ int multiplicity_to_weight(int64_t N, const int32_t* mult, double* w, cudaStream
 // Deterministic two-stage reductions into a device scalar; `partials` holds
 // kReducePartials doubles.
 constexpr int kReducePartials = 1024;
+int reduction_blocks(int64_t N);  // stage-1 CTAs (= partial sums) used for N entries
 int dot(int64_t N, const double* x, const double* y, double* out, double* partials, cudaStream_t s);
 int dot_f32(int64_t N, const float* x, const float* y, double* out, double* partials, cudaStream_t s);
 int sum(int64_t N, const double* x, double* out, double* partials, cudaStream_t s);

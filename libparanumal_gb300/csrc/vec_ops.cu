@@ -231,6 +231,8 @@ static inline int red_blocks(int64_t N) {
   return (int)b;
 }
 
+int reduction_blocks(int64_t N) { return red_blocks(N); }
+
 template <int KIND>
 static int reduce(int64_t N, const void* x, const void* y, double* out, double* partials, cudaStream_t s) {
   const int nb = red_blocks(N);
