@@ -46,6 +46,11 @@ def parse():
     ap.add_argument("--cpu-sample-nx", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--prec", default="f64", choices=["f64", "f32", "bf16g"],
+                    help="operator variant timed in the Ax workload (headline: f64)")
+    ap.add_argument("--solve", action="store_true", help="time-to-tolerance of the p-MG FPCG solve instead")
+    ap.add_argument("--solve-precs", default="FP64,FP32,BF16GEO")
+    ap.add_argument("--solve-reps", type=int, default=2)
     return ap.parse_args()
 
 
@@ -144,10 +149,47 @@ def run_reference(a):
     print(json.dumps(line), flush=True)
 
 
+def solve_settings(nx, N, prec, degrees="7,3,1", lam=0.0, **extra):
+    d = {"BOX NX": nx, "BOX NY": nx, "BOX NZ": nx, "BOX DIMX": 2, "BOX DIMY": 2, "BOX DIMZ": 2,
+         "BOX BOUNDARY FLAG": 1, "POLYNOMIAL DEGREE": N, "LAMBDA": lam, "MESH JITTER": 0.1,
+         "MESH JITTER SEED": 0, "LINEAR SOLVER": "FPCG", "PRECONDITIONER": "MULTIGRID",
+         "MULTIGRID DEGREES": degrees, "MULTIGRID SMOOTHER": "CHEBYSHEV",
+         "MULTIGRID CHEBYSHEV DEGREE": 2, "PARALMOND AGGREGATION": "SMOOTHED",
+         "PRECONDITIONER PRECISION": prec}
+    d.update(extra)
+    return d
+
+
+def run_solves(a):
+    """Time-to-1e-8 of FPCG + p-MG (7->3->1, Chebyshev 2, smoothed-aggregation AMG on N=1)
+    on a jittered box with the manufactured sine solution, for each preconditioner
+    precision. One JSON line; setup is outside the timed window (ellipticRun.cpp:190-210)."""
+    import libparanumal_gb300 as lpg
+    import __graft_entry__ as g
+    g.build()
+    res = {}
+    for prec in a.solve_precs.split(","):
+        t0 = time.time()
+        e = lpg.Elliptic(solve_settings(a.nx, a.N, prec))
+        setup = time.time() - t0
+        runs = [e.Run() for _ in range(a.solve_reps)]
+        best = min(runs, key=lambda r: r["solve_seconds"])
+        res[prec] = {"solve_seconds": best["solve_seconds"], "iterations": best["iterations"],
+                     "error_vs_manufactured": best["error"], "norm": best["norm"],
+                     "converged": best["converged"], "setup_seconds": setup,
+                     "mg_plevels": e.info("mg_plevels"), "amg_levels": e.info("mg_amglevels"),
+                     "coarse_n": e.info("coarse_n"), "nglobal": e.Nglobal}
+        e.close()
+    print(json.dumps({"workload": "FPCG + p-MG 7->3->1 time-to-1e-8, %d^3 jittered hex, N=%d, lambda=0"
+                      % (a.nx, a.N), "results": res}), flush=True)
+
+
 def main():
     a = parse()
     if a.impl == "reference":
         return run_reference(a)
+    if a.solve:
+        return run_solves(a)
     import numpy as np
     import torch
     import libparanumal_gb300 as lpg
@@ -178,9 +220,21 @@ def main():
     t_setup = time.time() - t_setup
     stream = torch.cuda.current_stream()
     sp = stream.cuda_stream
+    if a.prec == "f64":
+        qin, yout = q, Aq
+
+        def op():
+            e.Operator(qin, yout, sp)
+    else:
+        qin = q.float()
+        yout = torch.empty_like(qin)
+        bf = a.prec == "bf16g"
+
+        def op():
+            e.OperatorF32(qin, yout, bf, sp)
 
     for _ in range(a.warmup):
-        e.Operator(q, Aq, sp)
+        op()
     torch.cuda.synchronize()
 
     try:
@@ -200,7 +254,7 @@ def main():
     t0.record(stream)
     for k in range(a.steps):
         starts[k].record(stream)
-        e.Operator(q, Aq, sp)
+        op()
         ends[k].record(stream)
     t1.record(stream)
     torch.cuda.synchronize()
@@ -217,21 +271,21 @@ def main():
         ms = float(tt)
 
     # end to end through the C ABI with host buffers (pinned), copies inside the step
-    qh = torch.empty(Ng, dtype=torch.float64).pin_memory()
-    yh = torch.empty(Ng, dtype=torch.float64).pin_memory()
-    qh.copy_(q.cpu())
+    qh = torch.empty(Ng, dtype=qin.dtype).pin_memory()
+    yh = torch.empty(Ng, dtype=qin.dtype).pin_memory()
+    qh.copy_(qin.cpu())
     for _ in range(2):
-        q.copy_(qh, non_blocking=True)
-        e.Operator(q, Aq, sp)
-        yh.copy_(Aq, non_blocking=True)
+        qin.copy_(qh, non_blocking=True)
+        op()
+        yh.copy_(yout, non_blocking=True)
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     for _ in range(a.e2e_steps):
-        q.copy_(qh, non_blocking=True)
-        e.Operator(q, Aq, sp)
-        yh.copy_(Aq, non_blocking=True)
+        qin.copy_(qh, non_blocking=True)
+        op()
+        yh.copy_(yout, non_blocking=True)
     e1.record(stream)
     torch.cuda.synchronize()
     e2e_ms = e0.elapsed_time(e1) / a.e2e_steps
@@ -244,12 +298,12 @@ def main():
         dist.destroy_process_group()
         return
     peak, peak_kind = measured_peaks()
-    alg_bytes = Nl * 60 + Ng * 16
+    alg_bytes = {"f64": Nl * 60 + Ng * 16, "f32": Nl * 32 + Ng * 8, "bf16g": Nl * 18 + Ng * 8}[a.prec]
     flops = (12 * (a.N + 1) + 18) * Nl
     achieved = alg_bytes / (launch_ms * 1e-3) / 1e9
     traffic = None
     tfile = os.path.join(ROOT, "profiles", "ax_hex_f64_64cubed_N7.txt")
-    if os.path.exists(tfile):
+    if os.path.exists(tfile) and a.prec == "f64" and a.nx == 64 and a.N == 7:
         for line in open(tfile):
             if line.startswith("traffic_bytes_per_launch:"):
                 traffic = float(line.split(":")[1])
@@ -257,7 +311,7 @@ def main():
     out = {
         "metric": METRIC, "value": value, "unit": "GDOF/s", "n_gpus": world, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "vs_baseline": None, "dtype": a.prec, "data": "synthetic",
         "config": {"workload": workload_name(a.nx, a.N), "elements": a.nx ** 3, "N": a.N,
                    "local_nodes": Nl, "assembled_dofs": Ng, "lambda": 1.0, "jitter": 0.1,
                    "l2": "inputs %.1f GB > 129 MB L2, no flush between steps" % (alg_bytes / 1e9),
@@ -269,7 +323,8 @@ def main():
         "compute": {"fp64_flops_per_launch": flops, "achieved_tflops": flops / (launch_ms * 1e-3) / 1e12,
                     "fp64_nominal_tflops": 1.25},
         "e2e": {"value": world * Nl / (e2e_ms * 1e-3) / 1e9, "unit": "GDOF/s",
-                "h2d_bytes_per_step": Ng * 8, "d2h_bytes_per_step": Ng * 8, "ms_per_step": e2e_ms},
+                "h2d_bytes_per_step": Ng * qin.element_size(), "d2h_bytes_per_step": Ng * qin.element_size(),
+                "ms_per_step": e2e_ms},
         "gpu_launches": a.steps,
         "clocks": clk,
         "setup_seconds": t_setup,

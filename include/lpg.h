@@ -155,6 +155,11 @@ int lpg_elliptic_random_vector(lpg_elliptic *e, uint64_t seed, double *q, void *
 
 /* elliptic_t::Operator (ellipticOperator.cpp:29-106): Aq = A q, device pointers (Nglobal). */
 int lpg_elliptic_operator(lpg_elliptic *e, const double *q, double *Aq, void *stream);
+/* Reduced-precision operator of the same object (no reference counterpart; the
+ * reference is FP64 only): FP32 vectors, FP32 (bf16geo = 0) or BF16 (bf16geo = 1)
+ * geometric factors, FP32 arithmetic. The reduced-precision copies of the geometric
+ * factors are made on first use. */
+int lpg_elliptic_operator_f32(lpg_elliptic *e, const float *q, float *Aq, int bf16geo, void *stream);
 /* precon_t::Operator (include/precon.hpp:36-56): z = M^{-1} r, device pointers. */
 int lpg_elliptic_precon(lpg_elliptic *e, const double *r, double *z, void *stream);
 /* elliptic_t::Solve (ellipticSolve.cpp:29-39): (F)PCG on device vectors x (initial

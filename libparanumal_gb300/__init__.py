@@ -70,6 +70,7 @@ def lib():
         "lpg_elliptic_device_ptr": [vp, ctypes.c_char_p, ctypes.POINTER(ctypes.c_void_p)],
         "lpg_elliptic_random_vector": [vp, ctypes.c_uint64, vp, vp],
         "lpg_elliptic_operator": [vp, vp, vp, vp],
+        "lpg_elliptic_operator_f32": [vp, vp, vp, i32, vp],
         "lpg_elliptic_precon": [vp, vp, vp, vp],
         "lpg_elliptic_solve": [vp, vp, vp, f64, i32, ctypes.POINTER(ctypes.c_int)],
         "lpg_elliptic_rhs": [vp, vp, vp],
@@ -172,6 +173,11 @@ class Elliptic:
 
     def Operator(self, q, Aq, stream=0):
         check(lib().lpg_elliptic_operator(self.h, _ptr(q), _ptr(Aq), stream or None))
+
+    def OperatorF32(self, q, Aq, bf16geo=False, stream=0):
+        """Reduced-precision operator (FP32 vectors; FP32 or BF16 geometric factors)."""
+        check(lib().lpg_elliptic_operator_f32(self.h, _ptr(q), _ptr(Aq), 1 if bf16geo else 0,
+                                              stream or None))
 
     def precon(self, r, z, stream=0):
         check(lib().lpg_elliptic_precon(self.h, _ptr(r), _ptr(z), stream or None))

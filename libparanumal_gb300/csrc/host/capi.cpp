@@ -363,6 +363,16 @@ extern "C" int lpg_elliptic_operator(lpg_elliptic* e, const double* q, double* A
   LPG_GUARD_END
 }
 
+extern "C" int lpg_elliptic_operator_f32(lpg_elliptic* e, const float* q, float* Aq, int bf16geo, void* stream) {
+  if (!e || !q || !Aq) return set_error(LPG_ERR_INVALID, "null argument");
+  LPG_GUARD_BEGIN
+  cudaStream_t s = pick(e, stream);
+  int rc = e->el->make_f32(bf16geo != 0, s);
+  if (rc) return rc;
+  return e->el->OperatorF32(q, Aq, bf16geo ? Prec::BF16G : Prec::F32, s);
+  LPG_GUARD_END
+}
+
 extern "C" int lpg_elliptic_precon(lpg_elliptic* e, const double* r, double* z, void* stream) {
   if (!e || !r || !z) return set_error(LPG_ERR_INVALID, "null argument");
   LPG_GUARD_BEGIN
