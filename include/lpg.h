@@ -138,6 +138,8 @@ int lpg_elliptic_destroy(lpg_elliptic *e);
 #define LPG_INFO_MG_AMGLEVELS 7
 #define LPG_INFO_COARSE_N 8
 #define LPG_INFO_DEVICE_BYTES 9
+#define LPG_INFO_VCYCLES 10        /* V-cycles run with the learned fine smoother */
+#define LPG_INFO_FALLBACKS 11      /* of those, redone with the plain smoother */
 int64_t lpg_elliptic_info(const lpg_elliptic *e, int what);
 
 /* Copy a named setup array to host memory: "GlobalToLocal" (int32), "ownerLocal" (int32),
@@ -174,6 +176,40 @@ int lpg_elliptic_rhs(lpg_elliptic *e, double *r, void *stream);
  * xL_host (Nlocal doubles) may be NULL; solve_seconds is the wall time of the solve. */
 int lpg_elliptic_run(lpg_elliptic *e, double *xL_host, int *iters, double *norm, double *err,
                      double *solve_seconds);
+
+/* ------------------------------------------------------------------ learned smoother */
+/* No reference counterpart (spec addition). Element-local MLP
+ * 896 -> 256 -> 256 -> 256 -> 512 with GELU (tanh form) after the hidden layers; input =
+ * the element's 512 residual values and 6 x 64 face-neighbour traces divided by the
+ * element residual RMS s_e; the smoother's correction is s_e * invDiag * output,
+ * averaged over shared nodes. Parameter vector (FP32, lpg_mlp_param_count() = 492800):
+ * W0 (896x256 row-major), b0, W1 (256x256), b1, W2 (256x256), b2, W3 (256x512), b3. */
+int64_t lpg_mlp_param_count(void);
+/* floats of the activation workspace for a batch of B rows */
+int64_t lpg_mlp_workspace_floats(int64_t B);
+/* FP32 forward: Y (B x 512) = MLP(X (B x 896)); workspace keeps the activations for the
+ * backward pass. */
+int lpg_mlp_forward_f32(const float *params, int64_t B, const float *X, float *workspace, float *Y, void *stream);
+/* FP32 backward of the forward above: grads (param layout) of sum(dY . Y); work holds
+ * 2 x B x 256 floats. */
+int lpg_mlp_backward_f32(const float *params, int64_t B, const float *X, const float *workspace, const float *dY,
+                         float *grads, float *work, void *stream);
+/* Adam step (b1 0.9, b2 0.999, eps 1e-8; step counts from 1). */
+int lpg_mlp_adam_f32(int64_t n, float *w, const float *g, float *m, float *v, float lr, int step, void *stream);
+/* Inference path: BF16 tensor-core layers (FP32 accumulate) with BF16 activations and an
+ * FP32 output layer. Allocates its temporaries. */
+int lpg_mlp_forward_bf16(const float *params, int64_t B, const float *X, float *Y, void *stream);
+/* Trains the network on (residual, exact error) pairs from the plain p-MG FPCG solver of
+ * the problem in `settings` (N = 7, PRECONDITIONER = MULTIGRID) on random Gaussian-bump
+ * right-hand sides. weights_host gets lpg_mlp_param_count() floats, loss_history_host
+ * (may be NULL) the mean training loss of each epoch. */
+int lpg_smoother_train(const char *settings, int nsolves, int samples_per_solve, int epochs, int batch, float lr,
+                       uint64_t seed, float *weights_host, float *loss_history_host);
+/* Replaces the fine-level Chebyshev smoother of e's multigrid preconditioner by the
+ * network with these weights (BF16 inference); a V-cycle whose residual ratio exceeds
+ * `threshold` (0.5 in the task) is redone with the plain smoother. weights_host = NULL
+ * restores the plain smoother. */
+int lpg_elliptic_set_learned_smoother(lpg_elliptic *e, const float *weights_host, double threshold);
 
 #ifdef __cplusplus
 }

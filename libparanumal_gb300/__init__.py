@@ -19,7 +19,7 @@ LPG_OK = 0
 STATUS = {0: "OK", -1: "INVALID", -2: "CUDA", -3: "UNSUPPORTED", -4: "NOT_CONVERGED",
           -5: "ALLOC", -6: "SETTINGS", -7: "BREAKDOWN"}
 INFO = dict(nelements=0, np=1, nglobal=2, nlocal=3, n=4, allneumann=5, mg_plevels=6,
-            mg_amglevels=7, coarse_n=8, device_bytes=9)
+            mg_amglevels=7, coarse_n=8, device_bytes=9, vcycles=10, fallbacks=11)
 
 _lib = None
 
@@ -77,12 +77,24 @@ def lib():
         "lpg_elliptic_run": [vp, vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double),
                              ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)],
     }
+    sig.update({
+        "lpg_mlp_forward_f32": [vp, i64, vp, vp, vp, vp],
+        "lpg_mlp_backward_f32": [vp, i64, vp, vp, vp, vp, vp, vp],
+        "lpg_mlp_adam_f32": [i64, vp, vp, vp, vp, f32, i32, vp],
+        "lpg_mlp_forward_bf16": [vp, i64, vp, vp, vp],
+        "lpg_smoother_train": [ctypes.c_char_p, i32, i32, i32, i32, f32, ctypes.c_uint64, vp, vp],
+        "lpg_elliptic_set_learned_smoother": [vp, vp, f64],
+    })
     for name, args in sig.items():
         fn = getattr(L, name)
         fn.argtypes = args
         fn.restype = ctypes.c_int
     L.lpg_elliptic_info.argtypes = [vp, i32]
     L.lpg_elliptic_info.restype = i64
+    L.lpg_mlp_param_count.argtypes = []
+    L.lpg_mlp_param_count.restype = i64
+    L.lpg_mlp_workspace_floats.argtypes = [i64]
+    L.lpg_mlp_workspace_floats.restype = i64
     _lib = L
     return L
 
@@ -192,6 +204,16 @@ class Elliptic:
             check(st)
         return it.value
 
+    def set_learned_smoother(self, weights, threshold=0.5):
+        """Use the element-local network (FP32 weights, lpg_mlp_param_count() values) as the
+        fine-level smoother, with per-V-cycle fallback above `threshold`; None restores the
+        plain smoother."""
+        if weights is None:
+            check(lib().lpg_elliptic_set_learned_smoother(self.h, None, threshold))
+            return
+        w = np.ascontiguousarray(weights, dtype=np.float32)
+        check(lib().lpg_elliptic_set_learned_smoother(self.h, w.ctypes.data_as(ctypes.c_void_p), threshold))
+
     def Run(self, want_solution=False):
         xL = np.zeros(self.Nlocal) if want_solution else None
         it, nrm, err, sec = ctypes.c_int(0), ctypes.c_double(0), ctypes.c_double(0), ctypes.c_double(0)
@@ -202,6 +224,18 @@ class Elliptic:
             check(st)
         return dict(iterations=it.value, norm=nrm.value, error=err.value, solve_seconds=sec.value,
                     xL=xL, converged=(st == LPG_OK))
+
+
+def train_smoother(settings, nsolves=4, samples_per_solve=5000, epochs=30, batch=250, lr=1e-3, seed=7):
+    """Train the learned smoother on (residual, exact error) pairs of the plain solver of
+    `settings`; returns (weights float32[492800], per-epoch loss float32[epochs])."""
+    n = int(lib().lpg_mlp_param_count())
+    w = np.zeros(n, dtype=np.float32)
+    hist = np.zeros(epochs, dtype=np.float32)
+    check(lib().lpg_smoother_train(settings_text(settings).encode(), nsolves, samples_per_solve, epochs,
+                                   batch, lr, seed, w.ctypes.data_as(ctypes.c_void_p),
+                                   hist.ctypes.data_as(ctypes.c_void_p)))
+    return w, hist
 
 
 def ax_hex(prec, N, Nelements, g2l, ggeo, geo_stride, wJ, wJ_stride, D, lam, q, Aq, Nglobal,

@@ -2,6 +2,8 @@
 // kernel entry points for gather-scatter and vector operations. No C++ exception
 // crosses this boundary; every function returns an LPG status.
 #include "objects.hpp"
+#include "learned.hpp"
+#include "../mlp.hpp"
 
 #include <chrono>
 #include <cmath>
@@ -19,6 +21,7 @@ struct lpg_elliptic {
   std::unique_ptr<Elliptic> el;
   std::unique_ptr<Precon> precon;
   PCGWork work;
+  std::unique_ptr<LearnedSmoother> learned;
   bool flexible = false, stopRhs = false;
   double tol = 1e-8;
   int maxit = 5000;
@@ -269,6 +272,8 @@ extern "C" int64_t lpg_elliptic_info(const lpg_elliptic* e, int what) {
     case LPG_INFO_MG_AMGLEVELS: return e->precon ? e->precon->levels_amg() : 0;
     case LPG_INFO_COARSE_N: return e->precon ? e->precon->coarse_n() : 0;
     case LPG_INFO_DEVICE_BYTES: return device_bytes_in_use();
+    case LPG_INFO_VCYCLES: return e->precon ? e->precon->vcycles() : 0;
+    case LPG_INFO_FALLBACKS: return e->precon ? e->precon->fallbacks() : 0;
     default: return -1;
   }
 }
@@ -450,5 +455,110 @@ extern "C" int lpg_elliptic_run(lpg_elliptic* e, double* xL_host, int* iters, do
   if (solve_seconds) *solve_seconds = std::chrono::duration<double>(t1 - t0).count();
   if (xL_host && (rc = e->xL.download(xL_host, el->Nlocal, s))) return rc;
   return solveStatus;
+  LPG_GUARD_END
+}
+
+// ================================================================ learned smoother
+extern "C" int64_t lpg_mlp_param_count(void) { return kMlpParams; }
+extern "C" int64_t lpg_mlp_workspace_floats(int64_t B) { return B > 0 ? MLPActs::floats(B) : 0; }
+
+extern "C" int lpg_mlp_forward_f32(const float* params, int64_t B, const float* X, float* workspace, float* Y,
+                                   void* stream) {
+  if (!params || !X || !workspace || !Y || B <= 0 || B > INT32_MAX)
+    return set_error(LPG_ERR_INVALID, "mlp forward: bad arguments");
+  LPG_GUARD_BEGIN
+  cudaStream_t s = (cudaStream_t)stream;
+  MLPParams P = MLPParams::view(const_cast<float*>(params));
+  MLPActs A = MLPActs::view(workspace, B);
+  int rc = mlp_forward_f32(P, (int)B, X, A, s);
+  if (rc) return rc;
+  LPG_CUDA_TRY(cudaMemcpyAsync(Y, A.A[3], sizeof(float) * B * kMlpOut, cudaMemcpyDeviceToDevice, s));
+  return LPG_OK;
+  LPG_GUARD_END
+}
+
+extern "C" int lpg_mlp_backward_f32(const float* params, int64_t B, const float* X, const float* workspace,
+                                    const float* dY, float* grads, float* work, void* stream) {
+  if (!params || !X || !workspace || !dY || !grads || !work || B <= 0 || B > INT32_MAX)
+    return set_error(LPG_ERR_INVALID, "mlp backward: bad arguments");
+  LPG_GUARD_BEGIN
+  MLPParams P = MLPParams::view(const_cast<float*>(params));
+  MLPParams G = MLPParams::view(grads);
+  MLPActs A = MLPActs::view(const_cast<float*>(workspace), B);
+  return mlp_backward_f32(P, (int)B, X, A, dY, G, work, work + B * kMlpHidden, (cudaStream_t)stream);
+  LPG_GUARD_END
+}
+
+extern "C" int lpg_mlp_adam_f32(int64_t n, float* w, const float* g, float* m, float* v, float lr, int step,
+                                void* stream) {
+  if (n < 0 || (n > 0 && (!w || !g || !m || !v)) || step < 1) return set_error(LPG_ERR_INVALID, "adam: bad arguments");
+  return adam_step(n, w, g, m, v, lr, step, (cudaStream_t)stream);
+}
+
+extern "C" int lpg_mlp_forward_bf16(const float* params, int64_t B, const float* X, float* Y, void* stream) {
+  if (!params || !X || !Y || B <= 0 || B > INT32_MAX) return set_error(LPG_ERR_INVALID, "mlp bf16 forward: bad arguments");
+  LPG_GUARD_BEGIN
+  cudaStream_t s = (cudaStream_t)stream;
+  LearnedSmoother L;
+  int rc;
+  std::vector<float> host(kMlpParams);
+  LPG_CUDA_TRY(cudaMemcpyAsync(host.data(), params, sizeof(float) * kMlpParams, cudaMemcpyDeviceToHost, s));
+  LPG_CUDA_TRY(cudaStreamSynchronize(s));
+  if ((rc = L.load(host.data(), s)) || (rc = L.ensure_chunk(B))) return rc;
+  if ((rc = convert<float, __nv_bfloat16>(B * kMlpIn, X, L.X.p, s))) return rc;
+  MLPParams P = MLPParams::view(L.params.p);
+  if ((rc = bf16_linear((int)B, kMlpHidden, kMlpIn, L.X.p, L.Wt[0].p, P.b[0], true, true, L.H0.p, s))) return rc;
+  if ((rc = bf16_linear((int)B, kMlpHidden, kMlpHidden, L.H0.p, L.Wt[1].p, P.b[1], true, true, L.H1.p, s))) return rc;
+  if ((rc = bf16_linear((int)B, kMlpHidden, kMlpHidden, L.H1.p, L.Wt[2].p, P.b[2], true, true, L.H0.p, s))) return rc;
+  if ((rc = bf16_linear((int)B, kMlpOut, kMlpHidden, L.H0.p, L.Wt[3].p, P.b[3], false, false, Y, s))) return rc;
+  LPG_CUDA_TRY(cudaStreamSynchronize(s));
+  return LPG_OK;
+  LPG_GUARD_END
+}
+
+extern "C" int lpg_smoother_train(const char* settings, int nsolves, int samples_per_solve, int epochs, int batch,
+                                  float lr, uint64_t seed, float* weights_host, float* loss_history_host) {
+  if (!settings || !weights_host || nsolves < 1 || samples_per_solve < 1 || epochs < 1 || batch < 1 ||
+      (int64_t)nsolves * samples_per_solve < batch)
+    return set_error(LPG_ERR_INVALID, "smoother train: bad arguments");
+  LPG_GUARD_BEGIN
+  lpg_elliptic* e = nullptr;
+  int rc = lpg_elliptic_create(settings, &e);
+  if (rc) return rc;
+  std::unique_ptr<lpg_elliptic> owner(e);
+  if (e->precon->levels_p() < 1) return set_error(LPG_ERR_INVALID, "smoother train: PRECONDITIONER must be MULTIGRID");
+  const MeshConfig& c = e->mcfg;
+  BoxNumbering b{c.nx, c.ny, c.nz, e->el->mesh.N, c.bcflag == -1 ? 1 : 0, c.bcflag == 1 ? 1 : 0};
+  TrainOptions o;
+  o.nsolves = nsolves;
+  o.samplesPerSolve = samples_per_solve;
+  o.epochs = epochs;
+  o.batch = batch;
+  o.lr = lr;
+  o.seed = seed;
+  std::vector<float> w, hist;
+  if ((rc = train_smoother(&e->plat, e->el.get(), e->precon.get(), b, o, w, hist))) return rc;
+  std::memcpy(weights_host, w.data(), sizeof(float) * w.size());
+  if (loss_history_host) std::memcpy(loss_history_host, hist.data(), sizeof(float) * hist.size());
+  return LPG_OK;
+  LPG_GUARD_END
+}
+
+extern "C" int lpg_elliptic_set_learned_smoother(lpg_elliptic* e, const float* weights_host, double threshold) {
+  if (!e) return set_error(LPG_ERR_INVALID, "null argument");
+  LPG_GUARD_BEGIN
+  const MeshConfig& c = e->mcfg;
+  BoxNumbering b{c.nx, c.ny, c.nz, e->el->mesh.N, c.bcflag == -1 ? 1 : 0, c.bcflag == 1 ? 1 : 0};
+  if (!weights_host) {
+    int rc = e->precon->set_learned(nullptr, b, threshold);
+    e->learned.reset();
+    return rc;
+  }
+  auto L = std::make_unique<LearnedSmoother>();
+  int rc = L->load(weights_host, e->plat.stream);
+  if (rc) return rc;
+  if ((rc = e->precon->set_learned(L.get(), b, threshold))) return rc;
+  e->learned = std::move(L);
+  return LPG_OK;
   LPG_GUARD_END
 }

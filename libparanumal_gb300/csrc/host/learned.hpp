@@ -1,0 +1,42 @@
+// Learned fine-level smoother: inference object and training driver.
+#pragma once
+
+#include <vector>
+
+#include "objects.hpp"
+
+namespace lpg {
+
+struct LearnedSmoother {
+  static constexpr int64_t kChunk = 65536;  // elements per inference pass
+  bool ready = false;
+  DevBuf<float> params;                     // FP32 master weights (MLPParams layout)
+  DevBuf<__nv_bfloat16> Wt[4];              // BF16 transposed weights for inference
+  DevBuf<__nv_bfloat16> X, H0, H1;
+  DevBuf<float> out, scale;
+  int64_t chunk = 0;
+  int load(const float* hostParams, cudaStream_t s);
+  int ensure_chunk(int64_t rows);
+  // z (assembled, overwritten) = weighted average over copies of s_e invDiag .* MLP(features(r))
+  template <typename T>
+  int apply(const BoxNumbering& b, int64_t E, const int32_t* g2l, const T* r, const double* invDiag,
+            const double* weight, T* z, int64_t Nglobal, cudaStream_t s);
+};
+
+struct TrainOptions {
+  int nsolves = 4;
+  int samplesPerSolve = 5000;
+  int epochs = 30;
+  int batch = 250;
+  float lr = 1e-3f;
+  int bumps = 8;
+  double solveTol = 1e-10;
+  uint64_t seed = 7;
+};
+
+// Generates (residual, exact error) samples with the plain solver `plainMG` on `el` and
+// trains the network; returns FP32 weights and the per-epoch mean training loss.
+int train_smoother(Platform* plat, Elliptic* el, Precon* plainMG, const BoxNumbering& b, const TrainOptions& o,
+                   std::vector<float>& weights, std::vector<float>& lossHistory);
+
+}  // namespace lpg

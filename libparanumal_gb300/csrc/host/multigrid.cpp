@@ -10,6 +10,7 @@
 // The drand48 stream is seeded with 0 and consumed in the reference's order: p-level
 // Arnoldi vectors, then per AMG level the Arnoldi vector and the MIS-2 priorities.
 #include "objects.hpp"
+#include "learned.hpp"
 
 #include <algorithm>
 #include <cmath>
@@ -439,9 +440,26 @@ class MultiGrid : public Precon {
   DevBuf<double> aRhs0, aX0;
   DevBuf<float> in32, out32;
 
+  // learned fine-level smoother
+  LearnedSmoother* learned = nullptr;
+  BoxNumbering box{};
+  double threshold = 0.5;
+  int64_t nFallback = 0, nVcycle = 0;
+
   int levels_p() const override { return (int)p.size(); }
   int levels_amg() const override { return (int)a.size(); }
   int64_t coarse_n() const override { return coarseN; }
+  int64_t fallbacks() const override { return nFallback; }
+  int64_t vcycles() const override { return nVcycle; }
+  int set_learned(LearnedSmoother* L, const BoxNumbering& b, double thr) override {
+    if (p.empty()) return set_error(LPG_ERR_UNSUPPORTED, "a learned smoother needs at least one p-level");
+    if (fine->mesh.N != 7) return set_error(LPG_ERR_UNSUPPORTED, "the learned smoother is defined for N = 7");
+    learned = L;
+    box = b;
+    threshold = thr;
+    nFallback = nVcycle = 0;
+    return LPG_OK;
+  }
 
   int setup(Elliptic* el, const MeshConfig& c, const MGOptions& o);
   int apply(const double* r, double* z, cudaStream_t s) override;
@@ -452,6 +470,9 @@ class MultiGrid : public Precon {
   template <typename T> int op(Elliptic* el, const T* q, T* Aq, cudaStream_t s);
   template <typename T> int smooth(PLevel& L, const T* r, T* x, bool xIsZero, cudaStream_t s);
   template <typename T> int vcycle_p(int k, const T* rhs, T* x, cudaStream_t s);
+  template <typename T> int coarse_correct(int k, const T* RES, T* X, cudaStream_t s);
+  template <typename T> int vcycle_learned(const T* rhs, T* x, cudaStream_t s);
+  template <typename T> int dot_host(int64_t n, const T* x, const T* y, double& out, cudaStream_t s);
   int vcycle_a(int k, const double* rhs, double* x, cudaStream_t s);
   int smooth_a(ALevel& L, const double* b, double* x, bool xIsZero, cudaStream_t s);
   int setup_amg(Elliptic* el, Rand48& rng);
@@ -519,6 +540,15 @@ int MultiGrid::vcycle_p(int k, const T* RHS, T* X, cudaStream_t s) {
   if ((rc = smooth<T>(L, RHS, X, true, s))) return rc;
   if ((rc = op<T>(L.el, X, RES, s))) return rc;
   if ((rc = axpy<T>(N, T(1), RHS, T(-1), RES, s))) return rc;
+  if ((rc = coarse_correct<T>(k, RES, X, s))) return rc;
+  return smooth<T>(L, RHS, X, false, s);
+}
+
+// X += P (coarse-level V-cycle of the restricted residual RES)
+template <typename T>
+int MultiGrid::coarse_correct(int k, const T* RES, T* X, cudaStream_t s) {
+  PLevel& L = *p[k];
+  int rc;
   const bool last = (k + 1 == (int)p.size());
   T* weight = vec<T>(L.el->weightG, L.el->weightG32);
   const T* P = vec<T>(L.P64, L.P32);
@@ -555,7 +585,49 @@ int MultiGrid::vcycle_p(int k, const T* RHS, T* X, cudaStream_t s) {
                                     s)))
       return rc;
   }
-  return smooth<T>(L, RHS, X, false, s);
+  return LPG_OK;
+}
+
+template <typename T>
+int MultiGrid::dot_host(int64_t n, const T* x, const T* y, double& out, cudaStream_t s) {
+  int rc;
+  if constexpr (std::is_same<T, double>::value) rc = dot(n, x, y, plat->scalars.p + 2, plat->partials.p, s);
+  else rc = dot_f32(n, x, y, plat->scalars.p + 2, plat->partials.p, s);
+  if (rc) return rc;
+  LPG_CUDA_TRY(cudaMemcpyAsync(plat->hostScalars + 2, plat->scalars.p + 2, sizeof(double), cudaMemcpyDeviceToHost, s));
+  LPG_CUDA_TRY(cudaStreamSynchronize(s));
+  out = plat->hostScalars[2];
+  return LPG_OK;
+}
+
+// V-cycle whose fine-level smoother is the learned element-local map L:
+// X = L(RHS); X += coarse correction of RHS - A X; X += L(RHS - A X).
+// If the V-cycle leaves ||RHS - A X|| > threshold ||RHS||, it is redone with the plain
+// smoother (fallback), and the fallback is counted.
+template <typename T>
+int MultiGrid::vcycle_learned(const T* RHS, T* X, cudaStream_t s) {
+  PLevel& L = *p[0];
+  Elliptic* el = L.el;
+  const int64_t N = el->Nglobal, E = el->mesh.E;
+  T* RES = vec<T>(L.res64, L.res32);
+  T* D = vec<T>(s64[2], s32[2]);
+  int rc;
+  if ((rc = learned->apply<T>(box, E, el->g2l.p, RHS, L.invDiag64.p, el->weightG.p, X, N, s))) return rc;
+  if ((rc = op<T>(el, X, RES, s)) || (rc = axpy<T>(N, T(1), RHS, T(-1), RES, s))) return rc;
+  if ((rc = coarse_correct<T>(0, RES, X, s))) return rc;
+  if ((rc = op<T>(el, X, RES, s)) || (rc = axpy<T>(N, T(1), RHS, T(-1), RES, s))) return rc;
+  if ((rc = learned->apply<T>(box, E, el->g2l.p, RES, L.invDiag64.p, el->weightG.p, D, N, s))) return rc;
+  if ((rc = axpy<T>(N, T(1), D, T(1), X, s))) return rc;
+  // residual reduction of this V-cycle
+  if ((rc = op<T>(el, X, RES, s)) || (rc = axpy<T>(N, T(1), RHS, T(-1), RES, s))) return rc;
+  double rr, bb;
+  if ((rc = dot_host<T>(N, RES, RES, rr, s)) || (rc = dot_host<T>(N, RHS, RHS, bb, s))) return rc;
+  nVcycle++;
+  if (!(rr <= threshold * threshold * bb)) {
+    nFallback++;
+    return vcycle_p<T>(0, RHS, X, s);
+  }
+  return LPG_OK;
 }
 
 // ---------------------------------------------------------------- AMG V-cycle (device)
@@ -612,12 +684,14 @@ int MultiGrid::apply(const double* r, double* z, cudaStream_t s) {
   if (p.empty()) {
     rc = vcycle_a(0, r, z, s);
   } else if (!f32()) {
-    rc = vcycle_p<double>(0, r, z, s);
+    rc = learned ? vcycle_learned<double>(r, z, s) : vcycle_p<double>(0, r, z, s);
   } else {
     const int64_t N = fine->Nglobal;
     PLevel& L0 = *p[0];
     if ((rc = convert<double, float>(N, r, L0.rhs32.p, s))) return rc;
-    if ((rc = vcycle_p<float>(0, L0.rhs32.p, L0.x32.p, s))) return rc;
+    if (learned) rc = vcycle_learned<float>(L0.rhs32.p, L0.x32.p, s);
+    else rc = vcycle_p<float>(0, L0.rhs32.p, L0.x32.p, s);
+    if (rc) return rc;
     rc = convert<float, double>(N, L0.x32.p, z, s);
   }
   if (rc) return rc;
@@ -785,7 +859,7 @@ int MultiGrid::setup(Elliptic* el, const MeshConfig& c, const MGOptions& o) {
       if ((rc = L.res32.alloc(N)) || (rc = L.rhs32.alloc(N)) || (rc = L.x32.alloc(N))) return rc;
       if ((rc = L.invDiag32.alloc(N)) || (rc = convert<double, float>(N, L.invDiag64.p, L.invDiag32.p, s))) return rc;
       if ((rc = L.P32.alloc(L.P64.n)) || (rc = convert<double, float>(L.P64.n, L.P64.p, L.P32.p, s))) return rc;
-      L.invDiag64.release();
+      if (k > 0) L.invDiag64.release();  // the fine level keeps FP64 1/diag for a learned smoother
     }
   }
   if (f32()) {

@@ -141,12 +141,21 @@ struct Elliptic {
 };
 
 // ---------------------------------------------------------------- preconditioners
+struct LearnedSmoother;
+
 struct Precon {
   virtual ~Precon() = default;
   virtual int apply(const double* r, double* z, cudaStream_t s) = 0;
   virtual int levels_p() const { return 0; }
   virtual int levels_amg() const { return 0; }
   virtual int64_t coarse_n() const { return 0; }
+  // learned fine-level smoother with per-V-cycle fallback to the plain smoother when the
+  // V-cycle reduces the residual by less than `threshold` (ratio above it)
+  virtual int set_learned(LearnedSmoother*, const BoxNumbering&, double /*threshold*/) {
+    return set_error(LPG_ERR_UNSUPPORTED, "a learned smoother needs PRECONDITIONER = MULTIGRID");
+  }
+  virtual int64_t fallbacks() const { return 0; }
+  virtual int64_t vcycles() const { return 0; }
 };
 
 std::unique_ptr<Precon> make_identity(Elliptic* el);

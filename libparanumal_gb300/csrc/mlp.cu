@@ -1,0 +1,456 @@
+// Element-local MLP of the learned fine-level smoother (no reference counterpart).
+//
+// Network: 896 -> 256 -> 256 -> 256 -> 512, GELU (tanh form) after the hidden layers.
+// Input per element: its 512 residual values and the 6 x 64 residual values of the first
+// interior node layer of each face neighbour (zero on boundary faces), all divided by the
+// element's residual RMS s_e. Output: 512 values; the smoother's correction at the
+// element's nodes is s_e * invDiag * output, averaged over shared nodes.
+//
+// Training runs in FP32 (tiled SIMT GEMMs with fused bias/GELU epilogues, backward,
+// Adam); inference uses BF16 tensor-core tiles (mma.sync m16n8k16, FP32 accumulate)
+// with BF16 activations between layers and an FP32 output layer.
+#include "lpg_common.cuh"
+#include "lpg_internal.hpp"
+#include "mlp.hpp"
+
+namespace lpg {
+
+__device__ __forceinline__ float gelu_f(float z) {
+  const float c = 0.7978845608028654f;  // sqrt(2/pi)
+  const float u = c * (z + 0.044715f * z * z * z);
+  return 0.5f * z * (1.0f + tanhf(u));
+}
+__device__ __forceinline__ float gelu_grad_f(float z) {
+  const float c = 0.7978845608028654f;
+  const float u = c * (z + 0.044715f * z * z * z);
+  const float t = tanhf(u);
+  const float du = c * (1.0f + 3.0f * 0.044715f * z * z);
+  return 0.5f * (1.0f + t) + 0.5f * z * (1.0f - t * t) * du;
+}
+
+// ---------------------------------------------------------------- FP32 tiled GEMM
+// C[M x N] (+)= op(A)[M x K] * op(B)[K x N] (+ bias[N]); optional GELU with the
+// pre-activation stored in Z. Row-major; TA: A is stored K x M; TB: B is stored N x K.
+constexpr int SG_BM = 64, SG_BN = 64, SG_BK = 16;
+
+template <bool TA, bool TB>
+__global__ void __launch_bounds__(256)
+sgemm_kernel(const int M, const int N, const int K, const float* __restrict__ A, const int lda,
+             const float* __restrict__ B, const int ldb, float* __restrict__ C, const int ldc,
+             const float* __restrict__ bias, const int act, float* __restrict__ Z, const float beta) {
+  __shared__ float sA[SG_BK][SG_BM + 4];
+  __shared__ float sB[SG_BK][SG_BN + 4];
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  const int m0 = blockIdx.y * SG_BM, n0 = blockIdx.x * SG_BN;
+  float acc[4][4] = {};
+  for (int k0 = 0; k0 < K; k0 += SG_BK) {
+    for (int t = threadIdx.x; t < SG_BK * SG_BM; t += 256) {
+      const int kk = t / SG_BM, mm = t % SG_BM;
+      const int gm = m0 + mm, gk = k0 + kk;
+      float v = 0.f;
+      if (gm < M && gk < K) v = TA ? A[(int64_t)gk * lda + gm] : A[(int64_t)gm * lda + gk];
+      sA[kk][mm] = v;
+    }
+    for (int t = threadIdx.x; t < SG_BK * SG_BN; t += 256) {
+      const int kk = t / SG_BN, nn = t % SG_BN;
+      const int gn = n0 + nn, gk = k0 + kk;
+      float v = 0.f;
+      if (gn < N && gk < K) v = TB ? B[(int64_t)gn * ldb + gk] : B[(int64_t)gk * ldb + gn];
+      sB[kk][nn] = v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < SG_BK; ++kk) {
+      float a[4], b[4];
+#pragma unroll
+      for (int r = 0; r < 4; ++r) a[r] = sA[kk][ty * 4 + r];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) b[c] = sB[kk][tx * 4 + c];
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) acc[r][c] += a[r] * b[c];
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const int gm = m0 + ty * 4 + r;
+    if (gm >= M) continue;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const int gn = n0 + tx * 4 + c;
+      if (gn >= N) continue;
+      float v = acc[r][c];
+      if (bias) v += bias[gn];
+      const int64_t idx = (int64_t)gm * ldc + gn;
+      if (beta != 0.f) v += beta * C[idx];
+      if (act) {
+        if (Z) Z[idx] = v;
+        v = gelu_f(v);
+      }
+      C[idx] = v;
+    }
+  }
+}
+
+int sgemm(bool ta, bool tb, int M, int N, int K, const float* A, int lda, const float* B, int ldb, float* C,
+          int ldc, const float* bias, bool gelu, float* Z, float beta, cudaStream_t s) {
+  if (M <= 0 || N <= 0) return LPG_OK;
+  dim3 grid((N + SG_BN - 1) / SG_BN, (M + SG_BM - 1) / SG_BM);
+  if (!ta && !tb) sgemm_kernel<false, false><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc, bias, gelu, Z, beta);
+  else if (!ta && tb) sgemm_kernel<false, true><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc, bias, gelu, Z, beta);
+  else if (ta && !tb) sgemm_kernel<true, false><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc, bias, gelu, Z, beta);
+  else sgemm_kernel<true, true><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc, bias, gelu, Z, beta);
+  LPG_LAUNCH_CHECK("sgemm_kernel");
+  return LPG_OK;
+}
+
+// dZ = dA .* gelu'(Z) (in place on dA)
+__global__ void gelu_backward_kernel(const int64_t n, const float* __restrict__ Z, float* __restrict__ dA) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    dA[i] *= gelu_grad_f(Z[i]);
+}
+// db[c] = sum_r dZ[r][c]
+__global__ void bias_grad_kernel(const int rows, const int cols, const float* __restrict__ dZ, float* __restrict__ db) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= cols) return;
+  float s = 0.f;
+  for (int r = 0; r < rows; ++r) s += dZ[(int64_t)r * cols + c];
+  db[c] = s;
+}
+// MSE loss 0.5/B * sum (y - t)^2 ; dY = (y - t)/B ; loss accumulated into *loss
+__global__ void mse_kernel(const int64_t n, const float invB, const float* __restrict__ y, const float* __restrict__ t,
+                           float* __restrict__ dy, float* __restrict__ loss) {
+  float acc = 0.f;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float d = y[i] - t[i];
+    dy[i] = d * invB;
+    acc += 0.5f * d * d * invB;
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(loss, acc);
+}
+// Adam (Kingma & Ba): m = b1 m + (1-b1) g; v = b2 v + (1-b2) g^2; w -= lr mhat / (sqrt(vhat) + eps)
+__global__ void adam_kernel(const int64_t n, float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m,
+                            float* __restrict__ v, const float lr, const float b1, const float b2, const float eps,
+                            const float c1, const float c2) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    w[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+  }
+}
+
+static unsigned grid_n(int64_t n) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 4096)); }
+
+int mlp_forward_f32(const MLPParams& P, int B, const float* X, MLPActs& act, cudaStream_t s) {
+  const int dims[5] = {kMlpIn, kMlpHidden, kMlpHidden, kMlpHidden, kMlpOut};
+  const float* in = X;
+  int rc;
+  for (int l = 0; l < 4; ++l) {
+    const bool last = (l == 3);
+    if ((rc = sgemm(false, false, B, dims[l + 1], dims[l], in, dims[l], P.W[l], dims[l + 1], act.A[l], dims[l + 1],
+                    P.b[l], !last, last ? nullptr : act.Z[l], 0.f, s)))
+      return rc;
+    in = act.A[l];
+  }
+  return LPG_OK;
+}
+
+int mlp_backward_f32(const MLPParams& P, int B, const float* X, const MLPActs& act, const float* dY, MLPParams& G,
+                     float* work0, float* work1, cudaStream_t s) {
+  const int dims[5] = {kMlpIn, kMlpHidden, kMlpHidden, kMlpHidden, kMlpOut};
+  // dcur holds dL/d(pre-activation) of layer l
+  const float* dcur = dY;
+  int rc;
+  for (int l = 3; l >= 0; --l) {
+    const float* in = (l == 0) ? X : act.A[l - 1];
+    // dW[l] = in^T dcur ; db[l] = colsum(dcur)
+    if ((rc = sgemm(true, false, dims[l], dims[l + 1], B, in, dims[l], dcur, dims[l + 1], G.W[l], dims[l + 1], nullptr,
+                    false, nullptr, 0.f, s)))
+      return rc;
+    bias_grad_kernel<<<(dims[l + 1] + 127) / 128, 128, 0, s>>>(B, dims[l + 1], dcur, G.b[l]);
+    LPG_LAUNCH_CHECK("bias_grad_kernel");
+    if (l == 0) break;
+    float* dprev = (l % 2) ? work0 : work1;
+    // dA[l-1] = dcur W[l]^T, then times gelu'(Z[l-1])
+    if ((rc = sgemm(false, true, B, dims[l], dims[l + 1], dcur, dims[l + 1], P.W[l], dims[l + 1], dprev, dims[l],
+                    nullptr, false, nullptr, 0.f, s)))
+      return rc;
+    gelu_backward_kernel<<<grid_n((int64_t)B * dims[l]), 256, 0, s>>>((int64_t)B * dims[l], act.Z[l - 1], dprev);
+    LPG_LAUNCH_CHECK("gelu_backward_kernel");
+    dcur = dprev;
+  }
+  return LPG_OK;
+}
+
+int mse_loss(int64_t n, int B, const float* y, const float* t, float* dy, float* loss, cudaStream_t s) {
+  LPG_CUDA_TRY(cudaMemsetAsync(loss, 0, sizeof(float), s));
+  mse_kernel<<<grid_n(n), 256, 0, s>>>(n, 1.0f / (float)B, y, t, dy, loss);
+  LPG_LAUNCH_CHECK("mse_kernel");
+  return LPG_OK;
+}
+
+int adam_step(int64_t n, float* w, const float* g, float* m, float* v, float lr, int step, cudaStream_t s) {
+  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+  const float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
+  adam_kernel<<<grid_n(n), 256, 0, s>>>(n, w, g, m, v, lr, b1, b2, eps, c1, c2);
+  LPG_LAUNCH_CHECK("adam_kernel");
+  return LPG_OK;
+}
+
+// ---------------------------------------------------------------- BF16 tensor-core inference
+// Y[M x N] = act(X[M x K] W + b): X bf16 row-major (lda = K), Wt bf16 stored N x K
+// (k contiguous), FP32 accumulate in mma.sync.m16n8k16 tiles. CTA tile 128 x 64, BK 32,
+// 8 warps as 4 (M) x 2 (N), each warp 32 x 32 = 2 x 4 mma tiles. K and N are multiples of
+// 32 and 64 for every layer of this network; M is guarded.
+constexpr int TB_M = 128, TB_N = 64, TB_K = 32, TB_PAD = 8;
+
+__device__ __forceinline__ void mma_bf16_16816(float* c, const uint32_t* a, const uint32_t* b) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+template <int OUT_BF16>
+__global__ void __launch_bounds__(256)
+bf16_linear_kernel(const int M, const int N, const int K, const __nv_bfloat16* __restrict__ X,
+                   const __nv_bfloat16* __restrict__ Wt, const float* __restrict__ bias, const int act,
+                   void* __restrict__ Yv) {
+  __shared__ __align__(16) __nv_bfloat16 sA[TB_M][TB_K + TB_PAD];
+  __shared__ __align__(16) __nv_bfloat16 sB[TB_N][TB_K + TB_PAD];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int wm = warp % 4, wn = warp / 4;
+  const int g = lane >> 2, t = lane & 3;
+  const int m0 = blockIdx.y * TB_M, n0 = blockIdx.x * TB_N;
+  float acc[2][4][4] = {};
+  for (int k0 = 0; k0 < K; k0 += TB_K) {
+    // A tile: 128 x 32 bf16 = 512 x 16 B chunks, 2 per thread
+    for (int c = threadIdx.x; c < TB_M * TB_K / 8; c += 256) {
+      const int row = c / (TB_K / 8), col = (c % (TB_K / 8)) * 8;
+      const int gm = m0 + row;
+      uint4 v = make_uint4(0, 0, 0, 0);
+      if (gm < M) v = *reinterpret_cast<const uint4*>(X + (int64_t)gm * K + k0 + col);
+      *reinterpret_cast<uint4*>(&sA[row][col]) = v;
+    }
+    // B tile: 64 x 32 bf16 = 256 chunks, 1 per thread
+    for (int c = threadIdx.x; c < TB_N * TB_K / 8; c += 256) {
+      const int row = c / (TB_K / 8), col = (c % (TB_K / 8)) * 8;
+      *reinterpret_cast<uint4*>(&sB[row][col]) = *reinterpret_cast<const uint4*>(Wt + (int64_t)(n0 + row) * K + k0 + col);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < TB_K; kk += 16) {
+      uint32_t a[2][4], b[4][2];
+#pragma unroll
+      for (int im = 0; im < 2; ++im) {
+        const int r = wm * 32 + im * 16;
+        a[im][0] = *reinterpret_cast<const uint32_t*>(&sA[r + g][kk + t * 2]);
+        a[im][1] = *reinterpret_cast<const uint32_t*>(&sA[r + g + 8][kk + t * 2]);
+        a[im][2] = *reinterpret_cast<const uint32_t*>(&sA[r + g][kk + t * 2 + 8]);
+        a[im][3] = *reinterpret_cast<const uint32_t*>(&sA[r + g + 8][kk + t * 2 + 8]);
+      }
+#pragma unroll
+      for (int in = 0; in < 4; ++in) {
+        const int cidx = wn * 32 + in * 8 + g;
+        b[in][0] = *reinterpret_cast<const uint32_t*>(&sB[cidx][kk + t * 2]);
+        b[in][1] = *reinterpret_cast<const uint32_t*>(&sB[cidx][kk + t * 2 + 8]);
+      }
+#pragma unroll
+      for (int im = 0; im < 2; ++im)
+#pragma unroll
+        for (int in = 0; in < 4; ++in) mma_bf16_16816(acc[im][in], a[im], b[in]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int im = 0; im < 2; ++im)
+#pragma unroll
+    for (int in = 0; in < 4; ++in)
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int row = m0 + wm * 32 + im * 16 + g + h * 8;
+        const int col = n0 + wn * 32 + in * 8 + t * 2;
+        if (row >= M) continue;
+        float v0 = acc[im][in][h * 2 + 0] + bias[col];
+        float v1 = acc[im][in][h * 2 + 1] + bias[col + 1];
+        if (act) { v0 = gelu_f(v0); v1 = gelu_f(v1); }
+        if (OUT_BF16) {
+          __nv_bfloat162 p = __floats2bfloat162_rn(v0, v1);
+          *reinterpret_cast<__nv_bfloat162*>(reinterpret_cast<__nv_bfloat16*>(Yv) + (int64_t)row * N + col) = p;
+        } else {
+          float2 p = make_float2(v0, v1);
+          *reinterpret_cast<float2*>(reinterpret_cast<float*>(Yv) + (int64_t)row * N + col) = p;
+        }
+      }
+}
+
+int bf16_linear(int M, int N, int K, const __nv_bfloat16* X, const __nv_bfloat16* Wt, const float* bias, bool gelu,
+                bool outBf16, void* Y, cudaStream_t s) {
+  if (M <= 0) return LPG_OK;
+  if (N % TB_N || K % TB_K) return set_error(LPG_ERR_INVALID, "bf16_linear: N must be a multiple of 64 and K of 32");
+  dim3 grid(N / TB_N, (M + TB_M - 1) / TB_M);
+  if (outBf16) bf16_linear_kernel<1><<<grid, 256, 0, s>>>(M, N, K, X, Wt, bias, gelu, Y);
+  else bf16_linear_kernel<0><<<grid, 256, 0, s>>>(M, N, K, X, Wt, bias, gelu, Y);
+  LPG_LAUNCH_CHECK("bf16_linear_kernel");
+  return LPG_OK;
+}
+
+// W (K x N fp32 row-major) -> Wt (N x K bf16)
+__global__ void transpose_to_bf16_kernel(const int K, const int N, const float* __restrict__ W,
+                                         __nv_bfloat16* __restrict__ Wt) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < (int64_t)K * N; i += (int64_t)gridDim.x * blockDim.x) {
+    const int k = (int)(i / N), n = (int)(i % N);
+    Wt[(int64_t)n * K + k] = __float2bfloat16(W[i]);
+  }
+}
+int transpose_to_bf16(int K, int N, const float* W, __nv_bfloat16* Wt, cudaStream_t s) {
+  transpose_to_bf16_kernel<<<grid_n((int64_t)K * N), 256, 0, s>>>(K, N, W, Wt);
+  LPG_LAUNCH_CHECK("transpose_to_bf16_kernel");
+  return LPG_OK;
+}
+
+// ---------------------------------------------------------------- element features
+// Face f of element (ex,ey,ez) in the reference's numbering (meshBasisHex3D.cpp:60-90):
+// 0: k=0, 1: j=0, 2: i=N, 3: j=N, 4: i=0, 5: k=N. The trace of face f is the neighbour's
+// node layer next to the shared face (i=1 / i=N-1 ...), listed in face-node order.
+template <typename TIN, typename TOUT>
+__global__ void __launch_bounds__(256)
+features_kernel(const BoxNumbering b, const int64_t E, const int64_t e0, const int32_t* __restrict__ g2l,
+                const TIN* __restrict__ r, TOUT* __restrict__ X, float* __restrict__ scale) {
+  const int Nq = b.N + 1, Np = Nq * Nq * Nq, Nfp = Nq * Nq;
+  const int64_t eb = e0 + blockIdx.x;
+  if (eb >= E) return;
+  __shared__ float s_in[kMlpIn];
+  __shared__ float s_red[8];
+  const int ex = (int)(eb % b.nx), ey = (int)((eb / b.nx) % b.ny), ez = (int)(eb / ((int64_t)b.nx * b.ny));
+  for (int t = threadIdx.x; t < kMlpIn; t += blockDim.x) {
+    float v = 0.f;
+    if (t < Np) {
+      const int32_t g = g2l[eb * Np + t];
+      v = (g >= 0) ? (float)r[g] : 0.f;
+    } else {
+      const int f = (t - Np) / Nfp, m = (t - Np) % Nfp;
+      const int p = m % Nq, q = m / Nq;  // face-local coordinates in node order
+      int nx = ex, ny = ey, nz = ez, i = 0, j = 0, k = 0;
+      switch (f) {
+        case 0: nz = ez - 1; i = p; j = q; k = b.N - 1; break;
+        case 1: ny = ey - 1; i = p; k = q; j = b.N - 1; break;
+        case 2: nx = ex + 1; j = p; k = q; i = 1; break;
+        case 3: ny = ey + 1; i = p; k = q; j = 1; break;
+        case 4: nx = ex - 1; j = p; k = q; i = b.N - 1; break;
+        default: nz = ez + 1; i = p; j = q; k = 1; break;
+      }
+      if (b.periodic) { nx = (nx + b.nx) % b.nx; ny = (ny + b.ny) % b.ny; nz = (nz + b.nz) % b.nz; }
+      if (nx >= 0 && nx < b.nx && ny >= 0 && ny < b.ny && nz >= 0 && nz < b.nz) {
+        const int64_t en = nx + (int64_t)ny * b.nx + (int64_t)nz * b.nx * b.ny;
+        const int32_t g = g2l[en * Np + i + j * Nq + k * Nfp];
+        v = (g >= 0) ? (float)r[g] : 0.f;
+      }
+    }
+    s_in[t] = v;
+  }
+  __syncthreads();
+  float ss = 0.f;
+  for (int t = threadIdx.x; t < Np; t += blockDim.x) ss += s_in[t] * s_in[t];
+  for (int o = 16; o > 0; o >>= 1) ss += __shfl_down_sync(0xffffffffu, ss, o);
+  if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = ss;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float tot = 0.f;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += s_red[w];
+    s_red[0] = sqrtf(tot / (float)Np) + 1e-30f;
+    scale[blockIdx.x] = s_red[0];
+  }
+  __syncthreads();
+  const float inv = 1.f / s_red[0];
+  for (int t = threadIdx.x; t < kMlpIn; t += blockDim.x) X[blockIdx.x * (int64_t)kMlpIn + t] = (TOUT)(s_in[t] * inv);
+}
+
+template <typename TIN, typename TOUT>
+int element_features(const BoxNumbering& b, int64_t E, int64_t e0, int64_t count, const int32_t* g2l, const TIN* r,
+                     TOUT* X, float* scale, cudaStream_t s) {
+  if ((b.N + 1) * (b.N + 1) * (b.N + 1) + 6 * (b.N + 1) * (b.N + 1) != kMlpIn)
+    return set_error(LPG_ERR_UNSUPPORTED, "learned smoother needs N = 7 (896 inputs per element)");
+  if (count <= 0) return LPG_OK;
+  features_kernel<TIN, TOUT><<<(unsigned)count, 256, 0, s>>>(b, E, e0, g2l, r, X, scale);
+  LPG_LAUNCH_CHECK("features_kernel");
+  return LPG_OK;
+}
+template int element_features<double, float>(const BoxNumbering&, int64_t, int64_t, int64_t, const int32_t*,
+                                             const double*, float*, float*, cudaStream_t);
+template int element_features<double, __nv_bfloat16>(const BoxNumbering&, int64_t, int64_t, int64_t, const int32_t*,
+                                                     const double*, __nv_bfloat16*, float*, cudaStream_t);
+template int element_features<float, __nv_bfloat16>(const BoxNumbering&, int64_t, int64_t, int64_t, const int32_t*,
+                                                    const float*, __nv_bfloat16*, float*, cudaStream_t);
+
+// z_local = s_e * invDiag * out ; z[g] += weight[g] * z_local (average over copies)
+template <typename TV>
+__global__ void apply_correction_kernel(const int Np, const int64_t count, const int64_t e0,
+                                        const int32_t* __restrict__ g2l, const float* __restrict__ out,
+                                        const float* __restrict__ scale, const double* __restrict__ invDiag,
+                                        const double* __restrict__ weight, TV* __restrict__ z) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count * Np; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t el = i / Np;
+    const int n = (int)(i % Np);
+    const int32_t g = g2l[(e0 + el) * Np + n];
+    if (g < 0) continue;
+    const double v = (double)scale[el] * (double)out[el * kMlpOut + n] * invDiag[g] * weight[g];
+    atomicAdd(z + g, (TV)v);
+  }
+}
+template <typename TV>
+int apply_correction(int Np, int64_t count, int64_t e0, const int32_t* g2l, const float* out, const float* scale,
+                     const double* invDiag, const double* weight, TV* z, cudaStream_t s) {
+  if (count <= 0) return LPG_OK;
+  apply_correction_kernel<TV><<<grid_n(count * Np), 256, 0, s>>>(Np, count, e0, g2l, out, scale, invDiag, weight, z);
+  LPG_LAUNCH_CHECK("apply_correction_kernel");
+  return LPG_OK;
+}
+template int apply_correction<double>(int, int64_t, int64_t, const int32_t*, const float*, const float*, const double*,
+                                      const double*, double*, cudaStream_t);
+template int apply_correction<float>(int, int64_t, int64_t, const int32_t*, const float*, const float*, const double*,
+                                     const double*, float*, cudaStream_t);
+
+// training target: t = D .* e_local / s (network output units), e gathered from the dofs
+__global__ void target_kernel(const int Np, const int64_t count, const int32_t* __restrict__ elems,
+                              const int32_t* __restrict__ g2l, const double* __restrict__ e, const double* __restrict__ invDiag,
+                              const float* __restrict__ scale, float* __restrict__ T) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count * Np; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t el = i / Np;
+    const int n = (int)(i % Np);
+    const int32_t g = g2l[(int64_t)elems[el] * Np + n];
+    T[el * kMlpOut + n] = (g >= 0) ? (float)(e[g] / invDiag[g] / (double)scale[el]) : 0.f;
+  }
+}
+int training_targets(int Np, int64_t count, const int32_t* elems, const int32_t* g2l, const double* e,
+                     const double* invDiag, const float* scale, float* T, cudaStream_t s) {
+  if (count <= 0) return LPG_OK;
+  target_kernel<<<grid_n(count * Np), 256, 0, s>>>(Np, count, elems, g2l, e, invDiag, scale, T);
+  LPG_LAUNCH_CHECK("target_kernel");
+  return LPG_OK;
+}
+
+// features of a list of elements (training samples)
+template <typename TOUT>
+__global__ void gather_rows_kernel(const int64_t count, const int32_t* __restrict__ elems, const TOUT* __restrict__ Xall,
+                                   TOUT* __restrict__ X) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count * kMlpIn; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t el = i / kMlpIn;
+    X[i] = Xall[(int64_t)elems[el] * kMlpIn + (i % kMlpIn)];
+  }
+}
+int gather_rows(int64_t count, const int32_t* elems, const float* Xall, float* X, cudaStream_t s) {
+  if (count <= 0) return LPG_OK;
+  gather_rows_kernel<float><<<grid_n(count * kMlpIn), 256, 0, s>>>(count, elems, Xall, X);
+  LPG_LAUNCH_CHECK("gather_rows_kernel");
+  return LPG_OK;
+}
+
+}  // namespace lpg

@@ -1,0 +1,77 @@
+// Element-local MLP of the learned fine-level smoother: sizes, parameter layout and
+// kernel entry points (mlp.cu).
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "lpg_internal.hpp"
+
+namespace lpg {
+
+constexpr int kMlpIn = 896;      // 512 element residual values + 6 x 64 face traces (N = 7)
+constexpr int kMlpHidden = 256;
+constexpr int kMlpOut = 512;
+// parameter vector: W0 (896x256), b0, W1 (256x256), b1, W2 (256x256), b2, W3 (256x512), b3
+constexpr int64_t kMlpParams = (int64_t)kMlpIn * kMlpHidden + kMlpHidden + 2 * ((int64_t)kMlpHidden * kMlpHidden + kMlpHidden) +
+                               (int64_t)kMlpHidden * kMlpOut + kMlpOut;
+
+struct MLPParams {
+  float* W[4];
+  float* b[4];
+  static MLPParams view(float* base) {
+    MLPParams p;
+    const int dims[5] = {kMlpIn, kMlpHidden, kMlpHidden, kMlpHidden, kMlpOut};
+    int64_t off = 0;
+    for (int l = 0; l < 4; ++l) {
+      p.W[l] = base + off;
+      off += (int64_t)dims[l] * dims[l + 1];
+      p.b[l] = base + off;
+      off += dims[l + 1];
+    }
+    return p;
+  }
+};
+
+// Activations of a batch of B rows: A[l] = layer outputs (B x 256, last B x 512), Z[l] =
+// pre-activations of the hidden layers. Workspace floats: B * (3*256*2 + 512).
+struct MLPActs {
+  float* A[4];
+  float* Z[3];
+  static int64_t floats(int64_t B) { return B * (6 * (int64_t)kMlpHidden + kMlpOut); }
+  static MLPActs view(float* base, int64_t B) {
+    MLPActs a;
+    int64_t off = 0;
+    for (int l = 0; l < 3; ++l) { a.A[l] = base + off; off += B * kMlpHidden; }
+    a.A[3] = base + off;
+    off += B * kMlpOut;
+    for (int l = 0; l < 3; ++l) { a.Z[l] = base + off; off += B * kMlpHidden; }
+    return a;
+  }
+};
+
+int sgemm(bool ta, bool tb, int M, int N, int K, const float* A, int lda, const float* B, int ldb, float* C,
+          int ldc, const float* bias, bool gelu, float* Z, float beta, cudaStream_t s);
+int mlp_forward_f32(const MLPParams& P, int B, const float* X, MLPActs& act, cudaStream_t s);
+// gradients into G (same layout as P); work0/work1 hold B x 256 floats each
+int mlp_backward_f32(const MLPParams& P, int B, const float* X, const MLPActs& act, const float* dY, MLPParams& G,
+                     float* work0, float* work1, cudaStream_t s);
+int mse_loss(int64_t n, int B, const float* y, const float* t, float* dy, float* loss, cudaStream_t s);
+int adam_step(int64_t n, float* w, const float* g, float* m, float* v, float lr, int step, cudaStream_t s);
+
+int bf16_linear(int M, int N, int K, const __nv_bfloat16* X, const __nv_bfloat16* Wt, const float* bias, bool gelu,
+                bool outBf16, void* Y, cudaStream_t s);
+int transpose_to_bf16(int K, int N, const float* W, __nv_bfloat16* Wt, cudaStream_t s);
+
+template <typename TIN, typename TOUT>
+int element_features(const BoxNumbering& b, int64_t E, int64_t e0, int64_t count, const int32_t* g2l, const TIN* r,
+                     TOUT* X, float* scale, cudaStream_t s);
+template <typename TV>
+int apply_correction(int Np, int64_t count, int64_t e0, const int32_t* g2l, const float* out, const float* scale,
+                     const double* invDiag, const double* weight, TV* z, cudaStream_t s);
+int training_targets(int Np, int64_t count, const int32_t* elems, const int32_t* g2l, const double* e,
+                     const double* invDiag, const float* scale, float* T, cudaStream_t s);
+int gather_rows(int64_t count, const int32_t* elems, const float* Xall, float* X, cudaStream_t s);
+
+}  // namespace lpg

@@ -134,6 +134,12 @@ __global__ void convert_kernel<double, __nv_bfloat16>(const int64_t N, const dou
   for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x)
     y[n] = __double2bfloat16(x[n]);
 }
+template <>
+__global__ void convert_kernel<float, __nv_bfloat16>(const int64_t N, const float* __restrict__ x,
+                                                     __nv_bfloat16* __restrict__ y) {
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x)
+    y[n] = __float2bfloat16(x[n]);
+}
 template <typename Tin, typename Tout>
 int convert(int64_t N, const Tin* x, Tout* y, cudaStream_t s) {
   if (N <= 0) return LPG_OK;
@@ -182,6 +188,7 @@ template int fill<float>(int64_t, float, float*, cudaStream_t);
 template int convert<double, float>(int64_t, const double*, float*, cudaStream_t);
 template int convert<float, double>(int64_t, const float*, double*, cudaStream_t);
 template int convert<double, __nv_bfloat16>(int64_t, const double*, __nv_bfloat16*, cudaStream_t);
+template int convert<float, __nv_bfloat16>(int64_t, const float*, __nv_bfloat16*, cudaStream_t);
 
 // ---------------------------------------------------------------- reductions
 constexpr int kRedThreads = 512;
