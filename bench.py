@@ -51,6 +51,11 @@ def parse():
     ap.add_argument("--solve", action="store_true", help="time-to-tolerance of the p-MG FPCG solve instead")
     ap.add_argument("--solve-precs", default="FP64,FP32,BF16GEO")
     ap.add_argument("--solve-reps", type=int, default=2)
+    ap.add_argument("--learned", action="store_true", help="learned-smoother training and solve comparison")
+    ap.add_argument("--train-nx", type=int, default=32)
+    ap.add_argument("--train-samples", type=int, default=20000)
+    ap.add_argument("--train-solves", type=int, default=8)
+    ap.add_argument("--train-epochs", type=int, default=40)
     return ap.parse_args()
 
 
@@ -184,12 +189,45 @@ def run_solves(a):
                       % (a.nx, a.N), "results": res}), flush=True)
 
 
+def run_learned(a):
+    """Learned fine smoother (configs[3] of the task): train on (residual, exact error)
+    pairs of the plain p-MG FPCG on a 32^3 jittered box with random Gaussian-bump
+    right-hand sides (lognormal lambda, N=7), then solve the 64^3 problem with the plain
+    FP64, the FP32 and the learned+FP32 preconditioners. One JSON line."""
+    import libparanumal_gb300 as lpg
+    import __graft_entry__ as g
+    g.build()
+    law = {"LAMBDA": 1.0, "LAMBDA FIELD": "LOGNORMAL", "LAMBDA SEED": 2}
+    t0 = time.time()
+    w, hist = lpg.train_smoother(solve_settings(a.train_nx, 7, "FP64", **law), nsolves=a.train_solves,
+                                 samples_per_solve=a.train_samples // a.train_solves, epochs=a.train_epochs,
+                                 batch=250, lr=1e-3, seed=7)
+    t_train = time.time() - t0
+    out = {"workload": "learned fine smoother: train %d^3, solve %d^3 jittered hex N=7 lognormal lambda"
+                       % (a.train_nx, a.nx),
+           "train_seconds": t_train, "train_samples": a.train_samples, "train_epochs": a.train_epochs,
+           "loss_first": float(hist[0]), "loss_last": float(hist[-1]), "results": {}}
+    for name, prec, learned in (("FP64", "FP64", False), ("FP32", "FP32", False), ("learned+FP32", "FP32", True)):
+        e = lpg.Elliptic(solve_settings(a.nx, 7, prec, **law))
+        if learned:
+            e.set_learned_smoother(w, 0.5)
+        runs = [e.Run() for _ in range(a.solve_reps)]
+        best = min(runs, key=lambda r: r["solve_seconds"])
+        out["results"][name] = {"solve_seconds": best["solve_seconds"], "iterations": best["iterations"],
+                                "error_vs_manufactured": best["error"], "converged": best["converged"],
+                                "vcycles": e.info("vcycles"), "fallbacks": e.info("fallbacks")}
+        e.close()
+    print(json.dumps(out), flush=True)
+
+
 def main():
     a = parse()
     if a.impl == "reference":
         return run_reference(a)
     if a.solve:
         return run_solves(a)
+    if a.learned:
+        return run_learned(a)
     import numpy as np
     import torch
     import libparanumal_gb300 as lpg

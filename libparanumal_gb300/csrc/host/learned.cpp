@@ -2,15 +2,18 @@
 // the plain solver, MLP training with the project's own forward/backward/Adam kernels,
 // and inference with BF16 tensor-core tiles.
 //
-// Training samples: random Gaussian-bump right-hand sides b on a training mesh; the
-// exact error e = A^{-1} b of the zero initial guess comes from the plain p-MG FPCG solve
-// to 1e-10; each sampled element contributes (its normalised residual block and face
-// traces, D .* e restricted to it / s_e).
+// Training samples: random Gaussian-bump right-hand sides b on a training mesh. The plain
+// p-MG FPCG solve to 1e-10 gives x*; re-running it for k = 1..3 iterations gives the
+// residual r_k and the exact error e_k = x* - x_k of the plain solver's iterate. Each
+// sampled element contributes (its normalised residual block and face traces of r_k,
+// D .* e_k restricted to it / s_e). Residuals from the iteration are dominated by the
+// high-frequency content a smoother has to remove.
 #include "learned.hpp"
 
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 
 #include "../mlp.hpp"
 
@@ -19,6 +22,7 @@ namespace lpg {
 int LearnedSmoother::load(const float* hostParams, cudaStream_t s) {
   int rc;
   if ((rc = params.alloc(kMlpParams)) || (rc = params.upload(hostParams, kMlpParams, s))) return rc;
+  if ((rc = red.alloc(1)) || (rc = partials.alloc(kReducePartials))) return rc;
   MLPParams P = MLPParams::view(params.p);
   const int dims[5] = {kMlpIn, kMlpHidden, kMlpHidden, kMlpHidden, kMlpOut};
   for (int l = 0; l < 4; ++l) {
@@ -49,11 +53,18 @@ int LearnedSmoother::apply(const BoxNumbering& b, int64_t E, const int32_t* g2l,
   int rc;
   const int64_t C = std::min<int64_t>(E, kChunk);
   if ((rc = ensure_chunk(C))) return rc;
+  // floor of the element scales: kScaleFloor x the global residual RMS
+  if constexpr (std::is_same<T, double>::value) rc = dot(Nglobal, r, r, red.p, partials.p, s);
+  else rc = dot_f32(Nglobal, r, r, red.p, partials.p, s);
+  if (rc) return rc;
+  double rr = 0;
+  if ((rc = red.download(&rr, 1, s))) return rc;
+  const float sfloor = (float)(kScaleFloor * std::sqrt(rr / (double)std::max<int64_t>(Nglobal, 1)));
   LPG_CUDA_TRY(cudaMemsetAsync(z, 0, sizeof(T) * Nglobal, s));
   MLPParams P = MLPParams::view(params.p);
   for (int64_t e0 = 0; e0 < E; e0 += C) {
     const int64_t n = std::min<int64_t>(C, E - e0);
-    if ((rc = element_features<T, __nv_bfloat16>(b, E, e0, n, g2l, r, X.p, scale.p, s))) return rc;
+    if ((rc = element_features<T, __nv_bfloat16>(b, E, e0, n, g2l, r, X.p, scale.p, sfloor, s))) return rc;
     if ((rc = bf16_linear((int)n, kMlpHidden, kMlpIn, X.p, Wt[0].p, P.b[0], true, true, H0.p, s))) return rc;
     if ((rc = bf16_linear((int)n, kMlpHidden, kMlpHidden, H0.p, Wt[1].p, P.b[1], true, true, H1.p, s))) return rc;
     if ((rc = bf16_linear((int)n, kMlpHidden, kMlpHidden, H1.p, Wt[2].p, P.b[2], true, true, H0.p, s))) return rc;
@@ -68,6 +79,8 @@ template int LearnedSmoother::apply<float>(const BoxNumbering&, int64_t, const i
                                            const double*, float*, int64_t, cudaStream_t);
 
 // ---------------------------------------------------------------- training
+double lastKeptFraction = 0;
+
 int train_smoother(Platform* plat, Elliptic* el, Precon* plainMG, const BoxNumbering& b, const TrainOptions& o,
                    std::vector<float>& weights, std::vector<float>& lossHistory) {
   cudaStream_t s = plat->stream;
@@ -83,8 +96,49 @@ int train_smoother(Platform* plat, Elliptic* el, Precon* plainMG, const BoxNumbe
   if ((rc = Xtr.alloc(total * kMlpIn)) || (rc = Ttr.alloc(total * kMlpOut))) return rc;
   DevBuf<float> Xall, scaleAll;
   if ((rc = Xall.alloc(E * kMlpIn)) || (rc = scaleAll.alloc(E))) return rc;
-  DevBuf<double> rhs, x, r;
+  DevBuf<double> rhs, x, r, xstar;
   DevBuf<int32_t> elems;
+  DevBuf<float> Tall;
+  double keptFraction = 0;
+  if ((rc = xstar.alloc(Ng)) || (rc = Tall.alloc(E * kMlpOut))) return rc;
+  // 1D modal low-pass on the GLL nodes: F = V diag(degree <= 3) V^{-1}, V[i][m] = P_m(x_i)
+  DevBuf<double> lowpass;
+  {
+    const int Nq = el->mesh.Nq;
+    const std::vector<double>& xg = el->mesh.r1d;
+    std::vector<double> V(Nq * Nq), Vi(Nq * Nq, 0.0), F(Nq * Nq, 0.0);
+    for (int i = 0; i < Nq; ++i) {
+      double p0 = 1, p1 = xg[i];
+      V[i * Nq + 0] = 1;
+      if (Nq > 1) V[i * Nq + 1] = xg[i];
+      for (int m = 2; m < Nq; ++m) {
+        const double p2 = ((2 * m - 1) * xg[i] * p1 - (m - 1) * p0) / m;
+        V[i * Nq + m] = p2;
+        p0 = p1;
+        p1 = p2;
+      }
+    }
+    // Gauss-Jordan inverse of V (Nq <= 9)
+    std::vector<double> Aug(V);
+    for (int i = 0; i < Nq; ++i) Vi[i * Nq + i] = 1;
+    for (int c = 0; c < Nq; ++c) {
+      int piv = c;
+      for (int r2 = c + 1; r2 < Nq; ++r2)
+        if (std::fabs(Aug[r2 * Nq + c]) > std::fabs(Aug[piv * Nq + c])) piv = r2;
+      for (int j = 0; j < Nq; ++j) { std::swap(Aug[c * Nq + j], Aug[piv * Nq + j]); std::swap(Vi[c * Nq + j], Vi[piv * Nq + j]); }
+      const double d = Aug[c * Nq + c];
+      for (int j = 0; j < Nq; ++j) { Aug[c * Nq + j] /= d; Vi[c * Nq + j] /= d; }
+      for (int r2 = 0; r2 < Nq; ++r2) {
+        if (r2 == c) continue;
+        const double f = Aug[r2 * Nq + c];
+        for (int j = 0; j < Nq; ++j) { Aug[r2 * Nq + j] -= f * Aug[c * Nq + j]; Vi[r2 * Nq + j] -= f * Vi[c * Nq + j]; }
+      }
+    }
+    for (int i = 0; i < Nq; ++i)
+      for (int j = 0; j < Nq; ++j)
+        for (int m = 0; m <= std::min(3, Nq - 1); ++m) F[i * Nq + j] += V[i * Nq + m] * Vi[m * Nq + j];
+    if ((rc = lowpass.alloc(Nq * Nq)) || (rc = lowpass.upload(F.data(), Nq * Nq, s))) return rc;
+  }
   DevBuf<float> scaleSel;
   if ((rc = rhs.alloc(Ng)) || (rc = x.alloc(Ng)) || (rc = r.alloc(Ng)) || (rc = elems.alloc(o.samplesPerSolve)) ||
       (rc = scaleSel.alloc(o.samplesPerSolve)))
@@ -123,26 +177,56 @@ int train_smoother(Platform* plat, Elliptic* el, Precon* plainMG, const BoxNumbe
       if ((rc = el->BuildRhs(pass == 0 ? rhs.p : rhsNeg.p, s))) return rc;
     }
     if ((rc = axpy<double>(Ng, -1.0, rhsNeg.p, 1.0, rhs.p, s))) return rc;
-    // exact error of the zero guess: e = A^{-1} b by the plain p-MG FPCG
-    LPG_CUDA_TRY(cudaMemsetAsync(x.p, 0, sizeof(double) * Ng, s));
+    // converged solution x* of the plain p-MG FPCG
+    LPG_CUDA_TRY(cudaMemsetAsync(xstar.p, 0, sizeof(double) * Ng, s));
     LPG_CUDA_TRY(cudaMemcpyAsync(r.p, rhs.p, sizeof(double) * Ng, cudaMemcpyDeviceToDevice, s));
     PCGResult res;
-    if ((rc = pcg_solve(plat, el, plainMG, work, true, false, x.p, r.p, o.solveTol, 500, res))) return rc;
-    // features of every element for residual b, then a random subset of elements
-    if ((rc = element_features<double, float>(b, E, 0, E, el->g2l.p, rhs.p, Xall.p, scaleAll.p, s))) return rc;
+    if ((rc = pcg_solve(plat, el, plainMG, work, true, false, xstar.p, r.p, o.solveTol, 500, res))) return rc;
+    // a (residual, exact error) pair of the plain solver's trajectory: after k iterations
+    // the residual is r_k and the exact error is x* - x_k (the FPCG run is deterministic)
+    const int kIter = 1 + (sidx % 3);
+    LPG_CUDA_TRY(cudaMemsetAsync(x.p, 0, sizeof(double) * Ng, s));
+    LPG_CUDA_TRY(cudaMemcpyAsync(r.p, rhs.p, sizeof(double) * Ng, cudaMemcpyDeviceToDevice, s));
+    if ((rc = pcg_solve(plat, el, plainMG, work, true, false, x.p, r.p, 0.0, kIter, res))) return rc;
+    if ((rc = axpy<double>(Ng, 1.0, xstar.p, -1.0, x.p, s))) return rc;  // x := x* - x_k
+    // features of every element for residual r_k (scales floored at kScaleFloor x RMS),
+    // then a random subset of the elements whose residual is not negligible
+    double bb;
+    if ((rc = plat->norm2sq(Ng, r.p, bb))) return rc;
+    const double rms = std::sqrt(bb / (double)Ng);
+    if ((rc = element_features<double, float>(b, E, 0, E, el->g2l.p, r.p, Xall.p, scaleAll.p,
+                                              (float)(LearnedSmoother::kScaleFloor * rms), s)))
+      return rc;
+    std::vector<float> scHost(E), sel(o.samplesPerSolve);
+    if ((rc = scaleAll.download(scHost.data(), E, s))) return rc;
+    // targets of every element: the share of the exact error e_k outside the coarse
+    // (degree <= 3) space on each element -- what the fine-level smoother is responsible
+    // for; the remainder is the coarse levels' share
+    if ((rc = highpass_targets(el->mesh.Nq, E, el->g2l.p, x.p, invDiag.p, scaleAll.p, lowpass.p, Tall.p, s))) return rc;
+    std::vector<int32_t> cand;
+    for (int64_t e2 = 0; e2 < E; ++e2)
+      if (scHost[e2] >= 1e-2 * rms) cand.push_back((int32_t)e2);
+    keptFraction += (double)cand.size() / (double)E / o.nsolves;
+    if (cand.empty()) return set_error(LPG_ERR_INVALID, "smoother training: right-hand side is zero");
     std::vector<int32_t> pick(o.samplesPerSolve);
-    for (int i = 0; i < o.samplesPerSolve; ++i) pick[i] = (int32_t)std::min<int64_t>(E - 1, (int64_t)(rng.next() * E));
+    for (int i = 0; i < o.samplesPerSolve; ++i)
+      pick[i] = cand[std::min<size_t>(cand.size() - 1, (size_t)(rng.next() * cand.size()))];
     if ((rc = elems.upload(pick.data(), o.samplesPerSolve, s))) return rc;
     const int64_t base = (int64_t)sidx * o.samplesPerSolve;
     if ((rc = gather_rows(o.samplesPerSolve, elems.p, Xall.p, Xtr.p + base * kMlpIn, s))) return rc;
-    std::vector<float> scHost(E), sel(o.samplesPerSolve);
-    if ((rc = scaleAll.download(scHost.data(), E, s))) return rc;
-    for (int i = 0; i < o.samplesPerSolve; ++i) sel[i] = scHost[pick[i]];
-    if ((rc = scaleSel.upload(sel.data(), o.samplesPerSolve, s))) return rc;
-    if ((rc = training_targets((int)Np, o.samplesPerSolve, elems.p, el->g2l.p, x.p, invDiag.p, scaleSel.p,
-                               Ttr.p + base * kMlpOut, s)))
-      return rc;
+    (void)sel;
+    (void)scaleSel;
+    // rows of the selected elements (the target rows have kMlpOut = 512 entries)
+    {
+      std::vector<float> Th(E * kMlpOut), Ts((int64_t)o.samplesPerSolve * kMlpOut);
+      if ((rc = Tall.download(Th.data(), E * kMlpOut, s))) return rc;
+      for (int i = 0; i < o.samplesPerSolve; ++i)
+        std::memcpy(Ts.data() + (int64_t)i * kMlpOut, Th.data() + (int64_t)pick[i] * kMlpOut, sizeof(float) * kMlpOut);
+      LPG_CUDA_TRY(cudaMemcpyAsync(Ttr.p + base * kMlpOut, Ts.data(), sizeof(float) * Ts.size(), cudaMemcpyHostToDevice, s));
+      LPG_CUDA_TRY(cudaStreamSynchronize(s));
+    }
   }
+  lastKeptFraction = keptFraction;
   // initial parameters: Glorot-uniform weights, zero biases (seeded)
   std::vector<float> w0(kMlpParams, 0.f);
   {

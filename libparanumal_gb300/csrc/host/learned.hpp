@@ -9,7 +9,11 @@ namespace lpg {
 
 struct LearnedSmoother {
   static constexpr int64_t kChunk = 65536;  // elements per inference pass
+  // element scales are floored at this fraction of the global residual RMS, so elements
+  // with (near-)zero residual get small inputs instead of amplified noise
+  static constexpr double kScaleFloor = 1e-3;
   bool ready = false;
+  DevBuf<double> red, partials;
   DevBuf<float> params;                     // FP32 master weights (MLPParams layout)
   DevBuf<__nv_bfloat16> Wt[4];              // BF16 transposed weights for inference
   DevBuf<__nv_bfloat16> X, H0, H1;
@@ -32,7 +36,11 @@ struct TrainOptions {
   int bumps = 8;
   double solveTol = 1e-10;
   uint64_t seed = 7;
+  double targetCap = 4.0;   // keep samples whose RMS normalised target is at most this
 };
+
+// fraction of elements that passed the sample filter in the last training run
+extern double lastKeptFraction;
 
 // Generates (residual, exact error) samples with the plain solver `plainMG` on `el` and
 // trains the network; returns FP32 weights and the per-epoch mean training loss.

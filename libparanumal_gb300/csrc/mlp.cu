@@ -323,7 +323,7 @@ int transpose_to_bf16(int K, int N, const float* W, __nv_bfloat16* Wt, cudaStrea
 template <typename TIN, typename TOUT>
 __global__ void __launch_bounds__(256)
 features_kernel(const BoxNumbering b, const int64_t E, const int64_t e0, const int32_t* __restrict__ g2l,
-                const TIN* __restrict__ r, TOUT* __restrict__ X, float* __restrict__ scale) {
+                const TIN* __restrict__ r, TOUT* __restrict__ X, float* __restrict__ scale, const float sfloor) {
   const int Nq = b.N + 1, Np = Nq * Nq * Nq, Nfp = Nq * Nq;
   const int64_t eb = e0 + blockIdx.x;
   if (eb >= E) return;
@@ -365,7 +365,7 @@ features_kernel(const BoxNumbering b, const int64_t E, const int64_t e0, const i
   if (threadIdx.x == 0) {
     float tot = 0.f;
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += s_red[w];
-    s_red[0] = sqrtf(tot / (float)Np) + 1e-30f;
+    s_red[0] = fmaxf(sqrtf(tot / (float)Np), sfloor) + 1e-30f;
     scale[blockIdx.x] = s_red[0];
   }
   __syncthreads();
@@ -375,20 +375,20 @@ features_kernel(const BoxNumbering b, const int64_t E, const int64_t e0, const i
 
 template <typename TIN, typename TOUT>
 int element_features(const BoxNumbering& b, int64_t E, int64_t e0, int64_t count, const int32_t* g2l, const TIN* r,
-                     TOUT* X, float* scale, cudaStream_t s) {
+                     TOUT* X, float* scale, float sfloor, cudaStream_t s) {
   if ((b.N + 1) * (b.N + 1) * (b.N + 1) + 6 * (b.N + 1) * (b.N + 1) != kMlpIn)
     return set_error(LPG_ERR_UNSUPPORTED, "learned smoother needs N = 7 (896 inputs per element)");
   if (count <= 0) return LPG_OK;
-  features_kernel<TIN, TOUT><<<(unsigned)count, 256, 0, s>>>(b, E, e0, g2l, r, X, scale);
+  features_kernel<TIN, TOUT><<<(unsigned)count, 256, 0, s>>>(b, E, e0, g2l, r, X, scale, sfloor);
   LPG_LAUNCH_CHECK("features_kernel");
   return LPG_OK;
 }
 template int element_features<double, float>(const BoxNumbering&, int64_t, int64_t, int64_t, const int32_t*,
-                                             const double*, float*, float*, cudaStream_t);
+                                             const double*, float*, float*, float, cudaStream_t);
 template int element_features<double, __nv_bfloat16>(const BoxNumbering&, int64_t, int64_t, int64_t, const int32_t*,
-                                                     const double*, __nv_bfloat16*, float*, cudaStream_t);
+                                                     const double*, __nv_bfloat16*, float*, float, cudaStream_t);
 template int element_features<float, __nv_bfloat16>(const BoxNumbering&, int64_t, int64_t, int64_t, const int32_t*,
-                                                    const float*, __nv_bfloat16*, float*, cudaStream_t);
+                                                    const float*, __nv_bfloat16*, float*, float, cudaStream_t);
 
 // z_local = s_e * invDiag * out ; z[g] += weight[g] * z_local (average over copies)
 template <typename TV>
@@ -434,6 +434,56 @@ int training_targets(int Np, int64_t count, const int32_t* elems, const int32_t*
   if (count <= 0) return LPG_OK;
   target_kernel<<<grid_n(count * Np), 256, 0, s>>>(Np, count, elems, g2l, e, invDiag, scale, T);
   LPG_LAUNCH_CHECK("target_kernel");
+  return LPG_OK;
+}
+
+// High-pass training target: the exact error on each element minus its modal projection
+// onto Legendre degrees <= Nc per direction (F = V diag(mask) V^{-1}, applied as three
+// 1D contractions), in network output units: T = (e - F e) / (invDiag s_e).
+__global__ void __launch_bounds__(256)
+highpass_target_kernel(const int Nq, const int32_t* __restrict__ g2l, const double* __restrict__ e,
+                       const double* __restrict__ invDiag, const float* __restrict__ scale,
+                       const double* __restrict__ Fg, float* __restrict__ T) {
+  __shared__ double s_e[kMaxNq * kMaxNq * kMaxNq], s_a[kMaxNq * kMaxNq * kMaxNq], s_b[kMaxNq * kMaxNq * kMaxNq];
+  __shared__ double s_F[kMaxNq * kMaxNq];
+  __shared__ double s_d[kMaxNq * kMaxNq * kMaxNq];
+  const int64_t el = blockIdx.x;
+  const int Np = Nq * Nq * Nq;
+  for (int t = threadIdx.x; t < Nq * Nq; t += blockDim.x) s_F[t] = Fg[t];
+  for (int t = threadIdx.x; t < Np; t += blockDim.x) {
+    const int32_t g = g2l[el * Np + t];
+    s_e[t] = (g >= 0) ? e[g] : 0.0;
+    s_d[t] = (g >= 0) ? 1.0 / invDiag[g] : 0.0;
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < Np; t += blockDim.x) {  // i direction
+    const int i = t % Nq, jk = t / Nq;
+    double r = 0;
+    for (int m = 0; m < Nq; ++m) r += s_F[i * Nq + m] * s_e[jk * Nq + m];
+    s_a[t] = r;
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < Np; t += blockDim.x) {  // j direction
+    const int i = t % Nq, j = (t / Nq) % Nq, k = t / (Nq * Nq);
+    double r = 0;
+    for (int m = 0; m < Nq; ++m) r += s_F[j * Nq + m] * s_a[k * Nq * Nq + m * Nq + i];
+    s_b[t] = r;
+  }
+  __syncthreads();
+  const double inv = 1.0 / (double)scale[el];
+  for (int t = threadIdx.x; t < Np; t += blockDim.x) {  // k direction
+    const int ij = t % (Nq * Nq), k = t / (Nq * Nq);
+    double r = 0;
+    for (int m = 0; m < Nq; ++m) r += s_F[k * Nq + m] * s_b[m * Nq * Nq + ij];
+    T[el * kMlpOut + t] = (float)((s_e[t] - r) * s_d[t] * inv);
+  }
+}
+int highpass_targets(int Nq, int64_t E, const int32_t* g2l, const double* e, const double* invDiag, const float* scale,
+                     const double* F, float* T, cudaStream_t s) {
+  if (E <= 0) return LPG_OK;
+  if (Nq * Nq * Nq != kMlpOut) return set_error(LPG_ERR_UNSUPPORTED, "highpass targets need N = 7");
+  highpass_target_kernel<<<(unsigned)E, 256, 0, s>>>(Nq, g2l, e, invDiag, scale, F, T);
+  LPG_LAUNCH_CHECK("highpass_target_kernel");
   return LPG_OK;
 }
 

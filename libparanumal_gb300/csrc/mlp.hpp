@@ -65,13 +65,17 @@ int bf16_linear(int M, int N, int K, const __nv_bfloat16* X, const __nv_bfloat16
 int transpose_to_bf16(int K, int N, const float* W, __nv_bfloat16* Wt, cudaStream_t s);
 
 template <typename TIN, typename TOUT>
+// scale_e = max(RMS of the element's residual, sfloor); features = values / scale_e
 int element_features(const BoxNumbering& b, int64_t E, int64_t e0, int64_t count, const int32_t* g2l, const TIN* r,
-                     TOUT* X, float* scale, cudaStream_t s);
+                     TOUT* X, float* scale, float sfloor, cudaStream_t s);
 template <typename TV>
 int apply_correction(int Np, int64_t count, int64_t e0, const int32_t* g2l, const float* out, const float* scale,
                      const double* invDiag, const double* weight, TV* z, cudaStream_t s);
 int training_targets(int Np, int64_t count, const int32_t* elems, const int32_t* g2l, const double* e,
                      const double* invDiag, const float* scale, float* T, cudaStream_t s);
 int gather_rows(int64_t count, const int32_t* elems, const float* Xall, float* X, cudaStream_t s);
+// T (E x 512) = (e - F e) / (invDiag s_e) per element, F the 1D modal low-pass (Nq x Nq)
+int highpass_targets(int Nq, int64_t E, const int32_t* g2l, const double* e, const double* invDiag, const float* scale,
+                     const double* F, float* T, cudaStream_t s);
 
 }  // namespace lpg

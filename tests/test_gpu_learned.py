@@ -111,7 +111,8 @@ def test_learned_smoother_solve_with_fallback(trained, prec):
     discretisation error; the V-cycle/fallback counters are consistent. The comparison of
     iterations and fallbacks with the plain method is what the network gains (or not)."""
     w, _ = trained
-    s = learned_problem(10, **{"PRECONDITIONER PRECISION": prec})
+    # tolerance 1e-11 so that the algebraic error stays below the discretisation error
+    s = learned_problem(10, **{"PRECONDITIONER PRECISION": prec, "SOLVER TOLERANCE": 1e-11})
     plain = lpg.Elliptic(s).Run()
     e = lpg.Elliptic(s)
     e.set_learned_smoother(w, 0.5)
