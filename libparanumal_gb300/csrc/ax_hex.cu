@@ -11,6 +11,10 @@
 //     writes AqL, then an ogs Gather kernel re-reads it);
 //   * geometric-factor offsets are 64-bit (the reference's int offsets overflow at 112^3, N=7);
 //   * per-element lambda; FP64, FP32 and BF16-storage variants from one template.
+#include <cstdlib>
+#include <cstring>
+#include <type_traits>
+
 #include "lpg_common.cuh"
 #include "lpg_internal.hpp"
 
@@ -125,8 +129,269 @@ ax_hex_kernel(const int64_t Nelements, const int32_t* __restrict__ elementList,
   }
 }
 
+// ---------------------------------------------------------------- staged variant
+// Persistent CTAs walk groups of EPB elements. Each element's geometric factors (7 x Np)
+// and GlobalToLocal block (Np int32) are copied into a STAGES-deep shared-memory ring
+// with 16-byte cp.async, STAGES-1 groups ahead of the one being computed, so DRAM traffic
+// overlaps the contractions. D's rows and columns needed by a thread live in registers;
+// the t-direction contractions of the whole pencil run once per element (64 FMA each way).
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// Barrier over the NQ*NQ threads of one element (named barrier 1 + el) when that is a
+// whole number of warps, else over the CTA.
+template <int NQ>
+__device__ __forceinline__ void elem_sync(const int el) {
+  if constexpr ((NQ * NQ) % 32 == 0) {
+    asm volatile("bar.sync %0, %1;\n" ::"r"(1 + el), "r"(NQ * NQ) : "memory");
+  } else {
+    __syncthreads();
+  }
+}
+
+template <typename G> __device__ __forceinline__ float geo_to_float(G v);
+template <> __device__ __forceinline__ float geo_to_float<float>(float v) { return v; }
+template <> __device__ __forceinline__ float geo_to_float<__nv_bfloat16>(__nv_bfloat16 v) { return __bfloat162float(v); }
+
+template <int NQ, typename G>
+struct StagedLayout {
+  static constexpr int NP = NQ * NQ * NQ;
+  static constexpr int ROW_BYTES = NP * (int)sizeof(G);
+  static constexpr int GEO_BYTES = 7 * ROW_BYTES;
+  static constexpr int IDX_BYTES = NP * 4;
+  static constexpr int ELEM_BYTES = GEO_BYTES + IDX_BYTES;
+  static constexpr bool ok = (ROW_BYTES % 16 == 0) && (IDX_BYTES % 16 == 0);
+};
+
+// Dot product of NQ coefficients with a shared-memory row: 128-bit loads when the row is
+// 16-byte aligned and NQ is a multiple of 4.
+template <int NQ, bool VEC>
+__device__ __forceinline__ float row_dot(const float* __restrict__ row, const float* c) {
+  float acc = 0.f;
+  if constexpr (VEC) {
+    // two partial sums halve the dependent FMA chain
+    float acc1 = 0.f;
+#pragma unroll
+    for (int m = 0; m < NQ; m += 4) {
+      const float4 v = *reinterpret_cast<const float4*>(row + m);
+      acc += c[m] * v.x;
+      acc1 += c[m + 1] * v.y;
+      acc += c[m + 2] * v.z;
+      acc1 += c[m + 3] * v.w;
+    }
+    acc += acc1;
+  } else {
+#pragma unroll
+    for (int m = 0; m < NQ; ++m) acc += c[m] * row[m];
+  }
+  return acc;
+}
+
+template <int NQ, typename T, typename G, int EPB, int STAGES>
+__global__ void __launch_bounds__(NQ * NQ * EPB)
+ax_hex_staged_kernel(const int64_t Nelements, const int32_t* __restrict__ elementList,
+                     const int32_t* __restrict__ g2l, const G* __restrict__ ggeo, const int64_t geoStride,
+                     const G* __restrict__ wJ, const int64_t wJStride, const T* __restrict__ Dg, const T lambda,
+                     const T* __restrict__ lambdaE, const T* __restrict__ q, T* __restrict__ out) {
+  static_assert(std::is_same<T, float>::value, "staged kernel is FP32");
+  using L = StagedLayout<NQ, G>;
+  constexpr int NP = L::NP, NT = NQ * NQ * EPB;
+  constexpr int CHUNKS = L::ELEM_BYTES / 16;
+  constexpr int STAGE_BYTES = EPB * L::ELEM_BYTES;
+  constexpr bool VEC = (NQ % 4 == 0);
+  constexpr int RS = VEC ? NQ : NQ;          // row stride of s_q / s_Gqr
+  constexpr int TS = VEC ? NQ + 4 : NQ + 1;  // row stride of the transposed copies (bank-conflict padding)
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ __align__(16) float s_D[NQ][NQ];
+  __shared__ __align__(16) float s_q[EPB][NQ][RS];     // s_q[j][i]   = q(i,j,k)
+  __shared__ __align__(16) float s_qT[EPB][NQ][TS];    // s_qT[i][j]  = q(i,j,k)
+  __shared__ __align__(16) float s_Gqr[EPB][NQ][RS];   // s_Gqr[j][i]
+  __shared__ __align__(16) float s_GqsT[EPB][NQ][TS];  // s_GqsT[i][j]
+
+  const int i = threadIdx.x, j = threadIdx.y, el = threadIdx.z;
+  const int tid = i + NQ * (j + NQ * el);
+  for (int t = tid; t < NQ * NQ; t += NT) s_D[t / NQ][t % NQ] = Dg[t];
+  const int64_t ngroups = (Nelements + EPB - 1) / EPB;
+
+  auto issue = [&](const int64_t grp, const int stage) {
+    if (grp < ngroups) {
+      unsigned char* base = smem + stage * STAGE_BYTES;
+      for (int c = tid; c < EPB * CHUNKS; c += NT) {
+        const int le = c / CHUNKS;
+        const int off = (c % CHUNKS) * 16;
+        const int64_t ei = grp * EPB + le;
+        if (ei >= Nelements) continue;
+        const int64_t e = elementList ? (int64_t)elementList[ei] : ei;
+        const unsigned char* src;
+        if (off < L::GEO_BYTES) {
+          const int comp = off / L::ROW_BYTES, within = off % L::ROW_BYTES;
+          src = (comp < 6) ? reinterpret_cast<const unsigned char*>(ggeo + e * geoStride + (int64_t)comp * NP) + within
+                           : reinterpret_cast<const unsigned char*>(wJ + e * wJStride) + within;
+        } else {
+          src = reinterpret_cast<const unsigned char*>(g2l + e * NP) + (off - L::GEO_BYTES);
+        }
+        cp_async16(base + le * L::ELEM_BYTES + off, src);
+      }
+    }
+    cp_async_commit();
+  };
+
+#pragma unroll
+  for (int st = 0; st < STAGES - 1; ++st) issue(blockIdx.x + (int64_t)st * gridDim.x, st);
+  __syncthreads();
+  float Dr[NQ], Ds[NQ], DTi[NQ], DTj[NQ];
+#pragma unroll
+  for (int m = 0; m < NQ; ++m) {
+    Dr[m] = s_D[i][m];
+    Ds[m] = s_D[j][m];
+    DTi[m] = s_D[m][i];
+    DTj[m] = s_D[m][j];
+  }
+
+  for (int64_t it = 0;; ++it) {
+    const int64_t grp = blockIdx.x + it * gridDim.x;
+    if (grp >= ngroups) break;
+    issue(grp + (int64_t)(STAGES - 1) * gridDim.x, (int)((it + STAGES - 1) % STAGES));
+    cp_async_wait<STAGES - 1>();
+    __syncthreads();
+    const unsigned char* base = smem + (it % STAGES) * STAGE_BYTES + el * L::ELEM_BYTES;
+    const G* sg = reinterpret_cast<const G*>(base);
+    const int32_t* sidx = reinterpret_cast<const int32_t*>(base + L::GEO_BYTES);
+    const int64_t ei = grp * EPB + el;
+    const bool active = ei < Nelements;
+    const int64_t e = active ? (elementList ? (int64_t)elementList[ei] : ei) : 0;
+    const int node = j * NQ + i;
+
+    float r_q[NQ], r_Aq[NQ], qt[NQ], Gqt[NQ];
+    int32_t r_id[NQ];
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) {
+      const int32_t id = active ? sidx[k * NQ * NQ + node] : -1;
+      r_id[k] = id;
+      r_q[k] = (id >= 0) ? q[id] : 0.f;
+    }
+    const float lam = (lambdaE && active) ? lambdaE[e] : lambda;
+    // t-direction of the pencil: qt = D r_q (rows of D are broadcast reads)
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) qt[k] = row_dot<NQ, VEC>(&s_D[k][0], r_q);
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) {
+      const int off = k * NQ * NQ + node;
+      const float G00 = geo_to_float(sg[0 * NP + off]), G01 = geo_to_float(sg[1 * NP + off]);
+      const float G02 = geo_to_float(sg[2 * NP + off]), G11 = geo_to_float(sg[3 * NP + off]);
+      const float G12 = geo_to_float(sg[4 * NP + off]), G22 = geo_to_float(sg[5 * NP + off]);
+      const float GwJ = geo_to_float(sg[6 * NP + off]);
+      s_q[el][j][i] = r_q[k];
+      s_qT[el][i][j] = r_q[k];
+      elem_sync<NQ>(el);
+      const float qr = row_dot<NQ, VEC>(&s_q[el][j][0], Dr);    // sum_m D[i][m] q(m,j)
+      const float qs = row_dot<NQ, VEC>(&s_qT[el][i][0], Ds);   // sum_m D[j][m] q(i,m)
+      s_GqsT[el][i][j] = G01 * qr + G11 * qs + G12 * qt[k];
+      s_Gqr[el][j][i] = G00 * qr + G01 * qs + G02 * qt[k];
+      Gqt[k] = G02 * qr + G12 * qs + G22 * qt[k];
+      float Auk = GwJ * lam * r_q[k];
+      elem_sync<NQ>(el);
+      Auk += row_dot<NQ, VEC>(&s_GqsT[el][i][0], DTj);          // sum_m D[m][j] Gqs(i,m)
+      Auk += row_dot<NQ, VEC>(&s_Gqr[el][j][0], DTi);           // sum_m D[m][i] Gqr(m,j)
+      r_Aq[k] = Auk;
+      elem_sync<NQ>(el);
+    }
+    // transposed t-direction: r_Aq[m] += sum_k D[k][m] Gqt[k]
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) {
+#pragma unroll
+      for (int m = 0; m < NQ; m += (VEC ? 4 : 1)) {
+        if constexpr (VEC) {
+          const float4 d = *reinterpret_cast<const float4*>(&s_D[k][m]);
+          r_Aq[m] += d.x * Gqt[k];
+          r_Aq[m + 1] += d.y * Gqt[k];
+          r_Aq[m + 2] += d.z * Gqt[k];
+          r_Aq[m + 3] += d.w * Gqt[k];
+        } else {
+          r_Aq[m] += s_D[k][m] * Gqt[k];
+        }
+      }
+    }
+    if (active) {
+#pragma unroll
+      for (int k = 0; k < NQ; ++k)
+        if (r_id[k] >= 0) atomicAdd(out + r_id[k], r_Aq[k]);
+    }
+  }
+  cp_async_wait<0>();
+}
+
+template <int NQ, typename T, typename G, int EPB, int STAGES>
+static int launch_staged(const AxArgs<T, G>& a, cudaStream_t s) {
+  using L = StagedLayout<NQ, G>;
+  constexpr int smem = STAGES * EPB * L::ELEM_BYTES;
+  static int configured = -1;   // per instantiation: dynamic shared memory opt-in
+  static int ctasPerSM = 1;
+  static int numSMs = 152;
+  auto kern = ax_hex_staged_kernel<NQ, T, G, EPB, STAGES>;
+  if (configured < 0) {
+    LPG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    int dev = 0;
+    LPG_CUDA_TRY(cudaGetDevice(&dev));
+    LPG_CUDA_TRY(cudaDeviceGetAttribute(&numSMs, cudaDevAttrMultiProcessorCount, dev));
+    LPG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctasPerSM, kern, NQ * NQ * EPB, smem));
+    if (ctasPerSM < 1) return set_error(LPG_ERR_UNSUPPORTED, "staged Ax: kernel does not fit on an SM");
+    configured = 1;
+  }
+  const int64_t groups = (a.Nelements + EPB - 1) / EPB;
+  const int64_t grid = std::min<int64_t>(groups, (int64_t)numSMs * ctasPerSM);
+  if (grid <= 0) return LPG_OK;
+  kern<<<(unsigned)grid, dim3(NQ, NQ, EPB), smem, s>>>(a.Nelements, a.elementList, a.g2l, a.ggeo, a.geoStride, a.wJ,
+                                                        a.wJStride, a.D, a.lambda, a.lambdaE, a.q, a.out);
+  LPG_LAUNCH_CHECK("ax_hex_staged_kernel");
+  return LPG_OK;
+}
+
+static int staged_variant() {
+  static int v = -2;
+  if (v == -2) {
+    const char* e = std::getenv("LPG_AX_STAGED");
+    v = -1;
+    if (e) {
+      if (!std::strcmp(e, "off")) v = 0;
+      else if (!std::strcmp(e, "2x2")) v = 22;
+      else if (!std::strcmp(e, "2x3")) v = 23;
+      else if (!std::strcmp(e, "4x2")) v = 42;
+      else if (!std::strcmp(e, "4x3")) v = 43;
+    }
+  }
+  return v;
+}
+
+// the staged kernel needs 16-byte aligned rows (even Nq) and aligned strides/pointers
+template <int NQ, typename T, typename G>
+static bool staged_ok(const AxArgs<T, G>& a) {
+  using L = StagedLayout<NQ, G>;
+  if (!L::ok) return false;
+  auto al = [](const void* p) { return ((uintptr_t)p & 15) == 0; };
+  return al(a.ggeo) && al(a.wJ) && al(a.g2l) && ((a.geoStride * (int64_t)sizeof(G)) % 16 == 0) &&
+         ((a.wJStride * (int64_t)sizeof(G)) % 16 == 0);
+}
+
 template <int NQ, typename T, typename G, int INMODE, int OUTMODE>
 static int launch_ax(const AxArgs<T, G>& a, cudaStream_t s) {
+  if constexpr (std::is_same<T, float>::value && INMODE == IN_GATHER && OUTMODE == OUT_ASSEMBLE) {
+    if (staged_ok<NQ, T, G>(a)) {
+      // LPG_AX_STAGED = off | EPBxSTAGES (2x2, 2x3, 4x2, 4x3): tuning override
+      const int v = staged_variant();
+      if (v == 0) { /* fall through to the unstaged kernel */ }
+      else if (v == 22) return launch_staged<NQ, T, G, 2, 2>(a, s);
+      else if (v == 23) return launch_staged<NQ, T, G, 2, 3>(a, s);
+      else if (v == 43) return launch_staged<NQ, T, G, 4, 3>(a, s);
+      else if (v == 42) return launch_staged<NQ, T, G, 4, 2>(a, s);
+      else return launch_staged<NQ, T, G, 2, 2>(a, s);  // measured best for FP32 and BF16 geometry at N=7
+    }
+  }
   constexpr int EPB = elems_per_block<NQ>();
   if (a.Nelements <= 0) return LPG_OK;
   const int64_t blocks = (a.Nelements + EPB - 1) / EPB;
