@@ -208,34 +208,40 @@ ax_hex_staged_kernel(const int64_t Nelements, const int32_t* __restrict__ elemen
   constexpr int TS = VEC ? NQ + 4 : NQ + 1;  // row stride of the transposed copies (bank-conflict padding)
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ __align__(16) float s_D[NQ][NQ];
-  __shared__ __align__(16) float s_q[EPB][NQ][RS];     // s_q[j][i]   = q(i,j,k)
-  __shared__ __align__(16) float s_qT[EPB][NQ][TS];    // s_qT[i][j]  = q(i,j,k)
-  __shared__ __align__(16) float s_Gqr[EPB][NQ][RS];   // s_Gqr[j][i]
-  __shared__ __align__(16) float s_GqsT[EPB][NQ][TS];  // s_GqsT[i][j]
+  // layer slabs, double-buffered by layer parity so one barrier per layer suffices
+  // between reading a slab and overwriting it two layers later
+  __shared__ __align__(16) float s_q[2][EPB][NQ][RS];     // s_q[j][i]   = q(i,j,k)
+  __shared__ __align__(16) float s_qT[2][EPB][NQ][TS];    // s_qT[i][j]  = q(i,j,k)
+  __shared__ __align__(16) float s_Gqr[2][EPB][NQ][RS];   // s_Gqr[j][i]
+  __shared__ __align__(16) float s_GqsT[2][EPB][NQ][TS];  // s_GqsT[i][j]
 
   const int i = threadIdx.x, j = threadIdx.y, el = threadIdx.z;
   const int tid = i + NQ * (j + NQ * el);
   for (int t = tid; t < NQ * NQ; t += NT) s_D[t / NQ][t % NQ] = Dg[t];
   const int64_t ngroups = (Nelements + EPB - 1) / EPB;
 
+  // copy of one element group: 7 geometric-factor rows and the index row per element,
+  // each a contiguous run of 16-byte chunks (compile-time trip counts)
+  constexpr int ROW_CHUNKS = L::ROW_BYTES / 16, IDX_CHUNKS = L::IDX_BYTES / 16;
   auto issue = [&](const int64_t grp, const int stage) {
     if (grp < ngroups) {
       unsigned char* base = smem + stage * STAGE_BYTES;
-      for (int c = tid; c < EPB * CHUNKS; c += NT) {
-        const int le = c / CHUNKS;
-        const int off = (c % CHUNKS) * 16;
+#pragma unroll
+      for (int le = 0; le < EPB; ++le) {
         const int64_t ei = grp * EPB + le;
-        if (ei >= Nelements) continue;
-        const int64_t e = elementList ? (int64_t)elementList[ei] : ei;
-        const unsigned char* src;
-        if (off < L::GEO_BYTES) {
-          const int comp = off / L::ROW_BYTES, within = off % L::ROW_BYTES;
-          src = (comp < 6) ? reinterpret_cast<const unsigned char*>(ggeo + e * geoStride + (int64_t)comp * NP) + within
-                           : reinterpret_cast<const unsigned char*>(wJ + e * wJStride) + within;
-        } else {
-          src = reinterpret_cast<const unsigned char*>(g2l + e * NP) + (off - L::GEO_BYTES);
+        if (ei < Nelements) {
+          const int64_t e = elementList ? (int64_t)elementList[ei] : ei;
+          unsigned char* dst = base + le * L::ELEM_BYTES;
+#pragma unroll
+          for (int comp = 0; comp < 7; ++comp) {
+            const unsigned char* src =
+                (comp < 6) ? reinterpret_cast<const unsigned char*>(ggeo + e * geoStride + (int64_t)comp * NP)
+                           : reinterpret_cast<const unsigned char*>(wJ + e * wJStride);
+            for (int c = tid; c < ROW_CHUNKS; c += NT) cp_async16(dst + comp * L::ROW_BYTES + c * 16, src + c * 16);
+          }
+          const unsigned char* srci = reinterpret_cast<const unsigned char*>(g2l + e * NP);
+          for (int c = tid; c < IDX_CHUNKS; c += NT) cp_async16(dst + L::GEO_BYTES + c * 16, srci + c * 16);
         }
-        cp_async16(base + le * L::ELEM_BYTES + off, src);
       }
     }
     cp_async_commit();
@@ -286,20 +292,20 @@ ax_hex_staged_kernel(const int64_t Nelements, const int32_t* __restrict__ elemen
       const float G02 = geo_to_float(sg[2 * NP + off]), G11 = geo_to_float(sg[3 * NP + off]);
       const float G12 = geo_to_float(sg[4 * NP + off]), G22 = geo_to_float(sg[5 * NP + off]);
       const float GwJ = geo_to_float(sg[6 * NP + off]);
-      s_q[el][j][i] = r_q[k];
-      s_qT[el][i][j] = r_q[k];
+      const int b = k & 1;
+      s_q[b][el][j][i] = r_q[k];
+      s_qT[b][el][i][j] = r_q[k];
       elem_sync<NQ>(el);
-      const float qr = row_dot<NQ, VEC>(&s_q[el][j][0], Dr);    // sum_m D[i][m] q(m,j)
-      const float qs = row_dot<NQ, VEC>(&s_qT[el][i][0], Ds);   // sum_m D[j][m] q(i,m)
-      s_GqsT[el][i][j] = G01 * qr + G11 * qs + G12 * qt[k];
-      s_Gqr[el][j][i] = G00 * qr + G01 * qs + G02 * qt[k];
+      const float qr = row_dot<NQ, VEC>(&s_q[b][el][j][0], Dr);    // sum_m D[i][m] q(m,j)
+      const float qs = row_dot<NQ, VEC>(&s_qT[b][el][i][0], Ds);   // sum_m D[j][m] q(i,m)
+      s_GqsT[b][el][i][j] = G01 * qr + G11 * qs + G12 * qt[k];
+      s_Gqr[b][el][j][i] = G00 * qr + G01 * qs + G02 * qt[k];
       Gqt[k] = G02 * qr + G12 * qs + G22 * qt[k];
       float Auk = GwJ * lam * r_q[k];
       elem_sync<NQ>(el);
-      Auk += row_dot<NQ, VEC>(&s_GqsT[el][i][0], DTj);          // sum_m D[m][j] Gqs(i,m)
-      Auk += row_dot<NQ, VEC>(&s_Gqr[el][j][0], DTi);           // sum_m D[m][i] Gqr(m,j)
+      Auk += row_dot<NQ, VEC>(&s_GqsT[b][el][i][0], DTj);       // sum_m D[m][j] Gqs(i,m)
+      Auk += row_dot<NQ, VEC>(&s_Gqr[b][el][j][0], DTi);        // sum_m D[m][i] Gqr(m,j)
       r_Aq[k] = Auk;
-      elem_sync<NQ>(el);
     }
     // transposed t-direction: r_Aq[m] += sum_k D[k][m] Gqt[k]
 #pragma unroll
