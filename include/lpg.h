@@ -140,6 +140,7 @@ int lpg_elliptic_destroy(lpg_elliptic *e);
 #define LPG_INFO_DEVICE_BYTES 9
 #define LPG_INFO_VCYCLES 10        /* V-cycles run with the learned fine smoother */
 #define LPG_INFO_FALLBACKS 11      /* of those, redone with the plain smoother */
+#define LPG_INFO_HOST_CHUNKS 12    /* element chunks of the host-buffer operator (0 before its first call) */
 int64_t lpg_elliptic_info(const lpg_elliptic *e, int what);
 
 /* Copy a named setup array to host memory: "GlobalToLocal" (int32), "ownerLocal" (int32),
@@ -162,6 +163,17 @@ int lpg_elliptic_operator(lpg_elliptic *e, const double *q, double *Aq, void *st
  * geometric factors, FP32 arithmetic. The reduced-precision copies of the geometric
  * factors are made on first use. */
 int lpg_elliptic_operator_f32(lpg_elliptic *e, const float *q, float *Aq, int bf16geo, void *stream);
+/* elliptic_t::Operator (ellipticOperator.cpp:29-106) on HOST arrays, as the OCCA Serial
+ * backend's operator takes them: Aq_host = A q_host (Nglobal entries each), returning
+ * when Aq_host is filled. The upload of q, the operator and the download of Aq are
+ * pipelined over element chunks on the object's stream and two copy streams; overlap
+ * needs page-locked buffers (pageable ones give the same result, copied serially).
+ * Device work vectors are allocated on the first call. Calls on one object must not
+ * overlap. */
+int lpg_elliptic_operator_host(lpg_elliptic *e, const double *q_host, double *Aq_host);
+/* The same with FP32 vectors and FP32 (bf16geo = 0) or BF16 (bf16geo = 1) geometric
+ * factors (no reference counterpart). */
+int lpg_elliptic_operator_host_f32(lpg_elliptic *e, const float *q_host, float *Aq_host, int bf16geo);
 /* precon_t::Operator (include/precon.hpp:36-56): z = M^{-1} r, device pointers. */
 int lpg_elliptic_precon(lpg_elliptic *e, const double *r, double *z, void *stream);
 /* elliptic_t::Solve (ellipticSolve.cpp:29-39): (F)PCG on device vectors x (initial

@@ -19,7 +19,7 @@ LPG_OK = 0
 STATUS = {0: "OK", -1: "INVALID", -2: "CUDA", -3: "UNSUPPORTED", -4: "NOT_CONVERGED",
           -5: "ALLOC", -6: "SETTINGS", -7: "BREAKDOWN"}
 INFO = dict(nelements=0, np=1, nglobal=2, nlocal=3, n=4, allneumann=5, mg_plevels=6,
-            mg_amglevels=7, coarse_n=8, device_bytes=9, vcycles=10, fallbacks=11)
+            mg_amglevels=7, coarse_n=8, device_bytes=9, vcycles=10, fallbacks=11, host_chunks=12)
 
 _lib = None
 
@@ -71,6 +71,8 @@ def lib():
         "lpg_elliptic_random_vector": [vp, ctypes.c_uint64, vp, vp],
         "lpg_elliptic_operator": [vp, vp, vp, vp],
         "lpg_elliptic_operator_f32": [vp, vp, vp, i32, vp],
+        "lpg_elliptic_operator_host": [vp, vp, vp],
+        "lpg_elliptic_operator_host_f32": [vp, vp, vp, i32],
         "lpg_elliptic_precon": [vp, vp, vp, vp],
         "lpg_elliptic_solve": [vp, vp, vp, f64, i32, ctypes.POINTER(ctypes.c_int)],
         "lpg_elliptic_rhs": [vp, vp, vp],
@@ -125,6 +127,21 @@ def _ptr(x):
         return None
     if isinstance(x, int):
         return x
+    return x.data_ptr()
+
+
+def _host_ptr(x, dtype, n, writable=False):
+    """Address of a contiguous host array of n entries of dtype (numpy or CPU tensor)."""
+    if isinstance(x, np.ndarray):
+        if x.dtype != np.dtype(dtype) or not x.flags["C_CONTIGUOUS"] or x.size != n:
+            raise ValueError("host array must be contiguous %s of %d entries" % (dtype, n))
+        if writable and not x.flags["WRITEABLE"]:
+            raise ValueError("output array is read-only")
+        return x.ctypes.data
+    import torch
+    if (not isinstance(x, torch.Tensor) or x.is_cuda or str(x.dtype) != "torch." + dtype
+            or not x.is_contiguous() or x.numel() != n):
+        raise ValueError("host tensor must be a contiguous CPU %s tensor of %d entries" % (dtype, n))
     return x.data_ptr()
 
 
@@ -190,6 +207,19 @@ class Elliptic:
         """Reduced-precision operator (FP32 vectors; FP32 or BF16 geometric factors)."""
         check(lib().lpg_elliptic_operator_f32(self.h, _ptr(q), _ptr(Aq), 1 if bf16geo else 0,
                                               stream or None))
+
+    def OperatorHost(self, q, Aq, precision="FP64"):
+        """Aq = A q on host arrays (numpy arrays or CPU tensors of Nglobal entries: float64
+        for FP64, float32 for FP32 and BF16GEO). Upload, operator and download are pipelined
+        over element chunks; page-locked (pinned) tensors are needed for the overlap."""
+        dt = "float64" if precision == "FP64" else "float32"
+        pq, pa = _host_ptr(q, dt, self.Nglobal), _host_ptr(Aq, dt, self.Nglobal, writable=True)
+        if precision == "FP64":
+            check(lib().lpg_elliptic_operator_host(self.h, pq, pa))
+        elif precision in ("FP32", "BF16GEO"):
+            check(lib().lpg_elliptic_operator_host_f32(self.h, pq, pa, 1 if precision == "BF16GEO" else 0))
+        else:
+            raise ValueError("precision must be FP64, FP32 or BF16GEO")
 
     def precon(self, r, z, stream=0):
         check(lib().lpg_elliptic_precon(self.h, _ptr(r), _ptr(z), stream or None))

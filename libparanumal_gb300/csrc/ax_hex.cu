@@ -262,9 +262,11 @@ ax_hex_staged_kernel(const int64_t Nelements, const int32_t* __restrict__ elemen
   for (int64_t it = 0;; ++it) {
     const int64_t grp = blockIdx.x + it * gridDim.x;
     if (grp >= ngroups) break;
-    issue(grp + (int64_t)(STAGES - 1) * gridDim.x, (int)((it + STAGES - 1) % STAGES));
-    cp_async_wait<STAGES - 1>();
+    // this group's copies are complete, and after the barrier no thread still reads the
+    // stage of the previous group, which the next copy then refills
+    cp_async_wait<STAGES - 2>();
     __syncthreads();
+    issue(grp + (int64_t)(STAGES - 1) * gridDim.x, (int)((it + STAGES - 1) % STAGES));
     const unsigned char* base = smem + (it % STAGES) * STAGE_BYTES + el * L::ELEM_BYTES;
     const G* sg = reinterpret_cast<const G*>(base);
     const int32_t* sidx = reinterpret_cast<const int32_t*>(base + L::GEO_BYTES);

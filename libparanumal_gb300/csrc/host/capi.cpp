@@ -274,6 +274,7 @@ extern "C" int64_t lpg_elliptic_info(const lpg_elliptic* e, int what) {
     case LPG_INFO_DEVICE_BYTES: return device_bytes_in_use();
     case LPG_INFO_VCYCLES: return e->precon ? e->precon->vcycles() : 0;
     case LPG_INFO_FALLBACKS: return e->precon ? e->precon->fallbacks() : 0;
+    case LPG_INFO_HOST_CHUNKS: return e->el->pipe ? e->el->pipe->K : 0;
     default: return -1;
   }
 }
@@ -375,6 +376,23 @@ extern "C" int lpg_elliptic_operator_f32(lpg_elliptic* e, const float* q, float*
   int rc = e->el->make_f32(bf16geo != 0, s);
   if (rc) return rc;
   return e->el->OperatorF32(q, Aq, bf16geo ? Prec::BF16G : Prec::F32, s);
+  LPG_GUARD_END
+}
+
+extern "C" int lpg_elliptic_operator_host(lpg_elliptic* e, const double* q_host, double* Aq_host) {
+  if (!e || !q_host || !Aq_host) return set_error(LPG_ERR_INVALID, "null argument");
+  LPG_GUARD_BEGIN
+  return e->el->OperatorHost(q_host, Aq_host, e->plat.stream);
+  LPG_GUARD_END
+}
+
+extern "C" int lpg_elliptic_operator_host_f32(lpg_elliptic* e, const float* q_host, float* Aq_host, int bf16geo) {
+  if (!e || !q_host || !Aq_host) return set_error(LPG_ERR_INVALID, "null argument");
+  LPG_GUARD_BEGIN
+  cudaStream_t s = e->plat.stream;
+  int rc = e->el->make_f32(bf16geo != 0, s);
+  if (rc) return rc;
+  return e->el->OperatorHostF32(q_host, Aq_host, bf16geo ? Prec::BF16G : Prec::F32, s);
   LPG_GUARD_END
 }
 

@@ -194,6 +194,146 @@ int Elliptic::OperatorF32(const float* q, float* Aq, Prec prec, cudaStream_t s) 
   return ax_hex<float, float>(a, AxMode::Assemble, s);
 }
 
+// ---------------------------------------------------------------- host-buffer operator
+HostPipe::~HostPipe() {
+  for (cudaEvent_t ev : inReady) cudaEventDestroy(ev);
+  for (cudaEvent_t ev : chunkDone) cudaEventDestroy(ev);
+  if (h2d) cudaStreamDestroy(h2d);
+  if (d2h) cudaStreamDestroy(d2h);
+}
+
+int Elliptic::BuildPipe(cudaStream_t s) {
+  if (pipe) return LPG_OK;
+  auto p = std::make_unique<HostPipe>();
+  const int64_t E = mesh.E;
+  // at most 32 chunks of at least 4096 elements (a chunk still fills every SM)
+  p->K = (int)std::max<int64_t>(1, std::min<int64_t>(32, E / 4096));
+  const int K = p->K;
+  p->e0.resize(K + 1);
+  for (int c = 0; c <= K; ++c) p->e0[c] = E * c / K;
+  std::vector<int32_t> lo(std::max<int64_t>(E, 1)), hi(std::max<int64_t>(E, 1));
+  if (E > 0) {
+    DevBuf<int32_t> dlo, dhi;
+    int rc;
+    if ((rc = dlo.alloc(E)) || (rc = dhi.alloc(E))) return rc;
+    if ((rc = element_dof_range(mesh.N, E, g2l.p, dlo.p, dhi.p, s))) return rc;
+    LPG_CUDA_TRY(cudaMemcpyAsync(lo.data(), dlo.p, sizeof(int32_t) * E, cudaMemcpyDeviceToHost, s));
+    LPG_CUDA_TRY(cudaMemcpyAsync(hi.data(), dhi.p, sizeof(int32_t) * E, cudaMemcpyDeviceToHost, s));
+    LPG_CUDA_TRY(cudaStreamSynchronize(s));
+  }
+  p->inEnd.assign(K, 0);
+  p->outEnd.assign(K, Nglobal);
+  int64_t need = 0;
+  for (int c = 0; c < K; ++c) {
+    for (int64_t e = p->e0[c]; e < p->e0[c + 1]; ++e) need = std::max<int64_t>(need, (int64_t)hi[e] + 1);
+    p->inEnd[c] = std::min<int64_t>(need, Nglobal);
+  }
+  p->inEnd[K - 1] = Nglobal;
+  int64_t first = Nglobal;   // smallest entry touched by chunks c+1..K-1
+  for (int c = K - 1; c >= 0; --c) {
+    p->outEnd[c] = first;
+    for (int64_t e = p->e0[c]; e < p->e0[c + 1]; ++e) first = std::min<int64_t>(first, (int64_t)lo[e]);
+  }
+  LPG_CUDA_TRY(cudaStreamCreateWithFlags(&p->h2d, cudaStreamNonBlocking));
+  LPG_CUDA_TRY(cudaStreamCreateWithFlags(&p->d2h, cudaStreamNonBlocking));
+  p->inReady.assign(K, nullptr);
+  p->chunkDone.assign(K, nullptr);
+  for (int c = 0; c < K; ++c) {
+    LPG_CUDA_TRY(cudaEventCreateWithFlags(&p->inReady[c], cudaEventDisableTiming));
+    LPG_CUDA_TRY(cudaEventCreateWithFlags(&p->chunkDone[c], cudaEventDisableTiming));
+  }
+  pipe = std::move(p);
+  return LPG_OK;
+}
+
+// Upload pieces of q on the h2d stream, one operator launch per element chunk on s
+// (each waits for the piece it reads), download each final prefix of Aq on d2h.
+template <typename T, typename Launch>
+static int run_pipe(HostPipe& p, const T* qh, T* Aqh, T* dq, T* dAq, int64_t Nglobal, cudaStream_t s,
+                    Launch&& launch) {
+  auto body = [&]() -> int {
+    LPG_CUDA_TRY(cudaMemsetAsync(dAq, 0, sizeof(T) * Nglobal, s));
+    int64_t up = 0;
+    for (int c = 0; c < p.K; ++c) {
+      const int64_t end = p.inEnd[c];
+      if (end > up)
+        LPG_CUDA_TRY(cudaMemcpyAsync(dq + up, qh + up, sizeof(T) * (end - up), cudaMemcpyHostToDevice, p.h2d));
+      up = std::max(up, end);
+      LPG_CUDA_TRY(cudaEventRecord(p.inReady[c], p.h2d));
+    }
+    int64_t down = 0;
+    for (int c = 0; c < p.K; ++c) {
+      LPG_CUDA_TRY(cudaStreamWaitEvent(s, p.inReady[c], 0));
+      const int rc = launch(p.e0[c], p.e0[c + 1]);
+      if (rc) return rc;
+      LPG_CUDA_TRY(cudaEventRecord(p.chunkDone[c], s));
+      const int64_t end = p.outEnd[c];
+      if (end > down) {
+        LPG_CUDA_TRY(cudaStreamWaitEvent(p.d2h, p.chunkDone[c], 0));
+        LPG_CUDA_TRY(cudaMemcpyAsync(Aqh + down, dAq + down, sizeof(T) * (end - down), cudaMemcpyDeviceToHost,
+                                     p.d2h));
+        down = end;
+      }
+    }
+    return LPG_OK;
+  };
+  const int rc = body();
+  // nothing may still be copying into or out of the caller's buffers on return
+  const cudaError_t e1 = cudaStreamSynchronize(p.h2d);
+  const cudaError_t e2 = cudaStreamSynchronize(s);
+  const cudaError_t e3 = cudaStreamSynchronize(p.d2h);
+  if (rc) return rc;
+  if (e1 != cudaSuccess) return cuda_status(e1, "host operator: upload");
+  if (e2 != cudaSuccess) return cuda_status(e2, "host operator: operator");
+  if (e3 != cudaSuccess) return cuda_status(e3, "host operator: download");
+  return LPG_OK;
+}
+
+int Elliptic::OperatorHost(const double* qHost, double* AqHost, cudaStream_t s) {
+  int rc;
+  if ((rc = BuildPipe(s))) return rc;
+  if (!pipe->Aq.p && ((rc = pipe->q.alloc(std::max<int64_t>(Nglobal, 1))) ||
+                      (rc = pipe->Aq.alloc(std::max<int64_t>(Nglobal, 1)))))
+    return rc;
+  const int64_t Np = mesh.Np;
+  auto launch = [&](int64_t a0, int64_t a1) {
+    AxArgs<double, double> a;
+    a.N = mesh.N; a.Nelements = a1 - a0; a.g2l = g2l.p + a0 * Np;
+    a.ggeo = mesh.geo.p + a0 * 7 * Np; a.geoStride = 7 * Np; a.wJ = a.ggeo + 6 * Np; a.wJStride = 7 * Np;
+    a.D = mesh.D_d.p; a.lambda = lambda; a.lambdaE = hasLambdaE ? lambdaE.p + a0 : nullptr;
+    a.q = pipe->q.p; a.out = pipe->Aq.p; a.Nglobal = Nglobal;
+    return ax_hex<double, double>(a, AxMode::AccumulateAssembled, s);
+  };
+  return run_pipe<double>(*pipe, qHost, AqHost, pipe->q.p, pipe->Aq.p, Nglobal, s, launch);
+}
+
+int Elliptic::OperatorHostF32(const float* qHost, float* AqHost, Prec prec, cudaStream_t s) {
+  int rc;
+  if ((rc = BuildPipe(s))) return rc;
+  if (!pipe->Aq32.p && ((rc = pipe->q32.alloc(std::max<int64_t>(Nglobal, 1))) ||
+                        (rc = pipe->Aq32.alloc(std::max<int64_t>(Nglobal, 1)))))
+    return rc;
+  const int64_t Np = mesh.Np;
+  auto launch = [&](int64_t a0, int64_t a1) {
+    const float* lam = hasLambdaE ? lambdaE32.p + a0 : nullptr;
+    if (prec == Prec::BF16G) {
+      AxArgs<float, __nv_bfloat16> a;
+      a.N = mesh.N; a.Nelements = a1 - a0; a.g2l = g2l.p + a0 * Np;
+      a.ggeo = mesh.geo16.p + a0 * 7 * Np; a.geoStride = 7 * Np; a.wJ = a.ggeo + 6 * Np; a.wJStride = 7 * Np;
+      a.D = mesh.D32.p; a.lambda = (float)lambda; a.lambdaE = lam;
+      a.q = pipe->q32.p; a.out = pipe->Aq32.p; a.Nglobal = Nglobal;
+      return ax_hex<float, __nv_bfloat16>(a, AxMode::AccumulateAssembled, s);
+    }
+    AxArgs<float, float> a;
+    a.N = mesh.N; a.Nelements = a1 - a0; a.g2l = g2l.p + a0 * Np;
+    a.ggeo = mesh.geo32.p + a0 * 7 * Np; a.geoStride = 7 * Np; a.wJ = a.ggeo + 6 * Np; a.wJStride = 7 * Np;
+    a.D = mesh.D32.p; a.lambda = (float)lambda; a.lambdaE = lam;
+    a.q = pipe->q32.p; a.out = pipe->Aq32.p; a.Nglobal = Nglobal;
+    return ax_hex<float, float>(a, AxMode::AccumulateAssembled, s);
+  };
+  return run_pipe<float>(*pipe, qHost, AqHost, pipe->q32.p, pipe->Aq32.p, Nglobal, s, launch);
+}
+
 int Elliptic::BuildDiagonal(double* diagG, cudaStream_t s) {
   DevBuf<double> dL;
   int rc = dL.alloc(Nlocal);

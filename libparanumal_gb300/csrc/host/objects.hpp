@@ -110,6 +110,23 @@ struct Mesh {
 // ---------------------------------------------------------------- elliptic_t
 enum class Prec { F64 = 0, F32 = 1, BF16G = 2 };
 
+// Copy/compute pipeline of the host-buffer operator. Elements are cut into K chunks in
+// element order; chunk c reads assembled entries [0, inEnd[c]) and, once it has run,
+// entries [0, outEnd[c]) of the result are final (no later chunk touches them). With
+// the box numbering (entries grouped by owner element, owner = smallest element holding
+// the node) both are long prefixes, so the upload of q, the chunks' operator launches
+// and the download of Aq overlap on three streams.
+struct HostPipe {
+  int K = 0;
+  std::vector<int64_t> e0;          // K+1 chunk boundaries (elements)
+  std::vector<int64_t> inEnd, outEnd;
+  cudaStream_t h2d = nullptr, d2h = nullptr;
+  std::vector<cudaEvent_t> inReady, chunkDone;
+  DevBuf<double> q, Aq;
+  DevBuf<float> q32, Aq32;
+  ~HostPipe();
+};
+
 struct Elliptic {
   Platform* plat = nullptr;
   Mesh mesh;
@@ -133,6 +150,11 @@ struct Elliptic {
   int make_f32(bool bf16, cudaStream_t s);
   int Operator(const double* q, double* Aq, cudaStream_t s);
   int OperatorF32(const float* q, float* Aq, Prec prec, cudaStream_t s);
+  // Aq = A q with host buffers (page-locked for overlap); returns when Aq is filled
+  std::unique_ptr<HostPipe> pipe;
+  int BuildPipe(cudaStream_t s);
+  int OperatorHost(const double* qHost, double* AqHost, cudaStream_t s);
+  int OperatorHostF32(const float* qHost, float* AqHost, Prec prec, cudaStream_t s);
   int BuildDiagonal(double* diagG, cudaStream_t s);   // assembled diag(A)
   int BuildRhs(double* r, cudaStream_t s);            // forcing + lifting, gathered
   // host copy of the assembled N-degree stiffness (+lambda mass), COO sorted (row, col)

@@ -73,6 +73,8 @@ int solution_norms(int N, int64_t E, const double* EX, const double* EY, const d
 int operator_diagonal_local(int N, int64_t E, const double* geo, const double* D, double lambda,
                             const double* lambdaE, const int32_t* g2l, double rankBoost,
                             double* diagL, cudaStream_t s);
+// Per element: smallest (lo) and largest (hi) assembled index among its unmasked nodes.
+int element_dof_range(int N, int64_t E, const int32_t* g2l, int32_t* lo, int32_t* hi, cudaStream_t s);
 
 // ---------------------------------------------------------------- ogs + vectors
 template <typename T>

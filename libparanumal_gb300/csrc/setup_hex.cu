@@ -360,4 +360,38 @@ int operator_diagonal_local(int N, int64_t E, const double* geo, const double* D
   return LPG_OK;
 }
 
+// ---------------------------------------------------------------- element dof ranges
+// One warp per element: smallest and largest assembled index among its unmasked nodes
+// (lo = INT32_MAX, hi = -1 for an element with every node masked).
+__global__ void element_dof_range_kernel(const int Np, const int64_t E, const int32_t* __restrict__ g2l,
+                                         int32_t* __restrict__ lo, int32_t* __restrict__ hi) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t e = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; e < E; e += warps) {
+    int mn = INT32_MAX, mx = -1;
+    for (int n = lane; n < Np; n += 32) {
+      const int32_t id = g2l[e * Np + n];
+      if (id >= 0) {
+        mn = min(mn, id);
+        mx = max(mx, id);
+      }
+    }
+    mn = __reduce_min_sync(0xffffffffu, mn);
+    mx = __reduce_max_sync(0xffffffffu, mx);
+    if (lane == 0) {
+      lo[e] = mn;
+      hi[e] = mx;
+    }
+  }
+}
+
+int element_dof_range(int N, int64_t E, const int32_t* g2l, int32_t* lo, int32_t* hi, cudaStream_t s) {
+  if (E <= 0) return LPG_OK;
+  const int Np = (N + 1) * (N + 1) * (N + 1);
+  const int64_t blocks = std::min<int64_t>((E + 7) / 8, 152 * 16);
+  element_dof_range_kernel<<<(unsigned)blocks, 256, 0, s>>>(Np, E, g2l, lo, hi);
+  LPG_LAUNCH_CHECK("element_dof_range_kernel");
+  return LPG_OK;
+}
+
 }  // namespace lpg

@@ -154,6 +154,64 @@ def test_reduced_precision_operator(prec, tol):
     assert err < tol, err
 
 
+@pytest.mark.parametrize("bf16", [False, True])
+def test_reduced_precision_operator_many_groups(bf16):
+    """16384 elements: every persistent CTA of the staged FP32 / BF16-geometry kernel
+    walks many element groups through its shared-memory ring (the small cases give a
+    CTA one group). Checked against the oracle on three consecutive applications."""
+    cfg = box(**{"BOX NX": 32, "BOX NY": 32, "BOX NZ": 16})
+    e = lpg.Elliptic(cfg)
+    o = Oracle(cfg)
+    rng = np.random.default_rng(21)
+    tol = 2e-2 if bf16 else 2e-6
+    for _ in range(3):
+        qh = rng.uniform(-1, 1, e.Nglobal)
+        q = torch.tensor(qh, dtype=torch.float32, device="cuda")
+        Aq = torch.full_like(q, np.nan)
+        e.OperatorF32(q, Aq, bf16)
+        torch.cuda.synchronize()
+        err = rel_err(Aq.double().cpu().numpy(), o.operator(qh))
+        assert err < tol, err
+
+
+HOST_CASES = [
+    box(**{"BOX NX": 32, "BOX NY": 32, "BOX NZ": 16}),                 # 16384 elements: 4 chunks
+    box(**{"POLYNOMIAL DEGREE": 3, "BOX BOUNDARY FLAG": -1, "MESH JITTER": 0.0, "BOX NX": 24,
+           "BOX NY": 16, "BOX NZ": 24}),                              # periodic: the last chunk wraps
+    box(),                                                            # a single chunk
+]
+
+
+@pytest.mark.parametrize("cfg", HOST_CASES, ids=ids)
+def test_host_buffer_operator_matches_oracle(cfg):
+    """The host-buffer operator (upload, per-chunk operator and download pipelined over
+    element chunks) gives the oracle's Aq from pinned tensors and from pageable numpy
+    arrays, in FP64 and in the reduced precisions, on consecutive calls."""
+    e = lpg.Elliptic(cfg)
+    o = Oracle(cfg)
+    E = e.info("nelements")
+    rng = np.random.default_rng(3)
+    for pinned in (True, False, True):
+        qh = rng.uniform(-1, 1, e.Nglobal)
+        ref = o.operator(qh)
+        if pinned:
+            q = torch.tensor(qh).pin_memory()
+            Aq = torch.full_like(q, np.nan).pin_memory()
+        else:
+            q, Aq = qh.copy(), np.full_like(qh, np.nan)
+        e.OperatorHost(q, Aq)
+        out = Aq.numpy() if pinned else Aq
+        assert rel_err(out, ref) < 1e-12
+        for prec, tol in (("FP32", 2e-6), ("BF16GEO", 2e-2)):
+            q32 = np.ascontiguousarray(qh, dtype=np.float32)
+            A32 = np.full_like(q32, np.nan)
+            e.OperatorHost(q32, A32, prec)
+            assert rel_err(A32.astype(np.float64), ref) < tol, prec
+    assert e.info("host_chunks") == max(1, min(32, E // 4096))
+    with pytest.raises(ValueError):
+        e.OperatorHost(np.zeros(e.Nglobal + 1), np.zeros(e.Nglobal + 1))
+
+
 def test_gather_scatter_and_reductions():
     cfg = box(**{"POLYNOMIAL DEGREE": 4})
     e = lpg.Elliptic(cfg)
