@@ -57,6 +57,10 @@ def parse():
     ap.add_argument("--train-samples", type=int, default=20000)
     ap.add_argument("--train-solves", type=int, default=8)
     ap.add_argument("--train-epochs", type=int, default=40)
+    ap.add_argument("--rhs", default="sine", choices=["sine", "gauss"],
+                    help="learned mode: manufactured sine data or 16 Gaussian sources (seed 3)")
+    ap.add_argument("--train-pairs", default="MIXED", choices=["MIXED", "TRAJECTORY"],
+                    help="SMOOTHER TRAINING PAIRS of the training problem")
     return ap.parse_args()
 
 
@@ -206,33 +210,59 @@ def run_solves(a):
 
 
 def run_learned(a):
-    """Learned fine smoother (configs[3] of the task): train on (residual, exact error)
+    """Learned fine smoother (variable-coefficient screened Poisson): train on (residual, exact error)
     pairs of the plain p-MG FPCG on a 32^3 jittered box with random Gaussian-bump
-    right-hand sides (lognormal lambda, N=7), then solve the 64^3 problem with the plain
-    FP64, the FP32 and the learned+FP32 preconditioners. One JSON line."""
+    right-hand sides (lognormal lambda, N=7), then solve the nx^3 problem (manufactured
+    sine data, or with --rhs gauss 16 Gaussian sources, seed 3) with the plain FP64, the
+    FP32 and the learned+FP32 preconditioners. Each result carries the relative 2-norm
+    difference of its solution from the FP64 method's. One JSON line."""
+    import torch
     import libparanumal_gb300 as lpg
     import __graft_entry__ as g
     g.build()
+    torch.cuda.set_device(0)
     law = {"LAMBDA": 1.0, "LAMBDA FIELD": "LOGNORMAL", "LAMBDA SEED": 2}
+    rhs = {} if a.rhs == "sine" else {"RHS FIELD": "GAUSSIAN SOURCES", "RHS SEED": 3, "RHS SOURCES": 16}
+    tlaw = dict(law, **{"SMOOTHER TRAINING PAIRS": a.train_pairs})
     t0 = time.time()
-    w, hist = lpg.train_smoother(solve_settings(a.train_nx, 7, "FP64", **law), nsolves=a.train_solves,
+    w, hist = lpg.train_smoother(solve_settings(a.train_nx, 7, "FP64", **tlaw), nsolves=a.train_solves,
                                  samples_per_solve=a.train_samples // a.train_solves, epochs=a.train_epochs,
                                  batch=250, lr=1e-3, seed=7)
     t_train = time.time() - t0
-    out = {"workload": "learned fine smoother: train %d^3, solve %d^3 jittered hex N=7 lognormal lambda"
-                       % (a.train_nx, a.nx),
+    out = {"workload": "learned fine smoother: train %d^3, solve %d^3 jittered hex N=7 lognormal lambda, %s rhs"
+                       % (a.train_nx, a.nx, "manufactured sine" if a.rhs == "sine" else "16 Gaussian sources"),
            "train_seconds": t_train, "train_samples": a.train_samples, "train_epochs": a.train_epochs,
+           "train_pairs": a.train_pairs,
            "loss_first": float(hist[0]), "loss_last": float(hist[-1]), "results": {}}
+    x64 = None
     for name, prec, learned in (("FP64", "FP64", False), ("FP32", "FP32", False), ("learned+FP32", "FP32", True)):
-        e = lpg.Elliptic(solve_settings(a.nx, 7, prec, **law))
+        t1 = time.time()
+        e = lpg.Elliptic(solve_settings(a.nx, 7, prec, **law, **rhs))
+        setup = time.time() - t1
         if learned:
             e.set_learned_smoother(w, 0.5)
         runs = [e.Run() for _ in range(a.solve_reps)]
         best = min(runs, key=lambda r: r["solve_seconds"])
-        out["results"][name] = {"solve_seconds": best["solve_seconds"], "iterations": best["iterations"],
-                                "error_vs_manufactured": best["error"], "converged": best["converged"],
-                                "vcycles": e.info("vcycles"), "fallbacks": e.info("fallbacks")}
+        res = {"solve_seconds": best["solve_seconds"], "iterations": best["iterations"],
+               "converged": best["converged"], "vcycles": e.info("vcycles"), "fallbacks": e.info("fallbacks"),
+               "setup_seconds": setup, "nglobal": e.Nglobal}
+        if a.rhs == "sine":
+            res["error_vs_manufactured"] = best["error"]
+        # the assembled solution of the same solve, compared with the FP64 method's
+        r = torch.empty(e.Nglobal, dtype=torch.float64, device="cuda")
+        x = torch.zeros_like(r)
+        e.rhs(r)
+        e.Solve(x, r, tol=1e-8)
+        torch.cuda.synchronize()
+        if x64 is None:
+            x64 = x
+        else:
+            res["rel_diff_vs_fp64_solution"] = float((x - x64).norm() / x64.norm())
+            del x
+        del r
+        out["results"][name] = res
         e.close()
+        torch.cuda.empty_cache()
     print(json.dumps(out), flush=True)
 
 
@@ -346,12 +376,16 @@ def main():
     alg_bytes = {"f64": Nl * 60 + Ng * 16, "f32": Nl * 32 + Ng * 8, "bf16g": Nl * 18 + Ng * 8}[a.prec]
     flops = (12 * (a.N + 1) + 18) * Nl
     achieved = alg_bytes / (launch_ms * 1e-3) / 1e9
+    # DRAM bytes per launch: the ncu capture's bytes per element (24^3 case, traffic
+    # grows with the element count) times this workload's elements
     traffic = None
-    tfile = os.path.join(ROOT, "profiles", "ax_hex_f64_64cubed_N7.txt")
-    if os.path.exists(tfile) and a.prec == "f64" and a.nx == 64 and a.N == 7:
+    tfile = os.path.join(ROOT, "profiles", {"f64": "ax_hex_f64_64cubed_N7.txt",
+                                            "f32": "ax_hex_staged_f32_24cubed_N7_full.txt",
+                                            "bf16g": "ax_hex_staged_bf16g_24cubed_N7_full.txt"}[a.prec])
+    if os.path.exists(tfile) and a.N == 7:
         for line in open(tfile):
-            if line.startswith("traffic_bytes_per_launch:"):
-                traffic = float(line.split(":")[1])
+            if line.startswith("traffic_bytes_per_element:"):
+                traffic = float(line.split(":")[1].split()[0]) * a.nx ** 3
     value = job_throughput(Nl, world, ms)
     out = {
         "metric": METRIC, "value": value, "unit": "GDOF/s", "n_gpus": world, "steps": a.steps,

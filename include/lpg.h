@@ -190,11 +190,13 @@ int lpg_elliptic_run(lpg_elliptic *e, double *xL_host, int *iters, double *norm,
                      double *solve_seconds);
 
 /* ------------------------------------------------------------------ learned smoother */
-/* No reference counterpart (spec addition). Element-local MLP
+/* No reference counterpart. Element-local MLP
  * 896 -> 256 -> 256 -> 256 -> 512 with GELU (tanh form) after the hidden layers; input =
  * the element's 512 residual values and 6 x 64 face-neighbour traces divided by the
- * element residual RMS s_e; the smoother's correction is s_e * invDiag * output,
- * averaged over shared nodes. Parameter vector (FP32, lpg_mlp_param_count() = 492800):
+ * element residual RMS s_e; the network's correction is s_e * invDiag * output,
+ * averaged over shared nodes. As fine-level smoother it is added to a damped-Jacobi
+ * step (4/3/rho) invDiag * r, and each smoothing correction c is taken with the
+ * energy-optimal step (c.r)/(c.Ac). Parameter vector (FP32, lpg_mlp_param_count() = 492800):
  * W0 (896x256 row-major), b0, W1 (256x256), b1, W2 (256x256), b2, W3 (256x512), b3. */
 int64_t lpg_mlp_param_count(void);
 /* floats of the activation workspace for a batch of B rows */
@@ -213,14 +215,17 @@ int lpg_mlp_adam_f32(int64_t n, float *w, const float *g, float *m, float *v, fl
 int lpg_mlp_forward_bf16(const float *params, int64_t B, const float *X, float *Y, void *stream);
 /* Trains the network on (residual, exact error) pairs from the plain p-MG FPCG solver of
  * the problem in `settings` (N = 7, PRECONDITIONER = MULTIGRID) on random Gaussian-bump
- * right-hand sides. weights_host gets lpg_mlp_param_count() floats, loss_history_host
- * (may be NULL) the mean training loss of each epoch. */
+ * right-hand sides; with [SMOOTHER TRAINING PAIRS] MIXED (default; TRAJECTORY turns it
+ * off) every second sample set is a synthetic pair (random error e, r = A e). Targets are
+ * the error outside the element's degree <= 3 modal space minus the damped-Jacobi part.
+ * weights_host gets lpg_mlp_param_count() floats, loss_history_host (may be NULL) the
+ * mean training loss of each epoch. */
 int lpg_smoother_train(const char *settings, int nsolves, int samples_per_solve, int epochs, int batch, float lr,
                        uint64_t seed, float *weights_host, float *loss_history_host);
 /* Replaces the fine-level Chebyshev smoother of e's multigrid preconditioner by the
- * network with these weights (BF16 inference); a V-cycle whose residual ratio exceeds
- * `threshold` (0.5 in the task) is redone with the plain smoother. weights_host = NULL
- * restores the plain smoother. */
+ * damped-Jacobi + network smoother with these weights (BF16 inference); a V-cycle whose
+ * residual ratio ||r - A z|| / ||r|| exceeds `threshold` (e.g. 0.5) is redone with the
+ * plain smoother. weights_host = NULL restores the plain smoother. */
 int lpg_elliptic_set_learned_smoother(lpg_elliptic *e, const float *weights_host, double threshold);
 
 #ifdef __cplusplus

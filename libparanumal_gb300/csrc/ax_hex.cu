@@ -334,6 +334,189 @@ ax_hex_staged_kernel(const int64_t Nelements, const int32_t* __restrict__ elemen
   cp_async_wait<0>();
 }
 
+// ---------------------------------------------------------------- FP64 even-odd variant
+// GLL derivative matrices satisfy D[N-i][N-m] = -D[i][m], and so does D^T. Splitting a
+// line q_0..q_N into e_m = q_m + q_{N-m} and o_m = q_m - q_{N-m} (m < H = Nq/2), the two
+// outputs t and N-t of D q are A + B and B - A with A = sum_m Dp[t][m] e_m,
+// B = sum_m Dm[t][m] o_m, Dp/Dm[t][m] = (D[t][m] +- D[t][N-m]) / 2: Nq FMA for two
+// outputs instead of 2 Nq. GB300's FP64 operator is bound by the FP64 pipe, so the
+// operation count is the lever: 49 instead of 59 FP64 operations per node at N = 7.
+//
+// Per layer k of an element, thread (i, j) forms one even/odd value of its row (partner
+// (N-i, j) is lane ^ (Nq-1)) and one of its column (partner (i, N-j) is lane ^ 2Nq: the
+// row map eo_row puts rows j and N-j in the same warp); then threads with i < H take
+// the r-derivative pair (i, N-i) of row j and threads with i >= H the s-derivative pair
+// (i-H, N-i+H) of column j. The t-direction works on the register pencil. The
+// transposed derivatives repeat the pattern with D^T. Nq = 4 or 8 (N = 3, 7).
+template <int NQ>
+__device__ __forceinline__ int eo_row(const int jj) {
+  const int lo = 2 * (jj >> 2) + (jj & 1);
+  return (jj & 2) ? (NQ - 1 - lo) : lo;
+}
+
+template <int NQ>
+__device__ __forceinline__ void eo_sync(const int el) {
+  if constexpr ((NQ * NQ) % 32 == 0) elem_sync<NQ>(el);  // Nq = 8: the element's two warps
+  else __syncwarp();                                    // Nq = 4: an element is half a warp
+}
+
+template <int NQ>
+__global__ void __launch_bounds__(NQ * NQ * elems_per_block<NQ>(), 2)
+ax_hex_eo_kernel(const int64_t Nelements, const int32_t* __restrict__ elementList,
+                 const int32_t* __restrict__ g2l, const double* __restrict__ ggeo, const int64_t geoStride,
+                 const double* __restrict__ wJ, const int64_t wJStride, const double* __restrict__ Dg,
+                 const double lambda, const double* __restrict__ lambdaE, const double* __restrict__ q,
+                 double* __restrict__ out) {
+  static_assert(NQ == 4 || NQ == 8, "even-odd kernel: Nq = 4 or 8");
+  constexpr int NP = NQ * NQ * NQ, H = NQ / 2, N = NQ - 1;
+  constexpr int EPB = elems_per_block<NQ>();
+  constexpr unsigned FULL = 0xffffffffu;
+  __shared__ double s_Dp[H][H], s_Dm[H][H];   // even/odd tables of D
+  __shared__ double s_Tp[H][H], s_Tm[H][H];   // and of D^T
+  __shared__ double s_R[EPB][NQ][NQ];         // row j: e_0..e_{H-1}, o_0..o_{H-1} along i
+  __shared__ double s_S[EPB][NQ][NQ];         // column i: the same along j
+  __shared__ double s_dr[EPB][NQ][NQ];        // [j][i] r-derivative, then r-transposed term
+  __shared__ double s_ds[EPB][NQ][NQ];        // [j][i] s-derivative, then s-transposed term
+
+  const int i = threadIdx.x, jj = threadIdx.y, el = threadIdx.z;
+  const int j = eo_row<NQ>(jj);
+  const int tid = i + NQ * (jj + NQ * el);
+  for (int t = tid; t < H * H; t += NQ * NQ * EPB) {
+    const int a = t / H, m = t % H;
+    const double d0 = Dg[a * NQ + m], d1 = Dg[a * NQ + N - m];     // D[a][m], D[a][N-m]
+    const double t0 = Dg[m * NQ + a], t1 = Dg[(N - m) * NQ + a];   // D^T[a][m], D^T[a][N-m]
+    s_Dp[a][m] = 0.5 * (d0 + d1);
+    s_Dm[a][m] = 0.5 * (d0 - d1);
+    s_Tp[a][m] = 0.5 * (t0 + t1);
+    s_Tm[a][m] = 0.5 * (t0 - t1);
+  }
+
+  int64_t e = (int64_t)blockIdx.x * EPB + el;
+  const bool active = e < Nelements;
+  if (active && elementList) e = elementList[e];
+  if (!active) e = 0;
+
+  double r_q[NQ], r_Aq[NQ], qt[NQ], Gqt[NQ];
+  int32_t r_id[NQ];
+  const int64_t nodeBase = e * NP + j * NQ + i;
+#pragma unroll
+  for (int k = 0; k < NQ; ++k) {
+    const int32_t id = active ? __ldg(g2l + nodeBase + k * NQ * NQ) : -1;
+    r_id[k] = id;
+    r_q[k] = (id >= 0) ? q[id] : 0.0;
+  }
+  const double lam = (lambdaE && active) ? lambdaE[e] : lambda;
+  const double* gp = ggeo + e * geoStride + j * NQ + i;
+  const double* wp = wJ + e * wJStride + j * NQ + i;
+  __syncthreads();
+
+  // t-direction of the pencil, even/odd
+  {
+    double E[H], O[H];
+#pragma unroll
+    for (int m = 0; m < H; ++m) {
+      E[m] = r_q[m] + r_q[N - m];
+      O[m] = r_q[m] - r_q[N - m];
+    }
+#pragma unroll
+    for (int t = 0; t < H; ++t) {
+      double A = 0, B = 0;
+#pragma unroll
+      for (int m = 0; m < H; ++m) {
+        A += s_Dp[t][m] * E[m];
+        B += s_Dm[t][m] * O[m];
+      }
+      qt[t] = A + B;
+      qt[N - t] = B - A;
+    }
+  }
+
+  // the pair task of this thread: r-pair of row j (i < H) or s-pair of column j (i >= H)
+  const bool rtask = i < H;
+  const int pt = rtask ? i : i - H;
+  double* dst0 = rtask ? &s_dr[el][j][pt] : &s_ds[el][pt][j];
+  double* dst1 = rtask ? &s_dr[el][j][N - pt] : &s_ds[el][N - pt][j];
+  const double* line = rtask ? &s_R[el][j][0] : &s_S[el][j][0];
+
+#pragma unroll
+  for (int k = 0; k < NQ; ++k) {
+    const int off = k * NQ * NQ;
+    double G00 = 0, G01 = 0, G02 = 0, G11 = 0, G12 = 0, G22 = 0, GwJ = 0;
+    if (active) {
+      G00 = gp[0 * NP + off]; G01 = gp[1 * NP + off]; G02 = gp[2 * NP + off];
+      G11 = gp[3 * NP + off]; G12 = gp[4 * NP + off]; G22 = gp[5 * NP + off];
+      GwJ = wp[off];
+    }
+    // even/odd values of q along i (row j) and along j (column i)
+    const double v = r_q[k];
+    const double pr = __shfl_xor_sync(FULL, v, NQ - 1);
+    const double ps = __shfl_xor_sync(FULL, v, 2 * NQ);
+    if (i < H) s_R[el][j][i] = v + pr; else s_R[el][j][H + N - i] = pr - v;
+    if (j < H) s_S[el][i][j] = v + ps; else s_S[el][i][H + N - j] = ps - v;
+    eo_sync<NQ>(el);
+    {
+      double A = 0, B = 0;
+#pragma unroll
+      for (int m = 0; m < H; ++m) {
+        A += s_Dp[pt][m] * line[m];
+        B += s_Dm[pt][m] * line[H + m];
+      }
+      *dst0 = A + B;
+      *dst1 = B - A;
+    }
+    eo_sync<NQ>(el);
+    const double qr = s_dr[el][j][i], qs = s_ds[el][j][i];
+    const double Gqr = G00 * qr + G01 * qs + G02 * qt[k];
+    const double Gqs = G01 * qr + G11 * qs + G12 * qt[k];
+    Gqt[k] = G02 * qr + G12 * qs + G22 * qt[k];
+    const double mass = GwJ * lam * v;
+    // even/odd values of Gqr along i and of Gqs along j for the transposed derivatives
+    const double pr2 = __shfl_xor_sync(FULL, Gqr, NQ - 1);
+    const double ps2 = __shfl_xor_sync(FULL, Gqs, 2 * NQ);
+    if (i < H) s_R[el][j][i] = Gqr + pr2; else s_R[el][j][H + N - i] = pr2 - Gqr;
+    if (j < H) s_S[el][i][j] = Gqs + ps2; else s_S[el][i][H + N - j] = ps2 - Gqs;
+    eo_sync<NQ>(el);
+    {
+      double A = 0, B = 0;
+#pragma unroll
+      for (int m = 0; m < H; ++m) {
+        A += s_Tp[pt][m] * line[m];
+        B += s_Tm[pt][m] * line[H + m];
+      }
+      *dst0 = A + B;
+      *dst1 = B - A;
+    }
+    eo_sync<NQ>(el);
+    r_Aq[k] = mass + s_dr[el][j][i] + s_ds[el][j][i];
+  }
+
+  // transposed t-direction: r_Aq[t] += sum_m D[m][t] Gqt[m], even/odd
+  {
+    double E[H], O[H];
+#pragma unroll
+    for (int m = 0; m < H; ++m) {
+      E[m] = Gqt[m] + Gqt[N - m];
+      O[m] = Gqt[m] - Gqt[N - m];
+    }
+#pragma unroll
+    for (int t = 0; t < H; ++t) {
+      double A = 0, B = 0;
+#pragma unroll
+      for (int m = 0; m < H; ++m) {
+        A += s_Tp[t][m] * E[m];
+        B += s_Tm[t][m] * O[m];
+      }
+      r_Aq[t] += A + B;
+      r_Aq[N - t] += B - A;
+    }
+  }
+
+  if (!active) return;
+#pragma unroll
+  for (int k = 0; k < NQ; ++k)
+    if (r_id[k] >= 0) atomicAdd(out + r_id[k], r_Aq[k]);
+}
+
 template <int NQ, typename T, typename G, int EPB, int STAGES>
 static int launch_staged(const AxArgs<T, G>& a, cudaStream_t s) {
   using L = StagedLayout<NQ, G>;
@@ -405,6 +588,21 @@ static int launch_ax(const AxArgs<T, G>& a, cudaStream_t s) {
   const int64_t blocks = (a.Nelements + EPB - 1) / EPB;
   if (blocks > 0x7fffffffLL) return set_error(LPG_ERR_INVALID, "ax: too many elements");
   dim3 block(NQ, NQ, EPB);
+  if constexpr (std::is_same<T, double>::value && std::is_same<G, double>::value && INMODE == IN_GATHER &&
+                OUTMODE == OUT_ASSEMBLE && (NQ == 4 || NQ == 8)) {
+    // LPG_AX_FP64 = direct: tuning override back to the direct-contraction kernel
+    static const bool direct = [] {
+      const char* e = std::getenv("LPG_AX_FP64");
+      return e && !std::strcmp(e, "direct");
+    }();
+    if (!direct) {
+      ax_hex_eo_kernel<NQ><<<(unsigned)blocks, block, 0, s>>>(a.Nelements, a.elementList, a.g2l, a.ggeo,
+                                                               a.geoStride, a.wJ, a.wJStride, a.D, a.lambda,
+                                                               a.lambdaE, a.q, a.out);
+      LPG_LAUNCH_CHECK("ax_hex_eo_kernel");
+      return LPG_OK;
+    }
+  }
   ax_hex_kernel<NQ, T, G, INMODE, OUTMODE><<<(unsigned)blocks, block, 0, s>>>(
       a.Nelements, a.elementList, a.g2l, a.ggeo, a.geoStride, a.wJ, a.wJStride, a.D, a.lambda,
       a.lambdaE, a.q, a.out);

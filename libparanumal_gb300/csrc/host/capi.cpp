@@ -554,6 +554,10 @@ extern "C" int lpg_smoother_train(const char* settings, int nsolves, int samples
   o.batch = batch;
   o.lr = lr;
   o.seed = seed;
+  const std::string pairs = e->settings.get("SMOOTHER TRAINING PAIRS", "MIXED");
+  if (pairs != "MIXED" && pairs != "TRAJECTORY")
+    return set_error(LPG_ERR_SETTINGS, "SMOOTHER TRAINING PAIRS must be MIXED or TRAJECTORY");
+  o.synthetic = (pairs == "MIXED");
   std::vector<float> w, hist;
   if ((rc = train_smoother(&e->plat, e->el.get(), e->precon.get(), b, o, w, hist))) return rc;
   std::memcpy(weights_host, w.data(), sizeof(float) * w.size());

@@ -7,7 +7,10 @@
 // residual r_k and the exact error e_k = x* - x_k of the plain solver's iterate. Each
 // sampled element contributes (its normalised residual block and face traces of r_k,
 // D .* e_k restricted to it / s_e). Residuals from the iteration are dominated by the
-// high-frequency content a smoother has to remove.
+// high-frequency content a smoother has to remove. With SMOOTHER TRAINING PAIRS = MIXED
+// (default) every second sample set is synthetic instead: a random error e (lattice
+// noise after 0, 2 or 6 damped-Jacobi sweeps) and r = A e, which widens the residual
+// distribution toward what the post-smoothing step sees after a coarse correction.
 #include "learned.hpp"
 
 #include <algorithm>
@@ -92,6 +95,9 @@ int train_smoother(Platform* plat, Elliptic* el, Precon* plainMG, const BoxNumbe
   if ((rc = invDiag.alloc(Ng)) || (rc = el->BuildDiagonal(invDiag.p, s)) || (rc = inverse_f64(Ng, invDiag.p, invDiag.p, s)))
     return rc;
   const int64_t total = (int64_t)o.nsolves * o.samplesPerSolve;
+  // the smoother is w D^{-1} r + network correction with the reference's damped-Jacobi
+  // weight w = 4/3/rho (rho of D^{-1}A on the finest level); the network learns the rest
+  const double jacobiW = plainMG->fine_rho() > 0 ? (4.0 / 3.0) / plainMG->fine_rho() : 0.0;
   DevBuf<float> Xtr, Ttr;
   if ((rc = Xtr.alloc(total * kMlpIn)) || (rc = Ttr.alloc(total * kMlpOut))) return rc;
   DevBuf<float> Xall, scaleAll;
@@ -148,47 +154,60 @@ int train_smoother(Platform* plat, Elliptic* el, Precon* plainMG, const BoxNumbe
   PCGWork work;
   const MeshConfig& c = el->mesh.cfg;
   for (int sidx = 0; sidx < o.nsolves; ++sidx) {
-    // random Gaussian-bump right-hand side: o.bumps bumps, centres U(domain), widths
-    // U[0.05,0.2], signed unit amplitudes (sign by the sample stream)
-    std::vector<double> src(4 * o.bumps);
-    std::vector<double> sign(o.bumps);
-    for (int k = 0; k < o.bumps; ++k) {
-      src[4 * k + 0] = -c.dimx / 2 + c.dimx * rng.next();
-      src[4 * k + 1] = -c.dimy / 2 + c.dimy * rng.next();
-      src[4 * k + 2] = -c.dimz / 2 + c.dimz * rng.next();
-      src[4 * k + 3] = 0.05 + 0.15 * rng.next();
-      sign[k] = (rng.next() < 0.5) ? -1.0 : 1.0;
-    }
-    // signed bumps: split into positive and negative source sets and combine
-    DevBuf<double> rhsNeg;
-    if ((rc = rhsNeg.alloc(Ng))) return rc;
-    for (int pass = 0; pass < 2; ++pass) {
-      std::vector<double> sel;
-      for (int k = 0; k < o.bumps; ++k)
-        if ((sign[k] > 0) == (pass == 0)) sel.insert(sel.end(), src.begin() + 4 * k, src.begin() + 4 * k + 4);
-      el->rhsKind = 1;
-      el->sources = sel;
-      if (sel.empty()) {
-        LPG_CUDA_TRY(cudaMemsetAsync(pass == 0 ? rhs.p : rhsNeg.p, 0, sizeof(double) * Ng, s));
-        continue;
+    if (o.synthetic && (sidx % 2 == 1)) {
+      // synthetic pair: e = lattice noise after m damped-Jacobi sweeps (m = 0, 2, 6 gives
+      // rough to smoother errors), r = A e; x holds e
+      static const int sweeps[3] = {0, 2, 6};
+      const int m = sweeps[(sidx / 2) % 3];
+      if ((rc = lattice_random(b, Ng, el->owner.p, o.seed * 1000003ULL + (uint64_t)sidx, x.p, s))) return rc;
+      for (int j = 0; j < m; ++j) {
+        if ((rc = el->Operator(x.p, r.p, s))) return rc;
+        if ((rc = amxpy<double>(Ng, -2.0 / 3.0, invDiag.p, r.p, 1.0, x.p, s))) return rc;
       }
-      if ((rc = el->sources_d.alloc((int64_t)sel.size())) || (rc = el->sources_d.upload(sel.data(), (int64_t)sel.size(), s)))
-        return rc;
-      if ((rc = el->BuildRhs(pass == 0 ? rhs.p : rhsNeg.p, s))) return rc;
+      if ((rc = el->Operator(x.p, r.p, s))) return rc;
+    } else {
+      // random Gaussian-bump right-hand side: o.bumps bumps, centres U(domain), widths
+      // U[0.05,0.2], signed unit amplitudes (sign by the sample stream)
+      std::vector<double> src(4 * o.bumps);
+      std::vector<double> sign(o.bumps);
+      for (int k = 0; k < o.bumps; ++k) {
+        src[4 * k + 0] = -c.dimx / 2 + c.dimx * rng.next();
+        src[4 * k + 1] = -c.dimy / 2 + c.dimy * rng.next();
+        src[4 * k + 2] = -c.dimz / 2 + c.dimz * rng.next();
+        src[4 * k + 3] = 0.05 + 0.15 * rng.next();
+        sign[k] = (rng.next() < 0.5) ? -1.0 : 1.0;
+      }
+      // signed bumps: split into positive and negative source sets and combine
+      DevBuf<double> rhsNeg;
+      if ((rc = rhsNeg.alloc(Ng))) return rc;
+      for (int pass = 0; pass < 2; ++pass) {
+        std::vector<double> sel;
+        for (int k = 0; k < o.bumps; ++k)
+          if ((sign[k] > 0) == (pass == 0)) sel.insert(sel.end(), src.begin() + 4 * k, src.begin() + 4 * k + 4);
+        el->rhsKind = 1;
+        el->sources = sel;
+        if (sel.empty()) {
+          LPG_CUDA_TRY(cudaMemsetAsync(pass == 0 ? rhs.p : rhsNeg.p, 0, sizeof(double) * Ng, s));
+          continue;
+        }
+        if ((rc = el->sources_d.alloc((int64_t)sel.size())) || (rc = el->sources_d.upload(sel.data(), (int64_t)sel.size(), s)))
+          return rc;
+        if ((rc = el->BuildRhs(pass == 0 ? rhs.p : rhsNeg.p, s))) return rc;
+      }
+      if ((rc = axpy<double>(Ng, -1.0, rhsNeg.p, 1.0, rhs.p, s))) return rc;
+      // converged solution x* of the plain p-MG FPCG
+      LPG_CUDA_TRY(cudaMemsetAsync(xstar.p, 0, sizeof(double) * Ng, s));
+      LPG_CUDA_TRY(cudaMemcpyAsync(r.p, rhs.p, sizeof(double) * Ng, cudaMemcpyDeviceToDevice, s));
+      PCGResult res;
+      if ((rc = pcg_solve(plat, el, plainMG, work, true, false, xstar.p, r.p, o.solveTol, 500, res))) return rc;
+      // a (residual, exact error) pair of the plain solver's trajectory: after k iterations
+      // the residual is r_k and the exact error is x* - x_k (the FPCG run is deterministic)
+      const int kIter = 1 + (sidx % 3);
+      LPG_CUDA_TRY(cudaMemsetAsync(x.p, 0, sizeof(double) * Ng, s));
+      LPG_CUDA_TRY(cudaMemcpyAsync(r.p, rhs.p, sizeof(double) * Ng, cudaMemcpyDeviceToDevice, s));
+      if ((rc = pcg_solve(plat, el, plainMG, work, true, false, x.p, r.p, 0.0, kIter, res))) return rc;
+      if ((rc = axpy<double>(Ng, 1.0, xstar.p, -1.0, x.p, s))) return rc;  // x := x* - x_k
     }
-    if ((rc = axpy<double>(Ng, -1.0, rhsNeg.p, 1.0, rhs.p, s))) return rc;
-    // converged solution x* of the plain p-MG FPCG
-    LPG_CUDA_TRY(cudaMemsetAsync(xstar.p, 0, sizeof(double) * Ng, s));
-    LPG_CUDA_TRY(cudaMemcpyAsync(r.p, rhs.p, sizeof(double) * Ng, cudaMemcpyDeviceToDevice, s));
-    PCGResult res;
-    if ((rc = pcg_solve(plat, el, plainMG, work, true, false, xstar.p, r.p, o.solveTol, 500, res))) return rc;
-    // a (residual, exact error) pair of the plain solver's trajectory: after k iterations
-    // the residual is r_k and the exact error is x* - x_k (the FPCG run is deterministic)
-    const int kIter = 1 + (sidx % 3);
-    LPG_CUDA_TRY(cudaMemsetAsync(x.p, 0, sizeof(double) * Ng, s));
-    LPG_CUDA_TRY(cudaMemcpyAsync(r.p, rhs.p, sizeof(double) * Ng, cudaMemcpyDeviceToDevice, s));
-    if ((rc = pcg_solve(plat, el, plainMG, work, true, false, x.p, r.p, 0.0, kIter, res))) return rc;
-    if ((rc = axpy<double>(Ng, 1.0, xstar.p, -1.0, x.p, s))) return rc;  // x := x* - x_k
     // features of every element for residual r_k (scales floored at kScaleFloor x RMS),
     // then a random subset of the elements whose residual is not negligible
     double bb;
@@ -225,6 +244,11 @@ int train_smoother(Platform* plat, Elliptic* el, Precon* plainMG, const BoxNumbe
       LPG_CUDA_TRY(cudaMemcpyAsync(Ttr.p + base * kMlpOut, Ts.data(), sizeof(float) * Ts.size(), cudaMemcpyHostToDevice, s));
       LPG_CUDA_TRY(cudaStreamSynchronize(s));
     }
+    // the damped-Jacobi part w D^{-1} r is applied outside the network: in network
+    // output units (divided by invDiag s_e) it is w times the normalised residual input
+    if (jacobiW > 0 && (rc = subtract_inputs(o.samplesPerSolve, (float)jacobiW, Xtr.p + base * kMlpIn,
+                                             Ttr.p + base * kMlpOut, s)))
+      return rc;
   }
   lastKeptFraction = keptFraction;
   // initial parameters: Glorot-uniform weights, zero biases (seeded)

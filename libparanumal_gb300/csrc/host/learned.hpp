@@ -37,6 +37,9 @@ struct TrainOptions {
   double solveTol = 1e-10;
   uint64_t seed = 7;
   double targetCap = 4.0;   // keep samples whose RMS normalised target is at most this
+  // odd-numbered sample sets are synthetic: e = random lattice noise smoothed by 0, 2 or
+  // 6 damped-Jacobi sweeps, r = A e (no solve), instead of a solver-trajectory pair
+  bool synthetic = true;
 };
 
 // fraction of elements that passed the sample filter in the last training run

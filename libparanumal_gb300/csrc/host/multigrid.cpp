@@ -451,6 +451,10 @@ class MultiGrid : public Precon {
   int64_t coarse_n() const override { return coarseN; }
   int64_t fallbacks() const override { return nFallback; }
   int64_t vcycles() const override { return nVcycle; }
+  double fine_rho() const override {
+    if (p.empty()) return 0;
+    return opt.smoother == 0 ? p[0]->lambda1 : (4.0 / 3.0) / p[0]->lambda0;
+  }
   int set_learned(LearnedSmoother* L, const BoxNumbering& b, double thr) override {
     if (p.empty()) return set_error(LPG_ERR_UNSUPPORTED, "a learned smoother needs at least one p-level");
     if (fine->mesh.N != 7) return set_error(LPG_ERR_UNSUPPORTED, "the learned smoother is defined for N = 7");
@@ -600,26 +604,43 @@ int MultiGrid::dot_host(int64_t n, const T* x, const T* y, double& out, cudaStre
   return LPG_OK;
 }
 
-// V-cycle whose fine-level smoother is the learned element-local map L:
-// X = L(RHS); X += coarse correction of RHS - A X; X += L(RHS - A X).
-// If the V-cycle leaves ||RHS - A X|| > threshold ||RHS||, it is redone with the plain
-// smoother (fallback), and the fallback is counted.
+// V-cycle whose fine-level smoother is S(r) = (4/3/rho) D^{-1} r + L(r), a damped-Jacobi
+// step plus the learned element-local correction L, each smoothing correction c taken
+// with the energy-optimal step w = (c.r)/(c.Ac) (w = 0 if c.Ac <= 0):
+//   X = w1 S(RHS); X += coarse correction of RHS - A X; X += w2 S(RHS - A X).
+// The products A c come from the operator applications the cycle needs anyway (the
+// final residual is RES - w2 A c2). If the V-cycle leaves ||RHS - A X|| > threshold
+// ||RHS||, it is redone with the plain smoother (fallback), and the fallback is counted.
 template <typename T>
 int MultiGrid::vcycle_learned(const T* RHS, T* X, cudaStream_t s) {
   PLevel& L = *p[0];
   Elliptic* el = L.el;
   const int64_t N = el->Nglobal, E = el->mesh.E;
   T* RES = vec<T>(L.res64, L.res32);
+  T* AD = vec<T>(s64[1], s32[1]);
   T* D = vec<T>(s64[2], s32[2]);
+  const T* invDiag = vec<T>(L.invDiag64, L.invDiag32);
+  const double jacobiW = fine_rho() > 0 ? (4.0 / 3.0) / fine_rho() : 0.0;
+  auto step = [](double cr, double cAc) { return (cAc > 0 && std::isfinite(cr) && std::isfinite(cAc)) ? cr / cAc : 0.0; };
   int rc;
+  double cr, cAc;
+  // pre-smoothing: X = w1 c1, RES = RHS - w1 A c1
   if ((rc = learned->apply<T>(box, E, el->g2l.p, RHS, L.invDiag64.p, el->weightG.p, X, N, s))) return rc;
-  if ((rc = op<T>(el, X, RES, s)) || (rc = axpy<T>(N, T(1), RHS, T(-1), RES, s))) return rc;
+  if (jacobiW > 0 && (rc = amxpy<T>(N, (T)jacobiW, invDiag, RHS, T(1), X, s))) return rc;
+  if ((rc = op<T>(el, X, RES, s))) return rc;
+  if ((rc = dot_host<T>(N, X, RHS, cr, s)) || (rc = dot_host<T>(N, X, RES, cAc, s))) return rc;
+  const double w1 = step(cr, cAc);
+  if ((rc = axpy<T>(N, T(0), RHS, (T)w1, X, s)) || (rc = axpy<T>(N, T(1), RHS, (T)(-w1), RES, s))) return rc;
   if ((rc = coarse_correct<T>(0, RES, X, s))) return rc;
+  // post-smoothing: X += w2 c2, RES -= w2 A c2
   if ((rc = op<T>(el, X, RES, s)) || (rc = axpy<T>(N, T(1), RHS, T(-1), RES, s))) return rc;
   if ((rc = learned->apply<T>(box, E, el->g2l.p, RES, L.invDiag64.p, el->weightG.p, D, N, s))) return rc;
-  if ((rc = axpy<T>(N, T(1), D, T(1), X, s))) return rc;
+  if (jacobiW > 0 && (rc = amxpy<T>(N, (T)jacobiW, invDiag, RES, T(1), D, s))) return rc;
+  if ((rc = op<T>(el, D, AD, s))) return rc;
+  if ((rc = dot_host<T>(N, D, RES, cr, s)) || (rc = dot_host<T>(N, D, AD, cAc, s))) return rc;
+  const double w2 = step(cr, cAc);
+  if ((rc = axpy<T>(N, (T)w2, D, T(1), X, s)) || (rc = axpy<T>(N, (T)(-w2), AD, T(1), RES, s))) return rc;
   // residual reduction of this V-cycle
-  if ((rc = op<T>(el, X, RES, s)) || (rc = axpy<T>(N, T(1), RHS, T(-1), RES, s))) return rc;
   double rr, bb;
   if ((rc = dot_host<T>(N, RES, RES, rr, s)) || (rc = dot_host<T>(N, RHS, RHS, bb, s))) return rc;
   nVcycle++;

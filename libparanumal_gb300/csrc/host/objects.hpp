@@ -177,6 +177,8 @@ struct Precon {
     return set_error(LPG_ERR_UNSUPPORTED, "a learned smoother needs PRECONDITIONER = MULTIGRID");
   }
   virtual int64_t fallbacks() const { return 0; }
+  // spectral radius estimate of D^{-1} A on the finest p-level (0 without p-levels)
+  virtual double fine_rho() const { return 0; }
   virtual int64_t vcycles() const { return 0; }
 };
 

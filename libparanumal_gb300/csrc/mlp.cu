@@ -503,4 +503,20 @@ int gather_rows(int64_t count, const int32_t* elems, const float* Xall, float* X
   return LPG_OK;
 }
 
+// T[i][n] -= w * X[i][n] for the first kMlpOut inputs (the element's normalised
+// residual): targets of the network part of a damped-Jacobi + network smoother
+__global__ void subtract_inputs_kernel(const int64_t count, const float w, const float* __restrict__ X,
+                                       float* __restrict__ T) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count * kMlpOut; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t row = i / kMlpOut;
+    T[i] -= w * X[row * kMlpIn + (i % kMlpOut)];
+  }
+}
+int subtract_inputs(int64_t count, float w, const float* X, float* T, cudaStream_t s) {
+  if (count <= 0 || w == 0.f) return LPG_OK;
+  subtract_inputs_kernel<<<grid_n(count * kMlpOut), 256, 0, s>>>(count, w, X, T);
+  LPG_LAUNCH_CHECK("subtract_inputs_kernel");
+  return LPG_OK;
+}
+
 }  // namespace lpg

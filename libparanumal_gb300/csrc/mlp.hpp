@@ -74,6 +74,8 @@ int apply_correction(int Np, int64_t count, int64_t e0, const int32_t* g2l, cons
 int training_targets(int Np, int64_t count, const int32_t* elems, const int32_t* g2l, const double* e,
                      const double* invDiag, const float* scale, float* T, cudaStream_t s);
 int gather_rows(int64_t count, const int32_t* elems, const float* Xall, float* X, cudaStream_t s);
+// T[i][n] -= w X[i][n], n < kMlpOut (targets of a damped-Jacobi + network smoother)
+int subtract_inputs(int64_t count, float w, const float* X, float* T, cudaStream_t s);
 // T (E x 512) = (e - F e) / (invDiag s_e) per element, F the 1D modal low-pass (Nq x Nq)
 int highpass_targets(int Nq, int64_t E, const int32_t* g2l, const double* e, const double* invDiag, const float* scale,
                      const double* F, float* T, cudaStream_t s);
