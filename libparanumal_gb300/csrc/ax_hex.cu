@@ -361,7 +361,7 @@ __device__ __forceinline__ void eo_sync(const int el) {
 }
 
 template <int NQ>
-__global__ void __launch_bounds__(NQ * NQ * elems_per_block<NQ>(), 2)
+__global__ void __launch_bounds__(NQ * NQ * elems_per_block<NQ>(), 3)
 ax_hex_eo_kernel(const int64_t Nelements, const int32_t* __restrict__ elementList,
                  const int32_t* __restrict__ g2l, const double* __restrict__ ggeo, const int64_t geoStride,
                  const double* __restrict__ wJ, const int64_t wJStride, const double* __restrict__ Dg,
@@ -377,6 +377,10 @@ ax_hex_eo_kernel(const int64_t Nelements, const int32_t* __restrict__ elementLis
   __shared__ double s_S[EPB][NQ][NQ];         // column i: the same along j
   __shared__ double s_dr[EPB][NQ][NQ];        // [j][i] r-derivative, then r-transposed term
   __shared__ double s_ds[EPB][NQ][NQ];        // [j][i] s-derivative, then s-transposed term
+  // per-thread pencils of D_t q and of G_t . grad q, [k][thread] (kept out of registers so
+  // that three CTAs fit on an SM: the FP64 pipe needs the warps)
+  __shared__ double s_qt[NQ][NQ * NQ * EPB];
+  __shared__ double s_gt[NQ][NQ * NQ * EPB];
 
   const int i = threadIdx.x, jj = threadIdx.y, el = threadIdx.z;
   const int j = eo_row<NQ>(jj);
@@ -396,7 +400,7 @@ ax_hex_eo_kernel(const int64_t Nelements, const int32_t* __restrict__ elementLis
   if (active && elementList) e = elementList[e];
   if (!active) e = 0;
 
-  double r_q[NQ], r_Aq[NQ], qt[NQ], Gqt[NQ];
+  double r_q[NQ], r_Aq[NQ];
   int32_t r_id[NQ];
   const int64_t nodeBase = e * NP + j * NQ + i;
 #pragma unroll
@@ -426,8 +430,8 @@ ax_hex_eo_kernel(const int64_t Nelements, const int32_t* __restrict__ elementLis
         A += s_Dp[t][m] * E[m];
         B += s_Dm[t][m] * O[m];
       }
-      qt[t] = A + B;
-      qt[N - t] = B - A;
+      s_qt[t][tid] = A + B;
+      s_qt[N - t][tid] = B - A;
     }
   }
 
@@ -437,6 +441,11 @@ ax_hex_eo_kernel(const int64_t Nelements, const int32_t* __restrict__ elementLis
   double* dst0 = rtask ? &s_dr[el][j][pt] : &s_ds[el][pt][j];
   double* dst1 = rtask ? &s_dr[el][j][N - pt] : &s_ds[el][N - pt][j];
   const double* line = rtask ? &s_R[el][j][0] : &s_S[el][j][0];
+  // even/odd slot of this thread's node in its row (along i) and column (along j): the
+  // value is partner + sign * own (e for the first half, o for the second), written
+  // without branches so that no FP64 instruction issues twice in a diverged warp
+  const int slotR = (i < H) ? i : H + N - i, slotS = (j < H) ? j : H + N - j;
+  const double sgnR = (i < H) ? 1.0 : -1.0, sgnS = (j < H) ? 1.0 : -1.0;
 
 #pragma unroll
   for (int k = 0; k < NQ; ++k) {
@@ -451,8 +460,8 @@ ax_hex_eo_kernel(const int64_t Nelements, const int32_t* __restrict__ elementLis
     const double v = r_q[k];
     const double pr = __shfl_xor_sync(FULL, v, NQ - 1);
     const double ps = __shfl_xor_sync(FULL, v, 2 * NQ);
-    if (i < H) s_R[el][j][i] = v + pr; else s_R[el][j][H + N - i] = pr - v;
-    if (j < H) s_S[el][i][j] = v + ps; else s_S[el][i][H + N - j] = ps - v;
+    s_R[el][j][slotR] = fma(sgnR, v, pr);
+    s_S[el][i][slotS] = fma(sgnS, v, ps);
     eo_sync<NQ>(el);
     {
       double A = 0, B = 0;
@@ -465,16 +474,16 @@ ax_hex_eo_kernel(const int64_t Nelements, const int32_t* __restrict__ elementLis
       *dst1 = B - A;
     }
     eo_sync<NQ>(el);
-    const double qr = s_dr[el][j][i], qs = s_ds[el][j][i];
-    const double Gqr = G00 * qr + G01 * qs + G02 * qt[k];
-    const double Gqs = G01 * qr + G11 * qs + G12 * qt[k];
-    Gqt[k] = G02 * qr + G12 * qs + G22 * qt[k];
+    const double qr = s_dr[el][j][i], qs = s_ds[el][j][i], qtk = s_qt[k][tid];
+    const double Gqr = G00 * qr + G01 * qs + G02 * qtk;
+    const double Gqs = G01 * qr + G11 * qs + G12 * qtk;
+    s_gt[k][tid] = G02 * qr + G12 * qs + G22 * qtk;
     const double mass = GwJ * lam * v;
     // even/odd values of Gqr along i and of Gqs along j for the transposed derivatives
     const double pr2 = __shfl_xor_sync(FULL, Gqr, NQ - 1);
     const double ps2 = __shfl_xor_sync(FULL, Gqs, 2 * NQ);
-    if (i < H) s_R[el][j][i] = Gqr + pr2; else s_R[el][j][H + N - i] = pr2 - Gqr;
-    if (j < H) s_S[el][i][j] = Gqs + ps2; else s_S[el][i][H + N - j] = ps2 - Gqs;
+    s_R[el][j][slotR] = fma(sgnR, Gqr, pr2);
+    s_S[el][i][slotS] = fma(sgnS, Gqs, ps2);
     eo_sync<NQ>(el);
     {
       double A = 0, B = 0;
@@ -495,8 +504,9 @@ ax_hex_eo_kernel(const int64_t Nelements, const int32_t* __restrict__ elementLis
     double E[H], O[H];
 #pragma unroll
     for (int m = 0; m < H; ++m) {
-      E[m] = Gqt[m] + Gqt[N - m];
-      O[m] = Gqt[m] - Gqt[N - m];
+      const double g0 = s_gt[m][tid], g1 = s_gt[N - m][tid];
+      E[m] = g0 + g1;
+      O[m] = g0 - g1;
     }
 #pragma unroll
     for (int t = 0; t < H; ++t) {
