@@ -53,6 +53,7 @@ def parse():
     ap.add_argument("--solve-precs", default="FP64,FP32,BF16GEO")
     ap.add_argument("--solve-reps", type=int, default=2)
     ap.add_argument("--learned", action="store_true", help="learned-smoother training and solve comparison")
+    ap.add_argument("--mlp", action="store_true", help="learned-smoother MLP inference (lpg_mlp_forward_bf16) timing")
     ap.add_argument("--train-nx", type=int, default=32)
     ap.add_argument("--train-samples", type=int, default=20000)
     ap.add_argument("--train-solves", type=int, default=8)
@@ -266,6 +267,37 @@ def run_learned(a):
     print(json.dumps(out), flush=True)
 
 
+def run_mlp(a):
+    """Inference of the learned smoother's MLP through lpg_mlp_forward_bf16 (weights
+    converted to BF16 inside each call) on 65,536 and 262,144 random rows: 2 warm-up and
+    5 timed calls each. One JSON line; the kernel alone is seen in an ncu launch list."""
+    import numpy as np
+    import torch
+    import libparanumal_gb300 as lpg
+    import __graft_entry__ as g
+    from oracle import mlp
+    g.build()
+    torch.cuda.set_device(0)
+    L = lpg.lib()
+    theta = torch.tensor(mlp.glorot(3).astype(np.float32), device="cuda")
+    res = {}
+    for B in (65536, 262144):
+        X = torch.randn(B, 896, device="cuda")
+        Y = torch.empty(B, 512, device="cuda")
+        for _ in range(2):
+            lpg.check(L.lpg_mlp_forward_bf16(theta.data_ptr(), B, X.data_ptr(), Y.data_ptr(), None))
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(5):
+            lpg.check(L.lpg_mlp_forward_bf16(theta.data_ptr(), B, X.data_ptr(), Y.data_ptr(), None))
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / 5
+        res[str(B)] = {"ms_per_call_incl_weight_conversion": ms, "tflops": B * 492800 * 2 / ms / 1e9}
+    print(json.dumps({"workload": "learned-smoother MLP inference, BF16 tensor cores", "results": res}), flush=True)
+
+
 def main():
     a = parse()
     if a.impl == "reference":
@@ -274,6 +306,8 @@ def main():
         return run_solves(a)
     if a.learned:
         return run_learned(a)
+    if a.mlp:
+        return run_mlp(a)
     import numpy as np
     import torch
     import libparanumal_gb300 as lpg

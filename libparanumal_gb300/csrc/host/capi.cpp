@@ -524,11 +524,9 @@ extern "C" int lpg_mlp_forward_bf16(const float* params, int64_t B, const float*
   LPG_CUDA_TRY(cudaStreamSynchronize(s));
   if ((rc = L.load(host.data(), s)) || (rc = L.ensure_chunk(B))) return rc;
   if ((rc = convert<float, __nv_bfloat16>(B * kMlpIn, X, L.X.p, s))) return rc;
-  MLPParams P = MLPParams::view(L.params.p);
-  if ((rc = bf16_linear((int)B, kMlpHidden, kMlpIn, L.X.p, L.Wt[0].p, P.b[0], true, true, L.H0.p, s))) return rc;
-  if ((rc = bf16_linear((int)B, kMlpHidden, kMlpHidden, L.H0.p, L.Wt[1].p, P.b[1], true, true, L.H1.p, s))) return rc;
-  if ((rc = bf16_linear((int)B, kMlpHidden, kMlpHidden, L.H1.p, L.Wt[2].p, P.b[2], true, true, L.H0.p, s))) return rc;
-  if ((rc = bf16_linear((int)B, kMlpOut, kMlpHidden, L.H0.p, L.Wt[3].p, P.b[3], false, false, Y, s))) return rc;
+  if ((rc = L.forward_bf16(B, s))) return rc;
+  LPG_CUDA_TRY(cudaMemcpyAsync(Y, L.out.p, sizeof(float) * B * kMlpOut, cudaMemcpyDeviceToDevice, s));
+  if ((rc = L.check_tc(s))) return rc;
   LPG_CUDA_TRY(cudaStreamSynchronize(s));
   return LPG_OK;
   LPG_GUARD_END

@@ -15,6 +15,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <type_traits>
 
@@ -25,7 +26,8 @@ namespace lpg {
 int LearnedSmoother::load(const float* hostParams, cudaStream_t s) {
   int rc;
   if ((rc = params.alloc(kMlpParams)) || (rc = params.upload(hostParams, kMlpParams, s))) return rc;
-  if ((rc = red.alloc(1)) || (rc = partials.alloc(kReducePartials))) return rc;
+  if ((rc = red.alloc(1)) || (rc = partials.alloc(kReducePartials)) || (rc = tcErr.alloc(1))) return rc;
+  LPG_CUDA_TRY(cudaMemsetAsync(tcErr.p, 0, sizeof(int), s));
   MLPParams P = MLPParams::view(params.p);
   const int dims[5] = {kMlpIn, kMlpHidden, kMlpHidden, kMlpHidden, kMlpOut};
   for (int l = 0; l < 4; ++l) {
@@ -34,6 +36,35 @@ int LearnedSmoother::load(const float* hostParams, cudaStream_t s) {
   }
   LPG_CUDA_TRY(cudaStreamSynchronize(s));
   ready = true;
+  return LPG_OK;
+}
+
+// out (rows x 512) = MLP(X (rows x 896)): the fused tcgen05 kernel, or with
+// LPG_MLP_TC=off (a tuning override) the per-layer mma.sync kernels
+int LearnedSmoother::forward_bf16(int64_t rows, cudaStream_t s) {
+  static const bool layered = [] {
+    const char* e = std::getenv("LPG_MLP_TC");
+    return e && !std::strcmp(e, "off");
+  }();
+  MLPParams P = MLPParams::view(params.p);
+  int rc;
+  if (!layered) {
+    const __nv_bfloat16* w[4] = {Wt[0].p, Wt[1].p, Wt[2].p, Wt[3].p};
+    const float* bias[4] = {P.b[0], P.b[1], P.b[2], P.b[3]};
+    return mlp_forward_tc(rows, X.p, w, bias, out.p, tcErr.p, s);
+  }
+  if ((rc = bf16_linear((int)rows, kMlpHidden, kMlpIn, X.p, Wt[0].p, P.b[0], true, true, H0.p, s))) return rc;
+  if ((rc = bf16_linear((int)rows, kMlpHidden, kMlpHidden, H0.p, Wt[1].p, P.b[1], true, true, H1.p, s))) return rc;
+  if ((rc = bf16_linear((int)rows, kMlpHidden, kMlpHidden, H1.p, Wt[2].p, P.b[2], true, true, H0.p, s))) return rc;
+  return bf16_linear((int)rows, kMlpOut, kMlpHidden, H0.p, Wt[3].p, P.b[3], false, false, out.p, s);
+}
+
+// the tensor-core pipeline's timeout flag (waits for the stream)
+int LearnedSmoother::check_tc(cudaStream_t s) {
+  int code = 0;
+  int rc = tcErr.download(&code, 1, s);
+  if (rc) return rc;
+  if (code) return set_error(LPG_ERR_CUDA, "MLP tensor-core pipeline timed out (code " + std::to_string(code) + ")");
   return LPG_OK;
 }
 
@@ -68,13 +99,10 @@ int LearnedSmoother::apply(const BoxNumbering& b, int64_t E, const int32_t* g2l,
   for (int64_t e0 = 0; e0 < E; e0 += C) {
     const int64_t n = std::min<int64_t>(C, E - e0);
     if ((rc = element_features<T, __nv_bfloat16>(b, E, e0, n, g2l, r, X.p, scale.p, sfloor, s))) return rc;
-    if ((rc = bf16_linear((int)n, kMlpHidden, kMlpIn, X.p, Wt[0].p, P.b[0], true, true, H0.p, s))) return rc;
-    if ((rc = bf16_linear((int)n, kMlpHidden, kMlpHidden, H0.p, Wt[1].p, P.b[1], true, true, H1.p, s))) return rc;
-    if ((rc = bf16_linear((int)n, kMlpHidden, kMlpHidden, H1.p, Wt[2].p, P.b[2], true, true, H0.p, s))) return rc;
-    if ((rc = bf16_linear((int)n, kMlpOut, kMlpHidden, H0.p, Wt[3].p, P.b[3], false, false, out.p, s))) return rc;
+    if ((rc = forward_bf16(n, s))) return rc;
     if ((rc = apply_correction<T>(Np, n, e0, g2l, out.p, scale.p, invDiag, weight, z, s))) return rc;
   }
-  return LPG_OK;
+  return check_tc(s);
 }
 template int LearnedSmoother::apply<double>(const BoxNumbering&, int64_t, const int32_t*, const double*, const double*,
                                             const double*, double*, int64_t, cudaStream_t);

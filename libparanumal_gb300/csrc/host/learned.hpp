@@ -18,9 +18,12 @@ struct LearnedSmoother {
   DevBuf<__nv_bfloat16> Wt[4];              // BF16 transposed weights for inference
   DevBuf<__nv_bfloat16> X, H0, H1;
   DevBuf<float> out, scale;
+  DevBuf<int> tcErr;                        // timeout flag of the tensor-core kernel
   int64_t chunk = 0;
   int load(const float* hostParams, cudaStream_t s);
   int ensure_chunk(int64_t rows);
+  int forward_bf16(int64_t rows, cudaStream_t s);   // out = MLP(X) for `rows` rows
+  int check_tc(cudaStream_t s);
   // z (assembled, overwritten) = weighted average over copies of s_e invDiag .* MLP(features(r))
   template <typename T>
   int apply(const BoxNumbering& b, int64_t E, const int32_t* g2l, const T* r, const double* invDiag,

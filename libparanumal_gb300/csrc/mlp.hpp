@@ -63,6 +63,12 @@ int adam_step(int64_t n, float* w, const float* g, float* m, float* v, float lr,
 int bf16_linear(int M, int N, int K, const __nv_bfloat16* X, const __nv_bfloat16* Wt, const float* bias, bool gelu,
                 bool outBf16, void* Y, cudaStream_t s);
 int transpose_to_bf16(int K, int N, const float* W, __nv_bfloat16* Wt, cudaStream_t s);
+// Fused inference Y (B x 512, FP32) = MLP(X (B x 896, BF16)) on the tcgen05 tensor cores
+// (all four layers per 128-row tile on one SM). Wt[l]: BF16 weights stored N x K (K
+// contiguous), bias[l] FP32. errFlag (device int) is set to a nonzero code if a CTA's
+// pipeline timed out; the caller reads it after the stream has run.
+int mlp_forward_tc(int64_t B, const __nv_bfloat16* X, const __nv_bfloat16* const Wt[4], const float* const bias[4],
+                   float* Y, int* errFlag, cudaStream_t s);
 
 template <typename TIN, typename TOUT>
 // scale_e = max(RMS of the element's residual, sfloor); features = values / scale_e

@@ -1,0 +1,407 @@
+// Fused inference of the learned smoother's MLP (896 -> 256 -> 256 -> 256 -> 512, GELU)
+// on the 5th-generation tensor cores: tcgen05.mma (kind::f16, BF16 operands, FP32
+// accumulators in tensor memory), operands staged by TMA (cp.async.bulk.tensor) with
+// 128-byte swizzle, one CTA per SM walking 128-row tiles.
+//
+// Per tile the four layers run back to back without leaving the SM: layer 0 streams the
+// tile's input rows and W0 in 64-wide K blocks through a 3-stage ring; the hidden
+// activations go TMEM -> registers (bias, GELU, BF16) -> shared memory, where they are
+// the A operand of the next layer; the output layer's two 256-column halves fill all
+// 512 TMEM columns and are written to global memory in FP32. The weights (985 KB in
+// BF16) stay L2-resident across tiles.
+//
+// Warp roles (320 threads): warp 0 lane 0 issues TMA loads, warp 1 owns TMEM and its
+// lane 0 issues the MMAs, warps 2-9 run the epilogue (warp w reads TMEM lanes
+// 32 (w % 4) .. +31, one row per thread, and half of the columns: warps 2-5 the first,
+// 6-9 the second). Stages are handed over with mbarriers;
+// every wait is bounded by %globaltimer, and on a timeout the CTA records an error code,
+// waits (bounded) for its own copies and MMAs in flight, frees TMEM and returns.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <mutex>
+
+#include "lpg_common.cuh"
+#include "lpg_internal.hpp"
+#include "mlp.hpp"
+
+namespace lpg {
+namespace {
+
+constexpr int TM = 128;                         // rows per tile (MMA M)
+constexpr int TK = 64;                          // K block: 64 BF16 = one 128-byte swizzle row
+constexpr int NSTAGE = 3;
+constexpr int A_BYTES = TM * TK * 2;            // 16 KB
+constexpr int B_BYTES = 256 * TK * 2;           // 32 KB (N = 256 rows of W^T)
+constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
+constexpr int H_BYTES = TM * kMlpHidden * 2;    // hidden activations, 4 K blocks of 16 KB
+constexpr int NBIAS = 3 * kMlpHidden + kMlpOut;
+constexpr int L0_STEPS = kMlpIn / TK;           // 14
+constexpr int LH_STEPS = kMlpHidden / TK;       // 4
+constexpr int TILE_STEPS = L0_STEPS + 2 * LH_STEPS + 2 * LH_STEPS;
+constexpr int NBAR = 2 * NSTAGE + 4;            // full[], empty[], acc, hready, tfree, drain
+constexpr int SMEM_BYTES = 1024 + NSTAGE * STAGE_BYTES + H_BYTES + NBIAS * 4 + NBAR * 8 + 16;
+constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s per wait
+constexpr int EPI_WARPS = 8, THREADS = 32 * (2 + EPI_WARPS);
+static_assert(kMlpIn % TK == 0 && kMlpHidden == 256 && kMlpOut == 512, "layer shapes");
+
+// instruction descriptor of tcgen05.mma kind::f16: D FP32 (bits 4-5 = 1), A and B BF16
+// (bits 7-9, 10-12 = 1), both K-major, N >> 3 at bits 17-22, M >> 4 at bits 24-28
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((256u >> 3) << 17) | ((uint32_t)(TM >> 4) << 24);
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ unsigned long long gtimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+// waits until the phase of the given parity has completed; false after kWaitNs
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  const unsigned long long t0 = gtimer();
+  while (true) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if (gtimer() - t0 > kWaitNs) return false;
+  }
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, uint32_t bar, int x, int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(dst),
+      "l"((uint64_t)map), "r"(bar), "r"(x), "r"(y)
+      : "memory");
+}
+
+// shared-memory matrix descriptor: K-major operand in 128-byte swizzled rows, 8-row
+// groups 1024 bytes apart (stride byte offset), descriptor version 1 (bit 46)
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+  uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)1 << 16;               // leading byte offset (unused with 128-byte swizzle)
+  d |= (uint64_t)(1024 >> 4) << 32;     // stride byte offset
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)2 << 61;               // 128-byte swizzle
+  return d;
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+          tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate));
+}
+__device__ __forceinline__ void umma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// 32 consecutive FP32 columns of this thread's TMEM lane
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int c = 0; c < 32; ++c) v[c] = __uint_as_float(r[c]);
+}
+
+// GELU (tanh form) with the hardware tanh approximation (relative error ~2^-11, below
+// the BF16 rounding of the activations it produces)
+__device__ __forceinline__ float gelu_approx(float z) {
+  const float u = 0.7978845608028654f * (z + 0.044715f * z * z * z);
+  float t;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(u));
+  return 0.5f * z * (1.0f + t);
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+  const __nv_bfloat162 p = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<const uint32_t*>(&p);
+}
+
+struct TcMaps {
+  CUtensorMap x, w[4];
+};
+
+__global__ void __launch_bounds__(THREADS, 1)
+mlp_tc_kernel(const __grid_constant__ TcMaps maps, const float* __restrict__ b0, const float* __restrict__ b1,
+              const float* __restrict__ b2, const float* __restrict__ b3, float* __restrict__ Y, const int64_t rows,
+              const int ntiles, int* __restrict__ err) {
+  extern __shared__ unsigned char smem_raw[];
+  // 128-byte swizzled operands need 1024-byte aligned shared-memory offsets
+  unsigned char* smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+  unsigned char* stage0 = smem;
+  unsigned char* hbuf = smem + NSTAGE * STAGE_BYTES;
+  float* s_bias = reinterpret_cast<float*>(hbuf + H_BYTES);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(s_bias + NBIAS);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + NBAR);
+  __shared__ volatile int s_abort;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  auto full = [&](int s) { return smem_u32(&bars[s]); };
+  auto empty = [&](int s) { return smem_u32(&bars[NSTAGE + s]); };
+  const uint32_t accBar = smem_u32(&bars[2 * NSTAGE]), hBar = smem_u32(&bars[2 * NSTAGE + 1]);
+  const uint32_t freeBar = smem_u32(&bars[2 * NSTAGE + 2]), drainBar = smem_u32(&bars[2 * NSTAGE + 3]);
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < NSTAGE; ++s) {
+      mbar_init(full(s), 1);
+      mbar_init(empty(s), 1);
+    }
+    mbar_init(accBar, 1);
+    mbar_init(hBar, 32 * EPI_WARPS);
+    mbar_init(freeBar, 32 * EPI_WARPS);
+    mbar_init(drainBar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    s_abort = 0;
+  }
+  for (int t = threadIdx.x; t < NBIAS; t += blockDim.x)
+    s_bias[t] = t < 256 ? b0[t] : t < 512 ? b1[t - 256] : t < 768 ? b2[t - 512] : b3[t - 768];
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(512)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  auto fail = [&](int code) {
+    s_abort = 1;
+    atomicCAS(err, 0, code);
+  };
+  // control flow stays uniform in every warp: lane 0 waits (or reads the abort flag) and
+  // broadcasts the outcome, so whole warps take the same branches and reach the final
+  // barrier together
+  constexpr unsigned FULLMASK = 0xffffffffu;
+  auto wait0 = [&](uint32_t bar, uint32_t parity) {
+    int ok = 1;
+    if (lane == 0) ok = mbar_wait(bar, parity) ? 1 : 0;
+    return __shfl_sync(FULLMASK, ok, 0) != 0;
+  };
+  auto aborted = [&]() { return __shfl_sync(FULLMASK, lane == 0 ? (int)s_abort : 0, 0) != 0; };
+  // every lane observes the barrier itself (the epilogue lanes then read TMEM)
+  auto waitAll = [&](uint32_t bar, uint32_t parity) { return __all_sync(FULLMASK, mbar_wait(bar, parity) ? 1 : 0) != 0; };
+
+  if (warp == 0) {
+    // ------------------------------------------------------------ TMA producer (lane 0 issues)
+    int64_t step = 0;
+    for (int tile = blockIdx.x; tile < ntiles && !aborted(); tile += gridDim.x) {
+      const int row0 = tile * TM;
+      bool stop = false;
+      for (int st = 0; st < TILE_STEPS; ++st, ++step) {
+        const int s = (int)(step % NSTAGE);
+        if (!wait0(empty(s), (uint32_t)(((step / NSTAGE) & 1) ^ 1))) {
+          if (lane == 0) fail(1);
+          stop = true;
+          break;
+        }
+        if (lane == 0) {
+          const uint32_t a = smem_u32(stage0 + s * STAGE_BYTES), b = a + A_BYTES;
+          if (st < L0_STEPS) {
+            mbar_expect_tx(full(s), A_BYTES + B_BYTES);
+            tma_load_2d(a, &maps.x, full(s), st * TK, row0);
+            tma_load_2d(b, &maps.w[0], full(s), st * TK, 0);
+          } else {
+            const int r = st - L0_STEPS;            // W1 (4 blocks), W2 (4), W3 half 0 (4), half 1 (4)
+            const int layer = 1 + (r < 8 ? r / 4 : 2);
+            const int kb = r % 4, nh = (r >= 12) ? 1 : 0;
+            mbar_expect_tx(full(s), B_BYTES);
+            tma_load_2d(b, &maps.w[layer], full(s), kb * TK, nh * 256);
+          }
+        }
+        __syncwarp();
+      }
+      if (stop) break;
+    }
+    // every issued copy has landed before the CTA can exit (bounded)
+    for (int64_t k = (step > NSTAGE ? step - NSTAGE : 0); k < step; ++k)
+      if (!wait0(full((int)(k % NSTAGE)), (uint32_t)((k / NSTAGE) & 1)) && lane == 0) fail(2);
+  } else if (warp == 1) {
+    // ------------------------------------------------------------ MMA issuer (lane 0 issues)
+    int64_t step = 0;
+    uint32_t hcount = 0, tiles = 0;
+    bool stop = false;
+    for (int tile = blockIdx.x; tile < ntiles && !stop && !aborted(); tile += gridDim.x) {
+      for (int layer = 0; layer < 4 && !stop; ++layer) {
+        if (layer == 0 && tiles > 0 && !wait0(freeBar, (tiles - 1) & 1)) { if (lane == 0) fail(3); stop = true; break; }
+        if (layer > 0 && !wait0(hBar, hcount++ & 1)) { if (lane == 0) fail(4); stop = true; break; }
+        if (aborted()) { stop = true; break; }
+        tc_fence_after();
+        const int nsteps = layer == 0 ? L0_STEPS : (layer == 3 ? 2 * LH_STEPS : LH_STEPS);
+        for (int st = 0; st < nsteps; ++st, ++step) {
+          const int s = (int)(step % NSTAGE);
+          if (!wait0(full(s), (uint32_t)((step / NSTAGE) & 1))) { if (lane == 0) fail(5); stop = true; break; }
+          tc_fence_after();
+          if (lane == 0) {
+            const int kb = (layer == 3) ? (st % LH_STEPS) : st;
+            const uint32_t bAddr = smem_u32(stage0 + s * STAGE_BYTES) + A_BYTES;
+            const uint32_t aAddr =
+                layer == 0 ? smem_u32(stage0 + s * STAGE_BYTES) : smem_u32(hbuf) + kb * (TM * TK * 2);
+            const uint32_t dcol = layer == 1 ? 256u : (layer == 3 ? 256u * (uint32_t)(st / LH_STEPS) : 0u);
+#pragma unroll
+            for (int kk = 0; kk < TK / 16; ++kk)
+              umma_bf16(tmem + dcol, sw128_desc(aAddr + kk * 32), sw128_desc(bAddr + kk * 32),
+                        (kb > 0 || kk > 0) ? 1u : 0u);
+            umma_commit(empty(s));   // the stage is free once these MMAs have read it
+          }
+          __syncwarp();
+        }
+        if (stop) break;
+        if (lane == 0) umma_commit(accBar);   // this layer's accumulator is complete
+        __syncwarp();
+      }
+      ++tiles;
+    }
+    // no MMA may still run when TMEM is released (bounded)
+    if (lane == 0) umma_commit(drainBar);
+    __syncwarp();
+    if (!wait0(drainBar, 0) && lane == 0) fail(6);
+  } else {
+    // ------------------------------------------------------------ epilogue (warps 2-9)
+    const int q = warp & 3;
+    const int half = (warp - 2) / 4;  // which half of the columns this warp converts
+    const int rloc = 32 * q + lane;   // the tile row this thread owns (TMEM lane)
+    const uint32_t tlane = tmem + ((uint32_t)(32 * q) << 16);
+    uint32_t lc = 0;
+    bool stop = false;
+    for (int tile = blockIdx.x; tile < ntiles && !stop && !aborted(); tile += gridDim.x) {
+      const int64_t row = (int64_t)tile * TM + rloc;
+      for (int layer = 0; layer < 4; ++layer) {
+        if (!waitAll(accBar, lc++ & 1)) { if (lane == 0) fail(7); stop = true; break; }
+        tc_fence_after();
+        float v[32];
+        if (layer < 3) {
+          const uint32_t dcol = layer == 1 ? 256u : 0u;
+          const float* bias = s_bias + layer * 256;
+          for (int c0 = half * (kMlpHidden / 2); c0 < (half + 1) * (kMlpHidden / 2); c0 += 32) {
+            tmem_ld32(tlane + dcol + c0, v);
+            // columns c0..c0+31 -> K block c0/64, 16-byte chunks (c0%64)/8 .. +3 of row rloc,
+            // placed with the 128-byte swizzle (chunk ^ (row & 7)) the MMA descriptor expects
+            unsigned char* rowp = hbuf + (c0 / TK) * (TM * TK * 2) + rloc * 128;
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+              const int chunk = ((c0 % TK) / 8 + t) ^ (rloc & 7);
+              const float* bb = bias + c0 + 8 * t;
+              uint4 w;
+              w.x = pack_bf16(gelu_approx(v[8 * t + 0] + bb[0]), gelu_approx(v[8 * t + 1] + bb[1]));
+              w.y = pack_bf16(gelu_approx(v[8 * t + 2] + bb[2]), gelu_approx(v[8 * t + 3] + bb[3]));
+              w.z = pack_bf16(gelu_approx(v[8 * t + 4] + bb[4]), gelu_approx(v[8 * t + 5] + bb[5]));
+              w.w = pack_bf16(gelu_approx(v[8 * t + 6] + bb[6]), gelu_approx(v[8 * t + 7] + bb[7]));
+              *reinterpret_cast<uint4*>(rowp + chunk * 16) = w;
+            }
+          }
+          // the generic-proxy writes of H become visible to the tensor cores' async proxy
+          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+          tc_fence_before();
+          mbar_arrive(hBar);
+        } else {
+          const float* bias = s_bias + 3 * 256;
+          for (int c0 = half * (kMlpOut / 2); c0 < (half + 1) * (kMlpOut / 2); c0 += 32) {
+            tmem_ld32(tlane + c0, v);
+            if (row < rows) {
+              float4* dst = reinterpret_cast<float4*>(Y + row * kMlpOut + c0);
+#pragma unroll
+              for (int t = 0; t < 8; ++t)
+                dst[t] = make_float4(v[4 * t] + bias[c0 + 4 * t], v[4 * t + 1] + bias[c0 + 4 * t + 1],
+                                     v[4 * t + 2] + bias[c0 + 4 * t + 2], v[4 * t + 3] + bias[c0 + 4 * t + 3]);
+            }
+          }
+          tc_fence_before();
+          mbar_arrive(freeBar);
+        }
+      }
+    }
+  }
+
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 1)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512) : "memory");
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  });
+  return fn;
+}
+
+// 2D BF16 map of a row-major [outer x inner] matrix, box [boxOuter x 64], 128-byte swizzle
+int make_map(CUtensorMap* m, const void* base, uint64_t inner, uint64_t outer, uint32_t boxOuter) {
+  auto fn = encode_fn();
+  if (!fn) return set_error(LPG_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+  const cuuint64_t dims[2] = {inner, outer};
+  const cuuint64_t strides[1] = {inner * 2};
+  const cuuint32_t box[2] = {(cuuint32_t)TK, boxOuter};
+  const cuuint32_t estr[2] = {1, 1};
+  const CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return set_error(LPG_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+  return LPG_OK;
+}
+
+}  // namespace
+
+int mlp_forward_tc(int64_t B, const __nv_bfloat16* X, const __nv_bfloat16* const Wt[4], const float* const bias[4],
+                   float* Y, int* errFlag, cudaStream_t s) {
+  if (B <= 0) return LPG_OK;
+  if (B > (int64_t)INT32_MAX - TM) return set_error(LPG_ERR_INVALID, "mlp tc: too many rows");
+  auto al16 = [](const void* p) { return ((uintptr_t)p & 15) == 0; };
+  if (!al16(X) || !al16(Wt[0]) || !al16(Wt[1]) || !al16(Wt[2]) || !al16(Wt[3]) || !al16(Y))
+    return set_error(LPG_ERR_INVALID, "mlp tc: operands must be 16-byte aligned");
+  TcMaps maps;
+  int rc;
+  if ((rc = make_map(&maps.x, X, kMlpIn, (uint64_t)B, TM)) || (rc = make_map(&maps.w[0], Wt[0], kMlpIn, kMlpHidden, 256)) ||
+      (rc = make_map(&maps.w[1], Wt[1], kMlpHidden, kMlpHidden, 256)) ||
+      (rc = make_map(&maps.w[2], Wt[2], kMlpHidden, kMlpHidden, 256)) ||
+      (rc = make_map(&maps.w[3], Wt[3], kMlpHidden, kMlpOut, 256)))
+    return rc;
+  static int numSMs = 0;
+  if (!numSMs) {
+    int dev = 0;
+    LPG_CUDA_TRY(cudaGetDevice(&dev));
+    LPG_CUDA_TRY(cudaDeviceGetAttribute(&numSMs, cudaDevAttrMultiProcessorCount, dev));
+    LPG_CUDA_TRY(cudaFuncSetAttribute(mlp_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+  }
+  const int ntiles = (int)((B + TM - 1) / TM);
+  const int grid = ntiles < numSMs ? ntiles : numSMs;
+  LPG_CUDA_TRY(cudaMemsetAsync(errFlag, 0, sizeof(int), s));
+  mlp_tc_kernel<<<grid, THREADS, SMEM_BYTES, s>>>(maps, bias[0], bias[1], bias[2], bias[3], Y, B, ntiles, errFlag);
+  LPG_LAUNCH_CHECK("mlp_tc_kernel");
+  return LPG_OK;
+}
+
+}  // namespace lpg
