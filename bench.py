@@ -60,6 +60,7 @@ def parse():
     ap.add_argument("--train-epochs", type=int, default=40)
     ap.add_argument("--rhs", default="sine", choices=["sine", "gauss"],
                     help="learned mode: manufactured sine data or 16 Gaussian sources (seed 3)")
+    ap.add_argument("--learned-steps", type=int, default=2, help="LEARNED SMOOTHER STEPS of the learned solve")
     ap.add_argument("--train-pairs", default="MIXED", choices=["MIXED", "TRAJECTORY"],
                     help="SMOOTHER TRAINING PAIRS of the training problem")
     return ap.parse_args()
@@ -233,12 +234,13 @@ def run_learned(a):
     out = {"workload": "learned fine smoother: train %d^3, solve %d^3 jittered hex N=7 lognormal lambda, %s rhs"
                        % (a.train_nx, a.nx, "manufactured sine" if a.rhs == "sine" else "16 Gaussian sources"),
            "train_seconds": t_train, "train_samples": a.train_samples, "train_epochs": a.train_epochs,
-           "train_pairs": a.train_pairs,
+           "train_pairs": a.train_pairs, "learned_steps": a.learned_steps,
            "loss_first": float(hist[0]), "loss_last": float(hist[-1]), "results": {}}
     x64 = None
     for name, prec, learned in (("FP64", "FP64", False), ("FP32", "FP32", False), ("learned+FP32", "FP32", True)):
         t1 = time.time()
-        e = lpg.Elliptic(solve_settings(a.nx, 7, prec, **law, **rhs))
+        extra = {"LEARNED SMOOTHER STEPS": a.learned_steps} if learned else {}
+        e = lpg.Elliptic(solve_settings(a.nx, 7, prec, **law, **rhs, **extra))
         setup = time.time() - t1
         if learned:
             e.set_learned_smoother(w, 0.5)

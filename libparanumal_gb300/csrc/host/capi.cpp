@@ -147,6 +147,9 @@ int build(lpg_elliptic* h) {
     o.amgChebDegree = S.geti("PARALMOND CHEBYSHEV DEGREE", 2);
     o.amgUnsmoothed = S.is("PARALMOND AGGREGATION", "UNSMOOTHED");
     o.amgRugeStuben = S.is("PARALMOND STRENGTH", "RUGESTUBEN");
+    o.learnedSteps = S.geti("LEARNED SMOOTHER STEPS", 2);
+    if (o.learnedSteps < 1 || o.learnedSteps > 8)
+      return set_error(LPG_ERR_SETTINGS, "LEARNED SMOOTHER STEPS must be 1..8");
     if (S.get("PARALMOND CYCLE", "VCYCLE") != "VCYCLE")
       return set_error(LPG_ERR_UNSUPPORTED, "PARALMOND CYCLE must be VCYCLE");
     h->precon = make_multigrid(el, c, o, &rc);

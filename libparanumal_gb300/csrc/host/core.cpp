@@ -46,7 +46,8 @@ static const char* kKnownKeys[] = {
     // additions
     "MULTIGRID DEGREES", "PRECONDITIONER PRECISION", "FINE SMOOTHER", "MESH JITTER",
     "MESH JITTER SEED", "LAMBDA FIELD", "LAMBDA SEED", "RHS FIELD", "RHS SEED", "RHS SOURCES",
-    "SOLVER TOLERANCE", "MAXIMUM ITERATIONS", "SMOOTHER TRAINING PAIRS"};
+    "SOLVER TOLERANCE", "MAXIMUM ITERATIONS", "SMOOTHER TRAINING PAIRS",
+    "LEARNED SMOOTHER STEPS"};
 
 int Settings::parse(const std::string& text) {
   kv.clear();

@@ -80,8 +80,8 @@ int LearnedSmoother::ensure_chunk(int64_t rows) {
 
 // z = average over shared nodes of s_e * invDiag .* MLP(features(r))
 template <typename T>
-int LearnedSmoother::apply(const BoxNumbering& b, int64_t E, const int32_t* g2l, const T* r, const double* invDiag,
-                           const double* weight, T* z, int64_t Nglobal, cudaStream_t s) {
+int LearnedSmoother::apply(const BoxNumbering& b, int64_t E, const int32_t* g2l, const T* r, const T* coef, T* z,
+                           int64_t Nglobal, cudaStream_t s) {
   if (!ready) return set_error(LPG_ERR_INVALID, "learned smoother has no weights");
   const int Np = (b.N + 1) * (b.N + 1) * (b.N + 1);
   int rc;
@@ -100,14 +100,14 @@ int LearnedSmoother::apply(const BoxNumbering& b, int64_t E, const int32_t* g2l,
     const int64_t n = std::min<int64_t>(C, E - e0);
     if ((rc = element_features<T, __nv_bfloat16>(b, E, e0, n, g2l, r, X.p, scale.p, sfloor, s))) return rc;
     if ((rc = forward_bf16(n, s))) return rc;
-    if ((rc = apply_correction<T>(Np, n, e0, g2l, out.p, scale.p, invDiag, weight, z, s))) return rc;
+    if ((rc = apply_correction<T>(Np, n, e0, g2l, out.p, scale.p, coef, z, s))) return rc;
   }
   return check_tc(s);
 }
 template int LearnedSmoother::apply<double>(const BoxNumbering&, int64_t, const int32_t*, const double*, const double*,
-                                            const double*, double*, int64_t, cudaStream_t);
-template int LearnedSmoother::apply<float>(const BoxNumbering&, int64_t, const int32_t*, const float*, const double*,
-                                           const double*, float*, int64_t, cudaStream_t);
+                                            double*, int64_t, cudaStream_t);
+template int LearnedSmoother::apply<float>(const BoxNumbering&, int64_t, const int32_t*, const float*, const float*,
+                                           float*, int64_t, cudaStream_t);
 
 // ---------------------------------------------------------------- training
 double lastKeptFraction = 0;
@@ -304,15 +304,28 @@ int train_smoother(Platform* plat, Elliptic* el, Precon* plainMG, const BoxNumbe
   lossHistory.clear();
   int step = 0;
   const int64_t nb = total / B;
+  // minibatches: a fresh random permutation of all samples every epoch (the samples are
+  // stored grouped by sample set); learning rate with cosine decay to 5 % of o.lr
+  DevBuf<int32_t> perm;
+  DevBuf<float> Xb, Tb;
+  if ((rc = perm.alloc(total)) || (rc = Xb.alloc((int64_t)B * kMlpIn)) || (rc = Tb.alloc((int64_t)B * kMlpOut))) return rc;
+  std::vector<int32_t> order(total);
+  for (int64_t i = 0; i < total; ++i) order[i] = (int32_t)i;
+  const int64_t totalSteps = std::max<int64_t>(1, (int64_t)o.epochs * nb);
   for (int ep = 0; ep < o.epochs; ++ep) {
+    for (int64_t i = total - 1; i > 0; --i) std::swap(order[i], order[(int64_t)(rng.next() * (double)(i + 1)) % (i + 1)]);
+    if ((rc = perm.upload(order.data(), total, s))) return rc;
     double epLoss = 0;
     for (int64_t bi = 0; bi < nb; ++bi) {
-      const float* Xb = Xtr.p + bi * B * kMlpIn;
-      const float* Tb = Ttr.p + bi * B * kMlpOut;
-      if ((rc = mlp_forward_f32(P, B, Xb, A, s))) return rc;
-      if ((rc = mse_loss((int64_t)B * kMlpOut, B, A.A[3], Tb, dY.p, loss.p, s))) return rc;
-      if ((rc = mlp_backward_f32(P, B, Xb, A, dY.p, Gp, w0buf.p, w1buf.p, s))) return rc;
-      if ((rc = adam_step(kMlpParams, W.p, G.p, M1.p, M2.p, o.lr, ++step, s))) return rc;
+      if ((rc = gather_rows_w(B, kMlpIn, perm.p + bi * B, Xtr.p, Xb.p, s)) ||
+          (rc = gather_rows_w(B, kMlpOut, perm.p + bi * B, Ttr.p, Tb.p, s)))
+        return rc;
+      const double frac = (double)step / (double)totalSteps;
+      const float lr = (float)(o.lr * (0.05 + 0.95 * 0.5 * (1.0 + std::cos(3.14159265358979323846 * frac))));
+      if ((rc = mlp_forward_f32(P, B, Xb.p, A, s))) return rc;
+      if ((rc = mse_loss((int64_t)B * kMlpOut, B, A.A[3], Tb.p, dY.p, loss.p, s))) return rc;
+      if ((rc = mlp_backward_f32(P, B, Xb.p, A, dY.p, Gp, w0buf.p, w1buf.p, s))) return rc;
+      if ((rc = adam_step(kMlpParams, W.p, G.p, M1.p, M2.p, lr, ++step, s))) return rc;
       float lh;
       if ((rc = loss.download(&lh, 1, s))) return rc;
       epLoss += lh;

@@ -440,11 +440,14 @@ class MultiGrid : public Precon {
   DevBuf<double> aRhs0, aX0;
   DevBuf<float> in32, out32;
 
-  // learned fine-level smoother
+  // learned fine-level smoother; per fine dof: lcoef = weight / diag (the network
+  // correction's scaling) and ljac = (4/3/rho) / diag (its damped-Jacobi part), FP64 and FP32
   LearnedSmoother* learned = nullptr;
   BoxNumbering box{};
   double threshold = 0.5;
   int64_t nFallback = 0, nVcycle = 0;
+  DevBuf<double> lcoef64, ljac64;
+  DevBuf<float> lcoef32, ljac32;
 
   int levels_p() const override { return (int)p.size(); }
   int levels_amg() const override { return (int)a.size(); }
@@ -462,6 +465,21 @@ class MultiGrid : public Precon {
     box = b;
     threshold = thr;
     nFallback = nVcycle = 0;
+    if (!L) return LPG_OK;
+    // 1/diag of the fine level (the damped-Jacobi smoother stores it pre-scaled by 4/3/rho)
+    PLevel& F = *p[0];
+    const int64_t N = fine->Nglobal;
+    const double unscale = (opt.smoother == 1) ? 1.0 / F.lambda0 : 1.0;
+    const double jw = fine_rho() > 0 ? (4.0 / 3.0) / fine_rho() : 0.0;
+    cudaStream_t s = plat->stream;
+    int rc;
+    if ((rc = lcoef64.alloc(N)) || (rc = ljac64.alloc(N)) || (rc = lcoef32.alloc(N)) || (rc = ljac32.alloc(N)))
+      return rc;
+    if ((rc = amxpy<double>(N, unscale, F.invDiag64.p, fine->weightG.p, 0.0, lcoef64.p, s)) ||
+        (rc = axpy<double>(N, unscale * jw, F.invDiag64.p, 0.0, ljac64.p, s)) ||
+        (rc = convert<double, float>(N, lcoef64.p, lcoef32.p, s)) || (rc = convert<double, float>(N, ljac64.p, ljac32.p, s)))
+      return rc;
+    LPG_CUDA_TRY(cudaStreamSynchronize(s));
     return LPG_OK;
   }
 
@@ -605,12 +623,12 @@ int MultiGrid::dot_host(int64_t n, const T* x, const T* y, double& out, cudaStre
 }
 
 // V-cycle whose fine-level smoother is S(r) = (4/3/rho) D^{-1} r + L(r), a damped-Jacobi
-// step plus the learned element-local correction L, each smoothing correction c taken
-// with the energy-optimal step w = (c.r)/(c.Ac) (w = 0 if c.Ac <= 0):
-//   X = w1 S(RHS); X += coarse correction of RHS - A X; X += w2 S(RHS - A X).
-// The products A c come from the operator applications the cycle needs anyway (the
-// final residual is RES - w2 A c2). If the V-cycle leaves ||RHS - A X|| > threshold
-// ||RHS||, it is redone with the plain smoother (fallback), and the fallback is counted.
+// step plus the learned element-local correction L. A smoothing step takes c = S(RES)
+// with the energy-optimal step w = (c.RES)/(c.Ac) (w = 0 if c.Ac <= 0): X += w c,
+// RES -= w A c. Pre- and post-smoothing are opt.learnedSteps such steps around the
+// coarse correction (X = 0, RES = RHS at the start). If the V-cycle leaves
+// ||RHS - A X|| > threshold ||RHS||, it is redone with the plain smoother (fallback),
+// and the fallback is counted.
 template <typename T>
 int MultiGrid::vcycle_learned(const T* RHS, T* X, cudaStream_t s) {
   PLevel& L = *p[0];
@@ -619,27 +637,28 @@ int MultiGrid::vcycle_learned(const T* RHS, T* X, cudaStream_t s) {
   T* RES = vec<T>(L.res64, L.res32);
   T* AD = vec<T>(s64[1], s32[1]);
   T* D = vec<T>(s64[2], s32[2]);
-  const T* invDiag = vec<T>(L.invDiag64, L.invDiag32);
-  const double jacobiW = fine_rho() > 0 ? (4.0 / 3.0) / fine_rho() : 0.0;
-  auto step = [](double cr, double cAc) { return (cAc > 0 && std::isfinite(cr) && std::isfinite(cAc)) ? cr / cAc : 0.0; };
+  const T* coef = vec<T>(lcoef64, lcoef32);
+  const T* jac = vec<T>(ljac64, ljac32);
   int rc;
-  double cr, cAc;
-  // pre-smoothing: X = w1 c1, RES = RHS - w1 A c1
-  if ((rc = learned->apply<T>(box, E, el->g2l.p, RHS, L.invDiag64.p, el->weightG.p, X, N, s))) return rc;
-  if (jacobiW > 0 && (rc = amxpy<T>(N, (T)jacobiW, invDiag, RHS, T(1), X, s))) return rc;
-  if ((rc = op<T>(el, X, RES, s))) return rc;
-  if ((rc = dot_host<T>(N, X, RHS, cr, s)) || (rc = dot_host<T>(N, X, RES, cAc, s))) return rc;
-  const double w1 = step(cr, cAc);
-  if ((rc = axpy<T>(N, T(0), RHS, (T)w1, X, s)) || (rc = axpy<T>(N, T(1), RHS, (T)(-w1), RES, s))) return rc;
+  auto smooth_step = [&]() -> int {
+    int r;
+    double cr, cAc;
+    if ((r = learned->apply<T>(box, E, el->g2l.p, RES, coef, D, N, s))) return r;
+    if ((r = amxpy<T>(N, T(1), jac, RES, T(1), D, s))) return r;
+    if ((r = op<T>(el, D, AD, s))) return r;
+    if ((r = dot_host<T>(N, D, RES, cr, s)) || (r = dot_host<T>(N, D, AD, cAc, s))) return r;
+    const double w = (cAc > 0 && std::isfinite(cr) && std::isfinite(cAc)) ? cr / cAc : 0.0;
+    if ((r = axpy<T>(N, (T)w, D, T(1), X, s)) || (r = axpy<T>(N, (T)(-w), AD, T(1), RES, s))) return r;
+    return LPG_OK;
+  };
+  LPG_CUDA_TRY(cudaMemsetAsync(X, 0, sizeof(T) * N, s));
+  LPG_CUDA_TRY(cudaMemcpyAsync(RES, RHS, sizeof(T) * N, cudaMemcpyDeviceToDevice, s));
+  for (int k = 0; k < opt.learnedSteps; ++k)
+    if ((rc = smooth_step())) return rc;
   if ((rc = coarse_correct<T>(0, RES, X, s))) return rc;
-  // post-smoothing: X += w2 c2, RES -= w2 A c2
   if ((rc = op<T>(el, X, RES, s)) || (rc = axpy<T>(N, T(1), RHS, T(-1), RES, s))) return rc;
-  if ((rc = learned->apply<T>(box, E, el->g2l.p, RES, L.invDiag64.p, el->weightG.p, D, N, s))) return rc;
-  if (jacobiW > 0 && (rc = amxpy<T>(N, (T)jacobiW, invDiag, RES, T(1), D, s))) return rc;
-  if ((rc = op<T>(el, D, AD, s))) return rc;
-  if ((rc = dot_host<T>(N, D, RES, cr, s)) || (rc = dot_host<T>(N, D, AD, cAc, s))) return rc;
-  const double w2 = step(cr, cAc);
-  if ((rc = axpy<T>(N, (T)w2, D, T(1), X, s)) || (rc = axpy<T>(N, (T)(-w2), AD, T(1), RES, s))) return rc;
+  for (int k = 0; k < opt.learnedSteps; ++k)
+    if ((rc = smooth_step())) return rc;
   // residual reduction of this V-cycle
   double rr, bb;
   if ((rc = dot_host<T>(N, RES, RES, rr, s)) || (rc = dot_host<T>(N, RHS, RHS, bb, s))) return rc;

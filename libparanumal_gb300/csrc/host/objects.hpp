@@ -194,6 +194,7 @@ struct MGOptions {
   bool amgUnsmoothed = false;
   bool amgRugeStuben = false;
   bool amgOnly = false;           // PARALMOND: AMG on the fine matrix
+  int learnedSteps = 2;           // learned smoothing steps before and after the coarse correction
 };
 std::unique_ptr<Precon> make_multigrid(Elliptic* el, const MeshConfig& c, const MGOptions& o, int* status);
 

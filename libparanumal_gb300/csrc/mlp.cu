@@ -310,55 +310,54 @@ int transpose_to_bf16(int K, int N, const float* W, __nv_bfloat16* Wt, cudaStrea
 // node layer next to the shared face (i=1 / i=N-1 ...), listed in face-node order.
 template <typename TIN, typename TOUT>
 __global__ void __launch_bounds__(256)
-features_kernel(const BoxNumbering b, const int64_t E, const int64_t e0, const int32_t* __restrict__ g2l,
+features_kernel(const BoxNumbering b, const int64_t e0, const int64_t count, const int32_t* __restrict__ g2l,
                 const TIN* __restrict__ r, TOUT* __restrict__ X, float* __restrict__ scale, const float sfloor) {
-  const int Nq = b.N + 1, Np = Nq * Nq * Nq, Nfp = Nq * Nq;
-  const int64_t eb = e0 + blockIdx.x;
-  if (eb >= E) return;
-  __shared__ float s_in[kMlpIn];
-  __shared__ float s_red[8];
+  // one warp per element (Nq = 8): lane l holds inputs l, l + 32, ... (28 per lane); the
+  // element's own 512 nodes are the first 16, the 6 x 64 face values the other 12
+  constexpr int Nq = 8, N = Nq - 1, Np = Nq * Nq * Nq, Nfp = Nq * Nq, PER = kMlpIn / 32;
+  static_assert(Np + 6 * Nfp == kMlpIn, "896 inputs");
+  const int lane = threadIdx.x & 31;
+  const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (w >= count) return;   // uniform per warp
+  const int64_t eb = e0 + w;
   const int ex = (int)(eb % b.nx), ey = (int)((eb / b.nx) % b.ny), ez = (int)(eb / ((int64_t)b.nx * b.ny));
-  for (int t = threadIdx.x; t < kMlpIn; t += blockDim.x) {
-    float v = 0.f;
-    if (t < Np) {
-      const int32_t g = g2l[eb * Np + t];
-      v = (g >= 0) ? (float)r[g] : 0.f;
-    } else {
-      const int f = (t - Np) / Nfp, m = (t - Np) % Nfp;
-      const int p = m % Nq, q = m / Nq;  // face-local coordinates in node order
-      int nx = ex, ny = ey, nz = ez, i = 0, j = 0, k = 0;
-      switch (f) {
-        case 0: nz = ez - 1; i = p; j = q; k = b.N - 1; break;
-        case 1: ny = ey - 1; i = p; k = q; j = b.N - 1; break;
-        case 2: nx = ex + 1; j = p; k = q; i = 1; break;
-        case 3: ny = ey + 1; i = p; k = q; j = 1; break;
-        case 4: nx = ex - 1; j = p; k = q; i = b.N - 1; break;
-        default: nz = ez + 1; i = p; j = q; k = 1; break;
-      }
-      if (b.periodic) { nx = (nx + b.nx) % b.nx; ny = (ny + b.ny) % b.ny; nz = (nz + b.nz) % b.nz; }
-      if (nx >= 0 && nx < b.nx && ny >= 0 && ny < b.ny && nz >= 0 && nz < b.nz) {
-        const int64_t en = nx + (int64_t)ny * b.nx + (int64_t)nz * b.nx * b.ny;
-        const int32_t g = g2l[en * Np + i + j * Nq + k * Nfp];
-        v = (g >= 0) ? (float)r[g] : 0.f;
-      }
-    }
-    s_in[t] = v;
-  }
-  __syncthreads();
+  float v[PER];
   float ss = 0.f;
-  for (int t = threadIdx.x; t < Np; t += blockDim.x) ss += s_in[t] * s_in[t];
-  for (int o = 16; o > 0; o >>= 1) ss += __shfl_down_sync(0xffffffffu, ss, o);
-  if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = ss;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    float tot = 0.f;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += s_red[w];
-    s_red[0] = fmaxf(sqrtf(tot / (float)Np), sfloor) + 1e-30f;
-    scale[blockIdx.x] = s_red[0];
+#pragma unroll
+  for (int k = 0; k < Np / 32; ++k) {
+    const int32_t g = g2l[eb * Np + lane + 32 * k];
+    v[k] = (g >= 0) ? (float)r[g] : 0.f;
+    ss += v[k] * v[k];
   }
-  __syncthreads();
-  const float inv = 1.f / s_red[0];
-  for (int t = threadIdx.x; t < kMlpIn; t += blockDim.x) X[blockIdx.x * (int64_t)kMlpIn + t] = (TOUT)(s_in[t] * inv);
+#pragma unroll
+  for (int k = Np / 32; k < PER; ++k) {
+    const int t = lane + 32 * k - Np;
+    const int f = t / Nfp, m = t % Nfp;   // f is the same for the whole warp
+    const int p = m % Nq, q = m / Nq;      // face-local coordinates in node order
+    int nx = ex, ny = ey, nz = ez, i = 0, j = 0, kk = 0;
+    switch (f) {
+      case 0: nz = ez - 1; i = p; j = q; kk = N - 1; break;
+      case 1: ny = ey - 1; i = p; kk = q; j = N - 1; break;
+      case 2: nx = ex + 1; j = p; kk = q; i = 1; break;
+      case 3: ny = ey + 1; i = p; kk = q; j = 1; break;
+      case 4: nx = ex - 1; j = p; kk = q; i = N - 1; break;
+      default: nz = ez + 1; i = p; j = q; kk = 1; break;
+    }
+    if (b.periodic) { nx = (nx + b.nx) % b.nx; ny = (ny + b.ny) % b.ny; nz = (nz + b.nz) % b.nz; }
+    float val = 0.f;
+    if (nx >= 0 && nx < b.nx && ny >= 0 && ny < b.ny && nz >= 0 && nz < b.nz) {
+      const int64_t en = nx + (int64_t)ny * b.nx + (int64_t)nz * b.nx * b.ny;
+      const int32_t g = g2l[en * Np + i + j * Nq + kk * Nfp];
+      val = (g >= 0) ? (float)r[g] : 0.f;
+    }
+    v[k] = val;
+  }
+  for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
+  const float sc = fmaxf(sqrtf(ss / (float)Np), sfloor) + 1e-30f;
+  if (lane == 0) scale[w] = sc;
+  const float inv = 1.f / sc;
+#pragma unroll
+  for (int k = 0; k < PER; ++k) X[w * (int64_t)kMlpIn + lane + 32 * k] = (TOUT)(v[k] * inv);
 }
 
 template <typename TIN, typename TOUT>
@@ -367,7 +366,8 @@ int element_features(const BoxNumbering& b, int64_t E, int64_t e0, int64_t count
   if ((b.N + 1) * (b.N + 1) * (b.N + 1) + 6 * (b.N + 1) * (b.N + 1) != kMlpIn)
     return set_error(LPG_ERR_UNSUPPORTED, "learned smoother needs N = 7 (896 inputs per element)");
   if (count <= 0) return LPG_OK;
-  features_kernel<TIN, TOUT><<<(unsigned)count, 256, 0, s>>>(b, E, e0, g2l, r, X, scale, sfloor);
+  if (e0 < 0 || e0 + count > E) return set_error(LPG_ERR_INVALID, "element_features: chunk outside the mesh");
+  features_kernel<TIN, TOUT><<<(unsigned)((count * 32 + 255) / 256), 256, 0, s>>>(b, e0, count, g2l, r, X, scale, sfloor);
   LPG_LAUNCH_CHECK("features_kernel");
   return LPG_OK;
 }
@@ -378,33 +378,37 @@ template int element_features<double, __nv_bfloat16>(const BoxNumbering&, int64_
 template int element_features<float, __nv_bfloat16>(const BoxNumbering&, int64_t, int64_t, int64_t, const int32_t*,
                                                     const float*, __nv_bfloat16*, float*, float, cudaStream_t);
 
-// z_local = s_e * invDiag * out ; z[g] += weight[g] * z_local (average over copies)
+// z[g] += coef[g] * s_e * out (coef = weight / diag: the correction s_e invDiag out
+// averaged over the copies of g), in the vector's precision
 template <typename TV>
 __global__ void apply_correction_kernel(const int Np, const int64_t count, const int64_t e0,
                                         const int32_t* __restrict__ g2l, const float* __restrict__ out,
-                                        const float* __restrict__ scale, const double* __restrict__ invDiag,
-                                        const double* __restrict__ weight, TV* __restrict__ z) {
+                                        const float* __restrict__ scale, const TV* __restrict__ coef,
+                                        TV* __restrict__ z) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count * Np; i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t el = i / Np;
     const int n = (int)(i % Np);
     const int32_t g = g2l[(e0 + el) * Np + n];
     if (g < 0) continue;
-    const double v = (double)scale[el] * (double)out[el * kMlpOut + n] * invDiag[g] * weight[g];
-    atomicAdd(z + g, (TV)v);
+    const TV v = coef[g] * (TV)(scale[el] * out[el * kMlpOut + n]);
+    // nodes strictly inside the element (1 <= i,j,k <= N-1) have no other copy: a store
+    const int Nq = kMlpNq, a = n % Nq, bb = (n / Nq) % Nq, c = n / (Nq * Nq);
+    if (a > 0 && a < Nq - 1 && bb > 0 && bb < Nq - 1 && c > 0 && c < Nq - 1) z[g] = v;
+    else atomicAdd(z + g, v);
   }
 }
 template <typename TV>
 int apply_correction(int Np, int64_t count, int64_t e0, const int32_t* g2l, const float* out, const float* scale,
-                     const double* invDiag, const double* weight, TV* z, cudaStream_t s) {
+                     const TV* coef, TV* z, cudaStream_t s) {
   if (count <= 0) return LPG_OK;
-  apply_correction_kernel<TV><<<grid_n(count * Np), 256, 0, s>>>(Np, count, e0, g2l, out, scale, invDiag, weight, z);
+  apply_correction_kernel<TV><<<grid_n(count * Np), 256, 0, s>>>(Np, count, e0, g2l, out, scale, coef, z);
   LPG_LAUNCH_CHECK("apply_correction_kernel");
   return LPG_OK;
 }
 template int apply_correction<double>(int, int64_t, int64_t, const int32_t*, const float*, const float*, const double*,
-                                      const double*, double*, cudaStream_t);
-template int apply_correction<float>(int, int64_t, int64_t, const int32_t*, const float*, const float*, const double*,
-                                     const double*, float*, cudaStream_t);
+                                      double*, cudaStream_t);
+template int apply_correction<float>(int, int64_t, int64_t, const int32_t*, const float*, const float*, const float*,
+                                     float*, cudaStream_t);
 
 // training target: t = D .* e_local / s (network output units), e gathered from the dofs
 __global__ void target_kernel(const int Np, const int64_t count, const int32_t* __restrict__ elems,
@@ -488,6 +492,21 @@ int gather_rows(int64_t count, const int32_t* elems, const float* Xall, float* X
   if (count <= 0) return LPG_OK;
   gather_rows_kernel<float><<<grid_n(count * kMlpIn), 256, 0, s>>>(count, elems, Xall, X);
   LPG_LAUNCH_CHECK("gather_rows_kernel");
+  return LPG_OK;
+}
+
+// dst[i][:] = src[idx[i]][:] for rows of `width` floats (minibatch assembly)
+__global__ void gather_rows_w_kernel(const int64_t count, const int width, const int32_t* __restrict__ idx,
+                                     const float* __restrict__ src, float* __restrict__ dst) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count * width; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t row = i / width;
+    dst[i] = src[(int64_t)idx[row] * width + (i % width)];
+  }
+}
+int gather_rows_w(int64_t count, int width, const int32_t* idx, const float* src, float* dst, cudaStream_t s) {
+  if (count <= 0) return LPG_OK;
+  gather_rows_w_kernel<<<grid_n(count * width), 256, 0, s>>>(count, width, idx, src, dst);
+  LPG_LAUNCH_CHECK("gather_rows_w_kernel");
   return LPG_OK;
 }
 

@@ -13,6 +13,7 @@ namespace lpg {
 constexpr int kMlpIn = 896;      // 512 element residual values + 6 x 64 face traces (N = 7)
 constexpr int kMlpHidden = 256;
 constexpr int kMlpOut = 512;
+constexpr int kMlpNq = 8;        // the network is defined for N = 7 (8 x 8 x 8 nodes)
 // parameter vector: W0 (896x256), b0, W1 (256x256), b1, W2 (256x256), b2, W3 (256x512), b3
 constexpr int64_t kMlpParams = (int64_t)kMlpIn * kMlpHidden + kMlpHidden + 2 * ((int64_t)kMlpHidden * kMlpHidden + kMlpHidden) +
                                (int64_t)kMlpHidden * kMlpOut + kMlpOut;
@@ -74,12 +75,15 @@ template <typename TIN, typename TOUT>
 // scale_e = max(RMS of the element's residual, sfloor); features = values / scale_e
 int element_features(const BoxNumbering& b, int64_t E, int64_t e0, int64_t count, const int32_t* g2l, const TIN* r,
                      TOUT* X, float* scale, float sfloor, cudaStream_t s);
+// z[g] += coef[g] * scale[e] * out[e][n] over the local nodes (coef = weight / diag)
 template <typename TV>
 int apply_correction(int Np, int64_t count, int64_t e0, const int32_t* g2l, const float* out, const float* scale,
-                     const double* invDiag, const double* weight, TV* z, cudaStream_t s);
+                     const TV* coef, TV* z, cudaStream_t s);
 int training_targets(int Np, int64_t count, const int32_t* elems, const int32_t* g2l, const double* e,
                      const double* invDiag, const float* scale, float* T, cudaStream_t s);
 int gather_rows(int64_t count, const int32_t* elems, const float* Xall, float* X, cudaStream_t s);
+// dst[i][:] = src[idx[i]][:], rows of `width` floats
+int gather_rows_w(int64_t count, int width, const int32_t* idx, const float* src, float* dst, cudaStream_t s);
 // T[i][n] -= w X[i][n], n < kMlpOut (targets of a damped-Jacobi + network smoother)
 int subtract_inputs(int64_t count, float w, const float* X, float* T, cudaStream_t s);
 // T (E x 512) = (e - F e) / (invDiag s_e) per element, F the 1D modal low-pass (Nq x Nq)

@@ -56,12 +56,132 @@ pmg_coarsen_kernel(const int NqF, const int NqC, const int32_t* __restrict__ g2l
   }
 }
 
+// Tensor-product transfers for fixed (fine, coarse) node counts per direction: several
+// elements per CTA, Nq_f x Nq_f threads per element holding a fine k-pencil in
+// registers, the other two directions through shared memory. Same arithmetic as the
+// generic kernels above (ellipticPreconCoarsenHex3D.okl:209-294,
+// ellipticPreconProlongateHex3D.okl:216-301).
+template <int NQF, int NQC>
+constexpr int tp_elems() { return 256 / (NQF * NQF); }
+
+template <int NQF, int NQC, typename T>
+__global__ void __launch_bounds__(256)
+pmg_coarsen_tp_kernel(const int64_t E, const int32_t* __restrict__ g2lF, const T* __restrict__ wF,
+                      const T* __restrict__ xF, const T* __restrict__ Pg, const int32_t* __restrict__ g2lC,
+                      T* __restrict__ xC) {
+  constexpr int EPB = tp_elems<NQF, NQC>(), NPF = NQF * NQF * NQF, NPC = NQC * NQC * NQC;
+  __shared__ T s_P[NQF][NQC];                  // P[m][c] = l_c(x_m)
+  __shared__ T s_u[EPB][NQC][NQF][NQF];        // [kc][j][i]
+  __shared__ T s_v[EPB][NQC][NQC][NQF];        // [kc][jc][i]
+  const int i = threadIdx.x, j = threadIdx.y, el = threadIdx.z;
+  const int lt = i + NQF * j, tid = lt + NQF * NQF * el;
+  for (int t = tid; t < NQF * NQC; t += 256) s_P[t / NQC][t % NQC] = Pg[t];
+  const int64_t e = (int64_t)blockIdx.x * EPB + el;
+  const bool active = e < E;
+  T wx[NQF];
+#pragma unroll
+  for (int k = 0; k < NQF; ++k) {
+    const int32_t g = active ? g2lF[e * NPF + k * NQF * NQF + lt] : -1;
+    wx[k] = (g >= 0) ? wF[g] * xF[g] : T(0);
+  }
+  __syncthreads();
+#pragma unroll
+  for (int kc = 0; kc < NQC; ++kc) {
+    T u = 0;
+#pragma unroll
+    for (int k = 0; k < NQF; ++k) u += s_P[k][kc] * wx[k];
+    s_u[el][kc][j][i] = u;
+  }
+  __syncthreads();
+  for (int p = j; p < NQC * NQC; p += NQF) {
+    const int kc = p / NQC, jc = p % NQC;
+    T v = 0;
+#pragma unroll
+    for (int m = 0; m < NQF; ++m) v += s_P[m][jc] * s_u[el][kc][m][i];
+    s_v[el][kc][jc][i] = v;
+  }
+  __syncthreads();
+  if (!active) return;
+  for (int p = lt; p < NPC; p += NQF * NQF) {
+    const int kc = p / (NQC * NQC), jc = (p / NQC) % NQC, ic = p % NQC;
+    T c = 0;
+#pragma unroll
+    for (int m = 0; m < NQF; ++m) c += s_P[m][ic] * s_v[el][kc][jc][m];
+    const int32_t g = g2lC[e * NPC + p];
+    if (g >= 0) atomicAdd(xC + g, c);
+  }
+}
+
+template <int NQF, int NQC, typename T>
+__global__ void __launch_bounds__(256)
+pmg_prolong_tp_kernel(const int64_t E, const int32_t* __restrict__ g2lC, const T* __restrict__ xC,
+                      const T* __restrict__ Pg, const int32_t* __restrict__ g2lF, const int32_t* __restrict__ ownerF,
+                      T* __restrict__ xF) {
+  constexpr int EPB = tp_elems<NQF, NQC>(), NPF = NQF * NQF * NQF, NPC = NQC * NQC * NQC;
+  __shared__ T s_P[NQF][NQC];
+  __shared__ T s_c[EPB][NQC][NQC][NQC];        // coarse values [kc][jc][ic]
+  __shared__ T s_cf[EPB][NQC][NQC][NQF];       // [kc][jc][i]
+  const int i = threadIdx.x, j = threadIdx.y, el = threadIdx.z;
+  const int lt = i + NQF * j, tid = lt + NQF * NQF * el;
+  for (int t = tid; t < NQF * NQC; t += 256) s_P[t / NQC][t % NQC] = Pg[t];
+  const int64_t e = (int64_t)blockIdx.x * EPB + el;
+  const bool active = e < E;
+  for (int p = lt; p < NPC; p += NQF * NQF) {
+    const int32_t g = active ? g2lC[e * NPC + p] : -1;
+    s_c[el][p / (NQC * NQC)][(p / NQC) % NQC][p % NQC] = (g >= 0) ? xC[g] : T(0);
+  }
+  __syncthreads();
+  for (int p = j; p < NQC * NQC; p += NQF) {
+    const int kc = p / NQC, jc = p % NQC;
+    T v = 0;
+#pragma unroll
+    for (int m = 0; m < NQC; ++m) v += s_P[i][m] * s_c[el][kc][jc][m];
+    s_cf[el][kc][jc][i] = v;
+  }
+  __syncthreads();
+  if (!active) return;
+  T u[NQC];
+#pragma unroll
+  for (int kc = 0; kc < NQC; ++kc) {
+    T v = 0;
+#pragma unroll
+    for (int m = 0; m < NQC; ++m) v += s_P[j][m] * s_cf[el][kc][m][i];
+    u[kc] = v;
+  }
+  // the owning copy of each fine dof adds the value; nodes strictly inside the element
+  // (no other copy) are their own owners
+  const bool inner_ij = i > 0 && i < NQF - 1 && j > 0 && j < NQF - 1;
+#pragma unroll
+  for (int k = 0; k < NQF; ++k) {
+    T f = 0;
+#pragma unroll
+    for (int m = 0; m < NQC; ++m) f += s_P[k][m] * u[m];
+    const int64_t id = e * NPF + k * NQF * NQF + lt;
+    const int32_t g = g2lF[id];
+    if (g < 0) continue;
+    if ((inner_ij && k > 0 && k < NQF - 1) || ownerF[g] == (int32_t)id) xF[g] += f;
+  }
+}
+
+template <int NQF, int NQC>
+static bool tp_pair(int Nf, int Nc) { return Nf + 1 == NQF && Nc + 1 == NQC; }
+
 template <typename T>
 int pmg_coarsen(int Nf, int Nc, int64_t E, const int32_t* g2lF, const T* weightF, const T* xF,
                 const T* P, const int32_t* g2lC, T* xC, int64_t NglobalC, cudaStream_t s) {
   if (Nf + 1 > kMaxNq || Nc < 1 || Nc > Nf) return set_error(LPG_ERR_UNSUPPORTED, "pmg_coarsen: bad degrees");
   LPG_CUDA_TRY(cudaMemsetAsync(xC, 0, sizeof(T) * NglobalC, s));
   if (E <= 0) return LPG_OK;
+  if (tp_pair<8, 4>(Nf, Nc) || tp_pair<4, 2>(Nf, Nc)) {
+    if (Nf == 7) {
+      pmg_coarsen_tp_kernel<8, 4, T><<<(unsigned)((E + 3) / 4), dim3(8, 8, 4), 0, s>>>(E, g2lF, weightF, xF, P, g2lC, xC);
+    } else {
+      pmg_coarsen_tp_kernel<4, 2, T><<<(unsigned)((E + 15) / 16), dim3(4, 4, 16), 0, s>>>(E, g2lF, weightF, xF, P, g2lC,
+                                                                                           xC);
+    }
+    LPG_LAUNCH_CHECK("pmg_coarsen_tp_kernel");
+    return LPG_OK;
+  }
   pmg_coarsen_kernel<T><<<(unsigned)E, 256, 0, s>>>(Nf + 1, Nc + 1, g2lF, weightF, xF, P, g2lC, xC);
   LPG_LAUNCH_CHECK("pmg_coarsen_kernel");
   return LPG_OK;
@@ -116,6 +236,16 @@ int pmg_prolongate_map(int Nf, int Nc, int64_t E, const int32_t* g2lC, const T* 
                        const int32_t* g2lF, const int32_t* ownerF, T* xF, cudaStream_t s) {
   if (Nf + 1 > kMaxNq || Nc < 1 || Nc > Nf) return set_error(LPG_ERR_UNSUPPORTED, "pmg_prolongate: bad degrees");
   if (E <= 0) return LPG_OK;
+  if (tp_pair<8, 4>(Nf, Nc) || tp_pair<4, 2>(Nf, Nc)) {
+    if (Nf == 7) {
+      pmg_prolong_tp_kernel<8, 4, T><<<(unsigned)((E + 3) / 4), dim3(8, 8, 4), 0, s>>>(E, g2lC, xC, P, g2lF, ownerF, xF);
+    } else {
+      pmg_prolong_tp_kernel<4, 2, T><<<(unsigned)((E + 15) / 16), dim3(4, 4, 16), 0, s>>>(E, g2lC, xC, P, g2lF, ownerF,
+                                                                                           xF);
+    }
+    LPG_LAUNCH_CHECK("pmg_prolong_tp_kernel");
+    return LPG_OK;
+  }
   pmg_prolong_kernel<T><<<(unsigned)E, 256, 0, s>>>(Nf + 1, Nc + 1, g2lC, xC, P, g2lF, ownerF, xF);
   LPG_LAUNCH_CHECK("pmg_prolong_kernel");
   return LPG_OK;

@@ -214,10 +214,22 @@ __global__ void __launch_bounds__(kRedThreads)
 reduce_stage1(const int64_t N, const void* __restrict__ xv, const void* __restrict__ yv,
               double* __restrict__ partials) {
   double acc = 0;
-  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x) {
-    if (KIND == RED_DOT) acc += ((const double*)xv)[n] * ((const double*)yv)[n];
-    else if (KIND == RED_SUM) acc += ((const double*)xv)[n];
-    else acc += (double)((const float*)xv)[n] * (double)((const float*)yv)[n];
+  if (KIND == RED_DOT32) {
+    // FP32 products summed per thread with Kahan compensation on the FP32 pipe (GB300's
+    // FP64 pipe would bound this loop); one conversion per thread, then FP64 across threads
+    float s = 0.f, c = 0.f;
+    for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x) {
+      const float y = ((const float*)xv)[n] * ((const float*)yv)[n] - c;
+      const float t = s + y;
+      c = (t - s) - y;
+      s = t;
+    }
+    acc = (double)s - (double)c;
+  } else {
+    for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x) {
+      if (KIND == RED_DOT) acc += ((const double*)xv)[n] * ((const double*)yv)[n];
+      else acc += ((const double*)xv)[n];
+    }
   }
   acc = block_sum(acc);
   if (threadIdx.x == 0) partials[blockIdx.x] = acc;
