@@ -47,10 +47,11 @@ def parse():
     ap.add_argument("--cpu-sample-nx", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=5)
-    ap.add_argument("--prec", default="f64", choices=["f64", "f32", "bf16g"],
+    ap.add_argument("--prec", default="f64", choices=["f64", "df64", "f32", "bf16g"],
                     help="operator variant timed in the Ax workload (headline: f64)")
     ap.add_argument("--solve", action="store_true", help="time-to-tolerance of the p-MG FPCG solve instead")
-    ap.add_argument("--solve-precs", default="FP64,FP32,BF16GEO")
+    ap.add_argument("--solve-precs", default="FP64,FP32,BF16GEO,FP64+DF64,FP32+DF64,BF16GEO+DF64",
+                    help="preconditioner precisions; P+DF64 also runs the FP64 operator in double-FP32 words")
     ap.add_argument("--solve-reps", type=int, default=2)
     ap.add_argument("--learned", action="store_true", help="learned-smoother training and solve comparison")
     ap.add_argument("--mlp", action="store_true", help="learned-smoother MLP inference (lpg_mlp_forward_bf16) timing")
@@ -197,7 +198,10 @@ def run_solves(a):
     res = {}
     for prec in a.solve_precs.split(","):
         t0 = time.time()
-        e = lpg.Elliptic(solve_settings(a.nx, a.N, prec))
+        # "P+DF64": preconditioner precision P, FP64 operator applications in double-FP32 words
+        base, _, op = prec.partition("+")
+        extra = {"OPERATOR PRECISION": op} if op else {}
+        e = lpg.Elliptic(solve_settings(a.nx, a.N, base, **extra))
         setup = time.time() - t0
         runs = [e.Run() for _ in range(a.solve_reps)]
         best = min(runs, key=lambda r: r["solve_seconds"])
@@ -216,7 +220,8 @@ def run_learned(a):
     pairs of the plain p-MG FPCG on a 32^3 jittered box with random Gaussian-bump
     right-hand sides (lognormal lambda, N=7), then solve the nx^3 problem (manufactured
     sine data, or with --rhs gauss 16 Gaussian sources, seed 3) with the plain FP64, the
-    FP32 and the learned+FP32 preconditioners. Each result carries the relative 2-norm
+    FP32 and the learned+FP32 preconditioners, the last two also with the FP64 operator
+    applications in double-FP32 words (+DF64). Each result carries the relative 2-norm
     difference of its solution from the FP64 method's. One JSON line."""
     import torch
     import libparanumal_gb300 as lpg
@@ -237,9 +242,13 @@ def run_learned(a):
            "train_pairs": a.train_pairs, "learned_steps": a.learned_steps,
            "loss_first": float(hist[0]), "loss_last": float(hist[-1]), "results": {}}
     x64 = None
-    for name, prec, learned in (("FP64", "FP64", False), ("FP32", "FP32", False), ("learned+FP32", "FP32", True)):
+    variants = (("FP64", "FP64", False, False), ("FP32", "FP32", False, False), ("learned+FP32", "FP32", True, False),
+                ("FP32+DF64", "FP32", False, True), ("learned+FP32+DF64", "FP32", True, True))
+    for name, prec, learned, dw in variants:
         t1 = time.time()
         extra = {"LEARNED SMOOTHER STEPS": a.learned_steps} if learned else {}
+        if dw:
+            extra["OPERATOR PRECISION"] = "DF64"
         e = lpg.Elliptic(solve_settings(a.nx, 7, prec, **law, **rhs, **extra))
         setup = time.time() - t1
         if learned:
@@ -331,7 +340,10 @@ def main():
     lpg.lib()
 
     t_setup = time.time()
-    e = lpg.Elliptic(settings(a.nx, a.N))
+    st = settings(a.nx, a.N)
+    if a.prec == "df64":
+        st["OPERATOR PRECISION"] = "DF64"   # FP64 operator interface, double-FP32 arithmetic
+    e = lpg.Elliptic(st)
     Nl, Ng = e.Nlocal, e.Nglobal
     q = torch.empty(Ng, dtype=torch.float64, device="cuda")
     Aq = torch.empty_like(q)
@@ -340,7 +352,7 @@ def main():
     t_setup = time.time() - t_setup
     stream = torch.cuda.current_stream()
     sp = stream.cuda_stream
-    if a.prec == "f64":
+    if a.prec in ("f64", "df64"):
         qin, yout = q, Aq
 
         def op():
@@ -389,14 +401,14 @@ def main():
     # end to end through the C ABI's host-buffer operator: page-locked q in, Aq out; each
     # call uploads q, applies the operator and downloads Aq (pipelined over element
     # chunks) and returns with Aq filled, so host wall time is the step time
-    prec_name = {"f64": "FP64", "f32": "FP32", "bf16g": "BF16GEO"}[a.prec]
+    prec_name = {"f64": "FP64", "df64": "FP64", "f32": "FP32", "bf16g": "BF16GEO"}[a.prec]
     qh = qin.cpu().pin_memory()
     yh = torch.empty_like(qh).pin_memory()
     for _ in range(2):
         e.OperatorHost(qh, yh, prec_name)
     dev_out = yout.cpu()
     e2e_check = float((yh - dev_out).abs().max() / dev_out.abs().max())
-    if e2e_check > (1e-12 if a.prec == "f64" else 1e-5):
+    if e2e_check > (1e-12 if a.prec in ("f64", "df64") else 1e-5):
         raise RuntimeError("host-buffer operator differs from the device operator: %g" % e2e_check)
     if dist:
         dist.barrier()
@@ -409,7 +421,8 @@ def main():
         dist.destroy_process_group()
         return
     peak, peak_kind = measured_peaks()
-    alg_bytes = {"f64": Nl * 60 + Ng * 16, "f32": Nl * 32 + Ng * 8, "bf16g": Nl * 18 + Ng * 8}[a.prec]
+    alg_bytes = {"f64": Nl * 60 + Ng * 16, "df64": Nl * 60 + Ng * 16, "f32": Nl * 32 + Ng * 8,
+                 "bf16g": Nl * 18 + Ng * 8}[a.prec]
     flops = (12 * (a.N + 1) + 18) * Nl
     achieved = alg_bytes / (launch_ms * 1e-3) / 1e9
     # DRAM bytes per launch: the ncu capture's bytes per element (24^3 case, traffic
@@ -417,6 +430,7 @@ def main():
     traffic = None
     tfile = os.path.join(ROOT, "profiles", {"f64": "ax_hex_f64_64cubed_N7.txt",
                                             "f32": "ax_hex_staged_f32_24cubed_N7_full.txt",
+                                            "df64": "ax_hex_dw_24cubed_N7_full.txt",
                                             "bf16g": "ax_hex_staged_bf16g_24cubed_N7_full.txt"}[a.prec])
     if os.path.exists(tfile) and a.N == 7:
         for line in open(tfile):
@@ -435,12 +449,14 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                      "algorithmic_bytes_per_launch": alg_bytes, "launch_ms": launch_ms},
-        "compute": {"arith": "fp64" if a.prec == "f64" else "fp32", "flops_per_launch": flops,
+        "compute": {"arith": {"f64": "fp64", "df64": "double-fp32 words"}.get(a.prec, "fp32"),
+                    "flops_per_launch": flops,
                     "achieved_tflops": flops / (launch_ms * 1e-3) / 1e12,
                     "nominal_fp64_tflops": 1.25},
         "e2e": {"value": world * Nl / (e2e_ms * 1e-3) / 1e9, "unit": "GDOF/s",
                 "h2d_bytes_per_step": Ng * qin.element_size(), "d2h_bytes_per_step": Ng * qin.element_size(),
-                "ms_per_step": e2e_ms, "api": "lpg_elliptic_operator_host%s" % ("" if a.prec == "f64" else "_f32"),
+                "ms_per_step": e2e_ms,
+                "api": "lpg_elliptic_operator_host%s" % ("" if a.prec in ("f64", "df64") else "_f32"),
                 "host_chunks": e.info("host_chunks"), "max_rel_diff_vs_device": e2e_check},
         "gpu_launches": a.steps,
         "clocks": clk,

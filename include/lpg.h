@@ -163,6 +163,12 @@ int lpg_elliptic_operator(lpg_elliptic *e, const double *q, double *Aq, void *st
  * geometric factors, FP32 arithmetic. The reduced-precision copies of the geometric
  * factors are made on first use. */
 int lpg_elliptic_operator_f32(lpg_elliptic *e, const float *q, float *Aq, int bf16geo, void *stream);
+/* The same operator (device vectors, FP64 in and out) computed in double-FP32 words on
+ * the FP32 pipe -- no reference counterpart. 48-bit significands; agrees with the FP64
+ * operator to about 1e-14 relative (sums with absolute error ~2^-48 of the magnitudes
+ * summed); inputs below 2^-74 in magnitude lose the low word. N = 3 or 7. The setting
+ * [OPERATOR PRECISION] DF64 makes every FP64 operator application of the object use it. */
+int lpg_elliptic_operator_df64(lpg_elliptic *e, const double *q, double *Aq, void *stream);
 /* elliptic_t::Operator (ellipticOperator.cpp:29-106) on HOST arrays, as the OCCA Serial
  * backend's operator takes them: Aq_host = A q_host (Nglobal entries each), returning
  * when Aq_host is filled. The upload of q, the operator and the download of Aq are

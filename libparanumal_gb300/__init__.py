@@ -72,6 +72,7 @@ def lib():
         "lpg_elliptic_operator": [vp, vp, vp, vp],
         "lpg_elliptic_operator_f32": [vp, vp, vp, i32, vp],
         "lpg_elliptic_operator_host": [vp, vp, vp],
+        "lpg_elliptic_operator_df64": [vp, vp, vp, vp],
         "lpg_elliptic_operator_host_f32": [vp, vp, vp, i32],
         "lpg_elliptic_precon": [vp, vp, vp, vp],
         "lpg_elliptic_solve": [vp, vp, vp, f64, i32, ctypes.POINTER(ctypes.c_int)],
@@ -207,6 +208,10 @@ class Elliptic:
         """Reduced-precision operator (FP32 vectors; FP32 or BF16 geometric factors)."""
         check(lib().lpg_elliptic_operator_f32(self.h, _ptr(q), _ptr(Aq), 1 if bf16geo else 0,
                                               stream or None))
+
+    def OperatorDF64(self, q, Aq, stream=0):
+        """FP64-accurate operator in double-FP32 words (device vectors, FP64 in and out)."""
+        check(lib().lpg_elliptic_operator_df64(self.h, _ptr(q), _ptr(Aq), stream or None))
 
     def OperatorHost(self, q, Aq, precision="FP64"):
         """Aq = A q on host arrays (numpy arrays or CPU tensors of Nglobal entries: float64

@@ -15,6 +15,7 @@
 #include <cstring>
 #include <type_traits>
 
+#include "df64.cuh"
 #include "lpg_common.cuh"
 #include "lpg_internal.hpp"
 
@@ -525,6 +526,187 @@ ax_hex_eo_kernel(const int64_t Nelements, const int32_t* __restrict__ elementLis
 #pragma unroll
   for (int k = 0; k < NQ; ++k)
     if (r_id[k] >= 0) atomicAdd(out + r_id[k], r_Aq[k]);
+}
+
+// ---------------------------------------------------------------- double-word variant
+// The even-odd kernel above with every FP64 value held as a double-FP32 word (df64.cuh):
+// FP64-accurate (48-bit significands, sums with absolute error of order 2^-48 times the
+// magnitudes summed) on GB300's FP32 pipe, which runs ~64x the FP64 rate. q is read as
+// FP64 and split with integer operations; the geometric factors come pre-split
+// ([e][7][Np] hi/lo pairs, the same 8 bytes per value as FP64); each local result is
+// rebuilt exactly as FP64 hi + lo (one FP64 add) and assembled with FP64 atomics.
+template <int NQ>
+__global__ void __launch_bounds__(NQ * NQ * elems_per_block<NQ>(), 2)
+ax_hex_dw_kernel(const int64_t Nelements, const int32_t* __restrict__ elementList,
+                 const int32_t* __restrict__ g2l, const dw* __restrict__ ggeo, const int64_t geoStride,
+                 const dw* __restrict__ wJ, const int64_t wJStride, const double* __restrict__ Dg,
+                 const double lambda, const double* __restrict__ lambdaE, const double* __restrict__ q,
+                 double* __restrict__ out) {
+  static_assert(NQ == 4 || NQ == 8, "double-word kernel: Nq = 4 or 8");
+  constexpr int NP = NQ * NQ * NQ, H = NQ / 2, N = NQ - 1;
+  constexpr int EPB = elems_per_block<NQ>();
+  __shared__ dw s_Dp[H][H], s_Dm[H][H], s_Tp[H][H], s_Tm[H][H];
+  __shared__ dw s_R[EPB][NQ][NQ], s_S[EPB][NQ][NQ], s_dr[EPB][NQ][NQ], s_ds[EPB][NQ][NQ];
+  __shared__ dw s_qt[NQ][NQ * NQ * EPB], s_gt[NQ][NQ * NQ * EPB];
+
+  const int i = threadIdx.x, jj = threadIdx.y, el = threadIdx.z;
+  const int j = eo_row<NQ>(jj);
+  const int tid = i + NQ * (jj + NQ * el);
+  for (int t = tid; t < H * H; t += NQ * NQ * EPB) {
+    const int a = t / H, m = t % H;
+    const double d0 = Dg[a * NQ + m], d1 = Dg[a * NQ + N - m];
+    const double t0 = Dg[m * NQ + a], t1 = Dg[(N - m) * NQ + a];
+    s_Dp[a][m] = dw_from_double(0.5 * (d0 + d1));
+    s_Dm[a][m] = dw_from_double(0.5 * (d0 - d1));
+    s_Tp[a][m] = dw_from_double(0.5 * (t0 + t1));
+    s_Tm[a][m] = dw_from_double(0.5 * (t0 - t1));
+  }
+
+  int64_t e = (int64_t)blockIdx.x * EPB + el;
+  const bool active = e < Nelements;
+  if (active && elementList) e = elementList[e];
+  if (!active) e = 0;
+
+  dw r_q[NQ], r_Aq[NQ];
+  int32_t r_id[NQ];
+  const int64_t nodeBase = e * NP + j * NQ + i;
+#pragma unroll
+  for (int k = 0; k < NQ; ++k) {
+    const int32_t id = active ? __ldg(g2l + nodeBase + k * NQ * NQ) : -1;
+    r_id[k] = id;
+    r_q[k] = dw_from_double((id >= 0) ? q[id] : 0.0);
+  }
+  const dw lam = dw_from_double((lambdaE && active) ? lambdaE[e] : lambda);
+  const dw* gp = ggeo + e * geoStride + j * NQ + i;
+  const dw* wp = wJ + e * wJStride + j * NQ + i;
+  __syncthreads();
+
+  {
+    dw E[H], O[H];
+#pragma unroll
+    for (int m = 0; m < H; ++m) {
+      E[m] = dw_add(r_q[m], r_q[N - m]);
+      O[m] = dw_sub(r_q[m], r_q[N - m]);
+    }
+#pragma unroll
+    for (int t = 0; t < H; ++t) {
+      dw_acc A, B;
+#pragma unroll
+      for (int m = 0; m < H; ++m) {
+        A.mac(s_Dp[t][m], E[m]);
+        B.mac(s_Dm[t][m], O[m]);
+      }
+      const dw a = A.get(), b = B.get();
+      s_qt[t][tid] = dw_add(a, b);
+      s_qt[N - t][tid] = dw_sub(b, a);
+    }
+  }
+
+  const bool rtask = i < H;
+  const int pt = rtask ? i : i - H;
+  dw* dst0 = rtask ? &s_dr[el][j][pt] : &s_ds[el][pt][j];
+  dw* dst1 = rtask ? &s_dr[el][j][N - pt] : &s_ds[el][N - pt][j];
+  const dw* line = rtask ? &s_R[el][j][0] : &s_S[el][j][0];
+  const int slotR = (i < H) ? i : H + N - i, slotS = (j < H) ? j : H + N - j;
+  const float sgnR = (i < H) ? 1.f : -1.f, sgnS = (j < H) ? 1.f : -1.f;
+
+#pragma unroll
+  for (int k = 0; k < NQ; ++k) {
+    const int off = k * NQ * NQ;
+    const dw zero{0.f, 0.f};
+    const dw G00 = active ? gp[0 * NP + off] : zero, G01 = active ? gp[1 * NP + off] : zero;
+    const dw G02 = active ? gp[2 * NP + off] : zero, G11 = active ? gp[3 * NP + off] : zero;
+    const dw G12 = active ? gp[4 * NP + off] : zero, G22 = active ? gp[5 * NP + off] : zero;
+    const dw GwJ = active ? wp[off] : zero;
+    const dw v = r_q[k];
+    const dw pr = dw_shfl_xor(v, NQ - 1), ps = dw_shfl_xor(v, 2 * NQ);
+    s_R[el][j][slotR] = dw_add(pr, dw_scale_sign(sgnR, v));
+    s_S[el][i][slotS] = dw_add(ps, dw_scale_sign(sgnS, v));
+    eo_sync<NQ>(el);
+    {
+      dw_acc A, B;
+#pragma unroll
+      for (int m = 0; m < H; ++m) {
+        A.mac(s_Dp[pt][m], line[m]);
+        B.mac(s_Dm[pt][m], line[H + m]);
+      }
+      const dw a = A.get(), b = B.get();
+      *dst0 = dw_add(a, b);
+      *dst1 = dw_sub(b, a);
+    }
+    eo_sync<NQ>(el);
+    const dw qr = s_dr[el][j][i], qs = s_ds[el][j][i], qtk = s_qt[k][tid];
+    dw_acc ar, as, at;
+    ar.mac(G00, qr); ar.mac(G01, qs); ar.mac(G02, qtk);
+    as.mac(G01, qr); as.mac(G11, qs); as.mac(G12, qtk);
+    at.mac(G02, qr); at.mac(G12, qs); at.mac(G22, qtk);
+    const dw Gqr = ar.get(), Gqs = as.get();
+    s_gt[k][tid] = at.get();
+    const dw mass = dw_mul(dw_mul(GwJ, lam), v);
+    const dw pr2 = dw_shfl_xor(Gqr, NQ - 1), ps2 = dw_shfl_xor(Gqs, 2 * NQ);
+    s_R[el][j][slotR] = dw_add(pr2, dw_scale_sign(sgnR, Gqr));
+    s_S[el][i][slotS] = dw_add(ps2, dw_scale_sign(sgnS, Gqs));
+    eo_sync<NQ>(el);
+    {
+      dw_acc A, B;
+#pragma unroll
+      for (int m = 0; m < H; ++m) {
+        A.mac(s_Tp[pt][m], line[m]);
+        B.mac(s_Tm[pt][m], line[H + m]);
+      }
+      const dw a = A.get(), b = B.get();
+      *dst0 = dw_add(a, b);
+      *dst1 = dw_sub(b, a);
+    }
+    eo_sync<NQ>(el);
+    r_Aq[k] = dw_add(dw_add(mass, s_dr[el][j][i]), s_ds[el][j][i]);
+  }
+
+  {
+    dw E[H], O[H];
+#pragma unroll
+    for (int m = 0; m < H; ++m) {
+      const dw g0 = s_gt[m][tid], g1 = s_gt[N - m][tid];
+      E[m] = dw_add(g0, g1);
+      O[m] = dw_sub(g0, g1);
+    }
+#pragma unroll
+    for (int t = 0; t < H; ++t) {
+      dw_acc A, B;
+#pragma unroll
+      for (int m = 0; m < H; ++m) {
+        A.mac(s_Tp[t][m], E[m]);
+        B.mac(s_Tm[t][m], O[m]);
+      }
+      const dw a = A.get(), b = B.get();
+      r_Aq[t] = dw_add(r_Aq[t], dw_add(a, b));
+      r_Aq[N - t] = dw_add(r_Aq[N - t], dw_sub(b, a));
+    }
+  }
+
+  if (!active) return;
+#pragma unroll
+  for (int k = 0; k < NQ; ++k)
+    if (r_id[k] >= 0) atomicAdd(out + r_id[k], dw_to_double(r_Aq[k]));
+}
+
+int ax_hex_dw(const AxArgs<double, float2>& a, cudaStream_t s) {
+  if (a.Nelements <= 0) return LPG_OK;
+  if (a.N != 3 && a.N != 7) return set_error(LPG_ERR_UNSUPPORTED, "double-word operator: N must be 3 or 7");
+  if (a.Nglobal > 0) LPG_CUDA_TRY(cudaMemsetAsync(a.out, 0, sizeof(double) * a.Nglobal, s));
+  if (a.N == 7) {
+    const int64_t blocks = (a.Nelements + 3) / 4;
+    ax_hex_dw_kernel<8><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(
+        a.Nelements, a.elementList, a.g2l, reinterpret_cast<const dw*>(a.ggeo), a.geoStride,
+        reinterpret_cast<const dw*>(a.wJ), a.wJStride, a.D, a.lambda, a.lambdaE, a.q, a.out);
+  } else {
+    const int64_t blocks = (a.Nelements + 15) / 16;
+    ax_hex_dw_kernel<4><<<(unsigned)blocks, dim3(4, 4, 16), 0, s>>>(
+        a.Nelements, a.elementList, a.g2l, reinterpret_cast<const dw*>(a.ggeo), a.geoStride,
+        reinterpret_cast<const dw*>(a.wJ), a.wJStride, a.D, a.lambda, a.lambdaE, a.q, a.out);
+  }
+  LPG_LAUNCH_CHECK("ax_hex_dw_kernel");
+  return LPG_OK;
 }
 
 template <int NQ, typename T, typename G, int EPB, int STAGES>

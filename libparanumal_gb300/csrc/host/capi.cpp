@@ -103,6 +103,11 @@ int build(lpg_elliptic* h) {
   h->el = std::make_unique<Elliptic>();
   if ((rc = h->el->setup(&h->plat, c, N, lambda, lognormal ? &lamE : nullptr, h->plat.stream))) return rc;
   Elliptic* el = h->el.get();
+  const std::string opPrec = S.get("OPERATOR PRECISION", "FP64");
+  if (opPrec != "FP64" && opPrec != "DF64") return set_error(LPG_ERR_SETTINGS, "OPERATOR PRECISION must be FP64 or DF64");
+  if (opPrec == "DF64" && N != 3 && N != 7)
+    return set_error(LPG_ERR_UNSUPPORTED, "OPERATOR PRECISION DF64 needs POLYNOMIAL DEGREE 3 or 7");
+  el->opDW = (opPrec == "DF64");
   // right-hand side data
   const std::string rhsField = S.get("RHS FIELD", "SINE");
   if (rhsField == "GAUSSIAN SOURCES") {
@@ -369,6 +374,14 @@ extern "C" int lpg_elliptic_operator(lpg_elliptic* e, const double* q, double* A
   if (!e || !q || !Aq) return set_error(LPG_ERR_INVALID, "null argument");
   LPG_GUARD_BEGIN
   return e->el->Operator(q, Aq, pick(e, stream));
+  LPG_GUARD_END
+}
+
+extern "C" int lpg_elliptic_operator_df64(lpg_elliptic* e, const double* q, double* Aq, void* stream) {
+  if (!e || !q || !Aq) return set_error(LPG_ERR_INVALID, "null argument");
+  if (e->el->mesh.N != 3 && e->el->mesh.N != 7) return set_error(LPG_ERR_UNSUPPORTED, "DF64 operator: N must be 3 or 7");
+  LPG_GUARD_BEGIN
+  return e->el->OperatorDW(q, Aq, pick(e, stream));
   LPG_GUARD_END
 }
 

@@ -47,7 +47,7 @@ static const char* kKnownKeys[] = {
     "MULTIGRID DEGREES", "PRECONDITIONER PRECISION", "FINE SMOOTHER", "MESH JITTER",
     "MESH JITTER SEED", "LAMBDA FIELD", "LAMBDA SEED", "RHS FIELD", "RHS SEED", "RHS SOURCES",
     "SOLVER TOLERANCE", "MAXIMUM ITERATIONS", "SMOOTHER TRAINING PAIRS",
-    "LEARNED SMOOTHER STEPS"};
+    "LEARNED SMOOTHER STEPS", "OPERATOR PRECISION"};
 
 int Settings::parse(const std::string& text) {
   kv.clear();
@@ -140,6 +140,7 @@ template struct DevBuf<float>;
 template struct DevBuf<int32_t>;
 template struct DevBuf<int64_t>;
 template struct DevBuf<__nv_bfloat16>;
+template struct DevBuf<float2>;
 
 // ---------------------------------------------------------------- hashing
 uint64_t splitmix64(uint64_t x) {

@@ -88,6 +88,13 @@ int Mesh::make_f32(cudaStream_t s) {
   return convert<double, float>(Nq * Nq, D_d.p, D32.p, s);
 }
 
+int Mesh::make_dw(cudaStream_t s) {
+  if (geoDW.p) return LPG_OK;
+  int rc;
+  if ((rc = geoDW.alloc(E * 7 * Np))) return rc;
+  return split_to_float2(E * 7 * Np, geo.p, geoDW.p, s);
+}
+
 int Mesh::make_bf16(cudaStream_t s) {
   if (geo16.p) return LPG_OK;
   int rc;
@@ -166,7 +173,20 @@ int Elliptic::make_f32(bool bf16, cudaStream_t s) {
   return LPG_OK;
 }
 
+int Elliptic::OperatorDW(const double* q, double* Aq, cudaStream_t s) {
+  int rc;
+  if ((rc = mesh.make_dw(s))) return rc;
+  AxArgs<double, float2> a;
+  const int64_t Np = mesh.Np;
+  a.N = mesh.N; a.Nelements = mesh.E; a.g2l = g2l.p;
+  a.ggeo = mesh.geoDW.p; a.geoStride = 7 * Np; a.wJ = mesh.geoDW.p + 6 * Np; a.wJStride = 7 * Np;
+  a.D = mesh.D_d.p; a.lambda = lambda; a.lambdaE = hasLambdaE ? lambdaE.p : nullptr;
+  a.q = q; a.out = Aq; a.Nglobal = Nglobal;
+  return ax_hex_dw(a, s);
+}
+
 int Elliptic::Operator(const double* q, double* Aq, cudaStream_t s) {
+  if (opDW) return OperatorDW(q, Aq, s);
   AxArgs<double, double> a;
   const int64_t Np = mesh.Np;
   a.N = mesh.N; a.Nelements = mesh.E; a.g2l = g2l.p;
@@ -296,7 +316,16 @@ int Elliptic::OperatorHost(const double* qHost, double* AqHost, cudaStream_t s) 
                       (rc = pipe->Aq.alloc(std::max<int64_t>(Nglobal, 1)))))
     return rc;
   const int64_t Np = mesh.Np;
+  if (opDW && (rc = mesh.make_dw(s))) return rc;
   auto launch = [&](int64_t a0, int64_t a1) {
+    if (opDW) {
+      AxArgs<double, float2> a;
+      a.N = mesh.N; a.Nelements = a1 - a0; a.g2l = g2l.p + a0 * Np;
+      a.ggeo = mesh.geoDW.p + a0 * 7 * Np; a.geoStride = 7 * Np; a.wJ = a.ggeo + 6 * Np; a.wJStride = 7 * Np;
+      a.D = mesh.D_d.p; a.lambda = lambda; a.lambdaE = hasLambdaE ? lambdaE.p + a0 : nullptr;
+      a.q = pipe->q.p; a.out = pipe->Aq.p; a.Nglobal = 0;   // accumulate: the pipeline zeroed Aq
+      return ax_hex_dw(a, s);
+    }
     AxArgs<double, double> a;
     a.N = mesh.N; a.Nelements = a1 - a0; a.g2l = g2l.p + a0 * Np;
     a.ggeo = mesh.geo.p + a0 * 7 * Np; a.geoStride = 7 * Np; a.wJ = a.ggeo + 6 * Np; a.wJStride = 7 * Np;

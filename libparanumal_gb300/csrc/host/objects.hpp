@@ -102,9 +102,11 @@ struct Mesh {
   DevBuf<double> geo;             // [E][7][Np] FP64
   DevBuf<float> geo32, D32;       // FP32 copies (preconditioner)
   DevBuf<__nv_bfloat16> geo16;    // BF16 copy
+  DevBuf<float2> geoDW;           // double-word (hi, lo) copy for the double-word operator
   int setup(const MeshConfig& c, int N, cudaStream_t s);
   int make_f32(cudaStream_t s);
   int make_bf16(cudaStream_t s);
+  int make_dw(cudaStream_t s);
 };
 
 // ---------------------------------------------------------------- elliptic_t
@@ -148,7 +150,11 @@ struct Elliptic {
   int setup(Platform* p, const MeshConfig& c, int N, double lambda, const std::vector<double>* lamE,
             cudaStream_t s);
   int make_f32(bool bf16, cudaStream_t s);
+  // OPERATOR PRECISION: FP64 (default) or DF64 (double-FP32 words on the FP32 pipe,
+  // FP64-accurate) for every FP64 operator application of this object
+  bool opDW = false;
   int Operator(const double* q, double* Aq, cudaStream_t s);
+  int OperatorDW(const double* q, double* Aq, cudaStream_t s);
   int OperatorF32(const float* q, float* Aq, Prec prec, cudaStream_t s);
   // Aq = A q with host buffers (page-locked for overlap); returns when Aq is filled
   std::unique_ptr<HostPipe> pipe;

@@ -148,6 +148,22 @@ int convert(int64_t N, const Tin* x, Tout* y, cudaStream_t s) {
   return LPG_OK;
 }
 
+// x -> (hi, lo): hi = x rounded to FP32, lo = (x - hi) rounded to FP32 (setup-time split
+// of FP64 data for the double-word operator)
+__global__ void split_to_float2_kernel(const int64_t N, const double* __restrict__ x, float2* __restrict__ y) {
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x) {
+    const double v = x[n];
+    const float hi = __double2float_rn(v);
+    y[n] = make_float2(hi, __double2float_rn(v - (double)hi));
+  }
+}
+int split_to_float2(int64_t n, const double* x, float2* y, cudaStream_t s) {
+  if (n <= 0) return LPG_OK;
+  split_to_float2_kernel<<<grid_for(n, 256, kStreamCap), 256, 0, s>>>(n, x, y);
+  LPG_LAUNCH_CHECK("split_to_float2_kernel");
+  return LPG_OK;
+}
+
 __global__ void inverse_kernel(const int64_t N, const double* __restrict__ x, double* __restrict__ y,
                                const int guard) {
   for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x) {

@@ -174,6 +174,32 @@ def test_reduced_precision_operator_many_groups(bf16):
         assert err < tol, err
 
 
+DW_CASES = [
+    box(),                                                                     # jittered, N=7
+    box(**{"POLYNOMIAL DEGREE": 3, "BOX BOUNDARY FLAG": -1, "MESH JITTER": 0.0, "BOX NX": 3,
+           "BOX NY": 4, "BOX NZ": 2}),                                        # periodic, N=3
+    box(**{"LAMBDA FIELD": "LOGNORMAL", "LAMBDA SEED": 2, "BOX NX": 32, "BOX NY": 32, "BOX NZ": 16}),
+]
+
+
+@pytest.mark.parametrize("cfg", DW_CASES, ids=ids)
+def test_double_word_operator_matches_oracle(cfg):
+    """The double-FP32 operator agrees with the FP64 oracle to the FP64 bar (1e-12
+    relative, max-norm), also for inputs scaled by 1e-12 and 1e+12."""
+    e = lpg.Elliptic(cfg)
+    o = Oracle(cfg)
+    rng = np.random.default_rng(11)
+    for scale in (1.0, 1e-12, 1e12):
+        qh = scale * rng.uniform(-1, 1, e.Nglobal)
+        q = torch.tensor(qh, device="cuda")
+        Aq = torch.full_like(q, np.nan)
+        e.OperatorDF64(q, Aq)
+        torch.cuda.synchronize()
+        err = rel_err(Aq.cpu().numpy(), o.operator(qh))
+        print("double-word operator, scale %g: max rel err %.3g" % (scale, err))
+        assert err < 1e-12, (scale, err)
+
+
 HOST_CASES = [
     box(**{"BOX NX": 32, "BOX NY": 32, "BOX NZ": 16}),                 # 16384 elements: 4 chunks
     box(**{"POLYNOMIAL DEGREE": 3, "BOX BOUNDARY FLAG": -1, "MESH JITTER": 0.0, "BOX NX": 24,

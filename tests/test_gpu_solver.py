@@ -100,6 +100,20 @@ def test_mixed_precision_preconditioner_keeps_fp64_accuracy(prec):
     assert abs(r["error"] - ro["error"]) <= 0.01 * ro["error"]
 
 
+@pytest.mark.parametrize("prec", ["FP64", "FP32"])
+def test_double_word_outer_operator_solve(prec):
+    """OPERATOR PRECISION DF64: every FP64 operator application (outer FPCG, and the FP64
+    fine p-level) in double-FP32 words. The solve must behave as the FP64 method: same
+    iteration count (+-1) and the oracle's discretisation error and solution norm."""
+    s = dict(MG, **{"OPERATOR PRECISION": "DF64", "PRECONDITIONER PRECISION": prec})
+    r = lpg.Elliptic(s).Run()
+    ro = Oracle(MG).run()
+    assert r["converged"]
+    assert abs(r["iterations"] - ro["iterations"]) <= 1, (r["iterations"], ro["iterations"])
+    assert abs(r["error"] - ro["error"]) <= 0.01 * ro["error"]
+    assert abs(r["norm"] - ro["norm"]) < 1e-9 * ro["norm"]
+
+
 def test_lognormal_lambda_and_gaussian_sources_solve():
     s = dict(MG, **{"LAMBDA FIELD": "LOGNORMAL", "LAMBDA SEED": 2, "RHS FIELD": "GAUSSIAN SOURCES",
                     "RHS SEED": 3, "RHS SOURCES": 16})
