@@ -532,25 +532,18 @@ int MultiGrid::smooth(PLevel& L, const T* r, T* X, bool xIsZero, cudaStream_t s)
   const double invTheta = 1.0 / theta;
   const double sigma = theta / delta;
   double rho_n = 1. / sigma, rho_np1;
-  if (xIsZero) {
-    if ((rc = amxpy<T>(N, T(1), invDiag, r, T(0), RES, s))) return rc;
-  } else {
-    if ((rc = op<T>(L.el, X, RES, s))) return rc;
-    if ((rc = axpy<T>(N, T(1), r, T(-1), RES, s))) return rc;
-    if ((rc = amxpy<T>(N, T(1), invDiag, RES, T(0), RES, s))) return rc;
-  }
-  if ((rc = axpy<T>(N, (T)invTheta, RES, T(0), d, s))) return rc;
+  // same recurrence as the reference's loop (x += d before each application of A, and
+  // once at the end), with each x += d fused into the pass that produced d
+  if (!xIsZero && (rc = op<T>(L.el, X, RES, s))) return rc;
+  if ((rc = cheb_start<T>(N, invDiag, r, xIsZero ? nullptr : RES, RES, d, X, (T)invTheta, xIsZero, s))) return rc;
   for (int k = 0; k < opt.chebDegree; ++k) {
-    if (xIsZero && k == 0) rc = axpy<T>(N, T(1), d, T(0), X, s);
-    else rc = axpy<T>(N, T(1), d, T(1), X, s);
-    if (rc) return rc;
     if ((rc = op<T>(L.el, d, Ad, s))) return rc;
     rho_np1 = 1.0 / (2. * sigma - rho_n);
     const double rhoDivDelta = 2.0 * rho_np1 / delta;
-    if ((rc = cheb_update<T>(N, invDiag, Ad, RES, d, (T)(rho_np1 * rho_n), (T)rhoDivDelta, s))) return rc;
+    if ((rc = cheb_step<T>(N, invDiag, Ad, RES, d, X, (T)(rho_np1 * rho_n), (T)rhoDivDelta, s))) return rc;
     rho_n = rho_np1;
   }
-  return axpy<T>(N, T(1), d, T(1), X, s);
+  return LPG_OK;
 }
 
 template <typename T>

@@ -114,6 +114,13 @@ int add_scalar(int64_t N, const double* scalarDev, double scale, double* x, cuda
 // Chebyshev smoother vector updates (ellipticPreconMultiGridLevel.cpp:154-206)
 template <typename T>
 int cheb_update(int64_t N, const T* invDiag, const T* Ad, T* res, T* d, T a, T b, cudaStream_t s);
+// fused passes: start (res = invDiag (r - Ax) or invDiag r; d = invTheta res; x = d or x += d)
+// and step (res -= invDiag Ad; d = a d + b res; x += d)
+template <typename T>
+int cheb_start(int64_t N, const T* invDiag, const T* r, const T* Ax, T* res, T* d, T* x, T invTheta, bool xIsZero,
+               cudaStream_t s);
+template <typename T>
+int cheb_step(int64_t N, const T* invDiag, const T* Ad, T* res, T* d, T* x, T a, T b, cudaStream_t s);
 
 // ---------------------------------------------------------------- p-multigrid transfers
 // xC = assembled sum over coarse copies of P^T (weightF .* xF) per element (xC overwritten)

@@ -347,4 +347,55 @@ int cheb_update(int64_t N, const T* invDiag, const T* Ad, T* res, T* d, T a, T b
 template int cheb_update<double>(int64_t, const double*, const double*, double*, double*, double, double, cudaStream_t);
 template int cheb_update<float>(int64_t, const float*, const float*, float*, float*, float, float, cudaStream_t);
 
+// Fused Chebyshev passes (the same operations as the separate vector kernels, one sweep):
+// start: res = invDiag .* (r - Ax) (Ax == nullptr: res = invDiag .* r); d = invTheta res;
+//        x = d (xIsZero) or x += d
+// step:  res -= invDiag .* Ad; d = a d + b res; x += d
+template <typename T>
+__global__ void cheb_start_kernel(const int64_t N, const T* __restrict__ invDiag, const T* __restrict__ r,
+                                  const T* Ax, T* res, T* __restrict__ d, T* __restrict__ x, const T invTheta,
+                                  const int xIsZero) {   // Ax may alias res
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x) {
+    const T rn = Ax ? invDiag[n] * (r[n] - Ax[n]) : invDiag[n] * r[n];
+    res[n] = rn;
+    const T dn = invTheta * rn;
+    d[n] = dn;
+    x[n] = xIsZero ? dn : x[n] + dn;
+  }
+}
+template <typename T>
+__global__ void cheb_step_kernel(const int64_t N, const T* __restrict__ invDiag, const T* __restrict__ Ad,
+                                 T* __restrict__ res, T* __restrict__ d, T* __restrict__ x, const T a, const T b) {
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x) {
+    const T rn = res[n] - invDiag[n] * Ad[n];
+    res[n] = rn;
+    const T dn = b * rn + a * d[n];
+    d[n] = dn;
+    x[n] = x[n] + dn;
+  }
+}
+template <typename T>
+int cheb_start(int64_t N, const T* invDiag, const T* r, const T* Ax, T* res, T* d, T* x, T invTheta, bool xIsZero,
+               cudaStream_t s) {
+  if (N <= 0) return LPG_OK;
+  cheb_start_kernel<T><<<grid_for(N, 256, kStreamCap), 256, 0, s>>>(N, invDiag, r, Ax, res, d, x, invTheta,
+                                                                     xIsZero ? 1 : 0);
+  LPG_LAUNCH_CHECK("cheb_start_kernel");
+  return LPG_OK;
+}
+template <typename T>
+int cheb_step(int64_t N, const T* invDiag, const T* Ad, T* res, T* d, T* x, T a, T b, cudaStream_t s) {
+  if (N <= 0) return LPG_OK;
+  cheb_step_kernel<T><<<grid_for(N, 256, kStreamCap), 256, 0, s>>>(N, invDiag, Ad, res, d, x, a, b);
+  LPG_LAUNCH_CHECK("cheb_step_kernel");
+  return LPG_OK;
+}
+template int cheb_start<double>(int64_t, const double*, const double*, const double*, double*, double*, double*, double,
+                                bool, cudaStream_t);
+template int cheb_start<float>(int64_t, const float*, const float*, const float*, float*, float*, float*, float, bool,
+                               cudaStream_t);
+template int cheb_step<double>(int64_t, const double*, const double*, double*, double*, double*, double, double,
+                               cudaStream_t);
+template int cheb_step<float>(int64_t, const float*, const float*, float*, float*, float*, float, float, cudaStream_t);
+
 }  // namespace lpg
