@@ -141,6 +141,7 @@ int lpg_elliptic_destroy(lpg_elliptic *e);
 #define LPG_INFO_VCYCLES 10        /* V-cycles run with the learned fine smoother */
 #define LPG_INFO_FALLBACKS 11      /* of those, redone with the plain smoother */
 #define LPG_INFO_HOST_CHUNKS 12    /* element chunks of the host-buffer operator (0 before its first call) */
+#define LPG_INFO_IG_HISTORY 13     /* current dimension of the initial-guess history */
 int64_t lpg_elliptic_info(const lpg_elliptic *e, int what);
 
 /* Copy a named setup array to host memory: "GlobalToLocal" (int32), "ownerLocal" (int32),
@@ -189,6 +190,19 @@ int lpg_elliptic_solve(lpg_elliptic *e, double *x, double *r, double tol, int ma
 /* The assembled right-hand side of elliptic_t::Run (forcing, Dirichlet lifting,
  * Gather(Trans)) into a device vector r (Nglobal). */
 int lpg_elliptic_rhs(lpg_elliptic *e, double *r, void *stream);
+/* Initial-guess strategies of linearSolver_t (include/initialGuess.hpp:38-162), chosen by
+ * [INITIAL GUESS STRATEGY] NONE (default) | ZERO | CLASSIC | QR | EXTRAP with
+ * [INITIAL GUESS HISTORY SPACE DIMENSION] (1..32), [INITIAL GUESS EXTRAP DEGREE] and
+ * [INITIAL GUESS EXTRAP COEFFS METHOD] MINNORM | CPQR. lpg_elliptic_solve forms the initial
+ * guess from the history before the solve and adds the solution afterwards
+ * (linearSolver.cpp:30-43). lpg_elliptic_initial_guess only forms it
+ * (initialGuessStrategy_t::FormInitialGuess): x (Nglobal, device) from rhs (device). */
+int lpg_elliptic_initial_guess(lpg_elliptic *e, double *x, const double *rhs, void *stream);
+/* Extrapolation weights (Extrap::extrapCoeffs, initialGuess.cpp:440-468): coeffs_out gets
+ * `history` weights of the last `history` equally spaced solutions, exact one step ahead
+ * for polynomials of degree `degree`; cpqr = 0 minimum-norm, 1 column-pivoted QR basic
+ * solution. Host only. */
+int lpg_extrap_coeffs(int degree, int history, int cpqr, double *coeffs_out);
 /* elliptic_t::Run (ellipticRun.cpp:30-248): rhs, timed solve, scatter + AddBC, then the
  * mass-weighted solution norm and, for manufactured data, the error norm.
  * xL_host (Nlocal doubles) may be NULL; solve_seconds is the wall time of the solve. */

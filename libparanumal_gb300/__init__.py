@@ -19,7 +19,8 @@ LPG_OK = 0
 STATUS = {0: "OK", -1: "INVALID", -2: "CUDA", -3: "UNSUPPORTED", -4: "NOT_CONVERGED",
           -5: "ALLOC", -6: "SETTINGS", -7: "BREAKDOWN"}
 INFO = dict(nelements=0, np=1, nglobal=2, nlocal=3, n=4, allneumann=5, mg_plevels=6,
-            mg_amglevels=7, coarse_n=8, device_bytes=9, vcycles=10, fallbacks=11, host_chunks=12)
+            mg_amglevels=7, coarse_n=8, device_bytes=9, vcycles=10, fallbacks=11, host_chunks=12,
+            ig_history=13)
 
 _lib = None
 
@@ -73,6 +74,8 @@ def lib():
         "lpg_elliptic_operator_f32": [vp, vp, vp, i32, vp],
         "lpg_elliptic_operator_host": [vp, vp, vp],
         "lpg_elliptic_operator_df64": [vp, vp, vp, vp],
+        "lpg_elliptic_initial_guess": [vp, vp, vp, vp],
+        "lpg_extrap_coeffs": [i32, i32, i32, vp],
         "lpg_elliptic_operator_host_f32": [vp, vp, vp, i32],
         "lpg_elliptic_precon": [vp, vp, vp, vp],
         "lpg_elliptic_solve": [vp, vp, vp, f64, i32, ctypes.POINTER(ctypes.c_int)],
@@ -209,6 +212,10 @@ class Elliptic:
         check(lib().lpg_elliptic_operator_f32(self.h, _ptr(q), _ptr(Aq), 1 if bf16geo else 0,
                                               stream or None))
 
+    def initial_guess(self, x, rhs, stream=0):
+        """x = the configured initial-guess strategy's guess for rhs (device vectors)."""
+        check(lib().lpg_elliptic_initial_guess(self.h, _ptr(x), _ptr(rhs), stream or None))
+
     def OperatorDF64(self, q, Aq, stream=0):
         """FP64-accurate operator in double-FP32 words (device vectors, FP64 in and out)."""
         check(lib().lpg_elliptic_operator_df64(self.h, _ptr(q), _ptr(Aq), stream or None))
@@ -259,6 +266,13 @@ class Elliptic:
             check(st)
         return dict(iterations=it.value, norm=nrm.value, error=err.value, solve_seconds=sec.value,
                     xL=xL, converged=(st == LPG_OK))
+
+
+def extrap_coeffs(degree, history, cpqr=False):
+    """Extrapolation weights of the EXTRAP initial guess (host computation)."""
+    c = np.zeros(history)
+    check(lib().lpg_extrap_coeffs(degree, history, 1 if cpqr else 0, c.ctypes.data_as(ctypes.c_void_p)))
+    return c
 
 
 def train_smoother(settings, nsolves=4, samples_per_solve=5000, epochs=30, batch=250, lr=1e-3, seed=7):

@@ -55,7 +55,9 @@ def build_library(force=False, verbose=False, jobs=None):
     cu, cpp, hdrs = _sources()
     nvflags = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
                       "-Xcompiler", "-fPIC,-fopenmp", "-I" + INCLUDE]
-    ccflags = ["-O3", "-std=c++17", "-fPIC", "-fopenmp", "-I" + INCLUDE,
+    # -ffp-contract=off: host arithmetic rounds the same on x86-64 and aarch64 (where g++
+    # would otherwise fuse multiply-adds)
+    ccflags = ["-O3", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", "-I" + INCLUDE,
                "-I" + os.path.join(cuda, "include")]
     fp = _fingerprint(cu + cpp + hdrs + [__file__], nvflags + ccflags)
     stamp = os.path.join(OUT, "fingerprint")

@@ -2,6 +2,7 @@
 // kernel entry points for gather-scatter and vector operations. No C++ exception
 // crosses this boundary; every function returns an LPG status.
 #include "objects.hpp"
+#include "initial_guess.hpp"
 #include "learned.hpp"
 #include "../mlp.hpp"
 
@@ -22,6 +23,7 @@ struct lpg_elliptic {
   std::unique_ptr<Precon> precon;
   PCGWork work;
   std::unique_ptr<LearnedSmoother> learned;
+  std::unique_ptr<InitialGuess> ig;
   bool flexible = false, stopRhs = false;
   double tol = 1e-8;
   int maxit = 5000;
@@ -168,6 +170,8 @@ int build(lpg_elliptic* h) {
       (rc = h->norms.alloc(2)))
     return rc;
   if ((rc = h->work.ensure(Ng))) return rc;
+  h->ig = make_initial_guess(S, &h->plat, Ng, &rc);
+  if (rc) return rc;
   LPG_CUDA_TRY(cudaStreamSynchronize(h->plat.stream));
   return LPG_OK;
 }
@@ -283,6 +287,7 @@ extern "C" int64_t lpg_elliptic_info(const lpg_elliptic* e, int what) {
     case LPG_INFO_VCYCLES: return e->precon ? e->precon->vcycles() : 0;
     case LPG_INFO_FALLBACKS: return e->precon ? e->precon->fallbacks() : 0;
     case LPG_INFO_HOST_CHUNKS: return e->el->pipe ? e->el->pipe->K : 0;
+    case LPG_INFO_IG_HISTORY: return e->ig ? e->ig->history() : 0;
     default: return -1;
   }
 }
@@ -444,12 +449,38 @@ static int solve_impl(lpg_elliptic* e, double* x, double* r, double tol, int max
     if ((rc = sum(el->Nglobal, r, e->plat.scalars.p + 1, e->plat.partials.p, s))) return rc;
     if ((rc = add_scalar(el->Nglobal, e->plat.scalars.p + 1, -el->allNeumannScale * el->allNeumannScale, r, s))) return rc;
   }
+  // linearSolver_t::Solve (linearSolver.cpp:30-43): initial guess from the history,
+  // solve, then the new solution goes into the history
+  if ((rc = e->ig->form(x, r, s))) return rc;
   PCGResult res;
   if ((rc = pcg_solve(&e->plat, el, e->precon.get(), e->work, e->flexible, e->stopRhs, x, r, tol, maxit, res))) return rc;
   if (iters) *iters = res.iters;
+  if (!res.breakdown && (rc = e->ig->update(el, x, s))) return rc;
   if (res.breakdown) return set_error(LPG_ERR_BREAKDOWN, "(F)PCG breakdown: non-positive p.Ap or non-finite residual");
   if (res.iters >= maxit) return set_error(LPG_ERR_NOT_CONVERGED, "(F)PCG reached the iteration limit");
   return LPG_OK;
+}
+
+extern "C" int lpg_elliptic_initial_guess(lpg_elliptic* e, double* x, const double* rhs, void* stream) {
+  if (!e || !x || !rhs) return set_error(LPG_ERR_INVALID, "null argument");
+  LPG_GUARD_BEGIN
+  cudaStream_t s = pick(e, stream);
+  int rc = e->ig->form(x, rhs, s);
+  if (rc) return rc;
+  LPG_CUDA_TRY(cudaStreamSynchronize(s));
+  return LPG_OK;
+  LPG_GUARD_END
+}
+
+extern "C" int lpg_extrap_coeffs(int degree, int history, int cpqr, double* coeffs_out) {
+  if (!coeffs_out) return set_error(LPG_ERR_INVALID, "null argument");
+  LPG_GUARD_BEGIN
+  std::vector<double> c;
+  const int rc = extrap_coeffs(degree, history, cpqr != 0, c);
+  if (rc) return rc;
+  std::memcpy(coeffs_out, c.data(), sizeof(double) * c.size());
+  return LPG_OK;
+  LPG_GUARD_END
 }
 
 extern "C" int lpg_elliptic_solve(lpg_elliptic* e, double* x, double* r, double tol, int maxit, int* iters) {

@@ -47,7 +47,8 @@ static const char* kKnownKeys[] = {
     "MULTIGRID DEGREES", "PRECONDITIONER PRECISION", "FINE SMOOTHER", "MESH JITTER",
     "MESH JITTER SEED", "LAMBDA FIELD", "LAMBDA SEED", "RHS FIELD", "RHS SEED", "RHS SOURCES",
     "SOLVER TOLERANCE", "MAXIMUM ITERATIONS", "SMOOTHER TRAINING PAIRS",
-    "LEARNED SMOOTHER STEPS", "OPERATOR PRECISION"};
+    "LEARNED SMOOTHER STEPS", "OPERATOR PRECISION", "INITIAL GUESS STRATEGY",
+    "INITIAL GUESS HISTORY SPACE DIMENSION", "INITIAL GUESS EXTRAP DEGREE", "INITIAL GUESS EXTRAP COEFFS METHOD"};
 
 int Settings::parse(const std::string& text) {
   kv.clear();

@@ -132,6 +132,22 @@ template <typename T>
 int pmg_prolongate_map(int Nf, int Nc, int64_t E, const int32_t* g2lC, const T* xC, const T* P,
                        const int32_t* g2lF, const int32_t* ownerF, T* xF, cudaStream_t s);
 
+// ---------------------------------------------------------------- initial-guess history
+constexpr int kMaxHistory = 32;        // history space dimension limit
+constexpr int kMultiDotBlocks = 1024;  // partial sums per history vector
+struct HistCoeffs {
+  double v[kMaxHistory];
+};
+// partials[m * nblocks + b] (m < k): block shares of Q_m . x; *nblocks set
+int multi_dot(int64_t N, int k, const double* x, const double* Q, double* partials, int* nblocks, cudaStream_t s);
+// out = u + beta sum_m c[m] Q_m (u may be null = 0; out may alias u)
+int combine(int64_t N, int k, const double* u, double beta, const HistCoeffs& c, const double* Q, double* out,
+            cudaStream_t s);
+// rotations i = 0..dim-2 on column pairs (i, i+1) of Q and U, then column dim-1 = 0
+int givens_columns(int64_t N, int dim, const HistCoeffs& c, const HistCoeffs& sn, double* Q, double* U, cudaStream_t s);
+// x = sum_i d[i] H_{(i + shift) % nh}
+int extrap(int64_t N, int nh, int shift, const HistCoeffs& d, const double* H, double* x, cudaStream_t s);
+
 // ---------------------------------------------------------------- sparse / dense
 // y = alpha A x + beta y (CSR, FP64)
 int csr_spmv(int64_t Nrows, const int64_t* rowStarts, const int32_t* cols, const double* vals,

@@ -6,6 +6,8 @@
 // sums the partials in a fixed tree. The result stays in device memory, so the
 // caller decides when (and whether) to synchronise; the summation order depends
 // only on N, which makes repeated runs bit-identical.
+#include <algorithm>
+
 #include "lpg_common.cuh"
 #include "lpg_internal.hpp"
 
@@ -397,5 +399,107 @@ template int cheb_start<float>(int64_t, const float*, const float*, const float*
 template int cheb_step<double>(int64_t, const double*, const double*, double*, double*, double*, double, double,
                                cudaStream_t);
 template int cheb_step<float>(int64_t, const float*, const float*, float*, float*, float*, float, float, cudaStream_t);
+
+// ---------------------------------------------------------------- initial-guess history
+// Kernels of the initial-guess strategies (libs/linearSolver/okl/igBasisInnerProducts.okl,
+// igReconstruct.okl, igDropQRFirstColumn.okl, igExtrap.okl). History vectors are stored
+// contiguously, column m at Q + m N.
+
+// partials[m * nb + b] = block b's share of Q_m . x for m < k (host sums the nb entries)
+__global__ void __launch_bounds__(256)
+multi_dot_kernel(const int64_t N, const int k, const double* __restrict__ x, const double* __restrict__ Q,
+                 double* __restrict__ partials) {
+  __shared__ double s_w[8];
+  double acc[kMaxHistory];
+#pragma unroll
+  for (int m = 0; m < kMaxHistory; ++m) acc[m] = 0;
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x) {
+    const double xn = x[n];
+#pragma unroll
+    for (int m = 0; m < kMaxHistory; ++m)
+      if (m < k) acc[m] += Q[(int64_t)m * N + n] * xn;
+  }
+  for (int m = 0; m < k; ++m) {
+    double v = acc[m];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) s_w[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s_w[w];
+      partials[(int64_t)m * gridDim.x + blockIdx.x] = t;
+    }
+  }
+}
+int multi_dot(int64_t N, int k, const double* x, const double* Q, double* partials, int* nblocks, cudaStream_t s) {
+  if (k < 0 || k > kMaxHistory) return set_error(LPG_ERR_INVALID, "multi_dot: history dimension out of range");
+  const int nb = (int)std::max<int64_t>(1, std::min<int64_t>((N + 255) / 256, kMultiDotBlocks));
+  *nblocks = nb;
+  if (k == 0) return LPG_OK;
+  multi_dot_kernel<<<nb, 256, 0, s>>>(N, k, x, Q, partials);
+  LPG_LAUNCH_CHECK("multi_dot_kernel");
+  return LPG_OK;
+}
+
+// out = u + beta * sum_m c[m] Q_m  (out may be u)
+__global__ void combine_kernel(const int64_t N, const int k, const double* u, const double beta, const HistCoeffs c,
+                               const double* __restrict__ Q, double* out) {
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x) {
+    double r = u ? u[n] : 0.0;
+    for (int m = 0; m < k; ++m) r += beta * c.v[m] * Q[(int64_t)m * N + n];
+    out[n] = r;
+  }
+}
+int combine(int64_t N, int k, const double* u, double beta, const HistCoeffs& c, const double* Q, double* out,
+            cudaStream_t s) {
+  if (N <= 0) return LPG_OK;
+  combine_kernel<<<grid_for(N, 256, kStreamCap), 256, 0, s>>>(N, k, u, beta, c, Q, out);
+  LPG_LAUNCH_CHECK("combine_kernel");
+  return LPG_OK;
+}
+
+// Rotations i = 0..dim-2 applied in order to columns (i, i+1) of Q and U:
+// (Q_i, Q_i+1) <- (c Q_i + s Q_i+1, -s Q_i + c Q_i+1); then column dim-1 = 0
+__global__ void givens_columns_kernel(const int64_t N, const int dim, const HistCoeffs c, const HistCoeffs sn,
+                                      double* __restrict__ Q, double* __restrict__ U) {
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x) {
+    double q1 = Q[n], u1 = U[n];
+    for (int i = 0; i < dim - 1; ++i) {
+      const double q0 = q1, u0 = u1;
+      q1 = Q[(int64_t)(i + 1) * N + n];
+      u1 = U[(int64_t)(i + 1) * N + n];
+      Q[(int64_t)i * N + n] = c.v[i] * q0 + sn.v[i] * q1;
+      U[(int64_t)i * N + n] = c.v[i] * u0 + sn.v[i] * u1;
+      q1 = -sn.v[i] * q0 + c.v[i] * q1;
+      u1 = -sn.v[i] * u0 + c.v[i] * u1;
+    }
+    Q[(int64_t)(dim - 1) * N + n] = 0;
+    U[(int64_t)(dim - 1) * N + n] = 0;
+  }
+}
+int givens_columns(int64_t N, int dim, const HistCoeffs& c, const HistCoeffs& sn, double* Q, double* U, cudaStream_t s) {
+  if (N <= 0 || dim <= 0) return LPG_OK;
+  givens_columns_kernel<<<grid_for(N, 256, kStreamCap), 256, 0, s>>>(N, dim, c, sn, Q, U);
+  LPG_LAUNCH_CHECK("givens_columns_kernel");
+  return LPG_OK;
+}
+
+// x = sum_i d[i] * H_{(i + shift) % nh} over the nonzero d[i]
+__global__ void extrap_kernel(const int64_t N, const int nh, const int shift, const HistCoeffs d,
+                              const double* __restrict__ H, double* __restrict__ x) {
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x) {
+    double r = 0;
+    for (int i = 0; i < nh; ++i)
+      if (d.v[i] != 0.0) r += d.v[i] * H[(int64_t)((i + shift) % nh) * N + n];
+    x[n] = r;
+  }
+}
+int extrap(int64_t N, int nh, int shift, const HistCoeffs& d, const double* H, double* x, cudaStream_t s) {
+  if (N <= 0) return LPG_OK;
+  extrap_kernel<<<grid_for(N, 256, kStreamCap), 256, 0, s>>>(N, nh, shift, d, H, x);
+  LPG_LAUNCH_CHECK("extrap_kernel");
+  return LPG_OK;
+}
 
 }  // namespace lpg
