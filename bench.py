@@ -53,6 +53,7 @@ def parse():
     ap.add_argument("--solve-precs", default="FP64,FP32,BF16GEO,FP64+DF64,FP32+DF64,BF16GEO+DF64",
                     help="preconditioner precisions; P+DF64 also runs the FP64 operator in double-FP32 words")
     ap.add_argument("--solve-reps", type=int, default=2)
+    ap.add_argument("--solver", default="FPCG", choices=["FPCG", "NBFPCG", "PCG"], help="LINEAR SOLVER of --solve")
     ap.add_argument("--learned", action="store_true", help="learned-smoother training and solve comparison")
     ap.add_argument("--mlp", action="store_true", help="learned-smoother MLP inference (lpg_mlp_forward_bf16) timing")
     ap.add_argument("--train-nx", type=int, default=32)
@@ -201,6 +202,7 @@ def run_solves(a):
         # "P+DF64": preconditioner precision P, FP64 operator applications in double-FP32 words
         base, _, op = prec.partition("+")
         extra = {"OPERATOR PRECISION": op} if op else {}
+        extra["LINEAR SOLVER"] = a.solver
         e = lpg.Elliptic(solve_settings(a.nx, a.N, base, **extra))
         setup = time.time() - t0
         runs = [e.Run() for _ in range(a.solve_reps)]
@@ -211,8 +213,8 @@ def run_solves(a):
                      "mg_plevels": e.info("mg_plevels"), "amg_levels": e.info("mg_amglevels"),
                      "coarse_n": e.info("coarse_n"), "nglobal": e.Nglobal}
         e.close()
-    print(json.dumps({"workload": "FPCG + p-MG 7->3->1 time-to-1e-8, %d^3 jittered hex, N=%d, lambda=0"
-                      % (a.nx, a.N), "results": res}), flush=True)
+    print(json.dumps({"workload": "%s + p-MG 7->3->1 time-to-1e-8, %d^3 jittered hex, N=%d, lambda=0"
+                      % (a.solver, a.nx, a.N), "results": res}), flush=True)
 
 
 def run_learned(a):

@@ -24,7 +24,8 @@ struct lpg_elliptic {
   PCGWork work;
   std::unique_ptr<LearnedSmoother> learned;
   std::unique_ptr<InitialGuess> ig;
-  bool flexible = false, stopRhs = false;
+  bool flexible = false, stopRhs = false, nonblocking = false;
+  NBWork nbwork;
   double tol = 1e-8;
   int maxit = 5000;
   DevBuf<double> q_in, Aq_out, x, r, xL, norms;
@@ -130,8 +131,10 @@ int build(lpg_elliptic* h) {
   }
   // linear solver
   const std::string ls = S.get("LINEAR SOLVER", "PCG");
-  if (ls != "PCG" && ls != "FPCG") return set_error(LPG_ERR_UNSUPPORTED, "LINEAR SOLVER must be PCG or FPCG");
+  if (ls != "PCG" && ls != "FPCG" && ls != "NBFPCG")
+    return set_error(LPG_ERR_UNSUPPORTED, "LINEAR SOLVER must be PCG, FPCG or NBFPCG");
   h->flexible = (ls == "FPCG");
+  h->nonblocking = (ls == "NBFPCG");
   h->stopRhs = S.is("LINEAR SOLVER STOPPING CRITERION", "ABS/REL-RHS-2NORM");
   h->tol = S.getd("SOLVER TOLERANCE", 1e-8);
   h->maxit = S.geti("MAXIMUM ITERATIONS", 5000);
@@ -453,7 +456,9 @@ static int solve_impl(lpg_elliptic* e, double* x, double* r, double tol, int max
   // solve, then the new solution goes into the history
   if ((rc = e->ig->form(x, r, s))) return rc;
   PCGResult res;
-  if ((rc = pcg_solve(&e->plat, el, e->precon.get(), e->work, e->flexible, e->stopRhs, x, r, tol, maxit, res))) return rc;
+  if (e->nonblocking) rc = nbfpcg_solve(&e->plat, el, e->precon.get(), e->nbwork, x, r, tol, maxit, res);
+  else rc = pcg_solve(&e->plat, el, e->precon.get(), e->work, e->flexible, e->stopRhs, x, r, tol, maxit, res);
+  if (rc) return rc;
   if (iters) *iters = res.iters;
   if (!res.breakdown && (rc = e->ig->update(el, x, s))) return rc;
   if (res.breakdown) return set_error(LPG_ERR_BREAKDOWN, "(F)PCG breakdown: non-positive p.Ap or non-finite residual");

@@ -216,6 +216,15 @@ struct PCGWork {
 };
 int pcg_solve(Platform* plat, Elliptic* el, Precon* pc, PCGWork& w, bool flexible, bool stopRhs,
               double* x, double* r, double tol, int maxit, PCGResult& res);
+// non-blocking flexible PCG (linearSolverNBFPCG.cpp:72-186): fused update + 4 inner
+// products per iteration; stopping criterion relative to the initial residual
+struct NBWork {
+  DevBuf<double> u, p, w, n, m, s, z, q, Ax, partials;
+  std::vector<double> host;
+  int ensure(int64_t n);
+};
+int nbfpcg_solve(Platform* plat, Elliptic* el, Precon* pc, NBWork& w, double* x, double* r, double tol, int maxit,
+                 PCGResult& res);
 
 // degree schedule of the p-multigrid hierarchy (ellipticPreconMultiGrid.cpp:49-84)
 std::vector<int> degree_schedule(int N, const std::string& coarsening, const std::vector<int>& explicitList);

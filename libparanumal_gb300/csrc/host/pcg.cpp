@@ -65,6 +65,74 @@ int pcg_solve(Platform* plat, Elliptic* el, Precon* pc, PCGWork& w, bool flexibl
   return LPG_OK;
 }
 
+int NBWork::ensure(int64_t n) {
+  if (u.n == n) return LPG_OK;
+  int rc;
+  if ((rc = u.alloc(n)) || (rc = p.alloc(n)) || (rc = w.alloc(n)) || (rc = this->n.alloc(n)) || (rc = m.alloc(n)) ||
+      (rc = s.alloc(n)) || (rc = z.alloc(n)) || (rc = q.alloc(n)) || (rc = Ax.alloc(n)) || (rc = partials.alloc(4 * 1024)))
+    return rc;
+  host.resize(4 * 1024);
+  return LPG_OK;
+}
+
+// sums of the k block partial arrays, in block order (update0/1NBFPCG's host loop)
+static int nb_sums(NBWork& w, int k, int nb, cudaStream_t s, double* out) {
+  LPG_CUDA_TRY(cudaMemcpyAsync(w.host.data(), w.partials.p, sizeof(double) * k * nb, cudaMemcpyDeviceToHost, s));
+  LPG_CUDA_TRY(cudaStreamSynchronize(s));
+  for (int j = 0; j < k; ++j) {
+    double t = w.host[(size_t)j * nb];
+    for (int b = 1; b < nb; ++b) t += w.host[(size_t)j * nb + b];
+    out[j] = t;
+  }
+  return LPG_OK;
+}
+
+int nbfpcg_solve(Platform* plat, Elliptic* el, Precon* pc, NBWork& w, double* x, double* r, double tol, int maxit,
+                 PCGResult& res) {
+  const int64_t N = el->Nglobal;
+  cudaStream_t s = plat->stream;
+  int rc, nb = 0;
+  if ((rc = w.ensure(N))) return rc;
+  const size_t bytes = sizeof(double) * N;
+  if ((rc = el->Operator(x, w.Ax.p, s)) || (rc = axpy<double>(N, -1.0, w.Ax.p, 1.0, r, s))) return rc;
+  if ((rc = pc->apply(r, w.u.p, s))) return rc;
+  LPG_CUDA_TRY(cudaMemcpyAsync(w.p.p, w.u.p, bytes, cudaMemcpyDeviceToDevice, s));
+  if ((rc = el->Operator(w.p.p, w.w.p, s))) return rc;
+  double d3[3];
+  if ((rc = nb_dots3(N, w.u.p, r, w.w.p, w.partials.p, &nb, s)) || (rc = nb_sums(w, 3, nb, s, d3))) return rc;
+  if ((rc = pc->apply(w.w.p, w.m.p, s)) || (rc = el->Operator(w.m.p, w.n.p, s))) return rc;
+  LPG_CUDA_TRY(cudaMemcpyAsync(w.s.p, w.w.p, bytes, cudaMemcpyDeviceToDevice, s));
+  LPG_CUDA_TRY(cudaMemcpyAsync(w.q.p, w.m.p, bytes, cudaMemcpyDeviceToDevice, s));
+  LPG_CUDA_TRY(cudaMemcpyAsync(w.z.p, w.n.p, bytes, cudaMemcpyDeviceToDevice, s));
+  double gamma0 = d3[0], delta0 = d3[1], rdotr0 = d3[2];
+  double eta0 = delta0, alpha0 = gamma0 / eta0, beta0 = 0.0;
+  const double TOL = std::max(tol * tol * rdotr0, tol * tol);
+  int iter;
+  res.breakdown = false;
+  for (iter = 0; iter < maxit; ++iter) {
+    if (rdotr0 <= TOL) break;
+    double d4[4];
+    // x += a p, r -= a s, u -= a q, w -= a z, n = w - r, with the four inner products
+    if ((rc = nb_update(N, alpha0, w.p.p, w.s.p, w.q.p, w.z.p, x, r, w.u.p, w.w.p, w.n.p, w.partials.p, &nb, s)))
+      return rc;
+    if ((rc = pc->apply(w.n.p, w.m.p, s))) return rc;                             // m = M (w - r)
+    if ((rc = axpy<double>(N, 1.0, w.u.p, 1.0, w.m.p, s))) return rc;            // m += u
+    if ((rc = el->Operator(w.m.p, w.n.p, s))) return rc;                          // n = A m
+    if ((rc = nb_sums(w, 4, nb, s, d4))) return rc;
+    gamma0 = d4[0];
+    beta0 = -d4[1] / eta0;
+    delta0 = d4[2];
+    rdotr0 = d4[3];
+    if ((rc = nb_directions(N, beta0, w.u.p, w.w.p, w.m.p, w.n.p, w.p.p, w.s.p, w.q.p, w.z.p, s))) return rc;
+    eta0 = delta0 - beta0 * beta0 * eta0;
+    alpha0 = gamma0 / eta0;
+    if (!std::isfinite(rdotr0) || !std::isfinite(alpha0)) { res.breakdown = true; ++iter; break; }
+  }
+  res.iters = iter;
+  res.rdotr = rdotr0;
+  return LPG_OK;
+}
+
 std::vector<int> degree_schedule(int N, const std::string& coarsening, const std::vector<int>& explicitList) {
   std::vector<int> deg;
   if (!explicitList.empty()) {

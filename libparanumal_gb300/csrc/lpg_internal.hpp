@@ -148,6 +148,16 @@ int givens_columns(int64_t N, int dim, const HistCoeffs& c, const HistCoeffs& sn
 // x = sum_i d[i] H_{(i + shift) % nh}
 int extrap(int64_t N, int nh, int shift, const HistCoeffs& d, const double* H, double* x, cudaStream_t s);
 
+// ---------------------------------------------------------------- NBFPCG passes
+// partials[k * nb + b] (nb <= 1024 blocks, *nb set): u.r, u.w, r.r
+int nb_dots3(int64_t N, const double* u, const double* r, const double* w, double* partials, int* nb, cudaStream_t s);
+// x += a p; r -= a s; u -= a q; w -= a z; nv = w - r; partials: u.r, u.s, u.w, r.r
+int nb_update(int64_t N, double a, const double* p, const double* sv, const double* q, const double* z, double* x,
+              double* r, double* u, double* w, double* nv, double* partials, int* nb, cudaStream_t s);
+// p = u + beta p; s = w + beta s; q = m + beta q; z = nv + beta z
+int nb_directions(int64_t N, double beta, const double* u, const double* w, double* m, const double* nv, double* p,
+                  double* sv, double* q, double* z, cudaStream_t s);
+
 // ---------------------------------------------------------------- sparse / dense
 // y = alpha A x + beta y (CSR, FP64)
 int csr_spmv(int64_t Nrows, const int64_t* rowStarts, const int32_t* cols, const double* vals,

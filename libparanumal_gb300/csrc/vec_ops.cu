@@ -502,4 +502,98 @@ int extrap(int64_t N, int nh, int shift, const HistCoeffs& d, const double* H, d
   return LPG_OK;
 }
 
+// ---------------------------------------------------------------- NBFPCG
+// Fused passes of the non-blocking flexible PCG (okl/linearSolverUpdateNBFPCG.okl):
+// block partial sums land in partials[k * nb + b]; the host adds them in block order.
+template <int K>
+__device__ __forceinline__ void block_partials(double (&v)[K], double* partials) {
+  __shared__ double s_w[K][8];
+#pragma unroll
+  for (int k = 0; k < K; ++k)
+    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+  if ((threadIdx.x & 31) == 0)
+#pragma unroll
+    for (int k = 0; k < K; ++k) s_w[k][threadIdx.x >> 5] = v[k];
+  __syncthreads();
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      double t = 0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s_w[k][w];
+      partials[(int64_t)k * gridDim.x + blockIdx.x] = t;
+    }
+}
+
+// u.r, u.w, r.r (update0NBFPCG)
+__global__ void __launch_bounds__(256)
+nb_dots3_kernel(const int64_t N, const double* __restrict__ u, const double* __restrict__ r,
+                const double* __restrict__ w, double* __restrict__ partials) {
+  double v[3] = {0, 0, 0};
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x) {
+    const double un = u[n], rn = r[n];
+    v[0] += un * rn;
+    v[1] += un * w[n];
+    v[2] += rn * rn;
+  }
+  block_partials<3>(v, partials);
+}
+// x += a p; r -= a s; u -= a q; w -= a z; nv = w - r; then u.r, u.s, u.w, r.r (update1NBFPCG,
+// with the n = w - r of the next preconditioner input folded in)
+__global__ void __launch_bounds__(256)
+nb_update_kernel(const int64_t N, const double a, const double* __restrict__ p, const double* __restrict__ s,
+                 const double* __restrict__ q, const double* __restrict__ z, double* __restrict__ x,
+                 double* __restrict__ r, double* __restrict__ u, double* __restrict__ w, double* __restrict__ nv,
+                 double* __restrict__ partials) {
+  double v[4] = {0, 0, 0, 0};
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x) {
+    const double sn = s[n];
+    x[n] += a * p[n];
+    const double rn = r[n] - a * sn, un = u[n] - a * q[n], wn = w[n] - a * z[n];
+    r[n] = rn;
+    u[n] = un;
+    w[n] = wn;
+    nv[n] = wn - rn;
+    v[0] += un * rn;
+    v[1] += un * sn;
+    v[2] += un * wn;
+    v[3] += rn * rn;
+  }
+  block_partials<4>(v, partials);
+}
+static int nb_blocks(int64_t N) { return (int)std::max<int64_t>(1, std::min<int64_t>((N + 255) / 256, 1024)); }
+int nb_dots3(int64_t N, const double* u, const double* r, const double* w, double* partials, int* nb, cudaStream_t s) {
+  *nb = nb_blocks(N);
+  nb_dots3_kernel<<<*nb, 256, 0, s>>>(N, u, r, w, partials);
+  LPG_LAUNCH_CHECK("nb_dots3_kernel");
+  return LPG_OK;
+}
+int nb_update(int64_t N, double a, const double* p, const double* sv, const double* q, const double* z, double* x,
+              double* r, double* u, double* w, double* nv, double* partials, int* nb, cudaStream_t s) {
+  *nb = nb_blocks(N);
+  nb_update_kernel<<<*nb, 256, 0, s>>>(N, a, p, sv, q, z, x, r, u, w, nv, partials);
+  LPG_LAUNCH_CHECK("nb_update_kernel");
+  return LPG_OK;
+}
+// p = u + beta p; s = w + beta s; q = m + beta q; z = n + beta z (the search-direction
+// updates of linearSolverNBFPCG.cpp:159-169 in one pass)
+__global__ void __launch_bounds__(256)
+nb_directions_kernel(const int64_t N, const double beta, const double* __restrict__ u, const double* __restrict__ w,
+                     double* __restrict__ m, const double* __restrict__ nv, double* __restrict__ p,
+                     double* __restrict__ s, double* __restrict__ q, double* __restrict__ z) {
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x) {
+    const double un = u[n];
+    p[n] = un + beta * p[n];
+    s[n] = w[n] + beta * s[n];
+    q[n] = m[n] + beta * q[n];
+    z[n] = nv[n] + beta * z[n];
+  }
+}
+int nb_directions(int64_t N, double beta, const double* u, const double* w, double* m, const double* nv, double* p,
+                  double* sv, double* q, double* z, cudaStream_t s) {
+  if (N <= 0) return LPG_OK;
+  nb_directions_kernel<<<grid_for(N, 256, kStreamCap), 256, 0, s>>>(N, beta, u, w, m, nv, p, sv, q, z);
+  LPG_LAUNCH_CHECK("nb_directions_kernel");
+  return LPG_OK;
+}
+
 }  // namespace lpg

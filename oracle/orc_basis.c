@@ -82,7 +82,7 @@ static int set_key(orc_settings *s, const char *key, const char *val) {
   else if (IS("RHS FIELD")) s->rhs = V("GAUSSIAN SOURCES") ? ORC_RHS_GAUSSIAN_SOURCES : V("GAUSSIAN BUMPS") ? ORC_RHS_BUMPS : ORC_RHS_SINE;
   else if (IS("RHS SEED")) s->rhs_seed = strtoull(val, 0, 10);
   else if (IS("RHS SOURCES")) s->nsources = atoi(val);
-  else if (IS("LINEAR SOLVER")) s->solver = V("FPCG") ? ORC_FPCG : ORC_PCG;
+  else if (IS("LINEAR SOLVER")) s->solver = V("NBFPCG") ? ORC_NBFPCG : V("FPCG") ? ORC_FPCG : ORC_PCG;
   else if (IS("LINEAR SOLVER STOPPING CRITERION")) s->stop_rhs = V("ABS/REL-RHS-2NORM");
   else if (IS("PRECONDITIONER")) s->precon = V("JACOBI") ? ORC_PRE_JACOBI : V("MULTIGRID") ? ORC_PRE_MULTIGRID : V("PARALMOND") ? ORC_PRE_PARALMOND : ORC_PRE_NONE;
   else if (IS("MULTIGRID COARSENING")) s->mg_coarsening = V("ALLDEGREES") ? ORC_MG_ALLDEGREES : V("HALFDEGREES") ? ORC_MG_HALFDEGREES : ORC_MG_HALFDOFS;

@@ -19,7 +19,7 @@
 typedef long long hlong;
 
 /* ---------------- settings (subset of the reference's .rc keys) ---------------- */
-enum { ORC_PCG = 0, ORC_FPCG = 1 };
+enum { ORC_PCG = 0, ORC_FPCG = 1, ORC_NBFPCG = 2 };
 enum { ORC_PRE_NONE = 0, ORC_PRE_JACOBI = 1, ORC_PRE_MULTIGRID = 2, ORC_PRE_PARALMOND = 3 };
 enum { ORC_MG_HALFDOFS = 0, ORC_MG_HALFDEGREES = 1, ORC_MG_ALLDEGREES = 2, ORC_MG_LIST = 3 };
 enum { ORC_SMOOTH_CHEBYSHEV = 0, ORC_SMOOTH_JACOBI = 1 };

@@ -1127,8 +1127,65 @@ int orc_build_rhs(const orc_solver *S, double *r) {
   return 0;
 }
 
+/* NBFPCG, linearSolverNBFPCG.cpp:72-186 (Sanan's notation): one fused update of
+ * x, r, u = M r, w = A u-direction with four inner products per iteration, and the
+ * recurrences for p, s = A p, q = M s, z = A q; returns iterations */
+static int orc_nbfpcg(orc_solver *S, double *x, double *r, double tol, int maxit, double *res_out) {
+  const orc_elliptic *el = S->el;
+  const hlong N = el->ogs.Ngather;
+  double *u = dalloc(N), *p = dalloc(N), *w = dalloc(N), *n = dalloc(N), *m = dalloc(N);
+  double *s = dalloc(N), *z = dalloc(N), *q = dalloc(N), *Ax = dalloc(N);
+  orc_operator(el, x, Ax);
+  axpy(N, -1.0, Ax, 1.0, r);
+  precon_apply(S, r, u);
+  memcpy(p, u, sizeof(double) * (size_t)N);
+  orc_operator(el, p, w);
+  double gamma0 = dot(N, u, r), delta0 = dot(N, u, w), rdotr0 = dot(N, r, r);
+  precon_apply(S, w, m);
+  orc_operator(el, m, n);
+  memcpy(s, w, sizeof(double) * (size_t)N);
+  memcpy(q, m, sizeof(double) * (size_t)N);
+  memcpy(z, n, sizeof(double) * (size_t)N);
+  double eta0 = delta0, alpha0 = gamma0 / eta0, beta0 = 0.0;
+  const double TOL = fmax(tol * tol * rdotr0, tol * tol);
+  int iter;
+  for (iter = 0; iter < maxit; ++iter) {
+    if (rdotr0 <= TOL) break;
+    double ur = 0, us = 0, uw = 0, rr = 0;
+#pragma omp parallel for reduction(+ : ur, us, uw, rr)
+    for (hlong i = 0; i < N; ++i) {
+      x[i] += alpha0 * p[i];
+      r[i] -= alpha0 * s[i];
+      u[i] -= alpha0 * q[i];
+      w[i] -= alpha0 * z[i];
+      ur += u[i] * r[i];
+      us += u[i] * s[i];
+      uw += u[i] * w[i];
+      rr += r[i] * r[i];
+    }
+    for (hlong i = 0; i < N; ++i) n[i] = w[i] - r[i];
+    precon_apply(S, n, m);
+    axpy(N, 1.0, u, 1.0, m);
+    orc_operator(el, m, n);
+    gamma0 = ur;
+    beta0 = -us / eta0;
+    delta0 = uw;
+    rdotr0 = rr;
+    axpy(N, 1.0, u, beta0, p);
+    axpy(N, 1.0, w, beta0, s);
+    axpy(N, 1.0, m, beta0, q);
+    axpy(N, 1.0, n, beta0, z);
+    eta0 = delta0 - beta0 * beta0 * eta0;
+    alpha0 = gamma0 / eta0;
+  }
+  if (res_out) *res_out = sqrt(rdotr0);
+  free(u); free(p); free(w); free(n); free(m); free(s); free(z); free(q); free(Ax);
+  return iter;
+}
+
 /* (F)PCG, linearSolverPCG.cpp:67-171; returns iterations */
 int orc_pcg(orc_solver *S, double *x, double *r, double tol, int maxit, double *res_out) {
+  if (S->s.solver == ORC_NBFPCG) return orc_nbfpcg(S, x, r, tol, maxit, res_out);
   const orc_elliptic *el = S->el;
   const hlong N = el->ogs.Ngather;
   const int flexible = (S->s.solver == ORC_FPCG);

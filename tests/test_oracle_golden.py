@@ -73,3 +73,16 @@ def test_hessenberg_eigenvalues_match_numpy():
         ours = np.sort_complex(wr + 1j * wi)
         ref = np.sort_complex(np.linalg.eigvals(H))
         assert np.max(np.abs(ours - ref)) < 1e-10 * max(1, np.max(np.abs(ref)))
+
+
+def test_oracle_nbfpcg_matches_fpcg():
+    """The oracle's non-blocking FPCG restatement reaches the FPCG solution in the same
+    number of iterations (+-1) on a jittered Jacobi-preconditioned box."""
+    s = {"BOX NX": 3, "BOX NY": 3, "BOX NZ": 2, "BOX DIMX": 2, "BOX DIMY": 2, "BOX DIMZ": 2,
+         "BOX BOUNDARY FLAG": 1, "POLYNOMIAL DEGREE": 4, "LAMBDA": 0.5, "PRECONDITIONER": "JACOBI",
+         "MESH JITTER": 0.1}
+    a = Oracle(dict(s, **{"LINEAR SOLVER": "FPCG"})).run()
+    b = Oracle(dict(s, **{"LINEAR SOLVER": "NBFPCG"})).run()
+    assert abs(a["iterations"] - b["iterations"]) <= 1
+    assert abs(a["norm"] - b["norm"]) < 1e-9 * abs(a["norm"])
+    assert abs(a["error"] - b["error"]) < 1e-6 * a["error"]
