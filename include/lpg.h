@@ -205,9 +205,28 @@ int lpg_elliptic_initial_guess(lpg_elliptic *e, double *x, const double *rhs, vo
 int lpg_extrap_coeffs(int degree, int history, int cpqr, double *coeffs_out);
 /* elliptic_t::Run (ellipticRun.cpp:30-248): rhs, timed solve, scatter + AddBC, then the
  * mass-weighted solution norm and, for manufactured data, the error norm.
- * xL_host (Nlocal doubles) may be NULL; solve_seconds is the wall time of the solve. */
+ * xL_host (Nlocal doubles) may be NULL; solve_seconds is the wall time of the solve.
+ * With [OUTPUT TO FILE] = TRUE the solution is also written to
+ * <OUTPUT FILE NAME>_0000.vtu (ellipticRun.cpp:223-235). */
 int lpg_elliptic_run(lpg_elliptic *e, double *xL_host, int *iters, double *norm, double *err,
                      double *solve_seconds);
+/* elliptic_t::PlotFields (ellipticPlotFields.cpp:30-140): ASCII VTU UnstructuredGrid of the
+ * local field qL (Nlocal doubles, device) interpolated to the equispaced degree-(N+3) plot
+ * nodes of every element, each plot cube split into 6 tetrahedra (VTK type 10). */
+int lpg_elliptic_plot_fields(lpg_elliptic *e, const double *qL, const char *file_name);
+
+/* ------------------------------------------------------------------ Gmsh meshes */
+/* [MESH FILE] = <path> (instead of BOX) reads a Gmsh 2.2 ASCII hexahedral mesh
+ * (mesh_t::ReadGmshHex3D, meshReadGmshHex3D.cpp:33-170): type-5 hexahedra in file order,
+ * type-3 quadrilaterals as boundary faces whose physical tag is the boundary flag
+ * (1 Dirichlet, 2 Neumann). Both functions below are host only (no GPU needed).
+ * lpg_hex_mesh_info: element, node and tagged boundary-face counts. */
+int lpg_hex_mesh_info(const char *path, int64_t *nelements, int64_t *nnodes, int64_t *nboundary_faces);
+/* GlobalToLocal of the degree-N nodes of the mesh in `path` (mesh_t::ConnectNodes,
+ * meshConnectNodes.cpp:32-117, with the single-rank ogs ordering, ogsSetup.cpp:408-432):
+ * global_to_local gets nelements*(N+1)^3 entries (assembled dof, or -1 for Dirichlet
+ * nodes) unless NULL; nglobal gets the number of assembled dofs. */
+int lpg_hex_mesh_numbering(const char *path, int N, int32_t *global_to_local, int64_t *nglobal);
 
 /* ------------------------------------------------------------------ learned smoother */
 /* No reference counterpart. Element-local MLP

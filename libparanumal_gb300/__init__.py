@@ -90,6 +90,10 @@ def lib():
         "lpg_mlp_forward_bf16": [vp, i64, vp, vp, vp],
         "lpg_smoother_train": [ctypes.c_char_p, i32, i32, i32, i32, f32, ctypes.c_uint64, vp, vp],
         "lpg_elliptic_set_learned_smoother": [vp, vp, f64],
+        "lpg_elliptic_plot_fields": [vp, vp, ctypes.c_char_p],
+        "lpg_hex_mesh_info": [ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
+                              ctypes.POINTER(ctypes.c_int64)],
+        "lpg_hex_mesh_numbering": [ctypes.c_char_p, i32, vp, ctypes.POINTER(ctypes.c_int64)],
     })
     for name, args in sig.items():
         fn = getattr(L, name)
@@ -266,6 +270,26 @@ class Elliptic:
             check(st)
         return dict(iterations=it.value, norm=nrm.value, error=err.value, solve_seconds=sec.value,
                     xL=xL, converged=(st == LPG_OK))
+
+    def PlotFields(self, qL, file_name):
+        """VTU file of the local field qL (Nlocal doubles, device tensor or pointer)."""
+        check(lib().lpg_elliptic_plot_fields(self.h, _ptr(qL), str(file_name).encode()))
+
+
+def hex_mesh_info(path):
+    """(elements, nodes, tagged boundary faces) of a Gmsh hexahedral mesh (host only)."""
+    E, Nn, Nb = ctypes.c_int64(0), ctypes.c_int64(0), ctypes.c_int64(0)
+    check(lib().lpg_hex_mesh_info(str(path).encode(), ctypes.byref(E), ctypes.byref(Nn), ctypes.byref(Nb)))
+    return E.value, Nn.value, Nb.value
+
+
+def hex_mesh_numbering(path, N):
+    """(GlobalToLocal int32[E*(N+1)^3], Nglobal) of the degree-N nodes of a Gmsh mesh (host only)."""
+    E = hex_mesh_info(path)[0]
+    g2l = np.zeros(E * (N + 1) ** 3, dtype=np.int32)
+    ng = ctypes.c_int64(0)
+    check(lib().lpg_hex_mesh_numbering(str(path).encode(), N, g2l.ctypes.data_as(ctypes.c_void_p), ctypes.byref(ng)))
+    return g2l, ng.value
 
 
 def extrap_coeffs(degree, history, cpqr=False):

@@ -71,7 +71,6 @@ std::vector<int> parse_int_list(const std::string& v) {
 
 int build(lpg_elliptic* h) {
   Settings& S = h->settings;
-  if (S.get("MESH FILE", "BOX") != "BOX") return set_error(LPG_ERR_UNSUPPORTED, "only MESH FILE = BOX is supported");
   if (S.geti("ELEMENT TYPE", 12) != 12 || S.geti("MESH DIMENSION", 3) != 3)
     return set_error(LPG_ERR_UNSUPPORTED, "only hexahedra (ELEMENT TYPE 12, MESH DIMENSION 3) are supported");
   if (S.get("DISCRETIZATION", "CONTINUOUS") != "CONTINUOUS")
@@ -86,9 +85,20 @@ int build(lpg_elliptic* h) {
   c.bcflag = S.geti("BOX BOUNDARY FLAG", 1);
   c.jitter = S.getd("MESH JITTER", 0.0);
   c.jitterSeed = (uint64_t)std::strtoull(S.get("MESH JITTER SEED", "0").c_str(), nullptr, 10);
+  const std::string meshFile = S.get("MESH FILE", "BOX");
+  if (meshFile != "BOX") {
+    // hexahedral Gmsh mesh (mesh_t::ReadGmshHex3D); boundary tags 1 Dirichlet, 2 Neumann
+    auto f = std::make_shared<HexMeshData>();
+    int rcm = read_gmsh_hex(meshFile, *f);
+    if (rcm) return rcm;
+    if (S.get("RHS FIELD", "SINE") != "SINE")
+      return set_error(LPG_ERR_UNSUPPORTED, "a MESH FILE mesh supports RHS FIELD = SINE only");
+    if (c.jitter != 0.0) return set_error(LPG_ERR_UNSUPPORTED, "MESH JITTER applies to BOX meshes only");
+    c.file = f;
+  }
   const int N = S.geti("POLYNOMIAL DEGREE", 4);
   const double lambda = S.getd("LAMBDA", 1.0);
-  const int64_t E = (int64_t)c.nx * c.ny * c.nz;
+  const int64_t E = c.is_box() ? (int64_t)c.nx * c.ny * c.nz : c.file->E;
   std::vector<double> lamE;
   const bool lognormal = S.is("LAMBDA FIELD", "LOGNORMAL");
   if (lognormal) {
@@ -373,6 +383,7 @@ extern "C" int lpg_elliptic_random_vector(lpg_elliptic* e, uint64_t seed, double
   if (!e || !q) return set_error(LPG_ERR_INVALID, "null argument");
   LPG_GUARD_BEGIN
   const MeshConfig& c = e->mcfg;
+  if (!c.is_box()) return set_error(LPG_ERR_UNSUPPORTED, "random lattice vectors need MESH FILE = BOX");
   BoxNumbering b{c.nx, c.ny, c.nz, e->el->mesh.N, c.bcflag == -1 ? 1 : 0, c.bcflag == 1 ? 1 : 0};
   return lattice_random(b, e->el->Nglobal, e->el->owner.p, seed, q, pick(e, stream));
   LPG_GUARD_END
@@ -524,7 +535,49 @@ extern "C" int lpg_elliptic_run(lpg_elliptic* e, double* xL_host, int* iters, do
   if (err) *err = (el->rhsKind == 0) ? std::sqrt(nrm[1]) : -1.0;
   if (solve_seconds) *solve_seconds = std::chrono::duration<double>(t1 - t0).count();
   if (xL_host && (rc = e->xL.download(xL_host, el->Nlocal, s))) return rc;
+  if (e->settings.is("OUTPUT TO FILE", "TRUE")) {
+    const std::string name = e->settings.get("OUTPUT FILE NAME", "elliptic") + "_0000.vtu";
+    if ((rc = el->PlotFields(e->xL.p, name, s))) return rc;
+  }
   return solveStatus;
+  LPG_GUARD_END
+}
+
+extern "C" int lpg_elliptic_plot_fields(lpg_elliptic* e, const double* qL, const char* file_name) {
+  if (!e || !qL || !file_name) return set_error(LPG_ERR_INVALID, "null argument");
+  LPG_GUARD_BEGIN
+  return e->el->PlotFields(qL, file_name, e->plat.stream);
+  LPG_GUARD_END
+}
+
+// ================================================================ Gmsh meshes (host only)
+extern "C" int lpg_hex_mesh_info(const char* path, int64_t* nelements, int64_t* nnodes, int64_t* nboundary_faces) {
+  if (!path) return set_error(LPG_ERR_INVALID, "null argument");
+  LPG_GUARD_BEGIN
+  HexMeshData m;
+  const int rc = read_gmsh_hex(path, m);
+  if (rc) return rc;
+  if (nelements) *nelements = m.E;
+  if (nnodes) *nnodes = m.Nnodes;
+  if (nboundary_faces) *nboundary_faces = (int64_t)m.binfo.size() / 5;
+  return LPG_OK;
+  LPG_GUARD_END
+}
+
+extern "C" int lpg_hex_mesh_numbering(const char* path, int N, int32_t* global_to_local, int64_t* nglobal) {
+  if (!path) return set_error(LPG_ERR_INVALID, "null argument");
+  if (N < 1 || N > 8) return set_error(LPG_ERR_UNSUPPORTED, "POLYNOMIAL DEGREE must be 1..8");
+  LPG_GUARD_BEGIN
+  HexMeshData m;
+  int rc = read_gmsh_hex(path, m);
+  if (rc) return rc;
+  std::vector<double> r1d, w1d;
+  gll_nodes_weights(N, r1d, w1d);
+  HexNumbering num;
+  if ((rc = number_hex_nodes(m, N, r1d, num))) return rc;
+  if (global_to_local) std::memcpy(global_to_local, num.g2l.data(), sizeof(int32_t) * num.g2l.size());
+  if (nglobal) *nglobal = num.Nglobal;
+  return LPG_OK;
   LPG_GUARD_END
 }
 
@@ -596,6 +649,7 @@ extern "C" int lpg_smoother_train(const char* settings, int nsolves, int samples
   std::unique_ptr<lpg_elliptic> owner(e);
   if (e->precon->levels_p() < 1) return set_error(LPG_ERR_INVALID, "smoother train: PRECONDITIONER must be MULTIGRID");
   const MeshConfig& c = e->mcfg;
+  if (!c.is_box()) return set_error(LPG_ERR_UNSUPPORTED, "smoother training needs MESH FILE = BOX");
   BoxNumbering b{c.nx, c.ny, c.nz, e->el->mesh.N, c.bcflag == -1 ? 1 : 0, c.bcflag == 1 ? 1 : 0};
   TrainOptions o;
   o.nsolves = nsolves;
@@ -620,6 +674,7 @@ extern "C" int lpg_elliptic_set_learned_smoother(lpg_elliptic* e, const float* w
   if (!e) return set_error(LPG_ERR_INVALID, "null argument");
   LPG_GUARD_BEGIN
   const MeshConfig& c = e->mcfg;
+  if (!c.is_box() && weights_host) return set_error(LPG_ERR_UNSUPPORTED, "the learned smoother needs MESH FILE = BOX");
   BoxNumbering b{c.nx, c.ny, c.nz, e->el->mesh.N, c.bcflag == -1 ? 1 : 0, c.bcflag == 1 ? 1 : 0};
   if (!weights_host) {
     int rc = e->precon->set_learned(nullptr, b, threshold);

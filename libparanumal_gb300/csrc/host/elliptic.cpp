@@ -28,18 +28,26 @@ int Mesh::setup(const MeshConfig& c, int N_, cudaStream_t s) {
   Nq = N + 1;
   Np = Nq * Nq * Nq;
   if (N < 1 || N > 8) return set_error(LPG_ERR_UNSUPPORTED, "POLYNOMIAL DEGREE must be 1..8");
-  if (c.nx < 1 || c.ny < 1 || c.nz < 1) return set_error(LPG_ERR_INVALID, "BOX NX/NY/NZ must be >= 1");
-  E = (int64_t)c.nx * c.ny * c.nz;
+  if (c.is_box() && (c.nx < 1 || c.ny < 1 || c.nz < 1)) return set_error(LPG_ERR_INVALID, "BOX NX/NY/NZ must be >= 1");
+  E = c.is_box() ? (int64_t)c.nx * c.ny * c.nz : c.file->E;
   if (E * Np >= (int64_t)INT32_MAX) return set_error(LPG_ERR_UNSUPPORTED, "more than 2^31 local nodes");
   gll_nodes_weights(N, r1d, w1d);
   gll_derivative(N, r1d, D);
-
+  std::vector<double> ex(E * 8), ey(E * 8), ez(E * 8);
+  if (!c.is_box()) {
+    // vertex coordinates of the file's hexahedra (meshReadGmshHex3D.cpp:160-170)
+    const HexMeshData& f = *c.file;
+#pragma omp parallel for
+    for (int64_t i = 0; i < E * 8; ++i) {
+      const int64_t v = f.EToV[i];
+      ex[i] = f.VX[v]; ey[i] = f.VY[v]; ez[i] = f.VZ[v];
+    }
+  } else {
   // vertex coordinates per element (meshSetupBoxHex3D.cpp:112-152) + interior jitter
   const bool periodic = (c.bcflag == -1);
   const double dx = c.dimx / c.nx, dy = c.dimy / c.ny, dz = c.dimz / c.nz;
   const double X0 = -c.dimx / 2.0, Y0 = -c.dimy / 2.0, Z0 = -c.dimz / 2.0;
   const int64_t NnX = periodic ? c.nx : c.nx + 1, NnY = periodic ? c.ny : c.ny + 1;
-  std::vector<double> ex(E * 8), ey(E * 8), ez(E * 8);
   static const int ox[8] = {0, 1, 1, 0, 0, 1, 1, 0}, oy[8] = {0, 0, 1, 1, 0, 0, 1, 1}, oz[8] = {0, 0, 0, 0, 1, 1, 1, 1};
 #pragma omp parallel for
   for (int64_t e = 0; e < E; ++e) {
@@ -59,6 +67,7 @@ int Mesh::setup(const MeshConfig& c, int N_, cudaStream_t s) {
       ey[e * 8 + v] = y;
       ez[e * 8 + v] = z;
     }
+  }
   }
   int rc;
   if ((rc = EX.alloc(E * 8)) || (rc = EY.alloc(E * 8)) || (rc = EZ.alloc(E * 8))) return rc;
@@ -112,6 +121,7 @@ int Elliptic::setup(Platform* p, const MeshConfig& c, int N, double lam, const s
                     cudaStream_t s) {
   plat = p;
   lambda = lam;
+  if (!c.is_box()) return setup_file(c, N, lamE, s);
   if (c.bcflag != 1 && c.bcflag != -1)
     return set_error(LPG_ERR_UNSUPPORTED, "BOX BOUNDARY FLAG must be 1 (Dirichlet) or -1 (periodic)");
   if (c.bcflag == -1 && (c.nx < 2 || c.ny < 2 || c.nz < 2))
@@ -150,8 +160,36 @@ int Elliptic::setup(Platform* p, const MeshConfig& c, int N, double lam, const s
   if ((rc = box_numbering(b, base_d.p, g2l.p, owner.p, mult.p, Nglobal, s))) return rc;
   if ((rc = multiplicity_to_weight(Nglobal, mult.p, weightG.p, s))) return rc;
 
+  hasDirichlet = dirichlet;
+  return finish_setup(lamE, s);
+}
+
+// numbering of a file mesh on the host (union-find over connected face nodes), uploaded
+int Elliptic::setup_file(const MeshConfig& c, int N, const std::vector<double>* lamE, cudaStream_t s) {
+  int rc = mesh.setup(c, N, s);
+  if (rc) return rc;
+  Nlocal = mesh.E * mesh.Np;
+  HexNumbering num;
+  if ((rc = number_hex_nodes(*c.file, N, mesh.r1d, num))) return rc;
+  Nglobal = num.Nglobal;
+  if (Nglobal <= 0) return set_error(LPG_ERR_INVALID, "no unknowns after masking");
+  DevBuf<int32_t> mult;
+  if ((rc = g2l.alloc(Nlocal)) || (rc = owner.alloc(Nglobal)) || (rc = mult.alloc(Nglobal)) ||
+      (rc = weightG.alloc(Nglobal)))
+    return rc;
+  if ((rc = g2l.upload(num.g2l.data(), Nlocal, s)) || (rc = owner.upload(num.owner.data(), Nglobal, s)) ||
+      (rc = mult.upload(num.mult.data(), Nglobal, s)))
+    return rc;
+  if ((rc = multiplicity_to_weight(Nglobal, mult.p, weightG.p, s))) return rc;
+  hasDirichlet = num.hasDirichlet;
+  return finish_setup(lamE, s);
+}
+
+int Elliptic::finish_setup(const std::vector<double>* lamE, cudaStream_t s) {
+  int rc;
+  const int64_t E = mesh.E;
   hasLambdaE = (lamE != nullptr);
-  allNeumann = (lam == 0.0 && !hasLambdaE && !dirichlet);
+  allNeumann = (lambda == 0.0 && !hasLambdaE && !hasDirichlet);
   allNeumannScale = 1.0 / std::sqrt((double)Nglobal);
   if (hasLambdaE) {
     lambdaE_h = *lamE;
@@ -384,7 +422,7 @@ int Elliptic::BuildRhs(double* r, cudaStream_t s) {
   if ((rc = rhs_local(mesh.N, mesh.E, mesh.EX.p, mesh.EY.p, mesh.EZ.p, mesh.r1d_d.p, mesh.geo.p,
                       hasLambdaE ? lambdaE.p : nullptr, lambda, g2l.p, spec, rL.p, gL.p, s)))
     return rc;
-  if (rhsKind == 0 && mesh.cfg.bcflag == 1) {
+  if (rhsKind == 0 && hasDirichlet) {
     // Dirichlet lifting rhs -= A_e g (ellipticRhsBCHex3D.okl:60-290)
     AxArgs<double, double> a;
     const int64_t Np = mesh.Np;

@@ -15,6 +15,7 @@
 
 #include "../lpg_internal.hpp"
 #include "../lpg_errors.hpp"
+#include "hexmesh.hpp"
 
 namespace lpg {
 
@@ -90,6 +91,9 @@ struct MeshConfig {
   int bcflag = 1;
   double jitter = 0.0;
   uint64_t jitterSeed = 0;
+  // MESH FILE: a hexahedral mesh read from a Gmsh file (the box fields are then unused)
+  std::shared_ptr<const HexMeshData> file;
+  bool is_box() const { return !file; }
 };
 
 struct Mesh {
@@ -139,6 +143,7 @@ struct Elliptic {
   DevBuf<float> lambdaE32;
   int64_t Nglobal = 0, Nlocal = 0;
   bool allNeumann = false;
+  bool hasDirichlet = false;       // some nodes are masked (Dirichlet data lifted into the rhs)
   double allNeumannScale = 1;
   DevBuf<int32_t> g2l, owner;
   DevBuf<double> weightG;
@@ -149,6 +154,10 @@ struct Elliptic {
 
   int setup(Platform* p, const MeshConfig& c, int N, double lambda, const std::vector<double>* lamE,
             cudaStream_t s);
+  int setup_file(const MeshConfig& c, int N, const std::vector<double>* lamE, cudaStream_t s);
+  // VTU file of the local field qL (E*Np, device)
+  int PlotFields(const double* qL, const std::string& fileName, cudaStream_t s);
+  int finish_setup(const std::vector<double>* lamE, cudaStream_t s);
   int make_f32(bool bf16, cudaStream_t s);
   // OPERATOR PRECISION: FP64 (default) or DF64 (double-FP32 words on the FP32 pipe,
   // FP64-accurate) for every FP64 operator application of this object

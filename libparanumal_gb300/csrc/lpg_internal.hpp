@@ -158,6 +158,12 @@ int nb_update(int64_t N, double a, const double* p, const double* sv, const doub
 int nb_directions(int64_t N, double beta, const double* u, const double* w, double* m, const double* nv, double* p,
                   double* sv, double* q, double* z, cudaStream_t s);
 
+// ---------------------------------------------------------------- plot output
+// out[e][4][(N+4)^3] = x, y, z (trilinear image of the vertices) and qL interpolated by I
+// ((N+4) x (N+1), row-major) at the equispaced plot points pr (N+4 values), for E elements
+int plot_interp(int N, int64_t E, const double* I, const double* pr, const double* qL, const double* EX,
+                const double* EY, const double* EZ, double* out, cudaStream_t s);
+
 // ---------------------------------------------------------------- sparse / dense
 // y = alpha A x + beta y (CSR, FP64)
 int csr_spmv(int64_t Nrows, const int64_t* rowStarts, const int32_t* cols, const double* vals,

@@ -96,7 +96,11 @@ static int set_key(orc_settings *s, const char *key, const char *val) {
   else if (IS("SOLVER TOLERANCE")) s->tol = atof(val);
   else if (IS("MAXIMUM ITERATIONS")) s->maxit = atoi(val);
   /* keys accepted and ignored (fixed by this path or not relevant on the CPU) */
-  else if (IS("FORMAT") || IS("DATA FILE") || IS("MESH FILE") || IS("MESH DIMENSION") ||
+  else if (IS("MESH FILE")) {
+    if (strcmp(val, "BOX") == 0) s->mesh_file[0] = 0;
+    else snprintf(s->mesh_file, sizeof(s->mesh_file), "%s", val);
+  }
+  else if (IS("FORMAT") || IS("DATA FILE") || IS("MESH DIMENSION") ||
            IS("ELEMENT TYPE") || IS("THREAD MODEL") || IS("PLATFORM NUMBER") ||
            IS("DEVICE NUMBER") || IS("DISCRETIZATION") || IS("PARALMOND CYCLE") ||
            IS("OUTPUT TO FILE") || IS("VERBOSE") || IS("ELEMENT MAP") ||
@@ -146,7 +150,7 @@ int orc_parse_settings(const char *text, orc_settings *s) {
       char *e = strchr(tmp, ']');
       if (!e) { rc = -1; break; }
       *e = 0;
-      snprintf(key, sizeof(key), "%s", tmp + 1);
+      snprintf(key, sizeof(key), "%.255s", tmp + 1);
       trim(key);
       havekey = 1;
     } else if (havekey) {

@@ -52,6 +52,7 @@ typedef struct {
   int amg_cheb_degree;
   double tol;
   int maxit;
+  char mesh_file[1024]; /* MESH FILE: empty for BOX, else a Gmsh 2.2 ASCII hexahedral mesh */
 } orc_settings;
 
 int orc_parse_settings(const char *text, orc_settings *s);
@@ -104,6 +105,23 @@ typedef struct {
 
 orc_mesh *orc_mesh_build(const orc_settings *s, int N);
 void orc_mesh_free(orc_mesh *m);
+
+/* ---------------- Gmsh hexahedral meshes (orc_gmsh.c) ---------------- */
+typedef struct {
+  hlong Nnodes, Nelements, NboundaryFaces;
+  double *VX, *VY, *VZ;
+  long long *nodeTag;
+  hlong *EToV;       /* Nelements*8, 0-based node indices */
+  hlong *binfo;      /* NboundaryFaces*5: physical tag, 4 node indices */
+} orc_gmsh;
+int orc_read_gmsh_hex(const char *path, orc_gmsh *g);  /* 0 ok */
+void orc_gmsh_free(orc_gmsh *g);
+/* EToE/EToF by sorted face vertices, EToB (0 interior, tag or -1 on the boundary) */
+void orc_gmsh_connect(const orc_gmsh *g, hlong *EToE, int *EToF, int *EToB);
+/* R[((fM*6 + fP)*4 + rot)*Nfp + nM] = nP, or NULL if a node has no match */
+int *orc_face_node_matching(const orc_mesh *m);
+/* number of elements of the configured mesh (box or file), -1 on a file error */
+hlong orc_mesh_count(const orc_settings *s);
 
 /* ---------------- gather-scatter (libs/ogs, Signed + unique, single rank) ---------------- */
 typedef struct {

@@ -9,6 +9,7 @@
  *   libs/mesh/meshConnectNodes.cpp:32-117       global ids by min propagation, mapB
  *   libs/mesh/meshPhysicalNodesHex3D.cpp:31-112 trilinear vertex map
  *   libs/mesh/meshGeometricFactorsHex3D.cpp:31-193 ggeo (G00..G22) and wJ
+ * Meshes read from Gmsh files take their connectivity from orc_gmsh.c.
  *   solvers/elliptic/src/ellipticBoundarySetup.cpp:30-140 Dirichlet mask, weights
  *   libs/ogs/ogsSetup.cpp:44-470,867-886         ordering of gathered dofs and GlobalToLocal
  * Addition with no reference counterpart: interior-vertex jitter keyed by
@@ -21,10 +22,78 @@
 #include <stdlib.h>
 #include <string.h>
 
-static const int faceVertsHex[6][4] = {{0, 1, 2, 3}, {0, 1, 5, 4}, {1, 2, 6, 5},
-                                       {2, 3, 7, 6}, {0, 3, 7, 4}, {4, 5, 6, 7}};
+/* vertices of each face, every face listed the same way round (meshSetElementType.cpp:80-81) */
+static const int faceVertsHex[6][4] = {{0, 1, 2, 3}, {0, 4, 5, 1}, {1, 5, 6, 2},
+                                       {2, 6, 7, 3}, {0, 3, 7, 4}, {4, 7, 6, 5}};
+
+hlong orc_mesh_count(const orc_settings *s) {
+  if (!s->mesh_file[0]) return (hlong)s->nx * s->ny * s->nz;
+  orc_gmsh g;
+  const int rc = orc_read_gmsh_hex(s->mesh_file, &g);
+  const hlong E = rc ? -1 : g.Nelements;
+  orc_gmsh_free(&g);
+  return E;
+}
+
+static void reference_element(orc_mesh *m);
+static void connect_nodes(orc_mesh *m, const hlong *vmapM, const hlong *vmapP);
+static void physical_and_geometry(orc_mesh *m);
+
+/* mesh read from a Gmsh file: connectivity by face matching, node pairs on connected
+ * faces by the rotation-indexed permutation R */
+static orc_mesh *orc_mesh_build_file(const orc_settings *s, int N) {
+  orc_gmsh g;
+  if (orc_read_gmsh_hex(s->mesh_file, &g)) { orc_gmsh_free(&g); return NULL; }
+  orc_mesh *m = (orc_mesh *)calloc(1, sizeof(orc_mesh));
+  m->N = N; m->Nq = N + 1; m->Np = m->Nq * m->Nq * m->Nq; m->Nfp = m->Nq * m->Nq;
+  const hlong E = g.Nelements;
+  const int Np = m->Np, Nfp = m->Nfp;
+  m->Nelements = E;
+  m->EToV = (hlong *)malloc(sizeof(hlong) * E * 8);
+  m->EX = (double *)malloc(sizeof(double) * E * 8);
+  m->EY = (double *)malloc(sizeof(double) * E * 8);
+  m->EZ = (double *)malloc(sizeof(double) * E * 8);
+  for (hlong i = 0; i < E * 8; ++i) {
+    const hlong v = g.EToV[i];
+    m->EToV[i] = v; m->EX[i] = g.VX[v]; m->EY[i] = g.VY[v]; m->EZ[i] = g.VZ[v];
+  }
+  m->EToE = (hlong *)malloc(sizeof(hlong) * E * 6);
+  m->EToF = (int *)malloc(sizeof(int) * E * 6);
+  m->EToB = (int *)malloc(sizeof(int) * E * 6);
+  orc_gmsh_connect(&g, m->EToE, m->EToF, m->EToB);
+  orc_gmsh_free(&g);
+  reference_element(m);
+  int *R = orc_face_node_matching(m);
+  if (!R) { orc_mesh_free(m); return NULL; }
+  hlong *vmapM = (hlong *)malloc(sizeof(hlong) * E * 6 * Nfp);
+  hlong *vmapP = (hlong *)malloc(sizeof(hlong) * E * 6 * Nfp);
+  for (hlong e = 0; e < E; ++e)
+    for (int f = 0; f < 6; ++f) {
+      const hlong eP = m->EToE[e * 6 + f];
+      const int fP = m->EToF[e * 6 + f];
+      int rot = 0;
+      if (eP >= 0) {
+        const hlong v0P = m->EToV[eP * 8 + faceVertsHex[fP][0]];
+        for (; rot < 4; ++rot)
+          if (m->EToV[e * 8 + faceVertsHex[f][rot]] == v0P) break;
+      }
+      for (int n = 0; n < Nfp; ++n) {
+        const hlong id = e * 6 * Nfp + f * Nfp + n;
+        vmapM[id] = m->faceNodes[f * Nfp + n] + e * Np;
+        vmapP[id] = (eP < 0 || rot == 4) ? vmapM[id]
+                    : m->faceNodes[fP * Nfp + R[((f * 6 + fP) * 4 + rot) * Nfp + n]] + eP * Np;
+      }
+    }
+  free(R);
+  connect_nodes(m, vmapM, vmapP);
+  free(vmapM);
+  free(vmapP);
+  physical_and_geometry(m);
+  return m;
+}
 
 orc_mesh *orc_mesh_build(const orc_settings *s, int N) {
+  if (s->mesh_file[0]) return orc_mesh_build_file(s, N);
   orc_mesh *m = (orc_mesh *)calloc(1, sizeof(orc_mesh));
   m->N = N;
   m->Nq = N + 1;
@@ -32,7 +101,7 @@ orc_mesh *orc_mesh_build(const orc_settings *s, int N) {
   m->Nfp = m->Nq * m->Nq;
   m->nx = s->nx; m->ny = s->ny; m->nz = s->nz;
   const int nx = s->nx, ny = s->ny, nz = s->nz;
-  const int Nq = m->Nq, Np = m->Np, Nfp = m->Nfp;
+  const int Np = m->Np, Nfp = m->Nfp;
   const hlong E = (hlong)nx * ny * nz;
   m->Nelements = E;
   const int periodic = (s->bcflag == -1);
@@ -104,9 +173,30 @@ orc_mesh *orc_mesh_build(const orc_settings *s, int N) {
           }
         }
       }
-  (void)faceVertsHex;
+  reference_element(m);
 
-  /* ---- reference element */
+  /* ---- vmapM / vmapP (aligned faces: face-local node n matches face-local node n) */
+  hlong *vmapM = (hlong *)malloc(sizeof(hlong) * E * 6 * Nfp);
+  hlong *vmapP = (hlong *)malloc(sizeof(hlong) * E * 6 * Nfp);
+  for (hlong e = 0; e < E; ++e)
+    for (int f = 0; f < 6; ++f) {
+      const hlong eP = m->EToE[e * 6 + f];
+      const int fP = m->EToF[e * 6 + f];
+      for (int n = 0; n < Nfp; ++n) {
+        const hlong id = e * 6 * Nfp + f * Nfp + n;
+        vmapM[id] = m->faceNodes[f * Nfp + n] + e * Np;
+        vmapP[id] = (eP < 0) ? vmapM[id] : m->faceNodes[fP * Nfp + n] + eP * Np;
+      }
+    }
+  connect_nodes(m, vmapM, vmapP);
+  free(vmapM);
+  free(vmapP);
+  physical_and_geometry(m);
+  return m;
+}
+
+static void reference_element(orc_mesh *m) {
+  const int N = m->N, Nq = m->Nq, Np = m->Np, Nfp = m->Nfp;
   m->gllz = (double *)malloc(sizeof(double) * Nq);
   m->gllw = (double *)malloc(sizeof(double) * Nq);
   m->D = (double *)malloc(sizeof(double) * Nq * Nq);
@@ -135,21 +225,12 @@ orc_mesh *orc_mesh_build(const orc_settings *s, int N) {
     }
   }
 
-  /* ---- vmapM / vmapP (aligned faces: face-local node n matches face-local node n) */
-  hlong *vmapM = (hlong *)malloc(sizeof(hlong) * E * 6 * Nfp);
-  hlong *vmapP = (hlong *)malloc(sizeof(hlong) * E * 6 * Nfp);
-  for (hlong e = 0; e < E; ++e)
-    for (int f = 0; f < 6; ++f) {
-      const hlong eP = m->EToE[e * 6 + f];
-      const int fP = m->EToF[e * 6 + f];
-      for (int n = 0; n < Nfp; ++n) {
-        const hlong id = e * 6 * Nfp + f * Nfp + n;
-        vmapM[id] = m->faceNodes[f * Nfp + n] + e * Np;
-        vmapP[id] = (eP < 0) ? vmapM[id] : m->faceNodes[fP * Nfp + n] + eP * Np;
-      }
-    }
+}
 
-  /* ---- ConnectNodes: min propagation of 1-based local ids, boundary flags */
+/* ConnectNodes: min propagation of 1-based local ids, boundary flags */
+static void connect_nodes(orc_mesh *m, const hlong *vmapM, const hlong *vmapP) {
+  const hlong E = m->Nelements;
+  const int Np = m->Np, Nfp = m->Nfp;
   m->globalIds = (hlong *)malloc(sizeof(hlong) * E * Np);
   m->mapB = (int *)malloc(sizeof(int) * E * Np);
   for (hlong n = 0; n < E * Np; ++n) { m->globalIds[n] = 1 + n; m->mapB[n] = -1; }
@@ -176,9 +257,11 @@ orc_mesh *orc_mesh_build(const orc_settings *s, int N) {
       }
     if (!change) break;
   }
-  free(vmapM);
-  free(vmapP);
+}
 
+static void physical_and_geometry(orc_mesh *m) {
+  const hlong E = m->Nelements;
+  const int Nq = m->Nq, Np = m->Np;
   /* ---- physical nodes */
   m->x = (double *)malloc(sizeof(double) * E * Np);
   m->y = (double *)malloc(sizeof(double) * E * Np);
@@ -234,7 +317,6 @@ orc_mesh *orc_mesh_build(const orc_settings *s, int N) {
         }
   }
   if (bad) fprintf(stderr, "oracle: %d nodes with J < 1e-12\n", bad);
-  return m;
 }
 
 void orc_mesh_free(orc_mesh *m) {
@@ -248,8 +330,9 @@ void orc_mesh_free(orc_mesh *m) {
 /* ---------------------------------------------------------------- elliptic level */
 
 orc_elliptic *orc_elliptic_build(const orc_settings *s, int N, const double *lambdaE) {
-  orc_elliptic *el = (orc_elliptic *)calloc(1, sizeof(orc_elliptic));
   orc_mesh *m = orc_mesh_build(s, N);
+  if (!m) return NULL;
+  orc_elliptic *el = (orc_elliptic *)calloc(1, sizeof(orc_elliptic));
   el->mesh = m;
   el->lambda = s->lambda;
   const hlong E = m->Nelements;

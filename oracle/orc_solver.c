@@ -974,7 +974,12 @@ orc_solver *orc_create(const char *settings_text, int *status) {
   int rc = orc_parse_settings(settings_text, &S->s);
   if (status) *status = rc;
   if (rc != 0) { free(S); return NULL; }
-  const hlong E = (hlong)S->s.nx * S->s.ny * S->s.nz;
+  const hlong E = orc_mesh_count(&S->s);
+  if (E < 0 || (S->s.mesh_file[0] && S->s.rhs != ORC_RHS_SINE)) {
+    if (status) *status = -2;
+    free(S);
+    return NULL;
+  }
   if (S->s.lambda_field == 1) {
     /* lognormal(0,1) per element keyed by element id (no reference counterpart) */
     S->lambdaE = dalloc(E);
@@ -986,6 +991,12 @@ orc_solver *orc_create(const char *settings_text, int *status) {
     }
   }
   S->el = orc_elliptic_build(&S->s, S->s.N, S->lambdaE);
+  if (!S->el) {
+    if (status) *status = -3;
+    free(S->lambdaE);
+    free(S);
+    return NULL;
+  }
   if (S->s.precon == ORC_PRE_JACOBI) {
     const hlong N = S->el->ogs.Ngather;
     double *d = dalloc(N);

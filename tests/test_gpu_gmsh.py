@@ -1,0 +1,117 @@
+"""Meshes read from Gmsh files through the CUDA solver path, and VTU output.
+
+Parity: the same file solved by the library and by the oracle (identical iteration
+counts for FP64 paths, solution within 1e-7, norms within 1e-9); the file version of a
+box equals the library's own box solve; the VTU file's points and field equal the
+oracle's plot interpolation (ASCII %g, so 1e-5 relative)."""
+import re
+import xml.etree.ElementTree as ET
+
+import numpy as np
+import pytest
+import torch
+
+import libparanumal_gb300 as lpg
+from gmsh_mesh import write_box
+from gpu_helpers import rel_err
+from oracle.oracle import Oracle
+from oracle.plot import plot_cells, plot_interp
+
+pytestmark = pytest.mark.gpu
+
+BASE = {"BOX NX": 4, "BOX NY": 3, "BOX NZ": 3, "BOX DIMX": 2, "BOX DIMY": 2, "BOX DIMZ": 2,
+        "BOX BOUNDARY FLAG": 1, "POLYNOMIAL DEGREE": 5, "LAMBDA": 0.5, "PRECONDITIONER": "JACOBI",
+        "LINEAR SOLVER": "PCG"}
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    import __graft_entry__ as g
+    g.build()
+    torch.cuda.set_device(0)
+
+
+def mesh(tmp_path, **kw):
+    return write_box(str(tmp_path / "m.msh"), 4, 3, 3, **kw)
+
+
+CASES = {
+    "jacobi_rotated": (dict(shuffle_seed=1, rotate_seed=2, jitter=0.15, jitter_seed=3), {}),
+    "multigrid_rotated": (dict(rotate_seed=4, jitter=0.1, jitter_seed=5),
+                          {"POLYNOMIAL DEGREE": 7, "PRECONDITIONER": "MULTIGRID", "MULTIGRID DEGREES": "7,3,1",
+                           "PARALMOND AGGREGATION": "SMOOTHED", "LINEAR SOLVER": "FPCG", "LAMBDA": 0.0}),
+    "mixed_dirichlet_neumann": (dict(rotate_seed=6, tags=(1, 2, 2, 1, 2, 1)), {"LAMBDA": 1.0}),
+    "all_neumann": (dict(rotate_seed=8, tags=(2, 2, 2, 2, 2, 2)),
+                    {"LAMBDA": 0.0, "PRECONDITIONER": "MULTIGRID", "MULTIGRID DEGREES": "5,2,1",
+                     "LINEAR SOLVER": "FPCG"}),
+}
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_file_mesh_solve_matches_oracle(tmp_path, name):
+    kw, over = CASES[name]
+    s = dict(BASE, **over, **{"MESH FILE": mesh(tmp_path, **kw)})
+    r = lpg.Elliptic(s).Run(want_solution=True)
+    ro = Oracle(s).run()
+    assert r["converged"]
+    assert r["iterations"] == ro["iterations"], (r["iterations"], ro["iterations"])
+    assert abs(r["norm"] - ro["norm"]) < 1e-9 * abs(ro["norm"])
+    assert rel_err(r["xL"], ro["xL"]) < 1e-7
+
+
+def test_file_mesh_equals_box_on_gpu(tmp_path):
+    s = dict(BASE, **{"PRECONDITIONER": "MULTIGRID", "LINEAR SOLVER": "FPCG"})
+    rb = lpg.Elliptic(s).Run()
+    rf = lpg.Elliptic(dict(s, **{"MESH FILE": mesh(tmp_path, shuffle_seed=3, rotate_seed=9)})).Run()
+    assert rf["iterations"] == rb["iterations"]
+    assert abs(rf["norm"] - rb["norm"]) < 1e-11
+    # both solves stop at a 1e-8 relative residual: their solutions differ at that level,
+    # far below the discretisation error
+    assert abs(rf["error"] - rb["error"]) < 1e-4 * rb["error"]
+
+
+def _floats(node):
+    return np.array([float(t) for t in node.text.split()])
+
+
+def test_vtu_output_matches_oracle_plot_interpolation(tmp_path):
+    s = dict(BASE, **{"MESH FILE": mesh(tmp_path, rotate_seed=12, jitter=0.1, jitter_seed=1),
+                      "POLYNOMIAL DEGREE": 3, "OUTPUT TO FILE": "TRUE",
+                      "OUTPUT FILE NAME": str(tmp_path / "sol")})
+    e = lpg.Elliptic(s)
+    r = e.Run(want_solution=True)
+    o = Oracle(s)
+    E, N = o.info("nelements"), 3
+    root = ET.parse(str(tmp_path / "sol_0000.vtu")).getroot()
+    piece = root.find("UnstructuredGrid/Piece")
+    pNp = (N + 4) ** 3
+    assert int(piece.get("NumberOfPoints")) == E * pNp
+    assert int(piece.get("NumberOfCells")) == E * plot_cells(N)
+    pts = _floats(piece.find("Points/DataArray")).reshape(-1, 3)
+    fld = _floats(piece.find("PointData/DataArray"))
+    ref_xyz = np.stack([plot_interp(o.array(c), E, N).ravel() for c in ("x", "y", "z")], axis=1)
+    ref_q = plot_interp(r["xL"], E, N).ravel()
+    assert np.abs(pts - ref_xyz).max() < 1e-5 * np.abs(ref_xyz).max()
+    assert np.abs(fld - ref_q).max() < 1e-5 * np.abs(ref_q).max()
+    cells = piece.find("Cells")
+    arrays = {a.get("Name"): a for a in cells.findall("DataArray")}
+    conn = _floats(arrays["connectivity"]).astype(np.int64).reshape(-1, 4)
+    assert conn.min() == 0 and conn.max() == E * pNp - 1
+    v = pts[conn]
+    vol = np.einsum("ij,ij->i", v[:, 1] - v[:, 0], np.cross(v[:, 2] - v[:, 0], v[:, 3] - v[:, 0]))
+    assert (vol > 0).all()
+    assert np.array_equal(_floats(arrays["offsets"]).astype(np.int64), 4 * np.arange(1, len(conn) + 1))
+    assert (_floats(arrays["types"]) == 10).all()
+    # explicit entry on a device field
+    xL = torch.tensor(r["xL"], device="cuda")
+    e.PlotFields(xL, str(tmp_path / "again.vtu"))
+    assert re.sub(r"\s+", " ", open(tmp_path / "again.vtu").read()) == \
+        re.sub(r"\s+", " ", open(tmp_path / "sol_0000.vtu").read())
+
+
+def test_unsupported_file_mesh_features_fail_loudly(tmp_path):
+    f = mesh(tmp_path)
+    with pytest.raises(RuntimeError):
+        lpg.Elliptic(dict(BASE, **{"MESH FILE": f, "RHS FIELD": "GAUSSIAN SOURCES"}))
+    with pytest.raises(RuntimeError):
+        lpg.Elliptic(dict(BASE, **{"MESH FILE": str(tmp_path / "none.msh")}))
