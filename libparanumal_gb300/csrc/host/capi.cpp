@@ -152,9 +152,10 @@ int build(lpg_elliptic* h) {
   const std::string pre = S.get("PRECONDITIONER", "NONE");
   if (pre == "NONE") h->precon = make_identity(el);
   else if (pre == "JACOBI") h->precon = make_jacobi(el, &rc);
-  else if (pre == "MULTIGRID" || pre == "PARALMOND") {
+  else if (pre == "MULTIGRID" || pre == "PARALMOND" || pre == "SEMFEM") {
     MGOptions o;
-    o.amgOnly = (pre == "PARALMOND");
+    o.amgOnly = (pre == "PARALMOND" || pre == "SEMFEM");
+    o.semfem = (pre == "SEMFEM");
     o.degrees = degree_schedule(N, S.get("MULTIGRID COARSENING", "HALFDOFS"), parse_int_list(S.get("MULTIGRID DEGREES", "")));
     o.smoother = S.is("MULTIGRID SMOOTHER", "DAMPEDJACOBI") ? 1 : 0;
     o.chebDegree = S.geti("MULTIGRID CHEBYSHEV DEGREE", 2);

@@ -15,6 +15,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <unistd.h>
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -69,6 +70,12 @@ int Mesh::setup(const MeshConfig& c, int N_, cudaStream_t s) {
     }
   }
   }
+  return setup_vertices(ex, ey, ez, s);
+}
+
+// device vertex arrays, reference-element data and geometric factors of E elements
+int Mesh::setup_vertices(const std::vector<double>& ex, const std::vector<double>& ey, const std::vector<double>& ez,
+                         cudaStream_t s) {
   int rc;
   if ((rc = EX.alloc(E * 8)) || (rc = EY.alloc(E * 8)) || (rc = EZ.alloc(E * 8))) return rc;
   if ((rc = EX.upload(ex.data(), E * 8, s)) || (rc = EY.upload(ey.data(), E * 8, s)) ||
@@ -183,6 +190,70 @@ int Elliptic::setup_file(const MeshConfig& c, int N, const std::vector<double>* 
   if ((rc = multiplicity_to_weight(Nglobal, mult.p, weightG.p, s))) return rc;
   hasDirichlet = num.hasDirichlet;
   return finish_setup(lamE, s);
+}
+
+// SEMFEM low-order problem (mesh_t::SetupSEMFEM meshSetupSEMFEM.cpp:98-214 and
+// SEMFEMPrecon ellipticPreconSEMFEM.cpp:56-200, hexahedra): each degree-N element of `sem`
+// is cut into N^3 trilinear hexahedra with vertices at its GLL nodes; the degree-1 nodes
+// keep the assembled dof of the GLL node they sit on, so the FEM matrix acts on sem's
+// vectors. Only what BuildMatrix needs is set up (geometry, GlobalToLocal, lambda).
+int Elliptic::setup_semfem(const Elliptic& sem, cudaStream_t s) {
+  plat = sem.plat;
+  lambda = sem.lambda;
+  const int Ns = sem.mesh.N, Nq = Ns + 1, NpS = sem.mesh.Np;
+  const int64_t Esem = sem.mesh.E, Es = Esem * Ns * Ns * Ns;
+  mesh.cfg = sem.mesh.cfg;
+  mesh.N = 1; mesh.Nq = 2; mesh.Np = 8; mesh.E = Es;
+  if (Es * 8 >= (int64_t)INT32_MAX) return set_error(LPG_ERR_UNSUPPORTED, "SEMFEM: more than 2^31 local nodes");
+  gll_nodes_weights(1, mesh.r1d, mesh.w1d);
+  gll_derivative(1, mesh.r1d, mesh.D);
+  std::vector<double> vx(Esem * 8), vy(Esem * 8), vz(Esem * 8);
+  std::vector<int32_t> semMap(Esem * NpS);
+  int rc;
+  if ((rc = sem.mesh.EX.download(vx.data(), Esem * 8, s)) || (rc = sem.mesh.EY.download(vy.data(), Esem * 8, s)) ||
+      (rc = sem.mesh.EZ.download(vz.data(), Esem * 8, s)) || (rc = sem.g2l.download(semMap.data(), Esem * NpS, s)))
+    return rc;
+  static const int cx[8] = {0, 1, 1, 0, 0, 1, 1, 0}, cy[8] = {0, 0, 1, 1, 0, 0, 1, 1}, cz[8] = {0, 0, 0, 0, 1, 1, 1, 1};
+  const std::vector<double>& r = sem.mesh.r1d;
+  std::vector<double> ex(Es * 8), ey(Es * 8), ez(Es * 8);
+  std::vector<int32_t> map(Es * 8);
+  if (sem.hasLambdaE) lambdaE_h.resize(Es);
+#pragma omp parallel for
+  for (int64_t e = 0; e < Esem; ++e) {
+    const double* X = &vx[e * 8];
+    const double* Y = &vy[e * 8];
+    const double* Z = &vz[e * 8];
+    for (int k = 0; k < Ns; ++k)
+      for (int j = 0; j < Ns; ++j)
+        for (int i = 0; i < Ns; ++i) {
+          const int64_t es = ((e * Ns + k) * Ns + j) * Ns + i;
+          for (int v = 0; v < 8; ++v) {
+            const int a = i + cx[v], b = j + cy[v], c = k + cz[v];
+            // GLL node (a,b,c): trilinear image of the element's vertices (meshPhysicalNodesHex3D.cpp)
+            const double rr = r[a], ss = r[b], tt = r[c];
+            const double w[8] = {(1 - rr) * (1 - ss) * (1 - tt), (1 + rr) * (1 - ss) * (1 - tt),
+                                 (1 + rr) * (1 + ss) * (1 - tt), (1 - rr) * (1 + ss) * (1 - tt),
+                                 (1 - rr) * (1 - ss) * (1 + tt), (1 + rr) * (1 - ss) * (1 + tt),
+                                 (1 + rr) * (1 + ss) * (1 + tt), (1 - rr) * (1 + ss) * (1 + tt)};
+            double x = 0, y = 0, z = 0;
+            for (int q = 0; q < 8; ++q) { x += 0.125 * w[q] * X[q]; y += 0.125 * w[q] * Y[q]; z += 0.125 * w[q] * Z[q]; }
+            ex[es * 8 + v] = x; ey[es * 8 + v] = y; ez[es * 8 + v] = z;
+            // degree-1 node cx + 2 cy + 4 cz (tensor order) <- GLL node (a,b,c)
+            map[es * 8 + cx[v] + 2 * cy[v] + 4 * cz[v]] = semMap[e * NpS + a + b * Nq + c * Nq * Nq];
+          }
+          if (sem.hasLambdaE) lambdaE_h[es] = sem.lambdaE_h[e];
+        }
+  }
+  if ((rc = mesh.setup_vertices(ex, ey, ez, s))) return rc;
+  Nlocal = Es * 8;
+  Nglobal = sem.Nglobal;
+  if ((rc = g2l.alloc(Nlocal)) || (rc = g2l.upload(map.data(), Nlocal, s))) return rc;
+  hasLambdaE = sem.hasLambdaE;
+  hasDirichlet = sem.hasDirichlet;
+  allNeumann = sem.allNeumann;
+  allNeumannScale = sem.allNeumannScale;
+  LPG_CUDA_TRY(cudaStreamSynchronize(s));
+  return LPG_OK;
 }
 
 int Elliptic::finish_setup(const std::vector<double>* lamE, cudaStream_t s) {
@@ -437,83 +508,125 @@ int Elliptic::BuildRhs(double* r, cudaStream_t s) {
   return LPG_OK;
 }
 
-// Assembled stiffness (+ lambda mass) of this degree on the host, sorted (row, col)
-// with duplicates summed; element entries below 1e-7 are dropped as in the reference.
-int Elliptic::BuildMatrix(std::vector<int64_t>& rows, std::vector<int32_t>& cols, std::vector<double>& vals,
+// Assembled stiffness (+ lambda mass) of this degree on the host as CSR with columns
+// sorted and duplicates summed in element order; element entries below 1e-7 are dropped
+// as in the reference (ellipticBuildOperatorMatrixContinuous.cpp:697-880). Two passes: the
+// element loop writes every (row, col, val) straight into its row, at a slot fixed by the
+// order of the row's local copies (element order), then each row is stably sorted by
+// column and merged; this sums duplicates in the same order as one global stable sort.
+int Elliptic::BuildMatrix(std::vector<int64_t>& rowStarts, std::vector<int32_t>& cols, std::vector<double>& vals,
                           cudaStream_t s) {
   const int Nq = mesh.Nq, Np = mesh.Np;
-  const int64_t E = mesh.E;
+  const int64_t E = mesh.E, Ng = Nglobal;
   std::vector<double> geo(E * 7 * Np);
   std::vector<int32_t> map(Nlocal);
   int rc;
   if ((rc = mesh.geo.download(geo.data(), E * 7 * Np, s)) || (rc = g2l.download(map.data(), Nlocal, s))) return rc;
   const double* Dm = mesh.D.data();
-  struct NZ { int64_t row; int32_t col; double val; };
-  std::vector<std::vector<NZ>> parts;
-  int nthreads = 1;
-#ifdef _OPENMP
-  nthreads = omp_get_max_threads();
-#endif
-  parts.resize(nthreads);
-#pragma omp parallel
+  // unmasked nodes per element; slot of each local copy inside its row
+  std::vector<int32_t> live(E);
+#pragma omp parallel for
+  for (int64_t e = 0; e < E; ++e) {
+    int c = 0;
+    for (int n = 0; n < Np; ++n) c += (map[e * Np + n] >= 0);
+    live[e] = c;
+  }
+  std::vector<int64_t> rowCount(Ng + 1, 0), slot(Nlocal, 0);
+  for (int64_t L = 0; L < Nlocal; ++L) {
+    const int32_t g = map[L];
+    if (g < 0) continue;
+    slot[L] = rowCount[g + 1];
+    rowCount[g + 1] += live[L / Np];
+  }
+  for (int64_t g = 0; g < Ng; ++g) rowCount[g + 1] += rowCount[g];
+  const int64_t total = rowCount[Ng];
   {
-    int tid = 0;
-#ifdef _OPENMP
-    tid = omp_get_thread_num();
-#endif
-    std::vector<NZ>& out = parts[tid];
-#pragma omp for schedule(static)
-    for (int64_t e = 0; e < E; ++e) {
-      const double* gg = geo.data() + e * 7 * Np;
-      const double lam = hasLambdaE ? lambdaE_h[e] : lambda;
-      for (int nz = 0; nz < Nq; nz++) for (int ny = 0; ny < Nq; ny++) for (int nx = 0; nx < Nq; nx++) {
-        const int idn = nx + ny * Nq + nz * Nq * Nq;
-        const int32_t gn = map[e * Np + idn];
-        if (gn < 0) continue;
-        for (int mz = 0; mz < Nq; mz++) for (int my = 0; my < Nq; my++) for (int mx = 0; mx < Nq; mx++) {
-          const int idm = mx + my * Nq + mz * Nq * Nq;
-          const int32_t gm = map[e * Np + idm];
-          if (gm < 0) continue;
-          double val = 0;
-          int id;
-          if (ny == my && nz == mz)
-            for (int k = 0; k < Nq; k++) { id = k + ny * Nq + nz * Nq * Nq; val += gg[0 * Np + id] * Dm[nx + k * Nq] * Dm[mx + k * Nq]; }
-          if (nz == mz) {
-            id = mx + ny * Nq + nz * Nq * Nq; val += gg[1 * Np + id] * Dm[nx + mx * Nq] * Dm[my + ny * Nq];
-            id = nx + my * Nq + nz * Nq * Nq; val += gg[1 * Np + id] * Dm[mx + nx * Nq] * Dm[ny + my * Nq];
-          }
-          if (ny == my) {
-            id = mx + ny * Nq + nz * Nq * Nq; val += gg[2 * Np + id] * Dm[nx + mx * Nq] * Dm[mz + nz * Nq];
-            id = nx + ny * Nq + mz * Nq * Nq; val += gg[2 * Np + id] * Dm[mx + nx * Nq] * Dm[nz + mz * Nq];
-          }
-          if (nx == mx && nz == mz)
-            for (int k = 0; k < Nq; k++) { id = nx + k * Nq + nz * Nq * Nq; val += gg[3 * Np + id] * Dm[ny + k * Nq] * Dm[my + k * Nq]; }
-          if (nx == mx) {
-            id = nx + my * Nq + nz * Nq * Nq; val += gg[4 * Np + id] * Dm[ny + my * Nq] * Dm[mz + nz * Nq];
-            id = nx + ny * Nq + mz * Nq * Nq; val += gg[4 * Np + id] * Dm[my + ny * Nq] * Dm[nz + mz * Nq];
-          }
-          if (nx == mx && ny == my)
-            for (int k = 0; k < Nq; k++) { id = nx + ny * Nq + k * Nq * Nq; val += gg[5 * Np + id] * Dm[nz + k * Nq] * Dm[mz + k * Nq]; }
-          if (nx == mx && ny == my && nz == mz) val += gg[6 * Np + idn] * lam;
-          if (std::fabs(val) >= 1e-7) out.push_back(NZ{gn, gm, val});
+    // the element entries (12 bytes each) and the coarsening that follows must fit in host
+    // memory: refuse beyond a quarter of it rather than exhaust it
+    const long pages = sysconf(_SC_PHYS_PAGES), pageSize = sysconf(_SC_PAGE_SIZE);
+    const double hostBytes = (pages > 0 && pageSize > 0) ? (double)pages * (double)pageSize : 64e9;
+    if ((double)total * 12.0 > 0.25 * hostBytes)
+      return set_error(LPG_ERR_UNSUPPORTED, "assembled matrix too large for host AMG setup (" + std::to_string(total) +
+                                                " element entries); use MULTIGRID with a degree-1 coarse level");
+  }
+  std::vector<int32_t> ecol(total);
+  std::vector<double> eval(total);
+#pragma omp parallel for schedule(static)
+  for (int64_t e = 0; e < E; ++e) {
+    const double* gg = geo.data() + e * 7 * Np;
+    const double lam = hasLambdaE ? lambdaE_h[e] : lambda;
+    for (int nz = 0; nz < Nq; nz++) for (int ny = 0; ny < Nq; ny++) for (int nx = 0; nx < Nq; nx++) {
+      const int idn = nx + ny * Nq + nz * Nq * Nq;
+      const int32_t gn = map[e * Np + idn];
+      if (gn < 0) continue;
+      int64_t pos = rowCount[gn] + slot[e * Np + idn];
+      for (int mz = 0; mz < Nq; mz++) for (int my = 0; my < Nq; my++) for (int mx = 0; mx < Nq; mx++) {
+        const int idm = mx + my * Nq + mz * Nq * Nq;
+        const int32_t gm = map[e * Np + idm];
+        if (gm < 0) continue;
+        double val = 0;
+        int id;
+        if (ny == my && nz == mz)
+          for (int k = 0; k < Nq; k++) { id = k + ny * Nq + nz * Nq * Nq; val += gg[0 * Np + id] * Dm[nx + k * Nq] * Dm[mx + k * Nq]; }
+        if (nz == mz) {
+          id = mx + ny * Nq + nz * Nq * Nq; val += gg[1 * Np + id] * Dm[nx + mx * Nq] * Dm[my + ny * Nq];
+          id = nx + my * Nq + nz * Nq * Nq; val += gg[1 * Np + id] * Dm[mx + nx * Nq] * Dm[ny + my * Nq];
         }
+        if (ny == my) {
+          id = mx + ny * Nq + nz * Nq * Nq; val += gg[2 * Np + id] * Dm[nx + mx * Nq] * Dm[mz + nz * Nq];
+          id = nx + ny * Nq + mz * Nq * Nq; val += gg[2 * Np + id] * Dm[mx + nx * Nq] * Dm[nz + mz * Nq];
+        }
+        if (nx == mx && nz == mz)
+          for (int k = 0; k < Nq; k++) { id = nx + k * Nq + nz * Nq * Nq; val += gg[3 * Np + id] * Dm[ny + k * Nq] * Dm[my + k * Nq]; }
+        if (nx == mx) {
+          id = nx + my * Nq + nz * Nq * Nq; val += gg[4 * Np + id] * Dm[ny + my * Nq] * Dm[mz + nz * Nq];
+          id = nx + ny * Nq + mz * Nq * Nq; val += gg[4 * Np + id] * Dm[my + ny * Nq] * Dm[nz + mz * Nq];
+        }
+        if (nx == mx && ny == my)
+          for (int k = 0; k < Nq; k++) { id = nx + ny * Nq + k * Nq * Nq; val += gg[5 * Np + id] * Dm[nz + k * Nq] * Dm[mz + k * Nq]; }
+        if (nx == mx && ny == my && nz == mz) val += gg[6 * Np + idn] * lam;
+        ecol[pos] = (std::fabs(val) >= 1e-7) ? gm : -1;   // dropped entries keep their slot
+        eval[pos] = val;
+        ++pos;
       }
     }
   }
-  size_t total = 0;
-  for (auto& p : parts) total += p.size();
-  std::vector<NZ> all;
-  all.reserve(total);
-  for (auto& p : parts) { all.insert(all.end(), p.begin(), p.end()); std::vector<NZ>().swap(p); }
-  std::stable_sort(all.begin(), all.end(), [](const NZ& a, const NZ& b) {
-    return a.row < b.row || (a.row == b.row && a.col < b.col);
-  });
-  rows.clear(); cols.clear(); vals.clear();
-  rows.reserve(all.size() / 4); cols.reserve(all.size() / 4); vals.reserve(all.size() / 4);
-  for (size_t i = 0; i < all.size(); ++i) {
-    if (!rows.empty() && rows.back() == all[i].row && cols.back() == all[i].col) vals.back() += all[i].val;
-    else { rows.push_back(all[i].row); cols.push_back(all[i].col); vals.push_back(all[i].val); }
+  std::vector<double>().swap(geo);
+  // per row: stable sort by column, merge duplicates, drop marked entries
+  std::vector<int64_t> kept(Ng + 1, 0);
+#pragma omp parallel
+  {
+    std::vector<int32_t> idx;
+    std::vector<std::pair<int32_t, double>> row;
+#pragma omp for schedule(dynamic, 1024)
+    for (int64_t g = 0; g < Ng; ++g) {
+      const int64_t b = rowCount[g], n = rowCount[g + 1] - b;
+      idx.resize(n);
+      for (int64_t k = 0; k < n; ++k) idx[k] = (int32_t)k;
+      std::stable_sort(idx.begin(), idx.end(), [&](int32_t x, int32_t y) { return ecol[b + x] < ecol[b + y]; });
+      // compact in place through a small copy
+      row.clear();
+      for (int64_t k = 0; k < n; ++k) {
+        const int32_t c = ecol[b + idx[k]];
+        if (c < 0) continue;
+        const double v = eval[b + idx[k]];
+        if (!row.empty() && row.back().first == c) row.back().second += v;
+        else row.emplace_back(c, v);
+      }
+      for (size_t k = 0; k < row.size(); ++k) { ecol[b + k] = row[k].first; eval[b + k] = row[k].second; }
+      kept[g + 1] = (int64_t)row.size();
+    }
   }
+  for (int64_t g = 0; g < Ng; ++g) kept[g + 1] += kept[g];
+  cols.resize(kept[Ng]);
+  vals.resize(kept[Ng]);
+#pragma omp parallel for schedule(dynamic, 1024)
+  for (int64_t g = 0; g < Ng; ++g) {
+    const int64_t n = kept[g + 1] - kept[g];
+    std::copy(ecol.begin() + rowCount[g], ecol.begin() + rowCount[g] + n, cols.begin() + kept[g]);
+    std::copy(eval.begin() + rowCount[g], eval.begin() + rowCount[g] + n, vals.begin() + kept[g]);
+  }
+  rowStarts.swap(kept);
   return LPG_OK;
 }
 

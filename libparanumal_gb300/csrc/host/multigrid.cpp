@@ -14,6 +14,8 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <type_traits>
 #ifdef _OPENMP
@@ -23,12 +25,6 @@
 namespace lpg {
 
 // ================================================================ host sparse matrices
-struct NZ {
-  int64_t r;
-  int32_t c;
-  double v;
-};
-
 struct HCSR {
   int64_t n = 0, m = 0;
   std::vector<int64_t> rs;
@@ -36,28 +32,6 @@ struct HCSR {
   std::vector<double> vals;
   int64_t nnz() const { return (int64_t)cols.size(); }
 };
-
-static HCSR csr_from_coo(int64_t n, int64_t m, std::vector<NZ>& e) {
-  std::stable_sort(e.begin(), e.end(), [](const NZ& a, const NZ& b) { return a.r < b.r || (a.r == b.r && a.c < b.c); });
-  HCSR A;
-  A.n = n;
-  A.m = m;
-  A.rs.assign(n + 1, 0);
-  A.cols.reserve(e.size());
-  A.vals.reserve(e.size());
-  int64_t lastR = -1;
-  int32_t lastC = -1;
-  for (const NZ& z : e) {
-    if (z.r == lastR && z.c == lastC) { A.vals.back() += z.v; continue; }
-    A.cols.push_back(z.c);
-    A.vals.push_back(z.v);
-    A.rs[z.r + 1]++;
-    lastR = z.r;
-    lastC = z.c;
-  }
-  for (int64_t i = 0; i < n; ++i) A.rs[i + 1] += A.rs[i];
-  return A;
-}
 
 static void spmv_host(const HCSR& A, const double* x, double* y) {
 #pragma omp parallel for schedule(static)
@@ -346,18 +320,51 @@ static int amg_coarsen(ALevel& L, ALevel& Lc, std::vector<double>& nullv, double
   nullv.assign(cn.begin(), cn.end());
   if (!unsmoothed) {
     // P = (I - omega D^{-1} A) T, omega = 4/3/rho (parAlmondSmoothPrologator.cpp:33-301)
+    // Row i: the entry of T followed by the row's A entries mapped to aggregates, stably
+    // sorted by column and merged; rows are independent, so they are built in parallel
+    // (same sums, in the same order, as one stable sort of all entries).
     const double omega = (4. / 3.) / L.rho;
-    std::vector<NZ> pe;
-    pe.reserve(L.A.nnz() + N);
-    for (int64_t i = 0; i < N; ++i) {
-      pe.push_back(NZ{i, T.cols[i], T.vals[i]});
-      const double invDi = 1.0 / L.diagA[i];
-      for (int64_t j = L.A.rs[i]; j < L.A.rs[i + 1]; ++j) {
-        const int32_t col = L.A.cols[j];
-        pe.push_back(NZ{i, T.cols[col], -omega * invDi * L.A.vals[j] * T.vals[col]});
+    HCSR P;
+    P.n = N; P.m = Nc;
+    P.rs.assign(N + 1, 0);
+    std::vector<int64_t> start(N + 1, 0);
+    for (int64_t i = 0; i < N; ++i) start[i + 1] = start[i] + 1 + (L.A.rs[i + 1] - L.A.rs[i]);
+    std::vector<int32_t> pc(start[N]);
+    std::vector<double> pv(start[N]);
+#pragma omp parallel
+    {
+      std::vector<std::pair<int32_t, double>> row;
+#pragma omp for schedule(dynamic, 4096)
+      for (int64_t i = 0; i < N; ++i) {
+        row.clear();
+        row.emplace_back((int32_t)T.cols[i], T.vals[i]);
+        const double invDi = 1.0 / L.diagA[i];
+        for (int64_t j = L.A.rs[i]; j < L.A.rs[i + 1]; ++j) {
+          const int32_t col = L.A.cols[j];
+          row.emplace_back((int32_t)T.cols[col], -omega * invDi * L.A.vals[j] * T.vals[col]);
+        }
+        std::stable_sort(row.begin(), row.end(),
+                         [](const std::pair<int32_t, double>& x, const std::pair<int32_t, double>& y) {
+                           return x.first < y.first;
+                         });
+        int64_t k = start[i];
+        for (size_t q = 0; q < row.size(); ++q) {
+          if (k > start[i] && pc[k - 1] == row[q].first) { pv[k - 1] += row[q].second; continue; }
+          pc[k] = row[q].first; pv[k] = row[q].second; ++k;
+        }
+        P.rs[i + 1] = k - start[i];
       }
     }
-    L.P = csr_from_coo(N, Nc, pe);
+    for (int64_t i = 0; i < N; ++i) P.rs[i + 1] += P.rs[i];
+    P.cols.resize(P.rs[N]);
+    P.vals.resize(P.rs[N]);
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < N; ++i) {
+      const int64_t n = P.rs[i + 1] - P.rs[i];
+      std::copy(pc.begin() + start[i], pc.begin() + start[i] + n, P.cols.begin() + P.rs[i]);
+      std::copy(pv.begin() + start[i], pv.begin() + start[i] + n, P.vals.begin() + P.rs[i]);
+    }
+    L.P = std::move(P);
   } else {
     L.P = T;
   }
@@ -736,22 +743,24 @@ int MultiGrid::apply(const double* r, double* z, cudaStream_t s) {
 }
 
 // ---------------------------------------------------------------- setup
+// LPG_SETUP_TIMES=1 prints the host setup phases of the AMG hierarchy to stderr
+static void setup_time(const char* what, double& t0, int64_t a = -1, int64_t b = -1) {
+  static const bool on = std::getenv("LPG_SETUP_TIMES") != nullptr;
+  const double t = omp_get_wtime();
+  if (on) std::fprintf(stderr, "[lpg setup] %-22s %8.3f s  %lld %lld\n", what, t - t0, (long long)a, (long long)b);
+  t0 = t;
+}
+
 int MultiGrid::setup_amg(Elliptic* el, Rand48& rng) {
   cudaStream_t s = plat->stream;
-  std::vector<int64_t> rows;
-  std::vector<int32_t> cols;
-  std::vector<double> vals;
-  int rc = el->BuildMatrix(rows, cols, vals, s);
-  if (rc) return rc;
+  double t0 = omp_get_wtime();
   auto L0 = std::make_unique<ALevel>();
+  int rc = el->BuildMatrix(L0->A.rs, L0->A.cols, L0->A.vals, s);
+  if (rc) return rc;
   L0->A.n = L0->A.m = el->Nglobal;
-  L0->A.rs.assign(el->Nglobal + 1, 0);
-  for (int64_t r0 : rows) L0->A.rs[r0 + 1]++;
-  for (int64_t i = 0; i < el->Nglobal; ++i) L0->A.rs[i + 1] += L0->A.rs[i];
-  L0->A.cols.swap(cols);
-  L0->A.vals.swap(vals);
-  std::vector<int64_t>().swap(rows);
+  setup_time("matrix", t0, L0->A.n, L0->A.nnz());
   diag_setup(*L0, rng);
+  setup_time("level 0 smoother", t0);
   a.push_back(std::move(L0));
   const int64_t Nrows = a[0]->A.n;
   std::vector<double> nullv(Nrows, 1.0 / std::sqrt((double)Nrows));
@@ -765,6 +774,7 @@ int MultiGrid::setup_amg(Elliptic* el, Rand48& rng) {
       else { L.lambda1 = L.rho; L.lambda0 = L.rho / 10.; }
       auto Lc = std::make_unique<ALevel>();
       if ((rc = amg_coarsen(L, *Lc, nullv, theta, opt.amgRugeStuben, opt.amgUnsmoothed, rng))) return rc;
+      setup_time("coarsen", t0, Lc->A.n, Lc->A.nnz());
       a.push_back(std::move(Lc));
       if (!opt.amgRugeStuben) theta /= 2;
       const int64_t coarseSize = a.back()->A.n;
@@ -782,6 +792,7 @@ int MultiGrid::setup_amg(Elliptic* el, Rand48& rng) {
     for (int64_t i = 0; i < coarseN; ++i)
       for (int64_t j = 0; j < coarseN; ++j) dense[i * coarseN + j] += nullv[i] * nullv[j];
   if ((rc = dense_inverse(coarseN, dense))) return rc;
+  setup_time("coarse inverse", t0, coarseN);
   if ((rc = coarseInv.alloc(coarseN * coarseN)) || (rc = coarseInv.upload(dense.data(), coarseN * coarseN, s))) return rc;
   // device copies and work vectors
   for (size_t k = 0; k < a.size(); ++k) {
@@ -807,6 +818,15 @@ int MultiGrid::setup(Elliptic* el, const MeshConfig& c, const MGOptions& o) {
   rng.seed(0);  // srand48(rank) in buildParAlmondKernels (parAlmondKernels.cpp:55-58)
   int rc;
   if (o.amgOnly) {
+    if (o.semfem) {
+      // SEMFEMPrecon (ellipticPreconSEMFEM.cpp:56-247, hexahedra): parAlmond on the
+      // low-order matrix, applied to the degree-N vectors directly
+      auto fem = std::make_unique<Elliptic>();
+      if ((rc = fem->setup_semfem(*el, s))) return rc;
+      rc = setup_amg(fem.get(), rng);
+      fem.reset();   // the AMG levels own their matrices; the sub-mesh is no longer needed
+      return rc;
+    }
     if ((rc = setup_amg(el, rng))) return rc;
     return LPG_OK;
   }

@@ -108,6 +108,9 @@ struct Mesh {
   DevBuf<__nv_bfloat16> geo16;    // BF16 copy
   DevBuf<float2> geoDW;           // double-word (hi, lo) copy for the double-word operator
   int setup(const MeshConfig& c, int N, cudaStream_t s);
+  // E, N, r1d, w1d, D set: upload vertices, reference data, geometric factors
+  int setup_vertices(const std::vector<double>& ex, const std::vector<double>& ey, const std::vector<double>& ez,
+                     cudaStream_t s);
   int make_f32(cudaStream_t s);
   int make_bf16(cudaStream_t s);
   int make_dw(cudaStream_t s);
@@ -158,6 +161,8 @@ struct Elliptic {
   // VTU file of the local field qL (E*Np, device)
   int PlotFields(const double* qL, const std::string& fileName, cudaStream_t s);
   int finish_setup(const std::vector<double>* lamE, cudaStream_t s);
+  // low-order problem on the GLL sub-mesh of `sem` sharing its numbering (SEMFEM)
+  int setup_semfem(const Elliptic& sem, cudaStream_t s);
   int make_f32(bool bf16, cudaStream_t s);
   // OPERATOR PRECISION: FP64 (default) or DF64 (double-FP32 words on the FP32 pipe,
   // FP64-accurate) for every FP64 operator application of this object
@@ -173,7 +178,8 @@ struct Elliptic {
   int BuildDiagonal(double* diagG, cudaStream_t s);   // assembled diag(A)
   int BuildRhs(double* r, cudaStream_t s);            // forcing + lifting, gathered
   // host copy of the assembled N-degree stiffness (+lambda mass), COO sorted (row, col)
-  int BuildMatrix(std::vector<int64_t>& rows, std::vector<int32_t>& cols, std::vector<double>& vals,
+  // assembled operator matrix (CSR: Nglobal+1 row starts, sorted columns)
+  int BuildMatrix(std::vector<int64_t>& rowStarts, std::vector<int32_t>& cols, std::vector<double>& vals,
                   cudaStream_t s);
 };
 
@@ -209,6 +215,7 @@ struct MGOptions {
   bool amgUnsmoothed = false;
   bool amgRugeStuben = false;
   bool amgOnly = false;           // PARALMOND: AMG on the fine matrix
+  bool semfem = false;            // SEMFEM: AMG on the low-order matrix of the GLL sub-mesh
   int learnedSteps = 2;           // learned smoothing steps before and after the coarse correction
 };
 std::unique_ptr<Precon> make_multigrid(Elliptic* el, const MeshConfig& c, const MGOptions& o, int* status);

@@ -20,7 +20,7 @@ typedef long long hlong;
 
 /* ---------------- settings (subset of the reference's .rc keys) ---------------- */
 enum { ORC_PCG = 0, ORC_FPCG = 1, ORC_NBFPCG = 2 };
-enum { ORC_PRE_NONE = 0, ORC_PRE_JACOBI = 1, ORC_PRE_MULTIGRID = 2, ORC_PRE_PARALMOND = 3 };
+enum { ORC_PRE_NONE = 0, ORC_PRE_JACOBI = 1, ORC_PRE_MULTIGRID = 2, ORC_PRE_PARALMOND = 3, ORC_PRE_SEMFEM = 4 };
 enum { ORC_MG_HALFDOFS = 0, ORC_MG_HALFDEGREES = 1, ORC_MG_ALLDEGREES = 2, ORC_MG_LIST = 3 };
 enum { ORC_SMOOTH_CHEBYSHEV = 0, ORC_SMOOTH_JACOBI = 1 };
 enum { ORC_RHS_SINE = 0, ORC_RHS_GAUSSIAN_SOURCES = 1, ORC_RHS_BUMPS = 2 };
@@ -147,6 +147,9 @@ typedef struct {
 
 orc_elliptic *orc_elliptic_build(const orc_settings *s, int N, const double *lambdaE);
 void orc_elliptic_free(orc_elliptic *e);
+/* low-order (degree 1) elliptic on the GLL sub-mesh of a degree-N one, sharing its
+ * assembled numbering (mesh_t::SetupSEMFEM for hexahedra, meshSetupSEMFEM.cpp:30-214) */
+orc_elliptic *orc_semfem_build(const orc_elliptic *sem);
 
 /* element operators */
 void orc_partial_ax(const orc_elliptic *e, const double *q, double *AqL);

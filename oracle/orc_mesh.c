@@ -391,6 +391,48 @@ orc_elliptic *orc_elliptic_build(const orc_settings *s, int N, const double *lam
   return el;
 }
 
+/* SEMFEM sub-mesh (meshSetupSEMFEM.cpp:98-214, ellipticPreconSEMFEM.cpp:56-200 for
+ * hexahedra): every degree-N element is cut into N^3 trilinear hexahedra whose vertices
+ * are its GLL nodes; their degree-1 nodes keep the assembled dof of the GLL node they sit
+ * on (masked nodes stay masked), so the low-order matrix acts on the same vectors. */
+orc_elliptic *orc_semfem_build(const orc_elliptic *sem) {
+  const orc_mesh *M = sem->mesh;
+  const int N = M->N, Nq = M->Nq, Np = M->Np;
+  const hlong Es = M->Nelements * N * N * N;
+  orc_mesh *m = (orc_mesh *)calloc(1, sizeof(orc_mesh));
+  m->N = 1; m->Nq = 2; m->Np = 8; m->Nfp = 4;
+  m->Nelements = Es;
+  m->EX = (double *)malloc(sizeof(double) * Es * 8);
+  m->EY = (double *)malloc(sizeof(double) * Es * 8);
+  m->EZ = (double *)malloc(sizeof(double) * Es * 8);
+  orc_elliptic *el = (orc_elliptic *)calloc(1, sizeof(orc_elliptic));
+  el->mesh = m;
+  el->lambda = sem->lambda;
+  el->ogs.GlobalToLocal = (int *)malloc(sizeof(int) * Es * 8);
+  if (sem->lambdaE) el->lambdaE = (double *)malloc(sizeof(double) * Es);
+  static const int cx[8] = {0, 1, 1, 0, 0, 1, 1, 0}, cy[8] = {0, 0, 1, 1, 0, 0, 1, 1}, cz[8] = {0, 0, 0, 0, 1, 1, 1, 1};
+  for (hlong e = 0; e < M->Nelements; ++e)
+    for (int k = 0; k < N; ++k)
+      for (int j = 0; j < N; ++j)
+        for (int i = 0; i < N; ++i) {
+          const hlong es = ((e * N + k) * N + j) * N + i;
+          for (int v = 0; v < 8; ++v) {
+            /* vertex v in hexahedron order; degree-1 node a + 2b + 4c in tensor order */
+            const hlong id = e * Np + (i + cx[v]) + (j + cy[v]) * Nq + (k + cz[v]) * Nq * Nq;
+            m->EX[es * 8 + v] = M->x[id]; m->EY[es * 8 + v] = M->y[id]; m->EZ[es * 8 + v] = M->z[id];
+            el->ogs.GlobalToLocal[es * 8 + cx[v] + 2 * cy[v] + 4 * cz[v]] = sem->ogs.GlobalToLocal[id];
+          }
+          if (el->lambdaE) el->lambdaE[es] = sem->lambdaE[e];
+        }
+  reference_element(m);
+  physical_and_geometry(m);
+  el->ogs.Nlocal = Es * 8;
+  el->ogs.Ngather = sem->ogs.Ngather;
+  el->allNeumann = sem->allNeumann;
+  el->allNeumannScale = sem->allNeumannScale;
+  return el;
+}
+
 void orc_elliptic_free(orc_elliptic *e) {
   if (!e) return;
   orc_mesh_free(e->mesh);

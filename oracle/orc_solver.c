@@ -932,6 +932,16 @@ static orc_multigrid *build_multigrid(orc_solver *S) {
     mg_alloc_work(mg);
     return mg;
   }
+  if (S->s.precon == ORC_PRE_SEMFEM) {
+    /* SEMFEMPrecon (ellipticPreconSEMFEM.cpp:30-247, hexahedra): parAlmond AMG of the
+     * low-order matrix on the GLL sub-mesh, applied to the degree-N vectors directly */
+    mg->nP = 0;
+    orc_elliptic *fem = orc_semfem_build(S->el);
+    mg->owned[mg->nowned++] = fem;
+    amg_setup(mg, fem, &S->s, &S->rng);
+    mg_alloc_work(mg);
+    return mg;
+  }
   int deg[32];
   const int nd = degree_schedule(&S->s, S->s.N, deg);
   orc_elliptic *cur = S->el;
@@ -962,7 +972,7 @@ static orc_multigrid *build_multigrid(orc_solver *S) {
 static void precon_apply(orc_solver *S, const double *r, double *z) {
   const hlong N = S->el->ogs.Ngather;
   if (S->s.precon == ORC_PRE_JACOBI) amxpy(N, 1.0, S->invDiag, r, 0.0, z);
-  else if (S->s.precon == ORC_PRE_MULTIGRID || S->s.precon == ORC_PRE_PARALMOND) {
+  else if (S->s.precon == ORC_PRE_MULTIGRID || S->s.precon == ORC_PRE_PARALMOND || S->s.precon == ORC_PRE_SEMFEM) {
     /* level 0 rhs/x are the caller's buffers */
     vcycle(S->mg, 0, (double *)r, z);
   } else memcpy(z, r, sizeof(double) * N);
@@ -1004,7 +1014,7 @@ orc_solver *orc_create(const char *settings_text, int *status) {
     S->invDiag = dalloc(N);
     for (hlong i = 0; i < N; ++i) S->invDiag[i] = 1.0 / d[i];
     free(d);
-  } else if (S->s.precon == ORC_PRE_MULTIGRID || S->s.precon == ORC_PRE_PARALMOND) {
+  } else if (S->s.precon == ORC_PRE_MULTIGRID || S->s.precon == ORC_PRE_PARALMOND || S->s.precon == ORC_PRE_SEMFEM) {
     S->mg = build_multigrid(S);
   }
   return S;

@@ -17,7 +17,7 @@ from oracle.oracle import Oracle
 pytestmark = pytest.mark.gpu
 
 GOLDEN = ("testEllipticHex_C0", "testEllipticHex_C0_Jacobi", "testEllipticHex_C0_ParAlmond",
-          "testEllipticHex_C0_Multigrid", "testEllipticHex_C0_AllNeumann")
+          "testEllipticHex_C0_Multigrid", "testEllipticHex_C0_AllNeumann", "testEllipticHex_C0_Semfem")
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -36,7 +36,8 @@ def test_reference_golden_norms(reference_norms, name):
     assert r["converged"]
     assert abs(r["norm"] - case["norm"]) < reference_norms["tolerance"], (r["norm"], case["norm"])
     assert abs(r["norm"] - ro["norm"]) < 1e-9
-    assert abs(r["iterations"] - ro["iterations"]) <= (0 if "ParAlmond" not in name else 1), \
+    amg = "ParAlmond" in name or "Semfem" in name
+    assert abs(r["iterations"] - ro["iterations"]) <= (1 if amg else 0), \
         (r["iterations"], ro["iterations"])
 
 
@@ -112,6 +113,32 @@ def test_double_word_outer_operator_solve(prec):
     assert abs(r["iterations"] - ro["iterations"]) <= 1, (r["iterations"], ro["iterations"])
     assert abs(r["error"] - ro["error"]) <= 0.01 * ro["error"]
     assert abs(r["norm"] - ro["norm"]) < 1e-9 * ro["norm"]
+
+
+@pytest.mark.parametrize("over", [{}, {"LAMBDA FIELD": "LOGNORMAL", "LAMBDA SEED": 2},
+                                  {"LAMBDA": 0.0, "BOX BOUNDARY FLAG": -1}], ids=["jittered", "lognormal", "periodic"])
+def test_semfem_preconditioner_matches_oracle(over):
+    """SEMFEM (ellipticPreconSEMFEM.cpp): parAlmond AMG of the trilinear FEM matrix on the
+    GLL sub-mesh, applied to the degree-N vectors."""
+    s = dict(config1(), **{"BOX NX": 4, "BOX NY": 3, "BOX NZ": 3, "POLYNOMIAL DEGREE": 4, "MESH JITTER": 0.1,
+                           "LAMBDA": 1.0, "LINEAR SOLVER": "PCG", "PRECONDITIONER": "SEMFEM",
+                           "PARALMOND AGGREGATION": "UNSMOOTHED"})
+    s.update(over)
+    if over.get("BOX BOUNDARY FLAG") == -1:
+        s["MESH JITTER"] = 0.0
+    r = lpg.Elliptic(s).Run(want_solution=True)
+    ro = Oracle(s).run()
+    assert r["converged"]
+    assert abs(r["iterations"] - ro["iterations"]) <= 1, (r["iterations"], ro["iterations"])
+    assert rel_err(r["xL"], ro["xL"]) < 1e-7
+    e = lpg.Elliptic(s)
+    o = Oracle(s)
+    rng = np.random.default_rng(5)
+    rh = rng.standard_normal(e.Nglobal)
+    z = torch.zeros(e.Nglobal, dtype=torch.float64, device="cuda")
+    e.precon(torch.tensor(rh, device="cuda"), z)
+    torch.cuda.synchronize()
+    assert rel_err(z.cpu().numpy(), o.precon(rh)) < 1e-9
 
 
 def test_lognormal_lambda_and_gaussian_sources_solve():

@@ -11,7 +11,7 @@ from conftest import golden_case_settings
 from oracle.oracle import Oracle
 
 ON_PATH = ("testEllipticHex_C0", "testEllipticHex_C0_Jacobi", "testEllipticHex_C0_ParAlmond",
-           "testEllipticHex_C0_Multigrid", "testEllipticHex_C0_AllNeumann")
+           "testEllipticHex_C0_Multigrid", "testEllipticHex_C0_AllNeumann", "testEllipticHex_C0_Semfem")
 
 
 @pytest.mark.parametrize("name", ON_PATH)
@@ -24,9 +24,9 @@ def test_reference_golden_norm(reference_norms, name):
 
 
 def test_golden_cases_off_path_are_listed(reference_norms):
-    # SEMFEM and OAS preconditioners are other discretisation paths (out of scope).
+    # the overlapping additive Schwarz (OAS) preconditioner is out of scope
     off = set(reference_norms["cases"]) - set(ON_PATH)
-    assert off == {"testEllipticHex_C0_Semfem", "testEllipticHex_C0_OAS"}
+    assert off == {"testEllipticHex_C0_OAS"}
 
 
 def test_gll_nodes_weights():
