@@ -73,9 +73,11 @@ int build(lpg_elliptic* h) {
   Settings& S = h->settings;
   if (S.geti("ELEMENT TYPE", 12) != 12 || S.geti("MESH DIMENSION", 3) != 3)
     return set_error(LPG_ERR_UNSUPPORTED, "only hexahedra (ELEMENT TYPE 12, MESH DIMENSION 3) are supported");
-  if (S.get("DISCRETIZATION", "CONTINUOUS") != "CONTINUOUS")
-    return set_error(LPG_ERR_UNSUPPORTED, "only the CONTINUOUS discretization is supported");
+  const std::string disc = S.get("DISCRETIZATION", "CONTINUOUS");
+  if (disc != "CONTINUOUS" && disc != "IPDG")
+    return set_error(LPG_ERR_SETTINGS, "DISCRETIZATION must be CONTINUOUS or IPDG");
   MeshConfig& c = h->mcfg;
+  c.ipdg = (disc == "IPDG");
   c.nx = S.geti("BOX GLOBAL NX", 0) > 0 ? S.geti("BOX GLOBAL NX", 0) : S.geti("BOX NX", 10);
   c.ny = S.geti("BOX GLOBAL NY", 0) > 0 ? S.geti("BOX GLOBAL NY", 0) : S.geti("BOX NY", 10);
   c.nz = S.geti("BOX GLOBAL NZ", 0) > 0 ? S.geti("BOX GLOBAL NZ", 0) : S.geti("BOX NZ", 10);
@@ -121,6 +123,7 @@ int build(lpg_elliptic* h) {
   if (opPrec == "DF64" && N != 3 && N != 7)
     return set_error(LPG_ERR_UNSUPPORTED, "OPERATOR PRECISION DF64 needs POLYNOMIAL DEGREE 3 or 7");
   el->opDW = (opPrec == "DF64");
+  if (c.ipdg && el->opDW) return set_error(LPG_ERR_UNSUPPORTED, "OPERATOR PRECISION DF64 is defined for CONTINUOUS only");
   // right-hand side data
   const std::string rhsField = S.get("RHS FIELD", "SINE");
   if (rhsField == "GAUSSIAN SOURCES") {
@@ -152,6 +155,8 @@ int build(lpg_elliptic* h) {
   const std::string pre = S.get("PRECONDITIONER", "NONE");
   if (pre == "NONE") h->precon = make_identity(el);
   else if (pre == "JACOBI") h->precon = make_jacobi(el, &rc);
+  else if (c.ipdg && pre != "NONE" && pre != "JACOBI")
+    return set_error(LPG_ERR_UNSUPPORTED, "IPDG supports PRECONDITIONER NONE and JACOBI");
   else if (pre == "MULTIGRID" || pre == "PARALMOND" || pre == "SEMFEM") {
     MGOptions o;
     o.amgOnly = (pre == "PARALMOND" || pre == "SEMFEM");
@@ -384,7 +389,8 @@ extern "C" int lpg_elliptic_random_vector(lpg_elliptic* e, uint64_t seed, double
   if (!e || !q) return set_error(LPG_ERR_INVALID, "null argument");
   LPG_GUARD_BEGIN
   const MeshConfig& c = e->mcfg;
-  if (!c.is_box()) return set_error(LPG_ERR_UNSUPPORTED, "random lattice vectors need MESH FILE = BOX");
+  if (!c.is_box() || c.ipdg)
+    return set_error(LPG_ERR_UNSUPPORTED, "random lattice vectors need MESH FILE = BOX and CONTINUOUS");
   BoxNumbering b{c.nx, c.ny, c.nz, e->el->mesh.N, c.bcflag == -1 ? 1 : 0, c.bcflag == 1 ? 1 : 0};
   return lattice_random(b, e->el->Nglobal, e->el->owner.p, seed, q, pick(e, stream));
   LPG_GUARD_END
@@ -399,6 +405,7 @@ extern "C" int lpg_elliptic_operator(lpg_elliptic* e, const double* q, double* A
 
 extern "C" int lpg_elliptic_operator_df64(lpg_elliptic* e, const double* q, double* Aq, void* stream) {
   if (!e || !q || !Aq) return set_error(LPG_ERR_INVALID, "null argument");
+  if (e->el->ipdg) return set_error(LPG_ERR_UNSUPPORTED, "the double-word operator is CONTINUOUS only");
   if (e->el->mesh.N != 3 && e->el->mesh.N != 7) return set_error(LPG_ERR_UNSUPPORTED, "DF64 operator: N must be 3 or 7");
   LPG_GUARD_BEGIN
   return e->el->OperatorDW(q, Aq, pick(e, stream));
@@ -407,6 +414,7 @@ extern "C" int lpg_elliptic_operator_df64(lpg_elliptic* e, const double* q, doub
 
 extern "C" int lpg_elliptic_operator_f32(lpg_elliptic* e, const float* q, float* Aq, int bf16geo, void* stream) {
   if (!e || !q || !Aq) return set_error(LPG_ERR_INVALID, "null argument");
+  if (e->el->ipdg) return set_error(LPG_ERR_UNSUPPORTED, "reduced-precision operators are CONTINUOUS only");
   LPG_GUARD_BEGIN
   cudaStream_t s = pick(e, stream);
   int rc = e->el->make_f32(bf16geo != 0, s);
@@ -417,6 +425,7 @@ extern "C" int lpg_elliptic_operator_f32(lpg_elliptic* e, const float* q, float*
 
 extern "C" int lpg_elliptic_operator_host(lpg_elliptic* e, const double* q_host, double* Aq_host) {
   if (!e || !q_host || !Aq_host) return set_error(LPG_ERR_INVALID, "null argument");
+  if (e->el->ipdg) return set_error(LPG_ERR_UNSUPPORTED, "the host-buffer operator is CONTINUOUS only");
   LPG_GUARD_BEGIN
   return e->el->OperatorHost(q_host, Aq_host, e->plat.stream);
   LPG_GUARD_END
@@ -424,6 +433,7 @@ extern "C" int lpg_elliptic_operator_host(lpg_elliptic* e, const double* q_host,
 
 extern "C" int lpg_elliptic_operator_host_f32(lpg_elliptic* e, const float* q_host, float* Aq_host, int bf16geo) {
   if (!e || !q_host || !Aq_host) return set_error(LPG_ERR_INVALID, "null argument");
+  if (e->el->ipdg) return set_error(LPG_ERR_UNSUPPORTED, "the host-buffer operator is CONTINUOUS only");
   LPG_GUARD_BEGIN
   cudaStream_t s = e->plat.stream;
   int rc = e->el->make_f32(bf16geo != 0, s);

@@ -128,6 +128,7 @@ int Elliptic::setup(Platform* p, const MeshConfig& c, int N, double lam, const s
                     cudaStream_t s) {
   plat = p;
   lambda = lam;
+  if (c.ipdg) return setup_ipdg(c, N, lamE, s);
   if (!c.is_box()) return setup_file(c, N, lamE, s);
   if (c.bcflag != 1 && c.bcflag != -1)
     return set_error(LPG_ERR_UNSUPPORTED, "BOX BOUNDARY FLAG must be 1 (Dirichlet) or -1 (periodic)");
@@ -256,6 +257,65 @@ int Elliptic::setup_semfem(const Elliptic& sem, cudaStream_t s) {
   return LPG_OK;
 }
 
+// IPDG (ellipticSetup.cpp:66-81, ellipticBoundarySetup.cpp:89-93): every local node is an
+// unknown; trace maps from the mesh connectivity (box or file), geometric factors on the GPU.
+int Elliptic::setup_ipdg(const MeshConfig& c, int N, const std::vector<double>* lamE, cudaStream_t s) {
+  ipdg = true;
+  if (c.is_box() && c.bcflag != 1 && c.bcflag != -1)
+    return set_error(LPG_ERR_UNSUPPORTED, "BOX BOUNDARY FLAG must be 1 (Dirichlet) or -1 (periodic)");
+  if (c.is_box() && c.bcflag == -1 && (c.nx < 2 || c.ny < 2 || c.nz < 2))
+    return set_error(LPG_ERR_UNSUPPORTED, "periodic boxes need at least 2 elements per direction");
+  int rc = mesh.setup(c, N, s);
+  if (rc) return rc;
+  const int Nq = N + 1, Np = mesh.Np, Nfp = Nq * Nq;
+  const int64_t E = mesh.E;
+  Nlocal = E * Np;
+  Nglobal = Nlocal;
+  HexMeshData boxMesh;
+  const HexMeshData* hm = c.file.get();
+  if (!hm) {
+    boxMesh = box_hex_mesh(c.nx, c.ny, c.nz, c.bcflag);
+    hm = &boxMesh;
+  }
+  std::vector<int32_t> vP, mP;
+  if ((rc = hex_traces(*hm, N, mesh.r1d, vP, mP))) return rc;
+  hasDirichlet = false;
+  for (int b : hm->EToB) hasDirichlet = hasDirichlet || (b == 1);
+  std::vector<int32_t> iota(Nlocal);
+  for (int64_t n = 0; n < Nlocal; ++n) iota[n] = (int32_t)n;
+  DevBuf<int32_t> mapP;
+  DevBuf<double> hfac;
+  if ((rc = g2l.alloc(Nlocal)) || (rc = owner.alloc(Nlocal)) || (rc = weightG.alloc(Nlocal)) ||
+      (rc = vgeo.alloc(E * 10 * Np)) || (rc = sgeo.alloc(E * 5 * 6 * Nfp)) || (rc = g4.alloc(4 * Nlocal)) ||
+      (rc = vmapP.alloc(E * 6 * Nfp)) || (rc = mapP.alloc(E * 6 * Nfp)) || (rc = EToB.alloc(E * 6)) ||
+      (rc = hfac.alloc(E * 6 * Nfp)))
+    return rc;
+  if ((rc = g2l.upload(iota.data(), Nlocal, s)) || (rc = owner.upload(iota.data(), Nlocal, s)) ||
+      (rc = vmapP.upload(vP.data(), E * 6 * Nfp, s)) || (rc = mapP.upload(mP.data(), E * 6 * Nfp, s)) ||
+      (rc = EToB.upload(hm->EToB.data(), E * 6, s)) || (rc = fill<double>(Nlocal, 1.0, weightG.p, s)))
+    return rc;
+  tau = 2.0 * (N + 1) * (N + 3);
+  IpdgArgs a = ipdg_args();
+  a.hfac = hfac.p;
+  if ((rc = ipdg_geometry(a, mapP.p, s))) return rc;
+  if ((rc = finish_setup(lamE, s))) return rc;   // synchronises before the host vectors go
+  return LPG_OK;
+}
+
+IpdgArgs Elliptic::ipdg_args() const {
+  IpdgArgs a;
+  a.N = mesh.N;
+  a.E = mesh.E;
+  a.EX = mesh.EX.p; a.EY = mesh.EY.p; a.EZ = mesh.EZ.p;
+  a.D = mesh.D_d.p; a.r1d = mesh.r1d_d.p; a.w1d = mesh.w1d_d.p;
+  a.vgeo = vgeo.p; a.sgeo = sgeo.p;
+  a.vmapP = vmapP.p; a.EToB = EToB.p;
+  a.lambda = lambda; a.tau = tau;
+  a.lambdaE = hasLambdaE ? lambdaE.p : nullptr;
+  a.g4 = reinterpret_cast<double4_32a*>(g4.p);
+  return a;
+}
+
 int Elliptic::finish_setup(const std::vector<double>* lamE, cudaStream_t s) {
   int rc;
   const int64_t E = mesh.E;
@@ -295,6 +355,12 @@ int Elliptic::OperatorDW(const double* q, double* Aq, cudaStream_t s) {
 }
 
 int Elliptic::Operator(const double* q, double* Aq, cudaStream_t s) {
+  if (ipdg) {
+    IpdgArgs a = ipdg_args();
+    a.q = q;
+    a.out = Aq;
+    return ipdg_operator(a, s);
+  }
   if (opDW) return OperatorDW(q, Aq, s);
   AxArgs<double, double> a;
   const int64_t Np = mesh.Np;
@@ -473,6 +539,14 @@ int Elliptic::OperatorHostF32(const float* qHost, float* AqHost, Prec prec, cuda
 }
 
 int Elliptic::BuildDiagonal(double* diagG, cudaStream_t s) {
+  if (ipdg) {   // BuildOperatorDiagonalIpdgHex3D: no rank boost for the hexahedral IPDG diagonal
+    IpdgArgs a = ipdg_args();
+    a.out = diagG;
+    int rc = ipdg_diagonal(a, s);
+    if (rc) return rc;
+    LPG_CUDA_TRY(cudaStreamSynchronize(s));
+    return LPG_OK;
+  }
   DevBuf<double> dL;
   int rc = dL.alloc(Nlocal);
   if (rc) return rc;
@@ -493,7 +567,13 @@ int Elliptic::BuildRhs(double* r, cudaStream_t s) {
   if ((rc = rhs_local(mesh.N, mesh.E, mesh.EX.p, mesh.EY.p, mesh.EZ.p, mesh.r1d_d.p, mesh.geo.p,
                       hasLambdaE ? lambdaE.p : nullptr, lambda, g2l.p, spec, rL.p, gL.p, s)))
     return rc;
-  if (rhsKind == 0 && hasDirichlet) {
+  if (ipdg && rhsKind == 0) {
+    // weakly imposed boundary data (ellipticRhsBCIpdgHex3D.okl)
+    IpdgArgs a = ipdg_args();
+    a.out = rL.p;
+    if ((rc = ipdg_rhs_bc(a, s))) return rc;
+  }
+  if (rhsKind == 0 && hasDirichlet && !ipdg) {
     // Dirichlet lifting rhs -= A_e g (ellipticRhsBCHex3D.okl:60-290)
     AxArgs<double, double> a;
     const int64_t Np = mesh.Np;

@@ -204,6 +204,125 @@ int connect_hex_mesh(HexMeshData& m) {
   return LPG_OK;
 }
 
+namespace {
+
+// Face nodes of the degree-N hexahedron and the node pairing of two connected faces.
+// Nodes of face f are listed in local index order (faces t=-1, s=-1, r=+1, s=+1, r=-1,
+// t=+1 as in meshBasisHex3D.cpp); a node of face fM is paired with the node of face fP
+// that has the same bilinear weights on the four shared vertices, whatever the relative
+// orientation of the two faces. Tables are built on first use per (fM, fP, vertex
+// correspondence).
+struct FacePairing {
+  int Nq = 0, Nfp = 0;
+  std::vector<int> faceNodes;   // [6][Nfp]
+  std::vector<double> W;        // [6][Nfp][4]
+  std::vector<std::vector<int>> tables;
+  FacePairing(int N, const std::vector<double>& r1d) : Nq(N + 1), Nfp((N + 1) * (N + 1)) {
+    faceNodes.resize(6 * Nfp);
+    int cnt[6] = {0, 0, 0, 0, 0, 0};
+    for (int k = 0; k < Nq; ++k)
+      for (int j = 0; j < Nq; ++j)
+        for (int i = 0; i < Nq; ++i) {
+          const int n = i + j * Nq + k * Nfp;
+          if (k == 0) faceNodes[0 * Nfp + cnt[0]++] = n;
+          if (j == 0) faceNodes[1 * Nfp + cnt[1]++] = n;
+          if (i == N) faceNodes[2 * Nfp + cnt[2]++] = n;
+          if (j == N) faceNodes[3 * Nfp + cnt[3]++] = n;
+          if (i == 0) faceNodes[4 * Nfp + cnt[4]++] = n;
+          if (k == N) faceNodes[5 * Nfp + cnt[5]++] = n;
+        }
+    static const int cx[8] = {0, 1, 1, 0, 0, 1, 1, 0}, cy[8] = {0, 0, 1, 1, 0, 0, 1, 1}, cz[8] = {0, 0, 0, 0, 1, 1, 1, 1};
+    W.resize(6 * Nfp * 4);
+    for (int f = 0; f < 6; ++f)
+      for (int n = 0; n < Nfp; ++n) {
+        const int v = faceNodes[f * Nfp + n];
+        const double r = r1d[v % Nq], s = r1d[(v / Nq) % Nq], t = r1d[v / Nfp];
+        for (int a = 0; a < 4; ++a) {
+          const int c = kHexFaceVerts[f][a];
+          W[(f * Nfp + n) * 4 + a] = 0.125 * (cx[c] ? 1 + r : 1 - r) * (cy[c] ? 1 + s : 1 - s) * (cz[c] ? 1 + t : 1 - t);
+        }
+      }
+    tables.resize(6 * 6 * 256);
+  }
+  // T[nM] = nP for face f of element e and its neighbour face; nullptr on a mismatch
+  const std::vector<int>* pair(const HexMeshData& m, int64_t e, int f) {
+    const int64_t eP = m.EToE[e * 6 + f];
+    const int fP = m.EToF[e * 6 + f];
+    int sigma[4];
+    for (int a = 0; a < 4; ++a) {
+      const int64_t g = m.EToV[e * 8 + kHexFaceVerts[f][a]];
+      sigma[a] = -1;
+      for (int b = 0; b < 4; ++b)
+        if (m.EToV[eP * 8 + kHexFaceVerts[fP][b]] == g) sigma[a] = b;
+      if (sigma[a] < 0) return nullptr;
+    }
+    const int code = sigma[0] + 4 * sigma[1] + 16 * sigma[2] + 64 * sigma[3];
+    std::vector<int>& T = tables[(f * 6 + fP) * 256 + code];
+    if (!T.empty()) return &T;
+    T.assign(Nfp, -1);
+    for (int n = 0; n < Nfp; ++n)
+      for (int q = 0; q < Nfp; ++q) {
+        double d = 0;
+        for (int a = 0; a < 4; ++a) d += std::fabs(W[(f * Nfp + n) * 4 + a] - W[(fP * Nfp + q) * 4 + sigma[a]]);
+        if (d < 1e-10) { T[n] = q; break; }
+      }
+    for (int n = 0; n < Nfp; ++n)
+      if (T[n] < 0) { T.clear(); return nullptr; }
+    return &T;
+  }
+};
+
+}  // namespace
+
+int hex_traces(const HexMeshData& m, int N, const std::vector<double>& r1d, std::vector<int32_t>& vmapP,
+               std::vector<int32_t>& mapP) {
+  const int Nq = N + 1, Np = Nq * Nq * Nq, Nfp = Nq * Nq;
+  const int64_t E = m.E;
+  if (E * Np >= (int64_t)INT32_MAX || E * 6 * Nfp >= (int64_t)INT32_MAX)
+    return set_error(LPG_ERR_UNSUPPORTED, "more than 2^31 local nodes");
+  FacePairing fp(N, r1d);
+  vmapP.resize(E * 6 * Nfp);
+  mapP.resize(E * 6 * Nfp);
+  for (int64_t e = 0; e < E; ++e)
+    for (int f = 0; f < 6; ++f) {
+      const int64_t eP = m.EToE[e * 6 + f];
+      const int fP = m.EToF[e * 6 + f];
+      const std::vector<int>* T = (eP >= 0) ? fp.pair(m, e, f) : nullptr;
+      if (eP >= 0 && !T) return set_error(LPG_ERR_INVALID, "mesh: face nodes of connected faces do not match");
+      for (int n = 0; n < Nfp; ++n) {
+        const int64_t id = (e * 6 + f) * Nfp + n;
+        if (eP < 0) {
+          vmapP[id] = (int32_t)(e * Np + fp.faceNodes[f * Nfp + n]);
+          mapP[id] = (int32_t)id;
+        } else {
+          const int q = (*T)[n];
+          vmapP[id] = (int32_t)(eP * Np + fp.faceNodes[fP * Nfp + q]);
+          mapP[id] = (int32_t)((eP * 6 + fP) * Nfp + q);
+        }
+      }
+    }
+  return LPG_OK;
+}
+
+HexMeshData box_hex_mesh(int nx, int ny, int nz, int bcflag) {
+  HexMeshData m;
+  const bool periodic = (bcflag == -1);
+  const int64_t NnX = periodic ? nx : nx + 1, NnY = periodic ? ny : ny + 1, NnZ = periodic ? nz : nz + 1;
+  m.E = (int64_t)nx * ny * nz;
+  m.Nnodes = NnX * NnY * NnZ;
+  m.EToV.resize(m.E * 8);
+  static const int cx[8] = {0, 1, 1, 0, 0, 1, 1, 0}, cy[8] = {0, 0, 1, 1, 0, 0, 1, 1}, cz[8] = {0, 0, 0, 0, 1, 1, 1, 1};
+  for (int64_t e = 0; e < m.E; ++e) {
+    const int64_t i = e % nx, j = (e / nx) % ny, k = e / ((int64_t)nx * ny);
+    for (int v = 0; v < 8; ++v)
+      m.EToV[e * 8 + v] = (i + cx[v]) % NnX + ((j + cy[v]) % NnY) * NnX + ((k + cz[v]) % NnZ) * NnX * NnY;
+  }
+  connect_hex_mesh(m);
+  for (int64_t i = 0; i < m.E * 6; ++i)
+    if (m.EToE[i] < 0) m.EToB[i] = bcflag;
+  return m;
+}
+
 int number_hex_nodes(const HexMeshData& m, int N, const std::vector<double>& r1d, HexNumbering& out) {
   const int Nq = N + 1, Np = Nq * Nq * Nq, Nfp = Nq * Nq;
   const int64_t E = m.E, Nlocal = E * Np;

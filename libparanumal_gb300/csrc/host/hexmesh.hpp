@@ -50,4 +50,13 @@ struct HexNumbering {
 // numbering of the degree-N nodes (r1d: the N+1 GLL points)
 int number_hex_nodes(const HexMeshData& m, int N, const std::vector<double>& r1d, HexNumbering& out);
 
+// Trace maps of the degree-N face nodes ([E][6][Nfp], face nodes in local index order;
+// meshConnectFaceNodes.cpp:32-101): vmapP = volume node on the other side (itself on the
+// boundary), mapP = index of the paired face node (itself on the boundary).
+int hex_traces(const HexMeshData& m, int N, const std::vector<double>& r1d, std::vector<int32_t>& vmapP,
+               std::vector<int32_t>& mapP);
+// the box mesh's vertex connectivity as a HexMeshData (periodic wrap for bcflag -1; boundary
+// faces get EToB = bcflag)
+HexMeshData box_hex_mesh(int nx, int ny, int nz, int bcflag);
+
 }  // namespace lpg

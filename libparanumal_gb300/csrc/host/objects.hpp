@@ -94,6 +94,8 @@ struct MeshConfig {
   // MESH FILE: a hexahedral mesh read from a Gmsh file (the box fields are then unused)
   std::shared_ptr<const HexMeshData> file;
   bool is_box() const { return !file; }
+  // DISCRETIZATION = IPDG (every level of a hierarchy shares it)
+  bool ipdg = false;
 };
 
 struct Mesh {
@@ -154,6 +156,14 @@ struct Elliptic {
   int rhsKind = 0;                 // 0 sine, 1 Gaussian sources
   std::vector<double> sources;     // nsources*4
   DevBuf<double> sources_d;
+  // IPDG: unknowns are the local nodes (GlobalToLocal is the identity); face data
+  bool ipdg = false;
+  double tau = 0;
+  DevBuf<double> vgeo, sgeo, g4;
+  DevBuf<int32_t> vmapP;
+  DevBuf<int> EToB;
+  int setup_ipdg(const MeshConfig& c, int N, const std::vector<double>* lamE, cudaStream_t s);
+  IpdgArgs ipdg_args() const;
 
   int setup(Platform* p, const MeshConfig& c, int N, double lambda, const std::vector<double>* lamE,
             cudaStream_t s);

@@ -1,0 +1,388 @@
+// Interior-penalty DG discretisation of the screened Poisson operator on hexahedra
+// (DISCRETIZATION = IPDG): geometry, gradient, operator, boundary data of the rhs and
+// the operator diagonal.
+//
+// Reference: ellipticGradientHex3D.okl, ellipticAxIpdgHex3D.okl:34-84 (surface terms with
+// the homogeneous Dirichlet / Neumann mirror states of ellipticBoundary3D.h) and :363-642
+// (weak divergence), ellipticRhsBCIpdgHex3D.okl (boundary data), meshSurfaceGeometricFactors
+// Hex3D.cpp:31-175 (normals, WsJ, penalty scale), ellipticBuildOperatorDiagonal.cpp:874-990.
+//
+// Layout (per element, structure of arrays): vgeo [e][10][Np] = rx ry rz sx sy sz tx ty tz JW;
+// sgeo [e][5][6 Nfp] = nx ny nz WsJ hinv for the face nodes of faces 0..5 (local index order);
+// gradients [E Np] double4_32a = (qx, qy, qz, q).
+//
+// Kernels run one CTA per element with one thread per node. A node owns its accumulators:
+// the face terms of every face it lies on are added by that node's thread, in the face
+// order 0, 5, 1, 3, 2, 4, so no two threads write the same value.
+#include "lpg_common.cuh"
+#include "lpg_internal.hpp"
+
+namespace lpg {
+
+namespace {
+
+constexpr int kVgeo = 10;   // rx ry rz sx sy sz tx ty tz JW
+constexpr int kSgeo = 5;    // nx ny nz WsJ hinv
+
+__device__ __forceinline__ void node_coords(const double* ev, double r, double s, double t, double& x, double& y,
+                                            double& z) {
+  const double c[8] = {(1 - r) * (1 - s) * (1 - t), (1 + r) * (1 - s) * (1 - t), (1 + r) * (1 + s) * (1 - t),
+                       (1 - r) * (1 + s) * (1 - t), (1 - r) * (1 - s) * (1 + t), (1 + r) * (1 - s) * (1 + t),
+                       (1 + r) * (1 + s) * (1 + t), (1 - r) * (1 + s) * (1 + t)};
+  x = y = z = 0;
+#pragma unroll
+  for (int v = 0; v < 8; ++v) {
+    x += 0.125 * c[v] * ev[v];
+    y += 0.125 * c[v] * ev[8 + v];
+    z += 0.125 * c[v] * ev[16 + v];
+  }
+}
+
+// face index b of node (i,j,k) on face f (faces 0..5 = t-, s-, r+, s+, r-, t+)
+template <int NQ>
+__device__ __forceinline__ int face_slot(int f, int i, int j, int k) {
+  return (f == 0 || f == 5) ? i + j * NQ : (f == 1 || f == 3) ? i + k * NQ : j + k * NQ;
+}
+
+// ---------------------------------------------------------------- geometry
+template <int NQ>
+__global__ void __launch_bounds__(NQ * NQ * NQ)
+ipdg_geometry_kernel(const double* __restrict__ EX, const double* __restrict__ EY, const double* __restrict__ EZ,
+                     const double* __restrict__ Dg, const double* __restrict__ r1d, const double* __restrict__ w1d,
+                     double* __restrict__ vgeo, double* __restrict__ sgeo, double* __restrict__ hfac) {
+  constexpr int NP = NQ * NQ * NQ, NFP = NQ * NQ;
+  __shared__ double s_x[NP], s_y[NP], s_z[NP], s_D[NQ * NQ], s_ev[24];
+  const int64_t e = blockIdx.x;
+  const int n = threadIdx.x;
+  if (n < NQ * NQ) s_D[n] = Dg[n];
+  if (n < 8) { s_ev[n] = EX[e * 8 + n]; s_ev[8 + n] = EY[e * 8 + n]; s_ev[16 + n] = EZ[e * 8 + n]; }
+  __syncthreads();
+  const int i = n % NQ, j = (n / NQ) % NQ, k = n / NFP;
+  node_coords(s_ev, r1d[i], r1d[j], r1d[k], s_x[n], s_y[n], s_z[n]);
+  __syncthreads();
+  double xr = 0, xs = 0, xt = 0, yr = 0, ys = 0, yt = 0, zr = 0, zs = 0, zt = 0;
+#pragma unroll
+  for (int m = 0; m < NQ; ++m) {
+    const int ir = m + j * NQ + k * NFP, is = i + m * NQ + k * NFP, it = i + j * NQ + m * NFP;
+    const double dr = s_D[i * NQ + m], ds = s_D[j * NQ + m], dt = s_D[k * NQ + m];
+    xr += dr * s_x[ir]; xs += ds * s_x[is]; xt += dt * s_x[it];
+    yr += dr * s_y[ir]; ys += ds * s_y[is]; yt += dt * s_y[it];
+    zr += dr * s_z[ir]; zs += ds * s_z[is]; zt += dt * s_z[it];
+  }
+  const double J = xr * (ys * zt - zs * yt) - yr * (xs * zt - zs * xt) + zr * (xs * yt - ys * xt);
+  const double g[9] = {(ys * zt - zs * yt) / J,  -(xs * zt - zs * xt) / J, (xs * yt - ys * xt) / J,
+                       -(yr * zt - zr * yt) / J, (xr * zt - zr * xt) / J,  -(xr * yt - yr * xt) / J,
+                       (yr * zs - zr * ys) / J,  -(xr * zs - zr * xs) / J, (xr * ys - yr * xs) / J};
+  double* vg = vgeo + e * kVgeo * NP;
+#pragma unroll
+  for (int c = 0; c < 9; ++c) vg[c * NP + n] = g[c];
+  vg[9 * NP + n] = J * w1d[i] * w1d[j] * w1d[k];
+  // face factors of every face this node lies on
+  double* sg = sgeo + e * kSgeo * 6 * NFP;
+  const int faces[6] = {k == 0 ? 0 : -1, k == NQ - 1 ? 5 : -1, j == 0 ? 1 : -1,
+                        j == NQ - 1 ? 3 : -1, i == NQ - 1 ? 2 : -1, i == 0 ? 4 : -1};
+#pragma unroll
+  for (int q = 0; q < 6; ++q) {
+    const int f = faces[q];
+    if (f < 0) continue;
+    // outward normal direction +-(grad r | grad s | grad t)
+    const int c0 = (f == 0 || f == 5) ? 6 : (f == 1 || f == 3) ? 3 : 0;
+    const double sgn = (f == 0 || f == 1 || f == 4) ? -1.0 : 1.0;
+    const double nx = sgn * g[c0], ny = sgn * g[c0 + 1], nz = sgn * g[c0 + 2];
+    const double len = sqrt(nx * nx + ny * ny + nz * nz);
+    const double sJ = len * J;
+    const int b = face_slot<NQ>(f, i, j, k);
+    const int col = f * NFP + b;
+    const double wa = w1d[b % NQ], wb = w1d[b / NQ];
+    sg[0 * 6 * NFP + col] = nx / len;
+    sg[1 * 6 * NFP + col] = ny / len;
+    sg[2 * 6 * NFP + col] = nz / len;
+    sg[3 * 6 * NFP + col] = sJ * wa * wb;
+    hfac[e * 6 * NFP + col] = sJ / J;
+  }
+}
+
+// hinv = max(sJ/J) over the two sides of each face node (meshSurfaceGeometricFactorsHex3D.cpp:160-172)
+__global__ void ipdg_hinv_kernel(const int64_t nFaceNodes, const int nfpAll, const double* __restrict__ hfac,
+                                 const int32_t* __restrict__ mapP, double* __restrict__ sgeo) {
+  for (int64_t id = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; id < nFaceNodes;
+       id += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e = id / nfpAll;
+    const int c = (int)(id % nfpAll);
+    sgeo[(e * kSgeo + 4) * nfpAll + c] = fmax(hfac[id], hfac[mapP[id]]);
+  }
+}
+
+// ---------------------------------------------------------------- gradient
+template <int NQ>
+__global__ void __launch_bounds__(NQ * NQ * NQ)
+ipdg_gradient_kernel(const double* __restrict__ vgeo, const double* __restrict__ Dg, const double* __restrict__ q,
+                     double4_32a* __restrict__ g4) {
+  constexpr int NP = NQ * NQ * NQ, NFP = NQ * NQ;
+  __shared__ double s_q[NP], s_D[NQ * NQ];
+  const int64_t e = blockIdx.x;
+  const int n = threadIdx.x;
+  if (n < NQ * NQ) s_D[n] = Dg[n];
+  s_q[n] = q[e * NP + n];
+  __syncthreads();
+  const int i = n % NQ, j = (n / NQ) % NQ, k = n / NFP;
+  double qr = 0, qs = 0, qt = 0;
+#pragma unroll
+  for (int m = 0; m < NQ; ++m) {
+    qr += s_D[i * NQ + m] * s_q[m + j * NQ + k * NFP];
+    qs += s_D[j * NQ + m] * s_q[i + m * NQ + k * NFP];
+    qt += s_D[k * NQ + m] * s_q[i + j * NQ + m * NFP];
+  }
+  const double* vg = vgeo + e * kVgeo * NP + n;
+  double4_32a o;
+  o.x = vg[0 * NP] * qr + vg[3 * NP] * qs + vg[6 * NP] * qt;
+  o.y = vg[1 * NP] * qr + vg[4 * NP] * qs + vg[7 * NP] * qt;
+  o.z = vg[2 * NP] * qr + vg[5 * NP] * qs + vg[8 * NP] * qt;
+  o.w = s_q[n];
+  g4[e * NP + n] = o;
+}
+
+// ---------------------------------------------------------------- weak divergence (shared by Ax and rhs)
+// out_n = acc_n + sum_p D[p][i] ur(p,j,k) + D[p][j] us(i,p,k) + D[p][k] ut(i,j,p), with (ur, us, ut)
+// = (grad r, grad s, grad t) . (gx, gy, gz)
+template <int NQ>
+__device__ __forceinline__ double weak_divergence(const double* vg, double gx, double gy, double gz, double acc,
+                                                  double* s_ur, double* s_us, double* s_ut, const double* s_D) {
+  constexpr int NP = NQ * NQ * NQ, NFP = NQ * NQ;
+  const int n = threadIdx.x;
+  s_ur[n] = vg[0 * NP] * gx + vg[1 * NP] * gy + vg[2 * NP] * gz;
+  s_us[n] = vg[3 * NP] * gx + vg[4 * NP] * gy + vg[5 * NP] * gz;
+  s_ut[n] = vg[6 * NP] * gx + vg[7 * NP] * gy + vg[8 * NP] * gz;
+  __syncthreads();
+  const int i = n % NQ, j = (n / NQ) % NQ, k = n / NFP;
+  double v = acc;
+#pragma unroll
+  for (int p = 0; p < NQ; ++p) {
+    v += s_D[p * NQ + i] * s_ur[p + j * NQ + k * NFP];
+    v += s_D[p * NQ + j] * s_us[i + p * NQ + k * NFP];
+    v += s_D[p * NQ + k] * s_ut[i + j * NQ + p * NFP];
+  }
+  return v;
+}
+
+// ---------------------------------------------------------------- operator
+template <int NQ>
+__global__ void __launch_bounds__(NQ * NQ * NQ)
+ipdg_ax_kernel(const double* __restrict__ vgeo, const double* __restrict__ sgeo, const int32_t* __restrict__ vmapP,
+               const int* __restrict__ EToB, const double* __restrict__ Dg, const double lambda,
+               const double* __restrict__ lambdaE, const double tau, const double4_32a* __restrict__ g4,
+               double* __restrict__ Aq) {
+  constexpr int NP = NQ * NQ * NQ, NFP = NQ * NQ;
+  __shared__ double s_ur[NP], s_us[NP], s_ut[NP], s_D[NQ * NQ];
+  const int64_t e = blockIdx.x;
+  const int n = threadIdx.x;
+  if (n < NQ * NQ) s_D[n] = Dg[n];
+  const int i = n % NQ, j = (n / NQ) % NQ, k = n / NFP;
+  const double* vg = vgeo + e * kVgeo * NP + n;
+  const double4_32a GM = g4[e * NP + n];
+  const double JW = vg[9 * NP];
+  const double lam = lambdaE ? lambdaE[e] : lambda;
+  double gx = JW * GM.x, gy = JW * GM.y, gz = JW * GM.z, a = JW * lam * GM.w;
+  const double* sg = sgeo + e * kSgeo * 6 * NFP;
+  const int faces[6] = {k == 0 ? 0 : -1, k == NQ - 1 ? 5 : -1, j == 0 ? 1 : -1,
+                        j == NQ - 1 ? 3 : -1, i == NQ - 1 ? 2 : -1, i == 0 ? 4 : -1};
+#pragma unroll
+  for (int q = 0; q < 6; ++q) {
+    const int f = faces[q];
+    if (f < 0) continue;
+    const int col = f * NFP + face_slot<NQ>(f, i, j, k);
+    const double nx = sg[0 * 6 * NFP + col], ny = sg[1 * 6 * NFP + col], nz = sg[2 * 6 * NFP + col];
+    const double w = sg[3 * 6 * NFP + col], hinv = sg[4 * 6 * NFP + col];
+    double4_32a P = g4[vmapP[e * 6 * NFP + col]];
+    const int bc = EToB[e * 6 + f];
+    if (bc > 0) {
+      // homogeneous boundary state B (Dirichlet: q = 0, grad kept; Neumann: q kept, grad = 0),
+      // then the mirror state 2B - M
+      if (bc == 1) { P.x = GM.x; P.y = GM.y; P.z = GM.z; P.w = -GM.w; }
+      else { P.x = -GM.x; P.y = -GM.y; P.z = -GM.z; P.w = GM.w; }
+    }
+    const double dq = P.w - GM.w;
+    gx += 0.5 * w * nx * dq;
+    gy += 0.5 * w * ny * dq;
+    gz += 0.5 * w * nz * dq;
+    a += -0.5 * w * (nx * (P.x + GM.x) + ny * (P.y + GM.y) + nz * (P.z + GM.z) + tau * hinv * dq);
+  }
+  Aq[e * NP + n] = weak_divergence<NQ>(vg, gx, gy, gz, a, s_ur, s_us, s_ut, s_D);
+}
+
+// ---------------------------------------------------------------- rhs boundary data
+// rhs -= weak form of the boundary state of u = sin(pi x) sin(pi y) sin(pi z) (Dirichlet value,
+// or the Neumann data of the sine data file) against a zero interior state
+template <int NQ>
+__global__ void __launch_bounds__(NQ * NQ * NQ)
+ipdg_rhs_bc_kernel(const double* __restrict__ EX, const double* __restrict__ EY, const double* __restrict__ EZ,
+                   const double* __restrict__ r1d, const double* __restrict__ vgeo, const double* __restrict__ sgeo,
+                   const int* __restrict__ EToB, const double* __restrict__ Dg, const double tau,
+                   double* __restrict__ rhs) {
+  constexpr int NP = NQ * NQ * NQ, NFP = NQ * NQ;
+  __shared__ double s_ur[NP], s_us[NP], s_ut[NP], s_D[NQ * NQ], s_ev[24];
+  __shared__ int s_any;
+  const int64_t e = blockIdx.x;
+  const int n = threadIdx.x;
+  if (n == 0) {
+    int any = 0;
+    for (int f = 0; f < 6; ++f) any |= (EToB[e * 6 + f] > 0);
+    s_any = any;
+  }
+  if (n < NQ * NQ) s_D[n] = Dg[n];
+  if (n < 8) { s_ev[n] = EX[e * 8 + n]; s_ev[8 + n] = EY[e * 8 + n]; s_ev[16 + n] = EZ[e * 8 + n]; }
+  __syncthreads();
+  if (!s_any) return;   // uniform over the block
+  const int i = n % NQ, j = (n / NQ) % NQ, k = n / NFP;
+  double x, y, z;
+  node_coords(s_ev, r1d[i], r1d[j], r1d[k], x, y, z);
+  double gx = 0, gy = 0, gz = 0, a = 0;
+  const double* sg = sgeo + e * kSgeo * 6 * NFP;
+  const int faces[6] = {k == 0 ? 0 : -1, k == NQ - 1 ? 5 : -1, j == 0 ? 1 : -1,
+                        j == NQ - 1 ? 3 : -1, i == NQ - 1 ? 2 : -1, i == 0 ? 4 : -1};
+#pragma unroll
+  for (int q = 0; q < 6; ++q) {
+    const int f = faces[q];
+    if (f < 0) continue;
+    const int bc = EToB[e * 6 + f];
+    if (bc <= 0) continue;
+    const int col = f * NFP + face_slot<NQ>(f, i, j, k);
+    const double nx = sg[0 * 6 * NFP + col], ny = sg[1 * 6 * NFP + col], nz = sg[2 * 6 * NFP + col];
+    const double w = sg[3 * 6 * NFP + col], hinv = sg[4 * 6 * NFP + col];
+    double qP = 0, dx = 0, dy = 0, dz = 0;
+    const double sx = sin(LPG_PI * x), sy = sin(LPG_PI * y), sz = sin(LPG_PI * z);
+    if (bc == 1) qP = sx * sy * sz;
+    else {
+      dx = -LPG_PI * cos(LPG_PI * x) * sy * sz;
+      dy = -LPG_PI * sx * cos(LPG_PI * y) * sz;
+      dz = -LPG_PI * sx * sy * cos(LPG_PI * z);
+    }
+    gx += w * nx * qP;
+    gy += w * ny * qP;
+    gz += w * nz * qP;
+    a += -w * (nx * dx + ny * dy + nz * dz + tau * hinv * qP);
+  }
+  const double* vg = vgeo + e * kVgeo * NP + n;
+  rhs[e * NP + n] -= weak_divergence<NQ>(vg, gx, gy, gz, a, s_ur, s_us, s_ut, s_D);
+}
+
+// ---------------------------------------------------------------- diagonal
+template <int NQ>
+__global__ void __launch_bounds__(NQ * NQ * NQ)
+ipdg_diag_kernel(const double* __restrict__ vgeo, const double* __restrict__ sgeo, const int* __restrict__ EToB,
+                 const double* __restrict__ Dg, const double lambda, const double* __restrict__ lambdaE,
+                 const double tau, double* __restrict__ diag) {
+  constexpr int NP = NQ * NQ * NQ, NFP = NQ * NQ;
+  __shared__ double s_D[NQ * NQ];
+  const int64_t e = blockIdx.x;
+  const int n = threadIdx.x;
+  if (n < NQ * NQ) s_D[n] = Dg[n];
+  __syncthreads();
+  const int i = n % NQ, j = (n / NQ) % NQ, k = n / NFP;
+  const double* vg = vgeo + e * kVgeo * NP;
+  const double lam = lambdaE ? lambdaE[e] : lambda;
+  // (grad l_n, grad l_n) over the nodes of the three lines through n, + lambda (l_n, l_n)
+  double A = lam * vg[9 * NP + n];
+  for (int p = 0; p < NQ; ++p) {
+    // r-line (p, j, k), s-line (i, p, k), t-line (i, j, p); node n itself carries all three
+    const int pr = p + j * NQ + k * NFP, ps = i + p * NQ + k * NFP, pt = i + j * NQ + p * NFP;
+    {
+      const double br = s_D[p * NQ + i];
+      const double bs = (p == i) ? s_D[j * NQ + j] : 0.0, bt = (p == i) ? s_D[k * NQ + k] : 0.0;
+      const double dx = vg[0 * NP + pr] * br + vg[3 * NP + pr] * bs + vg[6 * NP + pr] * bt;
+      const double dy = vg[1 * NP + pr] * br + vg[4 * NP + pr] * bs + vg[7 * NP + pr] * bt;
+      const double dz = vg[2 * NP + pr] * br + vg[5 * NP + pr] * bs + vg[8 * NP + pr] * bt;
+      A += vg[9 * NP + pr] * (dx * dx + dy * dy + dz * dz);
+    }
+    if (p != j) {
+      const double bs = s_D[p * NQ + j];
+      const double dx = vg[3 * NP + ps] * bs, dy = vg[4 * NP + ps] * bs, dz = vg[5 * NP + ps] * bs;
+      A += vg[9 * NP + ps] * (dx * dx + dy * dy + dz * dz);
+    }
+    if (p != k) {
+      const double bt = s_D[p * NQ + k];
+      const double dx = vg[6 * NP + pt] * bt, dy = vg[7 * NP + pt] * bt, dz = vg[8 * NP + pt] * bt;
+      A += vg[9 * NP + pt] * (dx * dx + dy * dy + dz * dz);
+    }
+  }
+  // face terms at n itself: -2 c (n . grad l_n) + c tau hinv, c = (1 + D)(1 - N) WsJ / 2
+  const double* sg = sgeo + e * kSgeo * 6 * NFP;
+  const double dlx = vg[0 * NP + n] * s_D[i * NQ + i] + vg[3 * NP + n] * s_D[j * NQ + j] + vg[6 * NP + n] * s_D[k * NQ + k];
+  const double dly = vg[1 * NP + n] * s_D[i * NQ + i] + vg[4 * NP + n] * s_D[j * NQ + j] + vg[7 * NP + n] * s_D[k * NQ + k];
+  const double dlz = vg[2 * NP + n] * s_D[i * NQ + i] + vg[5 * NP + n] * s_D[j * NQ + j] + vg[8 * NP + n] * s_D[k * NQ + k];
+  const int faces[6] = {k == 0 ? 0 : -1, j == 0 ? 1 : -1, i == NQ - 1 ? 2 : -1,
+                        j == NQ - 1 ? 3 : -1, i == 0 ? 4 : -1, k == NQ - 1 ? 5 : -1};
+#pragma unroll
+  for (int q = 0; q < 6; ++q) {
+    const int f = faces[q];
+    if (f < 0) continue;
+    const int col = f * NFP + face_slot<NQ>(f, i, j, k);
+    const int bc = EToB[e * 6 + f];
+    const int bcD = (bc == 1), bcN = (bc > 0 && bc != 1);
+    const double c = 0.5 * (1 + bcD) * (1 - bcN) * sg[3 * 6 * NFP + col];
+    const double ndg = sg[0 * 6 * NFP + col] * dlx + sg[1 * 6 * NFP + col] * dly + sg[2 * 6 * NFP + col] * dlz;
+    A += -c * ndg - c * ndg + c * tau * sg[4 * 6 * NFP + col];
+  }
+  diag[e * NP + n] = A;
+}
+
+template <int NQ>
+int launch_all(int which, const IpdgArgs& a, cudaStream_t s) {
+  constexpr int NP = NQ * NQ * NQ;
+  const unsigned E = (unsigned)a.E;
+  if (a.E <= 0) return LPG_OK;
+  switch (which) {
+    case 0:
+      ipdg_geometry_kernel<NQ><<<E, NP, 0, s>>>(a.EX, a.EY, a.EZ, a.D, a.r1d, a.w1d, a.vgeo, a.sgeo, a.hfac);
+      LPG_LAUNCH_CHECK("ipdg_geometry_kernel");
+      return LPG_OK;
+    case 1:
+      ipdg_gradient_kernel<NQ><<<E, NP, 0, s>>>(a.vgeo, a.D, a.q, a.g4);
+      LPG_LAUNCH_CHECK("ipdg_gradient_kernel");
+      ipdg_ax_kernel<NQ><<<E, NP, 0, s>>>(a.vgeo, a.sgeo, a.vmapP, a.EToB, a.D, a.lambda, a.lambdaE, a.tau, a.g4,
+                                          a.out);
+      LPG_LAUNCH_CHECK("ipdg_ax_kernel");
+      return LPG_OK;
+    case 2:
+      ipdg_rhs_bc_kernel<NQ><<<E, NP, 0, s>>>(a.EX, a.EY, a.EZ, a.r1d, a.vgeo, a.sgeo, a.EToB, a.D, a.tau, a.out);
+      LPG_LAUNCH_CHECK("ipdg_rhs_bc_kernel");
+      return LPG_OK;
+    default:
+      ipdg_diag_kernel<NQ><<<E, NP, 0, s>>>(a.vgeo, a.sgeo, a.EToB, a.D, a.lambda, a.lambdaE, a.tau, a.out);
+      LPG_LAUNCH_CHECK("ipdg_diag_kernel");
+      return LPG_OK;
+  }
+}
+
+int dispatch(int which, const IpdgArgs& a, cudaStream_t s) {
+  switch (a.N) {
+    case 1: return launch_all<2>(which, a, s);
+    case 2: return launch_all<3>(which, a, s);
+    case 3: return launch_all<4>(which, a, s);
+    case 4: return launch_all<5>(which, a, s);
+    case 5: return launch_all<6>(which, a, s);
+    case 6: return launch_all<7>(which, a, s);
+    case 7: return launch_all<8>(which, a, s);
+    case 8: return launch_all<9>(which, a, s);
+    default: return set_error(LPG_ERR_UNSUPPORTED, "IPDG: N must be 1..8");
+  }
+}
+
+}  // namespace
+
+int ipdg_geometry(const IpdgArgs& a, const int32_t* mapP, cudaStream_t s) {
+  int rc = dispatch(0, a, s);
+  if (rc) return rc;
+  const int nfpAll = 6 * (a.N + 1) * (a.N + 1);
+  const int64_t nf = a.E * nfpAll;
+  if (nf <= 0) return LPG_OK;
+  const int64_t blocks = std::min<int64_t>((nf + 255) / 256, 152 * 16);
+  ipdg_hinv_kernel<<<(unsigned)blocks, 256, 0, s>>>(nf, nfpAll, a.hfac, mapP, a.sgeo);
+  LPG_LAUNCH_CHECK("ipdg_hinv_kernel");
+  return LPG_OK;
+}
+int ipdg_operator(const IpdgArgs& a, cudaStream_t s) { return dispatch(1, a, s); }
+int ipdg_rhs_bc(const IpdgArgs& a, cudaStream_t s) { return dispatch(2, a, s); }
+int ipdg_diagonal(const IpdgArgs& a, cudaStream_t s) { return dispatch(3, a, s); }
+
+}  // namespace lpg

@@ -22,4 +22,6 @@ template <> __device__ __forceinline__ float load_geo<float, float>(const float*
 
 constexpr int kMaxNq = 9;   // polynomial degree N <= 8 in the device kernels
 
+#define LPG_PI 3.14159265358979323846
+
 }  // namespace lpg

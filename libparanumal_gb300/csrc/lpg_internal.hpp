@@ -158,6 +158,29 @@ int nb_update(int64_t N, double a, const double* p, const double* sv, const doub
 int nb_directions(int64_t N, double beta, const double* u, const double* w, double* m, const double* nv, double* p,
                   double* sv, double* q, double* z, cudaStream_t s);
 
+// ---------------------------------------------------------------- IPDG
+// Interior-penalty DG operator pieces (DISCRETIZATION = IPDG); unknowns are the E*Np
+// local nodes. vgeo [e][10][Np] (rx..tz, JW), sgeo [e][5][6 Nfp] (nx, ny, nz, WsJ, hinv),
+// vmapP [e][6][Nfp] (neighbour volume node), EToB [e][6], g4 [E*Np] gradient scratch.
+struct IpdgArgs {
+  int N = 0;
+  int64_t E = 0;
+  const double *EX = nullptr, *EY = nullptr, *EZ = nullptr, *D = nullptr, *r1d = nullptr, *w1d = nullptr;
+  double *vgeo = nullptr, *sgeo = nullptr, *hfac = nullptr;
+  const int32_t* vmapP = nullptr;
+  const int* EToB = nullptr;
+  double lambda = 0, tau = 0;
+  const double* lambdaE = nullptr;
+  const double* q = nullptr;
+  double4_32a* g4 = nullptr;
+  double* out = nullptr;
+};
+// vgeo, sgeo (hfac = scratch [E][6 Nfp]); mapP = paired face node of each face node
+int ipdg_geometry(const IpdgArgs& a, const int32_t* mapP, cudaStream_t s);
+int ipdg_operator(const IpdgArgs& a, cudaStream_t s);   // out = A q (q, g4 scratch)
+int ipdg_rhs_bc(const IpdgArgs& a, cudaStream_t s);     // out -= boundary data terms
+int ipdg_diagonal(const IpdgArgs& a, cudaStream_t s);   // out = diag(A)
+
 // ---------------------------------------------------------------- plot output
 // out[e][4][(N+4)^3] = x, y, z (trilinear image of the vertices) and qL interpolated by I
 // ((N+4) x (N+1), row-major) at the equispaced plot points pr (N+4 values), for E elements

@@ -204,7 +204,6 @@ int lattice_random(const BoxNumbering& b, int64_t Nglobal, const int32_t* owner,
 }
 
 // ---------------------------------------------------------------- rhs / norms
-#define LPG_PI 3.14159265358979323846
 
 __device__ __forceinline__ void node_xyz(const double* __restrict__ EX, const double* __restrict__ EY,
                                          const double* __restrict__ EZ, int64_t e, double rn, double sn,

@@ -7,7 +7,7 @@ import os
 import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-SOURCES = ["orc_basis.c", "orc_mesh.c", "orc_gmsh.c", "orc_solver.c"]
+SOURCES = ["orc_basis.c", "orc_mesh.c", "orc_gmsh.c", "orc_ipdg.c", "orc_solver.c"]
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "liboracle.so")
 

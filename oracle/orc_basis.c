@@ -100,9 +100,14 @@ static int set_key(orc_settings *s, const char *key, const char *val) {
     if (strcmp(val, "BOX") == 0) s->mesh_file[0] = 0;
     else snprintf(s->mesh_file, sizeof(s->mesh_file), "%s", val);
   }
+  else if (IS("DISCRETIZATION")) {
+    if (V("IPDG")) s->ipdg = 1;
+    else if (V("CONTINUOUS")) s->ipdg = 0;
+    else return -1;
+  }
   else if (IS("FORMAT") || IS("DATA FILE") || IS("MESH DIMENSION") ||
            IS("ELEMENT TYPE") || IS("THREAD MODEL") || IS("PLATFORM NUMBER") ||
-           IS("DEVICE NUMBER") || IS("DISCRETIZATION") || IS("PARALMOND CYCLE") ||
+           IS("DEVICE NUMBER") || IS("PARALMOND CYCLE") ||
            IS("OUTPUT TO FILE") || IS("VERBOSE") || IS("ELEMENT MAP") ||
            IS("PRECONDITIONER PRECISION") || IS("FINE SMOOTHER") || IS("OUTPUT FILE NAME"))
     ;

@@ -18,6 +18,8 @@
 
 typedef long long hlong;
 
+#define ORC_PI 3.14159265358979323846
+
 /* ---------------- settings (subset of the reference's .rc keys) ---------------- */
 enum { ORC_PCG = 0, ORC_FPCG = 1, ORC_NBFPCG = 2 };
 enum { ORC_PRE_NONE = 0, ORC_PRE_JACOBI = 1, ORC_PRE_MULTIGRID = 2, ORC_PRE_PARALMOND = 3, ORC_PRE_SEMFEM = 4 };
@@ -52,6 +54,7 @@ typedef struct {
   int amg_cheb_degree;
   double tol;
   int maxit;
+  int ipdg;            /* DISCRETIZATION: 0 CONTINUOUS, 1 IPDG */
   char mesh_file[1024]; /* MESH FILE: empty for BOX, else a Gmsh 2.2 ASCII hexahedral mesh */
 } orc_settings;
 
@@ -101,6 +104,7 @@ typedef struct {
   double *wJ;        /* E*Np */
   hlong *globalIds;  /* E*Np */
   int *mapB;         /* E*Np (mesh level: -1 none, >0 flag) */
+  hlong *vmapP;      /* E*6*Nfp: volume node on the other side of each face node (self on the boundary) */
 } orc_mesh;
 
 orc_mesh *orc_mesh_build(const orc_settings *s, int N);
@@ -143,6 +147,11 @@ typedef struct {
   double *lambdaE;   /* per-element lambda or NULL */
   int allNeumann;
   double allNeumannScale;
+  /* IPDG (DISCRETIZATION = IPDG): unknowns are the E*Np local nodes */
+  int ipdg;
+  double tau;
+  double *vgeo;      /* E*10*Np: rx ry rz sx sy sz tx ty tz JW */
+  double *sgeo;      /* E*6*Nfp*5: nx ny nz WsJ hinv */
 } orc_elliptic;
 
 orc_elliptic *orc_elliptic_build(const orc_settings *s, int N, const double *lambdaE);
@@ -150,6 +159,13 @@ void orc_elliptic_free(orc_elliptic *e);
 /* low-order (degree 1) elliptic on the GLL sub-mesh of a degree-N one, sharing its
  * assembled numbering (mesh_t::SetupSEMFEM for hexahedra, meshSetupSEMFEM.cpp:30-214) */
 orc_elliptic *orc_semfem_build(const orc_elliptic *sem);
+
+/* IPDG (orc_ipdg.c) */
+void orc_ipdg_setup(orc_elliptic *el);
+void orc_ipdg_operator(const orc_elliptic *el, const double *q, double *Aq);
+void orc_ipdg_diagonal(const orc_elliptic *el, double *diag);
+/* rhs -= boundary terms of the Dirichlet / Neumann data of the manufactured solution */
+void orc_ipdg_rhs_bc(const orc_elliptic *el, double *rhs);
 
 /* element operators */
 void orc_partial_ax(const orc_elliptic *e, const double *q, double *AqL);

@@ -87,7 +87,7 @@ static orc_mesh *orc_mesh_build_file(const orc_settings *s, int N) {
   free(R);
   connect_nodes(m, vmapM, vmapP);
   free(vmapM);
-  free(vmapP);
+  m->vmapP = vmapP;
   physical_and_geometry(m);
   return m;
 }
@@ -190,7 +190,7 @@ orc_mesh *orc_mesh_build(const orc_settings *s, int N) {
     }
   connect_nodes(m, vmapM, vmapP);
   free(vmapM);
-  free(vmapP);
+  m->vmapP = vmapP;
   physical_and_geometry(m);
   return m;
 }
@@ -323,7 +323,7 @@ void orc_mesh_free(orc_mesh *m) {
   if (!m) return;
   free(m->EToV); free(m->EX); free(m->EY); free(m->EZ); free(m->EToB); free(m->EToE); free(m->EToF);
   free(m->gllz); free(m->gllw); free(m->D); free(m->r); free(m->s); free(m->t); free(m->faceNodes);
-  free(m->x); free(m->y); free(m->z); free(m->ggeo); free(m->wJ); free(m->globalIds); free(m->mapB);
+  free(m->x); free(m->y); free(m->z); free(m->ggeo); free(m->wJ); free(m->globalIds); free(m->mapB); free(m->vmapP);
   free(m);
 }
 
@@ -356,7 +356,9 @@ orc_elliptic *orc_elliptic_build(const orc_settings *s, int N, const double *lam
   for (hlong n = 0; n < Nlocal; ++n) firstDof[n] = -1;
   el->ogs.GlobalToLocal = (int *)malloc(sizeof(int) * Nlocal);
   hlong Ng = 0;
+  el->ipdg = s->ipdg;
   for (hlong n = 0; n < Nlocal; ++n) {
+    if (s->ipdg) { el->ogs.GlobalToLocal[n] = (int)Ng++; continue; }  /* IPDG: every local node is a dof */
     if (el->mapB[n] == 1) { el->ogs.GlobalToLocal[n] = -1; continue; }
     const hlong g = m->globalIds[n] - 1;
     if (firstDof[g] < 0) firstDof[g] = Ng++;
@@ -388,6 +390,7 @@ orc_elliptic *orc_elliptic_build(const orc_settings *s, int N, const double *lam
     const double c = (double)(el->ogs.rowStarts[i + 1] - el->ogs.rowStarts[i]);
     el->weightG[i] = (c > 0) ? 1.0 / c : 0.0;
   }
+  if (el->ipdg) orc_ipdg_setup(el);
   return el;
 }
 
@@ -437,7 +440,7 @@ void orc_elliptic_free(orc_elliptic *e) {
   if (!e) return;
   orc_mesh_free(e->mesh);
   free(e->ogs.rowStarts); free(e->ogs.colIds); free(e->ogs.firstCol); free(e->ogs.GlobalToLocal);
-  free(e->mapB); free(e->weightG); free(e->lambdaE);
+  free(e->mapB); free(e->weightG); free(e->lambdaE); free(e->vgeo); free(e->sgeo);
   free(e);
 }
 

@@ -29,7 +29,7 @@
 #include <omp.h>
 #endif
 
-#define ORC_PI 3.14159265358979323846
+
 
 /* ================================================================ element operators */
 
@@ -122,12 +122,14 @@ static double *scratchL(hlong n) {
 }
 
 void orc_operator(const orc_elliptic *el, const double *q, double *Aq) {
+  if (el->ipdg) { orc_ipdg_operator(el, q, Aq); return; }
   double *AqL = scratchL(el->ogs.Nlocal);
   orc_partial_ax(el, q, AqL);
   orc_gather_trans(&el->ogs, AqL, Aq);
 }
 
 void orc_build_diagonal(const orc_elliptic *el, double *diagA) {
+  if (el->ipdg) { orc_ipdg_diagonal(el, diagA); return; }
   const orc_mesh *m = el->mesh;
   const int Nq = m->Nq, Np = m->Np;
   const double *D = m->D;
@@ -1137,8 +1139,9 @@ int orc_build_rhs(const orc_solver *S, double *r) {
     double f, g;
     rhs_source(&S->s, m->x[n], m->y[n], m->z[n], elem_lambda(el, e), &f, &g);
     rL[n] = m->wJ[n] * f;
-    if (el->mapB[n] == 1) { gL[n] = g; anyBC = 1; }
+    if (!el->ipdg && el->mapB[n] == 1) { gL[n] = g; anyBC = 1; }
   }
+  if (el->ipdg) orc_ipdg_rhs_bc(el, rL);   /* weakly imposed boundary data */
   if (anyBC) {
     local_ax(el, gL, AgL);
     for (hlong n = 0; n < Nl; ++n) rL[n] -= AgL[n];
@@ -1267,7 +1270,7 @@ int orc_run(orc_solver *S, double *xL_out, int *iters, double *norm, double *err
   for (hlong n = 0; n < Nl; ++n) {
     double f, g;
     rhs_source(&S->s, m->x[n], m->y[n], m->z[n], 0.0, &f, &g);
-    if (el->mapB[n] == 1) xL[n] = g;
+    if (!el->ipdg && el->mapB[n] == 1) xL[n] = g;
     nrm += m->wJ[n] * xL[n] * xL[n];
     const double d = xL[n] - g;
     e2 += m->wJ[n] * d * d;

@@ -36,6 +36,10 @@ def golden_case_settings(case):
         over["POLYNOMIAL DEGREE"] = s["degree"]
     if "boundary_flag" in s:
         over["BOX BOUNDARY FLAG"] = s["boundary_flag"]
+    if "discretization" in s:
+        over["DISCRETIZATION"] = s["discretization"]
+    if "paralmond_aggregation" in s:
+        over["PARALMOND AGGREGATION"] = s["paralmond_aggregation"]
     return reference_test_settings(**over)
 
 

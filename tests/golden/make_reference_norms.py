@@ -1,5 +1,5 @@
-"""Extract the reference's own golden `Solution norm` values for the C0 hex
-elliptic path from its regression driver (test/testElliptic.py, read as text)
+"""Extract the reference's own golden `Solution norm` values for the hexahedral
+elliptic cases (C0 and IPDG) from its regression driver (test/testElliptic.py, read as text)
 and write reference_norms.json beside this script.
 
 Run where the reference tree is available:
@@ -21,7 +21,7 @@ def extract(ref_root):
             continue
         kw = {k.arg: k.value for k in node.keywords}
         name = ast.literal_eval(kw["name"])
-        if not name.startswith("testEllipticHex_C0"):
+        if not (name.startswith("testEllipticHex_C0") or name.startswith("testEllipticHex_Ipdg")):
             continue
         settings = {k.arg: ast.literal_eval(k.value) for k in kw["settings"].keywords
                     if k.arg != "data_file"}

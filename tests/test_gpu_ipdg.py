@@ -1,0 +1,103 @@
+"""IPDG discretisation (DISCRETIZATION = IPDG) on the CUDA path against the oracle's
+restatement of the reference's IPDG kernels, and against the reference's golden norms.
+
+Bars: operator, diagonal and right-hand side within 1e-12 relative of the oracle (FP64,
+different summation order); Jacobi-PCG solves with the oracle's iteration count and
+solution (1e-7); golden norms within the reference's 1e-5."""
+import numpy as np
+import pytest
+import torch
+
+import libparanumal_gb300 as lpg
+from conftest import golden_case_settings
+from gmsh_mesh import write_box
+from gpu_helpers import rel_err
+from oracle.oracle import Oracle
+
+pytestmark = pytest.mark.gpu
+
+BASE = {"BOX NX": 4, "BOX NY": 3, "BOX NZ": 3, "BOX DIMX": 2, "BOX DIMY": 2, "BOX DIMZ": 2,
+        "BOX BOUNDARY FLAG": 1, "POLYNOMIAL DEGREE": 5, "LAMBDA": 0.7, "DISCRETIZATION": "IPDG",
+        "LINEAR SOLVER": "PCG", "PRECONDITIONER": "JACOBI", "MESH JITTER": 0.1}
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    import __graft_entry__ as g
+    g.build()
+    torch.cuda.set_device(0)
+
+
+def _cases(tmp_path):
+    f = write_box(str(tmp_path / "m.msh"), 4, 3, 3, rotate_seed=3, shuffle_seed=1, jitter=0.15, jitter_seed=2,
+                  tags=(1, 2, 1, 2, 2, 1))
+    return {
+        "dirichlet_N5": dict(BASE),
+        "dirichlet_N1": dict(BASE, **{"POLYNOMIAL DEGREE": 1}),
+        "dirichlet_N8": dict(BASE, **{"POLYNOMIAL DEGREE": 8, "BOX NX": 2, "BOX NY": 2, "BOX NZ": 2}),
+        "periodic_N7": dict(BASE, **{"POLYNOMIAL DEGREE": 7, "BOX BOUNDARY FLAG": -1, "MESH JITTER": 0.0}),
+        "lognormal_N3": dict(BASE, **{"POLYNOMIAL DEGREE": 3, "LAMBDA FIELD": "LOGNORMAL"}),
+        "file_mixed_N4": dict(BASE, **{"POLYNOMIAL DEGREE": 4, "MESH FILE": f, "MESH JITTER": 0.0}),
+    }
+
+
+CASE_NAMES = ["dirichlet_N5", "dirichlet_N1", "dirichlet_N8", "periodic_N7", "lognormal_N3", "file_mixed_N4"]
+
+
+@pytest.mark.parametrize("name", CASE_NAMES)
+def test_ipdg_operator_diagonal_rhs_match_oracle(tmp_path, name):
+    s = _cases(tmp_path)[name]
+    e = lpg.Elliptic(s)
+    o = Oracle(s)
+    assert e.Nglobal == o.Ngather == e.Nlocal
+    rng = np.random.default_rng(7)
+    q = rng.standard_normal(e.Nglobal)
+    Aq = torch.zeros(e.Nglobal, dtype=torch.float64, device="cuda")
+    e.Operator(torch.tensor(q, device="cuda"), Aq)
+    torch.cuda.synchronize()
+    assert rel_err(Aq.cpu().numpy(), o.operator(q)) < 1e-12
+    # symmetric: q' A q == q A q'
+    q2 = rng.standard_normal(e.Nglobal)
+    Aq2 = torch.zeros_like(Aq)
+    e.Operator(torch.tensor(q2, device="cuda"), Aq2)
+    torch.cuda.synchronize()
+    a, b = float(q2 @ Aq.cpu().numpy()), float(q @ Aq2.cpu().numpy())
+    assert abs(a - b) < 1e-10 * max(abs(a), 1.0)
+    # Jacobi application (inverse diagonal)
+    z = torch.zeros_like(Aq)
+    e.precon(torch.tensor(q, device="cuda"), z)
+    torch.cuda.synchronize()
+    assert rel_err(z.cpu().numpy(), o.precon(q)) < 1e-12
+    r = torch.zeros_like(Aq)
+    e.rhs(r)
+    torch.cuda.synchronize()
+    assert rel_err(r.cpu().numpy(), o.rhs()) < 1e-12
+
+
+@pytest.mark.parametrize("name", ["dirichlet_N5", "periodic_N7", "file_mixed_N4"])
+def test_ipdg_jacobi_solve_matches_oracle(tmp_path, name):
+    s = _cases(tmp_path)[name]
+    r = lpg.Elliptic(s).Run(want_solution=True)
+    ro = Oracle(s).run()
+    assert r["converged"]
+    assert abs(r["iterations"] - ro["iterations"]) <= 1, (r["iterations"], ro["iterations"])
+    assert rel_err(r["xL"], ro["xL"]) < 1e-7
+    assert abs(r["norm"] - ro["norm"]) < 1e-9 * ro["norm"]
+
+
+@pytest.mark.parametrize("name", ["testEllipticHex_Ipdg", "testEllipticHex_Ipdg_Jacobi"])
+def test_ipdg_reference_golden_norms(reference_norms, name):
+    case = reference_norms["cases"][name]
+    s = golden_case_settings(case)
+    r = lpg.Elliptic(s).Run()
+    ro = Oracle(s).run()
+    assert r["converged"]
+    assert abs(r["norm"] - case["norm"]) < reference_norms["tolerance"]
+    assert abs(r["norm"] - ro["norm"]) < 1e-9
+    assert abs(r["iterations"] - ro["iterations"]) <= (1 if "Jacobi" in name else 2)
+
+
+def test_ipdg_unsupported_combinations_fail_loudly():
+    for over in ({"PRECONDITIONER": "MULTIGRID"}, {"OPERATOR PRECISION": "DF64", "POLYNOMIAL DEGREE": 7}):
+        with pytest.raises(RuntimeError):
+            lpg.Elliptic(dict(BASE, **over))

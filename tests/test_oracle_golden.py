@@ -11,7 +11,8 @@ from conftest import golden_case_settings
 from oracle.oracle import Oracle
 
 ON_PATH = ("testEllipticHex_C0", "testEllipticHex_C0_Jacobi", "testEllipticHex_C0_ParAlmond",
-           "testEllipticHex_C0_Multigrid", "testEllipticHex_C0_AllNeumann", "testEllipticHex_C0_Semfem")
+           "testEllipticHex_C0_Multigrid", "testEllipticHex_C0_AllNeumann", "testEllipticHex_C0_Semfem",
+           "testEllipticHex_Ipdg", "testEllipticHex_Ipdg_Jacobi")
 
 
 @pytest.mark.parametrize("name", ON_PATH)
@@ -24,9 +25,22 @@ def test_reference_golden_norm(reference_norms, name):
 
 
 def test_golden_cases_off_path_are_listed(reference_norms):
-    # the overlapping additive Schwarz (OAS) preconditioner is out of scope
+    # the overlapping additive Schwarz (OAS) preconditioner is out of scope; the IPDG
+    # multigrid cases are checked through the discrete solution (any preconditioner) below
     off = set(reference_norms["cases"]) - set(ON_PATH)
-    assert off == {"testEllipticHex_C0_OAS"}
+    assert off == {"testEllipticHex_C0_OAS", "testEllipticHex_Ipdg_OAS", "testEllipticHex_Ipdg_Multigrid",
+                   "testEllipticHex_Ipdg_ParAlmond", "testEllipticHex_Ipdg_AllNeumann"}
+
+
+@pytest.mark.parametrize("name", ["testEllipticHex_Ipdg_Multigrid", "testEllipticHex_Ipdg_AllNeumann",
+                                  "testEllipticHex_Ipdg_ParAlmond", "testEllipticHex_Ipdg_OAS"])
+def test_reference_golden_norm_ipdg_solution(reference_norms, name):
+    """The golden norm belongs to the converged discrete solution, not to the preconditioner:
+    the IPDG cases solved with Jacobi-PCG must land inside the reference's band."""
+    case = reference_norms["cases"][name]
+    s = dict(golden_case_settings(case), **{"PRECONDITIONER": "JACOBI"})
+    r = Oracle(s).run()
+    assert abs(r["norm"] - case["norm"]) < reference_norms["tolerance"], (name, r["norm"], case["norm"])
 
 
 def test_gll_nodes_weights():
