@@ -155,8 +155,10 @@ int build(lpg_elliptic* h) {
   const std::string pre = S.get("PRECONDITIONER", "NONE");
   if (pre == "NONE") h->precon = make_identity(el);
   else if (pre == "JACOBI") h->precon = make_jacobi(el, &rc);
-  else if (c.ipdg && pre != "NONE" && pre != "JACOBI")
-    return set_error(LPG_ERR_UNSUPPORTED, "IPDG supports PRECONDITIONER NONE and JACOBI");
+  else if (c.ipdg && pre == "SEMFEM")
+    return set_error(LPG_ERR_UNSUPPORTED, "SEMFEM is supported for CONTINUOUS only");
+  else if (c.ipdg && pre != "NONE" && pre != "JACOBI" && S.get("PRECONDITIONER PRECISION", "FP64") != "FP64")
+    return set_error(LPG_ERR_UNSUPPORTED, "IPDG multigrid runs in FP64 (PRECONDITIONER PRECISION FP64)");
   else if (pre == "MULTIGRID" || pre == "PARALMOND" || pre == "SEMFEM") {
     MGOptions o;
     o.amgOnly = (pre == "PARALMOND" || pre == "SEMFEM");

@@ -281,6 +281,7 @@ int Elliptic::setup_ipdg(const MeshConfig& c, int N, const std::vector<double>* 
   if ((rc = hex_traces(*hm, N, mesh.r1d, vP, mP))) return rc;
   hasDirichlet = false;
   for (int b : hm->EToB) hasDirichlet = hasDirichlet || (b == 1);
+  EToE_h = hm->EToE;
   std::vector<int32_t> iota(Nlocal);
   for (int64_t n = 0; n < Nlocal; ++n) iota[n] = (int32_t)n;
   DevBuf<int32_t> mapP;
@@ -594,8 +595,93 @@ int Elliptic::BuildRhs(double* r, cudaStream_t s) {
 // element loop writes every (row, col, val) straight into its row, at a slot fixed by the
 // order of the row's local copies (element order), then each row is stably sorted by
 // column and merged; this sums duplicates in the same order as one global stable sort.
+// IPDG matrix (the matrix of BuildOperatorMatrixIpdgHex3D, ellipticBuildOperatorMatrixIpdg.cpp:
+// 1316-1570) by probing the matrix-free operator: elements get a distance-2 colouring of the
+// face-neighbour graph, so for one colour and one local node n the vector with ones at node
+// n of every element of that colour returns, in each such element and its neighbours,
+// exactly column (e, n) of the matrix. ncolours * Np operator applications; entries with
+// |a| <= 1e-8 are dropped as in the reference.
+int Elliptic::BuildMatrixIpdg(std::vector<int64_t>& rowStarts, std::vector<int32_t>& cols, std::vector<double>& vals,
+                              cudaStream_t s) {
+  const int Np = mesh.Np;
+  const int64_t E = mesh.E;
+  std::vector<int> color(E, -1);
+  int ncolor = 0;
+  {
+    std::vector<int> mark;
+    for (int64_t e = 0; e < E; ++e) {
+      std::vector<int> used;
+      for (int f = 0; f < 6; ++f) {
+        const int64_t a = EToE_h[e * 6 + f];
+        if (a < 0) continue;
+        if (color[a] >= 0) used.push_back(color[a]);
+        for (int g = 0; g < 6; ++g) {
+          const int64_t b = EToE_h[a * 6 + g];
+          if (b >= 0 && color[b] >= 0) used.push_back(color[b]);
+        }
+      }
+      std::sort(used.begin(), used.end());
+      int c = 0;
+      for (int u : used) { if (u == c) ++c; else if (u > c) break; }
+      color[e] = c;
+      ncolor = std::max(ncolor, c + 1);
+    }
+  }
+  std::vector<std::vector<int64_t>> byColor(ncolor);
+  for (int64_t e = 0; e < E; ++e) byColor[color[e]].push_back(e);
+  struct Ent { int32_t col; double val; };
+  std::vector<std::vector<Ent>> rowsE(Nlocal);
+  DevBuf<double> v, Av;
+  int rc;
+  if ((rc = v.alloc(Nlocal)) || (rc = Av.alloc(Nlocal))) return rc;
+  std::vector<double> hv(Nlocal, 0.0), hA(Nlocal);
+  for (int c = 0; c < ncolor; ++c)
+    for (int n = 0; n < Np; ++n) {
+      for (int64_t e : byColor[c]) hv[e * Np + n] = 1.0;
+      if ((rc = v.upload(hv.data(), Nlocal, s)) || (rc = Operator(v.p, Av.p, s)) ||
+          (rc = Av.download(hA.data(), Nlocal, s)))
+        return rc;
+      for (int64_t e : byColor[c]) hv[e * Np + n] = 0.0;
+#pragma omp parallel for schedule(dynamic, 64)
+      for (size_t q = 0; q < byColor[c].size(); ++q) {
+        const int64_t e = byColor[c][q];
+        int64_t targets[7];
+        int nt = 0;
+        targets[nt++] = e;
+        for (int f = 0; f < 6; ++f) {
+          const int64_t a = EToE_h[e * 6 + f];
+          bool seen = (a < 0);
+          for (int t = 0; t < nt && !seen; ++t) seen = (targets[t] == a);
+          if (!seen) targets[nt++] = a;
+        }
+        const int32_t col = (int32_t)(e * Np + n);
+        for (int t = 0; t < nt; ++t)
+          for (int p = 0; p < Np; ++p) {
+            const int64_t row = targets[t] * Np + p;
+            const double a = hA[row];
+            // rows of different elements of this colour never coincide (distance-2 colouring)
+            if (std::fabs(a) > 1e-8) rowsE[row].push_back(Ent{col, a});
+          }
+      }
+    }
+  rowStarts.assign(Nlocal + 1, 0);
+  for (int64_t r = 0; r < Nlocal; ++r) {
+    std::sort(rowsE[r].begin(), rowsE[r].end(), [](const Ent& a, const Ent& b) { return a.col < b.col; });
+    rowStarts[r + 1] = rowStarts[r] + (int64_t)rowsE[r].size();
+  }
+  cols.resize(rowStarts[Nlocal]);
+  vals.resize(rowStarts[Nlocal]);
+  for (int64_t r = 0; r < Nlocal; ++r)
+    for (size_t k = 0; k < rowsE[r].size(); ++k) {
+      cols[rowStarts[r] + k] = rowsE[r][k].col;
+      vals[rowStarts[r] + k] = rowsE[r][k].val;
+    }
+  return LPG_OK;
+}
+
 int Elliptic::BuildMatrix(std::vector<int64_t>& rowStarts, std::vector<int32_t>& cols, std::vector<double>& vals,
                           cudaStream_t s) {
+  if (ipdg) return BuildMatrixIpdg(rowStarts, cols, vals, s);
   const int Nq = mesh.Nq, Np = mesh.Np;
   const int64_t E = mesh.E, Ng = Nglobal;
   std::vector<double> geo(E * 7 * Np);

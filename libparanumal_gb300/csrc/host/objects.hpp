@@ -162,7 +162,10 @@ struct Elliptic {
   DevBuf<double> vgeo, sgeo, g4;
   DevBuf<int32_t> vmapP;
   DevBuf<int> EToB;
+  std::vector<int64_t> EToE_h;     // element neighbours (host), for the matrix probing
   int setup_ipdg(const MeshConfig& c, int N, const std::vector<double>* lamE, cudaStream_t s);
+  int BuildMatrixIpdg(std::vector<int64_t>& rowStarts, std::vector<int32_t>& cols, std::vector<double>& vals,
+                      cudaStream_t s);
   IpdgArgs ipdg_args() const;
 
   int setup(Platform* p, const MeshConfig& c, int N, double lambda, const std::vector<double>* lamE,

@@ -33,6 +33,7 @@ int orc_get_array(const orc_solver *S, const char *name, void *out);
 int orc_operator_apply(const orc_solver *S, const double *q, double *Aq);
 int orc_partial_ax_apply(const orc_solver *S, const double *q, double *AqL);
 int orc_precon_apply(orc_solver *S, const double *r, double *z);
+int orc_matrix_apply(orc_solver *S, const double *x, double *y);
 int orc_gather(const orc_solver *S, const double *qL, double *qG, int trans);
 int orc_scatter_apply(const orc_solver *S, const double *qG, double *qL);
 int orc_build_rhs(const orc_solver *S, double *r);

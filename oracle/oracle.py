@@ -28,7 +28,7 @@ def lib():
         L.orc_info.restype = ctypes.c_longlong
         L.orc_info.argtypes = [vp, ip]
         L.orc_get_array.argtypes = [vp, cp, vp]
-        for f in ("orc_operator_apply", "orc_partial_ax_apply", "orc_precon_apply",
+        for f in ("orc_operator_apply", "orc_partial_ax_apply", "orc_precon_apply", "orc_matrix_apply",
                   "orc_scatter_apply"):
             getattr(L, f).argtypes = [vp, vp, vp]
         L.orc_gather.argtypes = [vp, vp, vp, ip]
@@ -109,6 +109,13 @@ class Oracle:
         q = np.ascontiguousarray(q, dtype=np.float64)
         out = np.zeros(self.Nlocal)
         lib().orc_partial_ax_apply(self.h, _p(q), _p(out))
+        return out
+
+    def matrix_apply(self, x):
+        """A x with the assembled matrix (explicitly built, as the AMG setup does)."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        out = np.zeros(self.Ngather)
+        lib().orc_matrix_apply(self.h, _p(x), _p(out))
         return out
 
     def precon(self, r):

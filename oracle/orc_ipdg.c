@@ -291,3 +291,85 @@ void orc_ipdg_diagonal(const orc_elliptic *el, double *diag) {
     }
   }
 }
+
+/* ---------------------------------------------------------------- assembled matrix
+ * BuildOperatorMatrixIpdgHex3D (ellipticBuildOperatorMatrixIpdg.cpp:1316-1570): for every
+ * element pair (e, e) and (e, face neighbour), the bilinear form of the operator above on
+ * the Lagrange basis, entries with |a| <= 1e-8 dropped; rows and columns are local nodes. */
+static void basis_grad(const orc_mesh *m, int mm, int p, double *br, double *bs, double *bt) {
+  const int Nq = m->Nq;
+  const int mi = mm % Nq, mj = (mm / Nq) % Nq, mk = mm / (Nq * Nq);
+  const int pi = p % Nq, pj = (p / Nq) % Nq, pk = p / (Nq * Nq);
+  *br = (pj == mj && pk == mk) ? m->D[pi * Nq + mi] : 0.0;
+  *bs = (pi == mi && pk == mk) ? m->D[pj * Nq + mj] : 0.0;
+  *bt = (pi == mi && pj == mj) ? m->D[pk * Nq + mk] : 0.0;
+}
+
+/* physical gradient of basis function mm at node p of the element whose vgeo is vg */
+static void phys_grad(const orc_mesh *m, const double *vg, int mm, int p, double *g) {
+  const int Np = m->Np;
+  double br, bs, bt;
+  basis_grad(m, mm, p, &br, &bs, &bt);
+  g[0] = vg[RX * Np + p] * br + vg[SX * Np + p] * bs + vg[TX * Np + p] * bt;
+  g[1] = vg[RY * Np + p] * br + vg[SY * Np + p] * bs + vg[TY * Np + p] * bt;
+  g[2] = vg[RZ * Np + p] * br + vg[SZ * Np + p] * bs + vg[TZ * Np + p] * bt;
+}
+
+hlong orc_ipdg_matrix(const orc_elliptic *el, hlong **rows, hlong **cols, double **vals) {
+  const orc_mesh *m = el->mesh;
+  const int Np = m->Np, Nfp = m->Nfp;
+  const hlong E = m->Nelements;
+  const hlong cap = E * Np * Np * 7;
+  hlong *R = (hlong *)malloc(sizeof(hlong) * cap), *C = (hlong *)malloc(sizeof(hlong) * cap);
+  double *V = (double *)malloc(sizeof(double) * cap);
+  hlong nnz = 0;
+  const double tol = 1e-8;
+  for (hlong e = 0; e < E; ++e) {
+    const double *vg = el->vgeo + e * NVGEO * Np;
+    const double lam = elam(el, e);
+    for (int n = 0; n < Np; ++n)
+      for (int mm = 0; mm < Np; ++mm) {
+        double Anm = 0;
+        for (int p = 0; p < Np; ++p) {
+          double gn[3], gm[3];
+          phys_grad(m, vg, n, p, gn);
+          phys_grad(m, vg, mm, p, gm);
+          Anm += vg[JW * Np + p] * (gn[0] * gm[0] + gn[1] * gm[1] + gn[2] * gm[2]);
+          if (n == p && mm == p) Anm += lam * vg[JW * Np + p];
+        }
+        for (int f = 0; f < 6; ++f) {
+          double AnmP = 0;
+          const hlong eN = m->EToE[e * 6 + f];
+          for (int b = 0; b < Nfp; ++b) {
+            const hlong id = (e * 6 + f) * Nfp + b;
+            const int vidM = m->faceNodes[f * Nfp + b];
+            const hlong vP = m->vmapP[id];
+            const int vidP = (int)(vP % Np);
+            const double *vgP = el->vgeo + (vP / Np) * NVGEO * Np;
+            const double *sg = el->sgeo + id * NSGEO;
+            const double w = sg[WSJ], pen = el->tau * sg[IH];
+            double gnM[3], gmM[3], gmP[3];
+            phys_grad(m, vg, n, vidM, gnM);
+            phys_grad(m, vg, mm, vidM, gmM);
+            phys_grad(m, vgP, mm, vidP, gmP);
+            const double ndnM = sg[NXs] * gnM[0] + sg[NYs] * gnM[1] + sg[NZs] * gnM[2];
+            const double ndmM = sg[NXs] * gmM[0] + sg[NYs] * gmM[1] + sg[NZs] * gmM[2];
+            const double ndmP = sg[NXs] * gmP[0] + sg[NYs] * gmP[1] + sg[NZs] * gmP[2];
+            const double lnM = (n == vidM), lmM = (mm == vidM), lmP = (mm == vidP);
+            Anm += -0.5 * w * lnM * ndmM - 0.5 * w * ndnM * lmM + 0.5 * w * pen * lnM * lmM;
+            if (eN < 0) {
+              const int bc = m->EToB[e * 6 + f];
+              const double qSgn = (bc == 1) ? -1.0 : 1.0, gSgn = (bc == 1) ? 1.0 : -1.0;
+              Anm += -0.5 * gSgn * w * lnM * ndmM + 0.5 * qSgn * w * ndnM * lmM - 0.5 * qSgn * w * pen * lnM * lmM;
+            } else {
+              AnmP += -0.5 * w * lnM * ndmP + 0.5 * w * ndnM * lmP - 0.5 * w * pen * lnM * lmP;
+            }
+          }
+          if (fabs(AnmP) > tol) { R[nnz] = e * Np + n; C[nnz] = eN * Np + mm; V[nnz] = AnmP; ++nnz; }
+        }
+        if (fabs(Anm) > tol) { R[nnz] = e * Np + n; C[nnz] = e * Np + mm; V[nnz] = Anm; ++nnz; }
+      }
+  }
+  *rows = R; *cols = C; *vals = V;
+  return nnz;
+}

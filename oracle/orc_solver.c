@@ -760,6 +760,17 @@ static void vcycle(orc_multigrid *mg, int k, double *RHS, double *X) {
 
 /* assembled continuous stiffness (+ lambda mass) matrix, element threshold 1e-7 */
 static orc_csr build_matrix(const orc_elliptic *el) {
+  if (el->ipdg) {
+    hlong *R, *C;
+    double *V;
+    const hlong n = orc_ipdg_matrix(el, &R, &C, &V);
+    orc_nz *e = (orc_nz *)malloc(sizeof(orc_nz) * (size_t)(n + 1));
+    for (hlong i = 0; i < n; ++i) { e[i].row = R[i]; e[i].col = C[i]; e[i].val = V[i]; }
+    free(R); free(C); free(V);
+    orc_csr A = csr_from_coo(el->ogs.Ngather, el->ogs.Ngather, e, n);
+    free(e);
+    return A;
+  }
   const orc_mesh *m = el->mesh;
   const int Nq = m->Nq, Np = m->Np;
   const double *D = m->D;
@@ -1091,6 +1102,15 @@ int orc_partial_ax_apply(const orc_solver *S, const double *q, double *AqL) {
 
 int orc_precon_apply(orc_solver *S, const double *r, double *z) {
   precon_apply(S, r, z);
+  return 0;
+}
+
+/* y = A x with the assembled matrix of the degree-N problem (the matrix the AMG levels start
+ * from; small cases only) */
+int orc_matrix_apply(orc_solver *S, const double *x, double *y) {
+  orc_csr A = build_matrix(S->el);
+  csr_spmv(&A, 1.0, x, 0.0, y);
+  csr_free(&A);
   return 0;
 }
 

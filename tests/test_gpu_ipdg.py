@@ -97,7 +97,43 @@ def test_ipdg_reference_golden_norms(reference_norms, name):
     assert abs(r["iterations"] - ro["iterations"]) <= (1 if "Jacobi" in name else 2)
 
 
+MG_CASES = {
+    "pmg_5_2_1": {"PRECONDITIONER": "MULTIGRID", "MULTIGRID DEGREES": "5,2,1", "LINEAR SOLVER": "FPCG"},
+    "pmg_halfdofs_N4_lognormal": {"PRECONDITIONER": "MULTIGRID", "POLYNOMIAL DEGREE": 4, "LAMBDA FIELD": "LOGNORMAL"},
+    "paralmond_N2": {"PRECONDITIONER": "PARALMOND", "POLYNOMIAL DEGREE": 2, "PARALMOND AGGREGATION": "UNSMOOTHED",
+                     "BOX NX": 6, "BOX NY": 5, "BOX NZ": 4},
+    "pmg_all_neumann_periodic": {"PRECONDITIONER": "MULTIGRID", "BOX BOUNDARY FLAG": -1, "LAMBDA": 0.0,
+                                 "MESH JITTER": 0.0, "POLYNOMIAL DEGREE": 3},
+}
+
+
+@pytest.mark.parametrize("name", sorted(MG_CASES))
+def test_ipdg_multigrid_matches_oracle(name):
+    """p-multigrid on IPDG levels (element-local transfers, Chebyshev on the IPDG diagonal)
+    with AMG on the degree-1 IPDG matrix; the library builds that matrix by probing its
+    operator, the oracle by the reference's explicit formula."""
+    s = dict(BASE, **MG_CASES[name])
+    r = lpg.Elliptic(s).Run(want_solution=True)
+    ro = Oracle(s).run()
+    assert r["converged"]
+    assert abs(r["iterations"] - ro["iterations"]) <= 1, (r["iterations"], ro["iterations"])
+    assert rel_err(r["xL"], ro["xL"]) < 1e-7
+    jac = Oracle(dict(s, **{"PRECONDITIONER": "JACOBI"})).run()
+    assert r["iterations"] < jac["iterations"]
+
+
+@pytest.mark.parametrize("name", ["testEllipticHex_Ipdg_Multigrid", "testEllipticHex_Ipdg_AllNeumann",
+                                  "testEllipticHex_Ipdg_ParAlmond"])
+def test_ipdg_multigrid_reference_golden_norms(reference_norms, name):
+    case = reference_norms["cases"][name]
+    s = golden_case_settings(case)
+    r = lpg.Elliptic(s).Run()
+    assert r["converged"]
+    assert abs(r["norm"] - case["norm"]) < reference_norms["tolerance"], (r["norm"], case["norm"])
+
+
 def test_ipdg_unsupported_combinations_fail_loudly():
-    for over in ({"PRECONDITIONER": "MULTIGRID"}, {"OPERATOR PRECISION": "DF64", "POLYNOMIAL DEGREE": 7}):
+    for over in ({"PRECONDITIONER": "SEMFEM"}, {"PRECONDITIONER": "MULTIGRID", "PRECONDITIONER PRECISION": "FP32"},
+                 {"OPERATOR PRECISION": "DF64", "POLYNOMIAL DEGREE": 7}):
         with pytest.raises(RuntimeError):
             lpg.Elliptic(dict(BASE, **over))

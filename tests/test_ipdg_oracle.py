@@ -37,3 +37,26 @@ def test_oracle_ipdg_error_converges_like_c0():
         errs.append(r["error"])
         assert r["error"] < 5 * rc["error"] + 1e-7
     assert all(b < 0.2 * a for a, b in zip(errs, errs[1:]))
+
+
+@pytest.mark.parametrize("over", [{"POLYNOMIAL DEGREE": 1}, {"POLYNOMIAL DEGREE": 2, "BOX BOUNDARY FLAG": -1,
+                                                              "MESH JITTER": 0.0, "BOX NX": 3, "BOX NY": 3},
+                                  {"POLYNOMIAL DEGREE": 3, "DISCRETIZATION": "CONTINUOUS"}],
+                         ids=["ipdg_N1", "ipdg_periodic_N2", "c0_N3"])
+def test_oracle_assembled_matrix_equals_operator(over):
+    """The explicitly assembled matrix (BuildOperatorMatrixIpdgHex3D / ...Continuous, the
+    AMG's level 0) and the matrix-free operator are the same linear map (up to the 1e-8
+    entry drop tolerance)."""
+    o = Oracle(dict(BASE, **over))
+    x = np.random.default_rng(3).standard_normal(o.Ngather)
+    Ax, Mx = o.operator(x), o.matrix_apply(x)
+    assert np.abs(Ax - Mx).max() < 1e-7 * np.abs(Ax).max()
+
+
+def test_oracle_ipdg_with_neumann_tags_matrix(tmp_path):
+    from gmsh_mesh import write_box
+    f = write_box(str(tmp_path / "m.msh"), 3, 2, 2, rotate_seed=4, tags=(1, 2, 2, 1, 2, 2))
+    o = Oracle(dict(BASE, **{"MESH FILE": f, "MESH JITTER": 0.0, "POLYNOMIAL DEGREE": 2}))
+    x = np.random.default_rng(5).standard_normal(o.Ngather)
+    Ax, Mx = o.operator(x), o.matrix_apply(x)
+    assert np.abs(Ax - Mx).max() < 1e-7 * np.abs(Ax).max()
