@@ -58,6 +58,7 @@ def parse():
                     help="PRECONDITIONER of --solve")
     ap.add_argument("--learned", action="store_true", help="learned-smoother training and solve comparison")
     ap.add_argument("--mlp", action="store_true", help="learned-smoother MLP inference (lpg_mlp_forward_bf16) timing")
+    ap.add_argument("--ipdg", action="store_true", help="IPDG operator (gradient + Ax) throughput")
     ap.add_argument("--train-nx", type=int, default=32)
     ap.add_argument("--train-samples", type=int, default=20000)
     ap.add_argument("--train-solves", type=int, default=8)
@@ -292,11 +293,11 @@ def run_mlp(a):
     import torch
     import libparanumal_gb300 as lpg
     import __graft_entry__ as g
-    from oracle import mlp
     g.build()
     torch.cuda.set_device(0)
     L = lpg.lib()
-    theta = torch.tensor(mlp.glorot(3).astype(np.float32), device="cuda")
+    gen = torch.Generator(device="cuda").manual_seed(3)
+    theta = (torch.rand(int(L.lpg_mlp_param_count()), device="cuda", generator=gen) - 0.5) * 0.1
     res = {}
     for B in (65536, 262144):
         X = torch.randn(B, 896, device="cuda")
@@ -315,6 +316,48 @@ def run_mlp(a):
     print(json.dumps({"workload": "learned-smoother MLP inference, BF16 tensor cores", "results": res}), flush=True)
 
 
+def run_ipdg(a):
+    """IPDG operator throughput (DISCRETIZATION = IPDG, gradient + interior-penalty Ax) on an
+    nx^3 jittered Dirichlet box at degree N: W warm-up and K timed applications on device
+    vectors larger than L2, CUDA events on the library's stream. One JSON line with the
+    algorithmic bytes of the two kernels per node and the HBM fraction they reach."""
+    import torch
+    import libparanumal_gb300 as lpg
+    import __graft_entry__ as g
+    g.build()
+    torch.cuda.set_device(0)
+    s = dict(settings(a.nx, a.N), **{"DISCRETIZATION": "IPDG", "PRECONDITIONER": "NONE", "MESH JITTER": 0.1})
+    e = lpg.Elliptic(s)
+    n = e.Nglobal
+    gen = torch.Generator(device="cuda").manual_seed(1)
+    q = torch.rand(n, dtype=torch.float64, device="cuda", generator=gen) * 2 - 1
+    Aq = torch.empty_like(q)
+    stream = e.device_ptr("stream")
+    torch_stream = torch.cuda.ExternalStream(stream)
+    for _ in range(max(3, a.warmup)):
+        e.Operator(q, Aq)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(torch_stream)
+    for _ in range(a.steps):
+        e.Operator(q, Aq)
+    e1.record(torch_stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / a.steps
+    Nq = a.N + 1
+    Np, Nfp = Nq ** 3, Nq * Nq
+    face = 6 * Nfp / Np * (5 * 8 + 4 + 32)      # sgeo + vmapP + neighbour gradient per face node
+    grad_bytes = 8 + 80 + 32                     # q, vgeo, gradient out
+    ax_bytes = 32 + 80 + face + 8                # own gradient, vgeo, faces, Aq out
+    hbm, hbm_src = measured_peaks()
+    achieved = n * (grad_bytes + ax_bytes) / (ms * 1e-3) / 1e9
+    print(json.dumps({"workload": "IPDG operator (gradient + Ax), %d^3 jittered hex, N=%d" % (a.nx, a.N),
+                      "metric": "ipdg_operator_gdofs", "value": n / (ms * 1e-3) / 1e9, "unit": "GDOF/s",
+                      "ms_per_apply": ms, "ndofs": n, "bytes_per_dof": grad_bytes + ax_bytes,
+                      "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "peak_source": hbm_src,
+                                   "frac": achieved / hbm, "unit": "GB/s"}}), flush=True)
+
+
 def main():
     a = parse()
     if a.impl == "reference":
@@ -325,6 +368,8 @@ def main():
         return run_learned(a)
     if a.mlp:
         return run_mlp(a)
+    if a.ipdg:
+        return run_ipdg(a)
     import numpy as np
     import torch
     import libparanumal_gb300 as lpg
