@@ -130,8 +130,8 @@ int Elliptic::setup(Platform* p, const MeshConfig& c, int N, double lam, const s
   lambda = lam;
   if (c.ipdg) return setup_ipdg(c, N, lamE, s);
   if (!c.is_box()) return setup_file(c, N, lamE, s);
-  if (c.bcflag != 1 && c.bcflag != -1)
-    return set_error(LPG_ERR_UNSUPPORTED, "BOX BOUNDARY FLAG must be 1 (Dirichlet) or -1 (periodic)");
+  if (c.bcflag != 1 && c.bcflag != -1 && c.bcflag != 2)
+    return set_error(LPG_ERR_UNSUPPORTED, "BOX BOUNDARY FLAG must be 1 (Dirichlet), 2 (Neumann) or -1 (periodic)");
   if (c.bcflag == -1 && (c.nx < 2 || c.ny < 2 || c.nz < 2))
     return set_error(LPG_ERR_UNSUPPORTED, "periodic boxes need at least 2 elements per direction");
   int rc = mesh.setup(c, N, s);
@@ -169,7 +169,36 @@ int Elliptic::setup(Platform* p, const MeshConfig& c, int N, double lam, const s
   if ((rc = multiplicity_to_weight(Nglobal, mult.p, weightG.p, s))) return rc;
 
   hasDirichlet = dirichlet;
+  if (c.bcflag == 2) {
+    // every boundary face node of a Neumann box carries the Neumann data
+    const int Nq = N + 1;
+    std::vector<int32_t> node, mask;
+    for (int64_t e = 0; e < E; ++e) {
+      const int i = (int)(e % c.nx), j = (int)((e / c.nx) % c.ny), k = (int)(e / ((int64_t)c.nx * c.ny));
+      const int fm = (k == 0 ? 1 : 0) | (j == 0 ? 2 : 0) | (i == c.nx - 1 ? 4 : 0) | (j == c.ny - 1 ? 8 : 0) |
+                     (i == 0 ? 16 : 0) | (k == c.nz - 1 ? 32 : 0);
+      if (!fm) continue;
+      for (int n = 0; n < Np; ++n) {
+        const int a = n % Nq, b = (n / Nq) % Nq, d = n / (Nq * Nq);
+        const int on = (d == 0 ? 1 : 0) | (b == 0 ? 2 : 0) | (a == N ? 4 : 0) | (b == N ? 8 : 0) | (a == 0 ? 16 : 0) |
+                       (d == N ? 32 : 0);
+        if (on & fm) { node.push_back((int32_t)(e * Np + n)); mask.push_back(on & fm); }
+      }
+    }
+    if ((rc = set_neumann_nodes(node, mask, s))) return rc;
+  }
   return finish_setup(lamE, s);
+}
+
+int Elliptic::set_neumann_nodes(const std::vector<int32_t>& node, const std::vector<int32_t>& mask, cudaStream_t s) {
+  neuCount = (int64_t)node.size();
+  if (!neuCount) return LPG_OK;
+  int rc;
+  if ((rc = neuNode.alloc(neuCount)) || (rc = neuMask.alloc(neuCount)) ||
+      (rc = neuNode.upload(node.data(), neuCount, s)) || (rc = neuMask.upload(mask.data(), neuCount, s)))
+    return rc;
+  LPG_CUDA_TRY(cudaStreamSynchronize(s));
+  return LPG_OK;
 }
 
 // numbering of a file mesh on the host (union-find over connected face nodes), uploaded
@@ -190,6 +219,26 @@ int Elliptic::setup_file(const MeshConfig& c, int N, const std::vector<double>* 
     return rc;
   if ((rc = multiplicity_to_weight(Nglobal, mult.p, weightG.p, s))) return rc;
   hasDirichlet = num.hasDirichlet;
+  {
+    // boundary face nodes whose node flag is a Neumann type (tag >= 2)
+    const HexMeshData& hm = *c.file;
+    const int Np = mesh.Np, Nq = N + 1;
+    std::vector<int32_t> node, mask;
+    for (int64_t e = 0; e < mesh.E; ++e) {
+      int fm = 0;
+      for (int f = 0; f < 6; ++f)
+        if (hm.EToE[e * 6 + f] < 0) fm |= 1 << f;
+      if (!fm) continue;
+      for (int n = 0; n < Np; ++n) {
+        if (num.flag[e * Np + n] < 2) continue;
+        const int a = n % Nq, b = (n / Nq) % Nq, d = n / (Nq * Nq);
+        const int on = (d == 0 ? 1 : 0) | (b == 0 ? 2 : 0) | (a == N ? 4 : 0) | (b == N ? 8 : 0) | (a == 0 ? 16 : 0) |
+                       (d == N ? 32 : 0);
+        if (on & fm) { node.push_back((int32_t)(e * Np + n)); mask.push_back(on & fm); }
+      }
+    }
+    if ((rc = set_neumann_nodes(node, mask, s))) return rc;
+  }
   return finish_setup(lamE, s);
 }
 
@@ -261,8 +310,8 @@ int Elliptic::setup_semfem(const Elliptic& sem, cudaStream_t s) {
 // unknown; trace maps from the mesh connectivity (box or file), geometric factors on the GPU.
 int Elliptic::setup_ipdg(const MeshConfig& c, int N, const std::vector<double>* lamE, cudaStream_t s) {
   ipdg = true;
-  if (c.is_box() && c.bcflag != 1 && c.bcflag != -1)
-    return set_error(LPG_ERR_UNSUPPORTED, "BOX BOUNDARY FLAG must be 1 (Dirichlet) or -1 (periodic)");
+  if (c.is_box() && c.bcflag != 1 && c.bcflag != -1 && c.bcflag != 2)
+    return set_error(LPG_ERR_UNSUPPORTED, "BOX BOUNDARY FLAG must be 1 (Dirichlet), 2 (Neumann) or -1 (periodic)");
   if (c.is_box() && c.bcflag == -1 && (c.nx < 2 || c.ny < 2 || c.nz < 2))
     return set_error(LPG_ERR_UNSUPPORTED, "periodic boxes need at least 2 elements per direction");
   int rc = mesh.setup(c, N, s);
@@ -567,6 +616,10 @@ int Elliptic::BuildRhs(double* r, cudaStream_t s) {
   RhsSpec spec{rhsKind, (int)(sources.size() / 4), sources_d.p};
   if ((rc = rhs_local(mesh.N, mesh.E, mesh.EX.p, mesh.EY.p, mesh.EZ.p, mesh.r1d_d.p, mesh.geo.p,
                       hasLambdaE ? lambdaE.p : nullptr, lambda, g2l.p, spec, rL.p, gL.p, s)))
+    return rc;
+  if (!ipdg && rhsKind == 0 && neuCount > 0 &&
+      (rc = neumann_flux(mesh.N, neuCount, neuNode.p, neuMask.p, mesh.EX.p, mesh.EY.p, mesh.EZ.p, mesh.r1d_d.p,
+                         mesh.w1d_d.p, rL.p, s)))
     return rc;
   if (ipdg && rhsKind == 0) {
     // weakly imposed boundary data (ellipticRhsBCIpdgHex3D.okl)

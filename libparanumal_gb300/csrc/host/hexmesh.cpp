@@ -403,12 +403,14 @@ int number_hex_nodes(const HexMeshData& m, int N, const std::vector<double>& r1d
       }
     }
   out.g2l.assign(Nlocal, -1);
+  out.flag.assign(Nlocal, 0);
   out.owner.clear();
   out.mult.clear();
   out.hasDirichlet = false;
   std::vector<int32_t> dofOf(Nlocal, -1);
   for (int64_t n = 0; n < Nlocal; ++n) {
     const int32_t root = uf.find((int32_t)n);
+    out.flag[n] = (int8_t)std::min(bc[root], 127);
     if (bc[root] == 1) { out.hasDirichlet = true; continue; }
     if (dofOf[root] < 0) {
       dofOf[root] = (int32_t)out.owner.size();

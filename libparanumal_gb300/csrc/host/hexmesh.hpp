@@ -46,6 +46,7 @@ struct HexNumbering {
   std::vector<int32_t> mult;    // [Nglobal] number of local copies
   int64_t Nglobal = 0;
   bool hasDirichlet = false;
+  std::vector<int8_t> flag;     // [E*Np] smallest positive boundary tag of the node (0 none, capped at 127)
 };
 // numbering of the degree-N nodes (r1d: the N+1 GLL points)
 int number_hex_nodes(const HexMeshData& m, int N, const std::vector<double>& r1d, HexNumbering& out);

@@ -156,6 +156,11 @@ struct Elliptic {
   int rhsKind = 0;                 // 0 sine, 1 Gaussian sources
   std::vector<double> sources;     // nsources*4
   DevBuf<double> sources_d;
+  // Neumann boundary data (CONTINUOUS): local nodes on Neumann-type boundary faces and, per
+  // node, the mask of those faces
+  DevBuf<int32_t> neuNode, neuMask;
+  int64_t neuCount = 0;
+  int set_neumann_nodes(const std::vector<int32_t>& node, const std::vector<int32_t>& mask, cudaStream_t s);
   // IPDG: unknowns are the local nodes (GlobalToLocal is the identity); face data
   bool ipdg = false;
   double tau = 0;

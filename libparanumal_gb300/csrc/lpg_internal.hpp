@@ -69,6 +69,10 @@ struct RhsSpec {
 int rhs_local(int N, int64_t E, const double* EX, const double* EY, const double* EZ,
               const double* r1d, const double* geo, const double* lambdaE, double lambda,
               const int32_t* g2l, RhsSpec spec, double* rL, double* gL, cudaStream_t s);
+// rL[node[t]] -= Neumann data terms of the faces in faceMask[t] (sine data file)
+int neumann_flux(int N, int64_t count, const int32_t* node, const int32_t* faceMask, const double* EX,
+                 const double* EY, const double* EZ, const double* r1d, const double* w1d, double* rL,
+                 cudaStream_t s);
 // Solution norm / error: sum of wJ*xL^2 and wJ*(xL-u)^2 (u manufactured, sine only) into
 // out[0], out[1] (device). xL gets Dirichlet data at masked nodes.
 int solution_norms(int N, int64_t E, const double* EX, const double* EY, const double* EZ,

@@ -258,6 +258,70 @@ __global__ void rhs_kernel(const int Nq, const int64_t Nlocal, const double* __r
   }
 }
 
+// Neumann data of the sine data file at boundary face nodes (ellipticRhsBCHex3D.okl:28-58):
+// rhs -= -WsJ n . grad_B with grad_B = -grad u as the data file states it. One thread per
+// listed local node; faceMask bit f = the node lies on boundary face f of its element.
+// Normals and surface Jacobians from the analytic derivatives of the trilinear map.
+__global__ void neumann_flux_kernel(const int Nq, const int64_t count, const int32_t* __restrict__ node,
+                                    const int32_t* __restrict__ faceMask, const double* __restrict__ EX,
+                                    const double* __restrict__ EY, const double* __restrict__ EZ,
+                                    const double* __restrict__ r1d, const double* __restrict__ w1d,
+                                    double* __restrict__ rL) {
+  const int Np = Nq * Nq * Nq;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < count; t += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t id = node[t];
+    const int64_t e = id / Np;
+    const int n = id % Np;
+    const int i = n % Nq, j = (n / Nq) % Nq, k = n / (Nq * Nq);
+    const double r = r1d[i], s = r1d[j], q = r1d[k];
+    double x, y, z;
+    node_xyz(EX, EY, EZ, e, r, s, q, x, y, z);
+    // d(x,y,z)/d(r,s,t): vertex v at corner (cx, cy, cz) has weight (1 +- r)(1 +- s)(1 +- t)/8
+    double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};   // J[a][c] = d x_a / d r_c
+    const double* V[3] = {EX + e * 8, EY + e * 8, EZ + e * 8};
+    for (int v = 0; v < 8; ++v) {
+      const int cx = (v == 1 || v == 2 || v == 5 || v == 6), cy = (v == 2 || v == 3 || v == 6 || v == 7), cz = (v >= 4);
+      const double fr = cx ? 1 + r : 1 - r, fs = cy ? 1 + s : 1 - s, ft = cz ? 1 + q : 1 - q;
+      const double dr = (cx ? 0.125 : -0.125) * fs * ft, ds = (cy ? 0.125 : -0.125) * fr * ft,
+                   dt = (cz ? 0.125 : -0.125) * fr * fs;
+      for (int a = 0; a < 3; ++a) { J[a][0] += dr * V[a][v]; J[a][1] += ds * V[a][v]; J[a][2] += dt * V[a][v]; }
+    }
+    const double xr = J[0][0], xs = J[0][1], xt = J[0][2], yr = J[1][0], ys = J[1][1], yt = J[1][2];
+    const double zr = J[2][0], zs = J[2][1], zt = J[2][2];
+    const double det = xr * (ys * zt - zs * yt) - yr * (xs * zt - zs * xt) + zr * (xs * yt - ys * xt);
+    const double g[9] = {(ys * zt - zs * yt) / det,  -(xs * zt - zs * xt) / det, (xs * yt - ys * xt) / det,
+                         -(yr * zt - zr * yt) / det, (xr * zt - zr * xt) / det,  -(xr * yt - yr * xt) / det,
+                         (yr * zs - zr * ys) / det,  -(xr * zs - zr * xs) / det, (xr * ys - yr * xs) / det};
+    const double sx = sin(LPG_PI * x), sy = sin(LPG_PI * y), sz = sin(LPG_PI * z);
+    const double ux = LPG_PI * cos(LPG_PI * x) * sy * sz, uy = LPG_PI * sx * cos(LPG_PI * y) * sz,
+                 uz = LPG_PI * sx * sy * cos(LPG_PI * z);
+    double acc = 0;
+    const int mask = faceMask[t];
+    for (int f = 0; f < 6; ++f) {
+      if (!(mask & (1 << f))) continue;
+      const int c0 = (f == 0 || f == 5) ? 6 : (f == 1 || f == 3) ? 3 : 0;
+      const double sg = (f == 0 || f == 1 || f == 4) ? -1.0 : 1.0;
+      const double nx = sg * g[c0], ny = sg * g[c0 + 1], nz = sg * g[c0 + 2];
+      const double len = sqrt(nx * nx + ny * ny + nz * nz);
+      const int b0 = (f == 0 || f == 5) ? i : (f == 1 || f == 3) ? i : j;
+      const int b1 = (f == 0 || f == 5) ? j : k;
+      const double wsJ = len * det * w1d[b0] * w1d[b1];
+      acc += wsJ * (nx * ux + ny * uy + nz * uz) / len;
+    }
+    rL[id] -= acc;
+  }
+}
+
+int neumann_flux(int N, int64_t count, const int32_t* node, const int32_t* faceMask, const double* EX,
+                 const double* EY, const double* EZ, const double* r1d, const double* w1d, double* rL,
+                 cudaStream_t s) {
+  if (count <= 0) return LPG_OK;
+  const int64_t blocks = std::min<int64_t>((count + 255) / 256, 152 * 16);
+  neumann_flux_kernel<<<(unsigned)blocks, 256, 0, s>>>(N + 1, count, node, faceMask, EX, EY, EZ, r1d, w1d, rL);
+  LPG_LAUNCH_CHECK("neumann_flux_kernel");
+  return LPG_OK;
+}
+
 int rhs_local(int N, int64_t E, const double* EX, const double* EY, const double* EZ,
               const double* r1d, const double* geo, const double* lambdaE, double lambda,
               const int32_t* g2l, RhsSpec spec, double* rL, double* gL, cudaStream_t s) {

@@ -166,6 +166,8 @@ void orc_ipdg_operator(const orc_elliptic *el, const double *q, double *Aq);
 void orc_ipdg_diagonal(const orc_elliptic *el, double *diag);
 /* rhs -= boundary terms of the Dirichlet / Neumann data of the manufactured solution */
 void orc_ipdg_rhs_bc(const orc_elliptic *el, double *rhs);
+/* unit outward normal and WsJ at face node b of face f of element e */
+void orc_face_geometry(const orc_mesh *m, hlong e, int f, int b, double *nrm, double *wsJ);
 /* assembled IPDG matrix as COO (malloc'ed arrays), returns the entry count */
 hlong orc_ipdg_matrix(const orc_elliptic *el, hlong **rows, hlong **cols, double **vals);
 

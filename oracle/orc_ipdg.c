@@ -373,3 +373,30 @@ hlong orc_ipdg_matrix(const orc_elliptic *el, hlong **rows, hlong **cols, double
   *rows = R; *cols = C; *vals = V;
   return nnz;
 }
+
+/* unit outward normal and WsJ = sJ w_a w_b at face node b of face f of element e, from the
+ * physical nodes (meshSurfaceGeometricFactorsHex3D.cpp:31-150); shared by the C0 Neumann
+ * boundary terms */
+void orc_face_geometry(const orc_mesh *m, hlong e, int f, int b, double *nrm, double *wsJ) {
+  const int Nq = m->Nq, Np = m->Np;
+  const int n = m->faceNodes[f * m->Nfp + b];
+  const int i = n % Nq, j = (n / Nq) % Nq, k = n / (Nq * Nq);
+  const double *x = m->x + e * Np, *y = m->y + e * Np, *z = m->z + e * Np, *D = m->D;
+  double xr = 0, xs = 0, xt = 0, yr = 0, ys = 0, yt = 0, zr = 0, zs = 0, zt = 0;
+  for (int q = 0; q < Nq; ++q) {
+    const int ir = q + j * Nq + k * Nq * Nq, is = i + q * Nq + k * Nq * Nq, it = i + j * Nq + q * Nq * Nq;
+    xr += D[i * Nq + q] * x[ir]; yr += D[i * Nq + q] * y[ir]; zr += D[i * Nq + q] * z[ir];
+    xs += D[j * Nq + q] * x[is]; ys += D[j * Nq + q] * y[is]; zs += D[j * Nq + q] * z[is];
+    xt += D[k * Nq + q] * x[it]; yt += D[k * Nq + q] * y[it]; zt += D[k * Nq + q] * z[it];
+  }
+  const double J = xr * (ys * zt - zs * yt) - yr * (xs * zt - zs * xt) + zr * (xs * yt - ys * xt);
+  double g[9] = {(ys * zt - zs * yt) / J,  -(xs * zt - zs * xt) / J, (xs * yt - ys * xt) / J,
+                 -(yr * zt - zr * yt) / J, (xr * zt - zr * xt) / J,  -(xr * yt - yr * xt) / J,
+                 (yr * zs - zr * ys) / J,  -(xr * zs - zr * xs) / J, (xr * ys - yr * xs) / J};
+  const int c0 = (f == 0 || f == 5) ? 6 : (f == 1 || f == 3) ? 3 : 0;
+  const double sg = (f == 0 || f == 1 || f == 4) ? -1.0 : 1.0;
+  const double nx = sg * g[c0], ny = sg * g[c0 + 1], nz = sg * g[c0 + 2];
+  const double len = sqrt(nx * nx + ny * ny + nz * nz);
+  nrm[0] = nx / len; nrm[1] = ny / len; nrm[2] = nz / len;
+  *wsJ = len * J * m->gllw[b % Nq] * m->gllw[b / Nq];
+}

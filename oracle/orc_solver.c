@@ -1162,6 +1162,25 @@ int orc_build_rhs(const orc_solver *S, double *r) {
     if (!el->ipdg && el->mapB[n] == 1) { gL[n] = g; anyBC = 1; }
   }
   if (el->ipdg) orc_ipdg_rhs_bc(el, rL);   /* weakly imposed boundary data */
+  if (!el->ipdg && S->s.rhs == ORC_RHS_SINE) {
+    /* Neumann data of the data file at every face node whose node flag is a Neumann type
+     * (ellipticRhsBCHex3D.okl:28-58: rhs -= -WsJ n . grad_B with grad_B = -grad u, as the
+     * data file states it); contributions of faces inside the domain cancel in the gather */
+    const int Nfp = m->Nfp;
+    for (hlong e = 0; e < m->Nelements; ++e)
+      for (int f = 0; f < 6; ++f)
+        for (int b = 0; b < Nfp; ++b) {
+          const hlong id = e * Np + m->faceNodes[f * Nfp + b];
+          if (el->mapB[id] < 2) continue;
+          double nrm[3], w;
+          orc_face_geometry(m, e, f, b, nrm, &w);
+          const double x = m->x[id], y = m->y[id], z = m->z[id];
+          const double ux = -ORC_PI * cos(ORC_PI * x) * sin(ORC_PI * y) * sin(ORC_PI * z);
+          const double uy = -ORC_PI * sin(ORC_PI * x) * cos(ORC_PI * y) * sin(ORC_PI * z);
+          const double uz = -ORC_PI * sin(ORC_PI * x) * sin(ORC_PI * y) * cos(ORC_PI * z);
+          rL[id] -= -w * (nrm[0] * ux + nrm[1] * uy + nrm[2] * uz);
+        }
+  }
   if (anyBC) {
     local_ax(el, gL, AgL);
     for (hlong n = 0; n < Nl; ++n) rL[n] -= AgL[n];

@@ -77,3 +77,15 @@ def test_bad_mesh_files_are_rejected(tmp_path):
         lpg.hex_mesh_info(str(p))
     with pytest.raises(RuntimeError):
         lpg.hex_mesh_info(str(tmp_path / "missing.msh"))
+
+
+@pytest.mark.parametrize("disc", ["CONTINUOUS", "IPDG"])
+def test_oracle_neumann_box_equals_neumann_tagged_file(tmp_path, disc):
+    """BOX BOUNDARY FLAG 2 (every face Neumann) and the same box as a file with every
+    boundary face tagged 2 give the same discrete solution, Neumann data included."""
+    s = dict(BASE, **{"BOX BOUNDARY FLAG": 2, "LAMBDA": 1.0, "DISCRETIZATION": disc})
+    f = write_box(str(tmp_path / "m.msh"), 3, 3, 2, rotate_seed=6, tags=(2, 2, 2, 2, 2, 2))
+    rb = Oracle(s).run()
+    rf = Oracle(dict(s, **{"MESH FILE": f})).run()
+    assert abs(rf["norm"] - rb["norm"]) < 1e-11 * rb["norm"]
+    assert abs(rf["iterations"] - rb["iterations"]) <= 1

@@ -59,6 +59,37 @@ def test_file_mesh_solve_matches_oracle(tmp_path, name):
     assert rel_err(r["xL"], ro["xL"]) < 1e-7
 
 
+@pytest.mark.parametrize("over", [{"BOX BOUNDARY FLAG": 2, "LAMBDA": 1.0},
+                                  {"BOX BOUNDARY FLAG": 2, "LAMBDA": 0.0, "PRECONDITIONER": "MULTIGRID",
+                                   "LINEAR SOLVER": "FPCG"},
+                                  {"BOX BOUNDARY FLAG": 2, "LAMBDA": 1.0, "DISCRETIZATION": "IPDG"}],
+                         ids=["c0_neumann_box", "c0_all_neumann_pmg", "ipdg_neumann_box"])
+def test_neumann_box_matches_oracle(over):
+    """BOX BOUNDARY FLAG 2: Neumann faces with the data file's Neumann data in the rhs."""
+    s = dict(BASE, **over)
+    e = lpg.Elliptic(s)
+    o = Oracle(s)
+    r = torch.zeros(e.Nglobal, dtype=torch.float64, device="cuda")
+    e.rhs(r)
+    torch.cuda.synchronize()
+    assert rel_err(r.cpu().numpy(), o.rhs()) < 1e-12
+    res = e.Run(want_solution=True)
+    ro = o.run()
+    assert res["converged"]
+    assert abs(res["iterations"] - ro["iterations"]) <= 1
+    assert rel_err(res["xL"], ro["xL"]) < 1e-7
+
+
+def test_neumann_tagged_file_rhs_matches_oracle(tmp_path):
+    s = dict(BASE, **{"MESH FILE": mesh(tmp_path, rotate_seed=5, jitter=0.1, jitter_seed=2, tags=(1, 2, 2, 1, 3, 2)),
+                      "LAMBDA": 1.0})
+    e = lpg.Elliptic(s)
+    r = torch.zeros(e.Nglobal, dtype=torch.float64, device="cuda")
+    e.rhs(r)
+    torch.cuda.synchronize()
+    assert rel_err(r.cpu().numpy(), Oracle(s).rhs()) < 1e-12
+
+
 def test_file_mesh_equals_box_on_gpu(tmp_path):
     s = dict(BASE, **{"PRECONDITIONER": "MULTIGRID", "LINEAR SOLVER": "FPCG"})
     rb = lpg.Elliptic(s).Run()
