@@ -159,7 +159,7 @@ int build(lpg_elliptic* h) {
     return set_error(LPG_ERR_UNSUPPORTED, "SEMFEM is supported for CONTINUOUS only");
   else if (c.ipdg && pre != "NONE" && pre != "JACOBI" && S.get("PRECONDITIONER PRECISION", "FP64") != "FP64")
     return set_error(LPG_ERR_UNSUPPORTED, "IPDG multigrid runs in FP64 (PRECONDITIONER PRECISION FP64)");
-  else if (pre == "MULTIGRID" || pre == "PARALMOND" || pre == "SEMFEM") {
+  else if (pre == "MULTIGRID" || pre == "PARALMOND" || pre == "SEMFEM" || pre == "OAS") {
     MGOptions o;
     o.amgOnly = (pre == "PARALMOND" || pre == "SEMFEM");
     o.semfem = (pre == "SEMFEM");
@@ -180,9 +180,10 @@ int build(lpg_elliptic* h) {
       return set_error(LPG_ERR_SETTINGS, "LEARNED SMOOTHER STEPS must be 1..8");
     if (S.get("PARALMOND CYCLE", "VCYCLE") != "VCYCLE")
       return set_error(LPG_ERR_UNSUPPORTED, "PARALMOND CYCLE must be VCYCLE");
-    h->precon = make_multigrid(el, c, o, &rc);
+    h->precon = (pre == "OAS") ? make_oas(el, c, o, &rc) : make_multigrid(el, c, o, &rc);
   } else {
-    return set_error(LPG_ERR_UNSUPPORTED, "PRECONDITIONER must be NONE, JACOBI, MULTIGRID or PARALMOND");
+    return set_error(LPG_ERR_UNSUPPORTED,
+                     "PRECONDITIONER must be NONE, JACOBI, MULTIGRID, PARALMOND, SEMFEM or OAS");
   }
   if (rc) return rc;
   if (!h->precon) return set_error(LPG_ERR_INVALID, "preconditioner setup failed");
@@ -660,7 +661,8 @@ extern "C" int lpg_smoother_train(const char* settings, int nsolves, int samples
   int rc = lpg_elliptic_create(settings, &e);
   if (rc) return rc;
   std::unique_ptr<lpg_elliptic> owner(e);
-  if (e->precon->levels_p() < 1) return set_error(LPG_ERR_INVALID, "smoother train: PRECONDITIONER must be MULTIGRID");
+  if (e->precon->levels_p() < 1 || e->settings.get("PRECONDITIONER", "") != "MULTIGRID")
+    return set_error(LPG_ERR_INVALID, "smoother train: PRECONDITIONER must be MULTIGRID");
   const MeshConfig& c = e->mcfg;
   if (!c.is_box()) return set_error(LPG_ERR_UNSUPPORTED, "smoother training needs MESH FILE = BOX");
   BoxNumbering b{c.nx, c.ny, c.nz, e->el->mesh.N, c.bcflag == -1 ? 1 : 0, c.bcflag == 1 ? 1 : 0};

@@ -492,6 +492,7 @@ class MultiGrid : public Precon {
 
   int setup(Elliptic* el, const MeshConfig& c, const MGOptions& o);
   int apply(const double* r, double* z, cudaStream_t s) override;
+  uint64_t rngAfter = 0;   // state of the random stream when setup finished
 
  private:
   bool f32() const { return opt.prec != Prec::F64; }
@@ -816,7 +817,13 @@ int MultiGrid::setup(Elliptic* el, const MeshConfig& c, const MGOptions& o) {
   cudaStream_t s = plat->stream;
   Rand48 rng;
   rng.seed(0);  // srand48(rank) in buildParAlmondKernels (parAlmondKernels.cpp:55-58)
+  if (o.rngGiven) rng.x = o.rngState;
   int rc;
+  struct SaveRng {
+    uint64_t& out;
+    Rand48& r;
+    ~SaveRng() { out = r.x; }
+  } saveRng{rngAfter, rng};
   if (o.amgOnly) {
     if (o.semfem) {
       // SEMFEMPrecon (ellipticPreconSEMFEM.cpp:56-247, hexahedra): parAlmond on the
@@ -932,6 +939,82 @@ std::unique_ptr<Precon> make_multigrid(Elliptic* el, const MeshConfig& c, const 
   *status = mg->setup(el, c, o);
   if (*status) return nullptr;
   return mg;
+}
+
+// ================================================================ OAS
+// OASPrecon (ellipticPreconOAS.cpp:30-223) on one rank: the one-ring patch is the whole
+// mesh, so the patch solve is this problem's p-multigrid V-cycle; the coarse problem is the
+// degree-1 problem with its own AMG (set up after the patch hierarchy on the same random
+// stream), reached by a direct N -> 1 transfer and added to the patch solution.
+class OASPrecon : public Precon {
+ public:
+  Elliptic* el = nullptr;
+  std::unique_ptr<MultiGrid> patch;
+  std::unique_ptr<Elliptic> elC;
+  std::unique_ptr<MultiGrid> coarse;
+  DevBuf<double> P64, rC, zC;
+
+  int levels_p() const override { return patch ? patch->levels_p() : 0; }
+  int levels_amg() const override { return coarse ? coarse->levels_amg() : 0; }
+  int64_t coarse_n() const override { return coarse ? coarse->coarse_n() : 0; }
+
+  int setup(Elliptic* e, const MeshConfig& c, const MGOptions& o) {
+    el = e;
+    cudaStream_t s = e->plat->stream;
+    const int N = e->mesh.N;
+    int rc;
+    MGOptions oc = o;
+    oc.amgOnly = true;
+    oc.semfem = false;
+    oc.prec = Prec::F64;
+    if (N > 1) {
+      patch = std::make_unique<MultiGrid>();
+      MGOptions op = o;
+      op.amgOnly = false;
+      op.semfem = false;
+      if ((rc = patch->setup(e, c, op))) return rc;
+      oc.rngGiven = true;
+      oc.rngState = patch->rngAfter;
+      elC = std::make_unique<Elliptic>();
+      if ((rc = elC->setup(e->plat, c, 1, e->lambda, e->hasLambdaE ? &e->lambdaE_h : nullptr, s))) return rc;
+      coarse = std::make_unique<MultiGrid>();
+      if ((rc = coarse->setup(elC.get(), c, oc))) return rc;
+      std::vector<double> P;
+      gll_interpolation(1, N, P);
+      if ((rc = P64.alloc((int64_t)P.size())) || (rc = P64.upload(P.data(), (int64_t)P.size(), s))) return rc;
+      if ((rc = rC.alloc(elC->Nglobal)) || (rc = zC.alloc(elC->Nglobal))) return rc;
+    } else {
+      coarse = std::make_unique<MultiGrid>();
+      if ((rc = coarse->setup(e, c, oc))) return rc;
+    }
+    LPG_CUDA_TRY(cudaStreamSynchronize(s));
+    return LPG_OK;
+  }
+
+  int apply(const double* r, double* z, cudaStream_t s) override {
+    if (!patch) return coarse->apply(r, z, s);
+    int rc;
+    const int N = el->mesh.N;
+    const int64_t E = el->mesh.E;
+    if ((rc = patch->apply(r, z, s))) return rc;
+    if ((rc = pmg_coarsen<double>(N, 1, E, el->g2l.p, el->weightG.p, r, P64.p, elC->g2l.p, rC.p, elC->Nglobal, s)))
+      return rc;
+    if ((rc = coarse->apply(rC.p, zC.p, s))) return rc;
+    if ((rc = pmg_prolongate_map<double>(N, 1, E, elC->g2l.p, zC.p, P64.p, el->g2l.p, el->owner.p, z, s))) return rc;
+    if (el->allNeumann) {
+      Platform* plat = el->plat;
+      if ((rc = sum(el->Nglobal, z, plat->scalars.p + 1, plat->partials.p, s))) return rc;
+      rc = add_scalar(el->Nglobal, plat->scalars.p + 1, -el->allNeumannScale * el->allNeumannScale, z, s);
+    }
+    return rc;
+  }
+};
+
+std::unique_ptr<Precon> make_oas(Elliptic* el, const MeshConfig& c, const MGOptions& o, int* status) {
+  auto p = std::make_unique<OASPrecon>();
+  *status = p->setup(el, c, o);
+  if (*status) return nullptr;
+  return p;
 }
 
 // ================================================================ Identity / Jacobi

@@ -234,9 +234,16 @@ struct MGOptions {
   bool amgRugeStuben = false;
   bool amgOnly = false;           // PARALMOND: AMG on the fine matrix
   bool semfem = false;            // SEMFEM: AMG on the low-order matrix of the GLL sub-mesh
+  // random stream of the setup: a fresh srand48(0) unless a state is handed over (OAS builds
+  // its coarse AMG after the patch hierarchy on one stream)
+  bool rngGiven = false;
+  uint64_t rngState = 0;
   int learnedSteps = 2;           // learned smoothing steps before and after the coarse correction
 };
 std::unique_ptr<Precon> make_multigrid(Elliptic* el, const MeshConfig& c, const MGOptions& o, int* status);
+// OAS (ellipticPreconOAS.cpp) on one rank: p-multigrid of the problem plus an additive
+// degree-1 AMG correction
+std::unique_ptr<Precon> make_oas(Elliptic* el, const MeshConfig& c, const MGOptions& o, int* status);
 
 // ---------------------------------------------------------------- linear solver
 struct PCGResult {

@@ -84,7 +84,7 @@ static int set_key(orc_settings *s, const char *key, const char *val) {
   else if (IS("RHS SOURCES")) s->nsources = atoi(val);
   else if (IS("LINEAR SOLVER")) s->solver = V("NBFPCG") ? ORC_NBFPCG : V("FPCG") ? ORC_FPCG : ORC_PCG;
   else if (IS("LINEAR SOLVER STOPPING CRITERION")) s->stop_rhs = V("ABS/REL-RHS-2NORM");
-  else if (IS("PRECONDITIONER")) s->precon = V("JACOBI") ? ORC_PRE_JACOBI : V("MULTIGRID") ? ORC_PRE_MULTIGRID : V("PARALMOND") ? ORC_PRE_PARALMOND : V("SEMFEM") ? ORC_PRE_SEMFEM : ORC_PRE_NONE;
+  else if (IS("PRECONDITIONER")) s->precon = V("JACOBI") ? ORC_PRE_JACOBI : V("MULTIGRID") ? ORC_PRE_MULTIGRID : V("PARALMOND") ? ORC_PRE_PARALMOND : V("SEMFEM") ? ORC_PRE_SEMFEM : V("OAS") ? ORC_PRE_OAS : ORC_PRE_NONE;
   else if (IS("MULTIGRID COARSENING")) s->mg_coarsening = V("ALLDEGREES") ? ORC_MG_ALLDEGREES : V("HALFDEGREES") ? ORC_MG_HALFDEGREES : ORC_MG_HALFDOFS;
   else if (IS("MULTIGRID DEGREES")) { s->mg_ndeg = parse_list(val, s->mg_degrees, 16); if (s->mg_ndeg > 0) s->mg_coarsening = ORC_MG_LIST; }
   else if (IS("MULTIGRID SMOOTHER")) s->mg_smoother = V("DAMPEDJACOBI") ? ORC_SMOOTH_JACOBI : ORC_SMOOTH_CHEBYSHEV;

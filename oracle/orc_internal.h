@@ -22,7 +22,8 @@ typedef long long hlong;
 
 /* ---------------- settings (subset of the reference's .rc keys) ---------------- */
 enum { ORC_PCG = 0, ORC_FPCG = 1, ORC_NBFPCG = 2 };
-enum { ORC_PRE_NONE = 0, ORC_PRE_JACOBI = 1, ORC_PRE_MULTIGRID = 2, ORC_PRE_PARALMOND = 3, ORC_PRE_SEMFEM = 4 };
+enum { ORC_PRE_NONE = 0, ORC_PRE_JACOBI = 1, ORC_PRE_MULTIGRID = 2, ORC_PRE_PARALMOND = 3, ORC_PRE_SEMFEM = 4,
+       ORC_PRE_OAS = 5 };
 enum { ORC_MG_HALFDOFS = 0, ORC_MG_HALFDEGREES = 1, ORC_MG_ALLDEGREES = 2, ORC_MG_LIST = 3 };
 enum { ORC_SMOOTH_CHEBYSHEV = 0, ORC_SMOOTH_JACOBI = 1 };
 enum { ORC_RHS_SINE = 0, ORC_RHS_GAUSSIAN_SOURCES = 1, ORC_RHS_BUMPS = 2 };

@@ -930,8 +930,13 @@ struct orc_solver {
   orc_elliptic *el;
   double *lambdaE;
   double *invDiag;        /* Jacobi */
-  orc_multigrid *mg;      /* MULTIGRID or PARALMOND */
+  orc_multigrid *mg;      /* MULTIGRID, PARALMOND, SEMFEM, or the patch hierarchy of OAS */
   orc_rand48 rng;
+  /* OAS: degree-1 problem, its AMG, and the direct transfer N -> 1 */
+  orc_elliptic *elC;
+  orc_multigrid *mgC;
+  orc_pmg_level oasL;
+  double *oasRC, *oasZC;
   double last_norm, last_err;
   int last_iters;
 };
@@ -988,6 +993,18 @@ static void precon_apply(orc_solver *S, const double *r, double *z) {
   else if (S->s.precon == ORC_PRE_MULTIGRID || S->s.precon == ORC_PRE_PARALMOND || S->s.precon == ORC_PRE_SEMFEM) {
     /* level 0 rhs/x are the caller's buffers */
     vcycle(S->mg, 0, (double *)r, z);
+  } else if (S->s.precon == ORC_PRE_OAS) {
+    if (S->s.N > 1) {
+      /* patch solve (MultiGridPrecon::Operator, with its zero mean), then the additive
+       * degree-1 correction prolongated onto it (ellipticPreconOAS.cpp:33-100) */
+      vcycle(S->mg, 0, (double *)r, z);
+      if (S->el->allNeumann) zero_mean(S->el, z);
+      pmg_coarsen(S->mg, &S->oasL, r, S->oasRC);
+      vcycle(S->mgC, 0, S->oasRC, S->oasZC);
+      pmg_prolongate(S->mg, &S->oasL, S->oasZC, z);
+    } else {
+      vcycle(S->mgC, 0, (double *)r, z);
+    }
   } else memcpy(z, r, sizeof(double) * N);
   if (S->el->allNeumann && S->s.precon != ORC_PRE_NONE) zero_mean(S->el, z);
 }
@@ -1029,6 +1046,28 @@ orc_solver *orc_create(const char *settings_text, int *status) {
     free(d);
   } else if (S->s.precon == ORC_PRE_MULTIGRID || S->s.precon == ORC_PRE_PARALMOND || S->s.precon == ORC_PRE_SEMFEM) {
     S->mg = build_multigrid(S);
+  } else if (S->s.precon == ORC_PRE_OAS) {
+    /* OASPrecon (ellipticPreconOAS.cpp:105-223) on one rank: the one-ring patch is the whole
+     * mesh, so the patch preconditioner is the p-multigrid of the problem itself; the coarse
+     * problem is the degree-1 problem with its own parAlmond AMG, whose setup continues the
+     * random stream after the patch hierarchy (srand48 is seeded once per process). */
+    if (S->s.N > 1) S->mg = build_multigrid(S);
+    else orc_srand48(&S->rng, 0);
+    S->elC = orc_elliptic_build(&S->s, 1, S->lambdaE);
+    S->mgC = (orc_multigrid *)calloc(1, sizeof(orc_multigrid));
+    amg_setup(S->mgC, S->elC, &S->s, &S->rng);
+    mg_alloc_work(S->mgC);
+    if (S->s.N > 1) {
+      orc_pmg_level *L = &S->oasL;
+      L->el = S->el; L->elC = S->elC; L->Nf = S->s.N; L->Nc = 1;
+      double rc1[2], rf[16];
+      orc_jacobiGLL(1, rc1, NULL);
+      orc_jacobiGLL(S->s.N, rf, NULL);
+      L->P = dalloc((S->s.N + 1) * 2);
+      orc_interp1D(1, rc1, S->s.N + 1, rf, L->P);
+      S->oasRC = dalloc(S->elC->ogs.Ngather);
+      S->oasZC = dalloc(S->elC->ogs.Ngather);
+    }
   }
   return S;
 }
@@ -1036,6 +1075,9 @@ orc_solver *orc_create(const char *settings_text, int *status) {
 void orc_destroy(orc_solver *S) {
   if (!S) return;
   if (S->mg) mg_free(S->mg);
+  if (S->mgC) mg_free(S->mgC);
+  orc_elliptic_free(S->elC);
+  free(S->oasL.P); free(S->oasRC); free(S->oasZC);
   orc_elliptic_free(S->el);
   free(S->invDiag);
   free(S->lambdaE);

@@ -123,7 +123,7 @@ def test_ipdg_multigrid_matches_oracle(name):
 
 
 @pytest.mark.parametrize("name", ["testEllipticHex_Ipdg_Multigrid", "testEllipticHex_Ipdg_AllNeumann",
-                                  "testEllipticHex_Ipdg_ParAlmond"])
+                                  "testEllipticHex_Ipdg_ParAlmond", "testEllipticHex_Ipdg_OAS"])
 def test_ipdg_multigrid_reference_golden_norms(reference_norms, name):
     case = reference_norms["cases"][name]
     s = golden_case_settings(case)

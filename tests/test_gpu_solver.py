@@ -17,7 +17,8 @@ from oracle.oracle import Oracle
 pytestmark = pytest.mark.gpu
 
 GOLDEN = ("testEllipticHex_C0", "testEllipticHex_C0_Jacobi", "testEllipticHex_C0_ParAlmond",
-          "testEllipticHex_C0_Multigrid", "testEllipticHex_C0_AllNeumann", "testEllipticHex_C0_Semfem")
+          "testEllipticHex_C0_Multigrid", "testEllipticHex_C0_AllNeumann", "testEllipticHex_C0_Semfem",
+          "testEllipticHex_C0_OAS")
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -36,7 +37,7 @@ def test_reference_golden_norms(reference_norms, name):
     assert r["converged"]
     assert abs(r["norm"] - case["norm"]) < reference_norms["tolerance"], (r["norm"], case["norm"])
     assert abs(r["norm"] - ro["norm"]) < 1e-9
-    amg = "ParAlmond" in name or "Semfem" in name
+    amg = "ParAlmond" in name or "Semfem" in name or "OAS" in name
     assert abs(r["iterations"] - ro["iterations"]) <= (1 if amg else 0), \
         (r["iterations"], ro["iterations"])
 
@@ -135,6 +136,28 @@ def test_semfem_preconditioner_matches_oracle(over):
     o = Oracle(s)
     rng = np.random.default_rng(5)
     rh = rng.standard_normal(e.Nglobal)
+    z = torch.zeros(e.Nglobal, dtype=torch.float64, device="cuda")
+    e.precon(torch.tensor(rh, device="cuda"), z)
+    torch.cuda.synchronize()
+    assert rel_err(z.cpu().numpy(), o.precon(rh)) < 1e-9
+
+
+@pytest.mark.parametrize("over", [{}, {"DISCRETIZATION": "IPDG"}, {"POLYNOMIAL DEGREE": 1},
+                                  {"LAMBDA": 0.0, "BOX BOUNDARY FLAG": -1, "MESH JITTER": 0.0, "BOX NX": 4}],
+                         ids=["c0", "ipdg", "c0_N1", "c0_all_neumann"])
+def test_oas_preconditioner_matches_oracle(over):
+    """OAS (ellipticPreconOAS.cpp) on one rank: p-multigrid of the whole mesh plus an additive
+    degree-1 AMG correction."""
+    s = dict(config1(), **{"BOX NX": 5, "BOX NY": 4, "BOX NZ": 3, "POLYNOMIAL DEGREE": 4, "MESH JITTER": 0.1,
+                           "LAMBDA": 1.0, "LINEAR SOLVER": "PCG", "PRECONDITIONER": "OAS"})
+    s.update(over)
+    r = lpg.Elliptic(s).Run(want_solution=True)
+    ro = Oracle(s).run()
+    assert r["converged"]
+    assert abs(r["iterations"] - ro["iterations"]) <= 1, (r["iterations"], ro["iterations"])
+    assert rel_err(r["xL"], ro["xL"]) < 1e-7
+    e, o = lpg.Elliptic(s), Oracle(s)
+    rh = np.random.default_rng(9).standard_normal(e.Nglobal)
     z = torch.zeros(e.Nglobal, dtype=torch.float64, device="cuda")
     e.precon(torch.tensor(rh, device="cuda"), z)
     torch.cuda.synchronize()
