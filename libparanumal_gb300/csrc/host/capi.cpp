@@ -155,6 +155,9 @@ int build(lpg_elliptic* h) {
   const std::string pre = S.get("PRECONDITIONER", "NONE");
   if (pre == "NONE") h->precon = make_identity(el);
   else if (pre == "JACOBI") h->precon = make_jacobi(el, &rc);
+  else if (pre == "MASSMATRIX")   // MassMatrixPrecon refuses hexahedra (ellipticPreconMassMatrix.cpp:34-35)
+    return set_error(LPG_ERR_UNSUPPORTED, "MASSMATRIX preconditioner is only available for triangle and "
+                                          "tetrahedra elements. Use JACOBI instead.");
   else if (c.ipdg && pre == "SEMFEM")
     return set_error(LPG_ERR_UNSUPPORTED, "SEMFEM is supported for CONTINUOUS only");
   else if (c.ipdg && pre != "NONE" && pre != "JACOBI" && S.get("PRECONDITIONER PRECISION", "FP64") != "FP64")

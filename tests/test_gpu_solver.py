@@ -164,6 +164,11 @@ def test_oas_preconditioner_matches_oracle(over):
     assert rel_err(z.cpu().numpy(), o.precon(rh)) < 1e-9
 
 
+def test_massmatrix_preconditioner_refused_for_hexahedra():
+    with pytest.raises(RuntimeError, match="MASSMATRIX"):
+        lpg.Elliptic(config1(**{"PRECONDITIONER": "MASSMATRIX", "LAMBDA": 1.0}))
+
+
 def test_lognormal_lambda_and_gaussian_sources_solve():
     s = dict(MG, **{"LAMBDA FIELD": "LOGNORMAL", "LAMBDA SEED": 2, "RHS FIELD": "GAUSSIAN SOURCES",
                     "RHS SEED": 3, "RHS SOURCES": 16})
