@@ -193,7 +193,7 @@ __device__ __forceinline__ float row_dot(const float* __restrict__ row, const fl
   return acc;
 }
 
-template <int NQ, typename T, typename G, int EPB, int STAGES>
+template <int NQ, typename T, typename G, int EPB, int STAGES, bool PF = false>
 __global__ void __launch_bounds__(NQ * NQ * EPB)
 ax_hex_staged_kernel(const int64_t Nelements, const int32_t* __restrict__ elementList,
                      const int32_t* __restrict__ g2l, const G* __restrict__ ggeo, const int64_t geoStride,
@@ -260,12 +260,38 @@ ax_hex_staged_kernel(const int64_t Nelements, const int32_t* __restrict__ elemen
     DTj[m] = s_D[m][j];
   }
 
+  const int node = j * NQ + i;
+  // PF: the gather of the next group's q through its staged index row is issued half-way
+  // through this group's layers (after a wait for that group's copy, which was issued at
+  // the start of this group), so its L2 latency overlaps the remaining layers
+  float n_q[PF ? NQ : 1];
+  int32_t n_id[PF ? NQ : 1];
+  auto gather_next = [&](const int64_t g, const int stage) {
+    if constexpr (PF) {
+      const int32_t* nidx = reinterpret_cast<const int32_t*>(smem + stage * STAGE_BYTES + el * L::ELEM_BYTES +
+                                                            L::GEO_BYTES);
+      const bool act = (g < ngroups) && (g * EPB + el < Nelements);
+#pragma unroll
+      for (int k = 0; k < NQ; ++k) {
+        const int32_t id = act ? nidx[k * NQ * NQ + node] : -1;
+        n_id[k] = id;
+        n_q[k] = (id >= 0) ? q[id] : 0.f;
+      }
+    }
+  };
+  if constexpr (PF) {
+    static_assert(STAGES == 2, "prefetching variant uses two stages");
+    cp_async_wait<0>();
+    __syncthreads();
+    gather_next(blockIdx.x, 0);
+  }
+
   for (int64_t it = 0;; ++it) {
     const int64_t grp = blockIdx.x + it * gridDim.x;
     if (grp >= ngroups) break;
     // this group's copies are complete, and after the barrier no thread still reads the
     // stage of the previous group, which the next copy then refills
-    cp_async_wait<STAGES - 2>();
+    if constexpr (!PF) cp_async_wait<STAGES - 2>();
     __syncthreads();
     issue(grp + (int64_t)(STAGES - 1) * gridDim.x, (int)((it + STAGES - 1) % STAGES));
     const unsigned char* base = smem + (it % STAGES) * STAGE_BYTES + el * L::ELEM_BYTES;
@@ -274,16 +300,21 @@ ax_hex_staged_kernel(const int64_t Nelements, const int32_t* __restrict__ elemen
     const int64_t ei = grp * EPB + el;
     const bool active = ei < Nelements;
     const int64_t e = active ? (elementList ? (int64_t)elementList[ei] : ei) : 0;
-    const int node = j * NQ + i;
 
     float r_q[NQ], r_Aq[NQ], qt[NQ], Gqt[NQ];
     int32_t r_id[NQ];
 #pragma unroll
     for (int k = 0; k < NQ; ++k) {
-      const int32_t id = active ? sidx[k * NQ * NQ + node] : -1;
-      r_id[k] = id;
-      r_q[k] = (id >= 0) ? q[id] : 0.f;
+      if constexpr (PF) {
+        r_id[k] = n_id[k];
+        r_q[k] = n_q[k];
+      } else {
+        const int32_t id = active ? sidx[k * NQ * NQ + node] : -1;
+        r_id[k] = id;
+        r_q[k] = (id >= 0) ? q[id] : 0.f;
+      }
     }
+    (void)sidx;
     const float lam = (lambdaE && active) ? lambdaE[e] : lambda;
     // t-direction of the pencil: qt = D r_q (rows of D are broadcast reads)
 #pragma unroll
@@ -309,6 +340,13 @@ ax_hex_staged_kernel(const int64_t Nelements, const int32_t* __restrict__ elemen
       Auk += row_dot<NQ, VEC>(&s_GqsT[b][el][i][0], DTj);       // sum_m D[m][j] Gqs(i,m)
       Auk += row_dot<NQ, VEC>(&s_Gqr[b][el][j][0], DTi);        // sum_m D[m][i] Gqr(m,j)
       r_Aq[k] = Auk;
+      if constexpr (PF) {
+        if (k == NQ / 2) {
+          cp_async_wait<0>();
+          __syncthreads();   // the next group's copy (both elements of the CTA) is visible
+          gather_next(grp + gridDim.x, (int)((it + 1) % STAGES));
+        }
+      }
     }
     // transposed t-direction: r_Aq[m] += sum_k D[k][m] Gqt[k]
 #pragma unroll
@@ -709,14 +747,14 @@ int ax_hex_dw(const AxArgs<double, float2>& a, cudaStream_t s) {
   return LPG_OK;
 }
 
-template <int NQ, typename T, typename G, int EPB, int STAGES>
+template <int NQ, typename T, typename G, int EPB, int STAGES, bool PF = false>
 static int launch_staged(const AxArgs<T, G>& a, cudaStream_t s) {
   using L = StagedLayout<NQ, G>;
   constexpr int smem = STAGES * EPB * L::ELEM_BYTES;
   static int configured = -1;   // per instantiation: dynamic shared memory opt-in
   static int ctasPerSM = 1;
   static int numSMs = 152;
-  auto kern = ax_hex_staged_kernel<NQ, T, G, EPB, STAGES>;
+  auto kern = ax_hex_staged_kernel<NQ, T, G, EPB, STAGES, PF>;
   if (configured < 0) {
     LPG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     int dev = 0;
@@ -746,6 +784,7 @@ static int staged_variant() {
       else if (!std::strcmp(e, "2x3")) v = 23;
       else if (!std::strcmp(e, "4x2")) v = 42;
       else if (!std::strcmp(e, "4x3")) v = 43;
+      else if (!std::strcmp(e, "2x2pf")) v = 122;
     }
   }
   return v;
@@ -765,14 +804,18 @@ template <int NQ, typename T, typename G, int INMODE, int OUTMODE>
 static int launch_ax(const AxArgs<T, G>& a, cudaStream_t s) {
   if constexpr (std::is_same<T, float>::value && INMODE == IN_GATHER && OUTMODE == OUT_ASSEMBLE) {
     if (staged_ok<NQ, T, G>(a)) {
-      // LPG_AX_STAGED = off | EPBxSTAGES (2x2, 2x3, 4x2, 4x3): tuning override
+      // LPG_AX_STAGED = off | EPBxSTAGES (2x2, 2x3, 4x2, 4x3) | 2x2pf: tuning override
       const int v = staged_variant();
       if (v == 0) { /* fall through to the unstaged kernel */ }
       else if (v == 22) return launch_staged<NQ, T, G, 2, 2>(a, s);
       else if (v == 23) return launch_staged<NQ, T, G, 2, 3>(a, s);
       else if (v == 43) return launch_staged<NQ, T, G, 4, 3>(a, s);
       else if (v == 42) return launch_staged<NQ, T, G, 4, 2>(a, s);
-      else return launch_staged<NQ, T, G, 2, 2>(a, s);  // measured best for FP32 and BF16 geometry at N=7
+      else if (v == 122) return launch_staged<NQ, T, G, 2, 2, true>(a, s);
+      // measured best at N=7: FP32 geometry with the next group's q gathered half-way
+      // through the current group (0.997 vs 1.112 ms at 64^3); BF16 geometry without it
+      else if constexpr (std::is_same<G, float>::value) return launch_staged<NQ, T, G, 2, 2, true>(a, s);
+      else return launch_staged<NQ, T, G, 2, 2>(a, s);
     }
   }
   constexpr int EPB = elems_per_block<NQ>();
