@@ -54,8 +54,9 @@ def parse():
                     help="preconditioner precisions; P+DF64 also runs the FP64 operator in double-FP32 words")
     ap.add_argument("--solve-reps", type=int, default=2)
     ap.add_argument("--solver", default="FPCG", choices=["FPCG", "NBFPCG", "PCG"], help="LINEAR SOLVER of --solve")
-    ap.add_argument("--precon", default="MULTIGRID", choices=["MULTIGRID", "SEMFEM", "PARALMOND", "JACOBI"],
+    ap.add_argument("--precon", default="MULTIGRID", choices=["MULTIGRID", "SEMFEM", "PARALMOND", "JACOBI", "OAS"],
                     help="PRECONDITIONER of --solve")
+    ap.add_argument("--disc", default="CONTINUOUS", choices=["CONTINUOUS", "IPDG"], help="DISCRETIZATION of --solve")
     ap.add_argument("--learned", action="store_true", help="learned-smoother training and solve comparison")
     ap.add_argument("--mlp", action="store_true", help="learned-smoother MLP inference (lpg_mlp_forward_bf16) timing")
     ap.add_argument("--ipdg", action="store_true", help="IPDG operator (gradient + Ax) throughput")
@@ -207,6 +208,7 @@ def run_solves(a):
         extra = {"OPERATOR PRECISION": op} if op else {}
         extra["LINEAR SOLVER"] = a.solver
         extra["PRECONDITIONER"] = a.precon
+        extra["DISCRETIZATION"] = a.disc
         e = lpg.Elliptic(solve_settings(a.nx, a.N, base, **extra))
         setup = time.time() - t0
         runs = [e.Run() for _ in range(a.solve_reps)]
@@ -218,8 +220,8 @@ def run_solves(a):
                      "coarse_n": e.info("coarse_n"), "nglobal": e.Nglobal}
         e.close()
     pre = "p-MG 7->3->1" if a.precon == "MULTIGRID" else a.precon
-    print(json.dumps({"workload": "%s + %s time-to-1e-8, %d^3 jittered hex, N=%d, lambda=0"
-                      % (a.solver, pre, a.nx, a.N), "results": res}), flush=True)
+    print(json.dumps({"workload": "%s + %s time-to-1e-8, %d^3 jittered hex, N=%d, lambda=0, %s"
+                      % (a.solver, pre, a.nx, a.N, a.disc), "results": res}), flush=True)
 
 
 def run_learned(a):
