@@ -658,6 +658,13 @@ int Elliptic::BuildMatrixIpdg(std::vector<int64_t>& rowStarts, std::vector<int32
                               cudaStream_t s) {
   const int Np = mesh.Np;
   const int64_t E = mesh.E;
+  {
+    // at most 7 element blocks per row, 12 bytes per entry: refuse beyond a quarter of host memory
+    const long pages = sysconf(_SC_PHYS_PAGES), pageSize = sysconf(_SC_PAGE_SIZE);
+    const double hostBytes = (pages > 0 && pageSize > 0) ? (double)pages * (double)pageSize : 64e9;
+    if ((double)Nlocal * 7.0 * Np * 12.0 > 0.25 * hostBytes)
+      return set_error(LPG_ERR_UNSUPPORTED, "IPDG matrix too large for host AMG setup; use MULTIGRID");
+  }
   std::vector<int> color(E, -1);
   int ncolor = 0;
   {
