@@ -140,6 +140,35 @@ def test_vtu_output_matches_oracle_plot_interpolation(tmp_path):
         re.sub(r"\s+", " ", open(tmp_path / "sol_0000.vtu").read())
 
 
+@pytest.mark.parametrize("precision", ["FP64", "FP32"])
+def test_host_buffer_operator_on_shuffled_file_mesh(tmp_path, precision):
+    """lpg_elliptic_operator_host(_f32) pipelines element chunks with prefix bounds computed
+    from the numbering; with a shuffled, rotated file mesh those bounds are loose but the
+    result must still equal the device operator (and the oracle)."""
+    s = dict(BASE, **{"MESH FILE": mesh(tmp_path, shuffle_seed=4, rotate_seed=5, jitter=0.1, jitter_seed=3),
+                      "POLYNOMIAL DEGREE": 7})
+    e = lpg.Elliptic(s)
+    dt = np.float64 if precision == "FP64" else np.float32
+    qh = np.random.default_rng(2).uniform(-1, 1, e.Nglobal).astype(dt)
+    Aq = np.zeros(e.Nglobal, dtype=dt)
+    e.OperatorHost(qh, Aq, precision)
+    ref = Oracle(s).operator(qh.astype(np.float64))
+    assert rel_err(Aq.astype(np.float64), ref) < (1e-12 if precision == "FP64" else 2e-6)
+
+
+def test_vtu_output_ipdg(tmp_path):
+    s = dict(BASE, **{"MESH FILE": mesh(tmp_path, rotate_seed=2), "POLYNOMIAL DEGREE": 2,
+                      "DISCRETIZATION": "IPDG", "PRECONDITIONER": "JACOBI",
+                      "OUTPUT TO FILE": "TRUE", "OUTPUT FILE NAME": str(tmp_path / "dg")})
+    r = lpg.Elliptic(s).Run(want_solution=True)
+    o = Oracle(s)
+    E, N = o.info("nelements"), 2
+    piece = ET.parse(str(tmp_path / "dg_0000.vtu")).getroot().find("UnstructuredGrid/Piece")
+    fld = _floats(piece.find("PointData/DataArray"))
+    ref_q = plot_interp(r["xL"], E, N).ravel()
+    assert np.abs(fld - ref_q).max() < 1e-5 * np.abs(ref_q).max()
+
+
 def test_unsupported_file_mesh_features_fail_loudly(tmp_path):
     f = mesh(tmp_path)
     with pytest.raises(RuntimeError):
