@@ -60,6 +60,7 @@ def parse():
     ap.add_argument("--learned", action="store_true", help="learned-smoother training and solve comparison")
     ap.add_argument("--mlp", action="store_true", help="learned-smoother MLP inference (lpg_mlp_forward_bf16) timing")
     ap.add_argument("--ipdg", action="store_true", help="IPDG operator (gradient + Ax) throughput")
+    ap.add_argument("--sequence", action="store_true", help="repeated solves with each initial-guess strategy")
     ap.add_argument("--train-nx", type=int, default=32)
     ap.add_argument("--train-samples", type=int, default=20000)
     ap.add_argument("--train-solves", type=int, default=8)
@@ -318,6 +319,54 @@ def run_mlp(a):
     print(json.dumps({"workload": "learned-smoother MLP inference, BF16 tensor cores", "results": res}), flush=True)
 
 
+def run_sequence(a):
+    """Repeated solves as a time stepper makes them (linearSolver_t with an initial-guess
+    strategy, initialGuess.cpp): K right-hand sides r(t) = sum_k exp(-(t/1.5 - k)^2 / 2) r_k
+    blending 10 Gaussian-source fields (16 sources each, seeds 3..12) of the same nx^3
+    jittered box, N=7, so the data drift smoothly through a 10-dimensional space; each solve
+    to 1e-8 relative to ||r|| (ABS/REL-RHS-2NORM) by FPCG + p-MG with the FP32 preconditioner
+    and double-FP32 outer operator, for each INITIAL GUESS STRATEGY. Per strategy: mean
+    iterations and wall time per solve over the last K-3 steps. One JSON line."""
+    import math
+    import torch
+    import libparanumal_gb300 as lpg
+    import __graft_entry__ as g
+    g.build()
+    torch.cuda.set_device(0)
+    base = solve_settings(a.nx, 7, "FP32", **{"OPERATOR PRECISION": "DF64",
+                                              "LINEAR SOLVER STOPPING CRITERION": "ABS/REL-RHS-2NORM"})
+    parts = []
+    for seed in range(3, 13):
+        e = lpg.Elliptic(dict(base, **{"RHS FIELD": "GAUSSIAN SOURCES", "RHS SEED": seed, "RHS SOURCES": 16}))
+        r = torch.zeros(e.Nglobal, dtype=torch.float64, device="cuda")
+        e.rhs(r)
+        parts.append(r)
+        e.close()
+    strategies = {"ZERO": {}, "CLASSIC": {"INITIAL GUESS HISTORY SPACE DIMENSION": 8},
+                  "QR": {"INITIAL GUESS HISTORY SPACE DIMENSION": 8},
+                  "EXTRAP": {"INITIAL GUESS HISTORY SPACE DIMENSION": 4, "INITIAL GUESS EXTRAP DEGREE": 2,
+                             "INITIAL GUESS EXTRAP COEFFS METHOD": "CPQR"}}
+    res = {}
+    K = max(a.steps, 6)
+    for name, over in strategies.items():
+        e = lpg.Elliptic(dict(base, **{"INITIAL GUESS STRATEGY": name}, **over))
+        x = torch.zeros_like(parts[0])
+        its, secs = [], []
+        for t in range(K):
+            rhs = sum(math.exp(-0.5 * (t / 1.5 - k) ** 2) * pk for k, pk in enumerate(parts))
+            torch.cuda.synchronize()
+            t0 = time.time()
+            its.append(e.Solve(x, rhs, tol=1e-8))
+            torch.cuda.synchronize()
+            secs.append(time.time() - t0)
+        e.close()
+        res[name] = {"iterations": its, "mean_iterations_after_3": sum(its[3:]) / (K - 3),
+                     "mean_seconds_after_3": sum(secs[3:]) / (K - 3)}
+    print(json.dumps({"workload": "%d repeated solves, r(t) blending 10 Gaussian-source fields, %d^3 jittered "
+                                  "hex, N=7, FPCG + p-MG (FP32+DF64), tol 1e-8 of ||r||" % (K, a.nx),
+                      "results": res}), flush=True)
+
+
 def run_ipdg(a):
     """IPDG operator throughput (DISCRETIZATION = IPDG, gradient + interior-penalty Ax) on an
     nx^3 jittered Dirichlet box at degree N: W warm-up and K timed applications on device
@@ -372,6 +421,8 @@ def main():
         return run_mlp(a)
     if a.ipdg:
         return run_ipdg(a)
+    if a.sequence:
+        return run_sequence(a)
     import numpy as np
     import torch
     import libparanumal_gb300 as lpg
