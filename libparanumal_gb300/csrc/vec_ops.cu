@@ -7,6 +7,7 @@
 // caller decides when (and whether) to synchronise; the summation order depends
 // only on N, which makes repeated runs bit-identical.
 #include <algorithm>
+#include <type_traits>
 
 #include "lpg_common.cuh"
 #include "lpg_internal.hpp"
@@ -405,30 +406,46 @@ template int cheb_step<float>(int64_t, const float*, const float*, float*, float
 // igReconstruct.okl, igDropQRFirstColumn.okl, igExtrap.okl). History vectors are stored
 // contiguously, column m at Q + m N.
 
+// The history kernels are instantiated for a compile-time bound K on the history dimension
+// (4, 8, 16 or 32, the smallest that holds k) and unrolled over it: the per-column
+// accumulators stay in registers and the k column loads of a node are independent, so each
+// thread keeps k loads in flight.
+template <typename F>
+static int history_dispatch(int k, F&& f) {
+  if (k <= 4) return f(std::integral_constant<int, 4>{});
+  if (k <= 8) return f(std::integral_constant<int, 8>{});
+  if (k <= 16) return f(std::integral_constant<int, 16>{});
+  return f(std::integral_constant<int, kMaxHistory>{});
+}
+
 // partials[m * nb + b] = block b's share of Q_m . x for m < k (host sums the nb entries)
+template <int K>
 __global__ void __launch_bounds__(256)
 multi_dot_kernel(const int64_t N, const int k, const double* __restrict__ x, const double* __restrict__ Q,
                  double* __restrict__ partials) {
   __shared__ double s_w[8];
-  double acc[kMaxHistory];
+  double acc[K];
 #pragma unroll
-  for (int m = 0; m < kMaxHistory; ++m) acc[m] = 0;
+  for (int m = 0; m < K; ++m) acc[m] = 0;
   for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x) {
     const double xn = x[n];
 #pragma unroll
-    for (int m = 0; m < kMaxHistory; ++m)
+    for (int m = 0; m < K; ++m)
       if (m < k) acc[m] += Q[(int64_t)m * N + n] * xn;
   }
-  for (int m = 0; m < k; ++m) {
-    double v = acc[m];
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    __syncthreads();
-    if ((threadIdx.x & 31) == 0) s_w[threadIdx.x >> 5] = v;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double t = 0;
-      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s_w[w];
-      partials[(int64_t)m * gridDim.x + blockIdx.x] = t;
+#pragma unroll
+  for (int m = 0; m < K; ++m) {
+    if (m < k) {
+      double v = acc[m];
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+      __syncthreads();
+      if ((threadIdx.x & 31) == 0) s_w[threadIdx.x >> 5] = v;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        double t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s_w[w];
+        partials[(int64_t)m * gridDim.x + blockIdx.x] = t;
+      }
     }
   }
 }
@@ -437,69 +454,105 @@ int multi_dot(int64_t N, int k, const double* x, const double* Q, double* partia
   const int nb = (int)std::max<int64_t>(1, std::min<int64_t>((N + 255) / 256, kMultiDotBlocks));
   *nblocks = nb;
   if (k == 0) return LPG_OK;
-  multi_dot_kernel<<<nb, 256, 0, s>>>(N, k, x, Q, partials);
-  LPG_LAUNCH_CHECK("multi_dot_kernel");
-  return LPG_OK;
+  return history_dispatch(k, [&](auto kb) {
+    multi_dot_kernel<decltype(kb)::value><<<nb, 256, 0, s>>>(N, k, x, Q, partials);
+    LPG_LAUNCH_CHECK("multi_dot_kernel");
+    return LPG_OK;
+  });
 }
 
 // out = u + beta * sum_m c[m] Q_m  (out may be u)
+template <int K>
 __global__ void combine_kernel(const int64_t N, const int k, const double* u, const double beta, const HistCoeffs c,
                                const double* __restrict__ Q, double* out) {
   for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x) {
+    double q[K];
+#pragma unroll
+    for (int m = 0; m < K; ++m) q[m] = m < k ? Q[(int64_t)m * N + n] : 0.0;
     double r = u ? u[n] : 0.0;
-    for (int m = 0; m < k; ++m) r += beta * c.v[m] * Q[(int64_t)m * N + n];
+#pragma unroll
+    for (int m = 0; m < K; ++m)
+      if (m < k) r += beta * c.v[m] * q[m];
     out[n] = r;
   }
 }
 int combine(int64_t N, int k, const double* u, double beta, const HistCoeffs& c, const double* Q, double* out,
             cudaStream_t s) {
   if (N <= 0) return LPG_OK;
-  combine_kernel<<<grid_for(N, 256, kStreamCap), 256, 0, s>>>(N, k, u, beta, c, Q, out);
-  LPG_LAUNCH_CHECK("combine_kernel");
-  return LPG_OK;
+  if (k < 0 || k > kMaxHistory) return set_error(LPG_ERR_INVALID, "combine: history dimension out of range");
+  return history_dispatch(k, [&](auto kb) {
+    combine_kernel<decltype(kb)::value><<<grid_for(N, 256, kStreamCap), 256, 0, s>>>(N, k, u, beta, c, Q, out);
+    LPG_LAUNCH_CHECK("combine_kernel");
+    return LPG_OK;
+  });
 }
 
 // Rotations i = 0..dim-2 applied in order to columns (i, i+1) of Q and U:
-// (Q_i, Q_i+1) <- (c Q_i + s Q_i+1, -s Q_i + c Q_i+1); then column dim-1 = 0
-__global__ void givens_columns_kernel(const int64_t N, const int dim, const HistCoeffs c, const HistCoeffs sn,
-                                      double* __restrict__ Q, double* __restrict__ U) {
-  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x) {
-    double q1 = Q[n], u1 = U[n];
-    for (int i = 0; i < dim - 1; ++i) {
-      const double q0 = q1, u0 = u1;
-      q1 = Q[(int64_t)(i + 1) * N + n];
-      u1 = U[(int64_t)(i + 1) * N + n];
-      Q[(int64_t)i * N + n] = c.v[i] * q0 + sn.v[i] * q1;
-      U[(int64_t)i * N + n] = c.v[i] * u0 + sn.v[i] * u1;
-      q1 = -sn.v[i] * q0 + c.v[i] * q1;
-      u1 = -sn.v[i] * u0 + c.v[i] * u1;
+// (Q_i, Q_i+1) <- (c Q_i + s Q_i+1, -s Q_i + c Q_i+1); then column dim-1 = 0.
+// A node's dim values of one array are loaded first, rotated in registers and stored;
+// Q and U are done one after the other.
+template <int K>
+__device__ __forceinline__ void givens_node(const int64_t N, const int64_t n, const int dim, const HistCoeffs& c,
+                                            const HistCoeffs& sn, double* __restrict__ Q) {
+  double q[K];
+#pragma unroll
+  for (int i = 0; i < K; ++i) q[i] = i < dim ? Q[(int64_t)i * N + n] : 0.0;
+#pragma unroll
+  for (int i = 0; i + 1 < K; ++i) {
+    if (i + 1 < dim) {
+      const double q0 = q[i], q1 = q[i + 1];
+      q[i] = c.v[i] * q0 + sn.v[i] * q1;
+      q[i + 1] = -sn.v[i] * q0 + c.v[i] * q1;
     }
-    Q[(int64_t)(dim - 1) * N + n] = 0;
-    U[(int64_t)(dim - 1) * N + n] = 0;
+  }
+#pragma unroll
+  for (int i = 0; i < K; ++i) {
+    if (i + 1 < dim) Q[(int64_t)i * N + n] = q[i];
+    else if (i + 1 == dim) Q[(int64_t)i * N + n] = 0;
+  }
+}
+template <int K>
+__global__ void __launch_bounds__(256)
+givens_columns_kernel(const int64_t N, const int dim, const HistCoeffs c, const HistCoeffs sn,
+                      double* __restrict__ Q, double* __restrict__ U) {
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x) {
+    givens_node<K>(N, n, dim, c, sn, Q);
+    givens_node<K>(N, n, dim, c, sn, U);
   }
 }
 int givens_columns(int64_t N, int dim, const HistCoeffs& c, const HistCoeffs& sn, double* Q, double* U, cudaStream_t s) {
   if (N <= 0 || dim <= 0) return LPG_OK;
-  givens_columns_kernel<<<grid_for(N, 256, kStreamCap), 256, 0, s>>>(N, dim, c, sn, Q, U);
-  LPG_LAUNCH_CHECK("givens_columns_kernel");
-  return LPG_OK;
+  if (dim > kMaxHistory) return set_error(LPG_ERR_INVALID, "givens_columns: history dimension out of range");
+  return history_dispatch(dim, [&](auto kb) {
+    givens_columns_kernel<decltype(kb)::value><<<grid_for(N, 256, kStreamCap), 256, 0, s>>>(N, dim, c, sn, Q, U);
+    LPG_LAUNCH_CHECK("givens_columns_kernel");
+    return LPG_OK;
+  });
 }
 
 // x = sum_i d[i] * H_{(i + shift) % nh} over the nonzero d[i]
+template <int K>
 __global__ void extrap_kernel(const int64_t N, const int nh, const int shift, const HistCoeffs d,
                               const double* __restrict__ H, double* __restrict__ x) {
   for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x) {
+    double h[K];
+#pragma unroll
+    for (int i = 0; i < K; ++i) h[i] = (i < nh && d.v[i] != 0.0) ? H[(int64_t)((i + shift) % nh) * N + n] : 0.0;
     double r = 0;
-    for (int i = 0; i < nh; ++i)
-      if (d.v[i] != 0.0) r += d.v[i] * H[(int64_t)((i + shift) % nh) * N + n];
+#pragma unroll
+    for (int i = 0; i < K; ++i)
+      if (i < nh && d.v[i] != 0.0) r += d.v[i] * h[i];
     x[n] = r;
   }
 }
 int extrap(int64_t N, int nh, int shift, const HistCoeffs& d, const double* H, double* x, cudaStream_t s) {
   if (N <= 0) return LPG_OK;
-  extrap_kernel<<<grid_for(N, 256, kStreamCap), 256, 0, s>>>(N, nh, shift, d, H, x);
-  LPG_LAUNCH_CHECK("extrap_kernel");
-  return LPG_OK;
+  if (nh < 1 || nh > kMaxHistory) return set_error(LPG_ERR_INVALID, "extrap: history dimension out of range");
+  return history_dispatch(nh, [&](auto kb) {
+    extrap_kernel<decltype(kb)::value><<<grid_for(N, 256, kStreamCap), 256, 0, s>>>(N, nh, shift, d, H, x);
+    LPG_LAUNCH_CHECK("extrap_kernel");
+    return LPG_OK;
+  });
 }
 
 // ---------------------------------------------------------------- NBFPCG

@@ -77,6 +77,46 @@ def test_initial_guess_sequence_matches_restatement(strategy, extra, make_ref):
         assert min(iters[3:]) < 0.9 * iters[0], iters
 
 
+LONG = [
+    ("CLASSIC", {"INITIAL GUESS HISTORY SPACE DIMENSION": 10}, lambda: ig.Classic(10), 12),
+    ("QR", {"INITIAL GUESS HISTORY SPACE DIMENSION": 5}, lambda: ig.RollingQR(5), 8),
+    ("QR", {"INITIAL GUESS HISTORY SPACE DIMENSION": 17}, lambda: ig.RollingQR(17), 20),
+    ("EXTRAP", {"INITIAL GUESS HISTORY SPACE DIMENSION": 18, "INITIAL GUESS EXTRAP DEGREE": 4},
+     lambda: ig.Extrap(18, 4), 20),
+]
+
+
+@pytest.mark.parametrize("strategy,extra,make_ref,steps", LONG,
+                         ids=["%s%d" % (c[0], c[1]["INITIAL GUESS HISTORY SPACE DIMENSION"]) for c in LONG])
+def test_long_history_matches_restatement(strategy, extra, make_ref, steps):
+    """History dimensions past 4 (the 8-, 16- and 32-column instances of the history
+    kernels), with the rolling QR basis filled and then dropping its first column: solutions
+    drawn from a 24-dimensional space, so the history directions stay independent."""
+    s = dict(BASE, **{"INITIAL GUESS STRATEGY": strategy}, **extra)
+    e = lpg.Elliptic(s)
+    o = Oracle(BASE)
+    N = e.Nglobal
+    rng = np.random.default_rng(29)
+    AU = [o.operator(rng.uniform(-1, 1, N)) for _ in range(24)]
+    ref = make_ref()
+    for t in range(steps):
+        rhs = sum(np.cos(0.37 * (k + 1) * t + k) * a for k, a in enumerate(AU))
+        r = torch.tensor(rhs, device="cuda")
+        x0 = torch.zeros(N, dtype=torch.float64, device="cuda")
+        e.initial_guess(x0, r)
+        gref = ref.form(np.zeros(N), rhs)
+        if np.linalg.norm(gref) > 0.0:
+            err = rel_err(x0.cpu().numpy(), gref)
+            assert err < 1e-9, (t, err)
+        x = torch.zeros(N, dtype=torch.float64, device="cuda")
+        e.Solve(x, r.clone(), tol=1e-8)
+        torch.cuda.synchronize()
+        if strategy == "EXTRAP":
+            ref.form(np.zeros(N), rhs)
+        ref.update(o.operator, x.cpu().numpy())
+    assert e.info("ig_history") == min(steps, extra["INITIAL GUESS HISTORY SPACE DIMENSION"]) or strategy == "CLASSIC"
+
+
 def test_bad_initial_guess_settings_are_errors():
     with pytest.raises(lpg.LPGError):
         lpg.Elliptic(dict(BASE, **{"INITIAL GUESS STRATEGY": "CLASSIC"}))          # no history dimension
