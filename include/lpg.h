@@ -162,7 +162,8 @@ int lpg_elliptic_operator(lpg_elliptic *e, const double *q, double *Aq, void *st
 /* Reduced-precision operator of the same object (no reference counterpart; the
  * reference is FP64 only): FP32 vectors, FP32 (bf16geo = 0) or BF16 (bf16geo = 1)
  * geometric factors, FP32 arithmetic. The reduced-precision copies of the geometric
- * factors are made on first use. */
+ * factors are made on first use. DISCRETIZATION = IPDG: FP32 volume and surface factors
+ * (bf16geo must be 0). */
 int lpg_elliptic_operator_f32(lpg_elliptic *e, const float *q, float *Aq, int bf16geo, void *stream);
 /* The same operator (device vectors, FP64 in and out) computed in double-FP32 words on
  * the FP32 pipe -- no reference counterpart. 48-bit significands; agrees with the FP64

@@ -160,8 +160,8 @@ int build(lpg_elliptic* h) {
                                           "tetrahedra elements. Use JACOBI instead.");
   else if (c.ipdg && pre == "SEMFEM")
     return set_error(LPG_ERR_UNSUPPORTED, "SEMFEM is supported for CONTINUOUS only");
-  else if (c.ipdg && pre != "NONE" && pre != "JACOBI" && S.get("PRECONDITIONER PRECISION", "FP64") != "FP64")
-    return set_error(LPG_ERR_UNSUPPORTED, "IPDG multigrid runs in FP64 (PRECONDITIONER PRECISION FP64)");
+  else if (c.ipdg && pre != "NONE" && pre != "JACOBI" && S.get("PRECONDITIONER PRECISION", "FP64") == "BF16GEO")
+    return set_error(LPG_ERR_UNSUPPORTED, "IPDG multigrid runs in FP64 or FP32 (PRECONDITIONER PRECISION)");
   else if (pre == "MULTIGRID" || pre == "PARALMOND" || pre == "SEMFEM" || pre == "OAS") {
     MGOptions o;
     o.amgOnly = (pre == "PARALMOND" || pre == "SEMFEM");
@@ -420,7 +420,7 @@ extern "C" int lpg_elliptic_operator_df64(lpg_elliptic* e, const double* q, doub
 
 extern "C" int lpg_elliptic_operator_f32(lpg_elliptic* e, const float* q, float* Aq, int bf16geo, void* stream) {
   if (!e || !q || !Aq) return set_error(LPG_ERR_INVALID, "null argument");
-  if (e->el->ipdg) return set_error(LPG_ERR_UNSUPPORTED, "reduced-precision operators are CONTINUOUS only");
+  if (e->el->ipdg && bf16geo) return set_error(LPG_ERR_UNSUPPORTED, "BF16 geometry is defined for CONTINUOUS only");
   LPG_GUARD_BEGIN
   cudaStream_t s = pick(e, stream);
   int rc = e->el->make_f32(bf16geo != 0, s);

@@ -383,8 +383,25 @@ int Elliptic::finish_setup(const std::vector<double>* lamE, cudaStream_t s) {
 }
 
 int Elliptic::make_f32(bool bf16, cudaStream_t s) {
-  int rc = bf16 ? mesh.make_bf16(s) : mesh.make_f32(s);
-  if (rc) return rc;
+  int rc;
+  if (ipdg) {
+    // FP32 copies of the IPDG volume and surface factors (the C0 geometric factors are not used)
+    if (bf16) return set_error(LPG_ERR_UNSUPPORTED, "BF16 geometry is defined for CONTINUOUS only");
+    const int64_t E = mesh.E, Np = mesh.Np, Nfp = (int64_t)mesh.Nq * mesh.Nq;
+    if (!vgeo32.p) {
+      if ((rc = vgeo32.alloc(E * 10 * Np)) || (rc = sgeo32.alloc(E * 5 * 6 * Nfp)) || (rc = g4_32.alloc(4 * Nlocal)))
+        return rc;
+      if ((rc = convert<double, float>(E * 10 * Np, vgeo.p, vgeo32.p, s)) ||
+          (rc = convert<double, float>(E * 5 * 6 * Nfp, sgeo.p, sgeo32.p, s)))
+        return rc;
+    }
+    if (!mesh.D32.p) {
+      const int Nq = mesh.Nq;
+      if ((rc = mesh.D32.alloc(Nq * Nq)) || (rc = convert<double, float>(Nq * Nq, mesh.D_d.p, mesh.D32.p, s))) return rc;
+    }
+  } else if ((rc = bf16 ? mesh.make_bf16(s) : mesh.make_f32(s))) {
+    return rc;
+  }
   if (!weightG32.p) {
     if ((rc = weightG32.alloc(Nglobal))) return rc;
     if ((rc = convert<double, float>(Nglobal, weightG.p, weightG32.p, s))) return rc;
@@ -423,6 +440,18 @@ int Elliptic::Operator(const double* q, double* Aq, cudaStream_t s) {
 
 int Elliptic::OperatorF32(const float* q, float* Aq, Prec prec, cudaStream_t s) {
   const int64_t Np = mesh.Np;
+  if (ipdg) {
+    if (prec != Prec::F32 || !vgeo32.p) return set_error(LPG_ERR_UNSUPPORTED, "IPDG: FP32 operator not prepared");
+    IpdgArgsF32 a;
+    a.N = mesh.N; a.E = mesh.E;
+    a.vgeo = vgeo32.p; a.sgeo = sgeo32.p; a.D = mesh.D32.p;
+    a.vmapP = vmapP.p; a.EToB = EToB.p;
+    a.lambda = (float)lambda; a.tau = (float)tau;
+    a.lambdaE = hasLambdaE ? lambdaE32.p : nullptr;
+    a.q = q; a.out = Aq;
+    a.g4 = reinterpret_cast<float4*>(g4_32.p);
+    return ipdg_operator_f32(a, s);
+  }
   if (prec == Prec::BF16G) {
     AxArgs<float, __nv_bfloat16> a;
     a.N = mesh.N; a.Nelements = mesh.E; a.g2l = g2l.p;

@@ -165,6 +165,7 @@ struct Elliptic {
   bool ipdg = false;
   double tau = 0;
   DevBuf<double> vgeo, sgeo, g4;
+  DevBuf<float> vgeo32, sgeo32, g4_32;  // FP32 copies and gradient scratch (preconditioner levels)
   DevBuf<int32_t> vmapP;
   DevBuf<int> EToB;
   std::vector<int64_t> EToE_h;     // element neighbours (host), for the matrix probing

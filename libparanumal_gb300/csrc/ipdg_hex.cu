@@ -9,11 +9,14 @@
 //
 // Layout (per element, structure of arrays): vgeo [e][10][Np] = rx ry rz sx sy sz tx ty tz JW;
 // sgeo [e][5][6 Nfp] = nx ny nz WsJ hinv for the face nodes of faces 0..5 (local index order);
-// gradients [E Np] double4_32a = (qx, qy, qz, q).
+// gradients [E Np] double4_32a = (qx, qy, qz, q). The FP32 preconditioner levels run the same
+// gradient and operator kernels on FP32 copies of vgeo and sgeo with float4 gradients.
 //
 // Kernels run one CTA per element with one thread per node. A node owns its accumulators:
 // the face terms of every face it lies on are added by that node's thread, in the face
 // order 0, 5, 1, 3, 2, 4, so no two threads write the same value.
+#include <type_traits>
+
 #include "lpg_common.cuh"
 #include "lpg_internal.hpp"
 
@@ -114,27 +117,29 @@ __global__ void ipdg_hinv_kernel(const int64_t nFaceNodes, const int nfpAll, con
 }
 
 // ---------------------------------------------------------------- gradient
-template <int NQ>
+// T = double (the operator) or float (the FP32 preconditioner levels); V4 the matching
+// 4-vector (double4_32a, float4)
+template <int NQ, typename T, typename V4>
 __global__ void __launch_bounds__(NQ * NQ * NQ)
-ipdg_gradient_kernel(const double* __restrict__ vgeo, const double* __restrict__ Dg, const double* __restrict__ q,
-                     double4_32a* __restrict__ g4) {
+ipdg_gradient_kernel(const T* __restrict__ vgeo, const T* __restrict__ Dg, const T* __restrict__ q,
+                     V4* __restrict__ g4) {
   constexpr int NP = NQ * NQ * NQ, NFP = NQ * NQ;
-  __shared__ double s_q[NP], s_D[NQ * NQ];
+  __shared__ T s_q[NP], s_D[NQ * NQ];
   const int64_t e = blockIdx.x;
   const int n = threadIdx.x;
   if (n < NQ * NQ) s_D[n] = Dg[n];
   s_q[n] = q[e * NP + n];
   __syncthreads();
   const int i = n % NQ, j = (n / NQ) % NQ, k = n / NFP;
-  double qr = 0, qs = 0, qt = 0;
+  T qr = 0, qs = 0, qt = 0;
 #pragma unroll
   for (int m = 0; m < NQ; ++m) {
     qr += s_D[i * NQ + m] * s_q[m + j * NQ + k * NFP];
     qs += s_D[j * NQ + m] * s_q[i + m * NQ + k * NFP];
     qt += s_D[k * NQ + m] * s_q[i + j * NQ + m * NFP];
   }
-  const double* vg = vgeo + e * kVgeo * NP + n;
-  double4_32a o;
+  const T* vg = vgeo + e * kVgeo * NP + n;
+  V4 o;
   o.x = vg[0 * NP] * qr + vg[3 * NP] * qs + vg[6 * NP] * qt;
   o.y = vg[1 * NP] * qr + vg[4 * NP] * qs + vg[7 * NP] * qt;
   o.z = vg[2 * NP] * qr + vg[5 * NP] * qs + vg[8 * NP] * qt;
@@ -145,9 +150,9 @@ ipdg_gradient_kernel(const double* __restrict__ vgeo, const double* __restrict__
 // ---------------------------------------------------------------- weak divergence (shared by Ax and rhs)
 // out_n = acc_n + sum_p D[p][i] ur(p,j,k) + D[p][j] us(i,p,k) + D[p][k] ut(i,j,p), with (ur, us, ut)
 // = (grad r, grad s, grad t) . (gx, gy, gz)
-template <int NQ>
-__device__ __forceinline__ double weak_divergence(const double* vg, double gx, double gy, double gz, double acc,
-                                                  double* s_ur, double* s_us, double* s_ut, const double* s_D) {
+template <int NQ, typename T>
+__device__ __forceinline__ T weak_divergence(const T* vg, T gx, T gy, T gz, T acc, T* s_ur, T* s_us, T* s_ut,
+                                             const T* s_D) {
   constexpr int NP = NQ * NQ * NQ, NFP = NQ * NQ;
   const int n = threadIdx.x;
   s_ur[n] = vg[0 * NP] * gx + vg[1 * NP] * gy + vg[2 * NP] * gz;
@@ -155,7 +160,7 @@ __device__ __forceinline__ double weak_divergence(const double* vg, double gx, d
   s_ut[n] = vg[6 * NP] * gx + vg[7 * NP] * gy + vg[8 * NP] * gz;
   __syncthreads();
   const int i = n % NQ, j = (n / NQ) % NQ, k = n / NFP;
-  double v = acc;
+  T v = acc;
 #pragma unroll
   for (int p = 0; p < NQ; ++p) {
     v += s_D[p * NQ + i] * s_ur[p + j * NQ + k * NFP];
@@ -166,24 +171,23 @@ __device__ __forceinline__ double weak_divergence(const double* vg, double gx, d
 }
 
 // ---------------------------------------------------------------- operator
-template <int NQ>
+template <int NQ, typename T, typename V4>
 __global__ void __launch_bounds__(NQ * NQ * NQ)
-ipdg_ax_kernel(const double* __restrict__ vgeo, const double* __restrict__ sgeo, const int32_t* __restrict__ vmapP,
-               const int* __restrict__ EToB, const double* __restrict__ Dg, const double lambda,
-               const double* __restrict__ lambdaE, const double tau, const double4_32a* __restrict__ g4,
-               double* __restrict__ Aq) {
+ipdg_ax_kernel(const T* __restrict__ vgeo, const T* __restrict__ sgeo, const int32_t* __restrict__ vmapP,
+               const int* __restrict__ EToB, const T* __restrict__ Dg, const T lambda,
+               const T* __restrict__ lambdaE, const T tau, const V4* __restrict__ g4, T* __restrict__ Aq) {
   constexpr int NP = NQ * NQ * NQ, NFP = NQ * NQ;
-  __shared__ double s_ur[NP], s_us[NP], s_ut[NP], s_D[NQ * NQ];
+  __shared__ T s_ur[NP], s_us[NP], s_ut[NP], s_D[NQ * NQ];
   const int64_t e = blockIdx.x;
   const int n = threadIdx.x;
   if (n < NQ * NQ) s_D[n] = Dg[n];
   const int i = n % NQ, j = (n / NQ) % NQ, k = n / NFP;
-  const double* vg = vgeo + e * kVgeo * NP + n;
-  const double4_32a GM = g4[e * NP + n];
-  const double JW = vg[9 * NP];
-  const double lam = lambdaE ? lambdaE[e] : lambda;
-  double gx = JW * GM.x, gy = JW * GM.y, gz = JW * GM.z, a = JW * lam * GM.w;
-  const double* sg = sgeo + e * kSgeo * 6 * NFP;
+  const T* vg = vgeo + e * kVgeo * NP + n;
+  const V4 GM = g4[e * NP + n];
+  const T JW = vg[9 * NP];
+  const T lam = lambdaE ? lambdaE[e] : lambda;
+  T gx = JW * GM.x, gy = JW * GM.y, gz = JW * GM.z, a = JW * lam * GM.w;
+  const T* sg = sgeo + e * kSgeo * 6 * NFP;
   const int faces[6] = {k == 0 ? 0 : -1, k == NQ - 1 ? 5 : -1, j == 0 ? 1 : -1,
                         j == NQ - 1 ? 3 : -1, i == NQ - 1 ? 2 : -1, i == 0 ? 4 : -1};
 #pragma unroll
@@ -191,9 +195,9 @@ ipdg_ax_kernel(const double* __restrict__ vgeo, const double* __restrict__ sgeo,
     const int f = faces[q];
     if (f < 0) continue;
     const int col = f * NFP + face_slot<NQ>(f, i, j, k);
-    const double nx = sg[0 * 6 * NFP + col], ny = sg[1 * 6 * NFP + col], nz = sg[2 * 6 * NFP + col];
-    const double w = sg[3 * 6 * NFP + col], hinv = sg[4 * 6 * NFP + col];
-    double4_32a P = g4[vmapP[e * 6 * NFP + col]];
+    const T nx = sg[0 * 6 * NFP + col], ny = sg[1 * 6 * NFP + col], nz = sg[2 * 6 * NFP + col];
+    const T w = sg[3 * 6 * NFP + col], hinv = sg[4 * 6 * NFP + col];
+    V4 P = g4[vmapP[e * 6 * NFP + col]];
     const int bc = EToB[e * 6 + f];
     if (bc > 0) {
       // homogeneous boundary state B (Dirichlet: q = 0, grad kept; Neumann: q kept, grad = 0),
@@ -201,13 +205,13 @@ ipdg_ax_kernel(const double* __restrict__ vgeo, const double* __restrict__ sgeo,
       if (bc == 1) { P.x = GM.x; P.y = GM.y; P.z = GM.z; P.w = -GM.w; }
       else { P.x = -GM.x; P.y = -GM.y; P.z = -GM.z; P.w = GM.w; }
     }
-    const double dq = P.w - GM.w;
-    gx += 0.5 * w * nx * dq;
-    gy += 0.5 * w * ny * dq;
-    gz += 0.5 * w * nz * dq;
-    a += -0.5 * w * (nx * (P.x + GM.x) + ny * (P.y + GM.y) + nz * (P.z + GM.z) + tau * hinv * dq);
+    const T dq = P.w - GM.w;
+    gx += T(0.5) * w * nx * dq;
+    gy += T(0.5) * w * ny * dq;
+    gz += T(0.5) * w * nz * dq;
+    a += T(-0.5) * w * (nx * (P.x + GM.x) + ny * (P.y + GM.y) + nz * (P.z + GM.z) + tau * hinv * dq);
   }
-  Aq[e * NP + n] = weak_divergence<NQ>(vg, gx, gy, gz, a, s_ur, s_us, s_ut, s_D);
+  Aq[e * NP + n] = weak_divergence<NQ, T>(vg, gx, gy, gz, a, s_ur, s_us, s_ut, s_D);
 }
 
 // ---------------------------------------------------------------- rhs boundary data
@@ -263,7 +267,7 @@ ipdg_rhs_bc_kernel(const double* __restrict__ EX, const double* __restrict__ EY,
     a += -w * (nx * dx + ny * dy + nz * dz + tau * hinv * qP);
   }
   const double* vg = vgeo + e * kVgeo * NP + n;
-  rhs[e * NP + n] -= weak_divergence<NQ>(vg, gx, gy, gz, a, s_ur, s_us, s_ut, s_D);
+  rhs[e * NP + n] -= weak_divergence<NQ, double>(vg, gx, gy, gz, a, s_ur, s_us, s_ut, s_D);
 }
 
 // ---------------------------------------------------------------- diagonal
@@ -326,6 +330,18 @@ ipdg_diag_kernel(const double* __restrict__ vgeo, const double* __restrict__ sge
   diag[e * NP + n] = A;
 }
 
+template <int NQ, typename T, typename V4>
+int launch_operator(int64_t E, const T* vgeo, const T* sgeo, const int32_t* vmapP, const int* EToB, const T* D,
+                    T lambda, const T* lambdaE, T tau, const T* q, V4* g4, T* out, cudaStream_t s) {
+  constexpr int NP = NQ * NQ * NQ;
+  if (E <= 0) return LPG_OK;
+  ipdg_gradient_kernel<NQ, T, V4><<<(unsigned)E, NP, 0, s>>>(vgeo, D, q, g4);
+  LPG_LAUNCH_CHECK("ipdg_gradient_kernel");
+  ipdg_ax_kernel<NQ, T, V4><<<(unsigned)E, NP, 0, s>>>(vgeo, sgeo, vmapP, EToB, D, lambda, lambdaE, tau, g4, out);
+  LPG_LAUNCH_CHECK("ipdg_ax_kernel");
+  return LPG_OK;
+}
+
 template <int NQ>
 int launch_all(int which, const IpdgArgs& a, cudaStream_t s) {
   constexpr int NP = NQ * NQ * NQ;
@@ -337,12 +353,8 @@ int launch_all(int which, const IpdgArgs& a, cudaStream_t s) {
       LPG_LAUNCH_CHECK("ipdg_geometry_kernel");
       return LPG_OK;
     case 1:
-      ipdg_gradient_kernel<NQ><<<E, NP, 0, s>>>(a.vgeo, a.D, a.q, a.g4);
-      LPG_LAUNCH_CHECK("ipdg_gradient_kernel");
-      ipdg_ax_kernel<NQ><<<E, NP, 0, s>>>(a.vgeo, a.sgeo, a.vmapP, a.EToB, a.D, a.lambda, a.lambdaE, a.tau, a.g4,
-                                          a.out);
-      LPG_LAUNCH_CHECK("ipdg_ax_kernel");
-      return LPG_OK;
+      return launch_operator<NQ, double, double4_32a>(a.E, a.vgeo, a.sgeo, a.vmapP, a.EToB, a.D, a.lambda, a.lambdaE,
+                                                      a.tau, a.q, a.g4, a.out, s);
     case 2:
       ipdg_rhs_bc_kernel<NQ><<<E, NP, 0, s>>>(a.EX, a.EY, a.EZ, a.r1d, a.vgeo, a.sgeo, a.EToB, a.D, a.tau, a.out);
       LPG_LAUNCH_CHECK("ipdg_rhs_bc_kernel");
@@ -382,6 +394,24 @@ int ipdg_geometry(const IpdgArgs& a, const int32_t* mapP, cudaStream_t s) {
   return LPG_OK;
 }
 int ipdg_operator(const IpdgArgs& a, cudaStream_t s) { return dispatch(1, a, s); }
+int ipdg_operator_f32(const IpdgArgsF32& a, cudaStream_t s) {
+  auto go = [&](auto nq) {
+    constexpr int NQ = decltype(nq)::value;
+    return launch_operator<NQ, float, float4>(a.E, a.vgeo, a.sgeo, a.vmapP, a.EToB, a.D, a.lambda, a.lambdaE, a.tau,
+                                              a.q, a.g4, a.out, s);
+  };
+  switch (a.N) {
+    case 1: return go(std::integral_constant<int, 2>{});
+    case 2: return go(std::integral_constant<int, 3>{});
+    case 3: return go(std::integral_constant<int, 4>{});
+    case 4: return go(std::integral_constant<int, 5>{});
+    case 5: return go(std::integral_constant<int, 6>{});
+    case 6: return go(std::integral_constant<int, 7>{});
+    case 7: return go(std::integral_constant<int, 8>{});
+    case 8: return go(std::integral_constant<int, 9>{});
+    default: return set_error(LPG_ERR_UNSUPPORTED, "IPDG: N must be 1..8");
+  }
+}
 int ipdg_rhs_bc(const IpdgArgs& a, cudaStream_t s) { return dispatch(2, a, s); }
 int ipdg_diagonal(const IpdgArgs& a, cudaStream_t s) { return dispatch(3, a, s); }
 

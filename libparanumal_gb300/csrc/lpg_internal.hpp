@@ -179,6 +179,20 @@ struct IpdgArgs {
   double4_32a* g4 = nullptr;
   double* out = nullptr;
 };
+// the operator on FP32 copies of vgeo, sgeo, D and lambdaE (preconditioner levels)
+struct IpdgArgsF32 {
+  int N = 0;
+  int64_t E = 0;
+  const float *vgeo = nullptr, *sgeo = nullptr, *D = nullptr;
+  const int32_t* vmapP = nullptr;
+  const int* EToB = nullptr;
+  float lambda = 0, tau = 0;
+  const float* lambdaE = nullptr;
+  const float* q = nullptr;
+  float4* g4 = nullptr;
+  float* out = nullptr;
+};
+int ipdg_operator_f32(const IpdgArgsF32& a, cudaStream_t s);
 // vgeo, sgeo (hfac = scratch [E][6 Nfp]); mapP = paired face node of each face node
 int ipdg_geometry(const IpdgArgs& a, const int32_t* mapP, cudaStream_t s);
 int ipdg_operator(const IpdgArgs& a, cudaStream_t s);   // out = A q (q, g4 scratch)

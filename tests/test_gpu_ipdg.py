@@ -132,8 +132,48 @@ def test_ipdg_multigrid_reference_golden_norms(reference_norms, name):
     assert abs(r["norm"] - case["norm"]) < reference_norms["tolerance"], (r["norm"], case["norm"])
 
 
+@pytest.mark.parametrize("name", ["dirichlet_N5", "dirichlet_N1", "periodic_N7", "lognormal_N3", "file_mixed_N4"])
+def test_ipdg_fp32_operator_matches_oracle(tmp_path, name):
+    """FP32 operator of the preconditioner levels (FP32 copies of vgeo/sgeo, float4
+    gradients) against the FP64 oracle applied to the same FP32-rounded input: 1e-5
+    relative to the largest entry (FP32 rounding of ~3 Nq-term sums)."""
+    s = _cases(tmp_path)[name]
+    e = lpg.Elliptic(s)
+    o = Oracle(s)
+    q = np.random.default_rng(11).standard_normal(e.Nglobal).astype(np.float32)
+    Aq = torch.zeros(e.Nglobal, dtype=torch.float32, device="cuda")
+    e.OperatorF32(torch.tensor(q, device="cuda"), Aq)
+    torch.cuda.synchronize()
+    err = rel_err(Aq.cpu().numpy().astype(np.float64), o.operator(q.astype(np.float64)))
+    assert err < 1e-5, err
+    with pytest.raises(RuntimeError):
+        e.OperatorF32(torch.tensor(q, device="cuda"), Aq, bf16geo=True)
+
+
+@pytest.mark.parametrize("name", ["pmg_5_2_1", "pmg_halfdofs_N4_lognormal", "pmg_all_neumann_periodic"])
+def test_ipdg_fp32_multigrid_reaches_the_fp64_solution(name):
+    """PRECONDITIONER PRECISION FP32 on IPDG levels inside the FP64 FPCG: same discrete
+    solution as the oracle (1e-7) in at most two iterations more than the FP64 V-cycle."""
+    s = dict(BASE, **MG_CASES[name])
+    s["LINEAR SOLVER"] = "FPCG"
+    r64 = lpg.Elliptic(s).Run()
+    r32 = lpg.Elliptic(dict(s, **{"PRECONDITIONER PRECISION": "FP32"})).Run(want_solution=True)
+    ro = Oracle(s).run()
+    assert r32["converged"]
+    assert r32["iterations"] <= r64["iterations"] + 2, (r32["iterations"], r64["iterations"])
+    assert rel_err(r32["xL"], ro["xL"]) < 1e-7
+
+
+def test_ipdg_fp32_oas_reference_golden_norm(reference_norms):
+    case = reference_norms["cases"]["testEllipticHex_Ipdg_OAS"]
+    s = dict(golden_case_settings(case), **{"PRECONDITIONER PRECISION": "FP32"})
+    r = lpg.Elliptic(s).Run()
+    assert r["converged"]
+    assert abs(r["norm"] - case["norm"]) < reference_norms["tolerance"], (r["norm"], case["norm"])
+
+
 def test_ipdg_unsupported_combinations_fail_loudly():
-    for over in ({"PRECONDITIONER": "SEMFEM"}, {"PRECONDITIONER": "MULTIGRID", "PRECONDITIONER PRECISION": "FP32"},
+    for over in ({"PRECONDITIONER": "SEMFEM"}, {"PRECONDITIONER": "MULTIGRID", "PRECONDITIONER PRECISION": "BF16GEO"},
                  {"OPERATOR PRECISION": "DF64", "POLYNOMIAL DEGREE": 7}):
         with pytest.raises(RuntimeError):
             lpg.Elliptic(dict(BASE, **over))
