@@ -370,9 +370,10 @@ def run_sequence(a):
 def run_ipdg(a):
     """IPDG operator throughput (DISCRETIZATION = IPDG, gradient + interior-penalty Ax) on an
     nx^3 jittered Dirichlet box at degree N: W warm-up and K timed applications on device
-    vectors larger than L2, CUDA events on the library's stream, for the FP64 operator and
-    the FP32 operator of the preconditioner levels. One JSON line with the algorithmic bytes
-    of the two kernels per node and the HBM fraction they reach."""
+    vectors larger than L2, CUDA events on the library's stream, for the FP64 operator, the
+    same operator in double-FP32 words (DF64) and the FP32 operator of the preconditioner
+    levels. One JSON line with the algorithmic bytes of the two kernels per node and the HBM
+    fraction they reach."""
     import torch
     import libparanumal_gb300 as lpg
     import __graft_entry__ as g
@@ -407,6 +408,16 @@ def run_ipdg(a):
     e1.record(torch_stream)
     torch.cuda.synchronize()
     ms32 = e0.elapsed_time(e1) / a.steps
+    # the FP64 operator in double-FP32 words (OPERATOR PRECISION DF64)
+    for _ in range(max(3, a.warmup)):
+        e.OperatorDF64(q, Aq)
+    torch.cuda.synchronize()
+    e0.record(torch_stream)
+    for _ in range(a.steps):
+        e.OperatorDF64(q, Aq)
+    e1.record(torch_stream)
+    torch.cuda.synchronize()
+    msdw = e0.elapsed_time(e1) / a.steps
     Nq = a.N + 1
     Np, Nfp = Nq ** 3, Nq * Nq
     hbm, hbm_src = measured_peaks()
@@ -425,6 +436,7 @@ def run_ipdg(a):
     out = {"workload": "IPDG operator (gradient + Ax), %d^3 jittered hex, N=%d" % (a.nx, a.N),
            "metric": "ipdg_operator_gdofs", "ndofs": n}
     out.update(line(ms, 8))
+    out["df64"] = line(msdw, 8)
     out["fp32"] = line(ms32, 4)
     print(json.dumps(out), flush=True)
 

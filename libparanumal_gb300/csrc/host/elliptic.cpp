@@ -409,7 +409,29 @@ int Elliptic::make_f32(bool bf16, cudaStream_t s) {
   return LPG_OK;
 }
 
+int Elliptic::OperatorIpdgDW(const double* q, double* Aq, cudaStream_t s) {
+  int rc;
+  const int64_t E = mesh.E, Np = mesh.Np, Nfp = (int64_t)mesh.Nq * mesh.Nq;
+  if (!vgeoDW.p) {
+    if ((rc = vgeoDW.alloc(E * 10 * Np)) || (rc = sgeoDW.alloc(E * 5 * 6 * Nfp)) || (rc = g8.alloc(8 * Nlocal)))
+      return rc;
+    if ((rc = split_to_float2(E * 10 * Np, vgeo.p, vgeoDW.p, s)) ||
+        (rc = split_to_float2(E * 5 * 6 * Nfp, sgeo.p, sgeoDW.p, s)))
+      return rc;
+  }
+  IpdgArgsDW a;
+  a.N = mesh.N; a.E = E;
+  a.vgeo = vgeoDW.p; a.sgeo = sgeoDW.p; a.D = mesh.D_d.p;
+  a.vmapP = vmapP.p; a.EToB = EToB.p;
+  a.lambda = lambda; a.tau = tau;
+  a.lambdaE = hasLambdaE ? lambdaE.p : nullptr;
+  a.q = q; a.out = Aq;
+  a.g8 = reinterpret_cast<float4*>(g8.p);
+  return ipdg_operator_dw(a, s);
+}
+
 int Elliptic::OperatorDW(const double* q, double* Aq, cudaStream_t s) {
+  if (ipdg) return OperatorIpdgDW(q, Aq, s);
   int rc;
   if ((rc = mesh.make_dw(s))) return rc;
   AxArgs<double, float2> a;
@@ -422,6 +444,7 @@ int Elliptic::OperatorDW(const double* q, double* Aq, cudaStream_t s) {
 }
 
 int Elliptic::Operator(const double* q, double* Aq, cudaStream_t s) {
+  if (ipdg && opDW) return OperatorIpdgDW(q, Aq, s);
   if (ipdg) {
     IpdgArgs a = ipdg_args();
     a.q = q;

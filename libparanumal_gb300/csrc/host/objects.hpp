@@ -166,6 +166,9 @@ struct Elliptic {
   double tau = 0;
   DevBuf<double> vgeo, sgeo, g4;
   DevBuf<float> vgeo32, sgeo32, g4_32;  // FP32 copies and gradient scratch (preconditioner levels)
+  DevBuf<float2> vgeoDW, sgeoDW;        // (hi, lo) copies for OPERATOR PRECISION DF64
+  DevBuf<float> g8;                     // double-word gradients, 8 floats per node
+  int OperatorIpdgDW(const double* q, double* Aq, cudaStream_t s);
   DevBuf<int32_t> vmapP;
   DevBuf<int> EToB;
   std::vector<int64_t> EToE_h;     // element neighbours (host), for the matrix probing

@@ -17,6 +17,7 @@
 // order 0, 5, 1, 3, 2, 4, so no two threads write the same value.
 #include <type_traits>
 
+#include "df64.cuh"
 #include "lpg_common.cuh"
 #include "lpg_internal.hpp"
 
@@ -214,6 +215,125 @@ ipdg_ax_kernel(const T* __restrict__ vgeo, const T* __restrict__ sgeo, const int
   Aq[e * NP + n] = weak_divergence<NQ, T>(vg, gx, gy, gz, a, s_ur, s_us, s_ut, s_D);
 }
 
+// ---------------------------------------------------------------- double-word operator
+// OPERATOR PRECISION = DF64: the gradient and operator kernels in double-FP32 words
+// (df64.cuh) on the FP32 pipe, with vgeo and sgeo split once into (hi, lo) pairs and the
+// gradients stored as four words per node (two float4: x.h x.l y.h y.l | z.h z.l w.h w.l).
+// q is split by integer operations; each result is rebuilt as hi + lo in FP64.
+struct dw4 {
+  dw x, y, z, w;
+};
+__device__ __forceinline__ dw4 load_dw4(const float4* __restrict__ g, int64_t node) {
+  const float4 a = g[2 * node], b = g[2 * node + 1];
+  return {{a.x, a.y}, {a.z, a.w}, {b.x, b.y}, {b.z, b.w}};
+}
+__device__ __forceinline__ dw ldw(const float2* __restrict__ p) {
+  const float2 v = *p;
+  return {v.x, v.y};
+}
+__device__ __forceinline__ dw dw_half(float c, dw x) { return {c * x.h, c * x.l}; }   // c = +-0.5: exact
+
+template <int NQ>
+__global__ void __launch_bounds__(NQ * NQ * NQ)
+ipdg_gradient_dw_kernel(const float2* __restrict__ vgeo, const double* __restrict__ Dg, const double* __restrict__ q,
+                        float4* __restrict__ g8) {
+  constexpr int NP = NQ * NQ * NQ, NFP = NQ * NQ;
+  __shared__ dw s_q[NP], s_D[NQ * NQ];
+  const int64_t e = blockIdx.x;
+  const int n = threadIdx.x;
+  if (n < NQ * NQ) s_D[n] = dw_from_double(Dg[n]);
+  const dw qn = dw_from_double(q[e * NP + n]);
+  s_q[n] = qn;
+  __syncthreads();
+  const int i = n % NQ, j = (n / NQ) % NQ, k = n / NFP;
+  dw_acc ar, as, at;
+#pragma unroll
+  for (int m = 0; m < NQ; ++m) {
+    ar.mac(s_D[i * NQ + m], s_q[m + j * NQ + k * NFP]);
+    as.mac(s_D[j * NQ + m], s_q[i + m * NQ + k * NFP]);
+    at.mac(s_D[k * NQ + m], s_q[i + j * NQ + m * NFP]);
+  }
+  const dw qr = ar.get(), qs = as.get(), qt = at.get();
+  const float2* vg = vgeo + e * kVgeo * NP + n;
+  dw_acc ox, oy, oz;
+  ox.mac(ldw(vg + 0 * NP), qr); ox.mac(ldw(vg + 3 * NP), qs); ox.mac(ldw(vg + 6 * NP), qt);
+  oy.mac(ldw(vg + 1 * NP), qr); oy.mac(ldw(vg + 4 * NP), qs); oy.mac(ldw(vg + 7 * NP), qt);
+  oz.mac(ldw(vg + 2 * NP), qr); oz.mac(ldw(vg + 5 * NP), qs); oz.mac(ldw(vg + 8 * NP), qt);
+  const dw gx = ox.get(), gy = oy.get(), gz = oz.get();
+  g8[2 * (e * NP + n)] = make_float4(gx.h, gx.l, gy.h, gy.l);
+  g8[2 * (e * NP + n) + 1] = make_float4(gz.h, gz.l, qn.h, qn.l);
+}
+
+template <int NQ>
+__global__ void __launch_bounds__(NQ * NQ * NQ)
+ipdg_ax_dw_kernel(const float2* __restrict__ vgeo, const float2* __restrict__ sgeo, const int32_t* __restrict__ vmapP,
+                  const int* __restrict__ EToB, const double* __restrict__ Dg, const double lambda,
+                  const double* __restrict__ lambdaE, const double tau, const float4* __restrict__ g8,
+                  double* __restrict__ Aq) {
+  constexpr int NP = NQ * NQ * NQ, NFP = NQ * NQ;
+  __shared__ dw s_ur[NP], s_us[NP], s_ut[NP], s_D[NQ * NQ];
+  const int64_t e = blockIdx.x;
+  const int n = threadIdx.x;
+  if (n < NQ * NQ) s_D[n] = dw_from_double(Dg[n]);
+  const int i = n % NQ, j = (n / NQ) % NQ, k = n / NFP;
+  const float2* vg = vgeo + e * kVgeo * NP + n;
+  const dw4 GM = load_dw4(g8, e * NP + n);
+  const dw JW = ldw(vg + 9 * NP);
+  const dw lam = dw_from_double(lambdaE ? lambdaE[e] : lambda);
+  const dw tauw = dw_from_double(tau);
+  dw gx = dw_mul(JW, GM.x), gy = dw_mul(JW, GM.y), gz = dw_mul(JW, GM.z), a = dw_mul(dw_mul(JW, lam), GM.w);
+  const float2* sg = sgeo + e * kSgeo * 6 * NFP;
+  const int faces[6] = {k == 0 ? 0 : -1, k == NQ - 1 ? 5 : -1, j == 0 ? 1 : -1,
+                        j == NQ - 1 ? 3 : -1, i == NQ - 1 ? 2 : -1, i == 0 ? 4 : -1};
+#pragma unroll
+  for (int q = 0; q < 6; ++q) {
+    const int f = faces[q];
+    if (f < 0) continue;
+    const int col = f * NFP + face_slot<NQ>(f, i, j, k);
+    const dw nx = ldw(sg + 0 * 6 * NFP + col), ny = ldw(sg + 1 * 6 * NFP + col), nz = ldw(sg + 2 * 6 * NFP + col);
+    const dw w = ldw(sg + 3 * 6 * NFP + col), hinv = ldw(sg + 4 * 6 * NFP + col);
+    dw4 P = load_dw4(g8, vmapP[e * 6 * NFP + col]);
+    const int bc = EToB[e * 6 + f];
+    if (bc > 0) {
+      // mirror state 2B - M of the homogeneous boundary state (Dirichlet / Neumann)
+      if (bc == 1) { P.x = GM.x; P.y = GM.y; P.z = GM.z; P.w = dw_neg(GM.w); }
+      else { P.x = dw_neg(GM.x); P.y = dw_neg(GM.y); P.z = dw_neg(GM.z); P.w = GM.w; }
+    }
+    const dw dq = dw_sub(P.w, GM.w);
+    const dw hwdq = dw_half(0.5f, dw_mul(w, dq));
+    gx = dw_add(gx, dw_mul(nx, hwdq));
+    gy = dw_add(gy, dw_mul(ny, hwdq));
+    gz = dw_add(gz, dw_mul(nz, hwdq));
+    dw_acc flux;
+    flux.mac(nx, dw_add(P.x, GM.x));
+    flux.mac(ny, dw_add(P.y, GM.y));
+    flux.mac(nz, dw_add(P.z, GM.z));
+    flux.mac(dw_mul(tauw, hinv), dq);
+    a = dw_add(a, dw_half(-0.5f, dw_mul(w, flux.get())));
+  }
+  // weak divergence
+  {
+    dw_acc r, s2, t;
+    r.mac(ldw(vg + 0 * NP), gx); r.mac(ldw(vg + 1 * NP), gy); r.mac(ldw(vg + 2 * NP), gz);
+    s2.mac(ldw(vg + 3 * NP), gx); s2.mac(ldw(vg + 4 * NP), gy); s2.mac(ldw(vg + 5 * NP), gz);
+    t.mac(ldw(vg + 6 * NP), gx); t.mac(ldw(vg + 7 * NP), gy); t.mac(ldw(vg + 8 * NP), gz);
+    s_ur[n] = r.get();
+    s_us[n] = s2.get();
+    s_ut[n] = t.get();
+  }
+  __syncthreads();
+  dw_acc v;
+  v.h = a.h;
+  v.l = a.l;
+#pragma unroll
+  for (int p = 0; p < NQ; ++p) {
+    v.mac(s_D[p * NQ + i], s_ur[p + j * NQ + k * NFP]);
+    v.mac(s_D[p * NQ + j], s_us[i + p * NQ + k * NFP]);
+    v.mac(s_D[p * NQ + k], s_ut[i + j * NQ + p * NFP]);
+  }
+  Aq[e * NP + n] = dw_to_double(v.get());
+}
+
 // ---------------------------------------------------------------- rhs boundary data
 // rhs -= weak form of the boundary state of u = sin(pi x) sin(pi y) sin(pi z) (Dirichlet value,
 // or the Neumann data of the sine data file) against a zero interior state
@@ -394,6 +514,31 @@ int ipdg_geometry(const IpdgArgs& a, const int32_t* mapP, cudaStream_t s) {
   return LPG_OK;
 }
 int ipdg_operator(const IpdgArgs& a, cudaStream_t s) { return dispatch(1, a, s); }
+int ipdg_operator_dw(const IpdgArgsDW& a, cudaStream_t s) {
+  auto go = [&](auto nq) {
+    constexpr int NQ = decltype(nq)::value;
+    constexpr int NP = NQ * NQ * NQ;
+    if (a.E <= 0) return (int)LPG_OK;
+    const unsigned E = (unsigned)a.E;
+    ipdg_gradient_dw_kernel<NQ><<<E, NP, 0, s>>>(a.vgeo, a.D, a.q, a.g8);
+    LPG_LAUNCH_CHECK("ipdg_gradient_dw_kernel");
+    ipdg_ax_dw_kernel<NQ><<<E, NP, 0, s>>>(a.vgeo, a.sgeo, a.vmapP, a.EToB, a.D, a.lambda, a.lambdaE, a.tau, a.g8,
+                                           a.out);
+    LPG_LAUNCH_CHECK("ipdg_ax_dw_kernel");
+    return (int)LPG_OK;
+  };
+  switch (a.N) {
+    case 1: return go(std::integral_constant<int, 2>{});
+    case 2: return go(std::integral_constant<int, 3>{});
+    case 3: return go(std::integral_constant<int, 4>{});
+    case 4: return go(std::integral_constant<int, 5>{});
+    case 5: return go(std::integral_constant<int, 6>{});
+    case 6: return go(std::integral_constant<int, 7>{});
+    case 7: return go(std::integral_constant<int, 8>{});
+    case 8: return go(std::integral_constant<int, 9>{});
+    default: return set_error(LPG_ERR_UNSUPPORTED, "IPDG: N must be 1..8");
+  }
+}
 int ipdg_operator_f32(const IpdgArgsF32& a, cudaStream_t s) {
   auto go = [&](auto nq) {
     constexpr int NQ = decltype(nq)::value;

@@ -193,6 +193,22 @@ struct IpdgArgsF32 {
   float* out = nullptr;
 };
 int ipdg_operator_f32(const IpdgArgsF32& a, cudaStream_t s);
+// the FP64 operator in double-FP32 words (OPERATOR PRECISION DF64): vgeo and sgeo split
+// into (hi, lo) pairs, gradients as 2 float4 per node, q and out FP64
+struct IpdgArgsDW {
+  int N = 0;
+  int64_t E = 0;
+  const float2 *vgeo = nullptr, *sgeo = nullptr;
+  const double* D = nullptr;
+  const int32_t* vmapP = nullptr;
+  const int* EToB = nullptr;
+  double lambda = 0, tau = 0;
+  const double* lambdaE = nullptr;
+  const double* q = nullptr;
+  float4* g8 = nullptr;
+  double* out = nullptr;
+};
+int ipdg_operator_dw(const IpdgArgsDW& a, cudaStream_t s);
 // vgeo, sgeo (hfac = scratch [E][6 Nfp]); mapP = paired face node of each face node
 int ipdg_geometry(const IpdgArgs& a, const int32_t* mapP, cudaStream_t s);
 int ipdg_operator(const IpdgArgs& a, cudaStream_t s);   // out = A q (q, g4 scratch)

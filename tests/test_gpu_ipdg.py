@@ -150,6 +150,45 @@ def test_ipdg_fp32_operator_matches_oracle(tmp_path, name):
         e.OperatorF32(torch.tensor(q, device="cuda"), Aq, bf16geo=True)
 
 
+@pytest.mark.parametrize("name", CASE_NAMES)
+def test_ipdg_df64_operator_matches_oracle(tmp_path, name):
+    """OPERATOR PRECISION DF64: the operator in double-FP32 words is held to the FP64 bar
+    (1e-12 relative to the largest entry), through the object's Operator and the C entry."""
+    s = dict(_cases(tmp_path)[name], **{"OPERATOR PRECISION": "DF64"})
+    e = lpg.Elliptic(s)
+    o = Oracle(_cases(tmp_path)[name])
+    q = np.random.default_rng(13).standard_normal(e.Nglobal)
+    qd = torch.tensor(q, device="cuda")
+    Aq = torch.zeros(e.Nglobal, dtype=torch.float64, device="cuda")
+    e.Operator(qd, Aq)
+    Aq2 = torch.zeros_like(Aq)
+    e.OperatorDF64(qd, Aq2)
+    torch.cuda.synchronize()
+    ref = o.operator(q)
+    assert rel_err(Aq.cpu().numpy(), ref) < 1e-12
+    assert torch.equal(Aq, Aq2)
+    # scale-independent: 1e-6 q and 1e6 q
+    for scale in (1e-6, 1e6):
+        e.Operator(qd * scale, Aq)
+        torch.cuda.synchronize()
+        assert rel_err(Aq.cpu().numpy(), ref * scale) < 1e-12
+
+
+def test_ipdg_df64_fp32_multigrid_solve_matches_oracle():
+    """FP32 p-levels inside FPCG whose operator runs in double-FP32 words: the oracle's
+    discrete solution (1e-7) in at most two iterations more than the all-FP64 solve."""
+    s = dict(BASE, **MG_CASES["pmg_5_2_1"])
+    s["POLYNOMIAL DEGREE"] = 5
+    ro = Oracle(s).run()
+    r64 = lpg.Elliptic(s).Run()
+    r = lpg.Elliptic(dict(s, **{"PRECONDITIONER PRECISION": "FP32", "OPERATOR PRECISION": "DF64"})).Run(
+        want_solution=True)
+    assert r["converged"]
+    assert r["iterations"] <= r64["iterations"] + 2
+    assert rel_err(r["xL"], ro["xL"]) < 1e-7
+    assert abs(r["norm"] - ro["norm"]) < 1e-9 * ro["norm"]
+
+
 @pytest.mark.parametrize("name", ["pmg_5_2_1", "pmg_halfdofs_N4_lognormal", "pmg_all_neumann_periodic"])
 def test_ipdg_fp32_multigrid_reaches_the_fp64_solution(name):
     """PRECONDITIONER PRECISION FP32 on IPDG levels inside the FP64 FPCG: same discrete
@@ -174,6 +213,6 @@ def test_ipdg_fp32_oas_reference_golden_norm(reference_norms):
 
 def test_ipdg_unsupported_combinations_fail_loudly():
     for over in ({"PRECONDITIONER": "SEMFEM"}, {"PRECONDITIONER": "MULTIGRID", "PRECONDITIONER PRECISION": "BF16GEO"},
-                 {"OPERATOR PRECISION": "DF64", "POLYNOMIAL DEGREE": 7}):
+                 {"OPERATOR PRECISION": "FP32"}):
         with pytest.raises(RuntimeError):
             lpg.Elliptic(dict(BASE, **over))
