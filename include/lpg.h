@@ -168,8 +168,8 @@ int lpg_elliptic_operator_f32(lpg_elliptic *e, const float *q, float *Aq, int bf
 /* The same operator (device vectors, FP64 in and out) computed in double-FP32 words on
  * the FP32 pipe -- no reference counterpart. 48-bit significands; agrees with the FP64
  * operator to about 1e-14 relative (sums with absolute error ~2^-48 of the magnitudes
- * summed); inputs below 2^-74 in magnitude lose the low word. N = 3 or 7 for
- * CONTINUOUS, any N for DISCRETIZATION = IPDG. The setting
+ * summed); inputs below 2^-74 in magnitude lose the low word. Any N (CONTINUOUS and
+ * IPDG). The setting
  * [OPERATOR PRECISION] DF64 makes every FP64 operator application of the object use it. */
 int lpg_elliptic_operator_df64(lpg_elliptic *e, const double *q, double *Aq, void *stream);
 /* elliptic_t::Operator (ellipticOperator.cpp:29-106) on HOST arrays, as the OCCA Serial

@@ -728,10 +728,95 @@ ax_hex_dw_kernel(const int64_t Nelements, const int32_t* __restrict__ elementLis
     if (r_id[k] >= 0) atomicAdd(out + r_id[k], dw_to_double(r_Aq[k]));
 }
 
+// Double-word operator for the degrees without an even-odd kernel (N = 1, 2, 4, 5, 6, 8):
+// one thread per node, EPB elements per CTA (at least 128 threads), direct Nq-term
+// contractions through shared memory, the same df64 building blocks and FP64 assembly.
+template <int NQ>
+constexpr int dw_generic_epb() {
+  return (NQ * NQ * NQ >= 128) ? 1 : 128 / (NQ * NQ * NQ);
+}
+
+template <int NQ>
+__global__ void __launch_bounds__(NQ * NQ * NQ * dw_generic_epb<NQ>())
+ax_hex_dw_generic_kernel(const int64_t Nelements, const int32_t* __restrict__ elementList,
+                         const int32_t* __restrict__ g2l, const dw* __restrict__ ggeo, const int64_t geoStride,
+                         const dw* __restrict__ wJ, const int64_t wJStride, const double* __restrict__ Dg,
+                         const double lambda, const double* __restrict__ lambdaE, const double* __restrict__ q,
+                         double* __restrict__ out) {
+  constexpr int NP = NQ * NQ * NQ, NFP = NQ * NQ, EPB = dw_generic_epb<NQ>();
+  __shared__ dw s_D[NQ * NQ];
+  __shared__ dw s_q[EPB][NP], s_r[EPB][NP], s_s[EPB][NP], s_t[EPB][NP];
+  const int el = threadIdx.x / NP, n = threadIdx.x % NP;
+  for (int t = threadIdx.x; t < NQ * NQ; t += blockDim.x) s_D[t] = dw_from_double(Dg[t]);
+  int64_t e = (int64_t)blockIdx.x * EPB + el;
+  const bool active = e < Nelements;
+  if (active && elementList) e = elementList[e];
+  if (!active) e = 0;
+  const int32_t id = active ? g2l[e * NP + n] : -1;
+  const dw qn = dw_from_double(id >= 0 ? q[id] : 0.0);
+  s_q[el][n] = qn;
+  __syncthreads();
+  const int i = n % NQ, j = (n / NQ) % NQ, k = n / NFP;
+  dw_acc ar, as, at;
+#pragma unroll
+  for (int m = 0; m < NQ; ++m) {
+    ar.mac(s_D[i * NQ + m], s_q[el][m + j * NQ + k * NFP]);
+    as.mac(s_D[j * NQ + m], s_q[el][i + m * NQ + k * NFP]);
+    at.mac(s_D[k * NQ + m], s_q[el][i + j * NQ + m * NFP]);
+  }
+  const dw qr = ar.get(), qs = as.get(), qt = at.get();
+  const dw* gp = ggeo + e * geoStride + n;
+  const dw G00 = gp[0 * NP], G01 = gp[1 * NP], G02 = gp[2 * NP], G11 = gp[3 * NP], G12 = gp[4 * NP],
+           G22 = gp[5 * NP];
+  const dw GwJ = wJ[e * wJStride + n];
+  const dw lam = dw_from_double((lambdaE && active) ? lambdaE[e] : lambda);
+  {
+    dw_acc gr, gs, gt;
+    gr.mac(G00, qr); gr.mac(G01, qs); gr.mac(G02, qt);
+    gs.mac(G01, qr); gs.mac(G11, qs); gs.mac(G12, qt);
+    gt.mac(G02, qr); gt.mac(G12, qs); gt.mac(G22, qt);
+    s_r[el][n] = gr.get();
+    s_s[el][n] = gs.get();
+    s_t[el][n] = gt.get();
+  }
+  const dw mass = dw_mul(dw_mul(GwJ, lam), qn);
+  __syncthreads();
+  dw_acc v;
+  v.h = mass.h;
+  v.l = mass.l;
+#pragma unroll
+  for (int p = 0; p < NQ; ++p) {
+    v.mac(s_D[p * NQ + i], s_r[el][p + j * NQ + k * NFP]);
+    v.mac(s_D[p * NQ + j], s_s[el][i + p * NQ + k * NFP]);
+    v.mac(s_D[p * NQ + k], s_t[el][i + j * NQ + p * NFP]);
+  }
+  if (id >= 0) atomicAdd(out + id, dw_to_double(v.get()));
+}
+
+template <int NQ>
+static int launch_dw_generic(const AxArgs<double, float2>& a, cudaStream_t s) {
+  constexpr int EPB = dw_generic_epb<NQ>();
+  const int64_t blocks = (a.Nelements + EPB - 1) / EPB;
+  ax_hex_dw_generic_kernel<NQ><<<(unsigned)blocks, NQ * NQ * NQ * EPB, 0, s>>>(
+      a.Nelements, a.elementList, a.g2l, reinterpret_cast<const dw*>(a.ggeo), a.geoStride,
+      reinterpret_cast<const dw*>(a.wJ), a.wJStride, a.D, a.lambda, a.lambdaE, a.q, a.out);
+  LPG_LAUNCH_CHECK("ax_hex_dw_generic_kernel");
+  return LPG_OK;
+}
+
 int ax_hex_dw(const AxArgs<double, float2>& a, cudaStream_t s) {
   if (a.Nelements <= 0) return LPG_OK;
-  if (a.N != 3 && a.N != 7) return set_error(LPG_ERR_UNSUPPORTED, "double-word operator: N must be 3 or 7");
+  if (a.N < 1 || a.N > 8) return set_error(LPG_ERR_UNSUPPORTED, "double-word operator: N must be 1..8");
   if (a.Nglobal > 0) LPG_CUDA_TRY(cudaMemsetAsync(a.out, 0, sizeof(double) * a.Nglobal, s));
+  switch (a.N) {
+    case 1: return launch_dw_generic<2>(a, s);
+    case 2: return launch_dw_generic<3>(a, s);
+    case 4: return launch_dw_generic<5>(a, s);
+    case 5: return launch_dw_generic<6>(a, s);
+    case 6: return launch_dw_generic<7>(a, s);
+    case 8: return launch_dw_generic<9>(a, s);
+    default: break;
+  }
   if (a.N == 7) {
     const int64_t blocks = (a.Nelements + 3) / 4;
     ax_hex_dw_kernel<8><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(

@@ -120,8 +120,6 @@ int build(lpg_elliptic* h) {
   Elliptic* el = h->el.get();
   const std::string opPrec = S.get("OPERATOR PRECISION", "FP64");
   if (opPrec != "FP64" && opPrec != "DF64") return set_error(LPG_ERR_SETTINGS, "OPERATOR PRECISION must be FP64 or DF64");
-  if (opPrec == "DF64" && !c.ipdg && N != 3 && N != 7)
-    return set_error(LPG_ERR_UNSUPPORTED, "OPERATOR PRECISION DF64 needs POLYNOMIAL DEGREE 3 or 7 (CONTINUOUS)");
   el->opDW = (opPrec == "DF64");
   // right-hand side data
   const std::string rhsField = S.get("RHS FIELD", "SINE");
@@ -410,8 +408,6 @@ extern "C" int lpg_elliptic_operator(lpg_elliptic* e, const double* q, double* A
 
 extern "C" int lpg_elliptic_operator_df64(lpg_elliptic* e, const double* q, double* Aq, void* stream) {
   if (!e || !q || !Aq) return set_error(LPG_ERR_INVALID, "null argument");
-  if (!e->el->ipdg && e->el->mesh.N != 3 && e->el->mesh.N != 7)
-    return set_error(LPG_ERR_UNSUPPORTED, "DF64 operator: N must be 3 or 7 (CONTINUOUS)");
   LPG_GUARD_BEGIN
   return e->el->OperatorDW(q, Aq, pick(e, stream));
   LPG_GUARD_END

@@ -234,7 +234,7 @@ __device__ __forceinline__ dw ldw(const float2* __restrict__ p) {
 __device__ __forceinline__ dw dw_half(float c, dw x) { return {c * x.h, c * x.l}; }   // c = +-0.5: exact
 
 template <int NQ>
-__global__ void __launch_bounds__(NQ * NQ * NQ)
+__global__ void __launch_bounds__(NQ * NQ * NQ, (NQ <= 8 ? 4 : 1))
 ipdg_gradient_dw_kernel(const float2* __restrict__ vgeo, const double* __restrict__ Dg, const double* __restrict__ q,
                         float4* __restrict__ g8) {
   constexpr int NP = NQ * NQ * NQ, NFP = NQ * NQ;
@@ -265,7 +265,7 @@ ipdg_gradient_dw_kernel(const float2* __restrict__ vgeo, const double* __restric
 }
 
 template <int NQ>
-__global__ void __launch_bounds__(NQ * NQ * NQ)
+__global__ void __launch_bounds__(NQ * NQ * NQ, (NQ <= 8 ? 3 : 1))
 ipdg_ax_dw_kernel(const float2* __restrict__ vgeo, const float2* __restrict__ sgeo, const int32_t* __restrict__ vmapP,
                   const int* __restrict__ EToB, const double* __restrict__ Dg, const double lambda,
                   const double* __restrict__ lambdaE, const double tau, const float4* __restrict__ g8,

@@ -32,7 +32,8 @@ struct AxArgs {
 template <typename T, typename G>
 int ax_hex(const AxArgs<T, G>& a, AxMode mode, cudaStream_t s);
 // Assembled operator in double-FP32 ("double-word") arithmetic: FP64 q and Aq, geometric
-// factors pre-split into (hi, lo) float pairs ([e][7][Np] float2), N = 3 or 7.
+// factors pre-split into (hi, lo) float pairs ([e][7][Np] float2), N = 1..8 (even-odd
+// kernels for N = 3 and 7).
 int ax_hex_dw(const AxArgs<double, float2>& a, cudaStream_t s);
 // FP64 -> (hi, lo) float pairs (hi = x rounded to FP32, lo = x - hi rounded to FP32)
 int split_to_float2(int64_t n, const double* x, float2* y, cudaStream_t s);

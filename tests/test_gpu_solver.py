@@ -116,6 +116,18 @@ def test_double_word_outer_operator_solve(prec):
     assert abs(r["norm"] - ro["norm"]) < 1e-9 * ro["norm"]
 
 
+def test_double_word_outer_operator_solve_degree5():
+    """OPERATOR PRECISION DF64 at a degree without an even-odd kernel (N = 5, p-MG 5,2,1,
+    FP32 p-levels): the FP64 method's iterations (+-1), error and norm."""
+    base = dict(MG, **{"POLYNOMIAL DEGREE": 5, "MULTIGRID DEGREES": "5,2,1"})
+    r = lpg.Elliptic(dict(base, **{"OPERATOR PRECISION": "DF64", "PRECONDITIONER PRECISION": "FP32"})).Run()
+    ro = Oracle(base).run()
+    assert r["converged"]
+    assert abs(r["iterations"] - ro["iterations"]) <= 1, (r["iterations"], ro["iterations"])
+    assert abs(r["error"] - ro["error"]) <= 0.01 * ro["error"]
+    assert abs(r["norm"] - ro["norm"]) < 1e-9 * ro["norm"]
+
+
 @pytest.mark.parametrize("over", [{}, {"LAMBDA FIELD": "LOGNORMAL", "LAMBDA SEED": 2},
                                   {"LAMBDA": 0.0, "BOX BOUNDARY FLAG": -1}], ids=["jittered", "lognormal", "periodic"])
 def test_semfem_preconditioner_matches_oracle(over):
