@@ -574,7 +574,7 @@ ax_hex_eo_kernel(const int64_t Nelements, const int32_t* __restrict__ elementLis
 // ([e][7][Np] hi/lo pairs, the same 8 bytes per value as FP64); each local result is
 // rebuilt exactly as FP64 hi + lo (one FP64 add) and assembled with FP64 atomics.
 template <int NQ>
-__global__ void __launch_bounds__(NQ * NQ * elems_per_block<NQ>(), 2)
+__global__ void __launch_bounds__(NQ * NQ * elems_per_block<NQ>(), (NQ == 4 ? 3 : 2))
 ax_hex_dw_kernel(const int64_t Nelements, const int32_t* __restrict__ elementList,
                  const int32_t* __restrict__ g2l, const dw* __restrict__ ggeo, const int64_t geoStride,
                  const dw* __restrict__ wJ, const int64_t wJStride, const double* __restrict__ Dg,
