@@ -48,6 +48,26 @@ __device__ __forceinline__ int face_slot(int f, int i, int j, int k) {
   return (f == 0 || f == 5) ? i + j * NQ : (f == 1 || f == 3) ? i + k * NQ : j + k * NQ;
 }
 
+// volume node of face slot b on face f (the inverse of face_slot)
+template <int NQ>
+__device__ __forceinline__ int face_node(int f, int b) {
+  constexpr int NFP = NQ * NQ;
+  const int a = b % NQ, c = b / NQ;
+  switch (f) {
+    case 0: return b;
+    case 5: return b + (NQ - 1) * NFP;
+    case 1: return a + c * NFP;
+    case 3: return a + (NQ - 1) * NQ + c * NFP;
+    case 2: return (NQ - 1) + a * NQ + c * NFP;
+    default: return a * NQ + c * NFP;   // face 4
+  }
+}
+
+// face of the opposite-face pair handled in phase ph (pairs (0,5), (1,3), (2,4)) by half h
+__device__ __forceinline__ int phase_face(int ph, int h) {
+  return ph == 0 ? (h ? 5 : 0) : ph == 1 ? (h ? 3 : 1) : (h ? 4 : 2);
+}
+
 // ---------------------------------------------------------------- geometry
 template <int NQ>
 __global__ void __launch_bounds__(NQ * NQ * NQ)
@@ -172,47 +192,68 @@ __device__ __forceinline__ T weak_divergence(const T* vg, T gx, T gy, T gz, T ac
 }
 
 // ---------------------------------------------------------------- operator
+// The face terms run in three phases, one per opposite-face pair (0,5), (1,3), (2,4): the
+// 2 Nfp face slots of a pair sit on consecutive threads (whole warps), no node lies on both
+// faces of a pair, and the node accumulators live in shared memory, so every node receives
+// its face terms in the reference's order 0,5,1,3,2,4 without divergent per-node face loops.
 template <int NQ, typename T, typename V4>
 __global__ void __launch_bounds__(NQ * NQ * NQ)
 ipdg_ax_kernel(const T* __restrict__ vgeo, const T* __restrict__ sgeo, const int32_t* __restrict__ vmapP,
                const int* __restrict__ EToB, const T* __restrict__ Dg, const T lambda,
                const T* __restrict__ lambdaE, const T tau, const V4* __restrict__ g4, T* __restrict__ Aq) {
   constexpr int NP = NQ * NQ * NQ, NFP = NQ * NQ;
-  __shared__ T s_ur[NP], s_us[NP], s_ut[NP], s_D[NQ * NQ];
+  static_assert(2 * NFP <= NP, "a face pair needs 2 Nfp threads");
+  __shared__ V4 s_M[NP], s_acc[NP];
+  __shared__ T s_D[NQ * NQ];
   const int64_t e = blockIdx.x;
   const int n = threadIdx.x;
   if (n < NQ * NQ) s_D[n] = Dg[n];
-  const int i = n % NQ, j = (n / NQ) % NQ, k = n / NFP;
   const T* vg = vgeo + e * kVgeo * NP + n;
-  const V4 GM = g4[e * NP + n];
-  const T JW = vg[9 * NP];
-  const T lam = lambdaE ? lambdaE[e] : lambda;
-  T gx = JW * GM.x, gy = JW * GM.y, gz = JW * GM.z, a = JW * lam * GM.w;
-  const T* sg = sgeo + e * kSgeo * 6 * NFP;
-  const int faces[6] = {k == 0 ? 0 : -1, k == NQ - 1 ? 5 : -1, j == 0 ? 1 : -1,
-                        j == NQ - 1 ? 3 : -1, i == NQ - 1 ? 2 : -1, i == 0 ? 4 : -1};
-#pragma unroll
-  for (int q = 0; q < 6; ++q) {
-    const int f = faces[q];
-    if (f < 0) continue;
-    const int col = f * NFP + face_slot<NQ>(f, i, j, k);
-    const T nx = sg[0 * 6 * NFP + col], ny = sg[1 * 6 * NFP + col], nz = sg[2 * 6 * NFP + col];
-    const T w = sg[3 * 6 * NFP + col], hinv = sg[4 * 6 * NFP + col];
-    V4 P = g4[vmapP[e * 6 * NFP + col]];
-    const int bc = EToB[e * 6 + f];
-    if (bc > 0) {
-      // homogeneous boundary state B (Dirichlet: q = 0, grad kept; Neumann: q kept, grad = 0),
-      // then the mirror state 2B - M
-      if (bc == 1) { P.x = GM.x; P.y = GM.y; P.z = GM.z; P.w = -GM.w; }
-      else { P.x = -GM.x; P.y = -GM.y; P.z = -GM.z; P.w = GM.w; }
-    }
-    const T dq = P.w - GM.w;
-    gx += T(0.5) * w * nx * dq;
-    gy += T(0.5) * w * ny * dq;
-    gz += T(0.5) * w * nz * dq;
-    a += T(-0.5) * w * (nx * (P.x + GM.x) + ny * (P.y + GM.y) + nz * (P.z + GM.z) + tau * hinv * dq);
+  {
+    const V4 GM = g4[e * NP + n];
+    const T JW = vg[9 * NP];
+    const T lam = lambdaE ? lambdaE[e] : lambda;
+    V4 acc;
+    acc.x = JW * GM.x;
+    acc.y = JW * GM.y;
+    acc.z = JW * GM.z;
+    acc.w = JW * lam * GM.w;
+    s_M[n] = GM;
+    s_acc[n] = acc;
   }
-  Aq[e * NP + n] = weak_divergence<NQ, T>(vg, gx, gy, gz, a, s_ur, s_us, s_ut, s_D);
+  __syncthreads();
+  const T* sg = sgeo + e * kSgeo * 6 * NFP;
+#pragma unroll
+  for (int ph = 0; ph < 3; ++ph) {
+    if (n < 2 * NFP) {
+      const int h = n / NFP, b = n - h * NFP;
+      const int f = phase_face(ph, h);
+      const int node = face_node<NQ>(f, b);
+      const int col = f * NFP + b;
+      const T nx = sg[0 * 6 * NFP + col], ny = sg[1 * 6 * NFP + col], nz = sg[2 * 6 * NFP + col];
+      const T w = sg[3 * 6 * NFP + col], hinv = sg[4 * 6 * NFP + col];
+      const V4 GM = s_M[node];
+      V4 P = g4[vmapP[e * 6 * NFP + col]];
+      const int bc = EToB[e * 6 + f];
+      if (bc > 0) {
+        // homogeneous boundary state B (Dirichlet: q = 0, grad kept; Neumann: q kept, grad = 0),
+        // then the mirror state 2B - M
+        if (bc == 1) { P.x = GM.x; P.y = GM.y; P.z = GM.z; P.w = -GM.w; }
+        else { P.x = -GM.x; P.y = -GM.y; P.z = -GM.z; P.w = GM.w; }
+      }
+      V4 acc = s_acc[node];
+      const T dq = P.w - GM.w;
+      acc.x += T(0.5) * w * nx * dq;
+      acc.y += T(0.5) * w * ny * dq;
+      acc.z += T(0.5) * w * nz * dq;
+      acc.w += T(-0.5) * w * (nx * (P.x + GM.x) + ny * (P.y + GM.y) + nz * (P.z + GM.z) + tau * hinv * dq);
+      s_acc[node] = acc;
+    }
+    __syncthreads();
+  }
+  const V4 acc = s_acc[n];
+  T* s_w = reinterpret_cast<T*>(s_M);   // the traces are no longer read: 3 Np values of scratch
+  Aq[e * NP + n] = weak_divergence<NQ, T>(vg, acc.x, acc.y, acc.z, acc.w, s_w, s_w + NP, s_w + 2 * NP, s_D);
 }
 
 // ---------------------------------------------------------------- double-word operator
@@ -271,60 +312,76 @@ ipdg_ax_dw_kernel(const float2* __restrict__ vgeo, const float2* __restrict__ sg
                   const double* __restrict__ lambdaE, const double tau, const float4* __restrict__ g8,
                   double* __restrict__ Aq) {
   constexpr int NP = NQ * NQ * NQ, NFP = NQ * NQ;
-  __shared__ dw s_ur[NP], s_us[NP], s_ut[NP], s_D[NQ * NQ];
+  static_assert(2 * NFP <= NP, "a face pair needs 2 Nfp threads");
+  __shared__ dw4 s_M[NP], s_acc[NP];
+  __shared__ dw s_D[NQ * NQ];
   const int64_t e = blockIdx.x;
   const int n = threadIdx.x;
   if (n < NQ * NQ) s_D[n] = dw_from_double(Dg[n]);
   const int i = n % NQ, j = (n / NQ) % NQ, k = n / NFP;
   const float2* vg = vgeo + e * kVgeo * NP + n;
-  const dw4 GM = load_dw4(g8, e * NP + n);
-  const dw JW = ldw(vg + 9 * NP);
-  const dw lam = dw_from_double(lambdaE ? lambdaE[e] : lambda);
-  const dw tauw = dw_from_double(tau);
-  dw gx = dw_mul(JW, GM.x), gy = dw_mul(JW, GM.y), gz = dw_mul(JW, GM.z), a = dw_mul(dw_mul(JW, lam), GM.w);
-  const float2* sg = sgeo + e * kSgeo * 6 * NFP;
-  const int faces[6] = {k == 0 ? 0 : -1, k == NQ - 1 ? 5 : -1, j == 0 ? 1 : -1,
-                        j == NQ - 1 ? 3 : -1, i == NQ - 1 ? 2 : -1, i == 0 ? 4 : -1};
-#pragma unroll
-  for (int q = 0; q < 6; ++q) {
-    const int f = faces[q];
-    if (f < 0) continue;
-    const int col = f * NFP + face_slot<NQ>(f, i, j, k);
-    const dw nx = ldw(sg + 0 * 6 * NFP + col), ny = ldw(sg + 1 * 6 * NFP + col), nz = ldw(sg + 2 * 6 * NFP + col);
-    const dw w = ldw(sg + 3 * 6 * NFP + col), hinv = ldw(sg + 4 * 6 * NFP + col);
-    dw4 P = load_dw4(g8, vmapP[e * 6 * NFP + col]);
-    const int bc = EToB[e * 6 + f];
-    if (bc > 0) {
-      // mirror state 2B - M of the homogeneous boundary state (Dirichlet / Neumann)
-      if (bc == 1) { P.x = GM.x; P.y = GM.y; P.z = GM.z; P.w = dw_neg(GM.w); }
-      else { P.x = dw_neg(GM.x); P.y = dw_neg(GM.y); P.z = dw_neg(GM.z); P.w = GM.w; }
-    }
-    const dw dq = dw_sub(P.w, GM.w);
-    const dw hwdq = dw_half(0.5f, dw_mul(w, dq));
-    gx = dw_add(gx, dw_mul(nx, hwdq));
-    gy = dw_add(gy, dw_mul(ny, hwdq));
-    gz = dw_add(gz, dw_mul(nz, hwdq));
-    dw_acc flux;
-    flux.mac(nx, dw_add(P.x, GM.x));
-    flux.mac(ny, dw_add(P.y, GM.y));
-    flux.mac(nz, dw_add(P.z, GM.z));
-    flux.mac(dw_mul(tauw, hinv), dq);
-    a = dw_add(a, dw_half(-0.5f, dw_mul(w, flux.get())));
+  {
+    const dw4 GM = load_dw4(g8, e * NP + n);
+    const dw JW = ldw(vg + 9 * NP);
+    const dw lam = dw_from_double(lambdaE ? lambdaE[e] : lambda);
+    s_M[n] = GM;
+    s_acc[n] = {dw_mul(JW, GM.x), dw_mul(JW, GM.y), dw_mul(JW, GM.z), dw_mul(dw_mul(JW, lam), GM.w)};
   }
+  __syncthreads();
+  // face terms by opposite-face pairs, as in ipdg_ax_kernel
+  const float2* sg = sgeo + e * kSgeo * 6 * NFP;
+  const dw tauw = dw_from_double(tau);
+#pragma unroll
+  for (int ph = 0; ph < 3; ++ph) {
+    if (n < 2 * NFP) {
+      const int h = n / NFP, b = n - h * NFP;
+      const int f = phase_face(ph, h);
+      const int node = face_node<NQ>(f, b);
+      const int col = f * NFP + b;
+      const dw nx = ldw(sg + 0 * 6 * NFP + col), ny = ldw(sg + 1 * 6 * NFP + col), nz = ldw(sg + 2 * 6 * NFP + col);
+      const dw w = ldw(sg + 3 * 6 * NFP + col), hinv = ldw(sg + 4 * 6 * NFP + col);
+      const dw4 GM = s_M[node];
+      dw4 P = load_dw4(g8, vmapP[e * 6 * NFP + col]);
+      const int bc = EToB[e * 6 + f];
+      if (bc > 0) {
+        // mirror state 2B - M of the homogeneous boundary state (Dirichlet / Neumann)
+        if (bc == 1) { P.x = GM.x; P.y = GM.y; P.z = GM.z; P.w = dw_neg(GM.w); }
+        else { P.x = dw_neg(GM.x); P.y = dw_neg(GM.y); P.z = dw_neg(GM.z); P.w = GM.w; }
+      }
+      dw4 acc = s_acc[node];
+      const dw dq = dw_sub(P.w, GM.w);
+      const dw hwdq = dw_half(0.5f, dw_mul(w, dq));
+      acc.x = dw_add(acc.x, dw_mul(nx, hwdq));
+      acc.y = dw_add(acc.y, dw_mul(ny, hwdq));
+      acc.z = dw_add(acc.z, dw_mul(nz, hwdq));
+      dw_acc flux;
+      flux.mac(nx, dw_add(P.x, GM.x));
+      flux.mac(ny, dw_add(P.y, GM.y));
+      flux.mac(nz, dw_add(P.z, GM.z));
+      flux.mac(dw_mul(tauw, hinv), dq);
+      acc.w = dw_add(acc.w, dw_half(-0.5f, dw_mul(w, flux.get())));
+      s_acc[node] = acc;
+    }
+    __syncthreads();
+  }
+  const dw4 acc = s_acc[n];
+  dw* s_ur = reinterpret_cast<dw*>(s_M);   // the traces are no longer read: 3 Np words of scratch
+  dw* s_us = s_ur + NP;
+  dw* s_ut = s_us + NP;
   // weak divergence
   {
     dw_acc r, s2, t;
-    r.mac(ldw(vg + 0 * NP), gx); r.mac(ldw(vg + 1 * NP), gy); r.mac(ldw(vg + 2 * NP), gz);
-    s2.mac(ldw(vg + 3 * NP), gx); s2.mac(ldw(vg + 4 * NP), gy); s2.mac(ldw(vg + 5 * NP), gz);
-    t.mac(ldw(vg + 6 * NP), gx); t.mac(ldw(vg + 7 * NP), gy); t.mac(ldw(vg + 8 * NP), gz);
+    r.mac(ldw(vg + 0 * NP), acc.x); r.mac(ldw(vg + 1 * NP), acc.y); r.mac(ldw(vg + 2 * NP), acc.z);
+    s2.mac(ldw(vg + 3 * NP), acc.x); s2.mac(ldw(vg + 4 * NP), acc.y); s2.mac(ldw(vg + 5 * NP), acc.z);
+    t.mac(ldw(vg + 6 * NP), acc.x); t.mac(ldw(vg + 7 * NP), acc.y); t.mac(ldw(vg + 8 * NP), acc.z);
     s_ur[n] = r.get();
     s_us[n] = s2.get();
     s_ut[n] = t.get();
   }
   __syncthreads();
   dw_acc v;
-  v.h = a.h;
-  v.l = a.l;
+  v.h = acc.w.h;
+  v.l = acc.w.l;
 #pragma unroll
   for (int p = 0; p < NQ; ++p) {
     v.mac(s_D[p * NQ + i], s_ur[p + j * NQ + k * NFP]);
