@@ -68,6 +68,29 @@ __device__ __forceinline__ int phase_face(int ph, int h) {
   return ph == 0 ? (h ? 5 : 0) : ph == 1 ? (h ? 3 : 1) : (h ? 4 : 2);
 }
 
+// Dynamic shared memory of the ax kernels (S = value, S4 = 4-vector): own traces, node
+// accumulators, the neighbour traces and surface factors of the 6 Nfp face slots (slot
+// t = phase * 2 Nfp + half * Nfp + b, the order the face phases use), and D.
+template <int NQ, typename S, typename S4>
+struct AxSmem {
+  static constexpr int NP = NQ * NQ * NQ, NFP = NQ * NQ, NS = 6 * NFP;
+  static constexpr size_t oM = 0;
+  static constexpr size_t oAcc = oM + sizeof(S4) * NP;
+  static constexpr size_t oP = oAcc + sizeof(S4) * NP;
+  static constexpr size_t oF = oP + sizeof(S4) * NS;
+  static constexpr size_t oD = oF + sizeof(S) * 5 * NS;
+  static constexpr size_t bytes = oD + sizeof(S) * NFP;
+};
+
+// slot t -> (face, face slot b)
+template <int NQ>
+__device__ __forceinline__ void slot_face(int t, int& f, int& b) {
+  constexpr int NFP = NQ * NQ;
+  const int ph = t / (2 * NFP), r = t - ph * 2 * NFP, h = r / NFP;
+  f = phase_face(ph, h);
+  b = r - h * NFP;
+}
+
 // ---------------------------------------------------------------- geometry
 template <int NQ>
 __global__ void __launch_bounds__(NQ * NQ * NQ)
@@ -203,11 +226,27 @@ ipdg_ax_kernel(const T* __restrict__ vgeo, const T* __restrict__ sgeo, const int
                const T* __restrict__ lambdaE, const T tau, const V4* __restrict__ g4, T* __restrict__ Aq) {
   constexpr int NP = NQ * NQ * NQ, NFP = NQ * NQ;
   static_assert(2 * NFP <= NP, "a face pair needs 2 Nfp threads");
-  __shared__ V4 s_M[NP], s_acc[NP];
-  __shared__ T s_D[NQ * NQ];
+  using L = AxSmem<NQ, T, V4>;
+  extern __shared__ __align__(32) unsigned char smem[];
+  V4* s_M = reinterpret_cast<V4*>(smem + L::oM);
+  V4* s_acc = reinterpret_cast<V4*>(smem + L::oAcc);
+  V4* s_P = reinterpret_cast<V4*>(smem + L::oP);
+  T* s_F = reinterpret_cast<T*>(smem + L::oF);
+  T* s_D = reinterpret_cast<T*>(smem + L::oD);
   const int64_t e = blockIdx.x;
   const int n = threadIdx.x;
   if (n < NQ * NQ) s_D[n] = Dg[n];
+  // stage the surface factors and neighbour traces of all 6 Nfp face slots at once, so the
+  // dependent vmapP -> trace loads are in flight together with the volume loads
+  const T* sg = sgeo + e * kSgeo * 6 * NFP;
+  for (int t = n; t < 6 * NFP; t += NP) {
+    int f, b;
+    slot_face<NQ>(t, f, b);
+    const int col = f * NFP + b;
+#pragma unroll
+    for (int c = 0; c < kSgeo; ++c) s_F[c * 6 * NFP + t] = sg[c * 6 * NFP + col];
+    s_P[t] = g4[vmapP[e * 6 * NFP + col]];
+  }
   const T* vg = vgeo + e * kVgeo * NP + n;
   {
     const V4 GM = g4[e * NP + n];
@@ -222,18 +261,17 @@ ipdg_ax_kernel(const T* __restrict__ vgeo, const T* __restrict__ sgeo, const int
     s_acc[n] = acc;
   }
   __syncthreads();
-  const T* sg = sgeo + e * kSgeo * 6 * NFP;
 #pragma unroll
   for (int ph = 0; ph < 3; ++ph) {
     if (n < 2 * NFP) {
-      const int h = n / NFP, b = n - h * NFP;
-      const int f = phase_face(ph, h);
+      const int t = ph * 2 * NFP + n;
+      int f, b;
+      slot_face<NQ>(t, f, b);
       const int node = face_node<NQ>(f, b);
-      const int col = f * NFP + b;
-      const T nx = sg[0 * 6 * NFP + col], ny = sg[1 * 6 * NFP + col], nz = sg[2 * 6 * NFP + col];
-      const T w = sg[3 * 6 * NFP + col], hinv = sg[4 * 6 * NFP + col];
+      const T nx = s_F[0 * 6 * NFP + t], ny = s_F[1 * 6 * NFP + t], nz = s_F[2 * 6 * NFP + t];
+      const T w = s_F[3 * 6 * NFP + t], hinv = s_F[4 * 6 * NFP + t];
       const V4 GM = s_M[node];
-      V4 P = g4[vmapP[e * 6 * NFP + col]];
+      V4 P = s_P[t];
       const int bc = EToB[e * 6 + f];
       if (bc > 0) {
         // homogeneous boundary state B (Dirichlet: q = 0, grad kept; Neumann: q kept, grad = 0),
@@ -313,11 +351,26 @@ ipdg_ax_dw_kernel(const float2* __restrict__ vgeo, const float2* __restrict__ sg
                   double* __restrict__ Aq) {
   constexpr int NP = NQ * NQ * NQ, NFP = NQ * NQ;
   static_assert(2 * NFP <= NP, "a face pair needs 2 Nfp threads");
-  __shared__ dw4 s_M[NP], s_acc[NP];
-  __shared__ dw s_D[NQ * NQ];
+  using L = AxSmem<NQ, dw, dw4>;
+  extern __shared__ __align__(32) unsigned char smem[];
+  dw4* s_M = reinterpret_cast<dw4*>(smem + L::oM);
+  dw4* s_acc = reinterpret_cast<dw4*>(smem + L::oAcc);
+  dw4* s_P = reinterpret_cast<dw4*>(smem + L::oP);
+  dw* s_F = reinterpret_cast<dw*>(smem + L::oF);
+  dw* s_D = reinterpret_cast<dw*>(smem + L::oD);
   const int64_t e = blockIdx.x;
   const int n = threadIdx.x;
   if (n < NQ * NQ) s_D[n] = dw_from_double(Dg[n]);
+  // stage surface factors and neighbour traces of all face slots, as in ipdg_ax_kernel
+  const float2* sg = sgeo + e * kSgeo * 6 * NFP;
+  for (int t = n; t < 6 * NFP; t += NP) {
+    int f, b;
+    slot_face<NQ>(t, f, b);
+    const int col = f * NFP + b;
+#pragma unroll
+    for (int c = 0; c < kSgeo; ++c) s_F[c * 6 * NFP + t] = ldw(sg + c * 6 * NFP + col);
+    s_P[t] = load_dw4(g8, vmapP[e * 6 * NFP + col]);
+  }
   const int i = n % NQ, j = (n / NQ) % NQ, k = n / NFP;
   const float2* vg = vgeo + e * kVgeo * NP + n;
   {
@@ -329,19 +382,18 @@ ipdg_ax_dw_kernel(const float2* __restrict__ vgeo, const float2* __restrict__ sg
   }
   __syncthreads();
   // face terms by opposite-face pairs, as in ipdg_ax_kernel
-  const float2* sg = sgeo + e * kSgeo * 6 * NFP;
   const dw tauw = dw_from_double(tau);
 #pragma unroll
   for (int ph = 0; ph < 3; ++ph) {
     if (n < 2 * NFP) {
-      const int h = n / NFP, b = n - h * NFP;
-      const int f = phase_face(ph, h);
+      const int t = ph * 2 * NFP + n;
+      int f, b;
+      slot_face<NQ>(t, f, b);
       const int node = face_node<NQ>(f, b);
-      const int col = f * NFP + b;
-      const dw nx = ldw(sg + 0 * 6 * NFP + col), ny = ldw(sg + 1 * 6 * NFP + col), nz = ldw(sg + 2 * 6 * NFP + col);
-      const dw w = ldw(sg + 3 * 6 * NFP + col), hinv = ldw(sg + 4 * 6 * NFP + col);
+      const dw nx = s_F[0 * 6 * NFP + t], ny = s_F[1 * 6 * NFP + t], nz = s_F[2 * 6 * NFP + t];
+      const dw w = s_F[3 * 6 * NFP + t], hinv = s_F[4 * 6 * NFP + t];
       const dw4 GM = s_M[node];
-      dw4 P = load_dw4(g8, vmapP[e * 6 * NFP + col]);
+      dw4 P = s_P[t];
       const int bc = EToB[e * 6 + f];
       if (bc > 0) {
         // mirror state 2B - M of the homogeneous boundary state (Dirichlet / Neumann)
@@ -514,7 +566,13 @@ int launch_operator(int64_t E, const T* vgeo, const T* sgeo, const int32_t* vmap
   if (E <= 0) return LPG_OK;
   ipdg_gradient_kernel<NQ, T, V4><<<(unsigned)E, NP, 0, s>>>(vgeo, D, q, g4);
   LPG_LAUNCH_CHECK("ipdg_gradient_kernel");
-  ipdg_ax_kernel<NQ, T, V4><<<(unsigned)E, NP, 0, s>>>(vgeo, sgeo, vmapP, EToB, D, lambda, lambdaE, tau, g4, out);
+  constexpr size_t smem = AxSmem<NQ, T, V4>::bytes;
+  static bool configured = false;   // per instantiation: dynamic shared memory opt-in
+  if (!configured) {
+    LPG_CUDA_TRY(cudaFuncSetAttribute(ipdg_ax_kernel<NQ, T, V4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    configured = true;
+  }
+  ipdg_ax_kernel<NQ, T, V4><<<(unsigned)E, NP, smem, s>>>(vgeo, sgeo, vmapP, EToB, D, lambda, lambdaE, tau, g4, out);
   LPG_LAUNCH_CHECK("ipdg_ax_kernel");
   return LPG_OK;
 }
@@ -579,8 +637,14 @@ int ipdg_operator_dw(const IpdgArgsDW& a, cudaStream_t s) {
     const unsigned E = (unsigned)a.E;
     ipdg_gradient_dw_kernel<NQ><<<E, NP, 0, s>>>(a.vgeo, a.D, a.q, a.g8);
     LPG_LAUNCH_CHECK("ipdg_gradient_dw_kernel");
-    ipdg_ax_dw_kernel<NQ><<<E, NP, 0, s>>>(a.vgeo, a.sgeo, a.vmapP, a.EToB, a.D, a.lambda, a.lambdaE, a.tau, a.g8,
-                                           a.out);
+    constexpr size_t smem = AxSmem<NQ, dw, dw4>::bytes;
+    static bool configured = false;   // per instantiation: dynamic shared memory opt-in
+    if (!configured) {
+      LPG_CUDA_TRY(cudaFuncSetAttribute(ipdg_ax_dw_kernel<NQ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      configured = true;
+    }
+    ipdg_ax_dw_kernel<NQ><<<E, NP, smem, s>>>(a.vgeo, a.sgeo, a.vmapP, a.EToB, a.D, a.lambda, a.lambdaE, a.tau, a.g8,
+                                              a.out);
     LPG_LAUNCH_CHECK("ipdg_ax_dw_kernel");
     return (int)LPG_OK;
   };
