@@ -46,7 +46,7 @@ def parse():
     ap.add_argument("--N", type=int, default=7)
     ap.add_argument("--cpu-sample-nx", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--e2e-steps", type=int, default=12)
     ap.add_argument("--prec", default="f64", choices=["f64", "df64", "f32", "bf16g"],
                     help="operator variant timed in the Ax workload (headline: f64)")
     ap.add_argument("--solve", action="store_true", help="time-to-tolerance of the p-MG FPCG solve instead")
@@ -540,7 +540,7 @@ def main():
     prec_name = {"f64": "FP64", "df64": "FP64", "f32": "FP32", "bf16g": "BF16GEO"}[a.prec]
     qh = qin.cpu().pin_memory()
     yh = torch.empty_like(qh).pin_memory()
-    for _ in range(2):
+    for _ in range(3):
         e.OperatorHost(qh, yh, prec_name)
     dev_out = yout.cpu()
     e2e_check = float((yh - dev_out).abs().max() / dev_out.abs().max())

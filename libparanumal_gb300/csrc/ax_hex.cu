@@ -962,6 +962,28 @@ int ax_hex(const AxArgs<T, G>& a, AxMode mode, cudaStream_t s) {
   return set_error(LPG_ERR_INVALID, "ax: bad mode");
 }
 
+int ax_wave_elements(int N, bool dw) {
+  int dev = 0, sms = 0, per = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return 1;
+  cudaError_t e = cudaErrorInvalidValue;
+  int epb = 1;
+  if (N == 7) {
+    epb = elems_per_block<8>();
+    e = dw ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, ax_hex_dw_kernel<8>, 8 * 8 * epb, 0)
+           : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, ax_hex_eo_kernel<8>, 8 * 8 * epb, 0);
+  } else if (N == 3) {
+    epb = elems_per_block<4>();
+    e = dw ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, ax_hex_dw_kernel<4>, 4 * 4 * epb, 0)
+           : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, ax_hex_eo_kernel<4>, 4 * 4 * epb, 0);
+  }
+  if (e != cudaSuccess || per < 1) {
+    cudaGetLastError();
+    return 1;
+  }
+  return sms * per * epb;
+}
+
 template int ax_hex<double, double>(const AxArgs<double, double>&, AxMode, cudaStream_t);
 template int ax_hex<float, float>(const AxArgs<float, float>&, AxMode, cudaStream_t);
 template int ax_hex<float, __nv_bfloat16>(const AxArgs<float, __nv_bfloat16>&, AxMode, cudaStream_t);

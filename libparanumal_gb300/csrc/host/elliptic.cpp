@@ -503,11 +503,17 @@ int Elliptic::BuildPipe(cudaStream_t s) {
   if (pipe) return LPG_OK;
   auto p = std::make_unique<HostPipe>();
   const int64_t E = mesh.E;
-  // at most 32 chunks of at least 4096 elements (a chunk still fills every SM)
+  // at most 32 chunks of at least 4096 elements (a chunk still fills every SM). For the
+  // FP64 operator, whose kernel time bounds the pipeline, the boundaries are rounded up to
+  // whole waves of the kernel so no chunk ends in a partly filled wave (64^3, N=7: 12.48 ->
+  // 12.05 ms per call); the double-word and FP32 pipelines are bound by the copies and keep
+  // even chunks (aligned, the double-word one was 3 % slower).
   p->K = (int)std::max<int64_t>(1, std::min<int64_t>(32, E / 4096));
   const int K = p->K;
+  const int64_t wave = opDW ? 1 : std::max(1, ax_wave_elements(mesh.N, false));
   p->e0.resize(K + 1);
-  for (int c = 0; c <= K; ++c) p->e0[c] = E * c / K;
+  for (int c = 0; c <= K; ++c) p->e0[c] = std::min<int64_t>(E, (E * c / K + wave - 1) / wave * wave);
+  p->e0[K] = E;
   std::vector<int32_t> lo(std::max<int64_t>(E, 1)), hi(std::max<int64_t>(E, 1));
   if (E > 0) {
     DevBuf<int32_t> dlo, dhi;
