@@ -142,6 +142,9 @@ int lpg_elliptic_destroy(lpg_elliptic *e);
 #define LPG_INFO_FALLBACKS 11      /* of those, redone with the plain smoother */
 #define LPG_INFO_HOST_CHUNKS 12    /* element chunks of the host-buffer operator (0 before its first call) */
 #define LPG_INFO_IG_HISTORY 13     /* current dimension of the initial-guess history */
+#define LPG_INFO_OPERATOR_APPLICATIONS 14 /* fine-level operator applications (FP64, double-word
+                                             and FP32) since creation: outer Krylov, smoother,
+                                             residual and setup applications */
 int64_t lpg_elliptic_info(const lpg_elliptic *e, int what);
 
 /* Copy a named setup array to host memory: "GlobalToLocal" (int32), "ownerLocal" (int32),

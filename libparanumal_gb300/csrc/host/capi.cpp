@@ -310,6 +310,7 @@ extern "C" int64_t lpg_elliptic_info(const lpg_elliptic* e, int what) {
     case LPG_INFO_FALLBACKS: return e->precon ? e->precon->fallbacks() : 0;
     case LPG_INFO_HOST_CHUNKS: return e->el->pipe ? e->el->pipe->K : 0;
     case LPG_INFO_IG_HISTORY: return e->ig ? e->ig->history() : 0;
+    case LPG_INFO_OPERATOR_APPLICATIONS: return e->el->nOps;
     default: return -1;
   }
 }

@@ -444,6 +444,7 @@ int Elliptic::OperatorDW(const double* q, double* Aq, cudaStream_t s) {
 }
 
 int Elliptic::Operator(const double* q, double* Aq, cudaStream_t s) {
+  ++nOps;
   if (ipdg && opDW) return OperatorIpdgDW(q, Aq, s);
   if (ipdg) {
     IpdgArgs a = ipdg_args();
@@ -462,6 +463,7 @@ int Elliptic::Operator(const double* q, double* Aq, cudaStream_t s) {
 }
 
 int Elliptic::OperatorF32(const float* q, float* Aq, Prec prec, cudaStream_t s) {
+  ++nOps;
   const int64_t Np = mesh.Np;
   if (ipdg) {
     if (prec != Prec::F32 || !vgeo32.p) return set_error(LPG_ERR_UNSUPPORTED, "IPDG: FP32 operator not prepared");

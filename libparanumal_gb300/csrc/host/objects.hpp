@@ -169,6 +169,7 @@ struct Elliptic {
   DevBuf<float2> vgeoDW, sgeoDW;        // (hi, lo) copies for OPERATOR PRECISION DF64
   DevBuf<float> g8;                     // double-word gradients, 8 floats per node
   int OperatorIpdgDW(const double* q, double* Aq, cudaStream_t s);
+  int64_t nOps = 0;   // applications through Operator and OperatorF32 (any precision)
   DevBuf<int32_t> vmapP;
   DevBuf<int> EToB;
   std::vector<int64_t> EToE_h;     // element neighbours (host), for the matrix probing

@@ -40,3 +40,13 @@ def test_null_arguments_are_rejected(L):
 
 def test_version(L):
     assert b"sm_103a" in L.lpg_version()
+
+
+def test_info_keys_match_the_header():
+    """The Python object's info() names map to the LPG_INFO_* values include/lpg.h defines."""
+    import os
+    import re
+    import libparanumal_gb300 as lpg
+    header = open(os.path.join(os.path.dirname(__file__), "..", "include", "lpg.h")).read()
+    defs = {m.group(1).lower(): int(m.group(2)) for m in re.finditer(r"#define LPG_INFO_(\w+) (\d+)", header)}
+    assert defs == lpg.INFO

@@ -72,6 +72,17 @@ MG = dict(config1(), **{"BOX NX": 6, "BOX NY": 5, "BOX NZ": 4, "POLYNOMIAL DEGRE
                         "PARALMOND AGGREGATION": "SMOOTHED"})
 
 
+def test_fine_operator_applications_per_iteration():
+    """FPCG + p-MG with Chebyshev degree 2: per iteration one outer application and six in
+    the V-cycle's fine level (pre-smoothing 2, residual 1, post-smoothing 1 + 2)."""
+    e = lpg.Elliptic(MG)
+    n0 = e.info("operator_applications")
+    r = e.Run()
+    ops = e.info("operator_applications") - n0
+    assert r["converged"]
+    assert 7 * r["iterations"] - 6 <= ops <= 7 * r["iterations"] + 2, (ops, r["iterations"])
+
+
 def test_pmg_fp64_iterations_match_oracle():
     r = lpg.Elliptic(MG).Run()
     ro = Oracle(MG).run()
