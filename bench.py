@@ -199,11 +199,15 @@ def run_solves(a):
     on a jittered box with the manufactured sine solution, for each preconditioner
     precision. One JSON line; setup is outside the timed window (ellipticRun.cpp:190-210).
     fine_ax counts the fine-level operator applications of the Run (right-hand-side
-    lifting, outer Krylov and smoother), in any precision."""
+    lifting, outer Krylov and smoother), in any precision; rel_diff_vs_fp64_solution is the
+    relative 2-norm difference of the local solution from the FP64 method's (when FP64 is
+    listed first)."""
+    import numpy as np
     import libparanumal_gb300 as lpg
     import __graft_entry__ as g
     g.build()
     res = {}
+    x64 = None   # local solution of the FP64 method (when FP64 is the first precision)
     for prec in a.solve_precs.split(","):
         t0 = time.time()
         # "P+DF64": preconditioner precision P, FP64 operator applications in double-FP32 words
@@ -215,16 +219,25 @@ def run_solves(a):
         e = lpg.Elliptic(solve_settings(a.nx, a.N, base, **extra))
         setup = time.time() - t0
         runs, ops = [], []
-        for _ in range(a.solve_reps):
+        for rep in range(a.solve_reps):
             n0 = e.info("operator_applications")
-            runs.append(e.Run())
+            # the first Run also returns the local solution (downloaded after the library's
+            # timed window) for the comparison with the FP64 solution
+            runs.append(e.Run(want_solution=(rep == 0)))
             ops.append(e.info("operator_applications") - n0)
+        xL = runs[0].pop("xL")
+        for r in runs[1:]:
+            r.pop("xL", None)
+        if prec == "FP64":
+            x64 = xL
         ibest = min(range(len(runs)), key=lambda i: runs[i]["solve_seconds"])
         best = runs[ibest]
         res[prec] = {"solve_seconds": best["solve_seconds"], "iterations": best["iterations"],
                      "error_vs_manufactured": best["error"], "norm": best["norm"],
                      "converged": best["converged"], "setup_seconds": setup,
                      "fine_ax": ops[ibest], "fine_ax_per_iteration": ops[ibest] / max(1, best["iterations"]),
+                     "rel_diff_vs_fp64_solution": (None if x64 is None else
+                                                   float(np.linalg.norm(xL - x64) / np.linalg.norm(x64))),
                      "mg_plevels": e.info("mg_plevels"), "amg_levels": e.info("mg_amglevels"),
                      "coarse_n": e.info("coarse_n"), "nglobal": e.Nglobal}
         e.close()
