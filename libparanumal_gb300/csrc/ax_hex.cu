@@ -399,7 +399,8 @@ __device__ __forceinline__ void eo_sync(const int el) {
   else __syncwarp();                                    // Nq = 4: an element is half a warp
 }
 
-template <int NQ>
+// MASS = false: lambda == 0 and no lambda field, the mass term and its wJ reads are left out
+template <int NQ, bool MASS = true>
 __global__ void __launch_bounds__(NQ * NQ * elems_per_block<NQ>(), 3)
 ax_hex_eo_kernel(const int64_t Nelements, const int32_t* __restrict__ elementList,
                  const int32_t* __restrict__ g2l, const double* __restrict__ ggeo, const int64_t geoStride,
@@ -493,7 +494,7 @@ ax_hex_eo_kernel(const int64_t Nelements, const int32_t* __restrict__ elementLis
     if (active) {
       G00 = gp[0 * NP + off]; G01 = gp[1 * NP + off]; G02 = gp[2 * NP + off];
       G11 = gp[3 * NP + off]; G12 = gp[4 * NP + off]; G22 = gp[5 * NP + off];
-      GwJ = wp[off];
+      if constexpr (MASS) GwJ = wp[off];
     }
     // even/odd values of q along i (row j) and along j (column i)
     const double v = r_q[k];
@@ -517,7 +518,6 @@ ax_hex_eo_kernel(const int64_t Nelements, const int32_t* __restrict__ elementLis
     const double Gqr = G00 * qr + G01 * qs + G02 * qtk;
     const double Gqs = G01 * qr + G11 * qs + G12 * qtk;
     s_gt[k][tid] = G02 * qr + G12 * qs + G22 * qtk;
-    const double mass = GwJ * lam * v;
     // even/odd values of Gqr along i and of Gqs along j for the transposed derivatives
     const double pr2 = __shfl_xor_sync(FULL, Gqr, NQ - 1);
     const double ps2 = __shfl_xor_sync(FULL, Gqs, 2 * NQ);
@@ -535,7 +535,10 @@ ax_hex_eo_kernel(const int64_t Nelements, const int32_t* __restrict__ elementLis
       *dst1 = B - A;
     }
     eo_sync<NQ>(el);
-    r_Aq[k] = mass + s_dr[el][j][i] + s_ds[el][j][i];
+    // the mass term lambda wJ q folded into the sum as one FMA
+    const double sum = s_dr[el][j][i] + s_ds[el][j][i];
+    if constexpr (MASS) r_Aq[k] = fma(GwJ * lam, v, sum);
+    else r_Aq[k] = sum;
   }
 
   // transposed t-direction: r_Aq[t] += sum_m D[m][t] Gqt[m], even/odd
@@ -916,9 +919,14 @@ static int launch_ax(const AxArgs<T, G>& a, cudaStream_t s) {
       return e && !std::strcmp(e, "direct");
     }();
     if (!direct) {
-      ax_hex_eo_kernel<NQ><<<(unsigned)blocks, block, 0, s>>>(a.Nelements, a.elementList, a.g2l, a.ggeo,
-                                                               a.geoStride, a.wJ, a.wJStride, a.D, a.lambda,
-                                                               a.lambdaE, a.q, a.out);
+      if (a.lambda == 0.0 && !a.lambdaE)
+        ax_hex_eo_kernel<NQ, false><<<(unsigned)blocks, block, 0, s>>>(a.Nelements, a.elementList, a.g2l, a.ggeo,
+                                                                      a.geoStride, a.wJ, a.wJStride, a.D, a.lambda,
+                                                                      a.lambdaE, a.q, a.out);
+      else
+        ax_hex_eo_kernel<NQ, true><<<(unsigned)blocks, block, 0, s>>>(a.Nelements, a.elementList, a.g2l, a.ggeo,
+                                                                     a.geoStride, a.wJ, a.wJStride, a.D, a.lambda,
+                                                                     a.lambdaE, a.q, a.out);
       LPG_LAUNCH_CHECK("ax_hex_eo_kernel");
       return LPG_OK;
     }
