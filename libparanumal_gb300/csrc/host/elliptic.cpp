@@ -557,7 +557,6 @@ template <typename T, typename Launch>
 static int run_pipe(HostPipe& p, const T* qh, T* Aqh, T* dq, T* dAq, int64_t Nglobal, cudaStream_t s,
                     Launch&& launch) {
   auto body = [&]() -> int {
-    LPG_CUDA_TRY(cudaMemsetAsync(dAq, 0, sizeof(T) * Nglobal, s));
     int64_t up = 0;
     for (int c = 0; c < p.K; ++c) {
       const int64_t end = p.inEnd[c];
@@ -566,8 +565,13 @@ static int run_pipe(HostPipe& p, const T* qh, T* Aqh, T* dq, T* dAq, int64_t Ngl
       up = std::max(up, end);
       LPG_CUDA_TRY(cudaEventRecord(p.inReady[c], p.h2d));
     }
-    int64_t down = 0;
+    // chunk c reads and accumulates only into dofs below inEnd[c] (its elements' dofs), so
+    // Aq is zeroed piece by piece ahead of each chunk instead of in one pass up front
+    int64_t down = 0, zeroed = 0;
     for (int c = 0; c < p.K; ++c) {
+      const int64_t zend = std::max<int64_t>(zeroed, p.inEnd[c]);
+      if (zend > zeroed) LPG_CUDA_TRY(cudaMemsetAsync(dAq + zeroed, 0, sizeof(T) * (zend - zeroed), s));
+      zeroed = zend;
       LPG_CUDA_TRY(cudaStreamWaitEvent(s, p.inReady[c], 0));
       const int rc = launch(p.e0[c], p.e0[c + 1]);
       if (rc) return rc;
