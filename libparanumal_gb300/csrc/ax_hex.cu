@@ -193,7 +193,8 @@ __device__ __forceinline__ float row_dot(const float* __restrict__ row, const fl
   return acc;
 }
 
-template <int NQ, typename T, typename G, int EPB, int STAGES, bool PF = false>
+// MASS = false: lambda == 0 and no lambda field, the wJ row is neither copied nor used
+template <int NQ, typename T, typename G, int EPB, int STAGES, bool PF = false, bool MASS = true>
 __global__ void __launch_bounds__(NQ * NQ * EPB)
 ax_hex_staged_kernel(const int64_t Nelements, const int32_t* __restrict__ elementList,
                      const int32_t* __restrict__ g2l, const G* __restrict__ ggeo, const int64_t geoStride,
@@ -234,7 +235,7 @@ ax_hex_staged_kernel(const int64_t Nelements, const int32_t* __restrict__ elemen
           const int64_t e = elementList ? (int64_t)elementList[ei] : ei;
           unsigned char* dst = base + le * L::ELEM_BYTES;
 #pragma unroll
-          for (int comp = 0; comp < 7; ++comp) {
+          for (int comp = 0; comp < (MASS ? 7 : 6); ++comp) {
             const unsigned char* src =
                 (comp < 6) ? reinterpret_cast<const unsigned char*>(ggeo + e * geoStride + (int64_t)comp * NP)
                            : reinterpret_cast<const unsigned char*>(wJ + e * wJStride);
@@ -325,7 +326,8 @@ ax_hex_staged_kernel(const int64_t Nelements, const int32_t* __restrict__ elemen
       const float G00 = geo_to_float(sg[0 * NP + off]), G01 = geo_to_float(sg[1 * NP + off]);
       const float G02 = geo_to_float(sg[2 * NP + off]), G11 = geo_to_float(sg[3 * NP + off]);
       const float G12 = geo_to_float(sg[4 * NP + off]), G22 = geo_to_float(sg[5 * NP + off]);
-      const float GwJ = geo_to_float(sg[6 * NP + off]);
+      float GwJ = 0.f;
+      if constexpr (MASS) GwJ = geo_to_float(sg[6 * NP + off]);
       const int b = k & 1;
       s_q[b][el][j][i] = r_q[k];
       s_qT[b][el][i][j] = r_q[k];
@@ -335,7 +337,8 @@ ax_hex_staged_kernel(const int64_t Nelements, const int32_t* __restrict__ elemen
       s_GqsT[b][el][i][j] = G01 * qr + G11 * qs + G12 * qt[k];
       s_Gqr[b][el][j][i] = G00 * qr + G01 * qs + G02 * qt[k];
       Gqt[k] = G02 * qr + G12 * qs + G22 * qt[k];
-      float Auk = GwJ * lam * r_q[k];
+      float Auk = 0.f;
+      if constexpr (MASS) Auk = GwJ * lam * r_q[k];
       elem_sync<NQ>(el);
       Auk += row_dot<NQ, VEC>(&s_GqsT[b][el][i][0], DTj);       // sum_m D[m][j] Gqs(i,m)
       Auk += row_dot<NQ, VEC>(&s_Gqr[b][el][j][0], DTi);        // sum_m D[m][i] Gqr(m,j)
@@ -835,14 +838,14 @@ int ax_hex_dw(const AxArgs<double, float2>& a, cudaStream_t s) {
   return LPG_OK;
 }
 
-template <int NQ, typename T, typename G, int EPB, int STAGES, bool PF = false>
+template <int NQ, typename T, typename G, int EPB, int STAGES, bool PF = false, bool MASS = true>
 static int launch_staged(const AxArgs<T, G>& a, cudaStream_t s) {
   using L = StagedLayout<NQ, G>;
   constexpr int smem = STAGES * EPB * L::ELEM_BYTES;
   static int configured = -1;   // per instantiation: dynamic shared memory opt-in
   static int ctasPerSM = 1;
   static int numSMs = 152;
-  auto kern = ax_hex_staged_kernel<NQ, T, G, EPB, STAGES, PF>;
+  auto kern = ax_hex_staged_kernel<NQ, T, G, EPB, STAGES, PF, MASS>;
   if (configured < 0) {
     LPG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     int dev = 0;
@@ -902,8 +905,12 @@ static int launch_ax(const AxArgs<T, G>& a, cudaStream_t s) {
       else if (v == 122) return launch_staged<NQ, T, G, 2, 2, true>(a, s);
       // measured best at N=7: FP32 geometry with the next group's q gathered half-way
       // through the current group (0.997 vs 1.112 ms at 64^3); BF16 geometry without it
-      else if constexpr (std::is_same<G, float>::value) return launch_staged<NQ, T, G, 2, 2, true>(a, s);
-      else return launch_staged<NQ, T, G, 2, 2>(a, s);
+      // (lambda = 0 without a lambda field: the instantiation without the mass term and wJ copy)
+      const bool noMass = (a.lambda == 0 && !a.lambdaE);
+      if constexpr (std::is_same<G, float>::value)
+        return noMass ? launch_staged<NQ, T, G, 2, 2, true, false>(a, s) : launch_staged<NQ, T, G, 2, 2, true>(a, s);
+      else
+        return noMass ? launch_staged<NQ, T, G, 2, 2, false, false>(a, s) : launch_staged<NQ, T, G, 2, 2>(a, s);
     }
   }
   constexpr int EPB = elems_per_block<NQ>();

@@ -154,12 +154,14 @@ def test_reduced_precision_operator(prec, tol):
     assert err < tol, err
 
 
+@pytest.mark.parametrize("lam", [1.0, 0.0])
 @pytest.mark.parametrize("bf16", [False, True])
-def test_reduced_precision_operator_many_groups(bf16):
+def test_reduced_precision_operator_many_groups(bf16, lam):
     """16384 elements: every persistent CTA of the staged FP32 / BF16-geometry kernel
     walks many element groups through its shared-memory ring (the small cases give a
-    CTA one group). Checked against the oracle on three consecutive applications."""
-    cfg = box(**{"BOX NX": 32, "BOX NY": 32, "BOX NZ": 16})
+    CTA one group). Checked against the oracle on three consecutive applications;
+    lambda = 0 runs the instantiation that neither copies nor uses wJ."""
+    cfg = box(**{"BOX NX": 32, "BOX NY": 32, "BOX NZ": 16, "LAMBDA": lam})
     e = lpg.Elliptic(cfg)
     o = Oracle(cfg)
     rng = np.random.default_rng(21)
