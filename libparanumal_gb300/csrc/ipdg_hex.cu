@@ -191,6 +191,70 @@ ipdg_gradient_kernel(const T* __restrict__ vgeo, const T* __restrict__ Dg, const
   g4[e * NP + n] = o;
 }
 
+// FP64 gradient with the even-odd split of D (Nq even; D[N-a][N-m] = -D[a][m] on GLL
+// points). Along each direction node i and its mirror N-i form a pair: with e_m = q_m +
+// q_{N-m}, o_m = q_m - q_{N-m} (m < Nq/2) and Dp, Dm the even and odd halves of D, the
+// lower node of the pair dots row min(i, N-i) of Dp with e, the upper one that row of Dm
+// with o, and the partial sums A, B are exchanged through shared memory: d(i) = A + B,
+// d(N-i) = B - A. Per node and direction: 1 + Nq/2 + 1 FP64 instructions instead of Nq.
+// Every selection between the two halves is an index, so warps do not diverge.
+template <int NQ>
+__global__ void __launch_bounds__(NQ * NQ * NQ)
+ipdg_gradient_eo_kernel(const double* __restrict__ vgeo, const double* __restrict__ Dg,
+                        const double* __restrict__ q, double4_32a* __restrict__ g4) {
+  constexpr int NP = NQ * NQ * NQ, NFP = NQ * NQ, H = NQ / 2, N = NQ - 1;
+  static_assert(NQ % 2 == 0, "even-odd gradient: Nq even");
+  __shared__ double s_q[NP];
+  __shared__ double s_eo[3][NP];       // e (lower half of each line) / o (upper half) per direction
+  __shared__ double s_x[3][NP];        // partial sums for the pair exchange
+  __shared__ double s_DpDm[2 * H * H]; // rows of Dp, then rows of Dm
+  const int64_t e = blockIdx.x;
+  const int n = threadIdx.x;
+  const int i = n % NQ, j = (n / NQ) % NQ, k = n / NFP;
+  if (n < H * H) {
+    const int a = n / H, m = n % H;
+    const double d0 = Dg[a * NQ + m], d1 = Dg[a * NQ + N - m];
+    s_DpDm[n] = 0.5 * (d0 + d1);
+    s_DpDm[H * H + n] = 0.5 * (d0 - d1);
+  }
+  const double qn = q[e * NP + n];
+  s_q[n] = qn;
+  __syncthreads();
+  // mirror nodes along r, s, t and the sign that forms e (lower half) or o (upper half)
+  const int pi = n + (N - 2 * i), pj = n + (N - 2 * j) * NQ, pk = n + (N - 2 * k) * NFP;
+  const double si = i < H ? 1.0 : -1.0, sj = j < H ? 1.0 : -1.0, sk = k < H ? 1.0 : -1.0;
+  s_eo[0][n] = fma(si, qn, s_q[pi]);   // i < H: e_i;  i >= H: o_{N-i} = q_{N-i} - q_i
+  s_eo[1][n] = fma(sj, qn, s_q[pj]);
+  s_eo[2][n] = fma(sk, qn, s_q[pk]);
+  __syncthreads();
+  const double* ci = s_DpDm + (i < H ? i * H : H * H + (N - i) * H);
+  const double* cj = s_DpDm + (j < H ? j * H : H * H + (N - j) * H);
+  const double* ck = s_DpDm + (k < H ? k * H : H * H + (N - k) * H);
+  double ar = 0, as = 0, at = 0;
+#pragma unroll
+  for (int m = 0; m < H; ++m) {
+    // e_m sits at line position m, o_m at position N - m
+    const int mi = i < H ? m : N - m, mj = j < H ? m : N - m, mk = k < H ? m : N - m;
+    ar = fma(ci[m], s_eo[0][mi + j * NQ + k * NFP], ar);
+    as = fma(cj[m], s_eo[1][i + mj * NQ + k * NFP], as);
+    at = fma(ck[m], s_eo[2][i + j * NQ + mk * NFP], at);
+  }
+  s_x[0][n] = ar;
+  s_x[1][n] = as;
+  s_x[2][n] = at;
+  __syncthreads();
+  const double qr = fma(si, s_x[0][pi], ar);   // lower: A + B, upper: B - A
+  const double qs = fma(sj, s_x[1][pj], as);
+  const double qt = fma(sk, s_x[2][pk], at);
+  const double* vg = vgeo + e * kVgeo * NP + n;
+  double4_32a o;
+  o.x = vg[0 * NP] * qr + vg[3 * NP] * qs + vg[6 * NP] * qt;
+  o.y = vg[1 * NP] * qr + vg[4 * NP] * qs + vg[7 * NP] * qt;
+  o.z = vg[2 * NP] * qr + vg[5 * NP] * qs + vg[8 * NP] * qt;
+  o.w = qn;
+  g4[e * NP + n] = o;
+}
+
 // ---------------------------------------------------------------- weak divergence (shared by Ax and rhs)
 // out_n = acc_n + sum_p D[p][i] ur(p,j,k) + D[p][j] us(i,p,k) + D[p][k] ut(i,j,p), with (ur, us, ut)
 // = (grad r, grad s, grad t) . (gx, gy, gz)
@@ -564,8 +628,13 @@ int launch_operator(int64_t E, const T* vgeo, const T* sgeo, const int32_t* vmap
                     T lambda, const T* lambdaE, T tau, const T* q, V4* g4, T* out, cudaStream_t s) {
   constexpr int NP = NQ * NQ * NQ;
   if (E <= 0) return LPG_OK;
-  ipdg_gradient_kernel<NQ, T, V4><<<(unsigned)E, NP, 0, s>>>(vgeo, D, q, g4);
-  LPG_LAUNCH_CHECK("ipdg_gradient_kernel");
+  if constexpr (std::is_same<T, double>::value && NQ % 2 == 0) {
+    ipdg_gradient_eo_kernel<NQ><<<(unsigned)E, NP, 0, s>>>(vgeo, D, q, g4);
+    LPG_LAUNCH_CHECK("ipdg_gradient_eo_kernel");
+  } else {
+    ipdg_gradient_kernel<NQ, T, V4><<<(unsigned)E, NP, 0, s>>>(vgeo, D, q, g4);
+    LPG_LAUNCH_CHECK("ipdg_gradient_kernel");
+  }
   constexpr size_t smem = AxSmem<NQ, T, V4>::bytes;
   static bool configured = false;   // per instantiation: dynamic shared memory opt-in
   if (!configured) {
