@@ -13,8 +13,17 @@ e2e     : same metric through the C ABI's host-buffer operator (lpg_elliptic_ope
           (pipelined over element chunks), timed by host wall clock
 roofline: algorithmic bytes Nlocal*60 + Nglobal*16 per application over the measured
           launch time, against the measured HBM copy bandwidth
+variants: the FP32, BF16-geometry and double-FP32-word operators of the same mesh (the
+          preconditioner levels' and the "+DF64" solves' outer operator), CUDA-event timed
+solve   : the time-to-1e-8 workloads (library Run window, setup outside): FPCG + p-MG 7->3->1
+          on the 80^3 jittered box (lambda=0, manufactured sine) per preconditioner and
+          operator precision, and on the 112^3 jittered box (lognormal lambda, 16 Gaussian
+          sources) plain FP64 against FP32+DF64 with and without the learned fine smoother
+          trained in the same run
 cpu_baseline: the oracle (CPU port of the reference algorithm) on a bounded sample
---impl reference: the reference's CPU implementation (oracle port) on all host threads
+--impl reference: the reference's CPU implementation on all host threads: its own partial-Ax and
+          gather kernels (translated from OKL, compiled with its release flags) on the full
+          64^3 workload
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--nx 64] [--N 7]
 Multi-GPU (torchrun): each rank runs an independent replica of the workload
@@ -44,8 +53,10 @@ def parse():
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--nx", type=int, default=64)
     ap.add_argument("--N", type=int, default=7)
-    ap.add_argument("--cpu-sample-nx", type=int, default=16)
+    ap.add_argument("--cpu-sample-nx", type=int, default=32)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-variants", action="store_true", help="skip the FP32/BF16GEO/DF64 operator variants")
+    ap.add_argument("--no-solves", action="store_true", help="skip the time-to-1e-8 solve blocks")
     ap.add_argument("--e2e-steps", type=int, default=12)
     ap.add_argument("--prec", default="f64", choices=["f64", "df64", "f32", "bf16g"],
                     help="operator variant timed in the Ax workload (headline: f64)")
@@ -140,30 +151,88 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def cpu_model():
+    """Host CPU model name and logical core count (lscpu, else /proc/cpuinfo)."""
+    name = None
+    try:
+        for line in subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout.splitlines():
+            if line.split(":")[0].strip() == "Model name":
+                name = line.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return {"model": name, "logical_cores": os.cpu_count()}
+
+
 def cpu_baseline(nx_sample, N, budget_s=12.0, nthreads=0):
-    """Oracle (CPU port of the reference algorithm) operator throughput on a bounded sample."""
+    """The reference's CPU operator on a bounded sample: its own ellipticPartialAxHex3D and
+    ogs gather kernels (translated from OKL, compiled with its release flags) on the oracle's
+    mesh arrays, all host threads; the oracle port when those kernels are not built."""
+    from oracle import refimpl
     from oracle.oracle import Oracle, threads
+    import numpy as np
     o = Oracle(settings(nx_sample, N))
     nl = o.Nlocal
+    host = cpu_model()
+    if refimpl.available():
+        r = refimpl.RefOperator.from_oracle(o, 1.0)
+        del o
+        q = np.random.default_rng(1).uniform(-1, 1, r.Ngather)
+        t1 = r.time(q, 1, nthreads)
+        reps = max(1, int(budget_s / max(t1, 1e-3)))
+        t = r.time(q, reps, nthreads)
+        used = nthreads if nthreads > 0 else refimpl.threads()
+        return {"value": nl * reps / t / 1e9, "unit": "GDOF/s", "cores": used, "kind": "reference",
+                "host": host, "build": "reference kernels translated from OKL, gcc -O3 -fopenmp -ftree-vectorize",
+                "sample": "%d^3-element jittered box, N=%d, lambda=1 (%d local nodes, working set %.2f GB), "
+                          "%d operator applications (ellipticPartialAxHex3D x2 + ogs Gather), %d OpenMP threads"
+                          % (nx_sample, N, nl, nl * 76 / 1e9, reps, used)}
     t1 = o.time_operator(1, nthreads)
     reps = max(1, int(budget_s / max(t1, 1e-3)))
     t = o.time_operator(reps, nthreads)
     used = nthreads if nthreads > 0 else threads()
-    return {"value": nl * reps / t / 1e9, "unit": "GDOF/s", "cores": used, "kind": "port",
+    return {"value": nl * reps / t / 1e9, "unit": "GDOF/s", "cores": used, "kind": "port", "host": host,
             "sample": "%d^3-element jittered box, N=%d, lambda=1 (%d local nodes), %d operator "
                       "applications, %d OpenMP threads" % (nx_sample, N, nl, reps, used)}
 
 
 def run_reference(a):
+    """The reference's CPU implementation of the headline workload (the 64^3, N=7 operator,
+    same config as the GPU arm): its own partial-Ax and gather kernels on all host threads,
+    W warm-up and K timed applications, one per step."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    base = cpu_baseline(a.cpu_sample_nx, a.N, budget_s=max(5.0, 2.0 * a.steps))
-    line = {"impl": "reference", "metric": METRIC, "value": base["value"], "unit": "GDOF/s",
+    import numpy as np
+    from oracle import refimpl
+    from oracle.oracle import Oracle
+    if not refimpl.available():
+        base = cpu_baseline(a.cpu_sample_nx, a.N, budget_s=max(5.0, 2.0 * a.steps))
+        value, cfg = base["value"], {"workload": workload_name(a.nx, a.N), "same_config": False}
+    else:
+        t0 = time.time()
+        o = Oracle(settings(a.nx, a.N))
+        r = refimpl.RefOperator.from_oracle(o, 1.0)
+        nl = o.Nlocal
+        del o
+        setup = time.time() - t0
+        q = np.random.default_rng(1).uniform(-1, 1, r.Ngather)
+        r.time(q, max(1, a.warmup) - 1)
+        t = r.time(q, a.steps)   # one more warm-up application inside, then K timed
+        used = refimpl.threads()
+        value = nl * a.steps / t / 1e9
+        cfg = {"workload": workload_name(a.nx, a.N), "same_config": True}
+        base = {"value": value, "unit": "GDOF/s", "cores": used, "kind": "reference", "host": cpu_model(),
+                "build": "reference kernels translated from OKL, gcc -O3 -fopenmp -ftree-vectorize",
+                "sample": "full workload: %d^3-element jittered box, N=%d, lambda=1 (%d local nodes), %d timed "
+                          "operator applications (ellipticPartialAxHex3D x2 + ogs Gather), %d OpenMP threads"
+                          % (a.nx, a.N, nl, a.steps, used),
+                "ms_per_step": t * 1e3 / a.steps, "setup_seconds": setup}
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "GDOF/s",
             "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup, "higher_is_better": True,
-            "dtype": "f64", "data": "synthetic", "config": {"workload": workload_name(a.nx, a.N)},
+            "dtype": "f64", "data": "synthetic", "config": cfg,
             "cpu_baseline": base, "vs_baseline": None,
-            "e2e": {"value": base["value"], "unit": "GDOF/s", "h2d_bytes_per_step": 0,
+            "e2e": {"value": value, "unit": "GDOF/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -192,6 +261,71 @@ def solve_settings(nx, N, prec, degrees="7,3,1", lam=0.0, **extra):
          "PRECONDITIONER PRECISION": prec}
     d.update(extra)
     return d
+
+
+def solve_variants(nx, variants, reps, law=None, learned_w=None, threshold=0.5, x_ref_name="FP64", **common):
+    """Time-to-1e-8 of FPCG + p-MG (7->3->1, Chebyshev 2, smoothed-aggregation AMG on N=1) on
+    an nx^3 jittered box, N=7, for each variant name: "P" or "P+DF64" (preconditioner
+    precision P in FP64 / FP32 / BF16GEO; +DF64: every FP64 operator application in
+    double-FP32 words), "learned+P[+DF64]" (the trained fine smoother in place of the
+    fine-level Chebyshev, with per-V-cycle fallback). The solve window is the library's
+    elliptic_t::Run window (after the right-hand side, to after scatter and norms;
+    ellipticRun.cpp:190-221); setup is outside it. Each result: best of `reps` Runs, with
+    iterations, fine-level operator applications, V-cycles and fallbacks, error against the
+    manufactured solution (sine data) and the relative 2-norm difference of the local
+    solution from variant `x_ref_name`'s (listed first)."""
+    import numpy as np
+    import torch
+    import libparanumal_gb300 as lpg
+    res, xref = {}, None
+    for name in variants:
+        learned = name.startswith("learned+")
+        base, _, op = name[len("learned+") if learned else 0:].partition("+")
+        extra = dict(law or {}, **common)
+        if op:
+            extra["OPERATOR PRECISION"] = op
+        t0 = time.time()
+        e = lpg.Elliptic(solve_settings(nx, 7, base, **extra))
+        if learned:
+            e.set_learned_smoother(learned_w, threshold)
+        setup = time.time() - t0
+        runs, ops = [], []
+        for rep in range(reps):
+            n0 = e.info("operator_applications")
+            runs.append(e.Run(want_solution=(rep == 0)))
+            ops.append(e.info("operator_applications") - n0)
+        xL = runs[0].pop("xL")
+        ib = min(range(reps), key=lambda i: runs[i]["solve_seconds"])
+        best = runs[ib]
+        r = {"solve_seconds": best["solve_seconds"], "solve_seconds_all": [x["solve_seconds"] for x in runs],
+             "iterations": best["iterations"], "converged": best["converged"], "fine_ax": ops[ib],
+             "setup_seconds": setup, "nglobal": e.Nglobal}
+        if learned:
+            r["vcycles"], r["fallbacks"] = e.info("vcycles"), e.info("fallbacks")
+        if best["error"] >= 0:
+            r["error_vs_manufactured"] = best["error"]
+        if name == x_ref_name:
+            xref = xL
+        elif xref is not None:
+            r["rel_diff_vs_%s_solution" % x_ref_name.lower()] = float(np.linalg.norm(xL - xref) / np.linalg.norm(xref))
+        del xL
+        res[name] = r
+        e.close()
+        torch.cuda.empty_cache()
+    return res
+
+
+def train_learned(train_nx=32, samples=20000, solves=8, epochs=40, pairs="MIXED"):
+    """Learned fine smoother trained on the GPU by the library's own kernels from the plain
+    p-MG FPCG of a train_nx^3 jittered box (N=7, lognormal lambda, random Gaussian-bump
+    right-hand sides). Returns (weights, summary)."""
+    import libparanumal_gb300 as lpg
+    law = {"LAMBDA": 1.0, "LAMBDA FIELD": "LOGNORMAL", "LAMBDA SEED": 2, "SMOOTHER TRAINING PAIRS": pairs}
+    t0 = time.time()
+    w, hist = lpg.train_smoother(solve_settings(train_nx, 7, "FP64", **law), nsolves=solves,
+                                 samples_per_solve=samples // solves, epochs=epochs, batch=250, lr=1e-3, seed=7)
+    return w, {"train_nx": train_nx, "train_samples": samples, "train_epochs": epochs, "train_pairs": pairs,
+               "train_seconds": time.time() - t0, "loss_first": float(hist[0]), "loss_last": float(hist[-1])}
 
 
 def run_solves(a):
@@ -462,6 +596,65 @@ def run_ipdg(a):
     print(json.dumps(out), flush=True)
 
 
+def time_operator_variants(e, q, a, stream, sp):
+    """CUDA-event time per application of the FP32, BF16-geometry and double-FP32-word
+    operators of object e (the same mesh as the headline FP64 workload), with their
+    algorithmic bytes per application and the achieved bandwidth."""
+    import torch
+    Nl, Ng = e.Nlocal, e.Nglobal
+    q32 = q.float()
+    y32 = torch.empty_like(q32)
+    y64 = torch.empty_like(q)
+    cases = {"fp32": (lambda: e.OperatorF32(q32, y32, False, sp), Nl * 32 + Ng * 8, "FP32 vectors and geometry"),
+             "bf16geo": (lambda: e.OperatorF32(q32, y32, True, sp), Nl * 18 + Ng * 8,
+                         "BF16 geometric factors, FP32 vectors and arithmetic"),
+             "df64": (lambda: e.OperatorDF64(q, y64, sp), Nl * 60 + Ng * 16,
+                      "FP64 in/out, double-FP32-word arithmetic (FP64 accuracy)")}
+    out = {}
+    for name, (op, nbytes, what) in cases.items():
+        for _ in range(max(3, a.warmup)):
+            op()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(a.steps):
+            op()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / a.steps
+        out[name] = {"arith": what, "ms_per_apply": ms, "gdofs_local": Nl / (ms * 1e-3) / 1e9,
+                     "roofline": {"bound": "hbm", "unit": "GB/s", "algorithmic_bytes_per_launch": nbytes,
+                                  "achieved": nbytes / (ms * 1e-3) / 1e9}}
+    return out
+
+
+def solve_blocks(a):
+    """The time-to-1e-8 workloads, each variant timed in the library's Run window:
+    (1) mixed precision: 80^3 jittered box, N=7, lambda=0, manufactured sine data, FPCG to
+        1e-8 with p-MG 7->3->1 (Chebyshev 2, smoothed-aggregation AMG on N=1) whose levels
+        run in FP64, FP32 or BF16-geometry FP32, the outer operator in FP64 or double-FP32 words;
+    (2) learned + mixed precision at scale: 112^3 jittered box, N=7, lognormal lambda (seed 2),
+        16 Gaussian sources (seed 3): plain FP64 p-MG against FP32+DF64 with and without the
+        learned fine smoother, trained in this run on 32^3 (20,000 pairs, 40 epochs)."""
+    t0 = time.time()
+    out = {}
+    out["mixed_80cubed"] = {
+        "workload": "FPCG + p-MG 7->3->1 time-to-1e-8, 80^3 jittered hex, N=7, lambda=0, manufactured sine",
+        "results": solve_variants(80, ["FP64", "FP32", "FP32+DF64", "BF16GEO+DF64"], a.solve_reps)}
+    w, train = train_learned()
+    law = {"LAMBDA": 1.0, "LAMBDA FIELD": "LOGNORMAL", "LAMBDA SEED": 2,
+           "RHS FIELD": "GAUSSIAN SOURCES", "RHS SEED": 3, "RHS SOURCES": 16}
+    res = solve_variants(112, ["FP64", "FP32+DF64", "learned+FP32+DF64"], a.solve_reps, law=law, learned_w=w,
+                         **{"LEARNED SMOOTHER STEPS": 2})
+    t64 = res["FP64"]["solve_seconds"]
+    out["learned_112cubed"] = {
+        "workload": "FPCG + p-MG 7->3->1 time-to-1e-8, 112^3 jittered hex, N=7, lognormal lambda, 16 Gaussian sources",
+        "training": train, "results": res,
+        "speedup_vs_fp64": {k: t64 / v["solve_seconds"] for k, v in res.items()}}
+    out["wall_seconds"] = time.time() - t0
+    return out
+
+
 def main():
     a = parse()
     if a.impl == "reference":
@@ -574,6 +767,14 @@ def main():
         e.OperatorHost(qh, yh, prec_name)
     e2e_ms = max_over_ranks((time.perf_counter() - t_e2e) * 1e3 / a.e2e_steps, dist, "cuda")
 
+    # the other operator variants of the same object, timed the same way (CUDA events on the
+    # launching stream, inputs far above L2): the FP32 and BF16-geometry operators of the
+    # preconditioner levels (the fine-level smoother and residual operator) and the FP64
+    # operator in double-FP32 words (the outer operator of the "+DF64" solves)
+    variants = {}
+    if a.prec == "f64" and world == 1 and not a.no_variants:
+        variants = time_operator_variants(e, q, a, stream, sp)
+
     if rank != 0:
         dist.destroy_process_group()
         return
@@ -619,6 +820,17 @@ def main():
         "clocks": clk,
         "setup_seconds": t_setup,
     }
+    if variants:
+        for v in variants.values():
+            v["roofline"]["peak"], v["roofline"]["peak_kind"] = peak, peak_kind
+            v["roofline"]["frac"] = v["roofline"]["achieved"] / peak
+        out["variants"] = variants
+    if world == 1 and not a.no_solves and a.nx == 64 and a.N == 7:
+        # free the operator workload before the solves
+        del q, Aq, qin, yout
+        e.close()
+        torch.cuda.empty_cache()
+        out["solve"] = solve_blocks(a)
     if not a.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(a.cpu_sample_nx, a.N)
     print(json.dumps(out), flush=True)

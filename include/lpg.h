@@ -120,8 +120,10 @@ int lpg_pcg_update_f64(int64_t N, double alpha, const double *p, const double *A
 
 /* ------------------------------------------------------------------ solver objects */
 /* elliptic_t (solvers/elliptic/elliptic.hpp:56-170) built from settings in the
- * reference's .rc format ([KEY] newline value). Supported keys are listed in
- * INTEGRATION.md; unknown keys fail with LPG_ERR_SETTINGS, as the reference aborts
+ * reference's .rc format ([KEY] newline value): the reference's keys for this path
+ * (ellipticSettings.cpp, parAlmondSettings.cpp, meshSettings.cpp, initialGuess.cpp) plus
+ * the additions documented beside their entry points; unknown keys fail with
+ * LPG_ERR_SETTINGS, as the reference aborts
  * (solvers/elliptic/src/ellipticSettings.cpp:144-146). */
 typedef struct lpg_elliptic lpg_elliptic;
 

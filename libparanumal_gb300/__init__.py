@@ -156,7 +156,7 @@ def _host_ptr(x, dtype, n, writable=False):
 class Elliptic:
     """elliptic_t for a box mesh (solvers/elliptic/elliptic.hpp:56-170).
 
-    Settings use the reference's .rc keys. Operator / precon /
+    Settings use the reference's .rc keys (lpg_elliptic_create). Operator / precon /
     Solve act on device vectors of length Nglobal.
     """
 

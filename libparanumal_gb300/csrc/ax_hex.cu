@@ -842,21 +842,20 @@ template <int NQ, typename T, typename G, int EPB, int STAGES, bool PF = false, 
 static int launch_staged(const AxArgs<T, G>& a, cudaStream_t s) {
   using L = StagedLayout<NQ, G>;
   constexpr int smem = STAGES * EPB * L::ELEM_BYTES;
-  static int configured = -1;   // per instantiation: dynamic shared memory opt-in
-  static int ctasPerSM = 1;
-  static int numSMs = 152;
+  static PerDeviceConfig perDevice;   // per instantiation: dynamic shared memory opt-in, occupancy
   auto kern = ax_hex_staged_kernel<NQ, T, G, EPB, STAGES, PF, MASS>;
-  if (configured < 0) {
-    LPG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    int dev = 0;
-    LPG_CUDA_TRY(cudaGetDevice(&dev));
-    LPG_CUDA_TRY(cudaDeviceGetAttribute(&numSMs, cudaDevAttrMultiProcessorCount, dev));
-    LPG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctasPerSM, kern, NQ * NQ * EPB, smem));
-    if (ctasPerSM < 1) return set_error(LPG_ERR_UNSUPPORTED, "staged Ax: kernel does not fit on an SM");
-    configured = 1;
-  }
+  KernelConfig cfg;
+  const int rc = perDevice.get(
+      [&](int, KernelConfig& c) {
+        LPG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        LPG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c.ctasPerSM, kern, NQ * NQ * EPB, smem));
+        if (c.ctasPerSM < 1) return set_error(LPG_ERR_UNSUPPORTED, "staged Ax: kernel does not fit on an SM");
+        return (int)LPG_OK;
+      },
+      &cfg);
+  if (rc) return rc;
   const int64_t groups = (a.Nelements + EPB - 1) / EPB;
-  const int64_t grid = std::min<int64_t>(groups, (int64_t)numSMs * ctasPerSM);
+  const int64_t grid = std::min<int64_t>(groups, (int64_t)cfg.numSMs * cfg.ctasPerSM);
   if (grid <= 0) return LPG_OK;
   kern<<<(unsigned)grid, dim3(NQ, NQ, EPB), smem, s>>>(a.Nelements, a.elementList, a.g2l, a.ggeo, a.geoStride, a.wJ,
                                                         a.wJStride, a.D, a.lambda, a.lambdaE, a.q, a.out);
@@ -891,6 +890,15 @@ static bool staged_ok(const AxArgs<T, G>& a) {
          ((a.wJStride * (int64_t)sizeof(G)) % 16 == 0);
 }
 
+// LPG_AX_FP64 = direct: tuning override back to the direct-contraction FP64 kernel
+static bool fp64_direct_override() {
+  static const bool direct = [] {
+    const char* e = std::getenv("LPG_AX_FP64");
+    return e && !std::strcmp(e, "direct");
+  }();
+  return direct;
+}
+
 template <int NQ, typename T, typename G, int INMODE, int OUTMODE>
 static int launch_ax(const AxArgs<T, G>& a, cudaStream_t s) {
   if constexpr (std::is_same<T, float>::value && INMODE == IN_GATHER && OUTMODE == OUT_ASSEMBLE) {
@@ -920,12 +928,7 @@ static int launch_ax(const AxArgs<T, G>& a, cudaStream_t s) {
   dim3 block(NQ, NQ, EPB);
   if constexpr (std::is_same<T, double>::value && std::is_same<G, double>::value && INMODE == IN_GATHER &&
                 OUTMODE == OUT_ASSEMBLE && (NQ == 4 || NQ == 8)) {
-    // LPG_AX_FP64 = direct: tuning override back to the direct-contraction kernel
-    static const bool direct = [] {
-      const char* e = std::getenv("LPG_AX_FP64");
-      return e && !std::strcmp(e, "direct");
-    }();
-    if (!direct) {
+    if (!fp64_direct_override()) {
       if (a.lambda == 0.0 && !a.lambdaE)
         ax_hex_eo_kernel<NQ, false><<<(unsigned)blocks, block, 0, s>>>(a.Nelements, a.elementList, a.g2l, a.ggeo,
                                                                       a.geoStride, a.wJ, a.wJStride, a.D, a.lambda,
@@ -977,7 +980,17 @@ int ax_hex(const AxArgs<T, G>& a, AxMode mode, cudaStream_t s) {
   return set_error(LPG_ERR_INVALID, "ax: bad mode");
 }
 
-int ax_wave_elements(int N, bool dw) {
+template <int NQ>
+static cudaError_t fp64_occupancy(int* per, bool dw, bool mass, int epb) {
+  if (dw) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per, ax_hex_dw_kernel<NQ>, NQ * NQ * epb, 0);
+  if (fp64_direct_override())
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        per, ax_hex_kernel<NQ, double, double, IN_GATHER, OUT_ASSEMBLE>, NQ * NQ * epb, 0);
+  return mass ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(per, ax_hex_eo_kernel<NQ, true>, NQ * NQ * epb, 0)
+              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(per, ax_hex_eo_kernel<NQ, false>, NQ * NQ * epb, 0);
+}
+
+int ax_wave_elements(int N, bool dw, bool mass) {
   int dev = 0, sms = 0, per = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
     return 1;
@@ -985,12 +998,10 @@ int ax_wave_elements(int N, bool dw) {
   int epb = 1;
   if (N == 7) {
     epb = elems_per_block<8>();
-    e = dw ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, ax_hex_dw_kernel<8>, 8 * 8 * epb, 0)
-           : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, ax_hex_eo_kernel<8>, 8 * 8 * epb, 0);
+    e = fp64_occupancy<8>(&per, dw, mass, epb);
   } else if (N == 3) {
     epb = elems_per_block<4>();
-    e = dw ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, ax_hex_dw_kernel<4>, 4 * 4 * epb, 0)
-           : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, ax_hex_eo_kernel<4>, 4 * 4 * epb, 0);
+    e = fp64_occupancy<4>(&per, dw, mass, epb);
   }
   if (e != cudaSuccess || per < 1) {
     cudaGetLastError();

@@ -505,17 +505,9 @@ int Elliptic::BuildPipe(cudaStream_t s) {
   if (pipe) return LPG_OK;
   auto p = std::make_unique<HostPipe>();
   const int64_t E = mesh.E;
-  // at most 32 chunks of at least 4096 elements (a chunk still fills every SM). For the
-  // FP64 operator, whose kernel time bounds the pipeline, the boundaries are rounded up to
-  // whole waves of the kernel so no chunk ends in a partly filled wave (64^3, N=7: 12.48 ->
-  // 12.05 ms per call); the double-word and FP32 pipelines are bound by the copies and keep
-  // even chunks (aligned, the double-word one was 3 % slower).
+  // at most 32 chunks of at least 4096 elements (a chunk still fills every SM)
   p->K = (int)std::max<int64_t>(1, std::min<int64_t>(32, E / 4096));
   const int K = p->K;
-  const int64_t wave = opDW ? 1 : std::max(1, ax_wave_elements(mesh.N, false));
-  p->e0.resize(K + 1);
-  for (int c = 0; c <= K; ++c) p->e0[c] = std::min<int64_t>(E, (E * c / K + wave - 1) / wave * wave);
-  p->e0[K] = E;
   std::vector<int32_t> lo(std::max<int64_t>(E, 1)), hi(std::max<int64_t>(E, 1));
   if (E > 0) {
     DevBuf<int32_t> dlo, dhi;
@@ -526,19 +518,33 @@ int Elliptic::BuildPipe(cudaStream_t s) {
     LPG_CUDA_TRY(cudaMemcpyAsync(hi.data(), dhi.p, sizeof(int32_t) * E, cudaMemcpyDeviceToHost, s));
     LPG_CUDA_TRY(cudaStreamSynchronize(s));
   }
-  p->inEnd.assign(K, 0);
-  p->outEnd.assign(K, Nglobal);
-  int64_t need = 0;
-  for (int c = 0; c < K; ++c) {
-    for (int64_t e = p->e0[c]; e < p->e0[c + 1]; ++e) need = std::max<int64_t>(need, (int64_t)hi[e] + 1);
-    p->inEnd[c] = std::min<int64_t>(need, Nglobal);
-  }
-  p->inEnd[K - 1] = Nglobal;
-  int64_t first = Nglobal;   // smallest entry touched by chunks c+1..K-1
-  for (int c = K - 1; c >= 0; --c) {
-    p->outEnd[c] = first;
-    for (int64_t e = p->e0[c]; e < p->e0[c + 1]; ++e) first = std::min<int64_t>(first, (int64_t)lo[e]);
-  }
+  // chunk boundaries rounded up to multiples of `wave` elements, and the prefixes of q each
+  // chunk reads and of Aq that are final after it
+  auto split = [&](PipeSplit& sp, int64_t wave) {
+    sp.e0.resize(K + 1);
+    for (int c = 0; c <= K; ++c) sp.e0[c] = std::min<int64_t>(E, (E * c / K + wave - 1) / wave * wave);
+    sp.e0[K] = E;
+    sp.inEnd.assign(K, 0);
+    sp.outEnd.assign(K, Nglobal);
+    int64_t need = 0;
+    for (int c = 0; c < K; ++c) {
+      for (int64_t e = sp.e0[c]; e < sp.e0[c + 1]; ++e) need = std::max<int64_t>(need, (int64_t)hi[e] + 1);
+      sp.inEnd[c] = std::min<int64_t>(need, Nglobal);
+    }
+    sp.inEnd[K - 1] = Nglobal;
+    int64_t first = Nglobal;   // smallest entry touched by chunks c+1..K-1
+    for (int c = K - 1; c >= 0; --c) {
+      sp.outEnd[c] = first;
+      for (int64_t e = sp.e0[c]; e < sp.e0[c + 1]; ++e) first = std::min<int64_t>(first, (int64_t)lo[e]);
+    }
+  };
+  // The FP64 kernel bounds its pipeline, so its chunks end on whole waves of the kernel
+  // instantiation this object launches (64^3, N=7: 12.48 -> 12.05 ms per call); the
+  // double-word and FP32 pipelines are bound by the copies and keep even chunks (aligned,
+  // the double-word one was 3 % slower).
+  const bool mass = !(lambda == 0.0 && !hasLambdaE);
+  split(p->native, opDW ? 1 : std::max(1, ax_wave_elements(mesh.N, false, mass)));
+  split(p->even, 1);
   LPG_CUDA_TRY(cudaStreamCreateWithFlags(&p->h2d, cudaStreamNonBlocking));
   LPG_CUDA_TRY(cudaStreamCreateWithFlags(&p->d2h, cudaStreamNonBlocking));
   p->inReady.assign(K, nullptr);
@@ -554,12 +560,12 @@ int Elliptic::BuildPipe(cudaStream_t s) {
 // Upload pieces of q on the h2d stream, one operator launch per element chunk on s
 // (each waits for the piece it reads), download each final prefix of Aq on d2h.
 template <typename T, typename Launch>
-static int run_pipe(HostPipe& p, const T* qh, T* Aqh, T* dq, T* dAq, int64_t Nglobal, cudaStream_t s,
-                    Launch&& launch) {
+static int run_pipe(HostPipe& p, const PipeSplit& sp, const T* qh, T* Aqh, T* dq, T* dAq, int64_t Nglobal,
+                    cudaStream_t s, Launch&& launch) {
   auto body = [&]() -> int {
     int64_t up = 0;
     for (int c = 0; c < p.K; ++c) {
-      const int64_t end = p.inEnd[c];
+      const int64_t end = sp.inEnd[c];
       if (end > up)
         LPG_CUDA_TRY(cudaMemcpyAsync(dq + up, qh + up, sizeof(T) * (end - up), cudaMemcpyHostToDevice, p.h2d));
       up = std::max(up, end);
@@ -569,14 +575,14 @@ static int run_pipe(HostPipe& p, const T* qh, T* Aqh, T* dq, T* dAq, int64_t Ngl
     // Aq is zeroed piece by piece ahead of each chunk instead of in one pass up front
     int64_t down = 0, zeroed = 0;
     for (int c = 0; c < p.K; ++c) {
-      const int64_t zend = std::max<int64_t>(zeroed, p.inEnd[c]);
+      const int64_t zend = std::max<int64_t>(zeroed, sp.inEnd[c]);
       if (zend > zeroed) LPG_CUDA_TRY(cudaMemsetAsync(dAq + zeroed, 0, sizeof(T) * (zend - zeroed), s));
       zeroed = zend;
       LPG_CUDA_TRY(cudaStreamWaitEvent(s, p.inReady[c], 0));
-      const int rc = launch(p.e0[c], p.e0[c + 1]);
+      const int rc = launch(sp.e0[c], sp.e0[c + 1]);
       if (rc) return rc;
       LPG_CUDA_TRY(cudaEventRecord(p.chunkDone[c], s));
-      const int64_t end = p.outEnd[c];
+      const int64_t end = sp.outEnd[c];
       if (end > down) {
         LPG_CUDA_TRY(cudaStreamWaitEvent(p.d2h, p.chunkDone[c], 0));
         LPG_CUDA_TRY(cudaMemcpyAsync(Aqh + down, dAq + down, sizeof(T) * (end - down), cudaMemcpyDeviceToHost,
@@ -622,7 +628,7 @@ int Elliptic::OperatorHost(const double* qHost, double* AqHost, cudaStream_t s) 
     a.q = pipe->q.p; a.out = pipe->Aq.p; a.Nglobal = Nglobal;
     return ax_hex<double, double>(a, AxMode::AccumulateAssembled, s);
   };
-  return run_pipe<double>(*pipe, qHost, AqHost, pipe->q.p, pipe->Aq.p, Nglobal, s, launch);
+  return run_pipe<double>(*pipe, pipe->native, qHost, AqHost, pipe->q.p, pipe->Aq.p, Nglobal, s, launch);
 }
 
 int Elliptic::OperatorHostF32(const float* qHost, float* AqHost, Prec prec, cudaStream_t s) {
@@ -649,7 +655,7 @@ int Elliptic::OperatorHostF32(const float* qHost, float* AqHost, Prec prec, cuda
     a.q = pipe->q32.p; a.out = pipe->Aq32.p; a.Nglobal = Nglobal;
     return ax_hex<float, float>(a, AxMode::AccumulateAssembled, s);
   };
-  return run_pipe<float>(*pipe, qHost, AqHost, pipe->q32.p, pipe->Aq32.p, Nglobal, s, launch);
+  return run_pipe<float>(*pipe, pipe->even, qHost, AqHost, pipe->q32.p, pipe->Aq32.p, Nglobal, s, launch);
 }
 
 int Elliptic::BuildDiagonal(double* diagG, cudaStream_t s) {

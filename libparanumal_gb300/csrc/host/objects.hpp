@@ -127,10 +127,16 @@ enum class Prec { F64 = 0, F32 = 1, BF16G = 2 };
 // the box numbering (entries grouped by owner element, owner = smallest element holding
 // the node) both are long prefixes, so the upload of q, the chunks' operator launches
 // and the download of Aq overlap on three streams.
-struct HostPipe {
-  int K = 0;
+struct PipeSplit {
   std::vector<int64_t> e0;          // K+1 chunk boundaries (elements)
   std::vector<int64_t> inEnd, outEnd;
+};
+struct HostPipe {
+  int K = 0;
+  // native: the FP64 kernel's chunks, ending on whole waves of that kernel (its time bounds
+  // the pipeline); even: equal chunks, for the double-word and FP32 pipelines, which the
+  // copies bound
+  PipeSplit native, even;
   cudaStream_t h2d = nullptr, d2h = nullptr;
   std::vector<cudaEvent_t> inReady, chunkDone;
   DevBuf<double> q, Aq;

@@ -636,11 +636,16 @@ int launch_operator(int64_t E, const T* vgeo, const T* sgeo, const int32_t* vmap
     LPG_LAUNCH_CHECK("ipdg_gradient_kernel");
   }
   constexpr size_t smem = AxSmem<NQ, T, V4>::bytes;
-  static bool configured = false;   // per instantiation: dynamic shared memory opt-in
-  if (!configured) {
-    LPG_CUDA_TRY(cudaFuncSetAttribute(ipdg_ax_kernel<NQ, T, V4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    configured = true;
-  }
+  static PerDeviceConfig perDevice;   // per instantiation: dynamic shared memory opt-in
+  KernelConfig cfg;
+  const int rc = perDevice.get(
+      [&](int, KernelConfig&) {
+        LPG_CUDA_TRY(cudaFuncSetAttribute(ipdg_ax_kernel<NQ, T, V4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)smem));
+        return (int)LPG_OK;
+      },
+      &cfg);
+  if (rc) return rc;
   ipdg_ax_kernel<NQ, T, V4><<<(unsigned)E, NP, smem, s>>>(vgeo, sgeo, vmapP, EToB, D, lambda, lambdaE, tau, g4, out);
   LPG_LAUNCH_CHECK("ipdg_ax_kernel");
   return LPG_OK;
@@ -707,11 +712,16 @@ int ipdg_operator_dw(const IpdgArgsDW& a, cudaStream_t s) {
     ipdg_gradient_dw_kernel<NQ><<<E, NP, 0, s>>>(a.vgeo, a.D, a.q, a.g8);
     LPG_LAUNCH_CHECK("ipdg_gradient_dw_kernel");
     constexpr size_t smem = AxSmem<NQ, dw, dw4>::bytes;
-    static bool configured = false;   // per instantiation: dynamic shared memory opt-in
-    if (!configured) {
-      LPG_CUDA_TRY(cudaFuncSetAttribute(ipdg_ax_dw_kernel<NQ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      configured = true;
-    }
+    static PerDeviceConfig perDevice;   // per instantiation: dynamic shared memory opt-in
+    KernelConfig cfg;
+    const int rc = perDevice.get(
+        [&](int, KernelConfig&) {
+          LPG_CUDA_TRY(cudaFuncSetAttribute(ipdg_ax_dw_kernel<NQ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)smem));
+          return (int)LPG_OK;
+        },
+        &cfg);
+    if (rc) return rc;
     ipdg_ax_dw_kernel<NQ><<<E, NP, smem, s>>>(a.vgeo, a.sgeo, a.vmapP, a.EToB, a.D, a.lambda, a.lambdaE, a.tau, a.g8,
                                               a.out);
     LPG_LAUNCH_CHECK("ipdg_ax_dw_kernel");

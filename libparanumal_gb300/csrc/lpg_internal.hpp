@@ -36,8 +36,9 @@ int ax_hex(const AxArgs<T, G>& a, AxMode mode, cudaStream_t s);
 // kernels for N = 3 and 7).
 int ax_hex_dw(const AxArgs<double, float2>& a, cudaStream_t s);
 // elements covered by one full wave (every SM at the kernel's occupancy) of the assembled
-// FP64 (dw = false) or double-word operator kernel at degree N; 1 where not known
-int ax_wave_elements(int N, bool dw);
+// FP64 (dw = false; mass = the instantiation with the lambda term) or double-word operator
+// kernel at degree N; 1 where not known
+int ax_wave_elements(int N, bool dw, bool mass);
 // FP64 -> (hi, lo) float pairs (hi = x rounded to FP32, lo = x - hi rounded to FP32)
 int split_to_float2(int64_t n, const double* x, float2* y, cudaStream_t s);
 

@@ -389,15 +389,17 @@ int mlp_forward_tc(int64_t B, const __nv_bfloat16* X, const __nv_bfloat16* const
       (rc = make_map(&maps.w[2], Wt[2], kMlpHidden, kMlpHidden, 256)) ||
       (rc = make_map(&maps.w[3], Wt[3], kMlpHidden, kMlpOut, 256)))
     return rc;
-  static int numSMs = 0;
-  if (!numSMs) {
-    int dev = 0;
-    LPG_CUDA_TRY(cudaGetDevice(&dev));
-    LPG_CUDA_TRY(cudaDeviceGetAttribute(&numSMs, cudaDevAttrMultiProcessorCount, dev));
-    LPG_CUDA_TRY(cudaFuncSetAttribute(mlp_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-  }
+  static PerDeviceConfig perDevice;   // dynamic shared memory opt-in per device
+  KernelConfig cfg;
+  rc = perDevice.get(
+      [&](int, KernelConfig&) {
+        LPG_CUDA_TRY(cudaFuncSetAttribute(mlp_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+        return (int)LPG_OK;
+      },
+      &cfg);
+  if (rc) return rc;
   const int ntiles = (int)((B + TM - 1) / TM);
-  const int grid = ntiles < numSMs ? ntiles : numSMs;
+  const int grid = ntiles < cfg.numSMs ? ntiles : cfg.numSMs;
   LPG_CUDA_TRY(cudaMemsetAsync(errFlag, 0, sizeof(int), s));
   mlp_tc_kernel<<<grid, THREADS, SMEM_BYTES, s>>>(maps, bias[0], bias[1], bias[2], bias[3], Y, B, ntiles, errFlag);
   LPG_LAUNCH_CHECK("mlp_tc_kernel");

@@ -31,7 +31,9 @@ def extract(ref_root):
 
 
 if __name__ == "__main__":
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("LIBPARANUMAL_DIR")
+    if not ref:
+        sys.exit("usage: make_reference_norms.py <libParanumal source tree> (or set LIBPARANUMAL_DIR)")
     data = {"tolerance": 1e-5, "tolerance_source": "test/test.py:63,129-137",
             "defaults_source": "test/testElliptic.py:34-59 (LAMBDA is not written to the .rc, so the "
                                "default 1.0 of solvers/elliptic/src/ellipticSettings.cpp applies)",

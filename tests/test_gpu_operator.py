@@ -9,6 +9,7 @@ import torch
 
 import libparanumal_gb300 as lpg
 from gpu_helpers import box, lattice_q, rel_err
+from oracle import refimpl
 from oracle.oracle import Oracle
 
 pytestmark = pytest.mark.gpu
@@ -70,6 +71,42 @@ def test_operator_matches_oracle(cfg):
         e.Operator(q, Aq)
         torch.cuda.synchronize()
         assert rel_err(Aq.cpu().numpy(), o.operator(qh)) < 1e-12
+
+
+REF_CASES = [box(**{"POLYNOMIAL DEGREE": N}) for N in range(1, 9)] + [
+    box(**{"POLYNOMIAL DEGREE": 3, "BOX BOUNDARY FLAG": -1, "MESH JITTER": 0.0}),   # periodic
+    box(**{"POLYNOMIAL DEGREE": 7, "LAMBDA": 0.0, "BOX NX": 4, "BOX NY": 4, "BOX NZ": 4}),
+]
+
+
+@pytest.mark.skipif(not refimpl.available(), reason="reference kernels not built here")
+@pytest.mark.parametrize("cfg", REF_CASES, ids=ids)
+def test_operator_matches_reference_kernels(cfg):
+    """The CUDA operators (FP64 and double-FP32 words) and the reference-contract partial Ax
+    against the reference's own ellipticPartialAxHex3D + ogs gather (translated from its OKL,
+    compiled for the host), both fed this library's own setup arrays."""
+    e = lpg.Elliptic(cfg)
+    N, E, Np = cfg["POLYNOMIAL DEGREE"], e.info("nelements"), e.info("np")
+    ggeo, wJ, D, g2lh = e.get("ggeo"), e.get("wJ"), e.get("D"), e.get("GlobalToLocal")
+    r = refimpl.RefOperator(N, E, g2lh, e.Nglobal, wJ, ggeo, D, cfg["LAMBDA"])
+    rng = np.random.default_rng(11)
+    qh = rng.uniform(-1, 1, e.Nglobal)
+    q = torch.tensor(qh, device="cuda")
+    ref = r.apply(qh)
+    Aq = torch.full_like(q, np.nan)
+    e.Operator(q, Aq)
+    torch.cuda.synchronize()
+    assert rel_err(Aq.cpu().numpy(), ref) < 1e-12
+    e.OperatorDF64(q, Aq)
+    torch.cuda.synchronize()
+    assert rel_err(Aq.cpu().numpy(), ref) < 1e-12
+    AqL = torch.full((E * Np,), np.nan, dtype=torch.float64, device="cuda")
+    dg = [torch.tensor(x, device="cuda") for x in (ggeo, wJ, D, g2lh)]
+    lpg.check(lpg.lib().lpg_partial_ax_hex_f64(N, E, None, dg[3].data_ptr(), dg[0].data_ptr(), 6 * Np,
+                                               dg[1].data_ptr(), Np, dg[2].data_ptr(), cfg["LAMBDA"], None,
+                                               q.data_ptr(), AqL.data_ptr(), None))
+    torch.cuda.synchronize()
+    assert rel_err(AqL.cpu().numpy(), r.partial_ax(qh)) < 1e-12
 
 
 def test_lattice_keyed_input_and_linearity():

@@ -40,8 +40,11 @@ def test_dot_noalloc_matches_allocating_dot_on_consecutive_calls():
 
 
 def test_dot_noalloc_rejects_sizes_beyond_its_maximum():
+    import __graft_entry__ as g
+    g.build()
     import libparanumal_gb300 as lpg
     L = lpg.lib()
+    torch.cuda.set_device(0)
     out = torch.zeros(1, dtype=torch.float64, device="cuda")
     st = L.lpg_dot_f64_noalloc((1 << 40) + 1, out.data_ptr(), out.data_ptr(), out.data_ptr(), None)
     assert st == -1
