@@ -29,6 +29,7 @@ extern "C" {
 #define LPG_ERR_ALLOC (-5)         /* device allocation failed */
 #define LPG_ERR_SETTINGS (-6)      /* unknown or malformed setting */
 #define LPG_ERR_BREAKDOWN (-7)     /* NaN/Inf or non-positive curvature in (F)PCG */
+#define LPG_ERR_TIMEOUT (-8)       /* a bounded wait inside a device pipeline ran out */
 
 /* Replaces LIBP_ABORT's message (include/utils.hpp:57-76): text of the last error on
  * this thread. */
@@ -41,6 +42,10 @@ int lpg_device_malloc(void **ptr, uint64_t bytes);
 int lpg_device_free(void *ptr);
 int lpg_memcpy_h2d(void *dst, const void *src, uint64_t bytes, void *stream);
 int lpg_memcpy_d2h(void *dst, const void *src, uint64_t bytes, void *stream);
+int lpg_memcpy_d2d(void *dst, const void *src, uint64_t bytes, void *stream);
+/* platform_t's DEVICE NUMBER (libs/core/platformDeviceConfig.cpp:80-100): makes `device` current for the
+ * calling thread; later objects and kernels use it. */
+int lpg_set_device(int device);
 int lpg_stream_sync(void *stream);
 
 /* ------------------------------------------------------------------ operator kernels */
@@ -118,6 +123,68 @@ int lpg_dot_f64_noalloc(int64_t N, const double *x, const double *y, double *res
 int lpg_pcg_update_f64(int64_t N, double alpha, const double *p, const double *Ap, double *x, double *r,
                        double *result_dev, void *stream);
 
+/* linAlg_t::norm2 (libs/linAlg/linAlg.cpp:154-167): result_dev = sqrt(x.x). */
+int lpg_norm2_f64(int64_t N, const double *x, double *result_dev, void *stream);
+/* JacobiPrecon::Operator (solvers/elliptic/src/ellipticPreconJacobi.cpp:42-):
+ * z = invDiag .* r. */
+int lpg_jacobi_f64(int64_t N, const double *invDiag, const double *r, double *z, void *stream);
+
+/* ------------------------------------------------------------------ p-multigrid level kernels */
+/* MGLevel::coarsen (solvers/elliptic/src/ellipticPreconMultiGridLevel.cpp:41-82 with
+ * ellipticPartialPreconCoarsenHex3D, okl/ellipticPreconCoarsenHex3D.okl:209-294): per element,
+ * the fine local values weightF .* rF (scattered by g2lF, masked nodes 0) are restricted by
+ * P^T in each direction and assembled into rC (NglobalC, overwritten) through g2lC.
+ * P is the (Nf+1) x (Nc+1) GLL interpolation matrix, row-major (P[i*(Nc+1)+j] = l_j(r_i)). */
+int lpg_pmg_restrict_f64(int Nf, int Nc, int64_t E, const int32_t *g2lF, const double *weightF,
+                         const double *rF, const double *P, const int32_t *g2lC, double *rC,
+                         int64_t NglobalC, void *stream);
+int lpg_pmg_restrict_f32(int Nf, int Nc, int64_t E, const int32_t *g2lF, const float *weightF,
+                         const float *rF, const float *P, const int32_t *g2lC, float *rC,
+                         int64_t NglobalC, void *stream);
+/* MGLevel::prolongate (ellipticPreconMultiGridLevel.cpp:84-125 with
+ * ellipticPartialPreconProlongateHex3D, okl/ellipticPreconProlongateHex3D.okl:216-301):
+ * xF += P xC, element by element; each fine dof is written once, by its owning local copy
+ * (ownerF[g] = the first local node of dof g, as lpg_elliptic_get("ownerLocal") returns). */
+int lpg_pmg_prolong_add_f64(int Nf, int Nc, int64_t E, const int32_t *g2lC, const double *xC,
+                            const double *P, const int32_t *g2lF, const int32_t *ownerF, double *xF,
+                            void *stream);
+int lpg_pmg_prolong_add_f32(int Nf, int Nc, int64_t E, const int32_t *g2lC, const float *xC,
+                            const float *P, const int32_t *g2lF, const int32_t *ownerF, float *xF,
+                            void *stream);
+/* MGLevel::smoothChebyshev (ellipticPreconMultiGridLevel.cpp:154-206) as two fused passes.
+ * start: res = invDiag .* (r - Ax) (xIsZero: res = invDiag .* r, Ax unused);
+ *        d = invTheta res; x = d (xIsZero) or x += d.
+ * update (one Chebyshev step after Ad = A d): res -= invDiag .* Ad; d = a d + b res; x += d. */
+int lpg_cheb_start_f64(int64_t N, const double *invDiag, const double *r, const double *Ax, double *res,
+                       double *d, double *x, double invTheta, int xIsZero, void *stream);
+int lpg_cheb_start_f32(int64_t N, const float *invDiag, const float *r, const float *Ax, float *res,
+                       float *d, float *x, float invTheta, int xIsZero, void *stream);
+int lpg_cheb_update_f64(int64_t N, const double *invDiag, const double *Ad, double *res, double *d,
+                        double *x, double a, double b, void *stream);
+int lpg_cheb_update_f32(int64_t N, const float *invDiag, const float *Ad, float *res, float *d, float *x,
+                        float a, float b, void *stream);
+
+/* ------------------------------------------------------------------ parAlmond level kernels */
+/* CSR matrices: int64 row starts (Nrows+1), int32 columns, FP64 values.
+ * parCSR::SpMV (libs/parAlmond/parAlmondparCSR.cpp:99-140, okl/SpMVcsr.okl):
+ * y = alpha A x + beta y (beta = 0 ignores y). */
+int lpg_csr_spmv_f64(int64_t Nrows, const int64_t *rowStarts, const int32_t *cols, const double *vals,
+                     double alpha, const double *x, double beta, double *y, void *stream);
+/* parCSR::smoothChebyshev (libs/parAlmond/parAlmondAMGSmoother.cpp:68-160, okl/SmoothChebyshev.okl:30-167):
+ * start (x = 0): r = diagInv .* b; d = invTheta r; x = d.
+ * residual: r = alpha r + diagInv .* (beta b - A x).
+ * update: d = a d + b r; x += d (lastIt: d is not stored). */
+int lpg_csr_cheb_start_f64(int64_t N, double invTheta, const double *diagInv, const double *b, double *r,
+                           double *d, double *x, void *stream);
+int lpg_csr_cheb_residual_f64(int64_t N, const int64_t *rowStarts, const int32_t *cols, const double *vals,
+                              double alpha, double beta, const double *diagInv, const double *b,
+                              const double *x, double *r, void *stream);
+int lpg_csr_cheb_update_f64(int64_t N, double a, double b, int lastIt, const double *r, double *d, double *x,
+                            void *stream);
+/* exactSolver_t::solve (libs/parAlmond/parAlmondCoarseExact.cpp:35-60, okl/dGEMV.okl):
+ * y = A x with the dense n x n inverse A, row-major. */
+int lpg_gemv_f64(int64_t n, const double *A, const double *x, double *y, void *stream);
+
 /* ------------------------------------------------------------------ solver objects */
 /* elliptic_t (solvers/elliptic/elliptic.hpp:56-170) built from settings in the
  * reference's .rc format ([KEY] newline value): the reference's keys for this path
@@ -147,6 +214,8 @@ int lpg_elliptic_destroy(lpg_elliptic *e);
 #define LPG_INFO_OPERATOR_APPLICATIONS 14 /* fine-level operator applications (FP64, double-word
                                              and FP32) since creation: outer Krylov, smoother,
                                              residual and setup applications */
+#define LPG_INFO_LEARNED_TIMEOUTS 15 /* learned V-cycles redone with the plain smoother because the
+                                        network's tensor-core pipeline reported a timeout */
 int64_t lpg_elliptic_info(const lpg_elliptic *e, int what);
 
 /* Copy a named setup array to host memory: "GlobalToLocal" (int32), "ownerLocal" (int32),
@@ -194,6 +263,10 @@ int lpg_elliptic_precon(lpg_elliptic *e, const double *r, double *z, void *strea
  * guess, overwritten) and r (right-hand side, overwritten by the residual).
  * Returns the iteration count in *iters. */
 int lpg_elliptic_solve(lpg_elliptic *e, double *x, double *r, double tol, int maxit, int *iters);
+/* elliptic_t::ZeroMean (ellipticZeroMean.cpp:29-37): removes the mean of the assembled
+ * vector q (Nglobal, device) when the problem has the constant null space (all-Neumann
+ * boundaries with lambda = 0); otherwise a no-op. */
+int lpg_elliptic_zero_mean(lpg_elliptic *e, double *q, void *stream);
 /* The assembled right-hand side of elliptic_t::Run (forcing, Dirichlet lifting,
  * Gather(Trans)) into a device vector r (Nglobal). */
 int lpg_elliptic_rhs(lpg_elliptic *e, double *r, void *stream);
@@ -273,6 +346,13 @@ int lpg_smoother_train(const char *settings, int nsolves, int samples_per_solve,
  * residual ratio ||r - A z|| / ||r|| exceeds `threshold` (e.g. 0.5) is redone with the
  * plain smoother. weights_host = NULL restores the plain smoother. */
 int lpg_elliptic_set_learned_smoother(lpg_elliptic *e, const float *weights_host, double threshold);
+/* Diagnostics (no reference counterpart): every following launch of the fused tensor-core
+ * MLP kernel first waits up to `ns` nanoseconds on a barrier that nothing signals, then
+ * gives up the way any of its bounded pipeline waits does -- records a timeout, issues no
+ * copy or MMA, frees its tensor memory and returns. The caller sees LPG_ERR_TIMEOUT from
+ * lpg_mlp_forward_bf16, and a learned V-cycle falls back to the plain smoother. 0 (the
+ * default) turns it off. Exists so the timeout path can be tested without a GPU fault. */
+int lpg_debug_mlp_hold(uint64_t ns);
 
 #ifdef __cplusplus
 }

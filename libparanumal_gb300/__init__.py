@@ -17,10 +17,10 @@ LIB_PATH = os.path.join(_HERE, "_build", "liblpg.so")
 
 LPG_OK = 0
 STATUS = {0: "OK", -1: "INVALID", -2: "CUDA", -3: "UNSUPPORTED", -4: "NOT_CONVERGED",
-          -5: "ALLOC", -6: "SETTINGS", -7: "BREAKDOWN"}
+          -5: "ALLOC", -6: "SETTINGS", -7: "BREAKDOWN", -8: "TIMEOUT"}
 INFO = dict(nelements=0, np=1, nglobal=2, nlocal=3, n=4, allneumann=5, mg_plevels=6,
             mg_amglevels=7, coarse_n=8, device_bytes=9, vcycles=10, fallbacks=11, host_chunks=12,
-            ig_history=13, operator_applications=14)
+            ig_history=13, operator_applications=14, learned_timeouts=15)
 
 _lib = None
 
@@ -51,6 +51,9 @@ def lib():
         "lpg_device_free": [vp],
         "lpg_memcpy_h2d": [vp, vp, ctypes.c_uint64, vp],
         "lpg_memcpy_d2h": [vp, vp, ctypes.c_uint64, vp],
+        "lpg_memcpy_d2d": [vp, vp, ctypes.c_uint64, vp],
+        "lpg_set_device": [i32],
+        "lpg_elliptic_zero_mean": [vp, vp, vp],
         "lpg_stream_sync": [vp],
         "lpg_ax_hex_f64": ax64,
         "lpg_ax_hex_f32": ax32,
@@ -65,6 +68,21 @@ def lib():
         "lpg_norm2sq_f64": [i64, vp, vp, vp],
         "lpg_dot_f64_noalloc": [i64, vp, vp, vp, vp],
         "lpg_pcg_update_f64": [i64, f64, vp, vp, vp, vp, vp, vp],
+        "lpg_norm2_f64": [i64, vp, vp, vp],
+        "lpg_jacobi_f64": [i64, vp, vp, vp, vp],
+        "lpg_pmg_restrict_f64": [i32, i32, i64, vp, vp, vp, vp, vp, vp, i64, vp],
+        "lpg_pmg_restrict_f32": [i32, i32, i64, vp, vp, vp, vp, vp, vp, i64, vp],
+        "lpg_pmg_prolong_add_f64": [i32, i32, i64, vp, vp, vp, vp, vp, vp, vp],
+        "lpg_pmg_prolong_add_f32": [i32, i32, i64, vp, vp, vp, vp, vp, vp, vp],
+        "lpg_cheb_start_f64": [i64, vp, vp, vp, vp, vp, vp, f64, i32, vp],
+        "lpg_cheb_start_f32": [i64, vp, vp, vp, vp, vp, vp, f32, i32, vp],
+        "lpg_cheb_update_f64": [i64, vp, vp, vp, vp, vp, f64, f64, vp],
+        "lpg_cheb_update_f32": [i64, vp, vp, vp, vp, vp, f32, f32, vp],
+        "lpg_csr_spmv_f64": [i64, vp, vp, vp, f64, vp, f64, vp, vp],
+        "lpg_csr_cheb_start_f64": [i64, f64, vp, vp, vp, vp, vp, vp],
+        "lpg_csr_cheb_residual_f64": [i64, vp, vp, vp, f64, f64, vp, vp, vp, vp, vp],
+        "lpg_csr_cheb_update_f64": [i64, f64, f64, i32, vp, vp, vp, vp],
+        "lpg_gemv_f64": [i64, vp, vp, vp, vp],
         "lpg_elliptic_create": [ctypes.c_char_p, ctypes.POINTER(ctypes.c_void_p)],
         "lpg_elliptic_destroy": [vp],
         "lpg_elliptic_get": [vp, ctypes.c_char_p, vp, ctypes.c_uint64],
@@ -90,6 +108,7 @@ def lib():
         "lpg_mlp_forward_bf16": [vp, i64, vp, vp, vp],
         "lpg_smoother_train": [ctypes.c_char_p, i32, i32, i32, i32, f32, ctypes.c_uint64, vp, vp],
         "lpg_elliptic_set_learned_smoother": [vp, vp, f64],
+        "lpg_debug_mlp_hold": [ctypes.c_uint64],
         "lpg_elliptic_plot_fields": [vp, vp, ctypes.c_char_p],
         "lpg_hex_mesh_info": [ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
                               ctypes.POINTER(ctypes.c_int64)],

@@ -35,7 +35,7 @@ ax_hex_kernel(const int64_t Nelements, const int32_t* __restrict__ elementList,
               const int32_t* __restrict__ g2l, const G* __restrict__ ggeo, const int64_t geoStride,
               const G* __restrict__ wJ, const int64_t wJStride, const T* __restrict__ Dg,
               const T lambda, const T* __restrict__ lambdaE, const T* __restrict__ q,
-              T* __restrict__ out) {
+              T* __restrict__ out, const T outScale) {
   constexpr int NP = NQ * NQ * NQ;
   constexpr int EPB = elems_per_block<NQ>();
   __shared__ T s_D[NQ][NQ];
@@ -121,7 +121,12 @@ ax_hex_kernel(const int64_t Nelements, const int32_t* __restrict__ elementList,
 #pragma unroll
   for (int k = 0; k < NQ; ++k) {
     if (OUTMODE == OUT_ASSEMBLE) {
-      if (r_id[k] >= 0) atomicAdd(out + r_id[k], r_Aq[k]);
+      // FP32: the scaled assembly of the fused residual; FP64 always adds A q itself
+      if constexpr (std::is_same<T, float>::value) {
+        if (r_id[k] >= 0) atomicAdd(out + r_id[k], outScale * r_Aq[k]);
+      } else {
+        if (r_id[k] >= 0) atomicAdd(out + r_id[k], r_Aq[k]);
+      }
     } else if (OUTMODE == OUT_LOCAL) {
       out[nodeBase + k * NQ * NQ] = r_Aq[k];
     } else {
@@ -199,7 +204,8 @@ __global__ void __launch_bounds__(NQ * NQ * EPB)
 ax_hex_staged_kernel(const int64_t Nelements, const int32_t* __restrict__ elementList,
                      const int32_t* __restrict__ g2l, const G* __restrict__ ggeo, const int64_t geoStride,
                      const G* __restrict__ wJ, const int64_t wJStride, const T* __restrict__ Dg, const T lambda,
-                     const T* __restrict__ lambdaE, const T* __restrict__ q, T* __restrict__ out) {
+                     const T* __restrict__ lambdaE, const T* __restrict__ q, T* __restrict__ out,
+                     const T outScale) {
   static_assert(std::is_same<T, float>::value, "staged kernel is FP32");
   using L = StagedLayout<NQ, G>;
   constexpr int NP = L::NP, NT = NQ * NQ * EPB;
@@ -370,7 +376,7 @@ ax_hex_staged_kernel(const int64_t Nelements, const int32_t* __restrict__ elemen
     if (active) {
 #pragma unroll
       for (int k = 0; k < NQ; ++k)
-        if (r_id[k] >= 0) atomicAdd(out + r_id[k], r_Aq[k]);
+        if (r_id[k] >= 0) atomicAdd(out + r_id[k], outScale * r_Aq[k]);
     }
   }
   cp_async_wait<0>();
@@ -858,7 +864,8 @@ static int launch_staged(const AxArgs<T, G>& a, cudaStream_t s) {
   const int64_t grid = std::min<int64_t>(groups, (int64_t)cfg.numSMs * cfg.ctasPerSM);
   if (grid <= 0) return LPG_OK;
   kern<<<(unsigned)grid, dim3(NQ, NQ, EPB), smem, s>>>(a.Nelements, a.elementList, a.g2l, a.ggeo, a.geoStride, a.wJ,
-                                                        a.wJStride, a.D, a.lambda, a.lambdaE, a.q, a.out);
+                                                        a.wJStride, a.D, a.lambda, a.lambdaE, a.q, a.out,
+                                                        a.outScale);
   LPG_LAUNCH_CHECK("ax_hex_staged_kernel");
   return LPG_OK;
 }
@@ -943,7 +950,7 @@ static int launch_ax(const AxArgs<T, G>& a, cudaStream_t s) {
   }
   ax_hex_kernel<NQ, T, G, INMODE, OUTMODE><<<(unsigned)blocks, block, 0, s>>>(
       a.Nelements, a.elementList, a.g2l, a.ggeo, a.geoStride, a.wJ, a.wJStride, a.D, a.lambda,
-      a.lambdaE, a.q, a.out);
+      a.lambdaE, a.q, a.out, a.outScale);
   LPG_LAUNCH_CHECK("ax_hex_kernel");
   return LPG_OK;
 }
@@ -965,6 +972,8 @@ static int dispatch_ax(const AxArgs<T, G>& a, cudaStream_t s) {
 
 template <typename T, typename G>
 int ax_hex(const AxArgs<T, G>& a, AxMode mode, cudaStream_t s) {
+  if (!std::is_same<T, float>::value && a.outScale != T(1))
+    return set_error(LPG_ERR_UNSUPPORTED, "ax: a scaled assembly is provided for FP32 only");
   switch (mode) {
     case AxMode::Assemble: {
       if (a.Nglobal > 0) LPG_CUDA_TRY(cudaMemsetAsync(a.out, 0, sizeof(T) * a.Nglobal, s));

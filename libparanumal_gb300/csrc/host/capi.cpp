@@ -212,6 +212,14 @@ extern "C" int lpg_device_malloc(void** ptr, uint64_t bytes) {
   LPG_CUDA_TRY(cudaMalloc(ptr, bytes));
   return LPG_OK;
 }
+extern "C" int lpg_set_device(int device) {
+  LPG_CUDA_TRY(cudaSetDevice(device));
+  return LPG_OK;
+}
+extern "C" int lpg_memcpy_d2d(void* dst, const void* src, uint64_t bytes, void* stream) {
+  LPG_CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, (cudaStream_t)stream));
+  return LPG_OK;
+}
 extern "C" int lpg_device_free(void* ptr) {
   LPG_CUDA_TRY(cudaFree(ptr));
   return LPG_OK;
@@ -272,6 +280,116 @@ extern "C" int lpg_pcg_update_f64(int64_t N, double alpha, const double* p, cons
   return pcg_update(N, alpha, p, Ap, x, r, result_dev, scratch, (cudaStream_t)stream);
 }
 
+extern "C" int lpg_norm2_f64(int64_t N, const double* x, double* result_dev, void* stream) {
+  if (N < 0 || !result_dev || (N > 0 && !x)) return set_error(LPG_ERR_INVALID, "norm2: bad arguments");
+  double* scratch;
+  int rc = reduction_scratch(&scratch);
+  if (rc) return rc;
+  return norm2(N, x, result_dev, scratch, (cudaStream_t)stream);
+}
+extern "C" int lpg_jacobi_f64(int64_t N, const double* invDiag, const double* r, double* z, void* stream) {
+  if (N < 0 || (N > 0 && (!invDiag || !r || !z))) return set_error(LPG_ERR_INVALID, "jacobi: bad arguments");
+  return amxpy<double>(N, 1.0, invDiag, r, 0.0, z, (cudaStream_t)stream);
+}
+
+// p-multigrid transfers and Chebyshev passes, FP64 and FP32 (the preconditioner levels'
+// precision)
+template <typename T>
+static int restrict_entry(int Nf, int Nc, int64_t E, const int32_t* g2lF, const T* weightF, const T* rF, const T* P,
+                          const int32_t* g2lC, T* rC, int64_t NglobalC, void* stream) {
+  if (Nf < 1 || Nf > 8 || Nc < 1 || Nc > Nf || E < 0 || NglobalC < 0 ||
+      (E > 0 && (!g2lF || !weightF || !rF || !P || !g2lC)) || (NglobalC > 0 && !rC))
+    return set_error(LPG_ERR_INVALID, "pmg restrict: bad arguments (1 <= Nc <= Nf <= 8)");
+  return pmg_coarsen<T>(Nf, Nc, E, g2lF, weightF, rF, P, g2lC, rC, NglobalC, (cudaStream_t)stream);
+}
+template <typename T>
+static int prolong_entry(int Nf, int Nc, int64_t E, const int32_t* g2lC, const T* xC, const T* P,
+                         const int32_t* g2lF, const int32_t* ownerF, T* xF, void* stream) {
+  if (Nf < 1 || Nf > 8 || Nc < 1 || Nc > Nf || E < 0 || (E > 0 && (!g2lC || !xC || !P || !g2lF || !ownerF || !xF)))
+    return set_error(LPG_ERR_INVALID, "pmg prolong: bad arguments (1 <= Nc <= Nf <= 8)");
+  return pmg_prolongate_map<T>(Nf, Nc, E, g2lC, xC, P, g2lF, ownerF, xF, (cudaStream_t)stream);
+}
+extern "C" int lpg_pmg_restrict_f64(int Nf, int Nc, int64_t E, const int32_t* g2lF, const double* weightF,
+                                    const double* rF, const double* P, const int32_t* g2lC, double* rC,
+                                    int64_t NglobalC, void* stream) {
+  return restrict_entry<double>(Nf, Nc, E, g2lF, weightF, rF, P, g2lC, rC, NglobalC, stream);
+}
+extern "C" int lpg_pmg_restrict_f32(int Nf, int Nc, int64_t E, const int32_t* g2lF, const float* weightF,
+                                    const float* rF, const float* P, const int32_t* g2lC, float* rC,
+                                    int64_t NglobalC, void* stream) {
+  return restrict_entry<float>(Nf, Nc, E, g2lF, weightF, rF, P, g2lC, rC, NglobalC, stream);
+}
+extern "C" int lpg_pmg_prolong_add_f64(int Nf, int Nc, int64_t E, const int32_t* g2lC, const double* xC,
+                                       const double* P, const int32_t* g2lF, const int32_t* ownerF, double* xF,
+                                       void* stream) {
+  return prolong_entry<double>(Nf, Nc, E, g2lC, xC, P, g2lF, ownerF, xF, stream);
+}
+extern "C" int lpg_pmg_prolong_add_f32(int Nf, int Nc, int64_t E, const int32_t* g2lC, const float* xC,
+                                       const float* P, const int32_t* g2lF, const int32_t* ownerF, float* xF,
+                                       void* stream) {
+  return prolong_entry<float>(Nf, Nc, E, g2lC, xC, P, g2lF, ownerF, xF, stream);
+}
+template <typename T>
+static int cheb_start_entry(int64_t N, const T* invDiag, const T* r, const T* Ax, T* res, T* d, T* x, T invTheta,
+                            int xIsZero, void* stream) {
+  if (N < 0 || (N > 0 && (!invDiag || !r || !res || !d || !x || (!xIsZero && !Ax))))
+    return set_error(LPG_ERR_INVALID, "cheb start: bad arguments");
+  return cheb_start<T>(N, invDiag, r, Ax, res, d, x, invTheta, xIsZero != 0, (cudaStream_t)stream);
+}
+template <typename T>
+static int cheb_step_entry(int64_t N, const T* invDiag, const T* Ad, T* res, T* d, T* x, T a, T b, void* stream) {
+  if (N < 0 || (N > 0 && (!invDiag || !Ad || !res || !d || !x))) return set_error(LPG_ERR_INVALID, "cheb step: bad arguments");
+  return cheb_step<T>(N, invDiag, Ad, res, d, x, a, b, (cudaStream_t)stream);
+}
+extern "C" int lpg_cheb_start_f64(int64_t N, const double* invDiag, const double* r, const double* Ax, double* res,
+                                  double* d, double* x, double invTheta, int xIsZero, void* stream) {
+  return cheb_start_entry<double>(N, invDiag, r, Ax, res, d, x, invTheta, xIsZero, stream);
+}
+extern "C" int lpg_cheb_start_f32(int64_t N, const float* invDiag, const float* r, const float* Ax, float* res,
+                                  float* d, float* x, float invTheta, int xIsZero, void* stream) {
+  return cheb_start_entry<float>(N, invDiag, r, Ax, res, d, x, invTheta, xIsZero, stream);
+}
+extern "C" int lpg_cheb_update_f64(int64_t N, const double* invDiag, const double* Ad, double* res, double* d,
+                                   double* x, double a, double b, void* stream) {
+  return cheb_step_entry<double>(N, invDiag, Ad, res, d, x, a, b, stream);
+}
+extern "C" int lpg_cheb_update_f32(int64_t N, const float* invDiag, const float* Ad, float* res, float* d, float* x,
+                                   float a, float b, void* stream) {
+  return cheb_step_entry<float>(N, invDiag, Ad, res, d, x, a, b, stream);
+}
+
+// parAlmond level kernels (CSR: int64 row starts, int32 columns, FP64 values)
+static bool csr_ok(int64_t n, const int64_t* rs, const int32_t* cols, const double* vals) {
+  return n >= 0 && (n == 0 || (rs && cols && vals));
+}
+extern "C" int lpg_csr_spmv_f64(int64_t Nrows, const int64_t* rowStarts, const int32_t* cols, const double* vals,
+                                double alpha, const double* x, double beta, double* y, void* stream) {
+  if (!csr_ok(Nrows, rowStarts, cols, vals) || (Nrows > 0 && (!x || !y)))
+    return set_error(LPG_ERR_INVALID, "csr spmv: bad arguments");
+  return csr_spmv(Nrows, rowStarts, cols, vals, alpha, x, beta, y, (cudaStream_t)stream);
+}
+extern "C" int lpg_csr_cheb_start_f64(int64_t N, double invTheta, const double* diagInv, const double* b, double* r,
+                                      double* d, double* x, void* stream) {
+  if (N < 0 || (N > 0 && (!diagInv || !b || !r || !d || !x))) return set_error(LPG_ERR_INVALID, "csr cheb start: bad arguments");
+  return csr_cheb_start(N, invTheta, diagInv, b, r, d, x, (cudaStream_t)stream);
+}
+extern "C" int lpg_csr_cheb_residual_f64(int64_t N, const int64_t* rowStarts, const int32_t* cols, const double* vals,
+                                         double alpha, double beta, const double* diagInv, const double* b,
+                                         const double* x, double* r, void* stream) {
+  if (!csr_ok(N, rowStarts, cols, vals) || (N > 0 && (!diagInv || !b || !x || !r)))
+    return set_error(LPG_ERR_INVALID, "csr cheb residual: bad arguments");
+  return csr_cheb_residual(N, rowStarts, cols, vals, alpha, beta, diagInv, b, x, r, (cudaStream_t)stream);
+}
+extern "C" int lpg_csr_cheb_update_f64(int64_t N, double a, double b, int lastIt, const double* r, double* d,
+                                       double* x, void* stream) {
+  if (N < 0 || (N > 0 && (!r || !d || !x))) return set_error(LPG_ERR_INVALID, "csr cheb update: bad arguments");
+  return csr_cheb_update(N, a, b, lastIt, r, d, x, (cudaStream_t)stream);
+}
+extern "C" int lpg_gemv_f64(int64_t n, const double* A, const double* x, double* y, void* stream) {
+  if (n < 0 || (n > 0 && (!A || !x || !y))) return set_error(LPG_ERR_INVALID, "gemv: bad arguments");
+  return gemv(n, A, x, y, (cudaStream_t)stream);
+}
+
 // ================================================================ solver objects
 extern "C" int lpg_elliptic_create(const char* settings, lpg_elliptic** out) {
   if (!settings || !out) return set_error(LPG_ERR_INVALID, "null argument");
@@ -311,6 +429,7 @@ extern "C" int64_t lpg_elliptic_info(const lpg_elliptic* e, int what) {
     case LPG_INFO_HOST_CHUNKS: return e->el->pipe ? e->el->pipe->K : 0;
     case LPG_INFO_IG_HISTORY: return e->ig ? e->ig->history() : 0;
     case LPG_INFO_OPERATOR_APPLICATIONS: return e->el->nOps;
+    case LPG_INFO_LEARNED_TIMEOUTS: return e->precon ? e->precon->learned_timeouts() : 0;
     default: return -1;
   }
 }
@@ -457,6 +576,18 @@ extern "C" int lpg_elliptic_precon(lpg_elliptic* e, const double* r, double* z, 
     return LPG_OK;
   }
   return e->precon->apply(r, z, s);
+  LPG_GUARD_END
+}
+
+extern "C" int lpg_elliptic_zero_mean(lpg_elliptic* e, double* q, void* stream) {
+  if (!e || !q) return set_error(LPG_ERR_INVALID, "null argument");
+  LPG_GUARD_BEGIN
+  Elliptic* el = e->el.get();
+  if (!el->allNeumann) return LPG_OK;
+  cudaStream_t s = stream ? (cudaStream_t)stream : e->plat.stream;
+  int rc;
+  if ((rc = sum(el->Nglobal, q, e->plat.scalars.p + 1, e->plat.partials.p, s))) return rc;
+  return add_scalar(el->Nglobal, e->plat.scalars.p + 1, -el->allNeumannScale * el->allNeumannScale, q, s);
   LPG_GUARD_END
 }
 
@@ -648,6 +779,11 @@ extern "C" int lpg_mlp_forward_bf16(const float* params, int64_t B, const float*
   LPG_CUDA_TRY(cudaStreamSynchronize(s));
   return LPG_OK;
   LPG_GUARD_END
+}
+
+extern "C" int lpg_debug_mlp_hold(uint64_t ns) {
+  mlp_tc_set_hold((unsigned long long)ns);
+  return LPG_OK;
 }
 
 extern "C" int lpg_smoother_train(const char* settings, int nsolves, int samples_per_solve, int epochs, int batch,

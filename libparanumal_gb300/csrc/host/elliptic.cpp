@@ -462,10 +462,12 @@ int Elliptic::Operator(const double* q, double* Aq, cudaStream_t s) {
   return ax_hex<double, double>(a, AxMode::Assemble, s);
 }
 
-int Elliptic::OperatorF32(const float* q, float* Aq, Prec prec, cudaStream_t s) {
+int Elliptic::OperatorF32(const float* q, float* Aq, Prec prec, cudaStream_t s, float accumulate) {
   ++nOps;
   const int64_t Np = mesh.Np;
+  const AxMode mode = accumulate != 0.f ? AxMode::AccumulateAssembled : AxMode::Assemble;
   if (ipdg) {
+    if (accumulate != 0.f) return set_error(LPG_ERR_UNSUPPORTED, "IPDG: no accumulating FP32 operator");
     if (prec != Prec::F32 || !vgeo32.p) return set_error(LPG_ERR_UNSUPPORTED, "IPDG: FP32 operator not prepared");
     IpdgArgsF32 a;
     a.N = mesh.N; a.E = mesh.E;
@@ -483,14 +485,16 @@ int Elliptic::OperatorF32(const float* q, float* Aq, Prec prec, cudaStream_t s) 
     a.ggeo = mesh.geo16.p; a.geoStride = 7 * Np; a.wJ = mesh.geo16.p + 6 * Np; a.wJStride = 7 * Np;
     a.D = mesh.D32.p; a.lambda = (float)lambda; a.lambdaE = hasLambdaE ? lambdaE32.p : nullptr;
     a.q = q; a.out = Aq; a.Nglobal = Nglobal;
-    return ax_hex<float, __nv_bfloat16>(a, AxMode::Assemble, s);
+    if (accumulate != 0.f) a.outScale = accumulate;
+    return ax_hex<float, __nv_bfloat16>(a, mode, s);
   }
   AxArgs<float, float> a;
   a.N = mesh.N; a.Nelements = mesh.E; a.g2l = g2l.p;
   a.ggeo = mesh.geo32.p; a.geoStride = 7 * Np; a.wJ = mesh.geo32.p + 6 * Np; a.wJStride = 7 * Np;
   a.D = mesh.D32.p; a.lambda = (float)lambda; a.lambdaE = hasLambdaE ? lambdaE32.p : nullptr;
   a.q = q; a.out = Aq; a.Nglobal = Nglobal;
-  return ax_hex<float, float>(a, AxMode::Assemble, s);
+  if (accumulate != 0.f) a.outScale = accumulate;
+  return ax_hex<float, float>(a, mode, s);
 }
 
 // ---------------------------------------------------------------- host-buffer operator

@@ -64,7 +64,7 @@ int LearnedSmoother::check_tc(cudaStream_t s) {
   int code = 0;
   int rc = tcErr.download(&code, 1, s);
   if (rc) return rc;
-  if (code) return set_error(LPG_ERR_CUDA, "MLP tensor-core pipeline timed out (code " + std::to_string(code) + ")");
+  if (code) return set_error(LPG_ERR_TIMEOUT, "MLP tensor-core pipeline timed out (code " + std::to_string(code) + ")");
   return LPG_OK;
 }
 

@@ -452,7 +452,7 @@ class MultiGrid : public Precon {
   LearnedSmoother* learned = nullptr;
   BoxNumbering box{};
   double threshold = 0.5;
-  int64_t nFallback = 0, nVcycle = 0;
+  int64_t nFallback = 0, nVcycle = 0, nTimeout = 0;
   DevBuf<double> lcoef64, ljac64;
   DevBuf<float> lcoef32, ljac32;
 
@@ -460,6 +460,7 @@ class MultiGrid : public Precon {
   int levels_amg() const override { return (int)a.size(); }
   int64_t coarse_n() const override { return coarseN; }
   int64_t fallbacks() const override { return nFallback; }
+  int64_t learned_timeouts() const override { return nTimeout; }
   int64_t vcycles() const override { return nVcycle; }
   double fine_rho() const override {
     if (p.empty()) return 0;
@@ -471,7 +472,7 @@ class MultiGrid : public Precon {
     learned = L;
     box = b;
     threshold = thr;
-    nFallback = nVcycle = 0;
+    nFallback = nVcycle = nTimeout = 0;
     if (!L) return LPG_OK;
     // 1/diag of the fine level (the damped-Jacobi smoother stores it pre-scaled by 4/3/rho)
     PLevel& F = *p[0];
@@ -498,6 +499,7 @@ class MultiGrid : public Precon {
   bool f32() const { return opt.prec != Prec::F64; }
   template <typename T> T* vec(DevBuf<double>& d, DevBuf<float>& f);
   template <typename T> int op(Elliptic* el, const T* q, T* Aq, cudaStream_t s);
+  template <typename T> int residual(Elliptic* el, const T* RHS, const T* X, T* RES, cudaStream_t s);
   template <typename T> int smooth(PLevel& L, const T* r, T* x, bool xIsZero, cudaStream_t s);
   template <typename T> int vcycle_p(int k, const T* rhs, T* x, cudaStream_t s);
   template <typename T> int coarse_correct(int k, const T* RES, T* X, cudaStream_t s);
@@ -518,6 +520,25 @@ int MultiGrid::op<double>(Elliptic* el, const double* q, double* Aq, cudaStream_
 template <>
 int MultiGrid::op<float>(Elliptic* el, const float* q, float* Aq, cudaStream_t s) {
   return el->OperatorF32(q, Aq, opt.prec, s);
+}
+
+// RES = RHS - A X. The C0 FP32 operator assembles straight into a copy of RHS with the
+// sign of the contributions flipped (one copy instead of a memset and an axpy pass).
+template <>
+int MultiGrid::residual<double>(Elliptic* el, const double* RHS, const double* X, double* RES, cudaStream_t s) {
+  int rc;
+  if ((rc = el->Operator(X, RES, s))) return rc;
+  return axpy<double>(el->Nglobal, 1.0, RHS, -1.0, RES, s);
+}
+template <>
+int MultiGrid::residual<float>(Elliptic* el, const float* RHS, const float* X, float* RES, cudaStream_t s) {
+  int rc;
+  if (el->ipdg) {
+    if ((rc = el->OperatorF32(X, RES, opt.prec, s))) return rc;
+    return axpy<float>(el->Nglobal, 1.f, RHS, -1.f, RES, s);
+  }
+  LPG_CUDA_TRY(cudaMemcpyAsync(RES, RHS, sizeof(float) * el->Nglobal, cudaMemcpyDeviceToDevice, s));
+  return el->OperatorF32(X, RES, opt.prec, s, -1.f);
 }
 
 // ---------------------------------------------------------------- p-level smoothing
@@ -548,7 +569,10 @@ int MultiGrid::smooth(PLevel& L, const T* r, T* X, bool xIsZero, cudaStream_t s)
     if ((rc = op<T>(L.el, d, Ad, s))) return rc;
     rho_np1 = 1.0 / (2. * sigma - rho_n);
     const double rhoDivDelta = 2.0 * rho_np1 / delta;
-    if ((rc = cheb_step<T>(N, invDiag, Ad, RES, d, X, (T)(rho_np1 * rho_n), (T)rhoDivDelta, s))) return rc;
+    // the last step's res and d are not read again: it writes x only
+    if ((rc = cheb_step<T>(N, invDiag, Ad, RES, d, X, (T)(rho_np1 * rho_n), (T)rhoDivDelta, s,
+                           k == opt.chebDegree - 1)))
+      return rc;
     rho_n = rho_np1;
   }
   return LPG_OK;
@@ -561,8 +585,7 @@ int MultiGrid::vcycle_p(int k, const T* RHS, T* X, cudaStream_t s) {
   T* RES = vec<T>(L.res64, L.res32);
   int rc;
   if ((rc = smooth<T>(L, RHS, X, true, s))) return rc;
-  if ((rc = op<T>(L.el, X, RES, s))) return rc;
-  if ((rc = axpy<T>(N, T(1), RHS, T(-1), RES, s))) return rc;
+  if ((rc = residual<T>(L.el, RHS, X, RES, s))) return rc;
   if ((rc = coarse_correct<T>(k, RES, X, s))) return rc;
   return smooth<T>(L, RHS, X, false, s);
 }
@@ -652,14 +675,28 @@ int MultiGrid::vcycle_learned(const T* RHS, T* X, cudaStream_t s) {
     if ((r = axpy<T>(N, (T)w, D, T(1), X, s)) || (r = axpy<T>(N, (T)(-w), AD, T(1), RES, s))) return r;
     return LPG_OK;
   };
-  LPG_CUDA_TRY(cudaMemsetAsync(X, 0, sizeof(T) * N, s));
-  LPG_CUDA_TRY(cudaMemcpyAsync(RES, RHS, sizeof(T) * N, cudaMemcpyDeviceToDevice, s));
-  for (int k = 0; k < opt.learnedSteps; ++k)
-    if ((rc = smooth_step())) return rc;
-  if ((rc = coarse_correct<T>(0, RES, X, s))) return rc;
-  if ((rc = op<T>(el, X, RES, s)) || (rc = axpy<T>(N, T(1), RHS, T(-1), RES, s))) return rc;
-  for (int k = 0; k < opt.learnedSteps; ++k)
-    if ((rc = smooth_step())) return rc;
+  // a tensor-core pipeline timeout inside the network (LPG_ERR_TIMEOUT) abandons the
+  // learned attempt: the V-cycle is redone with the plain smoother and counted
+  auto learned_part = [&]() -> int {
+    int r;
+    LPG_CUDA_TRY(cudaMemsetAsync(X, 0, sizeof(T) * N, s));
+    LPG_CUDA_TRY(cudaMemcpyAsync(RES, RHS, sizeof(T) * N, cudaMemcpyDeviceToDevice, s));
+    for (int k = 0; k < opt.learnedSteps; ++k)
+      if ((r = smooth_step())) return r;
+    if ((r = coarse_correct<T>(0, RES, X, s))) return r;
+    if ((r = residual<T>(el, RHS, X, RES, s))) return r;
+    for (int k = 0; k < opt.learnedSteps; ++k)
+      if ((r = smooth_step())) return r;
+    return LPG_OK;
+  };
+  rc = learned_part();
+  if (rc == LPG_ERR_TIMEOUT) {
+    nVcycle++;
+    nFallback++;
+    nTimeout++;
+    return vcycle_p<T>(0, RHS, X, s);
+  }
+  if (rc) return rc;
   // residual reduction of this V-cycle
   double rr, bb;
   if ((rc = dot_host<T>(N, RES, RES, rr, s)) || (rc = dot_host<T>(N, RHS, RHS, bb, s))) return rc;

@@ -198,7 +198,8 @@ struct Elliptic {
   bool opDW = false;
   int Operator(const double* q, double* Aq, cudaStream_t s);
   int OperatorDW(const double* q, double* Aq, cudaStream_t s);
-  int OperatorF32(const float* q, float* Aq, Prec prec, cudaStream_t s);
+  // accumulate = 0: Aq = A q; otherwise Aq += accumulate * A q (C0 only)
+  int OperatorF32(const float* q, float* Aq, Prec prec, cudaStream_t s, float accumulate = 0.f);
   // Aq = A q with host buffers (page-locked for overlap); returns when Aq is filled
   std::unique_ptr<HostPipe> pipe;
   int BuildPipe(cudaStream_t s);
@@ -227,6 +228,7 @@ struct Precon {
     return set_error(LPG_ERR_UNSUPPORTED, "a learned smoother needs PRECONDITIONER = MULTIGRID");
   }
   virtual int64_t fallbacks() const { return 0; }
+  virtual int64_t learned_timeouts() const { return 0; }
   // spectral radius estimate of D^{-1} A on the finest p-level (0 without p-levels)
   virtual double fine_rho() const { return 0; }
   virtual int64_t vcycles() const { return 0; }

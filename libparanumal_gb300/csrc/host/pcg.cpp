@@ -37,6 +37,13 @@ int pcg_solve(Platform* plat, Elliptic* el, Precon* pc, PCGWork& w, bool flexibl
   if (!stopRhs) TOL = std::max(tol * tol * rdotr0, tol * tol);
   int iter;
   res.breakdown = false;
+  // a NaN or Inf in the right-hand side or the initial guess: stop before iterating on it
+  if (!std::isfinite(rdotr0) || !std::isfinite(TOL)) {
+    res.breakdown = true;
+    res.iters = 0;
+    res.rdotr = rdotr0;
+    return LPG_OK;
+  }
   for (iter = 0; iter < maxit; ++iter) {
     if ((iter == 0 && rdotr0 == 0.0) || (iter > 0 && rdotr0 <= TOL)) break;
     if ((rc = pc->apply(r, w.z.p, s))) return rc;
@@ -109,6 +116,12 @@ int nbfpcg_solve(Platform* plat, Elliptic* el, Precon* pc, NBWork& w, double* x,
   const double TOL = std::max(tol * tol * rdotr0, tol * tol);
   int iter;
   res.breakdown = false;
+  if (!std::isfinite(rdotr0) || !std::isfinite(alpha0)) {
+    res.breakdown = true;
+    res.iters = 0;
+    res.rdotr = rdotr0;
+    return LPG_OK;
+  }
   for (iter = 0; iter < maxit; ++iter) {
     if (rdotr0 <= TOL) break;
     double d4[4];

@@ -27,6 +27,10 @@ struct AxArgs {
   const T* q = nullptr;
   T* out = nullptr;
   int64_t Nglobal = 0;
+  // assembled modes: out += outScale * A q (FP32 kernels only; FP64 requires 1). With
+  // out preset to b and outScale = -1 an AccumulateAssembled launch leaves the residual
+  // b - A q without a separate vector pass.
+  T outScale = T(1);
 };
 
 template <typename T, typename G>
@@ -116,6 +120,7 @@ int reduction_blocks(int64_t N);  // stage-1 CTAs (= partial sums) used for N en
 int dot(int64_t N, const double* x, const double* y, double* out, double* partials, cudaStream_t s);
 int dot_f32(int64_t N, const float* x, const float* y, double* out, double* partials, cudaStream_t s);
 int sum(int64_t N, const double* x, double* out, double* partials, cudaStream_t s);
+int norm2(int64_t N, const double* x, double* out, double* partials, cudaStream_t s);   // sqrt(x.x)
 int pcg_update(int64_t N, double alpha, const double* p, const double* Ap, double* x, double* r,
                double* out, double* partials, cudaStream_t s);
 int add_scalar(int64_t N, const double* scalarDev, double scale, double* x, cudaStream_t s);
@@ -129,7 +134,8 @@ template <typename T>
 int cheb_start(int64_t N, const T* invDiag, const T* r, const T* Ax, T* res, T* d, T* x, T invTheta, bool xIsZero,
                cudaStream_t s);
 template <typename T>
-int cheb_step(int64_t N, const T* invDiag, const T* Ad, T* res, T* d, T* x, T a, T b, cudaStream_t s);
+int cheb_step(int64_t N, const T* invDiag, const T* Ad, T* res, T* d, T* x, T a, T b, cudaStream_t s,
+              bool last = false);
 
 // ---------------------------------------------------------------- p-multigrid transfers
 // xC = assembled sum over coarse copies of P^T (weightF .* xF) per element (xC overwritten)

@@ -70,6 +70,10 @@ int transpose_to_bf16(int K, int N, const float* W, __nv_bfloat16* Wt, cudaStrea
 // pipeline timed out; the caller reads it after the stream has run.
 int mlp_forward_tc(int64_t B, const __nv_bfloat16* X, const __nv_bfloat16* const Wt[4], const float* const bias[4],
                    float* Y, int* errFlag, cudaStream_t s);
+// Diagnostics: every following mlp_forward_tc launch first waits up to ns nanoseconds on a
+// barrier that nothing signals, then records a pipeline timeout (code 8) before issuing any
+// copy or MMA; 0 turns this off.
+void mlp_tc_set_hold(unsigned long long ns);
 
 template <typename TIN, typename TOUT>
 // scale_e = max(RMS of the element's residual, sfloor); features = values / scale_e

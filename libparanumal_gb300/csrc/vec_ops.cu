@@ -255,11 +255,11 @@ reduce_stage1(const int64_t N, const void* __restrict__ xv, const void* __restri
 }
 
 __global__ void __launch_bounds__(kRedThreads)
-reduce_stage2(const int nparts, const double* __restrict__ partials, double* __restrict__ out) {
+reduce_stage2(const int nparts, const double* __restrict__ partials, double* __restrict__ out, const int root = 0) {
   double acc = 0;
   for (int i = threadIdx.x; i < nparts; i += blockDim.x) acc += partials[i];
   acc = block_sum(acc);
-  if (threadIdx.x == 0) *out = acc;
+  if (threadIdx.x == 0) *out = root ? sqrt(acc) : acc;
 }
 
 static inline int red_blocks(int64_t N) {
@@ -289,6 +289,14 @@ int dot_f32(int64_t N, const float* x, const float* y, double* out, double* part
 }
 int sum(int64_t N, const double* x, double* out, double* partials, cudaStream_t s) {
   return reduce<RED_SUM>(N, x, nullptr, out, partials, s);
+}
+int norm2(int64_t N, const double* x, double* out, double* partials, cudaStream_t s) {
+  const int nb = red_blocks(N);
+  reduce_stage1<RED_DOT><<<nb, kRedThreads, 0, s>>>(N, x, x, partials);
+  LPG_LAUNCH_CHECK("reduce_stage1");
+  reduce_stage2<<<1, kRedThreads, 0, s>>>(nb, partials, out, 1);
+  LPG_LAUNCH_CHECK("reduce_stage2");
+  return LPG_OK;
 }
 
 __global__ void __launch_bounds__(kRedThreads)
@@ -366,14 +374,17 @@ __global__ void cheb_start_kernel(const int64_t N, const T* __restrict__ invDiag
     x[n] = xIsZero ? dn : x[n] + dn;
   }
 }
-template <typename T>
+// LAST: the smoother's final step, whose res and d nobody reads again: only x is written
+template <typename T, bool LAST>
 __global__ void cheb_step_kernel(const int64_t N, const T* __restrict__ invDiag, const T* __restrict__ Ad,
                                  T* __restrict__ res, T* __restrict__ d, T* __restrict__ x, const T a, const T b) {
   for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x) {
     const T rn = res[n] - invDiag[n] * Ad[n];
-    res[n] = rn;
     const T dn = b * rn + a * d[n];
-    d[n] = dn;
+    if (!LAST) {
+      res[n] = rn;
+      d[n] = dn;
+    }
     x[n] = x[n] + dn;
   }
 }
@@ -387,9 +398,10 @@ int cheb_start(int64_t N, const T* invDiag, const T* r, const T* Ax, T* res, T* 
   return LPG_OK;
 }
 template <typename T>
-int cheb_step(int64_t N, const T* invDiag, const T* Ad, T* res, T* d, T* x, T a, T b, cudaStream_t s) {
+int cheb_step(int64_t N, const T* invDiag, const T* Ad, T* res, T* d, T* x, T a, T b, cudaStream_t s, bool last) {
   if (N <= 0) return LPG_OK;
-  cheb_step_kernel<T><<<grid_for(N, 256, kStreamCap), 256, 0, s>>>(N, invDiag, Ad, res, d, x, a, b);
+  if (last) cheb_step_kernel<T, true><<<grid_for(N, 256, kStreamCap), 256, 0, s>>>(N, invDiag, Ad, res, d, x, a, b);
+  else cheb_step_kernel<T, false><<<grid_for(N, 256, kStreamCap), 256, 0, s>>>(N, invDiag, Ad, res, d, x, a, b);
   LPG_LAUNCH_CHECK("cheb_step_kernel");
   return LPG_OK;
 }
@@ -398,8 +410,9 @@ template int cheb_start<double>(int64_t, const double*, const double*, const dou
 template int cheb_start<float>(int64_t, const float*, const float*, const float*, float*, float*, float*, float, bool,
                                cudaStream_t);
 template int cheb_step<double>(int64_t, const double*, const double*, double*, double*, double*, double, double,
-                               cudaStream_t);
-template int cheb_step<float>(int64_t, const float*, const float*, float*, float*, float*, float, float, cudaStream_t);
+                               cudaStream_t, bool);
+template int cheb_step<float>(int64_t, const float*, const float*, float*, float*, float*, float, float, cudaStream_t,
+                              bool);
 
 // ---------------------------------------------------------------- initial-guess history
 // Kernels of the initial-guess strategies (libs/linearSolver/okl/igBasisInnerProducts.okl,

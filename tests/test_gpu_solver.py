@@ -103,6 +103,36 @@ def test_pmg_preconditioner_application_matches_oracle():
     assert rel_err(z.cpu().numpy(), o.precon(rh)) < 1e-9
 
 
+@pytest.mark.parametrize("over", [
+    {"MULTIGRID SMOOTHER": "DAMPEDJACOBI"},
+    {"MULTIGRID SMOOTHER": "DAMPEDJACOBI", "PARALMOND SMOOTHER": "DAMPEDJACOBI"},
+    {"MULTIGRID SMOOTHER": "DAMPEDJACOBI", "MULTIGRID DEGREES": "7,5,3,1", "LAMBDA FIELD": "LOGNORMAL",
+     "LAMBDA SEED": 2, "LAMBDA": 1.0},
+], ids=["pmg", "pmg_and_amg", "7531_lognormal"])
+def test_damped_jacobi_smoother_matches_oracle(over):
+    """MGLevel::smoothJacobi (ellipticPreconMultiGridLevel.cpp:135-152) with the weight
+    4/3/rho from the level's Arnoldi estimate (:370-383), and parCSR::smoothDampedJacobi on
+    the AMG levels (parAlmondAMGSmoother.cpp): one preconditioner application against the
+    oracle (1e-9), then the FPCG solve (same iterations, solution 1e-7)."""
+    s = dict(MG, **over)
+    e = lpg.Elliptic(s)
+    o = Oracle(s)
+    rh = np.random.default_rng(5).standard_normal(e.Nglobal)
+    r = torch.tensor(rh, device="cuda")
+    z = torch.zeros_like(r)
+    e.precon(r, z)
+    torch.cuda.synchronize()
+    assert rel_err(z.cpu().numpy(), o.precon(rh)) < 1e-9
+    res = e.Run(want_solution=True)
+    ro = o.run()
+    assert res["converged"]
+    assert res["iterations"] == ro["iterations"], (res["iterations"], ro["iterations"])
+    assert rel_err(res["xL"], ro["xL"]) < 1e-7
+    # damped Jacobi is the weaker smoother: more iterations than Chebyshev on the same problem
+    rc = lpg.Elliptic(dict(s, **{"MULTIGRID SMOOTHER": "CHEBYSHEV", "PARALMOND SMOOTHER": "CHEBYSHEV"})).Run()
+    assert rc["iterations"] < res["iterations"]
+
+
 @pytest.mark.parametrize("prec", ["FP32", "BF16GEO"])
 def test_mixed_precision_preconditioner_keeps_fp64_accuracy(prec):
     s = dict(MG, **{"PRECONDITIONER PRECISION": prec})
