@@ -72,6 +72,10 @@ def parse():
     ap.add_argument("--mlp", action="store_true", help="learned-smoother MLP inference (lpg_mlp_forward_bf16) timing")
     ap.add_argument("--ipdg", action="store_true", help="IPDG operator (gradient + Ax) throughput")
     ap.add_argument("--sequence", action="store_true", help="repeated solves with each initial-guess strategy")
+    ap.add_argument("--heat", action="store_true", help="backward-Euler time steps with each initial-guess strategy")
+    ap.add_argument("--learned-pair", action="store_true", help="one plain and one learned FP32+DF64 solve")
+    ap.add_argument("--weights", default="", help="--learned-pair: network weights (.npy) instead of training")
+    ap.add_argument("--save-weights", default="", help="--learned-pair: write the trained weights (.npy)")
     ap.add_argument("--train-nx", type=int, default=32)
     ap.add_argument("--train-samples", type=int, default=20000)
     ap.add_argument("--train-solves", type=int, default=8)
@@ -443,6 +447,38 @@ def run_learned(a):
     print(json.dumps(out), flush=True)
 
 
+def run_learned_pair(a):
+    """One plain FP32+DF64 Run and one learned+FP32+DF64 Run (2 steps per side, fallback
+    threshold 0.5) on the nx^3 jittered box, N=7, lognormal lambda, sine data -- the pair
+    whose ncu launch list gives the per-component cost table. Weights: --weights PATH (a
+    .npy written by --save-weights), else trained in the run on 32^3 (20,000 pairs, 40
+    epochs) and written to --save-weights when given. One JSON line."""
+    import numpy as np
+    import torch
+    import libparanumal_gb300 as lpg
+    import __graft_entry__ as g
+    g.build()
+    torch.cuda.set_device(0)
+    if a.weights:
+        w, train = np.load(a.weights), {"loaded": a.weights}
+    else:
+        w, train = train_learned()
+        if a.save_weights:
+            np.save(a.save_weights, w)
+    law = {"LAMBDA": 1.0, "LAMBDA FIELD": "LOGNORMAL", "LAMBDA SEED": 2, "OPERATOR PRECISION": "DF64"}
+    out = {"workload": "plain vs learned FP32+DF64 FPCG + p-MG, %d^3 jittered hex, N=7, lognormal lambda, sine"
+                       % a.nx, "training": train}
+    for name, learned in (("FP32+DF64", False), ("learned+FP32+DF64", True)):
+        e = lpg.Elliptic(solve_settings(a.nx, 7, "FP32", **law))
+        if learned:
+            e.set_learned_smoother(w, 0.5)
+        r = e.Run()
+        out[name] = {"iterations": r["iterations"], "solve_seconds": r["solve_seconds"], "error": r["error"],
+                     "vcycles": e.info("vcycles"), "fallbacks": e.info("fallbacks")}
+        e.close()
+    print(json.dumps(out), flush=True)
+
+
 def run_mlp(a):
     """Inference of the learned smoother's MLP through lpg_mlp_forward_bf16 (weights
     converted to BF16 inside each call) on 65,536 and 262,144 random rows: 2 warm-up and
@@ -519,6 +555,62 @@ def run_sequence(a):
                      "mean_seconds_after_3": sum(secs[3:]) / (K - 3)}
     print(json.dumps({"workload": "%d repeated solves, r(t) blending 10 Gaussian-source fields, %d^3 jittered "
                                   "hex, N=7, FPCG + p-MG (FP32+DF64), tol 1e-8 of ||r||" % (K, a.nx),
+                      "results": res}), flush=True)
+
+
+def run_heat(a):
+    """A time-stepping caller (the ins velocity-solve pattern, insVelocitySolve.cpp:30-100):
+    backward Euler for u_t = Laplacian u on the nx^3 jittered box, N=7, Dirichlet,
+    (lambda M + K) u_{n+1} = lambda M u_n with lambda = 1/dt = 10, u_0 = the steady
+    manufactured solution (sine); each step forms lambda M u_n through lpg_elliptic_mass,
+    scales it to unit norm and solves to 1e-8 of ||r|| with FPCG + p-MG (FP32
+    preconditioner, double-FP32 outer operator) and one INITIAL GUESS STRATEGY. Per
+    strategy: iterations per step and mean wall time per step (mass product + solve) over
+    the steps after the first 3. One JSON line."""
+    import torch
+    import libparanumal_gb300 as lpg
+    import __graft_entry__ as g
+    g.build()
+    torch.cuda.set_device(0)
+    lam = 10.0
+    base = solve_settings(a.nx, 7, "FP32", lam=lam, **{"OPERATOR PRECISION": "DF64",
+                                                       "LINEAR SOLVER STOPPING CRITERION": "ABS/REL-RHS-2NORM"})
+    strategies = {"ZERO": {}, "CLASSIC": {"INITIAL GUESS HISTORY SPACE DIMENSION": 8},
+                  "QR": {"INITIAL GUESS HISTORY SPACE DIMENSION": 8},
+                  "EXTRAP": {"INITIAL GUESS HISTORY SPACE DIMENSION": 4, "INITIAL GUESS EXTRAP DEGREE": 2,
+                             "INITIAL GUESS EXTRAP COEFFS METHOD": "CPQR"}}
+    K = max(a.steps, 6)
+    res = {}
+    for name, over in strategies.items():
+        e = lpg.Elliptic(dict(base, **{"INITIAL GUESS STRATEGY": name}, **over))
+        # u_0: the steady manufactured solution (O(1) nodal values), from one solve
+        b0 = torch.zeros(e.Nglobal, dtype=torch.float64, device="cuda")
+        e.rhs(b0)
+        u = torch.zeros_like(b0)
+        steady = lpg.Elliptic(dict(base, **{"INITIAL GUESS STRATEGY": "ZERO"}))
+        steady.Solve(u, b0, tol=1e-10)
+        steady.close()
+        Mu, x = torch.empty_like(u), torch.zeros_like(u)
+        its, secs = [], []
+        for _ in range(K):
+            torch.cuda.synchronize()
+            t0 = time.time()
+            e.mass(u, Mu)
+            # unit-norm right-hand side (the system is linear: u_{n+1} = ||b_n|| x_n), so the
+            # tolerance means the same at every step while the field decays
+            nb = float(Mu.norm()) * lam
+            Mu.mul_(lam / nb)
+            its.append(e.Solve(x, Mu, tol=1e-8))
+            torch.mul(x, nb, out=u)
+            torch.cuda.synchronize()
+            secs.append(time.time() - t0)
+        e.close()
+        del u, Mu, x, b0
+        torch.cuda.empty_cache()
+        res[name] = {"iterations": its, "mean_iterations_after_3": sum(its[3:]) / (K - 3),
+                     "mean_seconds_after_3": sum(secs[3:]) / (K - 3)}
+    print(json.dumps({"workload": "backward-Euler heat steps (lambda = 1/dt = %g), %d^3 jittered hex, N=7, FPCG + "
+                                  "p-MG (FP32+DF64), tol 1e-8 of ||r||, %d steps" % (lam, a.nx, K),
                       "results": res}), flush=True)
 
 
@@ -669,6 +761,10 @@ def main():
         return run_ipdg(a)
     if a.sequence:
         return run_sequence(a)
+    if a.heat:
+        return run_heat(a)
+    if a.learned_pair:
+        return run_learned_pair(a)
     import numpy as np
     import torch
     import libparanumal_gb300 as lpg

@@ -267,6 +267,12 @@ int lpg_elliptic_solve(lpg_elliptic *e, double *x, double *r, double tol, int ma
  * vector q (Nglobal, device) when the problem has the constant null space (all-Neumann
  * boundaries with lambda = 0); otherwise a no-op. */
 int lpg_elliptic_zero_mean(lpg_elliptic *e, double *q, void *stream);
+/* The assembled (diagonal GLL) mass product Mu = Gather(Trans)(wJ .* Scatter(u)) of
+ * device vectors of length Nglobal (CONTINUOUS only): the lambda M u_old term that
+ * time-stepping callers of the screened-Poisson solve add to their right-hand side, as the
+ * ins velocity solve does (solvers/ins/src/insVelocitySolve.cpp:30-100: velocityRhsKernel
+ * forms RHS = MM RHS / nu + boundary data and the elliptic lambda is gamma / nu). */
+int lpg_elliptic_mass(lpg_elliptic *e, const double *u, double *Mu, void *stream);
 /* The assembled right-hand side of elliptic_t::Run (forcing, Dirichlet lifting,
  * Gather(Trans)) into a device vector r (Nglobal). */
 int lpg_elliptic_rhs(lpg_elliptic *e, double *r, void *stream);

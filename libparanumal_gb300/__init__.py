@@ -54,6 +54,7 @@ def lib():
         "lpg_memcpy_d2d": [vp, vp, ctypes.c_uint64, vp],
         "lpg_set_device": [i32],
         "lpg_elliptic_zero_mean": [vp, vp, vp],
+        "lpg_elliptic_mass": [vp, vp, vp, vp],
         "lpg_stream_sync": [vp],
         "lpg_ax_hex_f64": ax64,
         "lpg_ax_hex_f32": ax32,
@@ -258,6 +259,10 @@ class Elliptic:
 
     def precon(self, r, z, stream=0):
         check(lib().lpg_elliptic_precon(self.h, _ptr(r), _ptr(z), stream or None))
+
+    def mass(self, u, Mu, stream=0):
+        """Mu = M u, the assembled diagonal mass product (device vectors of Nglobal)."""
+        check(lib().lpg_elliptic_mass(self.h, _ptr(u), _ptr(Mu), stream or None))
 
     def rhs(self, r):
         check(lib().lpg_elliptic_rhs(self.h, _ptr(r), None))

@@ -334,7 +334,8 @@ static int cheb_start_entry(int64_t N, const T* invDiag, const T* r, const T* Ax
                             int xIsZero, void* stream) {
   if (N < 0 || (N > 0 && (!invDiag || !r || !res || !d || !x || (!xIsZero && !Ax))))
     return set_error(LPG_ERR_INVALID, "cheb start: bad arguments");
-  return cheb_start<T>(N, invDiag, r, Ax, res, d, x, invTheta, xIsZero != 0, (cudaStream_t)stream);
+  return cheb_start<T>(N, invDiag, r, xIsZero ? nullptr : Ax, res, d, x, invTheta, xIsZero != 0,
+                       (cudaStream_t)stream);
 }
 template <typename T>
 static int cheb_step_entry(int64_t N, const T* invDiag, const T* Ad, T* res, T* d, T* x, T a, T b, void* stream) {
@@ -588,6 +589,16 @@ extern "C" int lpg_elliptic_zero_mean(lpg_elliptic* e, double* q, void* stream) 
   int rc;
   if ((rc = sum(el->Nglobal, q, e->plat.scalars.p + 1, e->plat.partials.p, s))) return rc;
   return add_scalar(el->Nglobal, e->plat.scalars.p + 1, -el->allNeumannScale * el->allNeumannScale, q, s);
+  LPG_GUARD_END
+}
+
+extern "C" int lpg_elliptic_mass(lpg_elliptic* e, const double* u, double* Mu, void* stream) {
+  if (!e || !u || !Mu) return set_error(LPG_ERR_INVALID, "null argument");
+  LPG_GUARD_BEGIN
+  Elliptic* el = e->el.get();
+  if (el->ipdg) return set_error(LPG_ERR_UNSUPPORTED, "mass product: CONTINUOUS discretisation only");
+  cudaStream_t s = stream ? (cudaStream_t)stream : e->plat.stream;
+  return mass_apply(el->mesh.N, el->mesh.E, el->mesh.geo.p, el->g2l.p, u, Mu, el->Nglobal, s);
   LPG_GUARD_END
 }
 

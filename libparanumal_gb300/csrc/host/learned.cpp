@@ -78,24 +78,16 @@ int LearnedSmoother::ensure_chunk(int64_t rows) {
   return LPG_OK;
 }
 
-// z = average over shared nodes of s_e * invDiag .* MLP(features(r))
+// z += average over shared nodes of s_e * invDiag .* MLP(features(r))
 template <typename T>
 int LearnedSmoother::apply(const BoxNumbering& b, int64_t E, const int32_t* g2l, const T* r, const T* coef, T* z,
-                           int64_t Nglobal, cudaStream_t s) {
+                           int64_t Nglobal, float sfloor, cudaStream_t s) {
+  (void)Nglobal;
   if (!ready) return set_error(LPG_ERR_INVALID, "learned smoother has no weights");
   const int Np = (b.N + 1) * (b.N + 1) * (b.N + 1);
   int rc;
   const int64_t C = std::min<int64_t>(E, kChunk);
   if ((rc = ensure_chunk(C))) return rc;
-  // floor of the element scales: kScaleFloor x the global residual RMS
-  if constexpr (std::is_same<T, double>::value) rc = dot(Nglobal, r, r, red.p, partials.p, s);
-  else rc = dot_f32(Nglobal, r, r, red.p, partials.p, s);
-  if (rc) return rc;
-  double rr = 0;
-  if ((rc = red.download(&rr, 1, s))) return rc;
-  const float sfloor = (float)(kScaleFloor * std::sqrt(rr / (double)std::max<int64_t>(Nglobal, 1)));
-  LPG_CUDA_TRY(cudaMemsetAsync(z, 0, sizeof(T) * Nglobal, s));
-  MLPParams P = MLPParams::view(params.p);
   for (int64_t e0 = 0; e0 < E; e0 += C) {
     const int64_t n = std::min<int64_t>(C, E - e0);
     if ((rc = element_features<T, __nv_bfloat16>(b, E, e0, n, g2l, r, X.p, scale.p, sfloor, s))) return rc;
@@ -105,9 +97,9 @@ int LearnedSmoother::apply(const BoxNumbering& b, int64_t E, const int32_t* g2l,
   return check_tc(s);
 }
 template int LearnedSmoother::apply<double>(const BoxNumbering&, int64_t, const int32_t*, const double*, const double*,
-                                            double*, int64_t, cudaStream_t);
+                                            double*, int64_t, float, cudaStream_t);
 template int LearnedSmoother::apply<float>(const BoxNumbering&, int64_t, const int32_t*, const float*, const float*,
-                                           float*, int64_t, cudaStream_t);
+                                           float*, int64_t, float, cudaStream_t);
 
 // ---------------------------------------------------------------- training
 double lastKeptFraction = 0;

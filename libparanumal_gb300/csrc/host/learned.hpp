@@ -24,11 +24,12 @@ struct LearnedSmoother {
   int ensure_chunk(int64_t rows);
   int forward_bf16(int64_t rows, cudaStream_t s);   // out = MLP(X) for `rows` rows
   int check_tc(cudaStream_t s);
-  // z (assembled, overwritten) = sum over copies of coef .* s_e MLP(features(r)), coef =
-  // weight / diag (the average over copies of s_e invDiag .* output)
+  // z (assembled) += sum over copies of coef .* s_e MLP(features(r)), coef = weight / diag
+  // (the average over copies of s_e invDiag .* output). Element scales s_e are floored at
+  // sfloor (the caller's kScaleFloor x residual RMS).
   template <typename T>
   int apply(const BoxNumbering& b, int64_t E, const int32_t* g2l, const T* r, const T* coef, T* z, int64_t Nglobal,
-            cudaStream_t s);
+            float sfloor, cudaStream_t s);
 };
 
 struct TrainOptions {

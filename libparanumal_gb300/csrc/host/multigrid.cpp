@@ -664,16 +664,24 @@ int MultiGrid::vcycle_learned(const T* RHS, T* X, cudaStream_t s) {
   const T* coef = vec<T>(lcoef64, lcoef32);
   const T* jac = vec<T>(ljac64, ljac32);
   int rc;
+  // floor of the element scales: kScaleFloor x the RMS of the V-cycle's right-hand side
+  double bb;
+  if ((rc = dot_host<T>(N, RHS, RHS, bb, s))) return rc;
+  const float sfloor = (float)(LearnedSmoother::kScaleFloor * std::sqrt(bb / (double)std::max<int64_t>(N, 1)));
   auto smooth_step = [&]() -> int {
     int r;
-    double cr, cAc;
-    if ((r = learned->apply<T>(box, E, el->g2l.p, RES, coef, D, N, s))) return r;
-    if ((r = amxpy<T>(N, T(1), jac, RES, T(1), D, s))) return r;
+    // c = (4/3/rho) D^{-1} RES + network correction; AD = A c
+    if ((r = amxpy<T>(N, T(1), jac, RES, T(0), D, s))) return r;
+    if ((r = learned->apply<T>(box, E, el->g2l.p, RES, coef, D, N, sfloor, s))) return r;
     if ((r = op<T>(el, D, AD, s))) return r;
-    if ((r = dot_host<T>(N, D, RES, cr, s)) || (r = dot_host<T>(N, D, AD, cAc, s))) return r;
+    // w = (c.RES)/(c.Ac) from one two-product pass; X += w c, RES -= w A c in one pass
+    if ((r = dot2<T>(N, D, RES, AD, plat->scalars.p + 2, plat->partials.p, s))) return r;
+    LPG_CUDA_TRY(cudaMemcpyAsync(plat->hostScalars + 2, plat->scalars.p + 2, 2 * sizeof(double),
+                                 cudaMemcpyDeviceToHost, s));
+    LPG_CUDA_TRY(cudaStreamSynchronize(s));
+    const double cr = plat->hostScalars[2], cAc = plat->hostScalars[3];
     const double w = (cAc > 0 && std::isfinite(cr) && std::isfinite(cAc)) ? cr / cAc : 0.0;
-    if ((r = axpy<T>(N, (T)w, D, T(1), X, s)) || (r = axpy<T>(N, (T)(-w), AD, T(1), RES, s))) return r;
-    return LPG_OK;
+    return update2<T>(N, (T)w, D, AD, X, RES, s);
   };
   // a tensor-core pipeline timeout inside the network (LPG_ERR_TIMEOUT) abandons the
   // learned attempt: the V-cycle is redone with the plain smoother and counted
@@ -698,8 +706,8 @@ int MultiGrid::vcycle_learned(const T* RHS, T* X, cudaStream_t s) {
   }
   if (rc) return rc;
   // residual reduction of this V-cycle
-  double rr, bb;
-  if ((rc = dot_host<T>(N, RES, RES, rr, s)) || (rc = dot_host<T>(N, RHS, RHS, bb, s))) return rc;
+  double rr;
+  if ((rc = dot_host<T>(N, RES, RES, rr, s))) return rc;
   nVcycle++;
   if (!(rr <= threshold * threshold * bb)) {
     nFallback++;

@@ -91,6 +91,9 @@ int solution_norms(int N, int64_t E, const double* EX, const double* EY, const d
 int operator_diagonal_local(int N, int64_t E, const double* geo, const double* D, double lambda,
                             const double* lambdaE, const int32_t* g2l, double rankBoost,
                             double* diagL, cudaStream_t s);
+// Assembled diagonal mass product Mu = Gather(Trans)(wJ .* Scatter(u)) (Mu overwritten).
+int mass_apply(int N, int64_t E, const double* geo, const int32_t* g2l, const double* u, double* Mu, int64_t Nglobal,
+               cudaStream_t s);
 // Per element: smallest (lo) and largest (hi) assembled index among its unmasked nodes.
 int element_dof_range(int N, int64_t E, const int32_t* g2l, int32_t* lo, int32_t* hi, cudaStream_t s);
 
@@ -121,6 +124,11 @@ int dot(int64_t N, const double* x, const double* y, double* out, double* partia
 int dot_f32(int64_t N, const float* x, const float* y, double* out, double* partials, cudaStream_t s);
 int sum(int64_t N, const double* x, double* out, double* partials, cudaStream_t s);
 int norm2(int64_t N, const double* x, double* out, double* partials, cudaStream_t s);   // sqrt(x.x)
+// out2[0] = x.y, out2[1] = x.z in one pass (partials: kReducePartials doubles)
+template <typename T>
+int dot2(int64_t N, const T* x, const T* y, const T* z, double* out2, double* partials, cudaStream_t s);
+// x += a p; r -= a q
+template <typename T> int update2(int64_t N, T a, const T* p, const T* q, T* x, T* r, cudaStream_t s);
 int pcg_update(int64_t N, double alpha, const double* p, const double* Ap, double* x, double* r,
                double* out, double* partials, cudaStream_t s);
 int add_scalar(int64_t N, const double* scalarDev, double scale, double* x, cudaStream_t s);

@@ -379,7 +379,8 @@ template int element_features<float, __nv_bfloat16>(const BoxNumbering&, int64_t
                                                     const float*, __nv_bfloat16*, float*, float, cudaStream_t);
 
 // z[g] += coef[g] * s_e * out (coef = weight / diag: the correction s_e invDiag out
-// averaged over the copies of g), in the vector's precision
+// averaged over the copies of g), in the vector's precision; z holds the caller's
+// starting value (zero, or the damped-Jacobi part of the smoother)
 template <typename TV>
 __global__ void apply_correction_kernel(const int Np, const int64_t count, const int64_t e0,
                                         const int32_t* __restrict__ g2l, const float* __restrict__ out,
@@ -391,9 +392,10 @@ __global__ void apply_correction_kernel(const int Np, const int64_t count, const
     const int32_t g = g2l[(e0 + el) * Np + n];
     if (g < 0) continue;
     const TV v = coef[g] * (TV)(scale[el] * out[el * kMlpOut + n]);
-    // nodes strictly inside the element (1 <= i,j,k <= N-1) have no other copy: a store
+    // nodes strictly inside the element (1 <= i,j,k <= N-1) have no other copy: a plain
+    // read-modify-write
     const int Nq = kMlpNq, a = n % Nq, bb = (n / Nq) % Nq, c = n / (Nq * Nq);
-    if (a > 0 && a < Nq - 1 && bb > 0 && bb < Nq - 1 && c > 0 && c < Nq - 1) z[g] = v;
+    if (a > 0 && a < Nq - 1 && bb > 0 && bb < Nq - 1 && c > 0 && c < Nq - 1) z[g] += v;
     else atomicAdd(z + g, v);
   }
 }

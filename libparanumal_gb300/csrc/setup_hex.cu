@@ -448,6 +448,37 @@ __global__ void element_dof_range_kernel(const int Np, const int64_t E, const in
   }
 }
 
+// ---------------------------------------------------------------- assembled mass product
+// Mu[g] = sum over local copies n of g of wJ[n] u[g] (the diagonal GLL mass matrix,
+// assembled): wJ is row 6 of the packed [e][7][Np] factors. Interior nodes (one copy)
+// store, the others add atomically; Mu is zeroed first.
+__global__ void mass_apply_kernel(const int Nq, const int64_t Nlocal, const double* __restrict__ geo,
+                                  const int32_t* __restrict__ g2l, const double* __restrict__ u,
+                                  double* __restrict__ Mu) {
+  const int Np = Nq * Nq * Nq;
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < Nlocal; n += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t g = g2l[n];
+    if (g < 0) continue;
+    const int64_t e = n / Np;
+    const int l = (int)(n % Np);
+    const double v = geo[e * 7 * Np + 6 * Np + l] * u[g];
+    const int a = l % Nq, b = (l / Nq) % Nq, c = l / (Nq * Nq);
+    if (a > 0 && a < Nq - 1 && b > 0 && b < Nq - 1 && c > 0 && c < Nq - 1) Mu[g] = v;
+    else atomicAdd(Mu + g, v);
+  }
+}
+int mass_apply(int N, int64_t E, const double* geo, const int32_t* g2l, const double* u, double* Mu, int64_t Nglobal,
+               cudaStream_t s) {
+  if (Nglobal > 0) LPG_CUDA_TRY(cudaMemsetAsync(Mu, 0, sizeof(double) * Nglobal, s));
+  const int Nq = N + 1;
+  const int64_t Nlocal = E * Nq * Nq * Nq;
+  if (Nlocal <= 0) return LPG_OK;
+  const int64_t blocks = std::min<int64_t>((Nlocal + 255) / 256, 152 * 32);
+  mass_apply_kernel<<<(unsigned)blocks, 256, 0, s>>>(Nq, Nlocal, geo, g2l, u, Mu);
+  LPG_LAUNCH_CHECK("mass_apply_kernel");
+  return LPG_OK;
+}
+
 int element_dof_range(int N, int64_t E, const int32_t* g2l, int32_t* lo, int32_t* hi, cudaStream_t s) {
   if (E <= 0) return LPG_OK;
   const int Np = (N + 1) * (N + 1) * (N + 1);

@@ -299,6 +299,86 @@ int norm2(int64_t N, const double* x, double* out, double* partials, cudaStream_
   return LPG_OK;
 }
 
+// two inner products of x in one pass: out[0] = x.y, out[1] = x.z. FP32 data: products
+// summed per thread in FP32 with Kahan compensation (as dot_f32), FP64 across threads.
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads)
+dot2_stage1(const int64_t N, const T* __restrict__ x, const T* __restrict__ y, const T* __restrict__ z,
+            double* __restrict__ partials) {
+  double a, b;
+  if constexpr (std::is_same<T, float>::value) {
+    float sa = 0.f, ca = 0.f, sb = 0.f, cb = 0.f;
+    for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x) {
+      const float xv = x[n];
+      const float ya = xv * y[n] - ca, yb = xv * z[n] - cb;
+      const float ta = sa + ya, tb = sb + yb;
+      ca = (ta - sa) - ya;
+      cb = (tb - sb) - yb;
+      sa = ta;
+      sb = tb;
+    }
+    a = (double)sa - (double)ca;
+    b = (double)sb - (double)cb;
+  } else {
+    a = 0;
+    b = 0;
+    for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x) {
+      a += x[n] * y[n];
+      b += x[n] * z[n];
+    }
+  }
+  a = block_sum(a);
+  b = block_sum(b);
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = a;
+    partials[gridDim.x + blockIdx.x] = b;
+  }
+}
+__global__ void __launch_bounds__(kRedThreads)
+dot2_stage2(const int nparts, const double* __restrict__ partials, double* __restrict__ out) {
+  double a = 0, b = 0;
+  for (int i = threadIdx.x; i < nparts; i += blockDim.x) {
+    a += partials[i];
+    b += partials[nparts + i];
+  }
+  a = block_sum(a);
+  b = block_sum(b);
+  if (threadIdx.x == 0) {
+    out[0] = a;
+    out[1] = b;
+  }
+}
+template <typename T>
+int dot2(int64_t N, const T* x, const T* y, const T* z, double* out2, double* partials, cudaStream_t s) {
+  const int nb = std::min(red_blocks(N), kReducePartials / 2);
+  dot2_stage1<T><<<nb, kRedThreads, 0, s>>>(N, x, y, z, partials);
+  LPG_LAUNCH_CHECK("dot2_stage1");
+  dot2_stage2<<<1, kRedThreads, 0, s>>>(nb, partials, out2);
+  LPG_LAUNCH_CHECK("dot2_stage2");
+  return LPG_OK;
+}
+template int dot2<double>(int64_t, const double*, const double*, const double*, double*, double*, cudaStream_t);
+template int dot2<float>(int64_t, const float*, const float*, const float*, double*, double*, cudaStream_t);
+
+// x += a p; r -= a q
+template <typename T>
+__global__ void update2_kernel(const int64_t N, const T a, const T* __restrict__ p, const T* __restrict__ q,
+                               T* __restrict__ x, T* __restrict__ r) {
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x) {
+    x[n] += a * p[n];
+    r[n] -= a * q[n];
+  }
+}
+template <typename T>
+int update2(int64_t N, T a, const T* p, const T* q, T* x, T* r, cudaStream_t s) {
+  if (N <= 0) return LPG_OK;
+  update2_kernel<T><<<grid_for(N, 256, kStreamCap), 256, 0, s>>>(N, a, p, q, x, r);
+  LPG_LAUNCH_CHECK("update2_kernel");
+  return LPG_OK;
+}
+template int update2<double>(int64_t, double, const double*, const double*, double*, double*, cudaStream_t);
+template int update2<float>(int64_t, float, const float*, const float*, float*, float*, cudaStream_t);
+
 __global__ void __launch_bounds__(kRedThreads)
 pcg_update_stage1(const int64_t N, const double alpha, const double* __restrict__ p,
                   const double* __restrict__ Ap, double* __restrict__ x, double* __restrict__ r,

@@ -105,6 +105,35 @@ def test_training_reduces_loss(trained):
     assert hist[-1] < 0.7 * hist[0], hist
 
 
+@pytest.fixture(scope="module")
+def trained_full():
+    """The network as the benchmark trains it: 20,000 pairs from 8 plain solves on 32^3,
+    40 epochs (a few seconds on the GPU)."""
+    w, hist = lpg.train_smoother(learned_problem(32), nsolves=8, samples_per_solve=2500, epochs=40, batch=250,
+                                 lr=1e-3, seed=7)
+    return w, hist
+
+
+@pytest.mark.parametrize("prec", ["FP64", "FP32"])
+def test_trained_network_gains_over_the_smoother_without_it(trained_full, prec):
+    """What the trained network gains over the method without it: the same V-cycle with
+    the network's output zero (the damped-Jacobi part alone, energy-optimal steps, zero
+    weights) needs more FPCG iterations than with the trained network (measured: 12
+    without, 10 with, at 10^3 and 32^3, two steps per side). The fallback is switched off
+    for both (threshold 1e30), so every V-cycle uses the smoother under test."""
+    w, _ = trained_full
+    s = learned_problem(10, **{"PRECONDITIONER PRECISION": prec, "LEARNED SMOOTHER STEPS": 2})
+    runs = {}
+    for name, weights in (("trained", w), ("without network", np.zeros_like(w))):
+        e = lpg.Elliptic(s)
+        e.set_learned_smoother(weights, 1e30)
+        r = e.Run()
+        assert r["converged"] and e.info("fallbacks") == 0
+        runs[name] = r["iterations"]
+    print("iterations: trained network %d, without it %d" % (runs["trained"], runs["without network"]))
+    assert runs["trained"] < runs["without network"], runs
+
+
 @pytest.mark.parametrize("prec", ["FP64", "FP32"])
 def test_learned_smoother_solve_with_fallback(trained, prec):
     """FPCG with the learned fine smoother reaches the tolerance and the FP64 method's
