@@ -759,250 +759,6 @@ ax_hex_dw_kernel(const int64_t Nelements, const int32_t* __restrict__ elementLis
     if (r_id[k] >= 0) atomicAdd(out + r_id[k], dw_to_double(r_Aq[k]));
 }
 
-// Persistent form of the double-word kernel at Nq = 8: each CTA walks element groups
-// (grid = SMs x resident CTAs). While group g is computed, the next group's index rows are
-// copied into shared memory with 4-byte cp.async at its start, and half-way through its
-// layers the next group's q values are gathered into shared memory with 8-byte cp.async
-// through those indices, so neither dependent DRAM round trip stalls the next group's
-// start; the geometric factors of the next layer (across the group boundary too) are
-// loaded into registers one layer ahead. Each thread's prefetch slots are its own (no
-// cross-thread hand-over), double-buffered by group parity.
-constexpr int kDwPfBytes = 2 * 8 * 256 * (4 + 8);   // 2 buffers x Nq layers x 256 threads x (id + q)
-
-__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
-  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
-  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
-}
-
-__global__ void __launch_bounds__(256, 2)
-ax_hex_dw_persist_kernel(const int64_t Nelements, const int32_t* __restrict__ elementList,
-                         const int32_t* __restrict__ g2l, const dw* __restrict__ ggeo, const int64_t geoStride,
-                         const dw* __restrict__ wJ, const int64_t wJStride, const double* __restrict__ Dg,
-                         const double lambda, const double* __restrict__ lambdaE, const double* __restrict__ q,
-                         double* __restrict__ out) {
-  constexpr int NQ = 8, NP = NQ * NQ * NQ, H = NQ / 2, N = NQ - 1;
-  constexpr int EPB = elems_per_block<NQ>(), NT = NQ * NQ * EPB;
-  static_assert(NT == 256, "persistent double-word kernel: 4 elements of 64 threads");
-  __shared__ dw s_Dp[H][H], s_Dm[H][H], s_Tp[H][H], s_Tm[H][H];
-  __shared__ dw s_R[EPB][NQ][NQ], s_S[EPB][NQ][NQ], s_dr[EPB][NQ][NQ], s_ds[EPB][NQ][NQ];
-  __shared__ dw s_qt[NQ][NT], s_gt[NQ][NT];
-  extern __shared__ __align__(16) unsigned char pf[];
-  // buffer b: ids [NQ][NT] int32, then q [NQ][NT] double
-  auto pid = [&](int b, int k, int t) { return reinterpret_cast<int32_t*>(pf + b * (NQ * NT * 12)) + k * NT + t; };
-  auto pq = [&](int b, int k, int t) {
-    return reinterpret_cast<double*>(pf + b * (NQ * NT * 12) + NQ * NT * 4) + k * NT + t;
-  };
-
-  const int i = threadIdx.x, jj = threadIdx.y, el = threadIdx.z;
-  const int j = eo_row<NQ>(jj);
-  const int tid = i + NQ * (jj + NQ * el);
-  for (int t = tid; t < H * H; t += NT) {
-    const int a = t / H, m = t % H;
-    const double d0 = Dg[a * NQ + m], d1 = Dg[a * NQ + N - m];
-    const double t0 = Dg[m * NQ + a], t1 = Dg[(N - m) * NQ + a];
-    s_Dp[a][m] = dw_from_double(0.5 * (d0 + d1));
-    s_Dm[a][m] = dw_from_double(0.5 * (d0 - d1));
-    s_Tp[a][m] = dw_from_double(0.5 * (t0 + t1));
-    s_Tm[a][m] = dw_from_double(0.5 * (t0 - t1));
-  }
-  const int64_t ngroups = (Nelements + EPB - 1) / EPB;
-  const int node = j * NQ + i;
-  // element of this thread in group grp (and whether it exists)
-  auto elem_of = [&](int64_t grp, bool& act) -> int64_t {
-    const int64_t ei = grp * EPB + el;
-    act = (grp < ngroups) && (ei < Nelements);
-    if (!act) return 0;
-    return elementList ? (int64_t)elementList[ei] : ei;
-  };
-  // index rows of group grp into buffer b (inactive: -1, written directly)
-  auto issue_ids = [&](int64_t grp, int b) {
-    bool act;
-    const int64_t e = elem_of(grp, act);
-#pragma unroll
-    for (int k = 0; k < NQ; ++k) {
-      if (act) cp_async4(pid(b, k, tid), g2l + e * NP + k * NQ * NQ + node);
-      else *pid(b, k, tid) = -1;
-    }
-    cp_async_commit();
-  };
-  // q values through the index rows already in buffer b (masked: 0, written directly)
-  auto issue_q = [&](int b) {
-#pragma unroll
-    for (int k = 0; k < NQ; ++k) {
-      const int32_t id = *pid(b, k, tid);
-      if (id >= 0) cp_async8(pq(b, k, tid), q + id);
-      else *pq(b, k, tid) = 0.0;
-    }
-    cp_async_commit();
-  };
-
-  const dw zero{0.f, 0.f};
-  dw nG[7];
-  double nlam = lambda;
-  // geometric factors of layer k of element e into nG
-  auto load_G = [&](int64_t e, bool act, int k) {
-    const dw* gp = ggeo + e * geoStride + node + k * NQ * NQ;
-#pragma unroll
-    for (int c = 0; c < 6; ++c) nG[c] = act ? gp[c * NP] : zero;
-    nG[6] = act ? wJ[e * wJStride + node + k * NQ * NQ] : zero;
-  };
-
-  // prologue: the first group's indices, q values, layer-0 factors and lambda
-  {
-    const int64_t g0 = blockIdx.x;
-    issue_ids(g0, 0);
-    cp_async_wait<0>();
-    issue_q(0);
-    bool act;
-    const int64_t e0 = elem_of(g0, act);
-    load_G(e0, act, 0);
-    if (lambdaE && act) nlam = lambdaE[e0];
-  }
-  __syncthreads();
-
-  const bool rtask = i < H;
-  const int pt = rtask ? i : i - H;
-  dw* dst0 = rtask ? &s_dr[el][j][pt] : &s_ds[el][pt][j];
-  dw* dst1 = rtask ? &s_dr[el][j][N - pt] : &s_ds[el][N - pt][j];
-  const dw* line = rtask ? &s_R[el][j][0] : &s_S[el][j][0];
-  const int slotR = (i < H) ? i : H + N - i, slotS = (j < H) ? j : H + N - j;
-  const float sgnR = (i < H) ? 1.f : -1.f, sgnS = (j < H) ? 1.f : -1.f;
-
-  for (int64_t it = 0;; ++it) {
-    const int64_t grp = blockIdx.x + it * gridDim.x;
-    if (grp >= ngroups) break;
-    const int b = (int)(it & 1);
-    bool active;
-    const int64_t e = elem_of(grp, active);
-    const int64_t ngrp = grp + gridDim.x;
-    bool nact;
-    const int64_t en = elem_of(ngrp, nact);
-    // this group's q values (own slots, copied by this thread)
-    cp_async_wait<0>();
-    dw r_q[NQ], r_Aq[NQ];
-    int32_t r_id[NQ];
-#pragma unroll
-    for (int k = 0; k < NQ; ++k) {
-      r_id[k] = *pid(b, k, tid);
-      r_q[k] = dw_from_double(*pq(b, k, tid));
-    }
-    const dw lam = dw_from_double(nlam);
-    // the next group's index rows
-    issue_ids(ngrp, b ^ 1);
-
-    {
-      dw E[H], O[H];
-#pragma unroll
-      for (int m = 0; m < H; ++m) {
-        E[m] = dw_add(r_q[m], r_q[N - m]);
-        O[m] = dw_sub(r_q[m], r_q[N - m]);
-      }
-#pragma unroll
-      for (int t = 0; t < H; ++t) {
-        dw_acc A, B;
-#pragma unroll
-        for (int m = 0; m < H; ++m) {
-          A.mac(s_Dp[t][m], E[m]);
-          B.mac(s_Dm[t][m], O[m]);
-        }
-        const dw a = A.get(), bb = B.get();
-        s_qt[t][tid] = dw_add(a, bb);
-        s_qt[N - t][tid] = dw_sub(bb, a);
-      }
-    }
-
-#pragma unroll
-    for (int k = 0; k < NQ; ++k) {
-      const dw G00 = nG[0], G01 = nG[1], G02 = nG[2], G11 = nG[3], G12 = nG[4], G22 = nG[5], GwJ = nG[6];
-      // factors one layer ahead: the next layer of this element, or layer 0 of the next group
-      if (k + 1 < NQ) {
-        load_G(e, active, k + 1);
-      } else {
-        load_G(en, nact, 0);
-        nlam = (lambdaE && nact) ? lambdaE[en] : lambda;
-      }
-      if (k == NQ / 2) {
-        cp_async_wait<0>();   // the next group's index rows (this thread's own copies)
-        issue_q(b ^ 1);
-      }
-      const dw v = r_q[k];
-      const dw pr = dw_shfl_xor(v, NQ - 1), ps = dw_shfl_xor(v, 2 * NQ);
-      s_R[el][j][slotR] = dw_add(pr, dw_scale_sign(sgnR, v));
-      s_S[el][i][slotS] = dw_add(ps, dw_scale_sign(sgnS, v));
-      eo_sync<NQ>(el);
-      {
-        dw_acc A, B;
-#pragma unroll
-        for (int m = 0; m < H; ++m) {
-          A.mac(s_Dp[pt][m], line[m]);
-          B.mac(s_Dm[pt][m], line[H + m]);
-        }
-        const dw a = A.get(), bb = B.get();
-        *dst0 = dw_add(a, bb);
-        *dst1 = dw_sub(bb, a);
-      }
-      eo_sync<NQ>(el);
-      const dw qr = s_dr[el][j][i], qs = s_ds[el][j][i], qtk = s_qt[k][tid];
-      dw_acc ar, as, at;
-      ar.mac(G00, qr); ar.mac(G01, qs); ar.mac(G02, qtk);
-      as.mac(G01, qr); as.mac(G11, qs); as.mac(G12, qtk);
-      at.mac(G02, qr); at.mac(G12, qs); at.mac(G22, qtk);
-      const dw Gqr = ar.get(), Gqs = as.get();
-      s_gt[k][tid] = at.get();
-      const dw mass = dw_mul(dw_mul(GwJ, lam), v);
-      const dw pr2 = dw_shfl_xor(Gqr, NQ - 1), ps2 = dw_shfl_xor(Gqs, 2 * NQ);
-      s_R[el][j][slotR] = dw_add(pr2, dw_scale_sign(sgnR, Gqr));
-      s_S[el][i][slotS] = dw_add(ps2, dw_scale_sign(sgnS, Gqs));
-      eo_sync<NQ>(el);
-      {
-        dw_acc A, B;
-#pragma unroll
-        for (int m = 0; m < H; ++m) {
-          A.mac(s_Tp[pt][m], line[m]);
-          B.mac(s_Tm[pt][m], line[H + m]);
-        }
-        const dw a = A.get(), bb = B.get();
-        *dst0 = dw_add(a, bb);
-        *dst1 = dw_sub(bb, a);
-      }
-      eo_sync<NQ>(el);
-      r_Aq[k] = dw_add(dw_add(mass, s_dr[el][j][i]), s_ds[el][j][i]);
-    }
-
-    {
-      dw E[H], O[H];
-#pragma unroll
-      for (int m = 0; m < H; ++m) {
-        const dw g0 = s_gt[m][tid], g1 = s_gt[N - m][tid];
-        E[m] = dw_add(g0, g1);
-        O[m] = dw_sub(g0, g1);
-      }
-#pragma unroll
-      for (int t = 0; t < H; ++t) {
-        dw_acc A, B;
-#pragma unroll
-        for (int m = 0; m < H; ++m) {
-          A.mac(s_Tp[t][m], E[m]);
-          B.mac(s_Tm[t][m], O[m]);
-        }
-        const dw a = A.get(), bb = B.get();
-        r_Aq[t] = dw_add(r_Aq[t], dw_add(a, bb));
-        r_Aq[N - t] = dw_add(r_Aq[N - t], dw_sub(bb, a));
-      }
-    }
-    if (active) {
-#pragma unroll
-      for (int k = 0; k < NQ; ++k)
-        if (r_id[k] >= 0) atomicAdd(out + r_id[k], dw_to_double(r_Aq[k]));
-    }
-  }
-  cp_async_wait<0>();
-}
-
 // Double-word operator for the degrees without an even-odd kernel (N = 1, 2, 4, 5, 6, 8):
 // one thread per node, EPB elements per CTA (at least 128 threads), direct Nq-term
 // contractions through shared memory, the same df64 building blocks and FP64 assembly.
@@ -1094,37 +850,13 @@ int ax_hex_dw(const AxArgs<double, float2>& a, cudaStream_t s) {
   }
   if (a.N == 7) {
     const int64_t blocks = (a.Nelements + 3) / 4;
-    // LPG_AX_DW = layered | nonpersist: tuning overrides (one element group per CTA, with or
-    // without the one-layer-ahead factor loads)
-    static const int variant = [] {
+    // geometric factors loaded one layer ahead (64^3: 4.36 ms against 4.42 ms); LPG_AX_DW =
+    // noprefetch is a tuning override back to loads at the top of each layer
+    static const bool noprefetch = [] {
       const char* ev = std::getenv("LPG_AX_DW");
-      if (ev && !std::strcmp(ev, "layered")) return 1;
-      if (ev && !std::strcmp(ev, "nonpersist")) return 2;
-      return 0;
+      return ev && !std::strcmp(ev, "noprefetch");
     }();
-    if (variant == 0) {
-      static PerDeviceConfig perDevice;
-      KernelConfig cfg;
-      const int rc = perDevice.get(
-          [&](int, KernelConfig& c) {
-            LPG_CUDA_TRY(cudaFuncSetAttribute(ax_hex_dw_persist_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              kDwPfBytes));
-            LPG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c.ctasPerSM, ax_hex_dw_persist_kernel, 256,
-                                                                       kDwPfBytes));
-            if (c.ctasPerSM < 1) return set_error(LPG_ERR_UNSUPPORTED, "double-word Ax: kernel does not fit on an SM");
-            return (int)LPG_OK;
-          },
-          &cfg);
-      if (rc) return rc;
-      const int64_t grid = std::min<int64_t>(blocks, (int64_t)cfg.numSMs * cfg.ctasPerSM);
-      if (grid > 0)
-        ax_hex_dw_persist_kernel<<<(unsigned)grid, dim3(8, 8, 4), kDwPfBytes, s>>>(
-            a.Nelements, a.elementList, a.g2l, reinterpret_cast<const dw*>(a.ggeo), a.geoStride,
-            reinterpret_cast<const dw*>(a.wJ), a.wJStride, a.D, a.lambda, a.lambdaE, a.q, a.out);
-      LPG_LAUNCH_CHECK("ax_hex_dw_persist_kernel");
-      return LPG_OK;
-    }
-    if (variant == 1)
+    if (!noprefetch)
       ax_hex_dw_kernel<8, true><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(
           a.Nelements, a.elementList, a.g2l, reinterpret_cast<const dw*>(a.ggeo), a.geoStride,
           reinterpret_cast<const dw*>(a.wJ), a.wJStride, a.D, a.lambda, a.lambdaE, a.q, a.out);
