@@ -129,6 +129,31 @@ int lpg_norm2_f64(int64_t N, const double *x, double *result_dev, void *stream);
  * z = invDiag .* r. */
 int lpg_jacobi_f64(int64_t N, const double *invDiag, const double *r, double *z, void *stream);
 
+/* ------------------------------------------------------------------ partition and halo */
+/* Element partition of a box mesh into `nranks` slabs of whole element layers along z, for
+ * callers that split the operator across ranks (one process per GPU) as elliptic_t::Operator
+ * does with MPI (solvers/elliptic/src/ellipticOperator.cpp:29-106; halo_t, include/ogs.hpp:
+ * 347-400). Rank r gets NZ/P (+1 for r < NZ%P) layers, the per-rank count of
+ * meshSetupBoxHex3D.cpp:63-69 applied to z: the element range [e0, e1) of the single-rank
+ * order. Host only (no GPU). info (6 entries) gets e0, e1, the number of dofs the rank owns,
+ * the number of local dofs (owned first, then halo, each in global lattice order: the plane
+ * shared with rank r+1 is owned by r), and the lengths of the `below` and `above` lists.
+ * The arrays may be NULL (sizes only): global_to_local ((e1-e0)*(N+1)^3: local dof or -1 for
+ * a masked node, for lpg_ax_hex_f64 on the rank's elements), below / above (the rank's
+ * local indices of the plane shared with rank r-1 / r+1, in that plane's lattice order, so
+ * rank r's `above` pairs entry by entry with rank r+1's `below`), lattice (global lattice
+ * id X + NX*(Y + NY*Z) of each local dof, NX = nx*N+1, ...). bcflag 1 (Dirichlet: boundary
+ * lattice nodes masked) or 2 (Neumann); periodic boxes are not partitioned. */
+int lpg_box_partition(int nx, int ny, int nz, int N, int bcflag, int nranks, int rank, int64_t *info,
+                      int32_t *global_to_local, int32_t *below, int32_t *above, int64_t *lattice);
+/* The two device halves of a halo exchange (ogs extract kernel, libs/ogs/okl/ogsKernels.okl:167-;
+ * the exchange itself -- MPI, NCCL -- is the caller's): pack buf[i] = v[idx[i]] before
+ * sending, unpack_add v[idx[i]] += buf[i] for what was received. After every rank has
+ * assembled its elements' contributions to its local dofs, exchanging at each shared plane
+ * gives both ranks the full sums there. */
+int lpg_halo_pack_f64(int64_t n, const int32_t *idx, const double *v, double *buf, void *stream);
+int lpg_halo_unpack_add_f64(int64_t n, const int32_t *idx, const double *buf, double *v, void *stream);
+
 /* ------------------------------------------------------------------ p-multigrid level kernels */
 /* MGLevel::coarsen (solvers/elliptic/src/ellipticPreconMultiGridLevel.cpp:41-82 with
  * ellipticPartialPreconCoarsenHex3D, okl/ellipticPreconCoarsenHex3D.okl:209-294): per element,

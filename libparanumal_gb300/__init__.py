@@ -70,6 +70,9 @@ def lib():
         "lpg_dot_f64_noalloc": [i64, vp, vp, vp, vp],
         "lpg_pcg_update_f64": [i64, f64, vp, vp, vp, vp, vp, vp],
         "lpg_norm2_f64": [i64, vp, vp, vp],
+        "lpg_box_partition": [i32, i32, i32, i32, i32, i32, i32, vp, vp, vp, vp, vp],
+        "lpg_halo_pack_f64": [i64, vp, vp, vp, vp],
+        "lpg_halo_unpack_add_f64": [i64, vp, vp, vp, vp],
         "lpg_jacobi_f64": [i64, vp, vp, vp, vp],
         "lpg_pmg_restrict_f64": [i32, i32, i64, vp, vp, vp, vp, vp, vp, i64, vp],
         "lpg_pmg_restrict_f32": [i32, i32, i64, vp, vp, vp, vp, vp, vp, i64, vp],
@@ -314,6 +317,24 @@ def hex_mesh_numbering(path, N):
     ng = ctypes.c_int64(0)
     check(lib().lpg_hex_mesh_numbering(str(path).encode(), N, g2l.ctypes.data_as(ctypes.c_void_p), ctypes.byref(ng)))
     return g2l, ng.value
+
+
+def box_partition(nx, ny, nz, N, bcflag, nranks, rank):
+    """z-slab partition of a box for `rank` of `nranks` (host only): dict with e0, e1,
+    nowned, nlocal and the arrays global_to_local, below, above, lattice."""
+    info = np.zeros(6, dtype=np.int64)
+    L = lib()
+    check(L.lpg_box_partition(nx, ny, nz, N, bcflag, nranks, rank, info.ctypes.data_as(ctypes.c_void_p),
+                              None, None, None, None))
+    e0, e1, nowned, nlocal, nb, na = (int(v) for v in info)
+    g2l = np.zeros((e1 - e0) * (N + 1) ** 3, dtype=np.int32)
+    below, above = np.zeros(nb, dtype=np.int32), np.zeros(na, dtype=np.int32)
+    lattice = np.zeros(nlocal, dtype=np.int64)
+    vp = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    check(L.lpg_box_partition(nx, ny, nz, N, bcflag, nranks, rank, vp(info), vp(g2l), vp(below), vp(above),
+                              vp(lattice)))
+    return dict(e0=e0, e1=e1, nowned=nowned, nlocal=nlocal, global_to_local=g2l, below=below, above=above,
+                lattice=lattice)
 
 
 def extrap_coeffs(degree, history, cpqr=False):

@@ -287,6 +287,14 @@ extern "C" int lpg_norm2_f64(int64_t N, const double* x, double* result_dev, voi
   if (rc) return rc;
   return norm2(N, x, result_dev, scratch, (cudaStream_t)stream);
 }
+extern "C" int lpg_halo_pack_f64(int64_t n, const int32_t* idx, const double* v, double* buf, void* stream) {
+  if (n < 0 || (n > 0 && (!idx || !v || !buf))) return set_error(LPG_ERR_INVALID, "halo pack: bad arguments");
+  return halo_pack(n, idx, v, buf, (cudaStream_t)stream);
+}
+extern "C" int lpg_halo_unpack_add_f64(int64_t n, const int32_t* idx, const double* buf, double* v, void* stream) {
+  if (n < 0 || (n > 0 && (!idx || !v || !buf))) return set_error(LPG_ERR_INVALID, "halo unpack: bad arguments");
+  return halo_unpack_add(n, idx, buf, v, (cudaStream_t)stream);
+}
 extern "C" int lpg_jacobi_f64(int64_t N, const double* invDiag, const double* r, double* z, void* stream) {
   if (N < 0 || (N > 0 && (!invDiag || !r || !z))) return set_error(LPG_ERR_INVALID, "jacobi: bad arguments");
   return amxpy<double>(N, 1.0, invDiag, r, 0.0, z, (cudaStream_t)stream);

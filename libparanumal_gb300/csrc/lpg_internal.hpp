@@ -129,6 +129,9 @@ template <typename T>
 int dot2(int64_t N, const T* x, const T* y, const T* z, double* out2, double* partials, cudaStream_t s);
 // x += a p; r -= a q
 template <typename T> int update2(int64_t N, T a, const T* p, const T* q, T* x, T* r, cudaStream_t s);
+// halo exchange halves: buf[i] = v[idx[i]]; v[idx[i]] += buf[i]
+int halo_pack(int64_t n, const int32_t* idx, const double* v, double* buf, cudaStream_t s);
+int halo_unpack_add(int64_t n, const int32_t* idx, const double* buf, double* v, cudaStream_t s);
 int pcg_update(int64_t N, double alpha, const double* p, const double* Ap, double* x, double* r,
                double* out, double* partials, cudaStream_t s);
 int add_scalar(int64_t N, const double* scalarDev, double scale, double* x, cudaStream_t s);

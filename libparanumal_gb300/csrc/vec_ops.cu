@@ -379,6 +379,31 @@ int update2(int64_t N, T a, const T* p, const T* q, T* x, T* r, cudaStream_t s) 
 template int update2<double>(int64_t, double, const double*, const double*, double*, double*, cudaStream_t);
 template int update2<float>(int64_t, float, const float*, const float*, float*, float*, cudaStream_t);
 
+// halo exchange halves (the ogs extract kernel, libs/ogs/okl/ogsKernels.okl:167-): buf[i] =
+// v[idx[i]], and v[idx[i]] += buf[i] (the indices of one list are distinct)
+__global__ void halo_pack_kernel(const int64_t n, const int32_t* __restrict__ idx, const double* __restrict__ v,
+                                 double* __restrict__ buf) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    buf[i] = v[idx[i]];
+}
+__global__ void halo_unpack_add_kernel(const int64_t n, const int32_t* __restrict__ idx,
+                                       const double* __restrict__ buf, double* __restrict__ v) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    v[idx[i]] += buf[i];
+}
+int halo_pack(int64_t n, const int32_t* idx, const double* v, double* buf, cudaStream_t s) {
+  if (n <= 0) return LPG_OK;
+  halo_pack_kernel<<<grid_for(n, 256, kStreamCap), 256, 0, s>>>(n, idx, v, buf);
+  LPG_LAUNCH_CHECK("halo_pack_kernel");
+  return LPG_OK;
+}
+int halo_unpack_add(int64_t n, const int32_t* idx, const double* buf, double* v, cudaStream_t s) {
+  if (n <= 0) return LPG_OK;
+  halo_unpack_add_kernel<<<grid_for(n, 256, kStreamCap), 256, 0, s>>>(n, idx, buf, v);
+  LPG_LAUNCH_CHECK("halo_unpack_add_kernel");
+  return LPG_OK;
+}
+
 __global__ void __launch_bounds__(kRedThreads)
 pcg_update_stage1(const int64_t N, const double alpha, const double* __restrict__ p,
                   const double* __restrict__ Ap, double* __restrict__ x, double* __restrict__ r,
