@@ -493,6 +493,7 @@ class MultiGrid : public Precon {
 
   int setup(Elliptic* el, const MeshConfig& c, const MGOptions& o);
   int apply(const double* r, double* z, cudaStream_t s) override;
+  int apply_mixed(const double* r, double* z, const float** z32, cudaStream_t s) override;
   uint64_t rngAfter = 0;   // state of the random stream when setup finished
 
  private:
@@ -786,6 +787,22 @@ int MultiGrid::apply(const double* r, double* z, cudaStream_t s) {
     rc = add_scalar(fine->Nglobal, plat->scalars.p + 1, -fine->allNeumannScale * fine->allNeumannScale, z, s);
   }
   return rc;
+}
+
+// FP32 p-levels: the V-cycle's FP32 result is handed to the Krylov loop as it is (no FP64
+// copy); all-Neumann problems take the FP64 path, whose zero-mean step works on z
+int MultiGrid::apply_mixed(const double* r, double* z, const float** z32, cudaStream_t s) {
+  *z32 = nullptr;
+  if (p.empty() || !f32() || fine->allNeumann) return apply(r, z, s);
+  const int64_t N = fine->Nglobal;
+  PLevel& L0 = *p[0];
+  int rc;
+  if ((rc = convert<double, float>(N, r, L0.rhs32.p, s))) return rc;
+  if (learned) rc = vcycle_learned<float>(L0.rhs32.p, L0.x32.p, s);
+  else rc = vcycle_p<float>(0, L0.rhs32.p, L0.x32.p, s);
+  if (rc) return rc;
+  *z32 = L0.x32.p;
+  return LPG_OK;
 }
 
 // ---------------------------------------------------------------- setup

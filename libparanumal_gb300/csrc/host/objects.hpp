@@ -219,6 +219,13 @@ struct LearnedSmoother;
 struct Precon {
   virtual ~Precon() = default;
   virtual int apply(const double* r, double* z, cudaStream_t s) = 0;
+  // z = M^{-1} r for a Krylov loop that can take the result in FP32: a preconditioner
+  // that computes in FP32 sets *z32 to its FP32 result (valid until its next application)
+  // and leaves z unwritten; otherwise *z32 = nullptr and z is written as by apply
+  virtual int apply_mixed(const double* r, double* z, const float** z32, cudaStream_t s) {
+    *z32 = nullptr;
+    return apply(r, z, s);
+  }
   virtual int levels_p() const { return 0; }
   virtual int levels_amg() const { return 0; }
   virtual int64_t coarse_n() const { return 0; }

@@ -46,17 +46,27 @@ int pcg_solve(Platform* plat, Elliptic* el, Precon* pc, PCGWork& w, bool flexibl
   }
   for (iter = 0; iter < maxit; ++iter) {
     if ((iter == 0 && rdotr0 == 0.0) || (iter > 0 && rdotr0 <= TOL)) break;
-    if ((rc = pc->apply(r, w.z.p, s))) return rc;
+    const float* z32 = nullptr;
+    if ((rc = pc->apply_mixed(r, w.z.p, &z32, s))) return rc;
     rdotz2 = rdotz1;
-    if ((rc = plat->dot(N, r, w.z.p, rdotz1))) return rc;
-    if (flexible) {
-      double zdotAp;
-      if ((rc = plat->dot(N, w.z.p, w.Ap.p, zdotAp))) return rc;
-      beta = (iter == 0) ? 0.0 : -alpha * zdotAp / rdotz2;
+    double zdotAp = 0;
+    if (z32) {
+      // FP32 preconditioner output: r.z and z.Ap in one pass, z widened exactly to FP64
+      if ((rc = dot2_mixed(N, z32, r, w.Ap.p, plat->scalars.p + 4, plat->partials.p, s))) return rc;
+      LPG_CUDA_TRY(cudaMemcpyAsync(plat->hostScalars + 4, plat->scalars.p + 4, 2 * sizeof(double),
+                                   cudaMemcpyDeviceToHost, s));
+      LPG_CUDA_TRY(cudaStreamSynchronize(s));
+      rdotz1 = plat->hostScalars[4];
+      zdotAp = plat->hostScalars[5];
     } else {
-      beta = (iter == 0) ? 0.0 : rdotz1 / rdotz2;
+      if ((rc = plat->dot(N, r, w.z.p, rdotz1))) return rc;
+      if (flexible && (rc = plat->dot(N, w.z.p, w.Ap.p, zdotAp))) return rc;
     }
-    if ((rc = axpy<double>(N, 1.0, w.z.p, beta, w.p.p, s))) return rc;
+    if (flexible) beta = (iter == 0) ? 0.0 : -alpha * zdotAp / rdotz2;
+    else beta = (iter == 0) ? 0.0 : rdotz1 / rdotz2;
+    if (z32) rc = direction_mixed(N, z32, beta, w.p.p, s);
+    else rc = axpy<double>(N, 1.0, w.z.p, beta, w.p.p, s);
+    if (rc) return rc;
     if ((rc = el->Operator(w.p.p, w.Ap.p, s))) return rc;
     if ((rc = plat->dot(N, w.p.p, w.Ap.p, pAp))) return rc;
     if (!(pAp > 0.0) || !std::isfinite(pAp)) { res.breakdown = true; break; }

@@ -129,6 +129,10 @@ template <typename T>
 int dot2(int64_t N, const T* x, const T* y, const T* z, double* out2, double* partials, cudaStream_t s);
 // x += a p; r -= a q
 template <typename T> int update2(int64_t N, T a, const T* p, const T* q, T* x, T* r, cudaStream_t s);
+// FPCG with an FP32 preconditioner output z: out2 = (r.z, z.Ap) in FP64, and p = z + beta p
+int dot2_mixed(int64_t N, const float* z, const double* r, const double* Ap, double* out2, double* partials,
+               cudaStream_t s);
+int direction_mixed(int64_t N, const float* z, double beta, double* p, cudaStream_t s);
 // halo exchange halves: buf[i] = v[idx[i]]; v[idx[i]] += buf[i]
 int halo_pack(int64_t n, const int32_t* idx, const double* v, double* buf, cudaStream_t s);
 int halo_unpack_add(int64_t n, const int32_t* idx, const double* buf, double* v, cudaStream_t s);

@@ -360,6 +360,46 @@ int dot2(int64_t N, const T* x, const T* y, const T* z, double* out2, double* pa
 template int dot2<double>(int64_t, const double*, const double*, const double*, double*, double*, cudaStream_t);
 template int dot2<float>(int64_t, const float*, const float*, const float*, double*, double*, cudaStream_t);
 
+// FPCG with an FP32 preconditioner output z: out[0] = r.z, out[1] = z.Ap with z widened
+// exactly to FP64 and FP64 products; and p = z + beta p. z is read as FP32 and never
+// stored as FP64.
+__global__ void __launch_bounds__(kRedThreads)
+dot2_mixed_stage1(const int64_t N, const float* __restrict__ z, const double* __restrict__ r,
+                  const double* __restrict__ Ap, double* __restrict__ partials) {
+  double a = 0, b = 0;
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x) {
+    const double zn = (double)z[n];
+    a += r[n] * zn;
+    b += zn * Ap[n];
+  }
+  a = block_sum(a);
+  b = block_sum(b);
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = a;
+    partials[gridDim.x + blockIdx.x] = b;
+  }
+}
+int dot2_mixed(int64_t N, const float* z, const double* r, const double* Ap, double* out2, double* partials,
+               cudaStream_t s) {
+  const int nb = std::min(red_blocks(N), kReducePartials / 2);
+  dot2_mixed_stage1<<<nb, kRedThreads, 0, s>>>(N, z, r, Ap, partials);
+  LPG_LAUNCH_CHECK("dot2_mixed_stage1");
+  dot2_stage2<<<1, kRedThreads, 0, s>>>(nb, partials, out2);
+  LPG_LAUNCH_CHECK("dot2_stage2");
+  return LPG_OK;
+}
+__global__ void direction_mixed_kernel(const int64_t N, const float* __restrict__ z, const double beta,
+                                       double* __restrict__ p) {
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x)
+    p[n] = (double)z[n] + beta * p[n];
+}
+int direction_mixed(int64_t N, const float* z, double beta, double* p, cudaStream_t s) {
+  if (N <= 0) return LPG_OK;
+  direction_mixed_kernel<<<grid_for(N, 256, kStreamCap), 256, 0, s>>>(N, z, beta, p);
+  LPG_LAUNCH_CHECK("direction_mixed_kernel");
+  return LPG_OK;
+}
+
 // x += a p; r -= a q
 template <typename T>
 __global__ void update2_kernel(const int64_t N, const T a, const T* __restrict__ p, const T* __restrict__ q,
