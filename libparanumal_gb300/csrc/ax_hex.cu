@@ -884,14 +884,6 @@ static int launch_staged(const AxArgs<T, G>& a, cudaStream_t s) {
   const int rc = perDevice.get(
       [&](int, KernelConfig& c) {
         LPG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-        // LPG_AX_CARVEOUT = max: tuning override, the whole unified L1 as shared memory
-        static const bool maxShared = [] {
-          const char* ev = std::getenv("LPG_AX_CARVEOUT");
-          return ev && !std::strcmp(ev, "max");
-        }();
-        if (maxShared)
-          LPG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                            (int)cudaSharedmemCarveoutMaxShared));
         LPG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c.ctasPerSM, kern, NQ * NQ * EPB, smem));
         if (c.ctasPerSM < 1) return set_error(LPG_ERR_UNSUPPORTED, "staged Ax: kernel does not fit on an SM");
         return (int)LPG_OK;
