@@ -200,6 +200,21 @@ def cpu_baseline(nx_sample, N, budget_s=12.0, nthreads=0):
                       "applications, %d OpenMP threads" % (nx_sample, N, nl, reps, used)}
 
 
+def cpu_solve_sample(nx):
+    """The oracle port's FP64 p-MG FPCG solve (7->3->1, Chebyshev 2, smoothed-aggregation AMG)
+    on the nx^3 jittered box, N=7, lambda=0, sine data, all host threads: wall time of its Run
+    (right-hand side, solve, norms; setup outside) and iterations. kind "port": the
+    reference's own solver needs OCCA, MPI and LAPACK and is not built here."""
+    from oracle.oracle import Oracle, threads
+    t0 = time.time()
+    o = Oracle(solve_settings(nx, 7, "FP64"))
+    setup = time.time() - t0
+    t0 = time.time()
+    r = o.run()
+    return {"seconds": time.time() - t0, "iterations": r["iterations"], "error_vs_manufactured": r["error"],
+            "setup_seconds": setup, "cores": threads(), "kind": "port", "host": cpu_model()}
+
+
 def run_reference(a):
     """The reference's CPU implementation of the headline workload (the 64^3, N=7 operator,
     same config as the GPU arm): its own partial-Ax and gather kernels on all host threads,
@@ -735,6 +750,13 @@ def solve_blocks(a):
     out["mixed_80cubed"] = {
         "workload": "FPCG + p-MG 7->3->1 time-to-1e-8, 80^3 jittered hex, N=7, lambda=0, manufactured sine",
         "results": solve_variants(80, ["FP64", "FP32", "FP32+DF64", "BF16GEO+DF64"], a.solve_reps)}
+    # the same solve at a size the CPU finishes in seconds: the oracle port's FP64 p-MG FPCG
+    # (a restatement of the reference's solver, which cannot be built here) on all host
+    # threads beside the GPU variants on the same 32^3 problem
+    out["same_size_32cubed"] = {
+        "workload": "FPCG + p-MG 7->3->1 time-to-1e-8, 32^3 jittered hex, N=7, lambda=0, manufactured sine",
+        "cpu_port": cpu_solve_sample(32),
+        "gpu": solve_variants(32, ["FP64", "FP32+DF64"], a.solve_reps)}
     w, train = train_learned()
     law = {"LAMBDA": 1.0, "LAMBDA FIELD": "LOGNORMAL", "LAMBDA SEED": 2,
            "RHS FIELD": "GAUSSIAN SOURCES", "RHS SEED": 3, "RHS SOURCES": 16}
