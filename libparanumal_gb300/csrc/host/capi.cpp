@@ -792,7 +792,7 @@ extern "C" int lpg_mlp_forward_bf16(const float* params, int64_t B, const float*
   LPG_CUDA_TRY(cudaStreamSynchronize(s));
   if ((rc = L.load(host.data(), s)) || (rc = L.ensure_chunk(B))) return rc;
   if ((rc = convert<float, __nv_bfloat16>(B * kMlpIn, X, L.X.p, s))) return rc;
-  if ((rc = L.forward_bf16(B, s))) return rc;
+  if ((rc = L.forward_bf16(B, L.out.p, s))) return rc;
   LPG_CUDA_TRY(cudaMemcpyAsync(Y, L.out.p, sizeof(float) * B * kMlpOut, cudaMemcpyDeviceToDevice, s));
   if ((rc = L.check_tc(s))) return rc;
   LPG_CUDA_TRY(cudaStreamSynchronize(s));

@@ -39,9 +39,9 @@ int LearnedSmoother::load(const float* hostParams, cudaStream_t s) {
   return LPG_OK;
 }
 
-// out (rows x 512) = MLP(X (rows x 896)): the fused tcgen05 kernel, or with
+// dst (rows x 512) = MLP(X (rows x 896)): the fused tcgen05 kernel, or with
 // LPG_MLP_TC=off (a tuning override) the per-layer mma.sync kernels
-int LearnedSmoother::forward_bf16(int64_t rows, cudaStream_t s) {
+int LearnedSmoother::forward_bf16(int64_t rows, float* dst, cudaStream_t s) {
   static const bool layered = [] {
     const char* e = std::getenv("LPG_MLP_TC");
     return e && !std::strcmp(e, "off");
@@ -51,12 +51,12 @@ int LearnedSmoother::forward_bf16(int64_t rows, cudaStream_t s) {
   if (!layered) {
     const __nv_bfloat16* w[4] = {Wt[0].p, Wt[1].p, Wt[2].p, Wt[3].p};
     const float* bias[4] = {P.b[0], P.b[1], P.b[2], P.b[3]};
-    return mlp_forward_tc(rows, X.p, w, bias, out.p, tcErr.p, s);
+    return mlp_forward_tc(rows, X.p, w, bias, dst, tcErr.p, s);
   }
   if ((rc = bf16_linear((int)rows, kMlpHidden, kMlpIn, X.p, Wt[0].p, P.b[0], true, true, H0.p, s))) return rc;
   if ((rc = bf16_linear((int)rows, kMlpHidden, kMlpHidden, H0.p, Wt[1].p, P.b[1], true, true, H1.p, s))) return rc;
   if ((rc = bf16_linear((int)rows, kMlpHidden, kMlpHidden, H1.p, Wt[2].p, P.b[2], true, true, H0.p, s))) return rc;
-  return bf16_linear((int)rows, kMlpOut, kMlpHidden, H0.p, Wt[3].p, P.b[3], false, false, out.p, s);
+  return bf16_linear((int)rows, kMlpOut, kMlpHidden, H0.p, Wt[3].p, P.b[3], false, false, dst, s);
 }
 
 // the tensor-core pipeline's timeout flag (waits for the stream)
@@ -84,16 +84,34 @@ int LearnedSmoother::apply(const BoxNumbering& b, int64_t E, const int32_t* g2l,
                            int64_t Nglobal, float sfloor, cudaStream_t s) {
   (void)Nglobal;
   if (!ready) return set_error(LPG_ERR_INVALID, "learned smoother has no weights");
+  if (E != (int64_t)b.nx * b.ny * b.nz) return set_error(LPG_ERR_INVALID, "learned smoother: box element count");
   const int Np = (b.N + 1) * (b.N + 1) * (b.N + 1);
   int rc;
   const int64_t C = std::min<int64_t>(E, kChunk);
   if ((rc = ensure_chunk(C))) return rc;
+  static const bool atomic = [] {
+    const char* e = std::getenv("LPG_LEARNED_CORRECTION");
+    return e && !std::strcmp(e, "atomic");
+  }();
+  if (atomic) {
+    for (int64_t e0 = 0; e0 < E; e0 += C) {
+      const int64_t n = std::min<int64_t>(C, E - e0);
+      if ((rc = element_features<T, __nv_bfloat16>(b, E, e0, n, g2l, r, X.p, scale.p, sfloor, s))) return rc;
+      if ((rc = forward_bf16(n, out.p, s))) return rc;
+      if ((rc = apply_correction<T>(Np, n, e0, g2l, out.p, scale.p, coef, z, s))) return rc;
+    }
+    return check_tc(s);
+  }
+  if (allRows < E) {
+    if ((rc = outAll.alloc(E * kMlpOut)) || (rc = scaleAll.alloc(E))) return rc;
+    allRows = E;
+  }
   for (int64_t e0 = 0; e0 < E; e0 += C) {
     const int64_t n = std::min<int64_t>(C, E - e0);
-    if ((rc = element_features<T, __nv_bfloat16>(b, E, e0, n, g2l, r, X.p, scale.p, sfloor, s))) return rc;
-    if ((rc = forward_bf16(n, s))) return rc;
-    if ((rc = apply_correction<T>(Np, n, e0, g2l, out.p, scale.p, coef, z, s))) return rc;
+    if ((rc = element_features<T, __nv_bfloat16>(b, E, e0, n, g2l, r, X.p, scaleAll.p + e0, sfloor, s))) return rc;
+    if ((rc = forward_bf16(n, outAll.p + e0 * kMlpOut, s))) return rc;
   }
+  if ((rc = lattice_correction<T>(b, g2l, outAll.p, scaleAll.p, coef, z, s))) return rc;
   return check_tc(s);
 }
 template int LearnedSmoother::apply<double>(const BoxNumbering&, int64_t, const int32_t*, const double*, const double*,

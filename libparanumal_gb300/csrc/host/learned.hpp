@@ -18,15 +18,20 @@ struct LearnedSmoother {
   DevBuf<__nv_bfloat16> Wt[4];              // BF16 transposed weights for inference
   DevBuf<__nv_bfloat16> X, H0, H1;
   DevBuf<float> out, scale;
+  // outputs and scales of all E elements, for the one-pass lattice correction
+  DevBuf<float> outAll, scaleAll;
   DevBuf<int> tcErr;                        // timeout flag of the tensor-core kernel
-  int64_t chunk = 0;
+  int64_t chunk = 0, allRows = 0;
   int load(const float* hostParams, cudaStream_t s);
   int ensure_chunk(int64_t rows);
-  int forward_bf16(int64_t rows, cudaStream_t s);   // out = MLP(X) for `rows` rows
+  int forward_bf16(int64_t rows, float* dst, cudaStream_t s);   // dst = MLP(X) for `rows` rows
   int check_tc(cudaStream_t s);
   // z (assembled) += sum over copies of coef .* s_e MLP(features(r)), coef = weight / diag
   // (the average over copies of s_e invDiag .* output). Element scales s_e are floored at
-  // sfloor (the caller's kScaleFloor x residual RMS).
+  // sfloor (the caller's kScaleFloor x residual RMS). The network runs in chunks of kChunk
+  // elements; by default their outputs are kept for all elements and one lattice-node
+  // kernel sums each dof's copies (no atomics). LPG_LEARNED_CORRECTION=atomic (a tuning
+  // override) adds each chunk's copies with atomics instead.
   template <typename T>
   int apply(const BoxNumbering& b, int64_t E, const int32_t* g2l, const T* r, const T* coef, T* z, int64_t Nglobal,
             float sfloor, cudaStream_t s);

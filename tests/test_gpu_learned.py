@@ -162,3 +162,49 @@ def test_learned_smoother_solve_with_fallback(trained, prec):
     # restoring the plain smoother
     e.set_learned_smoother(None)
     assert e.Run()["iterations"] == plain["iterations"]
+
+
+_CHILD = r"""
+import json, sys
+import numpy as np
+import libparanumal_gb300 as lpg
+s = json.loads(sys.argv[1])
+e = lpg.Elliptic(s)
+e.set_learned_smoother(np.load(sys.argv[2]), 1e30)
+r = e.Run(want_solution=True)
+np.save(sys.argv[3], r["xL"][::97])
+print(json.dumps(dict(iterations=r["iterations"], converged=r["converged"], fallbacks=e.info("fallbacks"))))
+"""
+
+
+@pytest.mark.parametrize("nx,bc", [(42, 1), (6, 2), (5, -1)], ids=["dirichlet_2chunks", "neumann", "periodic"])
+def test_lattice_correction_matches_atomic_correction(trained, tmp_path, nx, bc):
+    """The network's correction summed per lattice node (one thread per dof over its
+    element copies, the default) against the per-element atomic sum
+    (LPG_LEARNED_CORRECTION=atomic), through whole FPCG solves: equal iterations and
+    solutions equal to 1e-9 (the two differ only in the order the copies are added). The
+    42^3 box has 74,088 elements, more than one inference chunk of 65,536."""
+    import json
+    import os
+    import subprocess
+    import sys
+    w, _ = trained
+    wf = tmp_path / "w.npy"
+    np.save(wf, w)
+    s = learned_problem(nx, **{"BOX BOUNDARY FLAG": bc, "PRECONDITIONER PRECISION": "FP64"})
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    res = {}
+    for mode in ("lattice", "atomic"):
+        env = dict(os.environ, PYTHONPATH=root)
+        env.pop("LPG_LEARNED_CORRECTION", None)
+        if mode == "atomic":
+            env["LPG_LEARNED_CORRECTION"] = "atomic"
+        out = tmp_path / (mode + ".npy")
+        p = subprocess.run([sys.executable, "-c", _CHILD, json.dumps(s), str(wf), str(out)], env=env, cwd=root,
+                           capture_output=True, text=True, timeout=600)
+        assert p.returncode == 0, p.stderr[-2000:]
+        res[mode] = json.loads(p.stdout.strip().splitlines()[-1]), np.load(out)
+    (a, xa), (b, xb) = res["lattice"], res["atomic"]
+    assert a["converged"] and b["converged"] and a["fallbacks"] == b["fallbacks"] == 0
+    assert a["iterations"] == b["iterations"], (a, b)
+    assert rel_err(xa, xb) < 1e-9
