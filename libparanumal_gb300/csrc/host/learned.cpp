@@ -102,16 +102,28 @@ int LearnedSmoother::apply(const BoxNumbering& b, int64_t E, const int32_t* g2l,
     }
     return check_tc(s);
   }
+  // chunks of whole element layers; after each chunk the lattice planes whose copies are
+  // all computed are summed while the chunk's outputs are still in L2: element layers
+  // [z0, z1) complete planes z0*N .. z1*N - 1 (the top plane waits for the next layer; the
+  // last chunk also takes plane nz*N, or plane 0 of a periodic box)
+  const int64_t layer = (int64_t)b.nx * b.ny;
+  const int64_t LC = std::min<int64_t>(E, std::max<int64_t>(1, kChunk / layer) * layer);
+  if (LC > chunk && (rc = ensure_chunk(LC))) return rc;
   if (allRows < E) {
     if ((rc = outAll.alloc(E * kMlpOut)) || (rc = scaleAll.alloc(E))) return rc;
     allRows = E;
   }
-  for (int64_t e0 = 0; e0 < E; e0 += C) {
-    const int64_t n = std::min<int64_t>(C, E - e0);
+  for (int64_t e0 = 0; e0 < E; e0 += LC) {
+    const int64_t n = std::min<int64_t>(LC, E - e0);
     if ((rc = element_features<T, __nv_bfloat16>(b, E, e0, n, g2l, r, X.p, scaleAll.p + e0, sfloor, s))) return rc;
     if ((rc = forward_bf16(n, outAll.p + e0 * kMlpOut, s))) return rc;
+    const int z0 = (int)(e0 / layer), z1 = (int)((e0 + n) / layer);
+    const bool last = (z1 == b.nz);
+    const int Zb = (b.periodic && z0 == 0) ? 1 : z0 * b.N;
+    const int Ze = z1 * b.N + ((last && !b.periodic) ? 1 : 0);
+    if ((rc = lattice_correction<T>(b, g2l, outAll.p, scaleAll.p, coef, z, Zb, Ze, s))) return rc;
+    if (last && b.periodic && (rc = lattice_correction<T>(b, g2l, outAll.p, scaleAll.p, coef, z, 0, 1, s))) return rc;
   }
-  if ((rc = lattice_correction<T>(b, g2l, outAll.p, scaleAll.p, coef, z, s))) return rc;
   return check_tc(s);
 }
 template int LearnedSmoother::apply<double>(const BoxNumbering&, int64_t, const int32_t*, const double*, const double*,

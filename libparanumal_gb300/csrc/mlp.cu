@@ -414,69 +414,73 @@ template int apply_correction<float>(int, int64_t, int64_t, const int32_t*, cons
 
 // copies of lattice coordinate X along one axis of n elements (degree kMlpNq - 1): the
 // element index and local index of each, one copy inside an element, two on an element face
-__device__ __forceinline__ int axis_copies(const int64_t X, const int n, const int periodic, int* e, int* a) {
+__device__ __forceinline__ int axis_copies(const int X, const int n, const int periodic, int* e, int* a) {
   constexpr int N = kMlpNq - 1;
-  const int64_t k = X / N;
-  if (X % N != 0) {
-    e[0] = (int)k;
-    a[0] = (int)(X % N);
+  const int k = X / N, r = X - k * N;
+  if (r != 0) {
+    e[0] = k;
+    a[0] = r;
     return 1;
   }
   if (periodic) {
-    e[0] = (int)((k - 1 + n) % n);
+    e[0] = (k - 1 + n) % n;
     a[0] = N;
-    e[1] = (int)(k % n);
+    e[1] = k % n;
     a[1] = 0;
     return 2;
   }
   int c = 0;
-  if (k - 1 >= 0) { e[c] = (int)(k - 1); a[c] = N; ++c; }
-  if (k < n) { e[c] = (int)k; a[c] = 0; ++c; }
+  if (k - 1 >= 0) { e[c] = k - 1; a[c] = N; ++c; }
+  if (k < n) { e[c] = k; a[c] = 0; ++c; }
   return c;
 }
 
+// block (x-run of a lattice row, Y = blockIdx.y, Z = Z0 + blockIdx.z); one thread per node
 template <typename TV>
-__global__ void lattice_correction_kernel(const BoxNumbering b, const int64_t NX, const int64_t NY, const int64_t nlat,
+__global__ void lattice_correction_kernel(const BoxNumbering b, const int NX, const int Z0,
                                           const int32_t* __restrict__ g2l, const float* __restrict__ out,
                                           const float* __restrict__ scale, const TV* __restrict__ coef,
                                           TV* __restrict__ z) {
   constexpr int Nq = kMlpNq, Np = Nq * Nq * Nq;
-  for (int64_t id = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; id < nlat; id += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t X = id % NX, Y = (id / NX) % NY, Z = id / (NX * NY);
-    int ex[2], ax[2], ey[2], ay[2], ez[2], az[2];
-    const int cx = axis_copies(X, b.nx, b.periodic, ex, ax);
-    const int cy = axis_copies(Y, b.ny, b.periodic, ey, ay);
-    const int cz = axis_copies(Z, b.nz, b.periodic, ez, az);
-    const int64_t e0 = ex[0] + (int64_t)b.nx * (ey[0] + (int64_t)b.ny * ez[0]);
-    const int32_t g = g2l[e0 * Np + ax[0] + Nq * (ay[0] + Nq * az[0])];
-    if (g < 0) continue;
-    TV sum = 0;
-    for (int k = 0; k < cz; ++k)
-      for (int j = 0; j < cy; ++j)
-        for (int i = 0; i < cx; ++i) {
-          const int64_t e = ex[i] + (int64_t)b.nx * (ey[j] + (int64_t)b.ny * ez[k]);
-          sum += (TV)(scale[e] * out[e * kMlpOut + ax[i] + Nq * (ay[j] + Nq * az[k])]);
-        }
-    z[g] += coef[g] * sum;
-  }
+  const int X = blockIdx.x * blockDim.x + threadIdx.x;
+  if (X >= NX) return;
+  int ex[2], ax[2], ey[2], ay[2], ez[2], az[2];
+  const int cx = axis_copies(X, b.nx, b.periodic, ex, ax);
+  const int cy = axis_copies((int)blockIdx.y, b.ny, b.periodic, ey, ay);
+  const int cz = axis_copies(Z0 + (int)blockIdx.z, b.nz, b.periodic, ez, az);
+  const int64_t nxy = (int64_t)b.nx * b.ny;
+  const int64_t e0 = ex[0] + (int64_t)b.nx * ey[0] + nxy * ez[0];
+  const int32_t g = g2l[e0 * Np + ax[0] + Nq * (ay[0] + Nq * az[0])];
+  if (g < 0) return;
+  TV sum = 0;
+  for (int k = 0; k < cz; ++k)
+    for (int j = 0; j < cy; ++j)
+      for (int i = 0; i < cx; ++i) {
+        const int64_t e = ex[i] + (int64_t)b.nx * ey[j] + nxy * ez[k];
+        sum += (TV)(scale[e] * out[e * kMlpOut + ax[i] + Nq * (ay[j] + Nq * az[k])]);
+      }
+  z[g] += coef[g] * sum;
 }
 template <typename TV>
 int lattice_correction(const BoxNumbering& b, const int32_t* g2l, const float* out, const float* scale,
-                       const TV* coef, TV* z, cudaStream_t s) {
+                       const TV* coef, TV* z, int Zbegin, int Zend, cudaStream_t s) {
   if (b.N != kMlpNq - 1) return set_error(LPG_ERR_UNSUPPORTED, "lattice correction: N = 7 only");
   const int64_t NX = (int64_t)b.nx * b.N + (b.periodic ? 0 : 1);
   const int64_t NY = (int64_t)b.ny * b.N + (b.periodic ? 0 : 1);
   const int64_t NZ = (int64_t)b.nz * b.N + (b.periodic ? 0 : 1);
-  const int64_t nlat = NX * NY * NZ;
-  if (nlat <= 0) return LPG_OK;
-  lattice_correction_kernel<TV><<<grid_n(nlat), 256, 0, s>>>(b, NX, NY, nlat, g2l, out, scale, coef, z);
+  if (NX > INT32_MAX / 2 || NY > 65535 || Zbegin < 0 || Zend > NZ || Zend - Zbegin > 65535)
+    return set_error(LPG_ERR_UNSUPPORTED, "lattice correction: lattice too large for the launch grid");
+  if (Zend <= Zbegin) return LPG_OK;
+  constexpr int T = 128;
+  const dim3 grid((unsigned)((NX + T - 1) / T), (unsigned)NY, (unsigned)(Zend - Zbegin));
+  lattice_correction_kernel<TV><<<grid, T, 0, s>>>(b, (int)NX, Zbegin, g2l, out, scale, coef, z);
   LPG_LAUNCH_CHECK("lattice_correction_kernel");
   return LPG_OK;
 }
 template int lattice_correction<double>(const BoxNumbering&, const int32_t*, const float*, const float*, const double*,
-                                        double*, cudaStream_t);
+                                        double*, int, int, cudaStream_t);
 template int lattice_correction<float>(const BoxNumbering&, const int32_t*, const float*, const float*, const float*,
-                                       float*, cudaStream_t);
+                                       float*, int, int, cudaStream_t);
 
 // training target: t = D .* e_local / s (network output units), e gathered from the dofs
 __global__ void target_kernel(const int Np, const int64_t count, const int32_t* __restrict__ elems,

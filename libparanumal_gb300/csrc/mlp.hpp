@@ -83,12 +83,13 @@ int element_features(const BoxNumbering& b, int64_t E, int64_t e0, int64_t count
 template <typename TV>
 int apply_correction(int Np, int64_t count, int64_t e0, const int32_t* g2l, const float* out, const float* scale,
                      const TV* coef, TV* z, cudaStream_t s);
-// The same correction for every element of a box at once, one thread per global lattice
-// node: z[g] += coef[g] * sum over the copies (e, n) of the node of scale[e] * out[e][n]
-// (out and scale hold all E elements). No atomics: each dof is written by one thread.
+// The same correction summed per global lattice node, one thread per node of the lattice
+// planes Zbegin <= Z < Zend: z[g] += coef[g] * sum over the copies (e, n) of the node of
+// scale[e] * out[e][n] (out and scale indexed by global element; the elements touching
+// those planes must be filled). No atomics: each dof is written by one thread.
 template <typename TV>
 int lattice_correction(const BoxNumbering& b, const int32_t* g2l, const float* out, const float* scale,
-                       const TV* coef, TV* z, cudaStream_t s);
+                       const TV* coef, TV* z, int Zbegin, int Zend, cudaStream_t s);
 int training_targets(int Np, int64_t count, const int32_t* elems, const int32_t* g2l, const double* e,
                      const double* invDiag, const float* scale, float* T, cudaStream_t s);
 int gather_rows(int64_t count, const int32_t* elems, const float* Xall, float* X, cudaStream_t s);

@@ -177,13 +177,17 @@ print(json.dumps(dict(iterations=r["iterations"], converged=r["converged"], fall
 """
 
 
-@pytest.mark.parametrize("nx,bc", [(42, 1), (6, 2), (5, -1)], ids=["dirichlet_2chunks", "neumann", "periodic"])
-def test_lattice_correction_matches_atomic_correction(trained, tmp_path, nx, bc):
+@pytest.mark.parametrize("dims,bc", [((42, 42, 42), 1), ((6, 6, 6), 2), ((5, 5, 5), -1), ((182, 182, 2), -1)],
+                         ids=["dirichlet_2chunks", "neumann", "periodic", "periodic_2chunks"])
+def test_lattice_correction_matches_atomic_correction(trained, tmp_path, dims, bc):
     """The network's correction summed per lattice node (one thread per dof over its
     element copies, the default) against the per-element atomic sum
     (LPG_LEARNED_CORRECTION=atomic), through whole FPCG solves: equal iterations and
-    solutions equal to 1e-9 (the two differ only in the order the copies are added). The
-    42^3 box has 74,088 elements, more than one inference chunk of 65,536."""
+    solutions equal to 1e-9 (the two differ only in the order the copies are added).
+    Inference runs in chunks of whole element layers of at most 65,536 elements and each
+    chunk's completed lattice planes are summed before the next: the 42^3 box runs 37 + 5
+    layers (the shared plane waits for the second chunk), the periodic 182 x 182 x 2 box one
+    layer per chunk (plane 0, shared by the last and first layers, comes last)."""
     import json
     import os
     import subprocess
@@ -191,7 +195,8 @@ def test_lattice_correction_matches_atomic_correction(trained, tmp_path, nx, bc)
     w, _ = trained
     wf = tmp_path / "w.npy"
     np.save(wf, w)
-    s = learned_problem(nx, **{"BOX BOUNDARY FLAG": bc, "PRECONDITIONER PRECISION": "FP64"})
+    s = learned_problem(dims[0], **{"BOX NY": dims[1], "BOX NZ": dims[2], "BOX BOUNDARY FLAG": bc,
+                                    "PRECONDITIONER PRECISION": "FP64"})
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
     res = {}
     for mode in ("lattice", "atomic"):
