@@ -179,7 +179,7 @@ print(json.dumps(dict(iterations=r["iterations"], converged=r["converged"], fall
 
 @pytest.mark.parametrize("dims,bc", [((42, 42, 42), 1), ((6, 6, 6), 2), ((5, 5, 5), -1), ((182, 182, 2), -1)],
                          ids=["dirichlet_2chunks", "neumann", "periodic", "periodic_2chunks"])
-def test_lattice_correction_matches_atomic_correction(trained, tmp_path, dims, bc):
+def test_lattice_correction_matches_atomic_correction(trained_full, tmp_path, dims, bc):
     """The network's correction summed per lattice node (one thread per dof over its
     element copies, the default) against the per-element atomic sum
     (LPG_LEARNED_CORRECTION=atomic), through whole FPCG solves: equal iterations and
@@ -192,11 +192,11 @@ def test_lattice_correction_matches_atomic_correction(trained, tmp_path, dims, b
     import os
     import subprocess
     import sys
-    w, _ = trained
+    w, _ = trained_full
     wf = tmp_path / "w.npy"
     np.save(wf, w)
     s = learned_problem(dims[0], **{"BOX NY": dims[1], "BOX NZ": dims[2], "BOX BOUNDARY FLAG": bc,
-                                    "PRECONDITIONER PRECISION": "FP64"})
+                                    "PRECONDITIONER PRECISION": "FP64", "MAXIMUM ITERATIONS": 60})
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
     res = {}
     for mode in ("lattice", "atomic"):
@@ -210,6 +210,6 @@ def test_lattice_correction_matches_atomic_correction(trained, tmp_path, dims, b
         assert p.returncode == 0, p.stderr[-2000:]
         res[mode] = json.loads(p.stdout.strip().splitlines()[-1]), np.load(out)
     (a, xa), (b, xb) = res["lattice"], res["atomic"]
-    assert a["converged"] and b["converged"] and a["fallbacks"] == b["fallbacks"] == 0
+    assert a["converged"] and b["converged"] and a["fallbacks"] == b["fallbacks"] == 0, (a, b)
     assert a["iterations"] == b["iterations"], (a, b)
     assert rel_err(xa, xb) < 1e-9
