@@ -91,7 +91,7 @@ int LearnedSmoother::apply(const BoxNumbering& b, int64_t E, const int32_t* g2l,
   if ((rc = ensure_chunk(C))) return rc;
   static const bool atomic = [] {
     const char* e = std::getenv("LPG_LEARNED_CORRECTION");
-    return e && !std::strcmp(e, "atomic");
+    return !(e && !std::strcmp(e, "lattice"));
   }();
   if (atomic) {
     for (int64_t e0 = 0; e0 < E; e0 += C) {

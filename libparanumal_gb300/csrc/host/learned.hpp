@@ -29,9 +29,10 @@ struct LearnedSmoother {
   // z (assembled) += sum over copies of coef .* s_e MLP(features(r)), coef = weight / diag
   // (the average over copies of s_e invDiag .* output). Element scales s_e are floored at
   // sfloor (the caller's kScaleFloor x residual RMS). The network runs in chunks of kChunk
-  // elements; by default their outputs are kept for all elements and one lattice-node
-  // kernel sums each dof's copies (no atomics). LPG_LEARNED_CORRECTION=atomic (a tuning
-  // override) adds each chunk's copies with atomics instead.
+  // elements and each chunk's copies are added with atomics (interior nodes with plain
+  // stores). LPG_LEARNED_CORRECTION=lattice (a tuning override, measured 3-7 % slower per
+  // solve at 64^3 and 112^3) keeps all outputs and sums each dof's copies in one thread per
+  // lattice node instead, in whole element layers as each chunk completes them.
   template <typename T>
   int apply(const BoxNumbering& b, int64_t E, const int32_t* g2l, const T* r, const T* coef, T* z, int64_t Nglobal,
             float sfloor, cudaStream_t s);

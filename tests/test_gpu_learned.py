@@ -177,17 +177,17 @@ print(json.dumps(dict(iterations=r["iterations"], converged=r["converged"], fall
 """
 
 
-@pytest.mark.parametrize("dims,bc", [((42, 42, 42), 1), ((6, 6, 6), 2), ((5, 5, 5), -1), ((182, 182, 2), -1)],
+@pytest.mark.parametrize("dims,bc", [((42, 42, 42), 1), ((6, 6, 6), 2), ((5, 5, 5), -1), ((42, 42, 42), -1)],
                          ids=["dirichlet_2chunks", "neumann", "periodic", "periodic_2chunks"])
 def test_lattice_correction_matches_atomic_correction(trained_full, tmp_path, dims, bc):
     """The network's correction summed per lattice node (one thread per dof over its
-    element copies, the default) against the per-element atomic sum
-    (LPG_LEARNED_CORRECTION=atomic), through whole FPCG solves: equal iterations and
-    solutions equal to 1e-9 (the two differ only in the order the copies are added).
-    Inference runs in chunks of whole element layers of at most 65,536 elements and each
-    chunk's completed lattice planes are summed before the next: the 42^3 box runs 37 + 5
-    layers (the shared plane waits for the second chunk), the periodic 182 x 182 x 2 box one
-    layer per chunk (plane 0, shared by the last and first layers, comes last)."""
+    element copies, LPG_LEARNED_CORRECTION=lattice) against the per-element atomic sum
+    (the default), through whole FPCG solves: equal iterations and solutions equal to 1e-9
+    (the two differ only in the order the copies are added). The lattice path runs the
+    network in chunks of whole element layers of at most 65,536 elements and sums each
+    chunk's completed lattice planes before the next: the 42^3 boxes run 37 + 5 layers (the
+    shared plane waits for the second chunk; plane 0 of the periodic box, shared by the
+    last and first layers, comes last)."""
     import json
     import os
     import subprocess
@@ -202,8 +202,8 @@ def test_lattice_correction_matches_atomic_correction(trained_full, tmp_path, di
     for mode in ("lattice", "atomic"):
         env = dict(os.environ, PYTHONPATH=root)
         env.pop("LPG_LEARNED_CORRECTION", None)
-        if mode == "atomic":
-            env["LPG_LEARNED_CORRECTION"] = "atomic"
+        if mode == "lattice":
+            env["LPG_LEARNED_CORRECTION"] = "lattice"
         out = tmp_path / (mode + ".npy")
         p = subprocess.run([sys.executable, "-c", _CHILD, json.dumps(s), str(wf), str(out)], env=env, cwd=root,
                            capture_output=True, text=True, timeout=600)
