@@ -759,6 +759,192 @@ ax_hex_dw_kernel(const int64_t Nelements, const int32_t* __restrict__ elementLis
     if (r_id[k] >= 0) atomicAdd(out + r_id[k], dw_to_double(r_Aq[k]));
 }
 
+// The double-word even-odd kernel with fewer registers and instructions, for three CTAs
+// (24 warps) per SM instead of two: each thread's q pencil lives in shared memory (it is
+// only read back by the same thread) instead of registers, the dof indices are re-read
+// from g2l at the end, and intermediate sums skip the renormalisation that their
+// consumers do not need (dw_add_u, dw_acc::raw). PFG as above.
+template <int NQ, bool PFG>
+__global__ void __launch_bounds__(NQ * NQ * elems_per_block<NQ>(), 3)
+ax_hex_dw_lean_kernel(const int64_t Nelements, const int32_t* __restrict__ elementList,
+                      const int32_t* __restrict__ g2l, const dw* __restrict__ ggeo, const int64_t geoStride,
+                      const dw* __restrict__ wJ, const int64_t wJStride, const double* __restrict__ Dg,
+                      const double lambda, const double* __restrict__ lambdaE, const double* __restrict__ q,
+                      double* __restrict__ out) {
+  static_assert(NQ == 8, "lean double-word kernel: Nq = 8");
+  constexpr int NP = NQ * NQ * NQ, H = NQ / 2, N = NQ - 1;
+  constexpr int EPB = elems_per_block<NQ>();
+  constexpr int NT = NQ * NQ * EPB;
+  __shared__ dw s_Dp[H][H], s_Dm[H][H], s_Tp[H][H], s_Tm[H][H];
+  __shared__ dw s_R[EPB][NQ][NQ], s_S[EPB][NQ][NQ], s_dr[EPB][NQ][NQ], s_ds[EPB][NQ][NQ];
+  // s_q: layer k of the thread's q pencil until layer k reads it, then that layer's
+  // t-contraction input G_t . grad q (the same thread writes and reads each slot)
+  __shared__ dw s_q[NQ][NT], s_qt[NQ][NT];
+
+  const int i = threadIdx.x, jj = threadIdx.y, el = threadIdx.z;
+  const int j = eo_row<NQ>(jj);
+  const int tid = i + NQ * (jj + NQ * el);
+  for (int t = tid; t < H * H; t += NT) {
+    const int a = t / H, m = t % H;
+    const double d0 = Dg[a * NQ + m], d1 = Dg[a * NQ + N - m];
+    const double t0 = Dg[m * NQ + a], t1 = Dg[(N - m) * NQ + a];
+    s_Dp[a][m] = dw_from_double(0.5 * (d0 + d1));
+    s_Dm[a][m] = dw_from_double(0.5 * (d0 - d1));
+    s_Tp[a][m] = dw_from_double(0.5 * (t0 + t1));
+    s_Tm[a][m] = dw_from_double(0.5 * (t0 - t1));
+  }
+
+  int64_t e = (int64_t)blockIdx.x * EPB + el;
+  const bool active = e < Nelements;
+  if (active && elementList) e = elementList[e];
+  if (!active) e = 0;
+
+  const int64_t nodeBase = e * NP + j * NQ + i;
+  {
+    int32_t id[NQ];
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) id[k] = active ? __ldg(g2l + nodeBase + k * NQ * NQ) : -1;
+    double qv[NQ];
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) qv[k] = (id[k] >= 0) ? q[id[k]] : 0.0;
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) s_q[k][tid] = dw_from_double(qv[k]);
+  }
+  const dw lam = dw_from_double((lambdaE && active) ? lambdaE[e] : lambda);
+  const dw* gp = ggeo + e * geoStride + j * NQ + i;
+  const dw* wp = wJ + e * wJStride + j * NQ + i;
+  __syncthreads();
+
+  {
+    dw E[H], O[H];
+#pragma unroll
+    for (int m = 0; m < H; ++m) {
+      const dw q0 = s_q[m][tid], q1 = s_q[N - m][tid];
+      E[m] = dw_add_u(q0, q1);
+      O[m] = dw_add_u(q0, dw_neg(q1));
+    }
+#pragma unroll
+    for (int t = 0; t < H; ++t) {
+      dw_acc A, B;
+#pragma unroll
+      for (int m = 0; m < H; ++m) {
+        A.mac(s_Dp[t][m], E[m]);
+        B.mac(s_Dm[t][m], O[m]);
+      }
+      const dw a = A.raw(), b = B.raw();
+      s_qt[t][tid] = dw_add_u(a, b);
+      s_qt[N - t][tid] = dw_add_u(b, dw_neg(a));
+    }
+  }
+
+  const bool rtask = i < H;
+  const int pt = rtask ? i : i - H;
+  dw* dst0 = rtask ? &s_dr[el][j][pt] : &s_ds[el][pt][j];
+  dw* dst1 = rtask ? &s_dr[el][j][N - pt] : &s_ds[el][N - pt][j];
+  const dw* line = rtask ? &s_R[el][j][0] : &s_S[el][j][0];
+  const int slotR = (i < H) ? i : H + N - i, slotS = (j < H) ? j : H + N - j;
+  const float sgnR = (i < H) ? 1.f : -1.f, sgnS = (j < H) ? 1.f : -1.f;
+
+  const dw zero{0.f, 0.f};
+  dw r_Aq[NQ];
+  dw nG[7];
+  if constexpr (PFG) {
+#pragma unroll
+    for (int c = 0; c < 6; ++c) nG[c] = active ? gp[c * NP] : zero;
+    nG[6] = active ? wp[0] : zero;
+  }
+#pragma unroll
+  for (int k = 0; k < NQ; ++k) {
+    const int off = k * NQ * NQ;
+    dw G00, G01, G02, G11, G12, G22, GwJ;
+    if constexpr (PFG) {
+      G00 = nG[0]; G01 = nG[1]; G02 = nG[2]; G11 = nG[3]; G12 = nG[4]; G22 = nG[5]; GwJ = nG[6];
+      if (k + 1 < NQ) {
+        const int noff = off + NQ * NQ;
+#pragma unroll
+        for (int c = 0; c < 6; ++c) nG[c] = active ? gp[c * NP + noff] : zero;
+        nG[6] = active ? wp[noff] : zero;
+      }
+    } else {
+      G00 = active ? gp[0 * NP + off] : zero; G01 = active ? gp[1 * NP + off] : zero;
+      G02 = active ? gp[2 * NP + off] : zero; G11 = active ? gp[3 * NP + off] : zero;
+      G12 = active ? gp[4 * NP + off] : zero; G22 = active ? gp[5 * NP + off] : zero;
+      GwJ = active ? wp[off] : zero;
+    }
+    const dw v = s_q[k][tid];
+    const dw pr = dw_shfl_xor(v, NQ - 1), ps = dw_shfl_xor(v, 2 * NQ);
+    s_R[el][j][slotR] = dw_add_u(pr, dw_scale_sign(sgnR, v));
+    s_S[el][i][slotS] = dw_add_u(ps, dw_scale_sign(sgnS, v));
+    eo_sync<NQ>(el);
+    {
+      dw_acc A, B;
+#pragma unroll
+      for (int m = 0; m < H; ++m) {
+        A.mac(s_Dp[pt][m], line[m]);
+        B.mac(s_Dm[pt][m], line[H + m]);
+      }
+      const dw a = A.raw(), b = B.raw();
+      *dst0 = dw_add_u(a, b);
+      *dst1 = dw_add_u(b, dw_neg(a));
+    }
+    eo_sync<NQ>(el);
+    const dw qr = s_dr[el][j][i], qs = s_ds[el][j][i], qtk = s_qt[k][tid];
+    dw_acc ar, as, at;
+    ar.mac(G00, qr); ar.mac(G01, qs); ar.mac(G02, qtk);
+    as.mac(G01, qr); as.mac(G11, qs); as.mac(G12, qtk);
+    at.mac(G02, qr); at.mac(G12, qs); at.mac(G22, qtk);
+    const dw Gqr = ar.raw(), Gqs = as.raw();
+    s_q[k][tid] = at.raw();
+    const dw mass = dw_mul(dw_mul(GwJ, lam), v);
+    const dw pr2 = dw_shfl_xor(Gqr, NQ - 1), ps2 = dw_shfl_xor(Gqs, 2 * NQ);
+    s_R[el][j][slotR] = dw_add_u(pr2, dw_scale_sign(sgnR, Gqr));
+    s_S[el][i][slotS] = dw_add_u(ps2, dw_scale_sign(sgnS, Gqs));
+    eo_sync<NQ>(el);
+    {
+      dw_acc A, B;
+#pragma unroll
+      for (int m = 0; m < H; ++m) {
+        A.mac(s_Tp[pt][m], line[m]);
+        B.mac(s_Tm[pt][m], line[H + m]);
+      }
+      const dw a = A.raw(), b = B.raw();
+      *dst0 = dw_add_u(a, b);
+      *dst1 = dw_add_u(b, dw_neg(a));
+    }
+    eo_sync<NQ>(el);
+    r_Aq[k] = dw_add_u(dw_add_u(mass, s_dr[el][j][i]), s_ds[el][j][i]);
+  }
+
+  {
+    dw E[H], O[H];
+#pragma unroll
+    for (int m = 0; m < H; ++m) {
+      const dw g0 = s_q[m][tid], g1 = s_q[N - m][tid];
+      E[m] = dw_add_u(g0, g1);
+      O[m] = dw_add_u(g0, dw_neg(g1));
+    }
+#pragma unroll
+    for (int t = 0; t < H; ++t) {
+      dw_acc A, B;
+#pragma unroll
+      for (int m = 0; m < H; ++m) {
+        A.mac(s_Tp[t][m], E[m]);
+        B.mac(s_Tm[t][m], O[m]);
+      }
+      const dw a = A.raw(), b = B.raw();
+      r_Aq[t] = dw_add_u(r_Aq[t], dw_add_u(a, b));
+      r_Aq[N - t] = dw_add_u(r_Aq[N - t], dw_add_u(b, dw_neg(a)));
+    }
+  }
+
+  if (!active) return;
+#pragma unroll
+  for (int k = 0; k < NQ; ++k) {
+    const int32_t id = __ldg(g2l + nodeBase + k * NQ * NQ);
+    if (id >= 0) atomicAdd(out + id, dw_to_double(r_Aq[k]));
+  }
+}
+
 // Double-word operator for the degrees without an even-odd kernel (N = 1, 2, 4, 5, 6, 8):
 // one thread per node, EPB elements per CTA (at least 128 threads), direct Nq-term
 // contractions through shared memory, the same df64 building blocks and FP64 assembly.
@@ -835,6 +1021,22 @@ static int launch_dw_generic(const AxArgs<double, float2>& a, cudaStream_t s) {
   return LPG_OK;
 }
 
+// N = 7 double-word kernel: geometric factors loaded one layer ahead (64^3: 4.36 ms
+// against 4.42 ms). LPG_AX_DW = noprefetch | lean | leanpf are tuning overrides: loads at
+// the top of each layer, and the three-CTA-per-SM kernel without / with the prefetch.
+enum class Dw7 { Prefetch, Plain, Lean, LeanPrefetch };
+static Dw7 dw7_variant() {
+  static const Dw7 v = [] {
+    const char* ev = std::getenv("LPG_AX_DW");
+    if (!ev) return Dw7::Prefetch;
+    if (!std::strcmp(ev, "noprefetch")) return Dw7::Plain;
+    if (!std::strcmp(ev, "lean")) return Dw7::Lean;
+    if (!std::strcmp(ev, "leanpf")) return Dw7::LeanPrefetch;
+    return Dw7::Prefetch;
+  }();
+  return v;
+}
+
 int ax_hex_dw(const AxArgs<double, float2>& a, cudaStream_t s) {
   if (a.Nelements <= 0) return LPG_OK;
   if (a.N < 1 || a.N > 8) return set_error(LPG_ERR_UNSUPPORTED, "double-word operator: N must be 1..8");
@@ -850,20 +1052,18 @@ int ax_hex_dw(const AxArgs<double, float2>& a, cudaStream_t s) {
   }
   if (a.N == 7) {
     const int64_t blocks = (a.Nelements + 3) / 4;
-    // geometric factors loaded one layer ahead (64^3: 4.36 ms against 4.42 ms); LPG_AX_DW =
-    // noprefetch is a tuning override back to loads at the top of each layer
-    static const bool noprefetch = [] {
-      const char* ev = std::getenv("LPG_AX_DW");
-      return ev && !std::strcmp(ev, "noprefetch");
-    }();
-    if (!noprefetch)
-      ax_hex_dw_kernel<8, true><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(
-          a.Nelements, a.elementList, a.g2l, reinterpret_cast<const dw*>(a.ggeo), a.geoStride,
-          reinterpret_cast<const dw*>(a.wJ), a.wJStride, a.D, a.lambda, a.lambdaE, a.q, a.out);
-    else
-      ax_hex_dw_kernel<8><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(
-          a.Nelements, a.elementList, a.g2l, reinterpret_cast<const dw*>(a.ggeo), a.geoStride,
-          reinterpret_cast<const dw*>(a.wJ), a.wJStride, a.D, a.lambda, a.lambdaE, a.q, a.out);
+#define LPG_DW_ARGS                                                                                   \
+  a.Nelements, a.elementList, a.g2l, reinterpret_cast<const dw*>(a.ggeo), a.geoStride,               \
+      reinterpret_cast<const dw*>(a.wJ), a.wJStride, a.D, a.lambda, a.lambdaE, a.q, a.out
+    switch (dw7_variant()) {
+      case Dw7::Prefetch: ax_hex_dw_kernel<8, true><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS); break;
+      case Dw7::Plain: ax_hex_dw_kernel<8><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS); break;
+      case Dw7::Lean: ax_hex_dw_lean_kernel<8, false><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS); break;
+      case Dw7::LeanPrefetch:
+        ax_hex_dw_lean_kernel<8, true><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS);
+        break;
+    }
+#undef LPG_DW_ARGS
   } else {
     const int64_t blocks = (a.Nelements + 15) / 16;
     ax_hex_dw_kernel<4><<<(unsigned)blocks, dim3(4, 4, 16), 0, s>>>(
@@ -1021,9 +1221,21 @@ int ax_hex(const AxArgs<T, G>& a, AxMode mode, cudaStream_t s) {
 
 template <int NQ>
 static cudaError_t fp64_occupancy(int* per, bool dw, bool mass, int epb) {
-  if (dw)
-    return NQ == 8 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(per, ax_hex_dw_kernel<NQ, true>, NQ * NQ * epb, 0)
-                   : cudaOccupancyMaxActiveBlocksPerMultiprocessor(per, ax_hex_dw_kernel<NQ>, NQ * NQ * epb, 0);
+  if (dw) {
+    if constexpr (NQ == 8) {
+      switch (dw7_variant()) {
+        case Dw7::Prefetch:
+          return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per, ax_hex_dw_kernel<8, true>, NQ * NQ * epb, 0);
+        case Dw7::Plain:
+          return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per, ax_hex_dw_kernel<8>, NQ * NQ * epb, 0);
+        case Dw7::Lean:
+          return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per, ax_hex_dw_lean_kernel<8, false>, NQ * NQ * epb, 0);
+        case Dw7::LeanPrefetch:
+          return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per, ax_hex_dw_lean_kernel<8, true>, NQ * NQ * epb, 0);
+      }
+    }
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per, ax_hex_dw_kernel<NQ>, NQ * NQ * epb, 0);
+  }
   if (fp64_direct_override())
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
         per, ax_hex_kernel<NQ, double, double, IN_GATHER, OUT_ASSEMBLE>, NQ * NQ * epb, 0);

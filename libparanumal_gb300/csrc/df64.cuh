@@ -47,6 +47,13 @@ __device__ __forceinline__ dw dw_add(dw x, dw y) {
   const float w = __fadd_rn(s.l, __fadd_rn(x.l, y.l));
   return dw_fast_two_sum(s.h, w);
 }
+// the sloppy sum without the final renormalisation: s.h exact TwoSum high part, low part
+// s.l + x.l + y.l (|low| of order ulp(|x| + |y|)). Every consumer here (products, sums,
+// the FP64 rebuild) takes an unnormalised pair; the error bound is that of dw_add.
+__device__ __forceinline__ dw dw_add_u(dw x, dw y) {
+  const dw s = dw_two_sum(x.h, y.h);
+  return {s.h, __fadd_rn(s.l, __fadd_rn(x.l, y.l))};
+}
 __device__ __forceinline__ dw dw_neg(dw x) { return {-x.h, -x.l}; }
 __device__ __forceinline__ dw dw_sub(dw x, dw y) { return dw_add(x, dw_neg(y)); }
 // sign * x for sign = +-1 (exact)
@@ -74,6 +81,7 @@ struct dw_acc {
     l = __fadd_rn(l, __fadd_rn(pl, s.l));
   }
   __device__ __forceinline__ dw get() const { return dw_fast_two_sum(h, l); }
+  __device__ __forceinline__ dw raw() const { return {h, l}; }   // unnormalised
 };
 
 __device__ __forceinline__ dw dw_from_double(double x) {
