@@ -763,8 +763,10 @@ ax_hex_dw_kernel(const int64_t Nelements, const int32_t* __restrict__ elementLis
 // (24 warps) per SM instead of two: each thread's q pencil lives in shared memory (it is
 // only read back by the same thread) instead of registers, the dof indices are re-read
 // from g2l at the end, and intermediate sums skip the renormalisation that their
-// consumers do not need (dw_add_u, dw_acc::raw). PFG as above.
-template <int NQ, bool PFG>
+// consumers do not need (dw_add_u, dw_acc::raw), sums start from their first product, and
+// the +-1 of the even/odd line values is folded into FMAs. PFG as above; MASS = false:
+// lambda == 0 and no lambda field, the mass term and its wJ reads are left out.
+template <int NQ, bool PFG, bool MASS = true>
 __global__ void __launch_bounds__(NQ * NQ * elems_per_block<NQ>(), 3)
 ax_hex_dw_lean_kernel(const int64_t Nelements, const int32_t* __restrict__ elementList,
                       const int32_t* __restrict__ g2l, const dw* __restrict__ ggeo, const int64_t geoStride,
@@ -810,7 +812,7 @@ ax_hex_dw_lean_kernel(const int64_t Nelements, const int32_t* __restrict__ eleme
 #pragma unroll
     for (int k = 0; k < NQ; ++k) s_q[k][tid] = dw_from_double(qv[k]);
   }
-  const dw lam = dw_from_double((lambdaE && active) ? lambdaE[e] : lambda);
+  const dw lam = MASS ? dw_from_double((lambdaE && active) ? lambdaE[e] : lambda) : dw{0.f, 0.f};
   const dw* gp = ggeo + e * geoStride + j * NQ + i;
   const dw* wp = wJ + e * wJStride + j * NQ + i;
   __syncthreads();
@@ -825,9 +827,9 @@ ax_hex_dw_lean_kernel(const int64_t Nelements, const int32_t* __restrict__ eleme
     }
 #pragma unroll
     for (int t = 0; t < H; ++t) {
-      dw_acc A, B;
+      dw_acc A(s_Dp[t][0], E[0]), B(s_Dm[t][0], O[0]);
 #pragma unroll
-      for (int m = 0; m < H; ++m) {
+      for (int m = 1; m < H; ++m) {
         A.mac(s_Dp[t][m], E[m]);
         B.mac(s_Dm[t][m], O[m]);
       }
@@ -848,10 +850,11 @@ ax_hex_dw_lean_kernel(const int64_t Nelements, const int32_t* __restrict__ eleme
   const dw zero{0.f, 0.f};
   dw r_Aq[NQ];
   dw nG[7];
+  nG[6] = zero;
   if constexpr (PFG) {
 #pragma unroll
     for (int c = 0; c < 6; ++c) nG[c] = active ? gp[c * NP] : zero;
-    nG[6] = active ? wp[0] : zero;
+    if constexpr (MASS) nG[6] = active ? wp[0] : zero;
   }
 #pragma unroll
   for (int k = 0; k < NQ; ++k) {
@@ -863,23 +866,23 @@ ax_hex_dw_lean_kernel(const int64_t Nelements, const int32_t* __restrict__ eleme
         const int noff = off + NQ * NQ;
 #pragma unroll
         for (int c = 0; c < 6; ++c) nG[c] = active ? gp[c * NP + noff] : zero;
-        nG[6] = active ? wp[noff] : zero;
+        if constexpr (MASS) nG[6] = active ? wp[noff] : zero;
       }
     } else {
       G00 = active ? gp[0 * NP + off] : zero; G01 = active ? gp[1 * NP + off] : zero;
       G02 = active ? gp[2 * NP + off] : zero; G11 = active ? gp[3 * NP + off] : zero;
       G12 = active ? gp[4 * NP + off] : zero; G22 = active ? gp[5 * NP + off] : zero;
-      GwJ = active ? wp[off] : zero;
+      if constexpr (MASS) GwJ = active ? wp[off] : zero;
     }
     const dw v = s_q[k][tid];
     const dw pr = dw_shfl_xor(v, NQ - 1), ps = dw_shfl_xor(v, 2 * NQ);
-    s_R[el][j][slotR] = dw_add_u(pr, dw_scale_sign(sgnR, v));
-    s_S[el][i][slotS] = dw_add_u(ps, dw_scale_sign(sgnS, v));
+    s_R[el][j][slotR] = dw_add_sign_u(pr, sgnR, v);
+    s_S[el][i][slotS] = dw_add_sign_u(ps, sgnS, v);
     eo_sync<NQ>(el);
     {
-      dw_acc A, B;
+      dw_acc A(s_Dp[pt][0], line[0]), B(s_Dm[pt][0], line[H]);
 #pragma unroll
-      for (int m = 0; m < H; ++m) {
+      for (int m = 1; m < H; ++m) {
         A.mac(s_Dp[pt][m], line[m]);
         B.mac(s_Dm[pt][m], line[H + m]);
       }
@@ -889,21 +892,22 @@ ax_hex_dw_lean_kernel(const int64_t Nelements, const int32_t* __restrict__ eleme
     }
     eo_sync<NQ>(el);
     const dw qr = s_dr[el][j][i], qs = s_ds[el][j][i], qtk = s_qt[k][tid];
-    dw_acc ar, as, at;
-    ar.mac(G00, qr); ar.mac(G01, qs); ar.mac(G02, qtk);
-    as.mac(G01, qr); as.mac(G11, qs); as.mac(G12, qtk);
-    at.mac(G02, qr); at.mac(G12, qs); at.mac(G22, qtk);
+    dw_acc ar(G00, qr), as(G01, qr), at(G02, qr);
+    ar.mac(G01, qs); ar.mac(G02, qtk);
+    as.mac(G11, qs); as.mac(G12, qtk);
+    at.mac(G12, qs); at.mac(G22, qtk);
     const dw Gqr = ar.raw(), Gqs = as.raw();
     s_q[k][tid] = at.raw();
-    const dw mass = dw_mul(dw_mul(GwJ, lam), v);
+    dw mass{0.f, 0.f};
+    if constexpr (MASS) mass = dw_mul(dw_mul(GwJ, lam), v);
     const dw pr2 = dw_shfl_xor(Gqr, NQ - 1), ps2 = dw_shfl_xor(Gqs, 2 * NQ);
-    s_R[el][j][slotR] = dw_add_u(pr2, dw_scale_sign(sgnR, Gqr));
-    s_S[el][i][slotS] = dw_add_u(ps2, dw_scale_sign(sgnS, Gqs));
+    s_R[el][j][slotR] = dw_add_sign_u(pr2, sgnR, Gqr);
+    s_S[el][i][slotS] = dw_add_sign_u(ps2, sgnS, Gqs);
     eo_sync<NQ>(el);
     {
-      dw_acc A, B;
+      dw_acc A(s_Tp[pt][0], line[0]), B(s_Tm[pt][0], line[H]);
 #pragma unroll
-      for (int m = 0; m < H; ++m) {
+      for (int m = 1; m < H; ++m) {
         A.mac(s_Tp[pt][m], line[m]);
         B.mac(s_Tm[pt][m], line[H + m]);
       }
@@ -912,7 +916,8 @@ ax_hex_dw_lean_kernel(const int64_t Nelements, const int32_t* __restrict__ eleme
       *dst1 = dw_add_u(b, dw_neg(a));
     }
     eo_sync<NQ>(el);
-    r_Aq[k] = dw_add_u(dw_add_u(mass, s_dr[el][j][i]), s_ds[el][j][i]);
+    if constexpr (MASS) r_Aq[k] = dw_add_u(dw_add_u(mass, s_dr[el][j][i]), s_ds[el][j][i]);
+    else r_Aq[k] = dw_add_u(s_dr[el][j][i], s_ds[el][j][i]);
   }
 
   {
@@ -925,9 +930,9 @@ ax_hex_dw_lean_kernel(const int64_t Nelements, const int32_t* __restrict__ eleme
     }
 #pragma unroll
     for (int t = 0; t < H; ++t) {
-      dw_acc A, B;
+      dw_acc A(s_Tp[t][0], E[0]), B(s_Tm[t][0], O[0]);
 #pragma unroll
-      for (int m = 0; m < H; ++m) {
+      for (int m = 1; m < H; ++m) {
         A.mac(s_Tp[t][m], E[m]);
         B.mac(s_Tm[t][m], O[m]);
       }
@@ -1052,15 +1057,20 @@ int ax_hex_dw(const AxArgs<double, float2>& a, cudaStream_t s) {
   }
   if (a.N == 7) {
     const int64_t blocks = (a.Nelements + 3) / 4;
+    const bool mass = a.lambdaE || a.lambda != 0.0;
 #define LPG_DW_ARGS                                                                                   \
   a.Nelements, a.elementList, a.g2l, reinterpret_cast<const dw*>(a.ggeo), a.geoStride,               \
       reinterpret_cast<const dw*>(a.wJ), a.wJStride, a.D, a.lambda, a.lambdaE, a.q, a.out
     switch (dw7_variant()) {
       case Dw7::Prefetch: ax_hex_dw_kernel<8, true><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS); break;
       case Dw7::Plain: ax_hex_dw_kernel<8><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS); break;
-      case Dw7::Lean: ax_hex_dw_lean_kernel<8, false><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS); break;
+      case Dw7::Lean:
+        if (mass) ax_hex_dw_lean_kernel<8, false, true><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS);
+        else ax_hex_dw_lean_kernel<8, false, false><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS);
+        break;
       case Dw7::LeanPrefetch:
-        ax_hex_dw_lean_kernel<8, true><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS);
+        if (mass) ax_hex_dw_lean_kernel<8, true, true><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS);
+        else ax_hex_dw_lean_kernel<8, true, false><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS);
         break;
     }
 #undef LPG_DW_ARGS
@@ -1229,9 +1239,11 @@ static cudaError_t fp64_occupancy(int* per, bool dw, bool mass, int epb) {
         case Dw7::Plain:
           return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per, ax_hex_dw_kernel<8>, NQ * NQ * epb, 0);
         case Dw7::Lean:
-          return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per, ax_hex_dw_lean_kernel<8, false>, NQ * NQ * epb, 0);
+          return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per, ax_hex_dw_lean_kernel<8, false, true>,
+                                                               NQ * NQ * epb, 0);
         case Dw7::LeanPrefetch:
-          return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per, ax_hex_dw_lean_kernel<8, true>, NQ * NQ * epb, 0);
+          return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per, ax_hex_dw_lean_kernel<8, true, true>,
+                                                               NQ * NQ * epb, 0);
       }
     }
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per, ax_hex_dw_kernel<NQ>, NQ * NQ * epb, 0);

@@ -54,6 +54,14 @@ __device__ __forceinline__ dw dw_add_u(dw x, dw y) {
   const dw s = dw_two_sum(x.h, y.h);
   return {s.h, __fadd_rn(s.l, __fadd_rn(x.l, y.l))};
 }
+// x + sign * y (sign = +-1) unnormalised, the sign folded into FMAs: fma(sign, b, c) is
+// the exactly rounded c + sign * b, so this is dw_add_u(x, {sign y.h, sign y.l}) bit for bit
+__device__ __forceinline__ dw dw_add_sign_u(dw x, float sign, dw y) {
+  const float s = fmaf(sign, y.h, x.h);
+  const float bb = __fsub_rn(s, x.h);
+  const float e = __fadd_rn(__fsub_rn(x.h, __fsub_rn(s, bb)), fmaf(sign, y.h, -bb));
+  return {s, __fadd_rn(e, fmaf(sign, y.l, x.l))};
+}
 __device__ __forceinline__ dw dw_neg(dw x) { return {-x.h, -x.l}; }
 __device__ __forceinline__ dw dw_sub(dw x, dw y) { return dw_add(x, dw_neg(y)); }
 // sign * x for sign = +-1 (exact)
@@ -71,6 +79,14 @@ __device__ __forceinline__ dw dw_mul(dw x, dw y) {
 // sum of double-word products
 struct dw_acc {
   float h = 0.f, l = 0.f;
+  dw_acc() = default;
+  // started with its first product (no TwoSum against zero)
+  __device__ __forceinline__ dw_acc(dw a, dw b) {
+    h = __fmul_rn(a.h, b.h);
+    float pl = fmaf(a.h, b.h, -h);
+    pl = fmaf(a.h, b.l, pl);
+    l = fmaf(a.l, b.h, pl);
+  }
   __device__ __forceinline__ void mac(dw a, dw b) {
     const float ph = __fmul_rn(a.h, b.h);
     float pl = fmaf(a.h, b.h, -ph);

@@ -218,6 +218,7 @@ DW_CASES = [
     box(**{"POLYNOMIAL DEGREE": 3, "BOX BOUNDARY FLAG": -1, "MESH JITTER": 0.0, "BOX NX": 3,
            "BOX NY": 4, "BOX NZ": 2}),                                        # periodic, N=3
     box(**{"LAMBDA FIELD": "LOGNORMAL", "LAMBDA SEED": 2, "BOX NX": 32, "BOX NY": 32, "BOX NZ": 16}),
+    box(**{"LAMBDA": 0.0, "BOX NX": 9, "BOX NY": 7, "BOX NZ": 5}),            # N=7 without the mass term
     # degrees without an even-odd kernel (thread-per-node double-word kernel)
     box(**{"POLYNOMIAL DEGREE": 1, "BOX NX": 6, "BOX NY": 5, "BOX NZ": 4}),
     box(**{"POLYNOMIAL DEGREE": 2, "BOX BOUNDARY FLAG": -1, "MESH JITTER": 0.0, "BOX NX": 3, "BOX NY": 4,
