@@ -145,6 +145,10 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
   const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
 }
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
@@ -764,7 +768,9 @@ ax_hex_dw_kernel(const int64_t Nelements, const int32_t* __restrict__ elementLis
 // only read back by the same thread) instead of registers, the dof indices are re-read
 // from g2l at the end, and intermediate sums skip the renormalisation that their
 // consumers do not need (dw_add_u, dw_acc::raw), sums start from their first product, and
-// the +-1 of the even/odd line values is folded into FMAs. PFG as above; MASS = false:
+// the +-1 of the even/odd line values is folded into FMAs. PFG: each thread copies its
+// own geometric factors of layer k+1 into shared memory with cp.async while layer k is
+// computed (double-buffered; no registers held across the layer); MASS = false:
 // lambda == 0 and no lambda field, the mass term and its wJ reads are left out.
 template <int NQ, bool PFG, bool MASS = true>
 __global__ void __launch_bounds__(NQ * NQ * elems_per_block<NQ>(), 3)
@@ -782,6 +788,8 @@ ax_hex_dw_lean_kernel(const int64_t Nelements, const int32_t* __restrict__ eleme
   // s_q: layer k of the thread's q pencil until layer k reads it, then that layer's
   // t-contraction input G_t . grad q (the same thread writes and reads each slot)
   __shared__ dw s_q[NQ][NT], s_qt[NQ][NT];
+  // PFG: geometric factors (6 + wJ) of two layers, each slot written and read by its thread
+  __shared__ dw s_G[PFG ? 2 : 1][PFG ? 7 : 1][PFG ? NT : 1];
 
   const int i = threadIdx.x, jj = threadIdx.y, el = threadIdx.z;
   const int j = eo_row<NQ>(jj);
@@ -849,25 +857,21 @@ ax_hex_dw_lean_kernel(const int64_t Nelements, const int32_t* __restrict__ eleme
 
   const dw zero{0.f, 0.f};
   dw r_Aq[NQ];
-  dw nG[7];
-  nG[6] = zero;
-  if constexpr (PFG) {
+  auto stage = [&](const int k) {
+    if (active) {
 #pragma unroll
-    for (int c = 0; c < 6; ++c) nG[c] = active ? gp[c * NP] : zero;
-    if constexpr (MASS) nG[6] = active ? wp[0] : zero;
-  }
+      for (int c = 0; c < 6; ++c) cp_async8(&s_G[k & 1][c][tid], gp + c * NP + k * NQ * NQ);
+      if constexpr (MASS) cp_async8(&s_G[k & 1][6][tid], wp + k * NQ * NQ);
+    }
+    cp_async_commit();
+  };
+  if constexpr (PFG) stage(0);
 #pragma unroll
   for (int k = 0; k < NQ; ++k) {
     const int off = k * NQ * NQ;
-    dw G00, G01, G02, G11, G12, G22, GwJ;
+    dw G00, G01, G02, G11, G12, G22, GwJ = zero;
     if constexpr (PFG) {
-      G00 = nG[0]; G01 = nG[1]; G02 = nG[2]; G11 = nG[3]; G12 = nG[4]; G22 = nG[5]; GwJ = nG[6];
-      if (k + 1 < NQ) {
-        const int noff = off + NQ * NQ;
-#pragma unroll
-        for (int c = 0; c < 6; ++c) nG[c] = active ? gp[c * NP + noff] : zero;
-        if constexpr (MASS) nG[6] = active ? wp[noff] : zero;
-      }
+      if (k + 1 < NQ) stage(k + 1);
     } else {
       G00 = active ? gp[0 * NP + off] : zero; G01 = active ? gp[1 * NP + off] : zero;
       G02 = active ? gp[2 * NP + off] : zero; G11 = active ? gp[3 * NP + off] : zero;
@@ -892,6 +896,15 @@ ax_hex_dw_lean_kernel(const int64_t Nelements, const int32_t* __restrict__ eleme
     }
     eo_sync<NQ>(el);
     const dw qr = s_dr[el][j][i], qs = s_ds[el][j][i], qtk = s_qt[k][tid];
+    if constexpr (PFG) {
+      if (k + 1 < NQ) cp_async_wait<1>();
+      else cp_async_wait<0>();
+      const int b = k & 1;
+      G00 = active ? s_G[b][0][tid] : zero; G01 = active ? s_G[b][1][tid] : zero;
+      G02 = active ? s_G[b][2][tid] : zero; G11 = active ? s_G[b][3][tid] : zero;
+      G12 = active ? s_G[b][4][tid] : zero; G22 = active ? s_G[b][5][tid] : zero;
+      if constexpr (MASS) GwJ = active ? s_G[b][6][tid] : zero;
+    }
     dw_acc ar(G00, qr), as(G01, qr), at(G02, qr);
     ar.mac(G01, qs); ar.mac(G02, qtk);
     as.mac(G11, qs); as.mac(G12, qtk);
