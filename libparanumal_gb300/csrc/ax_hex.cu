@@ -763,6 +763,18 @@ ax_hex_dw_kernel(const int64_t Nelements, const int32_t* __restrict__ elementLis
     if (r_id[k] >= 0) atomicAdd(out + r_id[k], dw_to_double(r_Aq[k]));
 }
 
+// n double words from 16-byte aligned shared memory, two per 128-bit load
+template <int n>
+__device__ __forceinline__ void ld_dw4x2(const dw* src, dw* v) {
+  const float4* p = reinterpret_cast<const float4*>(src);
+#pragma unroll
+  for (int t = 0; t < n / 2; ++t) {
+    const float4 x = p[t];
+    v[2 * t] = {x.x, x.y};
+    v[2 * t + 1] = {x.z, x.w};
+  }
+}
+
 // The double-word even-odd kernel with fewer registers and instructions, for three CTAs
 // (24 warps) per SM instead of two: each thread's q pencil lives in shared memory (it is
 // only read back by the same thread) instead of registers, the dof indices are re-read
@@ -772,8 +784,8 @@ ax_hex_dw_kernel(const int64_t Nelements, const int32_t* __restrict__ elementLis
 // own geometric factors of layer k+1 into shared memory with cp.async while layer k is
 // computed (double-buffered; no registers held across the layer); MASS = false:
 // lambda == 0 and no lambda field, the mass term and its wJ reads are left out.
-template <int NQ, bool PFG, bool MASS = true>
-__global__ void __launch_bounds__(NQ * NQ * elems_per_block<NQ>(), 3)
+template <int NQ, bool PFG, bool MASS = true, int MINB = 3>
+__global__ void __launch_bounds__(NQ * NQ * elems_per_block<NQ>(), MINB)
 ax_hex_dw_lean_kernel(const int64_t Nelements, const int32_t* __restrict__ elementList,
                       const int32_t* __restrict__ g2l, const dw* __restrict__ ggeo, const int64_t geoStride,
                       const dw* __restrict__ wJ, const int64_t wJStride, const double* __restrict__ Dg,
@@ -783,8 +795,9 @@ ax_hex_dw_lean_kernel(const int64_t Nelements, const int32_t* __restrict__ eleme
   constexpr int NP = NQ * NQ * NQ, H = NQ / 2, N = NQ - 1;
   constexpr int EPB = elems_per_block<NQ>();
   constexpr int NT = NQ * NQ * EPB;
-  __shared__ dw s_Dp[H][H], s_Dm[H][H], s_Tp[H][H], s_Tm[H][H];
-  __shared__ dw s_R[EPB][NQ][NQ], s_S[EPB][NQ][NQ], s_dr[EPB][NQ][NQ], s_ds[EPB][NQ][NQ];
+  __shared__ __align__(16) dw s_Dp[H][H], s_Dm[H][H], s_Tp[H][H], s_Tm[H][H];
+  __shared__ __align__(16) dw s_R[EPB][NQ][NQ], s_S[EPB][NQ][NQ];
+  __shared__ dw s_dr[EPB][NQ][NQ], s_ds[EPB][NQ][NQ];
   // s_q: layer k of the thread's q pencil until layer k reads it, then that layer's
   // t-contraction input G_t . grad q (the same thread writes and reads each slot)
   __shared__ dw s_q[NQ][NT], s_qt[NQ][NT];
@@ -856,7 +869,7 @@ ax_hex_dw_lean_kernel(const int64_t Nelements, const int32_t* __restrict__ eleme
   const float sgnR = (i < H) ? 1.f : -1.f, sgnS = (j < H) ? 1.f : -1.f;
 
   const dw zero{0.f, 0.f};
-  dw r_Aq[NQ];
+  // the local result of layer k goes to s_qt[k] once layer k has read its t-derivative
   auto stage = [&](const int k) {
     if (active) {
 #pragma unroll
@@ -884,11 +897,15 @@ ax_hex_dw_lean_kernel(const int64_t Nelements, const int32_t* __restrict__ eleme
     s_S[el][i][slotS] = dw_add_sign_u(ps, sgnS, v);
     eo_sync<NQ>(el);
     {
-      dw_acc A(s_Dp[pt][0], line[0]), B(s_Dm[pt][0], line[H]);
+      dw L[NQ], Dp[H], Dm[H];
+      ld_dw4x2<NQ>(line, L);
+      ld_dw4x2<H>(&s_Dp[pt][0], Dp);
+      ld_dw4x2<H>(&s_Dm[pt][0], Dm);
+      dw_acc A(Dp[0], L[0]), B(Dm[0], L[H]);
 #pragma unroll
       for (int m = 1; m < H; ++m) {
-        A.mac(s_Dp[pt][m], line[m]);
-        B.mac(s_Dm[pt][m], line[H + m]);
+        A.mac(Dp[m], L[m]);
+        B.mac(Dm[m], L[H + m]);
       }
       const dw a = A.raw(), b = B.raw();
       *dst0 = dw_add_u(a, b);
@@ -918,19 +935,23 @@ ax_hex_dw_lean_kernel(const int64_t Nelements, const int32_t* __restrict__ eleme
     s_S[el][i][slotS] = dw_add_sign_u(ps2, sgnS, Gqs);
     eo_sync<NQ>(el);
     {
-      dw_acc A(s_Tp[pt][0], line[0]), B(s_Tm[pt][0], line[H]);
+      dw L[NQ], Tp[H], Tm[H];
+      ld_dw4x2<NQ>(line, L);
+      ld_dw4x2<H>(&s_Tp[pt][0], Tp);
+      ld_dw4x2<H>(&s_Tm[pt][0], Tm);
+      dw_acc A(Tp[0], L[0]), B(Tm[0], L[H]);
 #pragma unroll
       for (int m = 1; m < H; ++m) {
-        A.mac(s_Tp[pt][m], line[m]);
-        B.mac(s_Tm[pt][m], line[H + m]);
+        A.mac(Tp[m], L[m]);
+        B.mac(Tm[m], L[H + m]);
       }
       const dw a = A.raw(), b = B.raw();
       *dst0 = dw_add_u(a, b);
       *dst1 = dw_add_u(b, dw_neg(a));
     }
     eo_sync<NQ>(el);
-    if constexpr (MASS) r_Aq[k] = dw_add_u(dw_add_u(mass, s_dr[el][j][i]), s_ds[el][j][i]);
-    else r_Aq[k] = dw_add_u(s_dr[el][j][i], s_ds[el][j][i]);
+    if constexpr (MASS) s_qt[k][tid] = dw_add_u(dw_add_u(mass, s_dr[el][j][i]), s_ds[el][j][i]);
+    else s_qt[k][tid] = dw_add_u(s_dr[el][j][i], s_ds[el][j][i]);
   }
 
   {
@@ -950,8 +971,8 @@ ax_hex_dw_lean_kernel(const int64_t Nelements, const int32_t* __restrict__ eleme
         B.mac(s_Tm[t][m], O[m]);
       }
       const dw a = A.raw(), b = B.raw();
-      r_Aq[t] = dw_add_u(r_Aq[t], dw_add_u(a, b));
-      r_Aq[N - t] = dw_add_u(r_Aq[N - t], dw_add_u(b, dw_neg(a)));
+      s_qt[t][tid] = dw_add_u(s_qt[t][tid], dw_add_u(a, b));
+      s_qt[N - t][tid] = dw_add_u(s_qt[N - t][tid], dw_add_u(b, dw_neg(a)));
     }
   }
 
@@ -959,7 +980,7 @@ ax_hex_dw_lean_kernel(const int64_t Nelements, const int32_t* __restrict__ eleme
 #pragma unroll
   for (int k = 0; k < NQ; ++k) {
     const int32_t id = __ldg(g2l + nodeBase + k * NQ * NQ);
-    if (id >= 0) atomicAdd(out + id, dw_to_double(r_Aq[k]));
+    if (id >= 0) atomicAdd(out + id, dw_to_double(s_qt[k][tid]));
   }
 }
 
@@ -1042,7 +1063,7 @@ static int launch_dw_generic(const AxArgs<double, float2>& a, cudaStream_t s) {
 // N = 7 double-word kernel: geometric factors loaded one layer ahead (64^3: 4.36 ms
 // against 4.42 ms). LPG_AX_DW = noprefetch | lean | leanpf are tuning overrides: loads at
 // the top of each layer, and the three-CTA-per-SM kernel without / with the prefetch.
-enum class Dw7 { Prefetch, Plain, Lean, LeanPrefetch };
+enum class Dw7 { Prefetch, Plain, Lean, Lean4, LeanPrefetch };
 static Dw7 dw7_variant() {
   static const Dw7 v = [] {
     const char* ev = std::getenv("LPG_AX_DW");
@@ -1050,6 +1071,7 @@ static Dw7 dw7_variant() {
     if (!std::strcmp(ev, "noprefetch")) return Dw7::Plain;
     if (!std::strcmp(ev, "lean")) return Dw7::Lean;
     if (!std::strcmp(ev, "leanpf")) return Dw7::LeanPrefetch;
+    if (!std::strcmp(ev, "lean4")) return Dw7::Lean4;
     return Dw7::Prefetch;
   }();
   return v;
@@ -1080,6 +1102,10 @@ int ax_hex_dw(const AxArgs<double, float2>& a, cudaStream_t s) {
       case Dw7::Lean:
         if (mass) ax_hex_dw_lean_kernel<8, false, true><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS);
         else ax_hex_dw_lean_kernel<8, false, false><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS);
+        break;
+      case Dw7::Lean4:
+        if (mass) ax_hex_dw_lean_kernel<8, false, true, 4><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS);
+        else ax_hex_dw_lean_kernel<8, false, false, 4><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS);
         break;
       case Dw7::LeanPrefetch:
         if (mass) ax_hex_dw_lean_kernel<8, true, true><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS);
@@ -1253,6 +1279,9 @@ static cudaError_t fp64_occupancy(int* per, bool dw, bool mass, int epb) {
           return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per, ax_hex_dw_kernel<8>, NQ * NQ * epb, 0);
         case Dw7::Lean:
           return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per, ax_hex_dw_lean_kernel<8, false, true>,
+                                                               NQ * NQ * epb, 0);
+        case Dw7::Lean4:
+          return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per, ax_hex_dw_lean_kernel<8, false, true, 4>,
                                                                NQ * NQ * epb, 0);
         case Dw7::LeanPrefetch:
           return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per, ax_hex_dw_lean_kernel<8, true, true>,
