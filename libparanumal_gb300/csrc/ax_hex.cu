@@ -784,7 +784,7 @@ __device__ __forceinline__ void ld_dw4x2(const dw* src, dw* v) {
 // own geometric factors of layer k+1 into shared memory with cp.async while layer k is
 // computed (double-buffered; no registers held across the layer); MASS = false:
 // lambda == 0 and no lambda field, the mass term and its wJ reads are left out.
-template <int NQ, bool PFG, bool MASS = true, int MINB = 3>
+template <int NQ, bool PFG, bool MASS = true, int MINB = 3, bool ROLL = false>
 __global__ void __launch_bounds__(NQ * NQ * elems_per_block<NQ>(), MINB)
 ax_hex_dw_lean_kernel(const int64_t Nelements, const int32_t* __restrict__ elementList,
                       const int32_t* __restrict__ g2l, const dw* __restrict__ ggeo, const int64_t geoStride,
@@ -879,7 +879,9 @@ ax_hex_dw_lean_kernel(const int64_t Nelements, const int32_t* __restrict__ eleme
     cp_async_commit();
   };
   if constexpr (PFG) stage(0);
-#pragma unroll
+  // a rolled layer loop (ROLL): 8x less code, fewer instruction-cache misses with four CTAs
+  // per SM in different phases
+#pragma unroll(ROLL ? 1 : NQ)
   for (int k = 0; k < NQ; ++k) {
     const int off = k * NQ * NQ;
     dw G00, G01, G02, G11, G12, G22, GwJ = zero;
@@ -1063,7 +1065,7 @@ static int launch_dw_generic(const AxArgs<double, float2>& a, cudaStream_t s) {
 // N = 7 double-word kernel: geometric factors loaded one layer ahead (64^3: 4.36 ms
 // against 4.42 ms). LPG_AX_DW = noprefetch | lean | leanpf are tuning overrides: loads at
 // the top of each layer, and the three-CTA-per-SM kernel without / with the prefetch.
-enum class Dw7 { Prefetch, Plain, Lean, Lean4, LeanPrefetch };
+enum class Dw7 { Prefetch, Plain, Lean, Lean4, Lean4Rolled, LeanPrefetch };
 static Dw7 dw7_variant() {
   static const Dw7 v = [] {
     const char* ev = std::getenv("LPG_AX_DW");
@@ -1072,6 +1074,7 @@ static Dw7 dw7_variant() {
     if (!std::strcmp(ev, "lean")) return Dw7::Lean;
     if (!std::strcmp(ev, "leanpf")) return Dw7::LeanPrefetch;
     if (!std::strcmp(ev, "lean4")) return Dw7::Lean4;
+    if (!std::strcmp(ev, "lean4r")) return Dw7::Lean4Rolled;
     return Dw7::Prefetch;
   }();
   return v;
@@ -1106,6 +1109,12 @@ int ax_hex_dw(const AxArgs<double, float2>& a, cudaStream_t s) {
       case Dw7::Lean4:
         if (mass) ax_hex_dw_lean_kernel<8, false, true, 4><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS);
         else ax_hex_dw_lean_kernel<8, false, false, 4><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS);
+        break;
+      case Dw7::Lean4Rolled:
+        if (mass)
+          ax_hex_dw_lean_kernel<8, false, true, 4, true><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS);
+        else
+          ax_hex_dw_lean_kernel<8, false, false, 4, true><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS);
         break;
       case Dw7::LeanPrefetch:
         if (mass) ax_hex_dw_lean_kernel<8, true, true><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS);
@@ -1282,6 +1291,9 @@ static cudaError_t fp64_occupancy(int* per, bool dw, bool mass, int epb) {
                                                                NQ * NQ * epb, 0);
         case Dw7::Lean4:
           return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per, ax_hex_dw_lean_kernel<8, false, true, 4>,
+                                                               NQ * NQ * epb, 0);
+        case Dw7::Lean4Rolled:
+          return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per, ax_hex_dw_lean_kernel<8, false, true, 4, true>,
                                                                NQ * NQ * epb, 0);
         case Dw7::LeanPrefetch:
           return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per, ax_hex_dw_lean_kernel<8, true, true>,
