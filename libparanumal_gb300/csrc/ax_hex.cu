@@ -149,6 +149,12 @@ __device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
   const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
 }
+// L2 prefetch of `bytes` (a multiple of 16) from global memory; skipped unless the address
+// is 16-byte aligned, as the bulk prefetch requires
+__device__ __forceinline__ void prefetch_l2_bulk(const void* gmem, unsigned bytes) {
+  if (((uintptr_t)gmem & 15u) == 0 && (bytes & 15u) == 0)
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;\n" ::"l"(gmem), "r"(bytes) : "memory");
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
@@ -784,7 +790,7 @@ __device__ __forceinline__ void ld_dw4x2(const dw* src, dw* v) {
 // own geometric factors of layer k+1 into shared memory with cp.async while layer k is
 // computed (double-buffered; no registers held across the layer); MASS = false:
 // lambda == 0 and no lambda field, the mass term and its wJ reads are left out.
-template <int NQ, bool PFG, bool MASS = true, int MINB = 3, bool ROLL = false>
+template <int NQ, bool PFG, bool MASS = true, int MINB = 3, bool ROLL = false, bool L2PF = false>
 __global__ void __launch_bounds__(NQ * NQ * elems_per_block<NQ>(), MINB)
 ax_hex_dw_lean_kernel(const int64_t Nelements, const int32_t* __restrict__ elementList,
                       const int32_t* __restrict__ g2l, const dw* __restrict__ ggeo, const int64_t geoStride,
@@ -823,6 +829,14 @@ ax_hex_dw_lean_kernel(const int64_t Nelements, const int32_t* __restrict__ eleme
   if (!active) e = 0;
 
   const int64_t nodeBase = e * NP + j * NQ + i;
+  // L2PF: one thread per element asks L2 for the element's geometric factors (and wJ) in
+  // one bulk prefetch each, so the per-layer loads of layers 1..N hit L2
+  if constexpr (L2PF) {
+    if (active && i == 0 && jj == 0) {
+      prefetch_l2_bulk(ggeo + e * geoStride, 6 * NP * sizeof(dw));
+      if constexpr (MASS) prefetch_l2_bulk(wJ + e * wJStride, NP * sizeof(dw));
+    }
+  }
   {
     int32_t id[NQ];
 #pragma unroll
@@ -1065,7 +1079,7 @@ static int launch_dw_generic(const AxArgs<double, float2>& a, cudaStream_t s) {
 // N = 7 double-word kernel: geometric factors loaded one layer ahead (64^3: 4.36 ms
 // against 4.42 ms). LPG_AX_DW = noprefetch | lean | leanpf are tuning overrides: loads at
 // the top of each layer, and the three-CTA-per-SM kernel without / with the prefetch.
-enum class Dw7 { Prefetch, Plain, Lean, Lean4, Lean4Rolled, LeanPrefetch };
+enum class Dw7 { Prefetch, Plain, Lean, Lean4, Lean4Rolled, Lean4RolledL2, LeanPrefetch };
 static Dw7 dw7_variant() {
   static const Dw7 v = [] {
     const char* ev = std::getenv("LPG_AX_DW");
@@ -1075,6 +1089,7 @@ static Dw7 dw7_variant() {
     if (!std::strcmp(ev, "leanpf")) return Dw7::LeanPrefetch;
     if (!std::strcmp(ev, "lean4")) return Dw7::Lean4;
     if (!std::strcmp(ev, "lean4r")) return Dw7::Lean4Rolled;
+    if (!std::strcmp(ev, "lean4rl2")) return Dw7::Lean4RolledL2;
     return Dw7::Prefetch;
   }();
   return v;
@@ -1115,6 +1130,13 @@ int ax_hex_dw(const AxArgs<double, float2>& a, cudaStream_t s) {
           ax_hex_dw_lean_kernel<8, false, true, 4, true><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS);
         else
           ax_hex_dw_lean_kernel<8, false, false, 4, true><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS);
+        break;
+      case Dw7::Lean4RolledL2:
+        if (mass)
+          ax_hex_dw_lean_kernel<8, false, true, 4, true, true><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS);
+        else
+          ax_hex_dw_lean_kernel<8, false, false, 4, true, true><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(
+              LPG_DW_ARGS);
         break;
       case Dw7::LeanPrefetch:
         if (mass) ax_hex_dw_lean_kernel<8, true, true><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS);
@@ -1295,6 +1317,9 @@ static cudaError_t fp64_occupancy(int* per, bool dw, bool mass, int epb) {
         case Dw7::Lean4Rolled:
           return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per, ax_hex_dw_lean_kernel<8, false, true, 4, true>,
                                                                NQ * NQ * epb, 0);
+        case Dw7::Lean4RolledL2:
+          return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+              per, ax_hex_dw_lean_kernel<8, false, true, 4, true, true>, NQ * NQ * epb, 0);
         case Dw7::LeanPrefetch:
           return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per, ax_hex_dw_lean_kernel<8, true, true>,
                                                                NQ * NQ * epb, 0);
