@@ -145,10 +145,6 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
   const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
 }
-__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
-}
 // L2 prefetch of `bytes` (a multiple of 16) from global memory; skipped unless the address
 // is 16-byte aligned, as the bulk prefetch requires
 __device__ __forceinline__ void prefetch_l2_bulk(const void* gmem, unsigned bytes) {
@@ -781,17 +777,25 @@ __device__ __forceinline__ void ld_dw4x2(const dw* src, dw* v) {
   }
 }
 
-// The double-word even-odd kernel with fewer registers and instructions, for three CTAs
-// (24 warps) per SM instead of two: each thread's q pencil lives in shared memory (it is
-// only read back by the same thread) instead of registers, the dof indices are re-read
-// from g2l at the end, and intermediate sums skip the renormalisation that their
-// consumers do not need (dw_add_u, dw_acc::raw), sums start from their first product, and
-// the +-1 of the even/odd line values is folded into FMAs. PFG: each thread copies its
-// own geometric factors of layer k+1 into shared memory with cp.async while layer k is
-// computed (double-buffered; no registers held across the layer); MASS = false:
-// lambda == 0 and no lambda field, the mass term and its wJ reads are left out.
-template <int NQ, bool PFG, bool MASS = true, int MINB = 3, bool ROLL = false, bool L2PF = false>
-__global__ void __launch_bounds__(NQ * NQ * elems_per_block<NQ>(), MINB)
+// The N = 7 double-word kernel for four CTAs (32 warps) per SM, against two for the
+// kernel above (64^3: 3.09 ms against 4.36 ms per application):
+// - each thread's q pencil lives in shared memory (only the same thread reads it back),
+//   and layer k's local result replaces its consumed t-derivative slot, so the thread
+//   holds no pencils in registers (64 registers); dof indices are re-read at the end;
+// - intermediate sums skip the renormalisation their consumers do not need (dw_add_u,
+//   dw_acc::raw), sums start from their first product, and the +-1 of the even/odd line
+//   values is folded into FMAs (~660 instructions per node against ~790);
+// - line values and D rows are read from shared memory two double words per 128-bit load;
+// - the layer loop is rolled (8x less code: instruction-cache misses were a stall with
+//   four CTAs in different phases);
+// - one thread per element asks L2 for the element's geometric factors (and wJ) in one
+//   bulk prefetch each, so the per-layer loads of layers 1..N hit L2.
+// Measured and not kept: the next layer's factors staged through shared memory with
+// cp.async (more shared-memory traffic; slower at three CTAs per SM), a register prefetch
+// (does not fit 64 registers). MASS = false: lambda == 0 and no lambda field, the mass term
+// and its wJ reads are left out.
+template <int NQ, bool MASS>
+__global__ void __launch_bounds__(NQ * NQ * elems_per_block<NQ>(), 4)
 ax_hex_dw_lean_kernel(const int64_t Nelements, const int32_t* __restrict__ elementList,
                       const int32_t* __restrict__ g2l, const dw* __restrict__ ggeo, const int64_t geoStride,
                       const dw* __restrict__ wJ, const int64_t wJStride, const double* __restrict__ Dg,
@@ -807,8 +811,6 @@ ax_hex_dw_lean_kernel(const int64_t Nelements, const int32_t* __restrict__ eleme
   // s_q: layer k of the thread's q pencil until layer k reads it, then that layer's
   // t-contraction input G_t . grad q (the same thread writes and reads each slot)
   __shared__ dw s_q[NQ][NT], s_qt[NQ][NT];
-  // PFG: geometric factors (6 + wJ) of two layers, each slot written and read by its thread
-  __shared__ dw s_G[PFG ? 2 : 1][PFG ? 7 : 1][PFG ? NT : 1];
 
   const int i = threadIdx.x, jj = threadIdx.y, el = threadIdx.z;
   const int j = eo_row<NQ>(jj);
@@ -829,13 +831,9 @@ ax_hex_dw_lean_kernel(const int64_t Nelements, const int32_t* __restrict__ eleme
   if (!active) e = 0;
 
   const int64_t nodeBase = e * NP + j * NQ + i;
-  // L2PF: one thread per element asks L2 for the element's geometric factors (and wJ) in
-  // one bulk prefetch each, so the per-layer loads of layers 1..N hit L2
-  if constexpr (L2PF) {
-    if (active && i == 0 && jj == 0) {
-      prefetch_l2_bulk(ggeo + e * geoStride, 6 * NP * sizeof(dw));
-      if constexpr (MASS) prefetch_l2_bulk(wJ + e * wJStride, NP * sizeof(dw));
-    }
+  if (active && i == 0 && jj == 0) {
+    prefetch_l2_bulk(ggeo + e * geoStride, 6 * NP * sizeof(dw));
+    if constexpr (MASS) prefetch_l2_bulk(wJ + e * wJStride, NP * sizeof(dw));
   }
   {
     int32_t id[NQ];
@@ -884,29 +882,14 @@ ax_hex_dw_lean_kernel(const int64_t Nelements, const int32_t* __restrict__ eleme
 
   const dw zero{0.f, 0.f};
   // the local result of layer k goes to s_qt[k] once layer k has read its t-derivative
-  auto stage = [&](const int k) {
-    if (active) {
-#pragma unroll
-      for (int c = 0; c < 6; ++c) cp_async8(&s_G[k & 1][c][tid], gp + c * NP + k * NQ * NQ);
-      if constexpr (MASS) cp_async8(&s_G[k & 1][6][tid], wp + k * NQ * NQ);
-    }
-    cp_async_commit();
-  };
-  if constexpr (PFG) stage(0);
-  // a rolled layer loop (ROLL): 8x less code, fewer instruction-cache misses with four CTAs
-  // per SM in different phases
-#pragma unroll(ROLL ? 1 : NQ)
+#pragma unroll 1
   for (int k = 0; k < NQ; ++k) {
     const int off = k * NQ * NQ;
-    dw G00, G01, G02, G11, G12, G22, GwJ = zero;
-    if constexpr (PFG) {
-      if (k + 1 < NQ) stage(k + 1);
-    } else {
-      G00 = active ? gp[0 * NP + off] : zero; G01 = active ? gp[1 * NP + off] : zero;
-      G02 = active ? gp[2 * NP + off] : zero; G11 = active ? gp[3 * NP + off] : zero;
-      G12 = active ? gp[4 * NP + off] : zero; G22 = active ? gp[5 * NP + off] : zero;
-      if constexpr (MASS) GwJ = active ? wp[off] : zero;
-    }
+    const dw G00 = active ? gp[0 * NP + off] : zero, G01 = active ? gp[1 * NP + off] : zero;
+    const dw G02 = active ? gp[2 * NP + off] : zero, G11 = active ? gp[3 * NP + off] : zero;
+    const dw G12 = active ? gp[4 * NP + off] : zero, G22 = active ? gp[5 * NP + off] : zero;
+    dw GwJ = zero;
+    if constexpr (MASS) GwJ = active ? wp[off] : zero;
     const dw v = s_q[k][tid];
     const dw pr = dw_shfl_xor(v, NQ - 1), ps = dw_shfl_xor(v, 2 * NQ);
     s_R[el][j][slotR] = dw_add_sign_u(pr, sgnR, v);
@@ -929,15 +912,6 @@ ax_hex_dw_lean_kernel(const int64_t Nelements, const int32_t* __restrict__ eleme
     }
     eo_sync<NQ>(el);
     const dw qr = s_dr[el][j][i], qs = s_ds[el][j][i], qtk = s_qt[k][tid];
-    if constexpr (PFG) {
-      if (k + 1 < NQ) cp_async_wait<1>();
-      else cp_async_wait<0>();
-      const int b = k & 1;
-      G00 = active ? s_G[b][0][tid] : zero; G01 = active ? s_G[b][1][tid] : zero;
-      G02 = active ? s_G[b][2][tid] : zero; G11 = active ? s_G[b][3][tid] : zero;
-      G12 = active ? s_G[b][4][tid] : zero; G22 = active ? s_G[b][5][tid] : zero;
-      if constexpr (MASS) GwJ = active ? s_G[b][6][tid] : zero;
-    }
     dw_acc ar(G00, qr), as(G01, qr), at(G02, qr);
     ar.mac(G01, qs); ar.mac(G02, qtk);
     as.mac(G11, qs); as.mac(G12, qtk);
@@ -1076,21 +1050,12 @@ static int launch_dw_generic(const AxArgs<double, float2>& a, cudaStream_t s) {
   return LPG_OK;
 }
 
-// N = 7 double-word kernel: geometric factors loaded one layer ahead (64^3: 4.36 ms
-// against 4.42 ms). LPG_AX_DW = noprefetch | lean | leanpf are tuning overrides: loads at
-// the top of each layer, and the three-CTA-per-SM kernel without / with the prefetch.
-enum class Dw7 { Prefetch, Plain, Lean, Lean4, Lean4Rolled, Lean4RolledL2, LeanPrefetch };
-static Dw7 dw7_variant() {
-  static const Dw7 v = [] {
+// N = 7 double-word kernel: the four-CTA kernel (ax_hex_dw_lean_kernel). LPG_AX_DW =
+// classic is a tuning override back to the two-CTA kernel with the register prefetch.
+static bool dw7_classic() {
+  static const bool v = [] {
     const char* ev = std::getenv("LPG_AX_DW");
-    if (!ev) return Dw7::Prefetch;
-    if (!std::strcmp(ev, "noprefetch")) return Dw7::Plain;
-    if (!std::strcmp(ev, "lean")) return Dw7::Lean;
-    if (!std::strcmp(ev, "leanpf")) return Dw7::LeanPrefetch;
-    if (!std::strcmp(ev, "lean4")) return Dw7::Lean4;
-    if (!std::strcmp(ev, "lean4r")) return Dw7::Lean4Rolled;
-    if (!std::strcmp(ev, "lean4rl2")) return Dw7::Lean4RolledL2;
-    return Dw7::Prefetch;
+    return ev && !std::strcmp(ev, "classic");
   }();
   return v;
 }
@@ -1114,35 +1079,12 @@ int ax_hex_dw(const AxArgs<double, float2>& a, cudaStream_t s) {
 #define LPG_DW_ARGS                                                                                   \
   a.Nelements, a.elementList, a.g2l, reinterpret_cast<const dw*>(a.ggeo), a.geoStride,               \
       reinterpret_cast<const dw*>(a.wJ), a.wJStride, a.D, a.lambda, a.lambdaE, a.q, a.out
-    switch (dw7_variant()) {
-      case Dw7::Prefetch: ax_hex_dw_kernel<8, true><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS); break;
-      case Dw7::Plain: ax_hex_dw_kernel<8><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS); break;
-      case Dw7::Lean:
-        if (mass) ax_hex_dw_lean_kernel<8, false, true><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS);
-        else ax_hex_dw_lean_kernel<8, false, false><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS);
-        break;
-      case Dw7::Lean4:
-        if (mass) ax_hex_dw_lean_kernel<8, false, true, 4><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS);
-        else ax_hex_dw_lean_kernel<8, false, false, 4><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS);
-        break;
-      case Dw7::Lean4Rolled:
-        if (mass)
-          ax_hex_dw_lean_kernel<8, false, true, 4, true><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS);
-        else
-          ax_hex_dw_lean_kernel<8, false, false, 4, true><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS);
-        break;
-      case Dw7::Lean4RolledL2:
-        if (mass)
-          ax_hex_dw_lean_kernel<8, false, true, 4, true, true><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS);
-        else
-          ax_hex_dw_lean_kernel<8, false, false, 4, true, true><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(
-              LPG_DW_ARGS);
-        break;
-      case Dw7::LeanPrefetch:
-        if (mass) ax_hex_dw_lean_kernel<8, true, true><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS);
-        else ax_hex_dw_lean_kernel<8, true, false><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS);
-        break;
-    }
+    if (dw7_classic())
+      ax_hex_dw_kernel<8, true><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS);
+    else if (mass)
+      ax_hex_dw_lean_kernel<8, true><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS);
+    else
+      ax_hex_dw_lean_kernel<8, false><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS);
 #undef LPG_DW_ARGS
   } else {
     const int64_t blocks = (a.Nelements + 15) / 16;
@@ -1303,29 +1245,13 @@ template <int NQ>
 static cudaError_t fp64_occupancy(int* per, bool dw, bool mass, int epb) {
   if (dw) {
     if constexpr (NQ == 8) {
-      switch (dw7_variant()) {
-        case Dw7::Prefetch:
-          return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per, ax_hex_dw_kernel<8, true>, NQ * NQ * epb, 0);
-        case Dw7::Plain:
-          return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per, ax_hex_dw_kernel<8>, NQ * NQ * epb, 0);
-        case Dw7::Lean:
-          return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per, ax_hex_dw_lean_kernel<8, false, true>,
-                                                               NQ * NQ * epb, 0);
-        case Dw7::Lean4:
-          return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per, ax_hex_dw_lean_kernel<8, false, true, 4>,
-                                                               NQ * NQ * epb, 0);
-        case Dw7::Lean4Rolled:
-          return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per, ax_hex_dw_lean_kernel<8, false, true, 4, true>,
-                                                               NQ * NQ * epb, 0);
-        case Dw7::Lean4RolledL2:
-          return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-              per, ax_hex_dw_lean_kernel<8, false, true, 4, true, true>, NQ * NQ * epb, 0);
-        case Dw7::LeanPrefetch:
-          return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per, ax_hex_dw_lean_kernel<8, true, true>,
-                                                               NQ * NQ * epb, 0);
-      }
+      return dw7_classic()
+                 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(per, ax_hex_dw_kernel<8, true>, NQ * NQ * epb, 0)
+                 : cudaOccupancyMaxActiveBlocksPerMultiprocessor(per, ax_hex_dw_lean_kernel<8, true>, NQ * NQ * epb,
+                                                                 0);
+    } else {
+      return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per, ax_hex_dw_kernel<NQ>, NQ * NQ * epb, 0);
     }
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per, ax_hex_dw_kernel<NQ>, NQ * NQ * epb, 0);
   }
   if (fp64_direct_override())
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
