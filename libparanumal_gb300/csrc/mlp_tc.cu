@@ -20,6 +20,8 @@
 #include <cudaTypedefs.h>
 
 #include <atomic>
+#include <cstdlib>
+#include <cstring>
 #include <mutex>
 
 #include "lpg_common.cuh"
@@ -356,6 +358,228 @@ mlp_tc_kernel(const __grid_constant__ TcMaps maps, const float* __restrict__ b0,
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512) : "memory");
 }
 
+// ---------------------------------------------------------------- two tiles in flight
+// The same network with two 128-row tiles per CTA in flight ("slots" 0 and 1, tiles
+// alternating): slot s accumulates in TMEM columns [256 s, 256 s + 256) and keeps its
+// hidden activations in its own shared-memory buffer, so one slot's epilogue (TMEM ->
+// bias, GELU, BF16 -> shared memory, or the FP32 output) runs while the tensor cores work
+// on the other slot. Work per tile is five jobs: layers 0, 1, 2 and the two 256-column
+// halves of the output layer; the MMA warp issues them slot 0, slot 1, slot 0, ... per
+// job kind, and each job waits until its slot's epilogue has drained the previous job
+// (which also means that job's activations are in place). The TMA producer streams the
+// K blocks of the same job sequence through a 2-stage ring (2 x 48 KB; the two 64 KB
+// activation buffers take the rest of shared memory). Epilogue warps: 4 x EPI2_G per
+// slot; warp w reads TMEM lanes 32 (w % 4) .. +31 and 256 / EPI2_G of the columns.
+constexpr int NSTAGE2 = 2;
+constexpr int EPI2_G = 2;
+constexpr int EPI2_WARPS = 2 * 4 * EPI2_G;
+constexpr int THREADS2 = 32 * (2 + EPI2_WARPS);
+constexpr int NBAR2 = 2 * NSTAGE2 + 4 + 2;     // full[], empty[], accFull[2], epiDone[2], drain, hold
+constexpr int SMEM2_BYTES = 1024 + NSTAGE2 * STAGE_BYTES + 2 * H_BYTES + NBAR2 * 8 + 16;
+static_assert(SMEM2_BYTES <= 232448 - 64, "two-slot MLP kernel: shared memory");
+constexpr int JOBS = 5;                        // L0, L1, L2, L3 columns 0-255, L3 columns 256-511
+
+__global__ void __launch_bounds__(THREADS2, 1)
+mlp_tc2_kernel(const __grid_constant__ TcMaps maps, const float* __restrict__ b0, const float* __restrict__ b1,
+               const float* __restrict__ b2, const float* __restrict__ b3, float* __restrict__ Y, const int64_t rows,
+               const int ntiles, int* __restrict__ err, const unsigned long long holdNs) {
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+  unsigned char* stage0 = smem;
+  unsigned char* hbuf0 = smem + NSTAGE2 * STAGE_BYTES;             // slot 0 activations, slot 1 after
+  uint64_t* bars = reinterpret_cast<uint64_t*>(hbuf0 + 2 * H_BYTES);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + NBAR2);
+  __shared__ volatile int s_abort;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  auto full = [&](int s) { return smem_u32(&bars[s]); };
+  auto empty = [&](int s) { return smem_u32(&bars[NSTAGE2 + s]); };
+  auto accFull = [&](int sl) { return smem_u32(&bars[2 * NSTAGE2 + sl]); };
+  auto epiDone = [&](int sl) { return smem_u32(&bars[2 * NSTAGE2 + 2 + sl]); };
+  const uint32_t drainBar = smem_u32(&bars[2 * NSTAGE2 + 4]), holdBar = smem_u32(&bars[2 * NSTAGE2 + 5]);
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < NSTAGE2; ++s) {
+      mbar_init(full(s), 1);
+      mbar_init(empty(s), 1);
+    }
+    for (int sl = 0; sl < 2; ++sl) {
+      mbar_init(accFull(sl), 1);
+      mbar_init(epiDone(sl), 32 * 4 * EPI2_G);
+    }
+    mbar_init(drainBar, 1);
+    mbar_init(holdBar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    s_abort = 0;
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(512)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  auto fail = [&](int code) {
+    s_abort = 1;
+    atomicCAS(err, 0, code);
+  };
+  if (holdNs) {
+    if (threadIdx.x == 0 && !mbar_wait(holdBar, 0, holdNs)) fail(8);
+    __syncthreads();
+  }
+  constexpr unsigned FULLMASK = 0xffffffffu;
+  auto wait0 = [&](uint32_t bar, uint32_t parity) {
+    int ok = 1;
+    if (lane == 0) ok = mbar_wait(bar, parity) ? 1 : 0;
+    return __shfl_sync(FULLMASK, ok, 0) != 0;
+  };
+  auto aborted = [&]() { return __shfl_sync(FULLMASK, lane == 0 ? (int)s_abort : 0, 0) != 0; };
+  auto waitAll = [&](uint32_t bar, uint32_t parity) { return __all_sync(FULLMASK, mbar_wait(bar, parity) ? 1 : 0) != 0; };
+  // the CTA's tiles: j-th tile blockIdx.x + j gridDim.x, slot j & 1; pairs p = j / 2
+  const int npairs = (ntiles - (int)blockIdx.x + 2 * (int)gridDim.x - 1) / (2 * (int)gridDim.x);
+  auto tile_of = [&](int p, int sl) { return (int)blockIdx.x + (2 * p + sl) * (int)gridDim.x; };
+  auto job_steps = [](int job) { return job == 0 ? L0_STEPS : LH_STEPS; };
+
+  if (warp == 0) {
+    // ------------------------------------------------------------ TMA producer (lane 0 issues)
+    int64_t step = 0;
+    bool stop = false;
+    for (int p = 0; p < npairs && !stop && !aborted(); ++p)
+      for (int job = 0; job < JOBS && !stop; ++job)
+        for (int sl = 0; sl < 2 && !stop; ++sl) {
+          const int tile = tile_of(p, sl);
+          if (tile >= ntiles) continue;
+          for (int st = 0; st < job_steps(job); ++st, ++step) {
+            const int s = (int)(step % NSTAGE2);
+            if (!wait0(empty(s), (uint32_t)(((step / NSTAGE2) & 1) ^ 1))) {
+              if (lane == 0) fail(1);
+              stop = true;
+              break;
+            }
+            if (lane == 0) {
+              const uint32_t a = smem_u32(stage0 + s * STAGE_BYTES), b = a + A_BYTES;
+              if (job == 0) {
+                mbar_expect_tx(full(s), A_BYTES + B_BYTES);
+                tma_load_2d(a, &maps.x, full(s), st * TK, tile * TM);
+                tma_load_2d(b, &maps.w[0], full(s), st * TK, 0);
+              } else {
+                const int layer = job < 3 ? job : 3, nh = job == 4 ? 1 : 0;
+                mbar_expect_tx(full(s), B_BYTES);
+                tma_load_2d(b, &maps.w[layer], full(s), st * TK, nh * 256);
+              }
+            }
+            __syncwarp();
+          }
+        }
+    for (int64_t k = (step > NSTAGE2 ? step - NSTAGE2 : 0); k < step; ++k)
+      if (!wait0(full((int)(k % NSTAGE2)), (uint32_t)((k / NSTAGE2) & 1)) && lane == 0) fail(2);
+  } else if (warp == 1) {
+    // ------------------------------------------------------------ MMA issuer (lane 0 issues)
+    int64_t step = 0;
+    uint32_t njob[2] = {0u, 0u};
+    bool stop = false;
+    for (int p = 0; p < npairs && !stop && !aborted(); ++p)
+      for (int job = 0; job < JOBS && !stop; ++job)
+        for (int sl = 0; sl < 2 && !stop; ++sl) {
+          if (tile_of(p, sl) >= ntiles) continue;
+          // the slot's epilogue has drained its previous job (TMEM free, activations written)
+          if (njob[sl] > 0 && !wait0(epiDone(sl), (njob[sl] - 1) & 1)) { if (lane == 0) fail(4); stop = true; break; }
+          if (aborted()) { stop = true; break; }
+          tc_fence_after();
+          const uint32_t hAddr = smem_u32(hbuf0 + sl * H_BYTES);
+          for (int st = 0; st < job_steps(job); ++st, ++step) {
+            const int s = (int)(step % NSTAGE2);
+            if (!wait0(full(s), (uint32_t)((step / NSTAGE2) & 1))) { if (lane == 0) fail(5); stop = true; break; }
+            tc_fence_after();
+            if (lane == 0) {
+              const uint32_t bAddr = smem_u32(stage0 + s * STAGE_BYTES) + A_BYTES;
+              const uint32_t aAddr = job == 0 ? smem_u32(stage0 + s * STAGE_BYTES) : hAddr + st * (TM * TK * 2);
+#pragma unroll
+              for (int kk = 0; kk < TK / 16; ++kk)
+                umma_bf16(tmem + 256u * (uint32_t)sl, sw128_desc(aAddr + kk * 32), sw128_desc(bAddr + kk * 32),
+                          (st > 0 || kk > 0) ? 1u : 0u);
+              umma_commit(empty(s));
+            }
+            __syncwarp();
+          }
+          if (stop) break;
+          if (lane == 0) umma_commit(accFull(sl));
+          __syncwarp();
+          ++njob[sl];
+        }
+    if (lane == 0) umma_commit(drainBar);
+    __syncwarp();
+    if (!wait0(drainBar, 0) && lane == 0) fail(6);
+  } else {
+    // ------------------------------------------------------------ epilogue (4 x EPI2_G warps per slot)
+    const int u = warp - 2;
+    const int sl = u / (4 * EPI2_G);
+    const int g = (u % (4 * EPI2_G)) / 4;          // column group
+    const int q = warp & 3;                         // TMEM lane quarter this warp may read
+    const int rloc = 32 * q + lane;
+    const uint32_t tlane = tmem + ((uint32_t)(32 * q) << 16) + 256u * (uint32_t)sl;
+    unsigned char* hb = hbuf0 + sl * H_BYTES;
+    constexpr int CW = 256 / EPI2_G;                // columns per warp
+    uint32_t n = 0;
+    bool stop = false;
+    for (int p = 0; p < npairs && !stop && !aborted(); ++p) {
+      const int tile = tile_of(p, sl);
+      if (tile >= ntiles) break;
+      const int64_t row = (int64_t)tile * TM + rloc;
+      for (int job = 0; job < JOBS; ++job) {
+        if (!waitAll(accFull(sl), n++ & 1)) { if (lane == 0) fail(7); stop = true; break; }
+        tc_fence_after();
+        float v[32];
+        if (job < 3) {
+          const float* bias = job == 0 ? b0 : job == 1 ? b1 : b2;
+          for (int c0 = g * CW; c0 < (g + 1) * CW; c0 += 32) {
+            tmem_ld32(tlane + c0, v);
+            unsigned char* rowp = hb + (c0 / TK) * (TM * TK * 2) + rloc * 128;
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+              const int chunk = ((c0 % TK) / 8 + t) ^ (rloc & 7);
+              const float4 bl = __ldg(reinterpret_cast<const float4*>(bias + c0 + 8 * t));
+              const float4 bh = __ldg(reinterpret_cast<const float4*>(bias + c0 + 8 * t + 4));
+              uint4 w;
+              w.x = pack_bf16(gelu_approx(v[8 * t + 0] + bl.x), gelu_approx(v[8 * t + 1] + bl.y));
+              w.y = pack_bf16(gelu_approx(v[8 * t + 2] + bl.z), gelu_approx(v[8 * t + 3] + bl.w));
+              w.z = pack_bf16(gelu_approx(v[8 * t + 4] + bh.x), gelu_approx(v[8 * t + 5] + bh.y));
+              w.w = pack_bf16(gelu_approx(v[8 * t + 6] + bh.z), gelu_approx(v[8 * t + 7] + bh.w));
+              *reinterpret_cast<uint4*>(rowp + chunk * 16) = w;
+            }
+          }
+          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        } else {
+          const int cbase = 256 * (job - 3);
+          for (int c0 = g * CW; c0 < (g + 1) * CW; c0 += 32) {
+            tmem_ld32(tlane + c0, v);
+            if (row < rows) {
+              float4* dst = reinterpret_cast<float4*>(Y + row * kMlpOut + cbase + c0);
+#pragma unroll
+              for (int t = 0; t < 8; ++t) {
+                const float4 bb = __ldg(reinterpret_cast<const float4*>(b3 + cbase + c0 + 4 * t));
+                dst[t] = make_float4(v[4 * t] + bb.x, v[4 * t + 1] + bb.y, v[4 * t + 2] + bb.z, v[4 * t + 3] + bb.w);
+              }
+            }
+          }
+        }
+        tc_fence_before();
+        mbar_arrive(epiDone(sl));
+      }
+    }
+  }
+
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 1)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512) : "memory");
+}
+
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
   static std::once_flag once;
@@ -404,11 +628,19 @@ int mlp_forward_tc(int64_t B, const __nv_bfloat16* X, const __nv_bfloat16* const
       (rc = make_map(&maps.w[2], Wt[2], kMlpHidden, kMlpHidden, 256)) ||
       (rc = make_map(&maps.w[3], Wt[3], kMlpHidden, kMlpOut, 256)))
     return rc;
+  if (!al16(bias[0]) || !al16(bias[1]) || !al16(bias[2]) || !al16(bias[3]))
+    return set_error(LPG_ERR_INVALID, "mlp tc: biases must be 16-byte aligned");
+  // LPG_MLP_TC=single (a tuning override): the one-tile-per-CTA kernel
+  static const bool single = [] {
+    const char* e = std::getenv("LPG_MLP_TC");
+    return e && !std::strcmp(e, "single");
+  }();
   static PerDeviceConfig perDevice;   // dynamic shared memory opt-in per device
   KernelConfig cfg;
   rc = perDevice.get(
       [&](int, KernelConfig&) {
         LPG_CUDA_TRY(cudaFuncSetAttribute(mlp_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+        LPG_CUDA_TRY(cudaFuncSetAttribute(mlp_tc2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM2_BYTES));
         return (int)LPG_OK;
       },
       &cfg);
@@ -416,9 +648,16 @@ int mlp_forward_tc(int64_t B, const __nv_bfloat16* X, const __nv_bfloat16* const
   const int ntiles = (int)((B + TM - 1) / TM);
   const int grid = ntiles < cfg.numSMs ? ntiles : cfg.numSMs;
   LPG_CUDA_TRY(cudaMemsetAsync(errFlag, 0, sizeof(int), s));
-  mlp_tc_kernel<<<grid, THREADS, SMEM_BYTES, s>>>(maps, bias[0], bias[1], bias[2], bias[3], Y, B, ntiles, errFlag,
-                                                  g_holdNs.load(std::memory_order_relaxed));
-  LPG_LAUNCH_CHECK("mlp_tc_kernel");
+  const unsigned long long hold = g_holdNs.load(std::memory_order_relaxed);
+  if (single) {
+    mlp_tc_kernel<<<grid, THREADS, SMEM_BYTES, s>>>(maps, bias[0], bias[1], bias[2], bias[3], Y, B, ntiles, errFlag,
+                                                    hold);
+    LPG_LAUNCH_CHECK("mlp_tc_kernel");
+  } else {
+    mlp_tc2_kernel<<<grid, THREADS2, SMEM2_BYTES, s>>>(maps, bias[0], bias[1], bias[2], bias[3], Y, B, ntiles, errFlag,
+                                                       hold);
+    LPG_LAUNCH_CHECK("mlp_tc2_kernel");
+  }
   return LPG_OK;
 }
 

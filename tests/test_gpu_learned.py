@@ -69,7 +69,9 @@ def test_adam_step_matches_restatement():
     assert rel_err(V.cpu().numpy(), vr) < 1e-6
 
 
-@pytest.mark.parametrize("B", [1, 130, 1000])
+# 39,559 rows = 310 tiles of 128 on 152 CTAs: every CTA runs a pair of tiles (both slots of
+# the two-tile kernel) and six of them a third tile alone, the last one partial
+@pytest.mark.parametrize("B", [1, 130, 1000, 39559])
 def test_bf16_tensor_core_inference_matches_fp32(B):
     L = lpg.lib()
     rng = np.random.default_rng(B)
@@ -81,6 +83,47 @@ def test_bf16_tensor_core_inference_matches_fp32(B):
     torch.cuda.synchronize()
     yref, _ = mlp.forward(theta.astype(np.float64), X.astype(np.float64))
     assert rel_err(Y.cpu().numpy(), yref) < 3e-2
+
+
+_MLP_CHILD = r"""
+import sys
+import numpy as np
+import torch
+import libparanumal_gb300 as lpg
+from oracle import mlp
+B = int(sys.argv[1])
+rng = np.random.default_rng(B)
+theta = torch.tensor(mlp.glorot(5).astype(np.float32), device="cuda")
+X = torch.tensor(rng.standard_normal((B, 896)).astype(np.float32), device="cuda")
+Y = torch.zeros((B, 512), dtype=torch.float32, device="cuda")
+lpg.check(lpg.lib().lpg_mlp_forward_bf16(theta.data_ptr(), B, X.data_ptr(), Y.data_ptr(), None))
+torch.cuda.synchronize()
+np.save(sys.argv[2], Y.cpu().numpy())
+"""
+
+
+@pytest.mark.parametrize("B", [130, 39559])
+def test_two_tile_mlp_kernel_equals_one_tile_kernel(tmp_path, B):
+    """The tensor-core MLP with two tiles in flight per CTA (the default) against the
+    one-tile kernel (LPG_MLP_TC=single): the same MMAs in the same K order and the same
+    epilogue arithmetic, so the outputs are bit for bit equal."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = {}
+    for mode in ("two", "single"):
+        env = dict(os.environ, PYTHONPATH=root)
+        env.pop("LPG_MLP_TC", None)
+        if mode == "single":
+            env["LPG_MLP_TC"] = "single"
+        f = tmp_path / (mode + ".npy")
+        p = subprocess.run([sys.executable, "-c", _MLP_CHILD, str(B), str(f)], env=env, cwd=root,
+                           capture_output=True, text=True, timeout=600)
+        assert p.returncode == 0, p.stderr[-2000:]
+        out[mode] = np.load(f)
+    assert np.all(np.isfinite(out["two"]))
+    assert np.array_equal(out["two"], out["single"])
 
 
 def learned_problem(nx, **over):
