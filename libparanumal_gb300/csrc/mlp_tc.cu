@@ -91,12 +91,6 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map
       : "memory");
 }
 
-// L2 prefetch of one box of a tiled tensor map (no shared memory, no completion)
-__device__ __forceinline__ void tma_prefetch_2d(const CUtensorMap* map, int x, int y) {
-  asm volatile("cp.async.bulk.prefetch.tensor.2d.L2.global.tile [%0, {%1, %2}];" ::"l"((uint64_t)map), "r"(x), "r"(y)
-               : "memory");
-}
-
 // shared-memory matrix descriptor: K-major operand in 128-byte swizzled rows, 8-row
 // groups 1024 bytes apart (stride byte offset), descriptor version 1 (bit 46)
 __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
@@ -385,7 +379,6 @@ constexpr int SMEM2_BYTES = 1024 + NSTAGE2 * STAGE_BYTES + 2 * H_BYTES + NBAR2 *
 static_assert(SMEM2_BYTES <= 232448 - 64, "two-slot MLP kernel: shared memory");
 constexpr int JOBS = 5;                        // L0, L1, L2, L3 columns 0-255, L3 columns 256-511
 
-template <bool PFX>
 __global__ void __launch_bounds__(THREADS2, 1)
 mlp_tc2_kernel(const __grid_constant__ TcMaps maps, const float* __restrict__ b0, const float* __restrict__ b1,
                const float* __restrict__ b2, const float* __restrict__ b3, float* __restrict__ Y, const int64_t rows,
@@ -460,14 +453,6 @@ mlp_tc2_kernel(const __grid_constant__ TcMaps maps, const float* __restrict__ b0
         for (int sl = 0; sl < 2 && !stop; ++sl) {
           const int tile = tile_of(p, sl);
           if (tile >= ntiles) continue;
-          // the next pair's input rows go to L2 while this pair's last layers run, so layer
-          // 0's K blocks of the next pair arrive at L2 latency instead of DRAM latency
-          if (PFX && job == 2 && sl == 0 && lane == 0)
-            for (int ns = 0; ns < 2; ++ns) {
-              const int nt = tile_of(p + 1, ns);
-              if (nt < ntiles && (int64_t)(nt + 1) * TM <= rows)   // whole tiles only
-                for (int kb = 0; kb < L0_STEPS; ++kb) tma_prefetch_2d(&maps.x, kb * TK, nt * TM);
-            }
           for (int st = 0; st < job_steps(job); ++st, ++step) {
             const int s = (int)(step % NSTAGE2);
             if (!wait0(empty(s), (uint32_t)(((step / NSTAGE2) & 1) ^ 1))) {
@@ -650,20 +635,12 @@ int mlp_forward_tc(int64_t B, const __nv_bfloat16* X, const __nv_bfloat16* const
     const char* e = std::getenv("LPG_MLP_TC");
     return e && !std::strcmp(e, "single");
   }();
-  // LPG_MLP_TC=nopfx: the two-tile kernel without the L2 prefetch of the next input rows
-  static const bool nopfx = [] {
-    const char* e = std::getenv("LPG_MLP_TC");
-    return e && !std::strcmp(e, "nopfx");
-  }();
   static PerDeviceConfig perDevice;   // dynamic shared memory opt-in per device
   KernelConfig cfg;
   rc = perDevice.get(
       [&](int, KernelConfig&) {
         LPG_CUDA_TRY(cudaFuncSetAttribute(mlp_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-        LPG_CUDA_TRY(
-            cudaFuncSetAttribute(mlp_tc2_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM2_BYTES));
-        LPG_CUDA_TRY(
-            cudaFuncSetAttribute(mlp_tc2_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM2_BYTES));
+        LPG_CUDA_TRY(cudaFuncSetAttribute(mlp_tc2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM2_BYTES));
         return (int)LPG_OK;
       },
       &cfg);
@@ -676,13 +653,9 @@ int mlp_forward_tc(int64_t B, const __nv_bfloat16* X, const __nv_bfloat16* const
     mlp_tc_kernel<<<grid, THREADS, SMEM_BYTES, s>>>(maps, bias[0], bias[1], bias[2], bias[3], Y, B, ntiles, errFlag,
                                                     hold);
     LPG_LAUNCH_CHECK("mlp_tc_kernel");
-  } else if (nopfx) {
-    mlp_tc2_kernel<false><<<grid, THREADS2, SMEM2_BYTES, s>>>(maps, bias[0], bias[1], bias[2], bias[3], Y, B, ntiles,
-                                                              errFlag, hold);
-    LPG_LAUNCH_CHECK("mlp_tc2_kernel");
   } else {
-    mlp_tc2_kernel<true><<<grid, THREADS2, SMEM2_BYTES, s>>>(maps, bias[0], bias[1], bias[2], bias[3], Y, B, ntiles,
-                                                             errFlag, hold);
+    mlp_tc2_kernel<<<grid, THREADS2, SMEM2_BYTES, s>>>(maps, bias[0], bias[1], bias[2], bias[3], Y, B, ntiles, errFlag,
+                                                       hold);
     LPG_LAUNCH_CHECK("mlp_tc2_kernel");
   }
   return LPG_OK;
