@@ -57,7 +57,7 @@ def test_repeated_solves_agree(prec):
     runs = []
     for _ in range(3):
         x = torch.zeros_like(r)
-        it = e.Solve(x, r, tol=1e-10)
+        it = e.Solve(x, r.clone(), tol=1e-10)   # the solve overwrites its right-hand side
         runs.append((it, x.cpu().numpy()))
     for it, x in runs[1:]:
         assert it == runs[0][0]
