@@ -414,253 +414,6 @@ __device__ __forceinline__ void eo_sync(const int el) {
   else __syncwarp();                                    // Nq = 4: an element is half a warp
 }
 
-// ---------------------------------------------------------------- FP32 even-odd staged
-// The staged FP32 / BF16-geometry kernel (N = 7) with the even-odd contractions of the
-// FP64 kernel below: the same persistent element groups, cp.async ring of geometric-factor
-// and index rows and half-way gather of the next group's q (PF), but the r and s
-// derivatives of a layer as "pair tasks" (threads i < 4 take the pair (i, 7-i) of their
-// row, the others the pair of their column, from even/odd line values that partners
-// exchange by warp shuffles) and the t-direction on the register pencil by even/odd
-// halves: 35 FMA per node instead of 59, and 4 instead of 8 128-bit row loads per node
-// and layer. BF16 geometry leaves this kernel issue- and shared-memory-bound, so the
-// operation count sets its time.
-// barrier of element el's two warps (el = 0, 1) with an immediate barrier id, so that the
-// kernel uses 3 of the SM's named barriers and barriers do not limit the CTAs per SM
-__device__ __forceinline__ void sync_el2(const int el) {
-  if (el == 0) asm volatile("bar.sync 1, 64;\n" ::: "memory");
-  else asm volatile("bar.sync 2, 64;\n" ::: "memory");
-}
-
-template <typename G, bool PF, bool MASS>
-__global__ void __launch_bounds__(128)
-ax_hex_staged_eo_kernel(const int64_t Nelements, const int32_t* __restrict__ elementList,
-                        const int32_t* __restrict__ g2l, const G* __restrict__ ggeo, const int64_t geoStride,
-                        const G* __restrict__ wJ, const int64_t wJStride, const float* __restrict__ Dg,
-                        const float lambda, const float* __restrict__ lambdaE, const float* __restrict__ q,
-                        float* __restrict__ out, const float outScale) {
-  constexpr int NQ = 8, H = 4, N = 7, EPB = 2, STAGES = 2;
-  using L = StagedLayout<NQ, G>;
-  constexpr int NP = L::NP, NT = NQ * NQ * EPB;
-  constexpr int STAGE_BYTES = EPB * L::ELEM_BYTES;
-  constexpr unsigned FULL = 0xffffffffu;
-  extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ __align__(16) float s_Dp[H][H], s_Dm[H][H], s_Tp[H][H], s_Tm[H][H];
-  __shared__ __align__(16) float s_R[EPB][NQ][NQ], s_S[EPB][NQ][NQ];   // even/odd lines
-  __shared__ float s_dr[EPB][NQ][NQ], s_ds[EPB][NQ][NQ];              // [j][i] derivatives
-
-  const int i = threadIdx.x, jj = threadIdx.y, el = threadIdx.z;
-  const int j = eo_row<NQ>(jj);
-  const int tid = i + NQ * (jj + NQ * el);
-  for (int t = tid; t < H * H; t += NT) {
-    const int a = t / H, m = t % H;
-    const float d0 = Dg[a * NQ + m], d1 = Dg[a * NQ + N - m];
-    const float t0 = Dg[m * NQ + a], t1 = Dg[(N - m) * NQ + a];
-    s_Dp[a][m] = 0.5f * (d0 + d1);
-    s_Dm[a][m] = 0.5f * (d0 - d1);
-    s_Tp[a][m] = 0.5f * (t0 + t1);
-    s_Tm[a][m] = 0.5f * (t0 - t1);
-  }
-  const int64_t ngroups = (Nelements + EPB - 1) / EPB;
-
-  constexpr int ROW_CHUNKS = L::ROW_BYTES / 16, IDX_CHUNKS = L::IDX_BYTES / 16;
-  auto issue = [&](const int64_t grp, const int stage) {
-    if (grp < ngroups) {
-      unsigned char* base = smem + stage * STAGE_BYTES;
-#pragma unroll
-      for (int le = 0; le < EPB; ++le) {
-        const int64_t ei = grp * EPB + le;
-        if (ei < Nelements) {
-          const int64_t e = elementList ? (int64_t)elementList[ei] : ei;
-          unsigned char* dst = base + le * L::ELEM_BYTES;
-#pragma unroll
-          for (int comp = 0; comp < (MASS ? 7 : 6); ++comp) {
-            const unsigned char* src =
-                (comp < 6) ? reinterpret_cast<const unsigned char*>(ggeo + e * geoStride + (int64_t)comp * NP)
-                           : reinterpret_cast<const unsigned char*>(wJ + e * wJStride);
-            for (int c = tid; c < ROW_CHUNKS; c += NT) cp_async16(dst + comp * L::ROW_BYTES + c * 16, src + c * 16);
-          }
-          const unsigned char* srci = reinterpret_cast<const unsigned char*>(g2l + e * NP);
-          for (int c = tid; c < IDX_CHUNKS; c += NT) cp_async16(dst + L::GEO_BYTES + c * 16, srci + c * 16);
-        }
-      }
-    }
-    cp_async_commit();
-  };
-
-  issue(blockIdx.x, 0);
-  __syncthreads();
-
-  // the pair task of this thread and its coefficients (constant over the layers)
-  const bool rtask = i < H;
-  const int pt = rtask ? i : i - H;
-  float* dst0 = rtask ? &s_dr[el][j][pt] : &s_ds[el][pt][j];
-  float* dst1 = rtask ? &s_dr[el][j][N - pt] : &s_ds[el][N - pt][j];
-  const float* line = rtask ? &s_R[el][j][0] : &s_S[el][j][0];
-  const int slotR = (i < H) ? i : H + N - i, slotS = (j < H) ? j : H + N - j;
-  const float sgnR = (i < H) ? 1.f : -1.f, sgnS = (j < H) ? 1.f : -1.f;
-  float cDp[H], cDm[H], cTp[H], cTm[H];
-#pragma unroll
-  for (int m = 0; m < H; ++m) {
-    cDp[m] = s_Dp[pt][m];
-    cDm[m] = s_Dm[pt][m];
-    cTp[m] = s_Tp[pt][m];
-    cTm[m] = s_Tm[pt][m];
-  }
-  // A + B and B - A of one pair task over a line (4 even, 4 odd values)
-  auto pair = [&](const float* cp, const float* cm, float& o0, float& o1) {
-    const float4 e4 = *reinterpret_cast<const float4*>(line);
-    const float4 d4 = *reinterpret_cast<const float4*>(line + H);
-    const float A = cp[0] * e4.x + cp[1] * e4.y + cp[2] * e4.z + cp[3] * e4.w;
-    const float B = cm[0] * d4.x + cm[1] * d4.y + cm[2] * d4.z + cm[3] * d4.w;
-    o0 = A + B;
-    o1 = B - A;
-  };
-
-  const int node = j * NQ + i;
-  float n_q[PF ? NQ : 1];
-  int32_t n_id[PF ? NQ : 1];
-  auto gather_next = [&](const int64_t g, const int stage) {
-    if constexpr (PF) {
-      const int32_t* nidx = reinterpret_cast<const int32_t*>(smem + stage * STAGE_BYTES + el * L::ELEM_BYTES +
-                                                            L::GEO_BYTES);
-      const bool act = (g < ngroups) && (g * EPB + el < Nelements);
-#pragma unroll
-      for (int k = 0; k < NQ; ++k) {
-        const int32_t id = act ? nidx[k * NQ * NQ + node] : -1;
-        n_id[k] = id;
-        n_q[k] = (id >= 0) ? q[id] : 0.f;
-      }
-    }
-  };
-  if constexpr (PF) {
-    cp_async_wait<0>();
-    __syncthreads();
-    gather_next(blockIdx.x, 0);
-  }
-
-  for (int64_t it = 0;; ++it) {
-    const int64_t grp = blockIdx.x + it * gridDim.x;
-    if (grp >= ngroups) break;
-    if constexpr (!PF) cp_async_wait<STAGES - 2>();
-    __syncthreads();
-    issue(grp + (int64_t)(STAGES - 1) * gridDim.x, (int)((it + STAGES - 1) % STAGES));
-    const unsigned char* base = smem + (it % STAGES) * STAGE_BYTES + el * L::ELEM_BYTES;
-    const G* sg = reinterpret_cast<const G*>(base);
-    const int32_t* sidx = reinterpret_cast<const int32_t*>(base + L::GEO_BYTES);
-    const int64_t ei = grp * EPB + el;
-    const bool active = ei < Nelements;
-    const int64_t e = active ? (elementList ? (int64_t)elementList[ei] : ei) : 0;
-
-    float r_q[NQ], r_Aq[NQ], qt[NQ], Gqt[NQ];
-    int32_t r_id[NQ];
-#pragma unroll
-    for (int k = 0; k < NQ; ++k) {
-      if constexpr (PF) {
-        r_id[k] = n_id[k];
-        r_q[k] = n_q[k];
-      } else {
-        const int32_t id = active ? sidx[k * NQ * NQ + node] : -1;
-        r_id[k] = id;
-        r_q[k] = (id >= 0) ? q[id] : 0.f;
-      }
-    }
-    (void)sidx;
-    const float lam = (lambdaE && active) ? lambdaE[e] : lambda;
-    // t-direction of the pencil, even/odd (D rows broadcast from shared memory)
-    {
-      float E[H], O[H];
-#pragma unroll
-      for (int m = 0; m < H; ++m) {
-        E[m] = r_q[m] + r_q[N - m];
-        O[m] = r_q[m] - r_q[N - m];
-      }
-#pragma unroll
-      for (int t = 0; t < H; ++t) {
-        float A = 0.f, B = 0.f;
-#pragma unroll
-        for (int m = 0; m < H; ++m) {
-          A += s_Dp[t][m] * E[m];
-          B += s_Dm[t][m] * O[m];
-        }
-        qt[t] = A + B;
-        qt[N - t] = B - A;
-      }
-    }
-#pragma unroll
-    for (int k = 0; k < NQ; ++k) {
-      const int off = k * NQ * NQ + node;
-      const float G00 = geo_to_float(sg[0 * NP + off]), G01 = geo_to_float(sg[1 * NP + off]);
-      const float G02 = geo_to_float(sg[2 * NP + off]), G11 = geo_to_float(sg[3 * NP + off]);
-      const float G12 = geo_to_float(sg[4 * NP + off]), G22 = geo_to_float(sg[5 * NP + off]);
-      float GwJ = 0.f;
-      if constexpr (MASS) GwJ = geo_to_float(sg[6 * NP + off]);
-      const float v = r_q[k];
-      const float pr = __shfl_xor_sync(FULL, v, NQ - 1), ps = __shfl_xor_sync(FULL, v, 2 * NQ);
-      s_R[el][j][slotR] = fmaf(sgnR, v, pr);
-      s_S[el][i][slotS] = fmaf(sgnS, v, ps);
-      sync_el2(el);
-      {
-        float o0, o1;
-        pair(cDp, cDm, o0, o1);
-        *dst0 = o0;
-        *dst1 = o1;
-      }
-      sync_el2(el);
-      const float qr = s_dr[el][j][i], qs = s_ds[el][j][i];
-      const float Gqr = G00 * qr + G01 * qs + G02 * qt[k];
-      const float Gqs = G01 * qr + G11 * qs + G12 * qt[k];
-      Gqt[k] = G02 * qr + G12 * qs + G22 * qt[k];
-      const float pr2 = __shfl_xor_sync(FULL, Gqr, NQ - 1), ps2 = __shfl_xor_sync(FULL, Gqs, 2 * NQ);
-      s_R[el][j][slotR] = fmaf(sgnR, Gqr, pr2);
-      s_S[el][i][slotS] = fmaf(sgnS, Gqs, ps2);
-      sync_el2(el);
-      {
-        float o0, o1;
-        pair(cTp, cTm, o0, o1);
-        *dst0 = o0;
-        *dst1 = o1;
-      }
-      sync_el2(el);
-      const float sum = s_dr[el][j][i] + s_ds[el][j][i];
-      if constexpr (MASS) r_Aq[k] = fmaf(GwJ * lam, v, sum);
-      else r_Aq[k] = sum;
-      if constexpr (PF) {
-        if (k == NQ / 2) {
-          cp_async_wait<0>();
-          __syncthreads();   // the next group's copy (both elements of the CTA) is visible
-          gather_next(grp + gridDim.x, (int)((it + 1) % STAGES));
-        }
-      }
-    }
-    // transposed t-direction: r_Aq[t] += sum_m D[m][t] Gqt[m], even/odd
-    {
-      float E[H], O[H];
-#pragma unroll
-      for (int m = 0; m < H; ++m) {
-        E[m] = Gqt[m] + Gqt[N - m];
-        O[m] = Gqt[m] - Gqt[N - m];
-      }
-#pragma unroll
-      for (int t = 0; t < H; ++t) {
-        float A = 0.f, B = 0.f;
-#pragma unroll
-        for (int m = 0; m < H; ++m) {
-          A += s_Tp[t][m] * E[m];
-          B += s_Tm[t][m] * O[m];
-        }
-        r_Aq[t] += A + B;
-        r_Aq[N - t] += B - A;
-      }
-    }
-    if (active) {
-#pragma unroll
-      for (int k = 0; k < NQ; ++k)
-        if (r_id[k] >= 0) atomicAdd(out + r_id[k], outScale * r_Aq[k]);
-    }
-  }
-  cp_async_wait<0>();
-}
-
 // MASS = false: lambda == 0 and no lambda field, the mass term and its wJ reads are left out
 template <int NQ, bool MASS = true>
 __global__ void __launch_bounds__(NQ * NQ * elems_per_block<NQ>(), 3)
@@ -1369,31 +1122,6 @@ static int launch_staged(const AxArgs<T, G>& a, cudaStream_t s) {
   return LPG_OK;
 }
 
-template <typename G, bool PF, bool MASS>
-static int launch_staged_eo(const AxArgs<float, G>& a, cudaStream_t s) {
-  using L = StagedLayout<8, G>;
-  constexpr int EPB = 2, smem = 2 * EPB * L::ELEM_BYTES;
-  static PerDeviceConfig perDevice;
-  auto kern = ax_hex_staged_eo_kernel<G, PF, MASS>;
-  KernelConfig cfg;
-  const int rc = perDevice.get(
-      [&](int, KernelConfig& c) {
-        LPG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-        LPG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c.ctasPerSM, kern, 128, smem));
-        if (c.ctasPerSM < 1) return set_error(LPG_ERR_UNSUPPORTED, "staged Ax: kernel does not fit on an SM");
-        return (int)LPG_OK;
-      },
-      &cfg);
-  if (rc) return rc;
-  const int64_t groups = (a.Nelements + EPB - 1) / EPB;
-  const int64_t grid = std::min<int64_t>(groups, (int64_t)cfg.numSMs * cfg.ctasPerSM);
-  if (grid <= 0) return LPG_OK;
-  kern<<<(unsigned)grid, dim3(8, 8, EPB), smem, s>>>(a.Nelements, a.elementList, a.g2l, a.ggeo, a.geoStride, a.wJ,
-                                                     a.wJStride, a.D, a.lambda, a.lambdaE, a.q, a.out, a.outScale);
-  LPG_LAUNCH_CHECK("ax_hex_staged_eo_kernel");
-  return LPG_OK;
-}
-
 static int staged_variant() {
   static int v = -2;
   if (v == -2) {
@@ -1406,9 +1134,6 @@ static int staged_variant() {
       else if (!std::strcmp(e, "4x2")) v = 42;
       else if (!std::strcmp(e, "4x3")) v = 43;
       else if (!std::strcmp(e, "2x2pf")) v = 122;
-      else if (!std::strcmp(e, "direct")) v = 1;
-      else if (!std::strcmp(e, "eonopf")) v = 2;
-      else if (!std::strcmp(e, "eopf")) v = 3;
     }
   }
   return v;
@@ -1445,19 +1170,10 @@ static int launch_ax(const AxArgs<T, G>& a, cudaStream_t s) {
       else if (v == 43) return launch_staged<NQ, T, G, 4, 3>(a, s);
       else if (v == 42) return launch_staged<NQ, T, G, 4, 2>(a, s);
       else if (v == 122) return launch_staged<NQ, T, G, 2, 2, true>(a, s);
-      const bool noMass = (a.lambda == 0 && !a.lambdaE);
-      if constexpr (NQ == 8) {
-        // N = 7: the even-odd staged kernel (LPG_AX_STAGED = direct: the direct-contraction one)
-        if (v != 1) {
-          const bool pf = (v == 3) || (v != 2 && std::is_same<G, float>::value);
-          if (pf)
-            return noMass ? launch_staged_eo<G, true, false>(a, s) : launch_staged_eo<G, true, true>(a, s);
-          return noMass ? launch_staged_eo<G, false, false>(a, s) : launch_staged_eo<G, false, true>(a, s);
-        }
-      }
       // measured best at N=7: FP32 geometry with the next group's q gathered half-way
       // through the current group (0.997 vs 1.112 ms at 64^3); BF16 geometry without it
       // (lambda = 0 without a lambda field: the instantiation without the mass term and wJ copy)
+      const bool noMass = (a.lambda == 0 && !a.lambdaE);
       if constexpr (std::is_same<G, float>::value)
         return noMass ? launch_staged<NQ, T, G, 2, 2, true, false>(a, s) : launch_staged<NQ, T, G, 2, 2, true>(a, s);
       else
