@@ -166,18 +166,6 @@ __device__ __forceinline__ void elem_sync(const int el) {
   }
 }
 
-// element barrier of the staged kernel: for two elements of 64 threads, immediate barrier
-// ids (1, 2), so the kernel uses 3 named barriers and barriers do not cap its CTAs per SM
-template <int NQ, int EPB>
-__device__ __forceinline__ void staged_sync(const int el) {
-  if constexpr (NQ * NQ == 64 && EPB == 2) {
-    if (el == 0) asm volatile("bar.sync 1, 64;\n" ::: "memory");
-    else asm volatile("bar.sync 2, 64;\n" ::: "memory");
-  } else {
-    elem_sync<NQ>(el);
-  }
-}
-
 template <typename G> __device__ __forceinline__ float geo_to_float(G v);
 template <> __device__ __forceinline__ float geo_to_float<float>(float v) { return v; }
 template <> __device__ __forceinline__ float geo_to_float<__nv_bfloat16>(__nv_bfloat16 v) { return __bfloat162float(v); }
@@ -217,15 +205,8 @@ __device__ __forceinline__ float row_dot(const float* __restrict__ row, const fl
 }
 
 // MASS = false: lambda == 0 and no lambda field, the wJ row is neither copied nor used
-// CTAs per SM the register allocation aims at: BF16 geometry (2 elements, 42 KB of shared
-// memory) fits five; FP32 geometry is held to three by its 69 KB of shared memory
-template <typename G, int EPB>
-constexpr int staged_min_blocks() {
-  return (std::is_same<G, __nv_bfloat16>::value && EPB == 2) ? 5 : 1;
-}
-
 template <int NQ, typename T, typename G, int EPB, int STAGES, bool PF = false, bool MASS = true>
-__global__ void __launch_bounds__(NQ * NQ * EPB, staged_min_blocks<G, EPB>())
+__global__ void __launch_bounds__(NQ * NQ * EPB)
 ax_hex_staged_kernel(const int64_t Nelements, const int32_t* __restrict__ elementList,
                      const int32_t* __restrict__ g2l, const G* __restrict__ ggeo, const int64_t geoStride,
                      const G* __restrict__ wJ, const int64_t wJStride, const T* __restrict__ Dg, const T lambda,
@@ -362,7 +343,7 @@ ax_hex_staged_kernel(const int64_t Nelements, const int32_t* __restrict__ elemen
       const int b = k & 1;
       s_q[b][el][j][i] = r_q[k];
       s_qT[b][el][i][j] = r_q[k];
-      staged_sync<NQ, EPB>(el);
+      elem_sync<NQ>(el);
       const float qr = row_dot<NQ, VEC>(&s_q[b][el][j][0], Dr);    // sum_m D[i][m] q(m,j)
       const float qs = row_dot<NQ, VEC>(&s_qT[b][el][i][0], Ds);   // sum_m D[j][m] q(i,m)
       s_GqsT[b][el][i][j] = G01 * qr + G11 * qs + G12 * qt[k];
@@ -370,7 +351,7 @@ ax_hex_staged_kernel(const int64_t Nelements, const int32_t* __restrict__ elemen
       Gqt[k] = G02 * qr + G12 * qs + G22 * qt[k];
       float Auk = 0.f;
       if constexpr (MASS) Auk = GwJ * lam * r_q[k];
-      staged_sync<NQ, EPB>(el);
+      elem_sync<NQ>(el);
       Auk += row_dot<NQ, VEC>(&s_GqsT[b][el][i][0], DTj);       // sum_m D[m][j] Gqs(i,m)
       Auk += row_dot<NQ, VEC>(&s_Gqr[b][el][j][0], DTi);        // sum_m D[m][i] Gqr(m,j)
       r_Aq[k] = Auk;
