@@ -370,15 +370,15 @@ mlp_tc_kernel(const __grid_constant__ TcMaps maps, const float* __restrict__ b0,
 // K blocks of the same job sequence through a 2-stage ring (2 x 48 KB; the two 64 KB
 // activation buffers take the rest of shared memory). Epilogue warps: 4 x EPI2_G per
 // slot; warp w reads TMEM lanes 32 (w % 4) .. +31 and 256 / EPI2_G of the columns.
+constexpr int NSTAGE2 = 2;
 constexpr int EPI2_G = 2;
 constexpr int EPI2_WARPS = 2 * 4 * EPI2_G;
 constexpr int THREADS2 = 32 * (2 + EPI2_WARPS);
-template <int NS> constexpr int nbar2() { return 2 * NS + 4 + 2; }   // full[], empty[], accFull[2], epiDone[2], drain, hold
-template <int NS> constexpr int smem2_bytes() { return 1024 + NS * STAGE_BYTES + 2 * H_BYTES + nbar2<NS>() * 8 + 16; }
-static_assert(smem2_bytes<2>() <= 232448 - 64, "two-slot MLP kernel: shared memory");
+constexpr int NBAR2 = 2 * NSTAGE2 + 4 + 2;     // full[], empty[], accFull[2], epiDone[2], drain, hold
+constexpr int SMEM2_BYTES = 1024 + NSTAGE2 * STAGE_BYTES + 2 * H_BYTES + NBAR2 * 8 + 16;
+static_assert(SMEM2_BYTES <= 232448 - 64, "two-slot MLP kernel: shared memory");
 constexpr int JOBS = 5;                        // L0, L1, L2, L3 columns 0-255, L3 columns 256-511
 
-template <int NSTAGE2>
 __global__ void __launch_bounds__(THREADS2, 1)
 mlp_tc2_kernel(const __grid_constant__ TcMaps maps, const float* __restrict__ b0, const float* __restrict__ b1,
                const float* __restrict__ b2, const float* __restrict__ b3, float* __restrict__ Y, const int64_t rows,
@@ -388,7 +388,7 @@ mlp_tc2_kernel(const __grid_constant__ TcMaps maps, const float* __restrict__ b0
   unsigned char* stage0 = smem;
   unsigned char* hbuf0 = smem + NSTAGE2 * STAGE_BYTES;             // slot 0 activations, slot 1 after
   uint64_t* bars = reinterpret_cast<uint64_t*>(hbuf0 + 2 * H_BYTES);
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + nbar2<NSTAGE2>());
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + NBAR2);
   __shared__ volatile int s_abort;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -635,19 +635,12 @@ int mlp_forward_tc(int64_t B, const __nv_bfloat16* X, const __nv_bfloat16* const
     const char* e = std::getenv("LPG_MLP_TC");
     return e && !std::strcmp(e, "single");
   }();
-  static const bool one = [] {
-    const char* e = std::getenv("LPG_MLP_TC");
-    return e && !std::strcmp(e, "two1");
-  }();
   static PerDeviceConfig perDevice;   // dynamic shared memory opt-in per device
   KernelConfig cfg;
   rc = perDevice.get(
       [&](int, KernelConfig&) {
         LPG_CUDA_TRY(cudaFuncSetAttribute(mlp_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-        LPG_CUDA_TRY(
-            cudaFuncSetAttribute(mlp_tc2_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem2_bytes<2>()));
-        LPG_CUDA_TRY(
-            cudaFuncSetAttribute(mlp_tc2_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem2_bytes<1>()));
+        LPG_CUDA_TRY(cudaFuncSetAttribute(mlp_tc2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM2_BYTES));
         return (int)LPG_OK;
       },
       &cfg);
@@ -660,13 +653,9 @@ int mlp_forward_tc(int64_t B, const __nv_bfloat16* X, const __nv_bfloat16* const
     mlp_tc_kernel<<<grid, THREADS, SMEM_BYTES, s>>>(maps, bias[0], bias[1], bias[2], bias[3], Y, B, ntiles, errFlag,
                                                     hold);
     LPG_LAUNCH_CHECK("mlp_tc_kernel");
-  } else if (one) {
-    mlp_tc2_kernel<1><<<grid, THREADS2, smem2_bytes<1>(), s>>>(maps, bias[0], bias[1], bias[2], bias[3], Y, B, ntiles,
-                                                               errFlag, hold);
-    LPG_LAUNCH_CHECK("mlp_tc2_kernel");
   } else {
-    mlp_tc2_kernel<2><<<grid, THREADS2, smem2_bytes<2>(), s>>>(maps, bias[0], bias[1], bias[2], bias[3], Y, B, ntiles,
-                                                               errFlag, hold);
+    mlp_tc2_kernel<<<grid, THREADS2, SMEM2_BYTES, s>>>(maps, bias[0], bias[1], bias[2], bias[3], Y, B, ntiles, errFlag,
+                                                       hold);
     LPG_LAUNCH_CHECK("mlp_tc2_kernel");
   }
   return LPG_OK;
