@@ -144,6 +144,31 @@ __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
   return *reinterpret_cast<const uint32_t*>(&p);
 }
 
+// 8 x 8 transpose of 16-byte chunks within each group of 8 lanes (b = lane & 7): on entry
+// lane b holds chunks 0..7 of its row b, on exit chunk m of lane b is chunk b of row m.
+// Three butterfly stages (lane distance 4, 2, 1); at each, the lanes of a pair swap the
+// chunks whose index bit differs from their lane bit.
+__device__ __forceinline__ void transpose8_chunks(float4* c, const int b) {
+  constexpr unsigned FULL = 0xffffffffu;
+#pragma unroll
+  for (int d = 4; d >= 1; d >>= 1) {
+    const bool hi = (b & d) != 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      if (k & d) continue;
+      const int k2 = k | d;
+      const float4 send = hi ? c[k] : c[k2];
+      float4 recv;
+      recv.x = __shfl_xor_sync(FULL, send.x, d);
+      recv.y = __shfl_xor_sync(FULL, send.y, d);
+      recv.z = __shfl_xor_sync(FULL, send.z, d);
+      recv.w = __shfl_xor_sync(FULL, send.w, d);
+      if (hi) c[k] = recv;
+      else c[k2] = recv;
+    }
+  }
+}
+
 struct TcMaps {
   CUtensorMap x, w[4];
 };
@@ -557,14 +582,22 @@ mlp_tc2_kernel(const __grid_constant__ TcMaps maps, const float* __restrict__ b0
           const int cbase = 256 * (job - 3);
           for (int c0 = g * CW; c0 < (g + 1) * CW; c0 += 32) {
             tmem_ld32(tlane + c0, v);
-            if (row < rows) {
-              float4* dst = reinterpret_cast<float4*>(Y + row * kMlpOut + cbase + c0);
+            float4 ch[8];
 #pragma unroll
-              for (int t = 0; t < 8; ++t) {
-                const float4 bb = __ldg(reinterpret_cast<const float4*>(b3 + cbase + c0 + 4 * t));
-                dst[t] = make_float4(v[4 * t] + bb.x, v[4 * t + 1] + bb.y, v[4 * t + 2] + bb.z, v[4 * t + 3] + bb.w);
-              }
+            for (int t = 0; t < 8; ++t) {
+              const float4 bb = __ldg(reinterpret_cast<const float4*>(b3 + cbase + c0 + 4 * t));
+              ch[t] = make_float4(v[4 * t] + bb.x, v[4 * t + 1] + bb.y, v[4 * t + 2] + bb.z, v[4 * t + 3] + bb.w);
             }
+            // each lane holds 8 16-byte chunks of its own row; an 8 x 8 transpose within
+            // groups of 8 lanes leaves lane b with chunk b of the group's 8 rows, so each
+            // store below writes whole 128-byte row segments (4 per warp) instead of 32
+            // separate 16-byte pieces
+            transpose8_chunks(ch, lane & 7);
+            const int64_t grow0 = (int64_t)tile * TM + 32 * q + 8 * (lane >> 3);
+#pragma unroll
+            for (int m = 0; m < 8; ++m)
+              if (grow0 + m < rows)
+                *reinterpret_cast<float4*>(Y + (grow0 + m) * kMlpOut + cbase + c0 + 4 * (lane & 7)) = ch[m];
           }
         }
         tc_fence_before();
