@@ -543,6 +543,15 @@ int MultiGrid::residual<float>(Elliptic* el, const float* RHS, const float* X, f
 }
 
 // ---------------------------------------------------------------- p-level smoothing
+// LPG_CHEB=unfused (a tuning override): the FP32 Chebyshev steps with a separate A d vector
+static bool cheb_unfused() {
+  static const bool v = [] {
+    const char* e = std::getenv("LPG_CHEB");
+    return e && !std::strcmp(e, "unfused");
+  }();
+  return v;
+}
+
 template <typename T>
 int MultiGrid::smooth(PLevel& L, const T* r, T* X, bool xIsZero, cudaStream_t s) {
   const int64_t N = L.el->Nglobal;
@@ -566,14 +575,23 @@ int MultiGrid::smooth(PLevel& L, const T* r, T* X, bool xIsZero, cudaStream_t s)
   // once at the end), with each x += d fused into the pass that produced d
   if (!xIsZero && (rc = op<T>(L.el, X, RES, s))) return rc;
   if ((rc = cheb_start<T>(N, invDiag, r, xIsZero ? nullptr : RES, RES, d, X, (T)invTheta, xIsZero, s))) return rc;
+  // FP32 C0 levels: the operator scatters -invDiag .* A d straight into the scaled residual
+  // (no A d vector, no memset of it, and the step pass reads 3 vectors instead of 5)
+  const bool fused = std::is_same<T, float>::value && !L.el->ipdg && !cheb_unfused();
   for (int k = 0; k < opt.chebDegree; ++k) {
-    if ((rc = op<T>(L.el, d, Ad, s))) return rc;
     rho_np1 = 1.0 / (2. * sigma - rho_n);
     const double rhoDivDelta = 2.0 * rho_np1 / delta;
-    // the last step's res and d are not read again: it writes x only
-    if ((rc = cheb_step<T>(N, invDiag, Ad, RES, d, X, (T)(rho_np1 * rho_n), (T)rhoDivDelta, s,
-                           k == opt.chebDegree - 1)))
-      return rc;
+    const bool last = (k == opt.chebDegree - 1);   // the last step's res and d are not read again
+    if constexpr (std::is_same<T, float>::value) {
+      if (fused) {
+        if ((rc = L.el->OperatorF32(d, RES, opt.prec, s, -1.f, invDiag))) return rc;
+        if ((rc = cheb_step_res<T>(N, RES, d, X, (T)(rho_np1 * rho_n), (T)rhoDivDelta, s, last))) return rc;
+        rho_n = rho_np1;
+        continue;
+      }
+    }
+    if ((rc = op<T>(L.el, d, Ad, s))) return rc;
+    if ((rc = cheb_step<T>(N, invDiag, Ad, RES, d, X, (T)(rho_np1 * rho_n), (T)rhoDivDelta, s, last))) return rc;
     rho_n = rho_np1;
   }
   return LPG_OK;

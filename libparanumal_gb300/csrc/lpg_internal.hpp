@@ -31,6 +31,10 @@ struct AxArgs {
   // out preset to b and outScale = -1 an AccumulateAssembled launch leaves the residual
   // b - A q without a separate vector pass.
   T outScale = T(1);
+  // FP32 assembled modes: when set, each contribution to dof g is also scaled by
+  // outScaleVec[g] (out += outScale * outScaleVec .* A q): with outScaleVec = 1/diag and
+  // outScale = -1 the operator updates a Chebyshev smoother's scaled residual in place
+  const T* outScaleVec = nullptr;
 };
 
 template <typename T, typename G>
@@ -151,6 +155,10 @@ int cheb_start(int64_t N, const T* invDiag, const T* r, const T* Ax, T* res, T* 
 template <typename T>
 int cheb_step(int64_t N, const T* invDiag, const T* Ad, T* res, T* d, T* x, T a, T b, cudaStream_t s,
               bool last = false);
+// the step when the operator already left res -= invDiag A d: d = a d + b res; x += d
+// (last: x += a d + b res, d not written)
+template <typename T>
+int cheb_step_res(int64_t N, const T* res, T* d, T* x, T a, T b, cudaStream_t s, bool last = false);
 
 // ---------------------------------------------------------------- p-multigrid transfers
 // xC = assembled sum over coarse copies of P^T (weightF .* xF) per element (xC overwritten)

@@ -550,6 +550,27 @@ int cheb_step(int64_t N, const T* invDiag, const T* Ad, T* res, T* d, T* x, T a,
   LPG_LAUNCH_CHECK("cheb_step_kernel");
   return LPG_OK;
 }
+// the step after an operator that already updated res (res -= invDiag A d)
+template <typename T, bool LAST>
+__global__ void cheb_step_res_kernel(const int64_t N, const T* __restrict__ res, T* __restrict__ d,
+                                     T* __restrict__ x, const T a, const T b) {
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x) {
+    const T dn = b * res[n] + a * d[n];
+    if (!LAST) d[n] = dn;
+    x[n] = x[n] + dn;
+  }
+}
+template <typename T>
+int cheb_step_res(int64_t N, const T* res, T* d, T* x, T a, T b, cudaStream_t s, bool last) {
+  if (N <= 0) return LPG_OK;
+  if (last) cheb_step_res_kernel<T, true><<<grid_for(N, 256, kStreamCap), 256, 0, s>>>(N, res, d, x, a, b);
+  else cheb_step_res_kernel<T, false><<<grid_for(N, 256, kStreamCap), 256, 0, s>>>(N, res, d, x, a, b);
+  LPG_LAUNCH_CHECK("cheb_step_res_kernel");
+  return LPG_OK;
+}
+template int cheb_step_res<double>(int64_t, const double*, double*, double*, double, double, cudaStream_t, bool);
+template int cheb_step_res<float>(int64_t, const float*, float*, float*, float, float, cudaStream_t, bool);
+
 template int cheb_start<double>(int64_t, const double*, const double*, const double*, double*, double*, double*, double,
                                 bool, cudaStream_t);
 template int cheb_start<float>(int64_t, const float*, const float*, const float*, float*, float*, float*, float, bool,
