@@ -35,7 +35,7 @@ ax_hex_kernel(const int64_t Nelements, const int32_t* __restrict__ elementList,
               const int32_t* __restrict__ g2l, const G* __restrict__ ggeo, const int64_t geoStride,
               const G* __restrict__ wJ, const int64_t wJStride, const T* __restrict__ Dg,
               const T lambda, const T* __restrict__ lambdaE, const T* __restrict__ q,
-              T* __restrict__ out, const T outScale, const T* __restrict__ outScaleVec) {
+              T* __restrict__ out, const T outScale) {
   constexpr int NP = NQ * NQ * NQ;
   constexpr int EPB = elems_per_block<NQ>();
   __shared__ T s_D[NQ][NQ];
@@ -123,8 +123,7 @@ ax_hex_kernel(const int64_t Nelements, const int32_t* __restrict__ elementList,
     if (OUTMODE == OUT_ASSEMBLE) {
       // FP32: the scaled assembly of the fused residual; FP64 always adds A q itself
       if constexpr (std::is_same<T, float>::value) {
-        if (r_id[k] >= 0)
-          atomicAdd(out + r_id[k], (outScaleVec ? outScale * outScaleVec[r_id[k]] : outScale) * r_Aq[k]);
+        if (r_id[k] >= 0) atomicAdd(out + r_id[k], outScale * r_Aq[k]);
       } else {
         if (r_id[k] >= 0) atomicAdd(out + r_id[k], r_Aq[k]);
       }
@@ -212,7 +211,7 @@ ax_hex_staged_kernel(const int64_t Nelements, const int32_t* __restrict__ elemen
                      const int32_t* __restrict__ g2l, const G* __restrict__ ggeo, const int64_t geoStride,
                      const G* __restrict__ wJ, const int64_t wJStride, const T* __restrict__ Dg, const T lambda,
                      const T* __restrict__ lambdaE, const T* __restrict__ q, T* __restrict__ out,
-                     const T outScale, const T* __restrict__ outScaleVec) {
+                     const T outScale) {
   static_assert(std::is_same<T, float>::value, "staged kernel is FP32");
   using L = StagedLayout<NQ, G>;
   constexpr int NP = L::NP, NT = NQ * NQ * EPB;
@@ -383,8 +382,7 @@ ax_hex_staged_kernel(const int64_t Nelements, const int32_t* __restrict__ elemen
     if (active) {
 #pragma unroll
       for (int k = 0; k < NQ; ++k)
-        if (r_id[k] >= 0)
-          atomicAdd(out + r_id[k], (outScaleVec ? outScale * outScaleVec[r_id[k]] : outScale) * r_Aq[k]);
+        if (r_id[k] >= 0) atomicAdd(out + r_id[k], outScale * r_Aq[k]);
     }
   }
   cp_async_wait<0>();
@@ -1119,7 +1117,7 @@ static int launch_staged(const AxArgs<T, G>& a, cudaStream_t s) {
   if (grid <= 0) return LPG_OK;
   kern<<<(unsigned)grid, dim3(NQ, NQ, EPB), smem, s>>>(a.Nelements, a.elementList, a.g2l, a.ggeo, a.geoStride, a.wJ,
                                                         a.wJStride, a.D, a.lambda, a.lambdaE, a.q, a.out,
-                                                        a.outScale, a.outScaleVec);
+                                                        a.outScale);
   LPG_LAUNCH_CHECK("ax_hex_staged_kernel");
   return LPG_OK;
 }
@@ -1204,7 +1202,7 @@ static int launch_ax(const AxArgs<T, G>& a, cudaStream_t s) {
   }
   ax_hex_kernel<NQ, T, G, INMODE, OUTMODE><<<(unsigned)blocks, block, 0, s>>>(
       a.Nelements, a.elementList, a.g2l, a.ggeo, a.geoStride, a.wJ, a.wJStride, a.D, a.lambda,
-      a.lambdaE, a.q, a.out, a.outScale, a.outScaleVec);
+      a.lambdaE, a.q, a.out, a.outScale);
   LPG_LAUNCH_CHECK("ax_hex_kernel");
   return LPG_OK;
 }
@@ -1226,10 +1224,8 @@ static int dispatch_ax(const AxArgs<T, G>& a, cudaStream_t s) {
 
 template <typename T, typename G>
 int ax_hex(const AxArgs<T, G>& a, AxMode mode, cudaStream_t s) {
-  if (!std::is_same<T, float>::value && (a.outScale != T(1) || a.outScaleVec))
+  if (!std::is_same<T, float>::value && a.outScale != T(1))
     return set_error(LPG_ERR_UNSUPPORTED, "ax: a scaled assembly is provided for FP32 only");
-  if (a.outScaleVec && (mode == AxMode::PartialLocal || mode == AxMode::LocalInSubtract))
-    return set_error(LPG_ERR_INVALID, "ax: a per-dof output scale needs an assembled mode");
   switch (mode) {
     case AxMode::Assemble: {
       if (a.Nglobal > 0) LPG_CUDA_TRY(cudaMemsetAsync(a.out, 0, sizeof(T) * a.Nglobal, s));

@@ -462,9 +462,7 @@ int Elliptic::Operator(const double* q, double* Aq, cudaStream_t s) {
   return ax_hex<double, double>(a, AxMode::Assemble, s);
 }
 
-int Elliptic::OperatorF32(const float* q, float* Aq, Prec prec, cudaStream_t s, float accumulate,
-                          const float* scaleVec) {
-  if (scaleVec && accumulate == 0.f) return set_error(LPG_ERR_INVALID, "OperatorF32: a dof scale needs accumulate");
+int Elliptic::OperatorF32(const float* q, float* Aq, Prec prec, cudaStream_t s, float accumulate) {
   ++nOps;
   const int64_t Np = mesh.Np;
   const AxMode mode = accumulate != 0.f ? AxMode::AccumulateAssembled : AxMode::Assemble;
@@ -488,7 +486,6 @@ int Elliptic::OperatorF32(const float* q, float* Aq, Prec prec, cudaStream_t s, 
     a.D = mesh.D32.p; a.lambda = (float)lambda; a.lambdaE = hasLambdaE ? lambdaE32.p : nullptr;
     a.q = q; a.out = Aq; a.Nglobal = Nglobal;
     if (accumulate != 0.f) a.outScale = accumulate;
-    a.outScaleVec = scaleVec;
     return ax_hex<float, __nv_bfloat16>(a, mode, s);
   }
   AxArgs<float, float> a;
@@ -497,7 +494,6 @@ int Elliptic::OperatorF32(const float* q, float* Aq, Prec prec, cudaStream_t s, 
   a.D = mesh.D32.p; a.lambda = (float)lambda; a.lambdaE = hasLambdaE ? lambdaE32.p : nullptr;
   a.q = q; a.out = Aq; a.Nglobal = Nglobal;
   if (accumulate != 0.f) a.outScale = accumulate;
-  a.outScaleVec = scaleVec;
   return ax_hex<float, float>(a, mode, s);
 }
 

@@ -574,18 +574,24 @@ int MultiGrid::smooth(PLevel& L, const T* r, T* X, bool xIsZero, cudaStream_t s)
   // same recurrence as the reference's loop (x += d before each application of A, and
   // once at the end), with each x += d fused into the pass that produced d
   if (!xIsZero && (rc = op<T>(L.el, X, RES, s))) return rc;
-  if ((rc = cheb_start<T>(N, invDiag, r, xIsZero ? nullptr : RES, RES, d, X, (T)invTheta, xIsZero, s))) return rc;
-  // FP32 C0 levels: the operator scatters -invDiag .* A d straight into the scaled residual
-  // (no A d vector, no memset of it, and the step pass reads 3 vectors instead of 5)
+  // FP32 C0 levels: the smoother keeps the unscaled residual u = r - A x, which the
+  // operator updates in place (u -= A d, assembled straight into it): no A d vector and no
+  // memset of it, and each step pass reads 4 vectors and writes 2 instead of 5 and 3
   const bool fused = std::is_same<T, float>::value && !L.el->ipdg && !cheb_unfused();
+  if (fused) {
+    if ((rc = cheb_start_u<T>(N, invDiag, r, xIsZero ? nullptr : RES, RES, d, X, (T)invTheta, xIsZero, s)))
+      return rc;
+  } else if ((rc = cheb_start<T>(N, invDiag, r, xIsZero ? nullptr : RES, RES, d, X, (T)invTheta, xIsZero, s))) {
+    return rc;
+  }
   for (int k = 0; k < opt.chebDegree; ++k) {
     rho_np1 = 1.0 / (2. * sigma - rho_n);
     const double rhoDivDelta = 2.0 * rho_np1 / delta;
     const bool last = (k == opt.chebDegree - 1);   // the last step's res and d are not read again
     if constexpr (std::is_same<T, float>::value) {
       if (fused) {
-        if ((rc = L.el->OperatorF32(d, RES, opt.prec, s, -1.f, invDiag))) return rc;
-        if ((rc = cheb_step_res<T>(N, RES, d, X, (T)(rho_np1 * rho_n), (T)rhoDivDelta, s, last))) return rc;
+        if ((rc = L.el->OperatorF32(d, RES, opt.prec, s, -1.f))) return rc;
+        if ((rc = cheb_step_u<T>(N, invDiag, RES, d, X, (T)(rho_np1 * rho_n), (T)rhoDivDelta, s, last))) return rc;
         rho_n = rho_np1;
         continue;
       }

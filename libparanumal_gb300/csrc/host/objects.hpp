@@ -199,10 +199,8 @@ struct Elliptic {
   int Operator(const double* q, double* Aq, cudaStream_t s);
   int OperatorDW(const double* q, double* Aq, cudaStream_t s);
   // accumulate = 0: Aq = A q; otherwise Aq += accumulate * A q (C0 only)
-  // accumulate != 0: Aq += accumulate * A q (C0 only), and with scaleVec each dof's
-  // contribution is also scaled by scaleVec[g]
-  int OperatorF32(const float* q, float* Aq, Prec prec, cudaStream_t s, float accumulate = 0.f,
-                  const float* scaleVec = nullptr);
+  // accumulate != 0: Aq += accumulate * A q (C0 only)
+  int OperatorF32(const float* q, float* Aq, Prec prec, cudaStream_t s, float accumulate = 0.f);
   // Aq = A q with host buffers (page-locked for overlap); returns when Aq is filled
   std::unique_ptr<HostPipe> pipe;
   int BuildPipe(cudaStream_t s);

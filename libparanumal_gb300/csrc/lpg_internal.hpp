@@ -31,10 +31,6 @@ struct AxArgs {
   // out preset to b and outScale = -1 an AccumulateAssembled launch leaves the residual
   // b - A q without a separate vector pass.
   T outScale = T(1);
-  // FP32 assembled modes: when set, each contribution to dof g is also scaled by
-  // outScaleVec[g] (out += outScale * outScaleVec .* A q): with outScaleVec = 1/diag and
-  // outScale = -1 the operator updates a Chebyshev smoother's scaled residual in place
-  const T* outScaleVec = nullptr;
 };
 
 template <typename T, typename G>
@@ -155,10 +151,14 @@ int cheb_start(int64_t N, const T* invDiag, const T* r, const T* Ax, T* res, T* 
 template <typename T>
 int cheb_step(int64_t N, const T* invDiag, const T* Ad, T* res, T* d, T* x, T a, T b, cudaStream_t s,
               bool last = false);
-// the step when the operator already left res -= invDiag A d: d = a d + b res; x += d
-// (last: x += a d + b res, d not written)
+// the same on the unscaled residual u = r - A x, which the operator updates in place
+// (u -= A d): start u = r - Ax (or r), d = invTheta invDiag u, x = d or x += d; step
+// d = a d + b invDiag u, x += d (last: d not written)
 template <typename T>
-int cheb_step_res(int64_t N, const T* res, T* d, T* x, T a, T b, cudaStream_t s, bool last = false);
+int cheb_start_u(int64_t N, const T* invDiag, const T* r, const T* Ax, T* u, T* d, T* x, T invTheta, bool xIsZero,
+                 cudaStream_t s);
+template <typename T>
+int cheb_step_u(int64_t N, const T* invDiag, const T* u, T* d, T* x, T a, T b, cudaStream_t s, bool last = false);
 
 // ---------------------------------------------------------------- p-multigrid transfers
 // xC = assembled sum over coarse copies of P^T (weightF .* xF) per element (xC overwritten)

@@ -550,26 +550,50 @@ int cheb_step(int64_t N, const T* invDiag, const T* Ad, T* res, T* d, T* x, T a,
   LPG_LAUNCH_CHECK("cheb_step_kernel");
   return LPG_OK;
 }
-// the step after an operator that already updated res (res -= invDiag A d)
-template <typename T, bool LAST>
-__global__ void cheb_step_res_kernel(const int64_t N, const T* __restrict__ res, T* __restrict__ d,
-                                     T* __restrict__ x, const T a, const T b) {
+// Chebyshev passes on the unscaled residual u = r - A x, which the operator updates in
+// place (u -= A d): start u = r - Ax (or r), d = invTheta invDiag u, x = d or x += d; step
+// d = a d + b invDiag u, x += d (last: d not written)
+template <typename T>
+__global__ void cheb_start_u_kernel(const int64_t N, const T* __restrict__ invDiag, const T* __restrict__ r,
+                                    const T* Ax, T* u, T* __restrict__ d, T* __restrict__ x, const T invTheta,
+                                    const int xIsZero) {   // Ax may alias u
   for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x) {
-    const T dn = b * res[n] + a * d[n];
+    const T un = Ax ? r[n] - Ax[n] : r[n];
+    u[n] = un;
+    const T dn = invTheta * (invDiag[n] * un);
+    d[n] = dn;
+    x[n] = xIsZero ? dn : x[n] + dn;
+  }
+}
+template <typename T, bool LAST>
+__global__ void cheb_step_u_kernel(const int64_t N, const T* __restrict__ invDiag, const T* __restrict__ u,
+                                   T* __restrict__ d, T* __restrict__ x, const T a, const T b) {
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x) {
+    const T dn = b * (invDiag[n] * u[n]) + a * d[n];
     if (!LAST) d[n] = dn;
     x[n] = x[n] + dn;
   }
 }
 template <typename T>
-int cheb_step_res(int64_t N, const T* res, T* d, T* x, T a, T b, cudaStream_t s, bool last) {
+int cheb_start_u(int64_t N, const T* invDiag, const T* r, const T* Ax, T* u, T* d, T* x, T invTheta, bool xIsZero,
+                 cudaStream_t s) {
   if (N <= 0) return LPG_OK;
-  if (last) cheb_step_res_kernel<T, true><<<grid_for(N, 256, kStreamCap), 256, 0, s>>>(N, res, d, x, a, b);
-  else cheb_step_res_kernel<T, false><<<grid_for(N, 256, kStreamCap), 256, 0, s>>>(N, res, d, x, a, b);
-  LPG_LAUNCH_CHECK("cheb_step_res_kernel");
+  cheb_start_u_kernel<T><<<grid_for(N, 256, kStreamCap), 256, 0, s>>>(N, invDiag, r, Ax, u, d, x, invTheta,
+                                                                       xIsZero ? 1 : 0);
+  LPG_LAUNCH_CHECK("cheb_start_u_kernel");
   return LPG_OK;
 }
-template int cheb_step_res<double>(int64_t, const double*, double*, double*, double, double, cudaStream_t, bool);
-template int cheb_step_res<float>(int64_t, const float*, float*, float*, float, float, cudaStream_t, bool);
+template <typename T>
+int cheb_step_u(int64_t N, const T* invDiag, const T* u, T* d, T* x, T a, T b, cudaStream_t s, bool last) {
+  if (N <= 0) return LPG_OK;
+  if (last) cheb_step_u_kernel<T, true><<<grid_for(N, 256, kStreamCap), 256, 0, s>>>(N, invDiag, u, d, x, a, b);
+  else cheb_step_u_kernel<T, false><<<grid_for(N, 256, kStreamCap), 256, 0, s>>>(N, invDiag, u, d, x, a, b);
+  LPG_LAUNCH_CHECK("cheb_step_u_kernel");
+  return LPG_OK;
+}
+template int cheb_start_u<float>(int64_t, const float*, const float*, const float*, float*, float*, float*, float, bool,
+                                 cudaStream_t);
+template int cheb_step_u<float>(int64_t, const float*, const float*, float*, float*, float, float, cudaStream_t, bool);
 
 template int cheb_start<double>(int64_t, const double*, const double*, const double*, double*, double*, double*, double,
                                 bool, cudaStream_t);
