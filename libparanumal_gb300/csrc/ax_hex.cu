@@ -415,7 +415,9 @@ __device__ __forceinline__ void eo_sync(const int el) {
 }
 
 // MASS = false: lambda == 0 and no lambda field, the mass term and its wJ reads are left out
-template <int NQ, bool MASS = true>
+// UNIT: lambda == 1 without a lambda field, the mass term is wJ q (one FP64 multiply fewer
+// per node, the same result: wJ * 1.0 is exact)
+template <int NQ, bool MASS = true, bool UNIT = false>
 __global__ void __launch_bounds__(NQ * NQ * elems_per_block<NQ>(), 3)
 ax_hex_eo_kernel(const int64_t Nelements, const int32_t* __restrict__ elementList,
                  const int32_t* __restrict__ g2l, const double* __restrict__ ggeo, const int64_t geoStride,
@@ -552,7 +554,8 @@ ax_hex_eo_kernel(const int64_t Nelements, const int32_t* __restrict__ elementLis
     eo_sync<NQ>(el);
     // the mass term lambda wJ q folded into the sum as one FMA
     const double sum = s_dr[el][j][i] + s_ds[el][j][i];
-    if constexpr (MASS) r_Aq[k] = fma(GwJ * lam, v, sum);
+    if constexpr (MASS && UNIT) r_Aq[k] = fma(GwJ, v, sum);
+    else if constexpr (MASS) r_Aq[k] = fma(GwJ * lam, v, sum);
     else r_Aq[k] = sum;
   }
 
@@ -794,7 +797,7 @@ __device__ __forceinline__ void ld_dw4x2(const dw* src, dw* v) {
 // cp.async (more shared-memory traffic; slower at three CTAs per SM), a register prefetch
 // (does not fit 64 registers). MASS = false: lambda == 0 and no lambda field, the mass term
 // and its wJ reads are left out.
-template <int NQ, bool MASS>
+template <int NQ, bool MASS, bool UNIT = false>
 __global__ void __launch_bounds__(NQ * NQ * elems_per_block<NQ>(), 4)
 ax_hex_dw_lean_kernel(const int64_t Nelements, const int32_t* __restrict__ elementList,
                       const int32_t* __restrict__ g2l, const dw* __restrict__ ggeo, const int64_t geoStride,
@@ -919,7 +922,8 @@ ax_hex_dw_lean_kernel(const int64_t Nelements, const int32_t* __restrict__ eleme
     const dw Gqr = ar.raw(), Gqs = as.raw();
     s_q[k][tid] = at.raw();
     dw mass{0.f, 0.f};
-    if constexpr (MASS) mass = dw_mul(dw_mul(GwJ, lam), v);
+    if constexpr (MASS && UNIT) mass = dw_mul(GwJ, v);   // lambda == 1: wJ q
+    else if constexpr (MASS) mass = dw_mul(dw_mul(GwJ, lam), v);
     const dw pr2 = dw_shfl_xor(Gqr, NQ - 1), ps2 = dw_shfl_xor(Gqs, 2 * NQ);
     s_R[el][j][slotR] = dw_add_sign_u(pr2, sgnR, Gqr);
     s_S[el][i][slotS] = dw_add_sign_u(ps2, sgnS, Gqs);
@@ -1081,6 +1085,8 @@ int ax_hex_dw(const AxArgs<double, float2>& a, cudaStream_t s) {
       reinterpret_cast<const dw*>(a.wJ), a.wJStride, a.D, a.lambda, a.lambdaE, a.q, a.out
     if (dw7_classic())
       ax_hex_dw_kernel<8, true><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS);
+    else if (mass && a.lambda == 1.0 && !a.lambdaE)
+      ax_hex_dw_lean_kernel<8, true, true><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS);
     else if (mass)
       ax_hex_dw_lean_kernel<8, true><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS);
     else
@@ -1192,6 +1198,10 @@ static int launch_ax(const AxArgs<T, G>& a, cudaStream_t s) {
         ax_hex_eo_kernel<NQ, false><<<(unsigned)blocks, block, 0, s>>>(a.Nelements, a.elementList, a.g2l, a.ggeo,
                                                                       a.geoStride, a.wJ, a.wJStride, a.D, a.lambda,
                                                                       a.lambdaE, a.q, a.out);
+      else if (a.lambda == 1.0 && !a.lambdaE)
+        ax_hex_eo_kernel<NQ, true, true><<<(unsigned)blocks, block, 0, s>>>(a.Nelements, a.elementList, a.g2l,
+                                                                           a.ggeo, a.geoStride, a.wJ, a.wJStride,
+                                                                           a.D, a.lambda, a.lambdaE, a.q, a.out);
       else
         ax_hex_eo_kernel<NQ, true><<<(unsigned)blocks, block, 0, s>>>(a.Nelements, a.elementList, a.g2l, a.ggeo,
                                                                      a.geoStride, a.wJ, a.wJStride, a.D, a.lambda,

@@ -23,6 +23,8 @@ CASES = [
     box(**{"POLYNOMIAL DEGREE": 4, "LAMBDA FIELD": "LOGNORMAL", "LAMBDA SEED": 2}),
     box(**{"POLYNOMIAL DEGREE": 8, "BOX NX": 2, "BOX NY": 2, "BOX NZ": 2}),
     box(**{"POLYNOMIAL DEGREE": 2, "BOX NX": 1, "BOX NY": 1, "BOX NZ": 1}),   # one element
+    box(**{"LAMBDA": 0.3}),                                  # N=7, lambda neither 0 nor 1
+    box(**{"POLYNOMIAL DEGREE": 3, "LAMBDA FIELD": "LOGNORMAL", "LAMBDA SEED": 2}),   # N=3 even-odd, field
 ]
 
 
@@ -76,6 +78,7 @@ def test_operator_matches_oracle(cfg):
 REF_CASES = [box(**{"POLYNOMIAL DEGREE": N}) for N in range(1, 9)] + [
     box(**{"POLYNOMIAL DEGREE": 3, "BOX BOUNDARY FLAG": -1, "MESH JITTER": 0.0}),   # periodic
     box(**{"POLYNOMIAL DEGREE": 7, "LAMBDA": 0.0, "BOX NX": 4, "BOX NY": 4, "BOX NZ": 4}),
+    box(**{"POLYNOMIAL DEGREE": 7, "LAMBDA": 2.5}),
 ]
 
 
@@ -219,6 +222,7 @@ DW_CASES = [
            "BOX NY": 4, "BOX NZ": 2}),                                        # periodic, N=3
     box(**{"LAMBDA FIELD": "LOGNORMAL", "LAMBDA SEED": 2, "BOX NX": 32, "BOX NY": 32, "BOX NZ": 16}),
     box(**{"LAMBDA": 0.0, "BOX NX": 9, "BOX NY": 7, "BOX NZ": 5}),            # N=7 without the mass term
+    box(**{"LAMBDA": 2.5}),                                                    # N=7, general constant lambda
     # degrees without an even-odd kernel (thread-per-node double-word kernel)
     box(**{"POLYNOMIAL DEGREE": 1, "BOX NX": 6, "BOX NY": 5, "BOX NZ": 4}),
     box(**{"POLYNOMIAL DEGREE": 2, "BOX BOUNDARY FLAG": -1, "MESH JITTER": 0.0, "BOX NX": 3, "BOX NY": 4,
