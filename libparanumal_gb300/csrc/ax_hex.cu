@@ -797,7 +797,7 @@ __device__ __forceinline__ void ld_dw4x2(const dw* src, dw* v) {
 // cp.async (more shared-memory traffic; slower at three CTAs per SM), a register prefetch
 // (does not fit 64 registers). MASS = false: lambda == 0 and no lambda field, the mass term
 // and its wJ reads are left out.
-template <int NQ, bool MASS, bool UNIT = false, bool PERSIST = false>
+template <int NQ, bool MASS, bool UNIT = false>
 __global__ void __launch_bounds__(NQ * NQ * elems_per_block<NQ>(), 4)
 ax_hex_dw_lean_kernel(const int64_t Nelements, const int32_t* __restrict__ elementList,
                       const int32_t* __restrict__ g2l, const dw* __restrict__ ggeo, const int64_t geoStride,
@@ -828,27 +828,16 @@ ax_hex_dw_lean_kernel(const int64_t Nelements, const int32_t* __restrict__ eleme
     s_Tm[a][m] = dw_from_double(0.5 * (t0 - t1));
   }
 
-  const int64_t ngroups = (Nelements + EPB - 1) / EPB;
-  auto elem_of = [&](const int64_t grp, bool& act) {
-    int64_t ee = grp * EPB + el;
-    act = grp < ngroups && ee < Nelements;
-    if (act && elementList) ee = elementList[ee];
-    return act ? ee : (int64_t)0;
-  };
-  // PERSIST: CTAs walk element groups; while a group is computed the next one's indices,
-  // geometric factors and (half-way) q values are requested into L2
-  for (int64_t grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
-  bool active;
-  const int64_t e = elem_of(grp, active);
-  bool nactive = false;
-  const int64_t en = PERSIST ? elem_of(grp + gridDim.x, nactive) : 0;
+  int64_t e = (int64_t)blockIdx.x * EPB + el;
+  const bool active = e < Nelements;
+  if (active && elementList) e = elementList[e];
+  if (!active) e = 0;
 
   const int64_t nodeBase = e * NP + j * NQ + i;
   if (active && i == 0 && jj == 0) {
     prefetch_l2_bulk(ggeo + e * geoStride, 6 * NP * sizeof(dw));
     if constexpr (MASS) prefetch_l2_bulk(wJ + e * wJStride, NP * sizeof(dw));
   }
-  if (PERSIST && nactive && i == 0 && jj == 0) prefetch_l2_bulk(g2l + en * NP, NP * sizeof(int32_t));
   {
     int32_t id[NQ];
 #pragma unroll
@@ -957,21 +946,6 @@ ax_hex_dw_lean_kernel(const int64_t Nelements, const int32_t* __restrict__ eleme
     eo_sync<NQ>(el);
     if constexpr (MASS) s_qt[k][tid] = dw_add_u(dw_add_u(mass, s_dr[el][j][i]), s_ds[el][j][i]);
     else s_qt[k][tid] = dw_add_u(s_dr[el][j][i], s_ds[el][j][i]);
-    if constexpr (PERSIST) {
-      if (k == NQ / 2 && nactive) {
-        // the next group's q values to L2 (its index row is there by now)
-        const int64_t nb = en * NP + j * NQ + i;
-#pragma unroll
-        for (int kk = 0; kk < NQ; ++kk) {
-          const int32_t id = __ldg(g2l + nb + kk * NQ * NQ);
-          if (id >= 0) asm volatile("prefetch.L2 [%0];" ::"l"(q + id));
-        }
-        if (i == 0 && jj == 0) {
-          prefetch_l2_bulk(ggeo + en * geoStride, 6 * NP * sizeof(dw));
-          if constexpr (MASS) prefetch_l2_bulk(wJ + en * wJStride, NP * sizeof(dw));
-        }
-      }
-    }
   }
 
   {
@@ -996,15 +970,11 @@ ax_hex_dw_lean_kernel(const int64_t Nelements, const int32_t* __restrict__ eleme
     }
   }
 
-  if (active) {
+  if (!active) return;
 #pragma unroll
-    for (int k = 0; k < NQ; ++k) {
-      const int32_t id = __ldg(g2l + nodeBase + k * NQ * NQ);
-      if (id >= 0) atomicAdd(out + id, dw_to_double(s_qt[k][tid]));
-    }
-  }
-  if (!PERSIST) break;
-  __syncthreads();   // the next group overwrites the shared pencils and lines
+  for (int k = 0; k < NQ; ++k) {
+    const int32_t id = __ldg(g2l + nodeBase + k * NQ * NQ);
+    if (id >= 0) atomicAdd(out + id, dw_to_double(s_qt[k][tid]));
   }
 }
 
@@ -1093,13 +1063,6 @@ static bool dw7_classic() {
   }();
   return v;
 }
-static bool dw7_persist() {
-  static const bool v = [] {
-    const char* ev = std::getenv("LPG_AX_DW");
-    return ev && !std::strcmp(ev, "persist");
-  }();
-  return v;
-}
 
 int ax_hex_dw(const AxArgs<double, float2>& a, cudaStream_t s) {
   if (a.Nelements <= 0) return LPG_OK;
@@ -1122,19 +1085,6 @@ int ax_hex_dw(const AxArgs<double, float2>& a, cudaStream_t s) {
       reinterpret_cast<const dw*>(a.wJ), a.wJStride, a.D, a.lambda, a.lambdaE, a.q, a.out
     if (dw7_classic())
       ax_hex_dw_kernel<8, true><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS);
-    else if (dw7_persist()) {
-      static PerDeviceConfig perDevice;
-      KernelConfig cfg;
-      const int prc = perDevice.get([](int, KernelConfig&) { return (int)LPG_OK; }, &cfg);
-      if (prc) return prc;
-      const unsigned pgrid = (unsigned)std::min<int64_t>(blocks, (int64_t)cfg.numSMs * 4);
-      if (mass && a.lambda == 1.0 && !a.lambdaE)
-        ax_hex_dw_lean_kernel<8, true, true, true><<<pgrid, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS);
-      else if (mass)
-        ax_hex_dw_lean_kernel<8, true, false, true><<<pgrid, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS);
-      else
-        ax_hex_dw_lean_kernel<8, false, false, true><<<pgrid, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS);
-    }
     else if (mass && a.lambda == 1.0 && !a.lambdaE)
       ax_hex_dw_lean_kernel<8, true, true><<<(unsigned)blocks, dim3(8, 8, 4), 0, s>>>(LPG_DW_ARGS);
     else if (mass)
