@@ -103,6 +103,54 @@ def test_pmg_preconditioner_application_matches_oracle():
     assert rel_err(z.cpu().numpy(), o.precon(rh)) < 1e-9
 
 
+_PRECON_CHILD = r"""
+import json, sys
+import numpy as np
+import torch
+import libparanumal_gb300 as lpg
+s = json.loads(sys.argv[1])
+e = lpg.Elliptic(s)
+rng = np.random.default_rng(2)
+r = torch.tensor(rng.standard_normal(e.Nglobal), device="cuda")
+z = torch.zeros_like(r)
+e.precon(r, z)
+torch.cuda.synchronize()
+np.save(sys.argv[2], z.cpu().numpy())
+"""
+
+
+@pytest.mark.parametrize("over", [{}, {"LAMBDA": 1.0, "LAMBDA FIELD": "LOGNORMAL", "LAMBDA SEED": 2}],
+                         ids=["lambda0", "lognormal"])
+def test_fp32_preconditioner_application_fused_and_separate_chebyshev(tmp_path, over):
+    """The FP32 p-MG V-cycle with the Chebyshev steps on the unscaled residual that the
+    operator updates in place (the default) against the same V-cycle with a separate A d
+    vector (LPG_CHEB=unfused) and against the oracle's FP64 V-cycle: the two FP32 paths
+    differ only in FP32 rounding order (1e-5), and both stay within FP32 accuracy of the
+    FP64 preconditioner (1e-4)."""
+    import json
+    import os
+    import subprocess
+    import sys
+    s = dict(MG, **{"PRECONDITIONER PRECISION": "FP32"}, **over)
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = {}
+    for mode in ("fused", "unfused"):
+        env = dict(os.environ, PYTHONPATH=root)
+        env.pop("LPG_CHEB", None)
+        if mode == "unfused":
+            env["LPG_CHEB"] = "unfused"
+        f = tmp_path / (mode + ".npy")
+        p = subprocess.run([sys.executable, "-c", _PRECON_CHILD, json.dumps(s), str(f)], env=env, cwd=root,
+                           capture_output=True, text=True, timeout=600)
+        assert p.returncode == 0, p.stderr[-2000:]
+        out[mode] = np.load(f)
+    o = Oracle(dict(MG, **over))
+    zo = o.precon(np.random.default_rng(2).standard_normal(o.Ngather))
+    assert rel_err(out["fused"], out["unfused"]) < 1e-5
+    assert rel_err(out["fused"], zo) < 1e-4
+    assert rel_err(out["unfused"], zo) < 1e-4
+
+
 @pytest.mark.parametrize("over", [
     {"MULTIGRID SMOOTHER": "DAMPEDJACOBI"},
     {"MULTIGRID SMOOTHER": "DAMPEDJACOBI", "PARALMOND SMOOTHER": "DAMPEDJACOBI"},
