@@ -74,6 +74,8 @@ def parse():
     ap.add_argument("--sequence", action="store_true", help="repeated solves with each initial-guess strategy")
     ap.add_argument("--heat", action="store_true", help="backward-Euler time steps with each initial-guess strategy")
     ap.add_argument("--learned-pair", action="store_true", help="one plain and one learned FP32+DF64 solve")
+    ap.add_argument("--gmsh", action="store_true", help="operator throughput on Gmsh meshes (lattice and random "
+                    "element order) against the box")
     ap.add_argument("--weights", default="", help="--learned-pair: network weights (.npy) instead of training")
     ap.add_argument("--save-weights", default="", help="--learned-pair: write the trained weights (.npy)")
     ap.add_argument("--train-nx", type=int, default=32)
@@ -705,6 +707,59 @@ def run_ipdg(a):
     print(json.dumps(out), flush=True)
 
 
+def run_gmsh(a):
+    """Operator throughput on hexahedral Gmsh meshes against the box: the a.nx^3 box written
+    as a Gmsh 2.2 file (shuffled node tags, randomly rotated element vertex lists, jittered
+    interior vertices), once with the hexahedra in lattice order and once in random order
+    (an element order without spatial locality). The FP64 operator and its FP32 /
+    BF16-geometry / double-word variants are timed on each (CUDA events, W warm-up and K
+    timed applications)."""
+    import tempfile
+    import torch
+    import libparanumal_gb300 as lpg
+    import __graft_entry__ as g
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from gmsh_mesh import write_box
+    g.build()
+    torch.cuda.set_device(0)
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    res = {}
+    with tempfile.TemporaryDirectory() as tmp:
+        meshes = {"box": None,
+                  "gmsh_lattice_order": dict(shuffle_seed=1, rotate_seed=2, jitter=0.1, jitter_seed=3),
+                  "gmsh_random_order": dict(shuffle_seed=1, rotate_seed=2, jitter=0.1, jitter_seed=3,
+                                            element_seed=4)}
+        for name, kw in meshes.items():
+            st = settings(a.nx, a.N)
+            if kw is not None:
+                path = write_box(os.path.join(tmp, name + ".msh"), a.nx, a.nx, a.nx, **kw)
+                st = {k: v for k, v in st.items() if not k.startswith("BOX N") and not k.startswith("MESH JITTER")}
+                st["MESH FILE"] = path
+            e = lpg.Elliptic(st)
+            q = (torch.rand(e.Nglobal, dtype=torch.float64, device="cuda", generator=torch.Generator(
+                device="cuda").manual_seed(1)) * 2 - 1)
+            y = torch.empty_like(q)
+            for _ in range(max(3, a.warmup)):
+                e.Operator(q, y, sp)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(a.steps):
+                e.Operator(q, y, sp)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / a.steps
+            v = time_operator_variants(e, q, a, stream, sp)
+            res[name] = {"elements": e.info("nelements"), "assembled_dofs": e.Nglobal,
+                         "fp64_ms_per_apply": ms, "fp64_gdofs_local": e.Nlocal / (ms * 1e-3) / 1e9,
+                         "variants_ms_per_apply": {k: x["ms_per_apply"] for k, x in v.items()}}
+            del e
+            torch.cuda.empty_cache()
+    print(json.dumps({"workload": "operator on %d^3 hexahedra, N=%d, lambda=1: box against Gmsh files" % (a.nx, a.N),
+                      "results": res}), flush=True)
+
+
 def time_operator_variants(e, q, a, stream, sp):
     """CUDA-event time per application of the FP32, BF16-geometry and double-FP32-word
     operators of object e (the same mesh as the headline FP64 workload), with their
@@ -789,6 +844,8 @@ def main():
         return run_heat(a)
     if a.learned_pair:
         return run_learned_pair(a)
+    if a.gmsh:
+        return run_gmsh(a)
     import numpy as np
     import torch
     import libparanumal_gb300 as lpg

@@ -41,7 +41,9 @@ def cube_rotations():
 
 
 def write_box(path, nx, ny, nz, dims=(2.0, 2.0, 2.0), shuffle_seed=None, rotate_seed=None, jitter=0.0,
-              jitter_seed=0, tags=(1, 1, 1, 1, 1, 1)):
+              jitter_seed=0, tags=(1, 1, 1, 1, 1, 1), element_seed=None):
+    """element_seed: the hexahedra are written in a random order (a mesh whose element
+    order carries no spatial locality)."""
     nnx, nny, nnz = nx + 1, ny + 1, nz + 1
     X0 = [-d / 2.0 for d in dims]
     h = [dims[0] / nx, dims[1] / ny, dims[2] / nz]
@@ -98,8 +100,11 @@ def write_box(path, nx, ny, nz, dims=(2.0, 2.0, 2.0), shuffle_seed=None, rotate_
         for tag, q in quads:
             fp.write("%d 3 2 %d %d %s\n" % (c, tag, tag, " ".join(map(str, q))))
             c += 1
-        for hx in hexes:
-            fp.write("%d 5 2 9 1 %s\n" % (c, " ".join(map(str, hx))))
+        order = range(len(hexes))
+        if element_seed is not None:
+            order = np.random.default_rng(element_seed).permutation(len(hexes))
+        for h_ in order:
+            fp.write("%d 5 2 9 1 %s\n" % (c, " ".join(map(str, hexes[h_]))))
             c += 1
         fp.write("$EndElements\n")
     return path
