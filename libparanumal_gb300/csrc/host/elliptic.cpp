@@ -202,6 +202,49 @@ int Elliptic::set_neumann_nodes(const std::vector<int32_t>& node, const std::vec
 }
 
 // numbering of a file mesh on the host (union-find over connected face nodes), uploaded
+// Element traversal order of the operators on a file mesh: Morton (Z-order) keys of the
+// element centroids, quantised to 21 bits per axis over the vertices' bounding box. In the
+// file's order (any order a mesh generator chose) concurrently running CTAs gather and
+// assemble dofs far apart; in this order neighbours run close together and share their
+// face dofs through L2.
+int Elliptic::morton_element_order(const HexMeshData& hm, cudaStream_t s) {
+  const int64_t E = hm.E;
+  if (E <= 1 || E > INT32_MAX) return LPG_OK;
+  auto spread = [](uint64_t v) {   // 21 bits -> every third bit of 63
+    v &= 0x1FFFFFull;
+    v = (v | (v << 32)) & 0x1F00000000FFFFull;
+    v = (v | (v << 16)) & 0x1F0000FF0000FFull;
+    v = (v | (v << 8)) & 0x100F00F00F00F00Full;
+    v = (v | (v << 4)) & 0x10C30C30C30C30C3ull;
+    v = (v | (v << 2)) & 0x1249249249249249ull;
+    return v;
+  };
+  double span[3];
+  for (int d = 0; d < 3; ++d) span[d] = (hm.hi[d] > hm.lo[d]) ? hm.hi[d] - hm.lo[d] : 1.0;
+  std::vector<std::pair<uint64_t, int32_t>> key((size_t)E);
+#pragma omp parallel for
+  for (int64_t e = 0; e < E; ++e) {
+    double c[3] = {0, 0, 0};
+    for (int v = 0; v < 8; ++v) {
+      const int64_t n = hm.EToV[e * 8 + v];
+      c[0] += hm.VX[n]; c[1] += hm.VY[n]; c[2] += hm.VZ[n];
+    }
+    const double lo[3] = {hm.lo[0], hm.lo[1], hm.lo[2]};
+    uint64_t q[3];
+    for (int d = 0; d < 3; ++d) {
+      const double t = (c[d] / 8.0 - lo[d]) / span[d];
+      q[d] = (uint64_t)std::min(2097151.0, std::max(0.0, t * 2097152.0));
+    }
+    key[(size_t)e] = {spread(q[0]) | (spread(q[1]) << 1) | (spread(q[2]) << 2), (int32_t)e};
+  }
+  std::sort(key.begin(), key.end());
+  std::vector<int32_t> order((size_t)E);
+  for (int64_t e = 0; e < E; ++e) order[(size_t)e] = key[(size_t)e].second;
+  int rc;
+  if ((rc = elemOrder.alloc(E)) || (rc = elemOrder.upload(order.data(), E, s))) return rc;
+  return LPG_OK;
+}
+
 int Elliptic::setup_file(const MeshConfig& c, int N, const std::vector<double>* lamE, cudaStream_t s) {
   int rc = mesh.setup(c, N, s);
   if (rc) return rc;
@@ -219,6 +262,7 @@ int Elliptic::setup_file(const MeshConfig& c, int N, const std::vector<double>* 
     return rc;
   if ((rc = multiplicity_to_weight(Nglobal, mult.p, weightG.p, s))) return rc;
   hasDirichlet = num.hasDirichlet;
+  if ((rc = morton_element_order(*c.file, s))) return rc;
   {
     // boundary face nodes whose node flag is a Neumann type (tag >= 2)
     const HexMeshData& hm = *c.file;
@@ -436,7 +480,7 @@ int Elliptic::OperatorDW(const double* q, double* Aq, cudaStream_t s) {
   if ((rc = mesh.make_dw(s))) return rc;
   AxArgs<double, float2> a;
   const int64_t Np = mesh.Np;
-  a.N = mesh.N; a.Nelements = mesh.E; a.g2l = g2l.p;
+  a.N = mesh.N; a.Nelements = mesh.E; a.elementList = elemOrder.p; a.g2l = g2l.p;
   a.ggeo = mesh.geoDW.p; a.geoStride = 7 * Np; a.wJ = mesh.geoDW.p + 6 * Np; a.wJStride = 7 * Np;
   a.D = mesh.D_d.p; a.lambda = lambda; a.lambdaE = hasLambdaE ? lambdaE.p : nullptr;
   a.q = q; a.out = Aq; a.Nglobal = Nglobal;
@@ -455,7 +499,7 @@ int Elliptic::Operator(const double* q, double* Aq, cudaStream_t s) {
   if (opDW) return OperatorDW(q, Aq, s);
   AxArgs<double, double> a;
   const int64_t Np = mesh.Np;
-  a.N = mesh.N; a.Nelements = mesh.E; a.g2l = g2l.p;
+  a.N = mesh.N; a.Nelements = mesh.E; a.elementList = elemOrder.p; a.g2l = g2l.p;
   a.ggeo = mesh.geo.p; a.geoStride = 7 * Np; a.wJ = mesh.geo.p + 6 * Np; a.wJStride = 7 * Np;
   a.D = mesh.D_d.p; a.lambda = lambda; a.lambdaE = hasLambdaE ? lambdaE.p : nullptr;
   a.q = q; a.out = Aq; a.Nglobal = Nglobal;
@@ -481,7 +525,7 @@ int Elliptic::OperatorF32(const float* q, float* Aq, Prec prec, cudaStream_t s, 
   }
   if (prec == Prec::BF16G) {
     AxArgs<float, __nv_bfloat16> a;
-    a.N = mesh.N; a.Nelements = mesh.E; a.g2l = g2l.p;
+    a.N = mesh.N; a.Nelements = mesh.E; a.elementList = elemOrder.p; a.g2l = g2l.p;
     a.ggeo = mesh.geo16.p; a.geoStride = 7 * Np; a.wJ = mesh.geo16.p + 6 * Np; a.wJStride = 7 * Np;
     a.D = mesh.D32.p; a.lambda = (float)lambda; a.lambdaE = hasLambdaE ? lambdaE32.p : nullptr;
     a.q = q; a.out = Aq; a.Nglobal = Nglobal;
@@ -489,7 +533,7 @@ int Elliptic::OperatorF32(const float* q, float* Aq, Prec prec, cudaStream_t s, 
     return ax_hex<float, __nv_bfloat16>(a, mode, s);
   }
   AxArgs<float, float> a;
-  a.N = mesh.N; a.Nelements = mesh.E; a.g2l = g2l.p;
+  a.N = mesh.N; a.Nelements = mesh.E; a.elementList = elemOrder.p; a.g2l = g2l.p;
   a.ggeo = mesh.geo32.p; a.geoStride = 7 * Np; a.wJ = mesh.geo32.p + 6 * Np; a.wJStride = 7 * Np;
   a.D = mesh.D32.p; a.lambda = (float)lambda; a.lambdaE = hasLambdaE ? lambdaE32.p : nullptr;
   a.q = q; a.out = Aq; a.Nglobal = Nglobal;

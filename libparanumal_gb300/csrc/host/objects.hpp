@@ -157,6 +157,10 @@ struct Elliptic {
   bool hasDirichlet = false;       // some nodes are masked (Dirichlet data lifted into the rhs)
   double allNeumannScale = 1;
   DevBuf<int32_t> g2l, owner;
+  // C0 meshes read from a file: the elements in Morton order of their centroids, the order
+  // in which the operators visit them (storage keeps the file's order); empty for boxes,
+  // whose lattice order already keeps neighbours together
+  DevBuf<int32_t> elemOrder;
   DevBuf<double> weightG;
   DevBuf<float> weightG32;
   int rhsKind = 0;                 // 0 sine, 1 Gaussian sources
@@ -187,6 +191,7 @@ struct Elliptic {
   int setup(Platform* p, const MeshConfig& c, int N, double lambda, const std::vector<double>* lamE,
             cudaStream_t s);
   int setup_file(const MeshConfig& c, int N, const std::vector<double>* lamE, cudaStream_t s);
+  int morton_element_order(const HexMeshData& hm, cudaStream_t s);
   // VTU file of the local field qL (E*Np, device)
   int PlotFields(const double* qL, const std::string& fileName, cudaStream_t s);
   int finish_setup(const std::vector<double>* lamE, cudaStream_t s);
