@@ -241,6 +241,8 @@ int lpg_elliptic_destroy(lpg_elliptic *e);
                                              residual and setup applications */
 #define LPG_INFO_LEARNED_TIMEOUTS 15 /* learned V-cycles redone with the plain smoother because the
                                         network's tensor-core pipeline reported a timeout */
+#define LPG_INFO_MORTON_ORDER 16   /* 1 if the operators visit the elements of a mesh file in Morton
+                                      order of their centroids (the file's order had no locality) */
 int64_t lpg_elliptic_info(const lpg_elliptic *e, int what);
 
 /* Copy a named setup array to host memory: "GlobalToLocal" (int32), "ownerLocal" (int32),

@@ -20,7 +20,7 @@ STATUS = {0: "OK", -1: "INVALID", -2: "CUDA", -3: "UNSUPPORTED", -4: "NOT_CONVER
           -5: "ALLOC", -6: "SETTINGS", -7: "BREAKDOWN", -8: "TIMEOUT"}
 INFO = dict(nelements=0, np=1, nglobal=2, nlocal=3, n=4, allneumann=5, mg_plevels=6,
             mg_amglevels=7, coarse_n=8, device_bytes=9, vcycles=10, fallbacks=11, host_chunks=12,
-            ig_history=13, operator_applications=14, learned_timeouts=15)
+            ig_history=13, operator_applications=14, learned_timeouts=15, morton_order=16)
 
 _lib = None
 

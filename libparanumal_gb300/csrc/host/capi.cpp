@@ -439,6 +439,7 @@ extern "C" int64_t lpg_elliptic_info(const lpg_elliptic* e, int what) {
     case LPG_INFO_IG_HISTORY: return e->ig ? e->ig->history() : 0;
     case LPG_INFO_OPERATOR_APPLICATIONS: return e->el->nOps;
     case LPG_INFO_LEARNED_TIMEOUTS: return e->precon ? e->precon->learned_timeouts() : 0;
+    case LPG_INFO_MORTON_ORDER: return e->el->elemOrder.p ? 1 : 0;
     default: return -1;
   }
 }

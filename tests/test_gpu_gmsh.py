@@ -90,10 +90,48 @@ def test_neumann_tagged_file_rhs_matches_oracle(tmp_path):
     assert rel_err(r.cpu().numpy(), Oracle(s).rhs()) < 1e-12
 
 
+@pytest.mark.parametrize("degree", [7, 3])
+def test_random_element_order_file_matches_oracle(tmp_path, degree):
+    """A 10^3 file whose hexahedra come in random order: the operators visit the elements
+    in Morton order of their centroids (the file's order has no locality), storage keeps the
+    file's order. FP64, double-word and FP32 operators against the oracle on the same file,
+    and a p-MG solve with the oracle's iteration count and solution."""
+    f = write_box(str(tmp_path / "r.msh"), 10, 10, 10, shuffle_seed=2, rotate_seed=3, jitter=0.1, jitter_seed=4,
+                  element_seed=5)
+    s = dict(BASE, **{"MESH FILE": f, "POLYNOMIAL DEGREE": degree, "LAMBDA": 1.0,
+                      "PRECONDITIONER": "MULTIGRID", "LINEAR SOLVER": "FPCG",
+                      "MULTIGRID DEGREES": "7,3,1" if degree == 7 else "3,1"})
+    e = lpg.Elliptic(s)
+    assert e.info("morton_order") == 1
+    o = Oracle(s)
+    qh = np.random.default_rng(7).uniform(-1, 1, e.Nglobal)
+    q = torch.tensor(qh, device="cuda")
+    ref = o.operator(qh)
+    Aq = torch.full_like(q, np.nan)
+    e.Operator(q, Aq)
+    torch.cuda.synchronize()
+    assert rel_err(Aq.cpu().numpy(), ref) < 1e-12
+    e.OperatorDF64(q, Aq)
+    torch.cuda.synchronize()
+    assert rel_err(Aq.cpu().numpy(), ref) < 1e-12
+    q32 = q.float()
+    A32 = torch.full_like(q32, np.nan)
+    e.OperatorF32(q32, A32)
+    torch.cuda.synchronize()
+    assert rel_err(A32.double().cpu().numpy(), ref) < 2e-6
+    r = e.Run(want_solution=True)
+    ro = o.run()
+    assert r["converged"]
+    assert abs(r["iterations"] - ro["iterations"]) <= 1, (r["iterations"], ro["iterations"])
+    assert rel_err(r["xL"], ro["xL"]) < 1e-7
+
+
 def test_file_mesh_equals_box_on_gpu(tmp_path):
     s = dict(BASE, **{"PRECONDITIONER": "MULTIGRID", "LINEAR SOLVER": "FPCG"})
     rb = lpg.Elliptic(s).Run()
-    rf = lpg.Elliptic(dict(s, **{"MESH FILE": mesh(tmp_path, shuffle_seed=3, rotate_seed=9)})).Run()
+    ef = lpg.Elliptic(dict(s, **{"MESH FILE": mesh(tmp_path, shuffle_seed=3, rotate_seed=9)}))
+    assert ef.info("morton_order") == 0   # elements in lattice order: the file's order is kept
+    rf = ef.Run()
     assert rf["iterations"] == rb["iterations"]
     assert abs(rf["norm"] - rb["norm"]) < 1e-11
     # both solves stop at a 1e-8 relative residual: their solutions differ at that level,
