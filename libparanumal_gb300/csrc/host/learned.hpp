@@ -29,8 +29,7 @@ struct LearnedSmoother {
   // z (assembled) += sum over copies of coef .* s_e MLP(features(r)), coef = weight / diag
   // (the average over copies of s_e invDiag .* output). Element scales s_e are floored at
   // sfloor (the caller's kScaleFloor x residual RMS). The network runs in chunks of kChunk
-  // elements and each chunk's copies are added with atomics (interior nodes with plain
-  // stores). LPG_LEARNED_CORRECTION=lattice (a tuning override, measured 3-7 % slower per
+  // elements and each chunk's copies are added with atomics. LPG_LEARNED_CORRECTION=lattice (a tuning override, measured 3-7 % slower per
   // solve at 64^3 and 112^3) keeps all outputs and sums each dof's copies in one thread per
   // lattice node instead, in whole element layers as each chunk completes them.
   template <typename T>

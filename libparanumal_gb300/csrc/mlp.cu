@@ -391,12 +391,10 @@ __global__ void apply_correction_kernel(const int Np, const int64_t count, const
     const int n = (int)(i % Np);
     const int32_t g = g2l[(e0 + el) * Np + n];
     if (g < 0) continue;
-    const TV v = coef[g] * (TV)(scale[el] * out[el * kMlpOut + n]);
-    // nodes strictly inside the element (1 <= i,j,k <= N-1) have no other copy: a plain
-    // read-modify-write
-    const int Nq = kMlpNq, a = n % Nq, bb = (n / Nq) % Nq, c = n / (Nq * Nq);
-    if (a > 0 && a < Nq - 1 && bb > 0 && bb < Nq - 1 && c > 0 && c < Nq - 1) z[g] += v;
-    else atomicAdd(z + g, v);
+    // every copy as a fire-and-forget atomic add, the nodes strictly inside the element
+    // too: a plain read-modify-write there waits for its load and splits each warp between
+    // the two paths (64^3 learned solve: 0.2531 against 0.2580 s)
+    atomicAdd(z + g, coef[g] * (TV)(scale[el] * out[el * kMlpOut + n]));
   }
 }
 template <typename TV>
