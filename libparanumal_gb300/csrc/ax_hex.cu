@@ -145,17 +145,6 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
   const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
 }
-// the same with an L2 cache policy (e.g. evict-first for data read once per application)
-__device__ __forceinline__ void cp_async16_hint(void* smem, const void* gmem, uint64_t policy) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "l"(policy)
-               : "memory");
-}
-__device__ __forceinline__ uint64_t l2_evict_first_policy() {
-  uint64_t p;
-  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;\n" : "=l"(p));
-  return p;
-}
 // L2 prefetch of `bytes` (a multiple of 16) from global memory; skipped unless the address
 // is 16-byte aligned, as the bulk prefetch requires
 __device__ __forceinline__ void prefetch_l2_bulk(const void* gmem, unsigned bytes) {
@@ -216,9 +205,7 @@ __device__ __forceinline__ float row_dot(const float* __restrict__ row, const fl
 }
 
 // MASS = false: lambda == 0 and no lambda field, the wJ row is neither copied nor used
-// EF: the geometric-factor and index rows (read once per application) are copied with an
-// L2 evict-first policy, so they do not push the gathered q and the assembled output out
-template <int NQ, typename T, typename G, int EPB, int STAGES, bool PF = false, bool MASS = true, bool EF = false>
+template <int NQ, typename T, typename G, int EPB, int STAGES, bool PF = false, bool MASS = true>
 __global__ void __launch_bounds__(NQ * NQ * EPB)
 ax_hex_staged_kernel(const int64_t Nelements, const int32_t* __restrict__ elementList,
                      const int32_t* __restrict__ g2l, const G* __restrict__ ggeo, const int64_t geoStride,
@@ -250,11 +237,6 @@ ax_hex_staged_kernel(const int64_t Nelements, const int32_t* __restrict__ elemen
   // copy of one element group: 7 geometric-factor rows and the index row per element,
   // each a contiguous run of 16-byte chunks (compile-time trip counts)
   constexpr int ROW_CHUNKS = L::ROW_BYTES / 16, IDX_CHUNKS = L::IDX_BYTES / 16;
-  const uint64_t policy = EF ? l2_evict_first_policy() : 0;
-  auto copy16 = [&](void* d, const void* g) {
-    if constexpr (EF) cp_async16_hint(d, g, policy);
-    else cp_async16(d, g);
-  };
   auto issue = [&](const int64_t grp, const int stage) {
     if (grp < ngroups) {
       unsigned char* base = smem + stage * STAGE_BYTES;
@@ -269,10 +251,10 @@ ax_hex_staged_kernel(const int64_t Nelements, const int32_t* __restrict__ elemen
             const unsigned char* src =
                 (comp < 6) ? reinterpret_cast<const unsigned char*>(ggeo + e * geoStride + (int64_t)comp * NP)
                            : reinterpret_cast<const unsigned char*>(wJ + e * wJStride);
-            for (int c = tid; c < ROW_CHUNKS; c += NT) copy16(dst + comp * L::ROW_BYTES + c * 16, src + c * 16);
+            for (int c = tid; c < ROW_CHUNKS; c += NT) cp_async16(dst + comp * L::ROW_BYTES + c * 16, src + c * 16);
           }
           const unsigned char* srci = reinterpret_cast<const unsigned char*>(g2l + e * NP);
-          for (int c = tid; c < IDX_CHUNKS; c += NT) copy16(dst + L::GEO_BYTES + c * 16, srci + c * 16);
+          for (int c = tid; c < IDX_CHUNKS; c += NT) cp_async16(dst + L::GEO_BYTES + c * 16, srci + c * 16);
         }
       }
     }
@@ -1120,12 +1102,12 @@ int ax_hex_dw(const AxArgs<double, float2>& a, cudaStream_t s) {
   return LPG_OK;
 }
 
-template <int NQ, typename T, typename G, int EPB, int STAGES, bool PF = false, bool MASS = true, bool EF = false>
+template <int NQ, typename T, typename G, int EPB, int STAGES, bool PF = false, bool MASS = true>
 static int launch_staged(const AxArgs<T, G>& a, cudaStream_t s) {
   using L = StagedLayout<NQ, G>;
   constexpr int smem = STAGES * EPB * L::ELEM_BYTES;
   static PerDeviceConfig perDevice;   // per instantiation: dynamic shared memory opt-in, occupancy
-  auto kern = ax_hex_staged_kernel<NQ, T, G, EPB, STAGES, PF, MASS, EF>;
+  auto kern = ax_hex_staged_kernel<NQ, T, G, EPB, STAGES, PF, MASS>;
   KernelConfig cfg;
   const int rc = perDevice.get(
       [&](int, KernelConfig& c) {
@@ -1158,7 +1140,6 @@ static int staged_variant() {
       else if (!std::strcmp(e, "4x2")) v = 42;
       else if (!std::strcmp(e, "4x3")) v = 43;
       else if (!std::strcmp(e, "2x2pf")) v = 122;
-      else if (!std::strcmp(e, "ef")) v = 7;
     }
   }
   return v;
@@ -1199,14 +1180,6 @@ static int launch_ax(const AxArgs<T, G>& a, cudaStream_t s) {
       // through the current group (0.997 vs 1.112 ms at 64^3); BF16 geometry without it
       // (lambda = 0 without a lambda field: the instantiation without the mass term and wJ copy)
       const bool noMass = (a.lambda == 0 && !a.lambdaE);
-      if (v == 7) {
-        if constexpr (std::is_same<G, float>::value)
-          return noMass ? launch_staged<NQ, T, G, 2, 2, true, false, true>(a, s)
-                        : launch_staged<NQ, T, G, 2, 2, true, true, true>(a, s);
-        else
-          return noMass ? launch_staged<NQ, T, G, 2, 2, false, false, true>(a, s)
-                        : launch_staged<NQ, T, G, 2, 2, false, true, true>(a, s);
-      }
       if constexpr (std::is_same<G, float>::value)
         return noMass ? launch_staged<NQ, T, G, 2, 2, true, false>(a, s) : launch_staged<NQ, T, G, 2, 2, true>(a, s);
       else
