@@ -68,6 +68,11 @@ int LearnedSmoother::check_tc(cudaStream_t s) {
   return LPG_OK;
 }
 
+int LearnedSmoother::clear_tc(cudaStream_t s) {
+  LPG_CUDA_TRY(cudaMemsetAsync(tcErr.p, 0, sizeof(int), s));
+  return LPG_OK;
+}
+
 int LearnedSmoother::ensure_chunk(int64_t rows) {
   if (chunk >= rows) return LPG_OK;
   int rc;
@@ -100,7 +105,7 @@ int LearnedSmoother::apply(const BoxNumbering& b, int64_t E, const int32_t* g2l,
       if ((rc = forward_bf16(n, out.p, s))) return rc;
       if ((rc = apply_correction<T>(Np, n, e0, g2l, out.p, scale.p, coef, z, s))) return rc;
     }
-    return check_tc(s);
+    return LPG_OK;
   }
   // chunks of whole element layers; after each chunk the lattice planes whose copies are
   // all computed are summed while the chunk's outputs are still in L2: element layers
@@ -124,7 +129,7 @@ int LearnedSmoother::apply(const BoxNumbering& b, int64_t E, const int32_t* g2l,
     if ((rc = lattice_correction<T>(b, g2l, outAll.p, scaleAll.p, coef, z, Zb, Ze, s))) return rc;
     if (last && b.periodic && (rc = lattice_correction<T>(b, g2l, outAll.p, scaleAll.p, coef, z, 0, 1, s))) return rc;
   }
-  return check_tc(s);
+  return LPG_OK;
 }
 template int LearnedSmoother::apply<double>(const BoxNumbering&, int64_t, const int32_t*, const double*, const double*,
                                             double*, int64_t, float, cudaStream_t);

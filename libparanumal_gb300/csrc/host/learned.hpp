@@ -25,13 +25,15 @@ struct LearnedSmoother {
   int load(const float* hostParams, cudaStream_t s);
   int ensure_chunk(int64_t rows);
   int forward_bf16(int64_t rows, float* dst, cudaStream_t s);   // dst = MLP(X) for `rows` rows
-  int check_tc(cudaStream_t s);
+  int check_tc(cudaStream_t s);            // waits for the stream; LPG_ERR_TIMEOUT if set
+  int clear_tc(cudaStream_t s);            // clears the timeout flag (stream-ordered)
   // z (assembled) += sum over copies of coef .* s_e MLP(features(r)), coef = weight / diag
   // (the average over copies of s_e invDiag .* output). Element scales s_e are floored at
   // sfloor (the caller's kScaleFloor x residual RMS). The network runs in chunks of kChunk
   // elements and each chunk's copies are added with atomics. LPG_LEARNED_CORRECTION=lattice (a tuning override, measured 3-7 % slower per
   // solve at 64^3 and 112^3) keeps all outputs and sums each dof's copies in one thread per
-  // lattice node instead, in whole element layers as each chunk completes them.
+  // lattice node instead, in whole element layers as each chunk completes them. The
+  // tensor-core timeout flag accumulates: clear_tc before, check_tc after a batch of calls.
   template <typename T>
   int apply(const BoxNumbering& b, int64_t E, const int32_t* g2l, const T* r, const T* coef, T* z, int64_t Nglobal,
             float sfloor, cudaStream_t s);

@@ -699,19 +699,16 @@ int MultiGrid::vcycle_learned(const T* RHS, T* X, cudaStream_t s) {
     if ((r = amxpy<T>(N, T(1), jac, RES, T(0), D, s))) return r;
     if ((r = learned->apply<T>(box, E, el->g2l.p, RES, coef, D, N, sfloor, s))) return r;
     if ((r = op<T>(el, D, AD, s))) return r;
-    // w = (c.RES)/(c.Ac) from one two-product pass; X += w c, RES -= w A c in one pass
+    // w = (c.RES)/(c.Ac) from one two-product pass; X += w c, RES -= w A c in one pass,
+    // which reads the two products from device memory (no host round trip per step)
     if ((r = dot2<T>(N, D, RES, AD, plat->scalars.p + 2, plat->partials.p, s))) return r;
-    LPG_CUDA_TRY(cudaMemcpyAsync(plat->hostScalars + 2, plat->scalars.p + 2, 2 * sizeof(double),
-                                 cudaMemcpyDeviceToHost, s));
-    LPG_CUDA_TRY(cudaStreamSynchronize(s));
-    const double cr = plat->hostScalars[2], cAc = plat->hostScalars[3];
-    const double w = (cAc > 0 && std::isfinite(cr) && std::isfinite(cAc)) ? cr / cAc : 0.0;
-    return update2<T>(N, (T)w, D, AD, X, RES, s);
+    return update2_dev<T>(N, plat->scalars.p + 2, D, AD, X, RES, s);
   };
   // a tensor-core pipeline timeout inside the network (LPG_ERR_TIMEOUT) abandons the
   // learned attempt: the V-cycle is redone with the plain smoother and counted
   auto learned_part = [&]() -> int {
     int r;
+    if ((r = learned->clear_tc(s))) return r;
     LPG_CUDA_TRY(cudaMemsetAsync(X, 0, sizeof(T) * N, s));
     LPG_CUDA_TRY(cudaMemcpyAsync(RES, RHS, sizeof(T) * N, cudaMemcpyDeviceToDevice, s));
     for (int k = 0; k < opt.learnedSteps; ++k)
@@ -720,7 +717,8 @@ int MultiGrid::vcycle_learned(const T* RHS, T* X, cudaStream_t s) {
     if ((r = residual<T>(el, RHS, X, RES, s))) return r;
     for (int k = 0; k < opt.learnedSteps; ++k)
       if ((r = smooth_step())) return r;
-    return LPG_OK;
+    // the network's tensor-core status, once per V-cycle (a timeout discards the V-cycle)
+    return learned->check_tc(s);
   };
   rc = learned_part();
   if (rc == LPG_ERR_TIMEOUT) {

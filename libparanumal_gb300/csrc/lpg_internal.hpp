@@ -129,6 +129,8 @@ template <typename T>
 int dot2(int64_t N, const T* x, const T* y, const T* z, double* out2, double* partials, cudaStream_t s);
 // x += a p; r -= a q
 template <typename T> int update2(int64_t N, T a, const T* p, const T* q, T* x, T* r, cudaStream_t s);
+// update2 with a = sc[0] / sc[1] from device memory (0 when sc[1] <= 0 or not finite)
+template <typename T> int update2_dev(int64_t N, const double* sc, const T* p, const T* q, T* x, T* r, cudaStream_t s);
 // FPCG with an FP32 preconditioner output z: out2 = (r.z, z.Ap) in FP64, and p = z + beta p
 int dot2_mixed(int64_t N, const float* z, const double* r, const double* Ap, double* out2, double* partials,
                cudaStream_t s);

@@ -67,7 +67,8 @@ int transpose_to_bf16(int K, int N, const float* W, __nv_bfloat16* Wt, cudaStrea
 // Fused inference Y (B x 512, FP32) = MLP(X (B x 896, BF16)) on the tcgen05 tensor cores
 // (all four layers per 128-row tile on one SM). Wt[l]: BF16 weights stored N x K (K
 // contiguous), bias[l] FP32. errFlag (device int) is set to a nonzero code if a CTA's
-// pipeline timed out; the caller reads it after the stream has run.
+// pipeline timed out and is never cleared here: the caller clears it, runs any number of
+// launches and reads it once after the stream has run.
 int mlp_forward_tc(int64_t B, const __nv_bfloat16* X, const __nv_bfloat16* const Wt[4], const float* const bias[4],
                    float* Y, int* errFlag, cudaStream_t s);
 // Diagnostics: every following mlp_forward_tc launch first waits up to ns nanoseconds on a

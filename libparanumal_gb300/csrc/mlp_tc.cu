@@ -680,7 +680,6 @@ int mlp_forward_tc(int64_t B, const __nv_bfloat16* X, const __nv_bfloat16* const
   if (rc) return rc;
   const int ntiles = (int)((B + TM - 1) / TM);
   const int grid = ntiles < cfg.numSMs ? ntiles : cfg.numSMs;
-  LPG_CUDA_TRY(cudaMemsetAsync(errFlag, 0, sizeof(int), s));
   const unsigned long long hold = g_holdNs.load(std::memory_order_relaxed);
   if (single) {
     mlp_tc_kernel<<<grid, THREADS, SMEM_BYTES, s>>>(maps, bias[0], bias[1], bias[2], bias[3], Y, B, ntiles, errFlag,

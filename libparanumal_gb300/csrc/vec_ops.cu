@@ -419,6 +419,28 @@ int update2(int64_t N, T a, const T* p, const T* q, T* x, T* r, cudaStream_t s) 
 template int update2<double>(int64_t, double, const double*, const double*, double*, double*, cudaStream_t);
 template int update2<float>(int64_t, float, const float*, const float*, float*, float*, cudaStream_t);
 
+// the same with the step w = num/den read from device memory (sc[0], sc[1]); w = 0 when
+// den <= 0 or either is not finite (no host round trip for the step length)
+template <typename T>
+__global__ void update2_dev_kernel(const int64_t N, const double* __restrict__ sc, const T* __restrict__ p,
+                                   const T* __restrict__ q, T* __restrict__ x, T* __restrict__ r) {
+  const double num = sc[0], den = sc[1];
+  const T a = (T)((den > 0 && isfinite(num) && isfinite(den)) ? num / den : 0.0);
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x) {
+    x[n] += a * p[n];
+    r[n] -= a * q[n];
+  }
+}
+template <typename T>
+int update2_dev(int64_t N, const double* sc, const T* p, const T* q, T* x, T* r, cudaStream_t s) {
+  if (N <= 0) return LPG_OK;
+  update2_dev_kernel<T><<<grid_for(N, 256, kStreamCap), 256, 0, s>>>(N, sc, p, q, x, r);
+  LPG_LAUNCH_CHECK("update2_dev_kernel");
+  return LPG_OK;
+}
+template int update2_dev<double>(int64_t, const double*, const double*, const double*, double*, double*, cudaStream_t);
+template int update2_dev<float>(int64_t, const double*, const float*, const float*, float*, float*, cudaStream_t);
+
 // halo exchange halves (the ogs extract kernel, libs/ogs/okl/ogsKernels.okl:167-): buf[i] =
 // v[idx[i]], and v[idx[i]] += buf[i] (the indices of one list are distinct)
 __global__ void halo_pack_kernel(const int64_t n, const int32_t* __restrict__ idx, const double* __restrict__ v,
