@@ -578,12 +578,16 @@ int MultiGrid::smooth(PLevel& L, const T* r, T* X, bool xIsZero, cudaStream_t s)
   // operator updates in place (u -= A d, assembled straight into it): no A d vector and no
   // memset of it, and each step pass reads 4 vectors and writes 2 instead of 5 and 3
   const bool fused = std::is_same<T, float>::value && !L.el->ipdg && !cheb_unfused();
-  if (fused) {
-    if ((rc = cheb_start_u<T>(N, invDiag, r, xIsZero ? nullptr : RES, RES, d, X, (T)invTheta, xIsZero, s)))
-      return rc;
-  } else if ((rc = cheb_start<T>(N, invDiag, r, xIsZero ? nullptr : RES, RES, d, X, (T)invTheta, xIsZero, s))) {
-    return rc;
+  bool started = false;
+  if constexpr (std::is_same<T, float>::value) {
+    if (fused) {
+      if ((rc = cheb_start_u<T>(N, invDiag, r, xIsZero ? nullptr : RES, RES, d, X, (T)invTheta, xIsZero, s)))
+        return rc;
+      started = true;
+    }
   }
+  if (!started && (rc = cheb_start<T>(N, invDiag, r, xIsZero ? nullptr : RES, RES, d, X, (T)invTheta, xIsZero, s)))
+    return rc;
   for (int k = 0; k < opt.chebDegree; ++k) {
     rho_np1 = 1.0 / (2. * sigma - rho_n);
     const double rhoDivDelta = 2.0 * rho_np1 / delta;
